@@ -1,0 +1,219 @@
+/*
+ * saigegpu.h -- C ABI of the GB300-native SAIGE step-1 hot path.
+ *
+ * One context owns one GPU, the decoded genotypes, the dense GRM resident in
+ * HBM and a multi-RHS PCG engine.  Every entry point returns an int status
+ * (SG_OK == 0); no C++ exception crosses the ABI.  Host buffers are owned by
+ * the caller; device memory is owned by the context.  A context is not
+ * thread-safe: use one per host thread, or serialise calls.
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the reference project; "FIT.cpp" = src/SAIGE/src/SAIGE_fitGLMM_fast.cpp,
+ * "RcppExports.cpp" = src/SAIGE/src/RcppExports.cpp).  The reference passes
+ * Armadillo float vectors; the *_f32 drop-ins keep that, and FP64 variants
+ * exist for the mixed-precision path.
+ *
+ * Vector layout: a block of k vectors of length n is "RHS-major": vector j
+ * occupies [j*n, (j+1)*n).  Matrices X (n x p) follow the same convention
+ * (column j contiguous), which is Armadillo's column-major layout.
+ */
+#ifndef SAIGEGPU_H
+#define SAIGEGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sg_ctx sg_ctx;
+
+enum sg_status {
+  SG_OK = 0,
+  SG_ERR_INVALID = 1,   /* bad argument or size */
+  SG_ERR_CUDA = 2,      /* CUDA runtime / launch failure */
+  SG_ERR_NOMEM = 3,     /* device allocation refused (incl. the context's HBM budget) */
+  SG_ERR_STATE = 4,     /* call out of order (e.g. no genotypes / no GRM yet) */
+  SG_ERR_IO = 5,        /* file could not be read */
+  SG_ERR_NUMERIC = 6,   /* NaN/Inf in inputs or a singular system */
+  SG_ERR_NOT_FOUND = 7, /* unknown request id */
+  SG_ERR_TIMEOUT = 8    /* a bounded device wait gave up */
+};
+
+/* GRM build precisions (sg_grm_build) */
+enum sg_grm_precision {
+  SG_GRM_FP32_SIMT = 0, /* FP32 standardised genotypes, FP32 CUDA-core SYRK */
+  SG_GRM_BF16_TC = 1,   /* BF16 genotypes, tcgen05 SYRK, FP32 accumulation in TMEM */
+  SG_GRM_BF16X3_TC = 2  /* split-BF16 (hi+lo, 3 products) tcgen05 SYRK: near-FP32 accuracy */
+};
+
+/* GRM.V product engines used inside the PCG (sg_set_matvec_mode) */
+enum sg_matvec_mode {
+  SG_MV_FP32_SIMT = 0,  /* FP32 K, FP32 operands, CUDA cores */
+  SG_MV_TF32_TC = 1,    /* tcgen05 kind::tf32 on the FP32 K, FP64 iterative refinement */
+  SG_MV_FP64_PLAIN = 2  /* plain FP64 GEMV (the single-RHS baseline) */
+};
+
+/* ------------------------------------------------------------ context */
+int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx **out);
+void sg_ctx_destroy(sg_ctx *ctx);
+const char *sg_last_error(const sg_ctx *ctx);
+int sg_device_bytes_in_use(const sg_ctx *ctx, uint64_t *bytes);
+int sg_set_matvec_mode(sg_ctx *ctx, int mode);
+/* GPU kernel launches issued by this context so far (for accounting). */
+int sg_kernel_launches(const sg_ctx *ctx, uint64_t *count);
+
+/* ------------------------------------------------------------ genotypes
+ * Replaces setgeno (FIT.cpp:2267-2275 -> genoClass::setGenoObj FIT.cpp:739-1024;
+ * RcppExports.cpp:725-737).  ``bed`` is the whole .bed file (with its 3-byte
+ * magic).  ``sub_1based``: subSampleInGeno (1-based .fam positions, analysis
+ * order).  ``pheno_mask``: indicatorGenoSamplesWithPheno (n_fam bytes).
+ * ``vr_random_markers``: the marker indices (0-based) of the random draw that
+ * the reference makes with arma::randi (FIT.cpp:866-868); markers in it with
+ * MAC >= min_mac_vr leave the GRM when is_var_ratio != 0 (FIT.cpp:521-547).
+ * Thresholds mirror setminMAFforGRM / setmaxMissingRateforGRM
+ * (FIT.cpp:4923-4930) and setminMAC_VarianceRatio (FIT.cpp:4970).
+ */
+int sg_setgeno(sg_ctx *ctx, const uint8_t *bed, uint64_t bed_len, int64_t n_fam, int64_t m_bim,
+               const int32_t *sub_1based, int64_t n_sub, const uint8_t *pheno_mask,
+               float min_maf, float max_missing, const int32_t *vr_random_markers,
+               int64_t n_vr_random, float min_mac_vr, int is_var_ratio, int is_diag_one);
+/* Same, reading the files; n_fam / m_bim are the line counts of .fam / .bim (FIT.cpp:760-787). */
+int sg_setgeno_files(sg_ctx *ctx, const char *bed_path, const char *bim_path, const char *fam_path,
+                     const int32_t *sub_1based, int64_t n_sub, const uint8_t *pheno_mask,
+                     float min_maf, float max_missing, const int32_t *vr_random_markers,
+                     int64_t n_vr_random, float min_mac_vr, int is_var_ratio, int is_diag_one);
+/* Uses a .bed image already in device memory (e.g. from sg_synth_bed). */
+int sg_setgeno_device(sg_ctx *ctx, const uint8_t *bed_dev, uint64_t bed_len, int64_t n_fam,
+                      int64_t m_bim, const int32_t *sub_1based, int64_t n_sub,
+                      const uint8_t *pheno_mask, float min_maf, float max_missing,
+                      const int32_t *vr_random_markers, int64_t n_vr_random, float min_mac_vr,
+                      int is_var_ratio, int is_diag_one);
+/* n = Nnomissing, m_total = M of the .bim, m_qc = GRM markers, m_vr = variance-ratio markers */
+int sg_geno_dims(sg_ctx *ctx, int64_t *n, int64_t *m_total, int64_t *m_qc, int64_t *m_vr);
+/* getAlleleFreqVec / invstdvVec / getMACVec (RcppExports.R:128-160): length m_qc */
+int sg_get_allele_freq(sg_ctx *ctx, float *out);
+int sg_get_invstd(sg_ctx *ctx, float *out);
+int sg_get_mac(sg_ctx *ctx, int32_t *out);
+/* getQCdMarkerIndex: m_total bytes, 1 for GRM markers */
+int sg_get_qc_marker_mask(sg_ctx *ctx, uint8_t *out);
+/* variance-ratio markers: freq, MAC and .bim index (getMACVec_forVarRatio, getIndexVec_forVarRatio) */
+int sg_get_vr_markers(sg_ctx *ctx, float *freq, int32_t *mac, int32_t *bim_index);
+/* re-packed 2-bit GRM genotypes, m_qc rows of ceil(n/4) bytes (genoVecofPointers) */
+int sg_get_packed_geno(sg_ctx *ctx, uint8_t *out);
+/* Get_OneSNP_Geno (FIT.cpp:223-273) / Get_OneSNP_Geno_forVarRatio (FIT.cpp:275-323) / Get_OneSNP_StdGeno (FIT.cpp:582-662) */
+int sg_get_onesnp_geno(sg_ctx *ctx, int64_t marker, int32_t *out);
+int sg_get_onesnp_geno_vr(sg_ctx *ctx, int64_t marker, int32_t *out);
+int sg_get_onesnp_stdgeno(sg_ctx *ctx, int64_t marker, float *out);
+
+/* ------------------------------------------------------------ GRM
+ * Builds K = Z Z' / M_qc in HBM (the reference never forms K; it applies
+ * Z_r(Z_r' x) per call, FIT.cpp:1635-1708 and gpuSymMatMult.cu:211-252).
+ */
+int sg_grm_build(sg_ctx *ctx, int precision);
+/* Get_Diagof_StdGeno (FIT.cpp:665-704): sum_m z^2 per sample.  The f32 form is
+ * accumulated in marker order in float exactly as the reference does. */
+int sg_grm_diag(sg_ctx *ctx, double *out);
+int sg_grm_diag_f32(sg_ctx *ctx, float *out);
+/* Copy the n x n GRM to the host (row-major; small n only). */
+int sg_grm_get(sg_ctx *ctx, float *out);
+/* K V for k vectors (RHS-major, FP64 in and out; the product runs in FP32). */
+int sg_grm_matmul(sg_ctx *ctx, const double *V, int64_t k, double *out);
+
+/* ------------------------------------------------------------ drop-ins for the Rcpp entry points */
+/* getCrossprodMatAndKin (FIT.cpp:1953-1981; RcppExports.cpp:664-671) */
+int sg_getCrossprodMatAndKin(sg_ctx *ctx, const float *b, float *out);
+/* getDiagOfSigma (FIT.cpp:2322-2365; RcppExports.cpp:774-782); tau[2] */
+int sg_getDiagOfSigma(sg_ctx *ctx, const float *w, const float *tau, float *out);
+/* getCrossprod (FIT.cpp:2397-2425; RcppExports.cpp:798-807) */
+int sg_getCrossprod(sg_ctx *ctx, const float *b, const float *w, const float *tau, float *out);
+/* getPCG1ofSigmaAndVector (FIT.cpp:2593-2809; RcppExports.cpp:900-911).  iters may be NULL. */
+int sg_getPCG1ofSigmaAndVector(sg_ctx *ctx, const float *w, const float *tau, const float *b,
+                               int maxiter, float tol, float *out, int32_t *iters);
+/* Multi-RHS FP64 solve: k independent columns, each stopped like the reference. */
+int sg_pcg_solve(sg_ctx *ctx, const double *w, const double *tau, const double *B, int64_t k,
+                 int maxiter, double tol, double *X, int32_t *iters);
+/* getSigma_X (FIT.cpp:3347-3366) and getSigma_G (FIT.cpp:3394-3398) */
+int sg_getSigma_X(sg_ctx *ctx, const float *w, const float *tau, const float *X, int64_t p,
+                  int maxiter, float tol, float *out);
+int sg_getSigma_G(sg_ctx *ctx, const float *w, const float *tau, const float *g, int maxiter,
+                  float tol, float *out);
+/* getCoefficients (FIT.cpp:3167-3199; RcppExports.cpp:1019-1031).  Outputs:
+ * Sigma_iY[n], Sigma_iX[n*p], cov[p*p], alpha[p], eta[n]. */
+int sg_getCoefficients(sg_ctx *ctx, const float *Y, const float *X, int64_t p, const float *w,
+                       const float *tau, int maxiter, float tol, float *Sigma_iY, float *Sigma_iX,
+                       float *cov, float *alpha, float *eta);
+/* GetTrace (FIT.cpp:3113-3160; RcppExports.cpp:1000-1015).  Probes: counter hash of
+ * (probe_seed, run, sample), the reference's comm.set.seed(200)+rbinom stream stand-in. */
+int sg_GetTrace(sg_ctx *ctx, const float *Sigma_iX, const float *X, int64_t p, const float *w,
+                const float *tau, const float *cov, int nrun, int maxiter, float tol,
+                float trace_cv_cutoff, uint64_t probe_seed, float *trace, int32_t *nrun_used);
+/* GetTrace_q (FIT.cpp:3409-3472): trace[0] = tr(P), trace[1] = tr(PK) */
+int sg_GetTrace_q(sg_ctx *ctx, const float *Sigma_iX, const float *X, int64_t p, const float *w,
+                  const float *tau, const float *cov, int nrun, int maxiter, float tol,
+                  float trace_cv_cutoff, uint64_t probe_seed, float *trace, int32_t *nrun_used);
+/* getAIScore (FIT.cpp:3279-3295; RcppExports.cpp:1067-1084): YPAPY, Trace, AI and PY[n]. */
+int sg_getAIScore(sg_ctx *ctx, const float *Y, const float *X, int64_t p, const float *w,
+                  const float *tau, const float *Sigma_iY, const float *Sigma_iX, const float *cov,
+                  int nrun, int maxiter, float tol, float trace_cv_cutoff, uint64_t probe_seed,
+                  float *YPAPY, float *Trace, float *AI, float *PY);
+/* getAIScore_q (FIT.cpp:3479-3531): YPAPY, YPA0PY, Trace[2], AI[4] (col-major 2x2), PY[n] */
+int sg_getAIScore_q(sg_ctx *ctx, const float *Y, const float *X, int64_t p, const float *w,
+                    const float *tau, const float *Sigma_iY, const float *Sigma_iX,
+                    const float *cov, int nrun, int maxiter, float tol, float trace_cv_cutoff,
+                    uint64_t probe_seed, float *YPAPY, float *YPA0PY, float *Trace, float *AI,
+                    float *PY);
+/* fitglmmaiRPCG (FIT.cpp:3302-3341; RcppExports.cpp:1088-1106): tau[2] updated in place */
+int sg_fitglmmaiRPCG(sg_ctx *ctx, const float *Y, const float *X, int64_t p, const float *w,
+                     float *tau, const float *Sigma_iY, const float *Sigma_iX, const float *cov,
+                     int nrun, int maxiter, float tol_pcg, float tol, float trace_cv_cutoff,
+                     uint64_t probe_seed);
+/* fitglmmaiRPCG_q (FIT.cpp:3610-3662; RcppExports.cpp:1170-1206) */
+int sg_fitglmmaiRPCG_q(sg_ctx *ctx, const float *Y, const float *X, int64_t p, const float *w,
+                       float *tau, const float *Sigma_iY, const float *Sigma_iX, const float *cov,
+                       int nrun, int maxiter, float tol_pcg, float tol, float trace_cv_cutoff,
+                       uint64_t probe_seed);
+
+/* ------------------------------------------------------------ batched solve engine
+ * Continuous batching of PCG columns over the resident GRM.  A "phenotype
+ * slot" holds W, tau and a sample mask; columns (right-hand sides) are
+ * admitted against a slot, advance one PCG iteration per engine step together
+ * with every other in-flight column, and retire on their own stopping rule
+ * (the reference's sum r^2 <= tol or maxiter).  A column's result does not
+ * depend on which other columns shared its steps.
+ */
+int sg_engine_reserve(sg_ctx *ctx, int64_t max_columns, int64_t max_phenos);
+/* Define/replace phenotype slot ``slot``: w[n] (0 or NaN-free), tau[2], mask[n] (1 = sample in
+ * this phenotype's subset; NULL = all). */
+int sg_engine_set_pheno(sg_ctx *ctx, int64_t slot, const double *w, const double *tau,
+                        const uint8_t *mask);
+/* Queue k columns.  kind 0 = PCG solve of Sigma x = b, kind 1 = one GRM product K b.
+ * ids[k] receives request ids. */
+int sg_engine_submit(sg_ctx *ctx, int64_t slot, int kind, const double *B, int64_t k, int maxiter,
+                     double tol, int64_t *ids);
+/* Submit Rademacher probes (counter hash of seed, run0+j, sample) as PCG (kind 0) or product (kind 1) columns. */
+int sg_engine_submit_probes(sg_ctx *ctx, int64_t slot, int kind, uint64_t seed, int64_t run0,
+                            int64_t k, int maxiter, double tol, int64_t *ids);
+/* Run up to max_steps engine steps (admitting queued columns as slots free up).
+ * Returns after the step in which at least one column retired, or when idle. */
+int sg_engine_run(sg_ctx *ctx, int64_t max_steps, int64_t *n_finished);
+/* Fetch and release a finished column: x[n], iterations.  SG_ERR_STATE if not finished. */
+int sg_engine_fetch(sg_ctx *ctx, int64_t id, double *x, int32_t *iters);
+int sg_engine_cancel(sg_ctx *ctx, int64_t id);
+/* counters: [0]=engine steps, [1]=columns retired, [2]=column-iterations, [3]=GRM passes */
+int sg_engine_stats(sg_ctx *ctx, int64_t *stats4);
+
+/* ------------------------------------------------------------ synthetic cohorts (benchmarks / tests)
+ * Writes a SNP-major .bed image (with magic) for n samples x m markers into device memory owned by
+ * the context: p_m ~ U(0.01,0.5) by marker hash, HWE genotypes, missing with probability miss_rate.
+ * The exact integer recipe is documented in saigegpu/synth.py and reproduced there on the CPU. */
+int sg_synth_bed(sg_ctx *ctx, uint64_t seed, int64_t n, int64_t m, double miss_rate,
+                 uint8_t **bed_dev, uint64_t *bed_len);
+int sg_synth_bed_to_host(sg_ctx *ctx, uint8_t *host, uint64_t len);
+/* g = Z b / sqrt(M_qc) with b_m ~ N(0,1) from the counter hash (polygenic signal). */
+int sg_synth_genetic_value(sg_ctx *ctx, uint64_t seed, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SAIGEGPU_H */

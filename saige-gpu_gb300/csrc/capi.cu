@@ -1,0 +1,1540 @@
+// C ABI of libsaigegpu (include/saigegpu.h): context, genotype set-up, GRM
+// build, the continuous-batching PCG engine and the drop-ins for the
+// reference's Rcpp entry points.  Host-side arithmetic that the reference does
+// with Armadillo on p x p matrices (inverse of X' Sigma^-1 X, the 2x2 AI
+// solve, tau updates) and the O(n) combinations around the solves run here in
+// FP64; everything O(n^2) or larger runs in the CUDA kernels.
+#include "sg_internal.h"
+#include "../../include/saigegpu.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <fstream>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+using namespace sg;
+
+namespace {
+
+struct Req {
+  int64_t id = 0;
+  int64_t slot = 0;
+  int kind = 0;       // 0 PCG, 1 product
+  int maxiter = 0;
+  double tol = 0.0;
+  bool probe = false;
+  uint64_t seed = 0;
+  int64_t run = 0;
+  std::vector<double> b;
+  int state = 0;      // 0 queued, 1 running, 2 done
+  int64_t col = -1;
+  std::vector<double> x;
+  int32_t iters = 0;
+};
+
+struct Engine {
+  int64_t cap_cols = 0, cap_ph = 0, np = 0, nblk = 0, stage_cols = 0;
+  double *X = nullptr, *R = nullptr, *Z = nullptr, *P = nullptr, *B = nullptr, *part = nullptr;
+  double *winv = nullptr, *minv = nullptr, *Yd = nullptr;
+  float *Pf = nullptr, *Yf = nullptr;
+  ColState* d_st = nullptr;
+  PhenoState* d_ph = nullptr;
+  int32_t* d_cols = nullptr;
+  std::vector<ColState> h_st;
+  std::vector<int64_t> col_req;
+  std::vector<PhenoState> h_ph;
+  std::vector<char> ph_set;
+  std::deque<int64_t> queue;
+  std::unordered_map<int64_t, Req> reqs;
+  int64_t next_id = 1;
+  int64_t hi_col = 0;
+  int64_t n_active = 0;
+  int64_t steps = 0, retired = 0, col_iters = 0, grm_passes = 0;
+};
+
+}  // namespace
+
+struct sg_ctx {
+  int device = 0;
+  uint64_t budget = 0;
+  uint64_t in_use = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  uint64_t launches = 0;
+  int mv_mode = SG_MV_FP32_SIMT;
+  std::unordered_map<void*, size_t> allocs;
+  // genotypes
+  bool have_geno = false;
+  int64_t n_fam = 0, m_bim = 0, nn = 0, m_qc = 0, m_vr = 0, pitch = 0;
+  int is_diag_one = 0;
+  uint8_t* d_packed = nullptr;
+  uint8_t* d_packed_vr = nullptr;
+  float* d_lut = nullptr;
+  float* d_lut_vr = nullptr;
+  std::vector<float> freq, invstd, vr_freq;
+  std::vector<int32_t> mac, vr_mac, vr_index;
+  std::vector<uint8_t> qc_mask;
+  // GRM
+  bool have_grm = false;
+  int64_t np = 0;
+  float* d_K = nullptr;
+  double* d_diag = nullptr;
+  float* d_diag32 = nullptr;
+  std::vector<double> diag;
+  std::vector<float> diag32;
+  // synthetic bed image
+  uint8_t* d_synth = nullptr;
+  uint64_t synth_len = 0;
+  Engine eng;
+};
+
+// ------------------------------------------------------------------ helpers
+static int set_err(sg_ctx* c, int code, const char* fmt, ...) {
+  if (!c) return code;
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  c->err = buf;
+  return code;
+}
+
+#define SG_CUDA(c, call)                                                                  \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return set_err((c), SG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+#define SG_LAUNCHED(c, n)                                                                     \
+  do {                                                                                        \
+    (c)->launches += (n);                                                                     \
+    cudaError_t e_ = cudaGetLastError();                                                      \
+    if (e_ != cudaSuccess) return set_err((c), SG_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
+  } while (0)
+
+#define SG_TRY(x)            \
+  do {                       \
+    int r_ = (x);            \
+    if (r_ != SG_OK) return r_; \
+  } while (0)
+
+static int dev_alloc(sg_ctx* c, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  if (c->budget && c->in_use + bytes > c->budget)
+    return set_err(c, SG_ERR_NOMEM, "HBM budget exceeded: %zu + %zu > %llu", (size_t)c->in_use,
+                   bytes, (unsigned long long)c->budget);
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return set_err(c, SG_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  }
+  c->allocs[*p] = bytes;
+  c->in_use += bytes;
+  return SG_OK;
+}
+
+template <typename T>
+static int dev_alloc_t(sg_ctx* c, T** p, size_t count) {
+  return dev_alloc(c, reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+static void dev_free(sg_ctx* c, void* p) {
+  if (!p) return;
+  auto it = c->allocs.find(p);
+  if (it != c->allocs.end()) {
+    c->in_use -= it->second;
+    c->allocs.erase(it);
+  }
+  cudaFree(p);
+}
+template <typename T>
+static void dev_free_t(sg_ctx* c, T*& p) {
+  dev_free(c, (void*)p);
+  p = nullptr;
+}
+
+static int sync(sg_ctx* c) {
+  SG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return SG_OK;
+}
+
+static bool all_finite(const float* v, int64_t n) {
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+static bool all_finite(const double* v, int64_t n) {
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+// ------------------------------------------------------------------ context
+extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out) {
+  if (!out) return SG_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) {
+    cudaGetLastError();
+    return SG_ERR_CUDA;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return SG_ERR_CUDA;
+  sg_ctx* c = new sg_ctx();
+  c->device = device;
+  c->budget = hbm_budget_bytes;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return SG_ERR_CUDA;
+  }
+  *out = c;
+  return SG_OK;
+}
+
+extern "C" void sg_ctx_destroy(sg_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->allocs) cudaFree(kv.first);
+  c->allocs.clear();
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" const char* sg_last_error(const sg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+extern "C" int sg_device_bytes_in_use(const sg_ctx* c, uint64_t* bytes) {
+  if (!c || !bytes) return SG_ERR_INVALID;
+  *bytes = c->in_use;
+  return SG_OK;
+}
+
+extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
+  if (!c) return SG_ERR_INVALID;
+  if (mode != SG_MV_FP32_SIMT && mode != SG_MV_TF32_TC && mode != SG_MV_FP64_PLAIN)
+    return set_err(c, SG_ERR_INVALID, "unknown matvec mode %d", mode);
+  if (mode == SG_MV_TF32_TC && !tc_available())
+    return set_err(c, SG_ERR_INVALID, "tcgen05 path needs an sm_103a device");
+  c->mv_mode = mode;
+  return SG_OK;
+}
+
+extern "C" int sg_kernel_launches(const sg_ctx* c, uint64_t* count) {
+  if (!c || !count) return SG_ERR_INVALID;
+  *count = c->launches;
+  return SG_OK;
+}
+
+// ------------------------------------------------------------------ genotypes
+static void free_geno(sg_ctx* c) {
+  dev_free_t(c, c->d_packed);
+  dev_free_t(c, c->d_packed_vr);
+  dev_free_t(c, c->d_lut);
+  dev_free_t(c, c->d_lut_vr);
+  dev_free_t(c, c->d_K);
+  dev_free_t(c, c->d_diag);
+  dev_free_t(c, c->d_diag32);
+  c->have_geno = false;
+  c->have_grm = false;
+}
+
+// raw: device .bed body re-pitched (m_bim rows of raw_pitch bytes, zero padded)
+static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_t n_fam,
+                        int64_t m_bim, const int32_t* sub_1based, int64_t n_sub,
+                        const uint8_t* pheno_mask, float min_maf, float max_missing,
+                        const int32_t* vr_markers, int64_t n_vr, float min_mac_vr,
+                        int is_var_ratio, int is_diag_one) {
+  const int64_t nn = n_sub;
+  // pheno mask bits (bit 2s of word s/16) and the variance-ratio candidate flags
+  const int64_t nwords = (n_fam + 15) / 16;
+  std::vector<uint32_t> maskbits(nwords + 1, 0u);
+  for (int64_t i = 0; i < n_fam; ++i)
+    if (!pheno_mask || pheno_mask[i]) maskbits[i / 16] |= 1u << (2 * (i % 16));
+  std::vector<uint8_t> vrflag(m_bim, 0);
+  for (int64_t k = 0; k < n_vr; ++k) {
+    if (vr_markers[k] < 0 || vr_markers[k] >= m_bim)
+      return set_err(c, SG_ERR_INVALID, "variance-ratio marker index %d out of range", vr_markers[k]);
+    vrflag[vr_markers[k]] = 1;
+  }
+  std::vector<int32_t> sub0(nn);
+  bool identity = (nn == n_fam);
+  for (int64_t k = 0; k < nn; ++k) {
+    const int32_t s = sub_1based ? sub_1based[k] : (int32_t)(k + 1);
+    if (s < 1 || s > n_fam) return set_err(c, SG_ERR_INVALID, "subSampleInGeno[%lld] = %d out of range", (long long)k, s);
+    sub0[k] = s - 1;
+    if (sub0[k] != k) identity = false;
+  }
+  uint32_t* d_mask = nullptr;
+  uint8_t* d_vrflag = nullptr;
+  MarkerQC* d_qc = nullptr;
+  int32_t* d_sub = nullptr;
+  SG_TRY(dev_alloc_t(c, &d_mask, maskbits.size()));
+  SG_TRY(dev_alloc_t(c, &d_vrflag, (size_t)std::max<int64_t>(m_bim, 1)));
+  SG_TRY(dev_alloc_t(c, &d_qc, (size_t)std::max<int64_t>(m_bim, 1)));
+  SG_TRY(dev_alloc_t(c, &d_sub, (size_t)std::max<int64_t>(nn, 1)));
+  SG_CUDA(c, cudaMemcpyAsync(d_mask, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  if (m_bim) SG_CUDA(c, cudaMemcpyAsync(d_vrflag, vrflag.data(), m_bim, cudaMemcpyHostToDevice, c->stream));
+  if (nn) SG_CUDA(c, cudaMemcpyAsync(d_sub, sub0.data(), nn * 4, cudaMemcpyHostToDevice, c->stream));
+  launch_marker_qc(raw, raw_pitch, m_bim, n_fam, d_mask, nn, min_maf, max_missing, d_vrflag,
+                   min_mac_vr, is_var_ratio, d_qc, c->stream);
+  SG_LAUNCHED(c, 1);
+  std::vector<MarkerQC> qc(m_bim);
+  if (m_bim) SG_CUDA(c, cudaMemcpyAsync(qc.data(), d_qc, m_bim * sizeof(MarkerQC), cudaMemcpyDeviceToHost, c->stream));
+  SG_TRY(sync(c));
+  // marker compaction in .bim order (SNPIdx_new / SNPIdx_vr, FIT.cpp:900-947)
+  std::vector<int32_t> src_qc, src_vr;
+  c->freq.clear(); c->invstd.clear(); c->mac.clear(); c->qc_mask.assign(m_bim, 0);
+  c->vr_freq.clear(); c->vr_mac.clear(); c->vr_index.clear();
+  for (int64_t i = 0; i < m_bim; ++i) {
+    if (qc[i].pass_qc) {
+      src_qc.push_back((int32_t)i);
+      c->freq.push_back(qc[i].freq);
+      c->invstd.push_back(qc[i].invstd);
+      c->mac.push_back(qc[i].mac);
+      c->qc_mask[i] = 1;
+    }
+    if (qc[i].pass_vr) {
+      src_vr.push_back((int32_t)i);
+      c->vr_freq.push_back(qc[i].freq);
+      c->vr_mac.push_back(qc[i].mac);
+      c->vr_index.push_back((int32_t)i);
+    }
+  }
+  c->nn = nn;
+  c->n_fam = n_fam;
+  c->m_bim = m_bim;
+  c->m_qc = (int64_t)src_qc.size();
+  c->m_vr = (int64_t)src_vr.size();
+  c->is_diag_one = is_diag_one;
+  c->pitch = round_up(std::max<int64_t>((nn + 3) / 4, 1), kPitchAlign);
+  int32_t* d_src = nullptr;
+  const int64_t nsrc = std::max<int64_t>(c->m_qc + c->m_vr, 1);
+  SG_TRY(dev_alloc_t(c, &d_src, (size_t)nsrc));
+  std::vector<int32_t> srcs(src_qc);
+  srcs.insert(srcs.end(), src_vr.begin(), src_vr.end());
+  if (!srcs.empty())
+    SG_CUDA(c, cudaMemcpyAsync(d_src, srcs.data(), srcs.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  SG_TRY(dev_alloc_t(c, &c->d_packed, (size_t)std::max<int64_t>(c->m_qc * c->pitch, 16)));
+  SG_TRY(dev_alloc_t(c, &c->d_packed_vr, (size_t)std::max<int64_t>(c->m_vr * c->pitch, 16)));
+  SG_TRY(dev_alloc_t(c, &c->d_lut, (size_t)std::max<int64_t>(c->m_qc * 4, 4)));
+  SG_TRY(dev_alloc_t(c, &c->d_lut_vr, (size_t)std::max<int64_t>(c->m_vr * 4, 4)));
+  launch_repack(raw, raw_pitch, d_src, d_qc, c->m_qc, d_sub, nn, identity ? 1 : 0, c->d_packed,
+                c->pitch, c->stream);
+  launch_repack(raw, raw_pitch, d_src + c->m_qc, d_qc, c->m_vr, d_sub, nn, identity ? 1 : 0,
+                c->d_packed_vr, c->pitch, c->stream);
+  launch_lut(d_qc, d_src, c->m_qc, c->d_lut, c->stream);
+  launch_lut(d_qc, d_src + c->m_qc, c->m_vr, c->d_lut_vr, c->stream);
+  SG_LAUNCHED(c, 4);
+  SG_TRY(sync(c));
+  dev_free(c, d_src);
+  dev_free(c, d_mask);
+  dev_free(c, d_vrflag);
+  dev_free(c, d_qc);
+  dev_free(c, d_sub);
+  // GRM diagonal from the packed genotypes
+  SG_TRY(dev_alloc_t(c, &c->d_diag, (size_t)std::max<int64_t>(nn, 1)));
+  SG_TRY(dev_alloc_t(c, &c->d_diag32, (size_t)std::max<int64_t>(nn, 1)));
+  launch_diag(c->d_packed, c->pitch, c->d_lut, c->m_qc, nn, c->d_diag, c->d_diag32, c->stream);
+  SG_LAUNCHED(c, 1);
+  c->diag.resize(nn);
+  c->diag32.resize(nn);
+  if (nn) {
+    SG_CUDA(c, cudaMemcpyAsync(c->diag.data(), c->d_diag, nn * 8, cudaMemcpyDeviceToHost, c->stream));
+    SG_CUDA(c, cudaMemcpyAsync(c->diag32.data(), c->d_diag32, nn * 4, cudaMemcpyDeviceToHost, c->stream));
+  }
+  SG_TRY(sync(c));
+  c->have_geno = true;
+  return SG_OK;
+}
+
+static int setgeno_common(sg_ctx* c, const uint8_t* bed, bool on_device, uint64_t bed_len,
+                          int64_t n_fam, int64_t m_bim, const int32_t* sub_1based, int64_t n_sub,
+                          const uint8_t* pheno_mask, float min_maf, float max_missing,
+                          const int32_t* vr_markers, int64_t n_vr, float min_mac_vr,
+                          int is_var_ratio, int is_diag_one) {
+  if (!c) return SG_ERR_INVALID;
+  if (!bed || n_fam <= 0 || m_bim < 0 || n_sub <= 0 || n_sub > n_fam || (n_vr > 0 && !vr_markers))
+    return set_err(c, SG_ERR_INVALID, "setgeno: invalid arguments");
+  const int64_t nb = (n_fam + 3) / 4;
+  if (bed_len < (uint64_t)(3 + nb * m_bim))
+    return set_err(c, SG_ERR_INVALID, "setgeno: .bed has %llu bytes, need %lld",
+                   (unsigned long long)bed_len, (long long)(3 + nb * m_bim));
+  uint8_t magic[3];
+  if (on_device) {
+    SG_CUDA(c, cudaMemcpy(magic, bed, 3, cudaMemcpyDeviceToHost));
+  } else {
+    memcpy(magic, bed, 3);
+  }
+  if (magic[0] != 0x6C || magic[1] != 0x1B || magic[2] != 0x01)
+    return set_err(c, SG_ERR_INVALID, "setgeno: not a SNP-major PLINK .bed (magic %02x %02x %02x)",
+                   magic[0], magic[1], magic[2]);
+  free_geno(c);
+  const int64_t raw_pitch = round_up(std::max<int64_t>(nb, 1), kPitchAlign);
+  uint8_t* raw = nullptr;
+  SG_TRY(dev_alloc_t(c, &raw, (size_t)std::max<int64_t>(raw_pitch * m_bim, 16)));
+  SG_CUDA(c, cudaMemsetAsync(raw, 0, raw_pitch * std::max<int64_t>(m_bim, 1), c->stream));
+  if (m_bim)
+    SG_CUDA(c, cudaMemcpy2DAsync(raw, raw_pitch, bed + 3, nb, nb, m_bim,
+                                 on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 c->stream));
+  int rc = setgeno_core(c, raw, raw_pitch, n_fam, m_bim, sub_1based, n_sub, pheno_mask, min_maf,
+                        max_missing, vr_markers, n_vr, min_mac_vr, is_var_ratio, is_diag_one);
+  cudaStreamSynchronize(c->stream);
+  dev_free(c, raw);
+  return rc;
+}
+
+extern "C" int sg_setgeno(sg_ctx* c, const uint8_t* bed, uint64_t bed_len, int64_t n_fam,
+                          int64_t m_bim, const int32_t* sub_1based, int64_t n_sub,
+                          const uint8_t* pheno_mask, float min_maf, float max_missing,
+                          const int32_t* vr, int64_t n_vr, float min_mac_vr, int is_var_ratio,
+                          int is_diag_one) {
+  return setgeno_common(c, bed, false, bed_len, n_fam, m_bim, sub_1based, n_sub, pheno_mask, min_maf,
+                        max_missing, vr, n_vr, min_mac_vr, is_var_ratio, is_diag_one);
+}
+
+extern "C" int sg_setgeno_device(sg_ctx* c, const uint8_t* bed_dev, uint64_t bed_len, int64_t n_fam,
+                                 int64_t m_bim, const int32_t* sub_1based, int64_t n_sub,
+                                 const uint8_t* pheno_mask, float min_maf, float max_missing,
+                                 const int32_t* vr, int64_t n_vr, float min_mac_vr, int is_var_ratio,
+                                 int is_diag_one) {
+  return setgeno_common(c, bed_dev, true, bed_len, n_fam, m_bim, sub_1based, n_sub, pheno_mask,
+                        min_maf, max_missing, vr, n_vr, min_mac_vr, is_var_ratio, is_diag_one);
+}
+
+static int64_t count_lines(const char* path, bool* ok) {
+  std::ifstream f(path);
+  if (!f.is_open()) {
+    *ok = false;
+    return 0;
+  }
+  *ok = true;
+  int64_t n = 0;
+  std::string s;
+  while (std::getline(f, s)) ++n;
+  return n;
+}
+
+extern "C" int sg_setgeno_files(sg_ctx* c, const char* bed_path, const char* bim_path,
+                                const char* fam_path, const int32_t* sub_1based, int64_t n_sub,
+                                const uint8_t* pheno_mask, float min_maf, float max_missing,
+                                const int32_t* vr, int64_t n_vr, float min_mac_vr, int is_var_ratio,
+                                int is_diag_one) {
+  if (!c || !bed_path || !bim_path || !fam_path) return SG_ERR_INVALID;
+  bool ok1, ok2;
+  const int64_t n_fam = count_lines(fam_path, &ok1);
+  const int64_t m_bim = count_lines(bim_path, &ok2);
+  if (!ok1 || !ok2) return set_err(c, SG_ERR_IO, "cannot open %s", ok1 ? bim_path : fam_path);
+  std::ifstream f(bed_path, std::ios::binary);
+  if (!f.is_open()) return set_err(c, SG_ERR_IO, "cannot open %s", bed_path);
+  std::vector<uint8_t> bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  return sg_setgeno(c, bytes.data(), bytes.size(), n_fam, m_bim, sub_1based, n_sub, pheno_mask,
+                    min_maf, max_missing, vr, n_vr, min_mac_vr, is_var_ratio, is_diag_one);
+}
+
+#define NEED_GENO(c) \
+  do { if (!(c)) return SG_ERR_INVALID; if (!(c)->have_geno) return set_err((c), SG_ERR_STATE, "setgeno has not run"); } while (0)
+#define NEED_GRM(c) \
+  do { NEED_GENO(c); if (!(c)->have_grm) return set_err((c), SG_ERR_STATE, "sg_grm_build has not run"); } while (0)
+
+extern "C" int sg_geno_dims(sg_ctx* c, int64_t* n, int64_t* m_total, int64_t* m_qc, int64_t* m_vr) {
+  NEED_GENO(c);
+  if (n) *n = c->nn;
+  if (m_total) *m_total = c->m_bim;
+  if (m_qc) *m_qc = c->m_qc;
+  if (m_vr) *m_vr = c->m_vr;
+  return SG_OK;
+}
+extern "C" int sg_get_allele_freq(sg_ctx* c, float* out) {
+  NEED_GENO(c);
+  std::copy(c->freq.begin(), c->freq.end(), out);
+  return SG_OK;
+}
+extern "C" int sg_get_invstd(sg_ctx* c, float* out) {
+  NEED_GENO(c);
+  std::copy(c->invstd.begin(), c->invstd.end(), out);
+  return SG_OK;
+}
+extern "C" int sg_get_mac(sg_ctx* c, int32_t* out) {
+  NEED_GENO(c);
+  std::copy(c->mac.begin(), c->mac.end(), out);
+  return SG_OK;
+}
+extern "C" int sg_get_qc_marker_mask(sg_ctx* c, uint8_t* out) {
+  NEED_GENO(c);
+  std::copy(c->qc_mask.begin(), c->qc_mask.end(), out);
+  return SG_OK;
+}
+extern "C" int sg_get_vr_markers(sg_ctx* c, float* freq, int32_t* mac, int32_t* bim_index) {
+  NEED_GENO(c);
+  if (freq) std::copy(c->vr_freq.begin(), c->vr_freq.end(), freq);
+  if (mac) std::copy(c->vr_mac.begin(), c->vr_mac.end(), mac);
+  if (bim_index) std::copy(c->vr_index.begin(), c->vr_index.end(), bim_index);
+  return SG_OK;
+}
+extern "C" int sg_get_packed_geno(sg_ctx* c, uint8_t* out) {
+  NEED_GENO(c);
+  const int64_t nb = (c->nn + 3) / 4;
+  if (c->m_qc)
+    SG_CUDA(c, cudaMemcpy2D(out, nb, c->d_packed, c->pitch, nb, c->m_qc, cudaMemcpyDeviceToHost));
+  return SG_OK;
+}
+
+static int onesnp(sg_ctx* c, const uint8_t* packed, const float* lut, int64_t m, int64_t marker,
+                  int32_t* g, float* z) {
+  NEED_GENO(c);
+  if (marker < 0 || marker >= m) return set_err(c, SG_ERR_INVALID, "marker %lld out of range", (long long)marker);
+  int32_t* dg = nullptr;
+  float* dz = nullptr;
+  SG_TRY(dev_alloc_t(c, &dg, (size_t)c->nn));
+  SG_TRY(dev_alloc_t(c, &dz, (size_t)c->nn));
+  launch_unpack_marker(packed + marker * c->pitch, c->nn, lut + 4 * marker, dg, dz, c->stream);
+  SG_LAUNCHED(c, 1);
+  if (g) SG_CUDA(c, cudaMemcpyAsync(g, dg, c->nn * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (z) SG_CUDA(c, cudaMemcpyAsync(z, dz, c->nn * 4, cudaMemcpyDeviceToHost, c->stream));
+  SG_TRY(sync(c));
+  dev_free(c, dg);
+  dev_free(c, dz);
+  return SG_OK;
+}
+extern "C" int sg_get_onesnp_geno(sg_ctx* c, int64_t marker, int32_t* out) {
+  NEED_GENO(c);
+  return onesnp(c, c->d_packed, c->d_lut, c->m_qc, marker, out, nullptr);
+}
+extern "C" int sg_get_onesnp_geno_vr(sg_ctx* c, int64_t marker, int32_t* out) {
+  NEED_GENO(c);
+  return onesnp(c, c->d_packed_vr, c->d_lut_vr, c->m_vr, marker, out, nullptr);
+}
+extern "C" int sg_get_onesnp_stdgeno(sg_ctx* c, int64_t marker, float* out) {
+  NEED_GENO(c);
+  return onesnp(c, c->d_packed, c->d_lut, c->m_qc, marker, nullptr, out);
+}
+
+// ------------------------------------------------------------------ GRM build
+extern "C" int sg_grm_build(sg_ctx* c, int precision) {
+  NEED_GENO(c);
+  if (precision != SG_GRM_FP32_SIMT && precision != SG_GRM_BF16_TC && precision != SG_GRM_BF16X3_TC)
+    return set_err(c, SG_ERR_INVALID, "unknown GRM precision %d", precision);
+  if (precision != SG_GRM_FP32_SIMT && !tc_available())
+    return set_err(c, SG_ERR_INVALID, "tcgen05 SYRK needs an sm_103a device");
+  if (c->m_qc == 0) return set_err(c, SG_ERR_STATE, "no marker passed QC");
+  dev_free_t(c, c->d_K);
+  c->have_grm = false;
+  const int64_t np = round_up(c->nn, kRowTile);
+  const int64_t mp = round_up(c->m_qc, kMarkerTile);
+  c->np = np;
+  SG_TRY(dev_alloc_t(c, &c->d_K, (size_t)(np * np)));
+  const float scale = 1.0f / (float)c->m_qc;
+  if (precision == SG_GRM_FP32_SIMT) {
+    float* Z = nullptr;
+    SG_TRY(dev_alloc_t(c, &Z, (size_t)(np * mp)));
+    launch_zbuild_f32(c->d_packed, c->pitch, c->d_lut, c->m_qc, c->nn, np, mp, Z, c->stream);
+    launch_gemm_nt_f32(Z, mp, Z, mp, c->d_K, np, np, np, mp, scale, 2, c->stream);
+    SG_LAUNCHED(c, 2);
+    SG_TRY(sync(c));
+    dev_free(c, Z);
+  } else {
+    void* Zh = nullptr;
+    void* Zl = nullptr;
+    SG_TRY(dev_alloc(c, &Zh, (size_t)(np * mp * 2)));
+    if (precision == SG_GRM_BF16X3_TC) SG_TRY(dev_alloc(c, &Zl, (size_t)(np * mp * 2)));
+    launch_zbuild_bf16(c->d_packed, c->pitch, c->d_lut, c->m_qc, c->nn, np, mp, Zh, Zl, c->stream);
+    SG_LAUNCHED(c, 1);
+    cudaError_t e = tc_syrk_bf16(Zh, Zl, np, mp, c->d_K, scale, c->stream);
+    if (e != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 SYRK: %s", cudaGetErrorString(e));
+    SG_LAUNCHED(c, 1);
+    SG_TRY(sync(c));
+    dev_free(c, Zh);
+    dev_free(c, Zl);
+  }
+  c->have_grm = true;
+  return SG_OK;
+}
+
+extern "C" int sg_grm_diag(sg_ctx* c, double* out) {
+  NEED_GENO(c);
+  std::copy(c->diag.begin(), c->diag.end(), out);
+  return SG_OK;
+}
+extern "C" int sg_grm_diag_f32(sg_ctx* c, float* out) {
+  NEED_GENO(c);
+  std::copy(c->diag32.begin(), c->diag32.end(), out);
+  return SG_OK;
+}
+extern "C" int sg_grm_get(sg_ctx* c, float* out) {
+  NEED_GRM(c);
+  SG_CUDA(c, cudaMemcpy2D(out, c->nn * 4, c->d_K, c->np * 4, c->nn * 4, c->nn, cudaMemcpyDeviceToHost));
+  return SG_OK;
+}
+
+// ------------------------------------------------------------------ engine
+static void engine_free(sg_ctx* c) {
+  Engine& e = c->eng;
+  dev_free_t(c, e.X); dev_free_t(c, e.R); dev_free_t(c, e.Z); dev_free_t(c, e.P);
+  dev_free_t(c, e.B); dev_free_t(c, e.part); dev_free_t(c, e.winv); dev_free_t(c, e.minv);
+  dev_free_t(c, e.Yd); dev_free_t(c, e.Pf); dev_free_t(c, e.Yf); dev_free_t(c, e.d_st);
+  dev_free_t(c, e.d_ph); dev_free_t(c, e.d_cols);
+  e.cap_cols = e.cap_ph = 0;
+}
+
+static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
+  NEED_GRM(c);
+  Engine& e = c->eng;
+  max_columns = round_up(std::max<int64_t>(max_columns, 32), 32);
+  max_phenos = std::max<int64_t>(max_phenos, 1);
+  if (e.cap_cols >= max_columns && e.cap_ph >= max_phenos && e.np == c->np) return SG_OK;
+  for (auto& kv : e.reqs)
+    if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "engine busy: cannot grow while columns run");
+  max_columns = std::max(max_columns, e.np == c->np ? e.cap_cols : 0);
+  max_phenos = std::max(max_phenos, e.np == c->np ? e.cap_ph : 0);
+  std::vector<PhenoState> old_ph = e.h_ph;
+  std::vector<char> old_set = e.ph_set;
+  engine_free(c);
+  const int64_t np = c->np;
+  e.np = np;
+  e.nblk = pcg_nblk(np);
+  e.stage_cols = std::min<int64_t>(max_columns, 256);
+  const size_t V = (size_t)(max_columns * np);
+  SG_TRY(dev_alloc_t(c, &e.X, V)); SG_TRY(dev_alloc_t(c, &e.R, V));
+  SG_TRY(dev_alloc_t(c, &e.Z, V)); SG_TRY(dev_alloc_t(c, &e.P, V));
+  SG_TRY(dev_alloc_t(c, &e.Pf, V)); SG_TRY(dev_alloc_t(c, &e.Yf, V));
+  SG_TRY(dev_alloc_t(c, &e.B, (size_t)(e.stage_cols * np)));
+  SG_TRY(dev_alloc_t(c, &e.part, (size_t)(max_columns * e.nblk * 2)));
+  SG_TRY(dev_alloc_t(c, &e.winv, (size_t)(max_phenos * np)));
+  SG_TRY(dev_alloc_t(c, &e.minv, (size_t)(max_phenos * np)));
+  SG_TRY(dev_alloc_t(c, &e.d_st, (size_t)max_columns));
+  SG_TRY(dev_alloc_t(c, &e.d_ph, (size_t)max_phenos));
+  SG_TRY(dev_alloc_t(c, &e.d_cols, (size_t)max_columns));
+  SG_CUDA(c, cudaMemsetAsync(e.Pf, 0, V * 4, c->stream));
+  SG_CUDA(c, cudaMemsetAsync(e.P, 0, V * 8, c->stream));
+  SG_CUDA(c, cudaMemsetAsync(e.winv, 0, (size_t)(max_phenos * np) * 8, c->stream));
+  SG_CUDA(c, cudaMemsetAsync(e.minv, 0, (size_t)(max_phenos * np) * 8, c->stream));
+  e.cap_cols = max_columns;
+  e.cap_ph = max_phenos;
+  e.h_st.assign(max_columns, ColState{});
+  for (auto& s : e.h_st) { s.kind = -1; s.active = 0; }
+  SG_CUDA(c, cudaMemcpyAsync(e.d_st, e.h_st.data(), max_columns * sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+  e.col_req.assign(max_columns, -1);
+  e.h_ph.assign(max_phenos, PhenoState{0.0, 0.0});
+  e.ph_set.assign(max_phenos, 0);
+  e.hi_col = 0;
+  e.n_active = 0;
+  e.queue.clear();
+  e.reqs.clear();
+  SG_TRY(sync(c));
+  (void)old_ph; (void)old_set;
+  return SG_OK;
+}
+
+extern "C" int sg_engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
+  return engine_reserve(c, max_columns, max_phenos);
+}
+
+// getDiagOfSigma in FP64 (FIT.cpp:2322-2365) for the Jacobi preconditioner
+static void diag_sigma_f64(const sg_ctx* c, const double* w, const double* tau, double* d) {
+  for (int64_t i = 0; i < c->nn; ++i) {
+    double v = c->is_diag_one ? tau[1] + tau[0] / w[i]
+                              : tau[1] * c->diag[i] / (double)c->m_qc + tau[0] / w[i];
+    d[i] = v < 1e-4 ? 1e-4 : v;
+  }
+}
+
+extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, const double* tau,
+                                   const uint8_t* mask) {
+  NEED_GRM(c);
+  Engine& e = c->eng;
+  if (e.cap_ph == 0) SG_TRY(engine_reserve(c, 128, std::max<int64_t>(slot + 1, 1)));
+  if (slot < 0 || slot >= e.cap_ph) return set_err(c, SG_ERR_INVALID, "phenotype slot %lld out of range", (long long)slot);
+  if (!w || !tau) return set_err(c, SG_ERR_INVALID, "null w/tau");
+  if (!all_finite(tau, 2)) return set_err(c, SG_ERR_NUMERIC, "tau is not finite");
+  for (int64_t i = 0; i < c->nn; ++i)
+    if ((!mask || mask[i]) && !(std::isfinite(w[i]) && w[i] > 0.0))
+      return set_err(c, SG_ERR_NUMERIC, "W[%lld] = %g is not a positive finite weight", (long long)i, w[i]);
+  for (auto& kv : e.reqs)
+    if (kv.second.state == 1 && kv.second.slot == slot)
+      return set_err(c, SG_ERR_STATE, "phenotype slot %lld has columns in flight", (long long)slot);
+  std::vector<double> d(c->nn), winv(e.np, 0.0), minv(e.np, 0.0);
+  diag_sigma_f64(c, w, tau, d.data());
+  for (int64_t i = 0; i < c->nn; ++i) {
+    if (mask && !mask[i]) continue;
+    winv[i] = 1.0 / w[i];
+    minv[i] = 1.0 / d[i];
+  }
+  SG_CUDA(c, cudaMemcpyAsync(e.winv + slot * e.np, winv.data(), e.np * 8, cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(c, cudaMemcpyAsync(e.minv + slot * e.np, minv.data(), e.np * 8, cudaMemcpyHostToDevice, c->stream));
+  e.h_ph[slot] = PhenoState{tau[0], tau[1]};
+  SG_CUDA(c, cudaMemcpyAsync(e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), cudaMemcpyHostToDevice, c->stream));
+  e.ph_set[slot] = 1;
+  return sync(c);
+}
+
+static int engine_submit_common(sg_ctx* c, int64_t slot, int kind, const double* B, bool probe,
+                                uint64_t seed, int64_t run0, int64_t k, int maxiter, double tol,
+                                int64_t* ids) {
+  NEED_GRM(c);
+  Engine& e = c->eng;
+  if (slot < 0 || slot >= e.cap_ph || !e.ph_set[slot])
+    return set_err(c, SG_ERR_STATE, "phenotype slot %lld not set", (long long)slot);
+  if (kind != 0 && kind != 1) return set_err(c, SG_ERR_INVALID, "kind must be 0 or 1");
+  if (k < 0 || (!probe && k > 0 && !B)) return set_err(c, SG_ERR_INVALID, "bad RHS block");
+  if (!probe && !all_finite(B, k * c->nn)) return set_err(c, SG_ERR_NUMERIC, "right-hand side has NaN/Inf");
+  for (int64_t j = 0; j < k; ++j) {
+    Req r;
+    r.id = e.next_id++;
+    r.slot = slot;
+    r.kind = kind;
+    r.maxiter = maxiter;
+    r.tol = tol;
+    r.probe = probe;
+    r.seed = seed;
+    r.run = run0 + j;
+    if (!probe) r.b.assign(B + j * c->nn, B + (j + 1) * c->nn);
+    if (ids) ids[j] = r.id;
+    e.queue.push_back(r.id);
+    e.reqs.emplace(r.id, std::move(r));
+  }
+  return SG_OK;
+}
+
+extern "C" int sg_engine_submit(sg_ctx* c, int64_t slot, int kind, const double* B, int64_t k,
+                                int maxiter, double tol, int64_t* ids) {
+  return engine_submit_common(c, slot, kind, B, false, 0, 0, k, maxiter, tol, ids);
+}
+extern "C" int sg_engine_submit_probes(sg_ctx* c, int64_t slot, int kind, uint64_t seed, int64_t run0,
+                                       int64_t k, int maxiter, double tol, int64_t* ids) {
+  return engine_submit_common(c, slot, kind, nullptr, true, seed, run0, k, maxiter, tol, ids);
+}
+
+// Move queued requests into free columns, staged through e.B, and initialise them.
+static int engine_admit(sg_ctx* c) {
+  Engine& e = c->eng;
+  while (!e.queue.empty()) {
+    std::vector<int32_t> cols;
+    std::vector<int64_t> admitted;
+    int64_t col = 0;
+    while (!e.queue.empty() && (int64_t)cols.size() < e.stage_cols) {
+      while (col < e.cap_cols && e.col_req[col] != -1) ++col;
+      if (col >= e.cap_cols) break;
+      const int64_t id = e.queue.front();
+      e.queue.pop_front();
+      auto it = e.reqs.find(id);
+      if (it == e.reqs.end()) continue;  // cancelled
+      Req& r = it->second;
+      const int64_t sel = (int64_t)cols.size();
+      if (r.probe) {
+        launch_probe_fill(e.np, c->nn, r.seed, r.run, 1, e.B + sel * e.np, c->stream);
+        c->launches += 1;
+      } else {
+        SG_CUDA(c, cudaMemcpyAsync(e.B + sel * e.np, r.b.data(), c->nn * 8, cudaMemcpyHostToDevice, c->stream));
+        if (e.np > c->nn)
+          SG_CUDA(c, cudaMemsetAsync(e.B + sel * e.np + c->nn, 0, (e.np - c->nn) * 8, c->stream));
+      }
+      ColState s{};
+      s.pheno = (int32_t)r.slot;
+      s.kind = r.kind;
+      s.maxiter = r.maxiter;
+      s.tol = r.tol;
+      e.h_st[col] = s;
+      SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &e.h_st[col], sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+      e.col_req[col] = id;
+      r.col = col;
+      r.state = 1;
+      cols.push_back((int32_t)col);
+      admitted.push_back(id);
+      e.hi_col = std::max(e.hi_col, col + 1);
+      ++col;
+    }
+    if (cols.empty()) break;
+    SG_CUDA(c, cudaMemcpyAsync(e.d_cols, cols.data(), cols.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    launch_pcg_init(e.np, e.cap_cols, e.d_cols, (int64_t)cols.size(), e.d_st, e.d_ph, e.minv, e.B,
+                    e.X, e.R, e.Z, e.P, e.Pf, e.part, e.nblk, c->stream);
+    SG_LAUNCHED(c, 2);
+    // for the FP64 plain engine the product columns read P: stage b there too
+    if (c->mv_mode == SG_MV_FP64_PLAIN) {
+      for (size_t k = 0; k < cols.size(); ++k) {
+        if (e.h_st[cols[k]].kind == 1)
+          SG_CUDA(c, cudaMemcpyAsync(e.P + (int64_t)cols[k] * e.np, e.B + (int64_t)k * e.np, e.np * 8,
+                                     cudaMemcpyDeviceToDevice, c->stream));
+      }
+    }
+    // staging buffer is reused by the next batch: wait for init to read it
+    SG_TRY(sync(c));
+    e.n_active += (int64_t)cols.size();
+    if ((int64_t)cols.size() < e.stage_cols) break;
+  }
+  return SG_OK;
+}
+
+static int engine_gemm(sg_ctx* c, int64_t ncols, bool* used_yf) {
+  Engine& e = c->eng;
+  *used_yf = true;
+  if (c->mv_mode == SG_MV_FP64_PLAIN) {
+    *used_yf = false;
+    if (!e.Yd) SG_TRY(dev_alloc_t(c, &e.Yd, (size_t)(e.cap_cols * e.np)));
+    for (int64_t col = 0; col < ncols; ++col) {
+      if (!e.h_st[col].active) continue;
+      launch_gemv_f64(c->d_K, e.np, e.np, e.P + col * e.np, e.Yd + col * e.np, c->stream);
+      c->launches += 1;
+    }
+    return SG_OK;
+  }
+  if (c->mv_mode == SG_MV_TF32_TC) {
+    cudaError_t err = tc_gemm_tf32(c->d_K, e.np, e.Pf, ncols, e.Yf, c->stream);
+    if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 GRM.V: %s", cudaGetErrorString(err));
+    c->launches += 1;
+    return SG_OK;
+  }
+  launch_gemm_nt_f32(c->d_K, e.np, e.Pf, e.np, e.Yf, e.np, e.np, ncols, e.np, 1.0f, 1, c->stream);
+  c->launches += 1;
+  return SG_OK;
+}
+
+// One engine step over columns [0, hi_col): GRM product + the FP64 PCG vector work.
+static int engine_step(sg_ctx* c, int64_t* n_finished) {
+  Engine& e = c->eng;
+  const int64_t ncols = round_up(e.hi_col, 32);
+  bool yf = true;
+  SG_TRY(engine_gemm(c, ncols, &yf));
+  const float* Yf = yf ? e.Yf : nullptr;
+  const double* Yd = yf ? nullptr : e.Yd;
+  launch_pcg_sigma_dot(e.np, e.hi_col, e.d_st, e.d_ph, e.winv, e.minv, e.P, Yf, Yd, e.part, e.nblk, c->stream);
+  launch_pcg_alpha(e.hi_col, e.d_st, e.part, e.nblk, c->stream);
+  launch_pcg_update(e.np, e.hi_col, e.d_st, e.d_ph, e.winv, e.minv, e.X, e.R, e.Z, e.P, Yf, Yd,
+                    e.part, e.nblk, c->stream);
+  launch_pcg_beta(e.hi_col, e.d_st, e.part, e.nblk, c->stream);
+  launch_pcg_dir(e.np, e.hi_col, e.d_st, e.Z, e.P, e.Pf, c->stream);
+  SG_LAUNCHED(c, 5);
+  SG_CUDA(c, cudaMemcpyAsync(e.h_st.data(), e.d_st, e.hi_col * sizeof(ColState), cudaMemcpyDeviceToHost, c->stream));
+  SG_TRY(sync(c));
+  e.steps += 1;
+  e.grm_passes += 1;
+  int64_t fin = 0;
+  for (int64_t col = 0; col < e.hi_col; ++col) {
+    const int64_t id = e.col_req[col];
+    if (id < 0) continue;
+    ColState& s = e.h_st[col];
+    e.col_iters += 1;
+    if (s.active) continue;
+    auto it = e.reqs.find(id);
+    if (it != e.reqs.end()) {
+      Req& r = it->second;
+      r.x.resize(c->nn);
+      SG_CUDA(c, cudaMemcpyAsync(r.x.data(), e.X + col * e.np, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
+      r.iters = s.kind == 1 ? 1 : s.iter;
+      r.state = 2;
+      r.col = -1;
+    }
+    e.col_req[col] = -1;
+    s.kind = -1;
+    s.active = 0;
+    s.just_done = 0;
+    SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+    e.n_active -= 1;
+    e.retired += 1;
+    ++fin;
+  }
+  while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
+  SG_TRY(sync(c));
+  *n_finished += fin;
+  return SG_OK;
+}
+
+// Columns admitted with r'r <= tol retire without a step (iter = 0, x = 0).
+static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
+  Engine& e = c->eng;
+  if (e.hi_col == 0) return SG_OK;
+  SG_CUDA(c, cudaMemcpyAsync(e.h_st.data(), e.d_st, e.hi_col * sizeof(ColState), cudaMemcpyDeviceToHost, c->stream));
+  SG_TRY(sync(c));
+  for (int64_t col = 0; col < e.hi_col; ++col) {
+    const int64_t id = e.col_req[col];
+    if (id < 0) continue;
+    ColState& s = e.h_st[col];
+    if (s.kind != 0 || s.active || !s.just_done) continue;
+    auto it = e.reqs.find(id);
+    if (it != e.reqs.end()) {
+      it->second.x.assign(c->nn, 0.0);
+      it->second.iters = 0;
+      it->second.state = 2;
+      it->second.col = -1;
+    }
+    e.col_req[col] = -1;
+    s.kind = -1;
+    s.just_done = 0;
+    SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+    e.n_active -= 1;
+    e.retired += 1;
+    *n_finished += 1;
+  }
+  while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
+  return sync(c);
+}
+
+extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) {
+  NEED_GRM(c);
+  Engine& e = c->eng;
+  if (e.cap_cols == 0) return set_err(c, SG_ERR_STATE, "engine not reserved");
+  int64_t fin = 0;
+  for (int64_t s = 0; s < max_steps; ++s) {
+    SG_TRY(engine_admit(c));
+    SG_TRY(engine_retire_immediate(c, &fin));
+    if (fin > 0) break;
+    if (e.n_active == 0) break;
+    SG_TRY(engine_step(c, &fin));
+    if (fin > 0) break;
+  }
+  if (n_finished) *n_finished = fin;
+  return SG_OK;
+}
+
+extern "C" int sg_engine_fetch(sg_ctx* c, int64_t id, double* x, int32_t* iters) {
+  if (!c) return SG_ERR_INVALID;
+  Engine& e = c->eng;
+  auto it = e.reqs.find(id);
+  if (it == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
+  if (it->second.state != 2) return set_err(c, SG_ERR_STATE, "request %lld not finished", (long long)id);
+  if (x) std::copy(it->second.x.begin(), it->second.x.end(), x);
+  if (iters) *iters = it->second.iters;
+  e.reqs.erase(it);
+  return SG_OK;
+}
+
+extern "C" int sg_engine_cancel(sg_ctx* c, int64_t id) {
+  if (!c) return SG_ERR_INVALID;
+  Engine& e = c->eng;
+  auto it = e.reqs.find(id);
+  if (it == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
+  Req& r = it->second;
+  if (r.state == 1 && r.col >= 0) {
+    ColState s{};
+    s.kind = -1;
+    s.active = 0;
+    e.h_st[r.col] = s;
+    SG_CUDA(c, cudaMemcpyAsync(e.d_st + r.col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+    SG_CUDA(c, cudaMemsetAsync(e.Pf + r.col * e.np, 0, e.np * 4, c->stream));
+    e.col_req[r.col] = -1;
+    e.n_active -= 1;
+    while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
+    SG_TRY(sync(c));
+  }
+  e.reqs.erase(it);  // a queued id is skipped at admission
+  return SG_OK;
+}
+
+extern "C" int sg_engine_stats(sg_ctx* c, int64_t* s4) {
+  if (!c || !s4) return SG_ERR_INVALID;
+  s4[0] = c->eng.steps;
+  s4[1] = c->eng.retired;
+  s4[2] = c->eng.col_iters;
+  s4[3] = c->eng.grm_passes;
+  return SG_OK;
+}
+
+// ------------------------------------------------------------------ drop-in helpers (FP64 host LA)
+namespace {
+
+// run the engine until every id in ``ids`` has finished
+int run_until(sg_ctx* c, const std::vector<int64_t>& ids) {
+  Engine& e = c->eng;
+  for (;;) {
+    bool all = true;
+    for (int64_t id : ids) {
+      auto it = e.reqs.find(id);
+      if (it != e.reqs.end() && it->second.state != 2) { all = false; break; }
+    }
+    if (all) return SG_OK;
+    int64_t fin = 0;
+    const int64_t before = e.steps;
+    SG_TRY(sg_engine_run(c, 1 << 20, &fin));
+    if (fin == 0 && e.steps == before && e.n_active == 0 && e.queue.empty())
+      return set_err(c, SG_ERR_STATE, "engine idle with unfinished requests");
+  }
+}
+
+int fetch(sg_ctx* c, int64_t id, double* x, int32_t* it) { return sg_engine_fetch(c, id, x, it); }
+
+// Drop-ins run on phenotype slot 0 with capacity for one probe block.
+int dropin_setup(sg_ctx* c, const float* w, const float* tau, int64_t cols) {
+  NEED_GRM(c);
+  Engine& e = c->eng;
+  if (e.cap_cols < cols || e.cap_ph < 1 || e.np != c->np) SG_TRY(engine_reserve(c, std::max<int64_t>(cols, 128), 1));
+  std::vector<double> wd(c->nn);
+  for (int64_t i = 0; i < c->nn; ++i) wd[i] = w[i];
+  const double td[2] = {tau[0], tau[1]};
+  return sg_engine_set_pheno(c, 0, wd.data(), td, nullptr);
+}
+
+void f2d(const float* a, int64_t n, std::vector<double>& out) {
+  out.resize(n);
+  for (int64_t i = 0; i < n; ++i) out[i] = a[i];
+}
+
+// inverse of a symmetric positive definite matrix (upper triangle used, like
+// arma::symmatu) by Cholesky; falls back to the pseudo-inverse from a Jacobi
+// eigen-decomposition (arma::pinv) when it is not positive definite.
+std::vector<double> inv_sympd(const std::vector<double>& A0, int p) {
+  std::vector<double> A(p * p);
+  for (int i = 0; i < p; ++i)
+    for (int j = 0; j < p; ++j) A[i + j * p] = (i <= j) ? A0[i + j * p] : A0[j + i * p];
+  std::vector<double> L(p * p, 0.0);
+  bool ok = true;
+  for (int j = 0; j < p && ok; ++j) {
+    double s = A[j + j * p];
+    for (int k = 0; k < j; ++k) s -= L[j + k * p] * L[j + k * p];
+    if (!(s > 0.0)) { ok = false; break; }
+    L[j + j * p] = std::sqrt(s);
+    for (int i = j + 1; i < p; ++i) {
+      double t = A[i + j * p];
+      for (int k = 0; k < j; ++k) t -= L[i + k * p] * L[j + k * p];
+      L[i + j * p] = t / L[j + j * p];
+    }
+  }
+  std::vector<double> inv(p * p, 0.0);
+  if (ok) {
+    std::vector<double> Li(p * p, 0.0);  // L^-1
+    for (int j = 0; j < p; ++j) {
+      Li[j + j * p] = 1.0 / L[j + j * p];
+      for (int i = j + 1; i < p; ++i) {
+        double s = 0.0;
+        for (int k = j; k < i; ++k) s += L[i + k * p] * Li[k + j * p];
+        Li[i + j * p] = -s / L[i + i * p];
+      }
+    }
+    for (int i = 0; i < p; ++i)
+      for (int j = 0; j < p; ++j) {
+        double s = 0.0;
+        for (int k = std::max(i, j); k < p; ++k) s += Li[k + i * p] * Li[k + j * p];
+        inv[i + j * p] = s;
+      }
+    return inv;
+  }
+  // Jacobi eigen-decomposition, pseudo-inverse with tolerance p * max|lambda| * eps
+  std::vector<double> V(p * p, 0.0), D(A);
+  for (int i = 0; i < p; ++i) V[i + i * p] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int i = 0; i < p; ++i)
+      for (int j = i + 1; j < p; ++j) off += D[i + j * p] * D[i + j * p];
+    if (off < 1e-30) break;
+    for (int pi = 0; pi < p; ++pi)
+      for (int q = pi + 1; q < p; ++q) {
+        const double apq = D[pi + q * p];
+        if (std::fabs(apq) < 1e-300) continue;
+        const double theta = (D[q + q * p] - D[pi + pi * p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < p; ++k) {
+          const double dkp = D[k + pi * p], dkq = D[k + q * p];
+          D[k + pi * p] = cs * dkp - sn * dkq;
+          D[k + q * p] = sn * dkp + cs * dkq;
+        }
+        for (int k = 0; k < p; ++k) {
+          const double dpk = D[pi + k * p], dqk = D[q + k * p];
+          D[pi + k * p] = cs * dpk - sn * dqk;
+          D[q + k * p] = sn * dpk + cs * dqk;
+        }
+        for (int k = 0; k < p; ++k) {
+          const double vkp = V[k + pi * p], vkq = V[k + q * p];
+          V[k + pi * p] = cs * vkp - sn * vkq;
+          V[k + q * p] = sn * vkp + cs * vkq;
+        }
+      }
+  }
+  double mx = 0.0;
+  for (int i = 0; i < p; ++i) mx = std::max(mx, std::fabs(D[i + i * p]));
+  const double tolv = p * mx * 2.220446049250313e-16;
+  for (int i = 0; i < p; ++i)
+    for (int j = 0; j < p; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < p; ++k) {
+        const double l = D[k + k * p];
+        if (std::fabs(l) > tolv) s += V[i + k * p] * V[j + k * p] / l;
+      }
+      inv[i + j * p] = s;
+    }
+  return inv;
+}
+
+// P v = Sv - SX cov (SX' v) with SX n x p (column-major), cov p x p
+void p_apply(int64_t n, int p, const double* Sv, const double* SX, const double* cov, const double* v,
+             double* out) {
+  std::vector<double> t(p, 0.0), u(p, 0.0);
+  for (int j = 0; j < p; ++j) {
+    double s = 0.0;
+    for (int64_t i = 0; i < n; ++i) s += SX[i + j * n] * v[i];
+    t[j] = s;
+  }
+  for (int i = 0; i < p; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < p; ++j) s += cov[i + j * p] * t[j];
+    u[i] = s;
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < p; ++j) s += SX[i + j * n] * u[j];
+    out[i] = Sv[i] - s;
+  }
+}
+
+double dot(int64_t n, const double* a, const double* b) {
+  double s = 0.0;
+  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+double cal_cv(const std::vector<double>& x) {
+  const int64_t n = (int64_t)x.size();
+  double m = 0.0;
+  for (double v : x) m += v;
+  m /= n;
+  double ss = 0.0;
+  for (double v : x) ss += (v - m) * (v - m);
+  const double sd = std::sqrt(ss / (n - 1));
+  return (sd / m) / n;
+}
+
+struct TraceOut {
+  double tr1 = 0.0, tr0 = 0.0;
+  int nrun = 0;
+};
+
+// GetTrace / GetTrace_q on the engine: each block of probes is submitted as
+// PCG columns (Sigma^-1 u) and product columns (K u) together.
+int trace_probes(sg_ctx* c, const std::vector<double>& SX, int p, const std::vector<double>& cov,
+                 int nrun, int maxiter, double tol, double cutoff, uint64_t seed, bool quant,
+                 const std::vector<int64_t>& extra_ids, TraceOut* out) {
+  const int64_t n = c->nn;
+  std::vector<double> t1, t0;
+  int start = 0, end = nrun;
+  std::vector<double> u(n), su(n), au(n), pu(n);
+  bool first = true;
+  for (;;) {
+    const int k = end - start;
+    std::vector<int64_t> pid(k), aid(k);
+    SG_TRY(sg_engine_submit_probes(c, 0, 0, seed, start, k, maxiter, tol, pid.data()));
+    SG_TRY(sg_engine_submit_probes(c, 0, 1, seed, start, k, maxiter, tol, aid.data()));
+    std::vector<int64_t> all(pid);
+    all.insert(all.end(), aid.begin(), aid.end());
+    if (first) all.insert(all.end(), extra_ids.begin(), extra_ids.end());
+    first = false;
+    SG_TRY(run_until(c, all));
+    for (int j = 0; j < k; ++j) {
+      for (int64_t i = 0; i < n; ++i) u[i] = (hash3(seed, (uint64_t)(start + j), (uint64_t)i) >> 63) ? 1.0 : -1.0;
+      SG_TRY(fetch(c, pid[j], su.data(), nullptr));
+      SG_TRY(fetch(c, aid[j], au.data(), nullptr));
+      p_apply(n, p, su.data(), SX.data(), cov.data(), u.data(), pu.data());
+      t1.push_back(dot(n, au.data(), pu.data()));
+      t0.push_back(dot(n, u.data(), pu.data()));
+    }
+    const double cv1 = cal_cv(t1);
+    const double cv0 = quant ? cal_cv(t0) : 0.0;
+    if (cv1 > cutoff || (quant && cv0 > cutoff)) {
+      start = end;
+      end += 10;
+      continue;
+    }
+    break;
+  }
+  double s1 = 0.0, s0 = 0.0;
+  for (double v : t1) s1 += v;
+  for (double v : t0) s0 += v;
+  out->tr1 = s1 / t1.size();
+  out->tr0 = s0 / t0.size();
+  out->nrun = (int)t1.size();
+  return SG_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ drop-ins
+extern "C" int sg_grm_matmul(sg_ctx* c, const double* V, int64_t k, double* out) {
+  NEED_GRM(c);
+  if (k <= 0 || !V || !out) return set_err(c, SG_ERR_INVALID, "bad arguments");
+  Engine& e = c->eng;
+  if (e.cap_ph < 1 || !e.ph_set[0]) {
+    std::vector<float> w(c->nn, 1.0f);
+    const float tau[2] = {1.0f, 0.0f};
+    SG_TRY(dropin_setup(c, w.data(), tau, std::min<int64_t>(k, 256)));
+  }
+  std::vector<int64_t> ids(k);
+  SG_TRY(sg_engine_submit(c, 0, 1, V, k, 1, 0.0, ids.data()));
+  SG_TRY(run_until(c, ids));
+  for (int64_t j = 0; j < k; ++j) SG_TRY(fetch(c, ids[j], out + j * c->nn, nullptr));
+  return SG_OK;
+}
+
+extern "C" int sg_getCrossprodMatAndKin(sg_ctx* c, const float* b, float* out) {
+  NEED_GRM(c);
+  std::vector<double> bd, od(c->nn);
+  f2d(b, c->nn, bd);
+  SG_TRY(sg_grm_matmul(c, bd.data(), 1, od.data()));
+  for (int64_t i = 0; i < c->nn; ++i) out[i] = (float)od[i];
+  return SG_OK;
+}
+
+extern "C" int sg_getDiagOfSigma(sg_ctx* c, const float* w, const float* tau, float* out) {
+  NEED_GENO(c);
+  // float arithmetic in the reference's order: (tau1 * diag) / M + tau0 / w, floored at 1e-4
+  const float M = (float)c->m_qc;
+  for (int64_t i = 0; i < c->nn; ++i) {
+    float v = c->is_diag_one ? tau[1] + tau[0] / w[i] : (tau[1] * c->diag32[i]) / M + tau[0] / w[i];
+    out[i] = v < 1e-4f ? 1e-4f : v;
+  }
+  return SG_OK;
+}
+
+extern "C" int sg_getCrossprod(sg_ctx* c, const float* b, const float* w, const float* tau, float* out) {
+  NEED_GRM(c);
+  const int64_t n = c->nn;
+  if (tau[1] == 0.0f) {
+    for (int64_t i = 0; i < n; ++i) out[i] = tau[0] * (b[i] * (1.0f / w[i]));
+    return SG_OK;
+  }
+  std::vector<float> kb(n);
+  SG_TRY(sg_getCrossprodMatAndKin(c, b, kb.data()));
+  for (int64_t i = 0; i < n; ++i) out[i] = tau[0] * (b[i] * (1.0f / w[i])) + tau[1] * kb[i];
+  return SG_OK;
+}
+
+extern "C" int sg_pcg_solve(sg_ctx* c, const double* w, const double* tau, const double* B, int64_t k,
+                            int maxiter, double tol, double* X, int32_t* iters) {
+  NEED_GRM(c);
+  if (k <= 0 || !w || !tau || !B || !X) return set_err(c, SG_ERR_INVALID, "bad arguments");
+  Engine& e = c->eng;
+  if (e.cap_cols < std::min<int64_t>(k, 256) || e.cap_ph < 1)
+    SG_TRY(engine_reserve(c, std::min<int64_t>(std::max<int64_t>(k, 128), 2048), 1));
+  SG_TRY(sg_engine_set_pheno(c, 0, w, tau, nullptr));
+  std::vector<int64_t> ids(k);
+  SG_TRY(sg_engine_submit(c, 0, 0, B, k, maxiter, tol, ids.data()));
+  SG_TRY(run_until(c, ids));
+  for (int64_t j = 0; j < k; ++j) SG_TRY(fetch(c, ids[j], X + j * c->nn, iters ? iters + j : nullptr));
+  return SG_OK;
+}
+
+static int solve_f32(sg_ctx* c, const float* w, const float* tau, const float* B, int64_t k, int maxiter,
+                     float tol, float* out, int32_t* iters) {
+  NEED_GRM(c);
+  const int64_t n = c->nn;
+  if (!all_finite(w, n) || !all_finite(tau, 2)) return set_err(c, SG_ERR_NUMERIC, "W or tau not finite");
+  std::vector<double> wd, bd, xd(n * k);
+  f2d(w, n, wd);
+  f2d(B, n * k, bd);
+  const double td[2] = {tau[0], tau[1]};
+  SG_TRY(sg_pcg_solve(c, wd.data(), td, bd.data(), k, maxiter, (double)tol, xd.data(), iters));
+  for (int64_t i = 0; i < n * k; ++i) out[i] = (float)xd[i];
+  return SG_OK;
+}
+
+extern "C" int sg_getPCG1ofSigmaAndVector(sg_ctx* c, const float* w, const float* tau, const float* b,
+                                          int maxiter, float tol, float* out, int32_t* iters) {
+  return solve_f32(c, w, tau, b, 1, maxiter, tol, out, iters);
+}
+extern "C" int sg_getSigma_X(sg_ctx* c, const float* w, const float* tau, const float* X, int64_t p,
+                             int maxiter, float tol, float* out) {
+  return solve_f32(c, w, tau, X, p, maxiter, tol, out, nullptr);
+}
+extern "C" int sg_getSigma_G(sg_ctx* c, const float* w, const float* tau, const float* g, int maxiter,
+                             float tol, float* out) {
+  return solve_f32(c, w, tau, g, 1, maxiter, tol, out, nullptr);
+}
+
+extern "C" int sg_getCoefficients(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* w,
+                                  const float* tau, int maxiter, float tol, float* Sigma_iY,
+                                  float* Sigma_iX, float* cov, float* alpha, float* eta) {
+  NEED_GRM(c);
+  const int64_t n = c->nn;
+  if (p <= 0) return set_err(c, SG_ERR_INVALID, "p must be positive");
+  std::vector<float> B(n * (p + 1));
+  std::copy(Y, Y + n, B.begin());
+  std::copy(X, X + n * p, B.begin() + n);
+  std::vector<float> S(n * (p + 1));
+  SG_TRY(solve_f32(c, w, tau, B.data(), p + 1, maxiter, tol, S.data(), nullptr));
+  std::vector<double> SY(n), SX(n * p), Xd, Yd;
+  for (int64_t i = 0; i < n; ++i) SY[i] = S[i];
+  for (int64_t i = 0; i < n * p; ++i) SX[i] = S[n + i];
+  f2d(X, n * p, Xd);
+  f2d(Y, n, Yd);
+  std::vector<double> XtSX(p * p);
+  for (int a = 0; a < p; ++a)
+    for (int b = 0; b < p; ++b) XtSX[a + b * p] = dot(n, &Xd[a * n], &SX[b * n]);
+  std::vector<double> cv = inv_sympd(XtSX, (int)p);
+  std::vector<double> sxy(p), al(p, 0.0);
+  for (int j = 0; j < p; ++j) sxy[j] = dot(n, &SX[j * n], Yd.data());
+  for (int i = 0; i < p; ++i)
+    for (int j = 0; j < p; ++j) al[i] += cv[i + j * p] * sxy[j];
+  for (int64_t i = 0; i < n; ++i) {
+    double sxa = 0.0;
+    for (int j = 0; j < p; ++j) sxa += SX[i + j * n] * al[j];
+    eta[i] = (float)(Yd[i] - (double)tau[0] * (SY[i] - sxa) / (double)w[i]);
+    Sigma_iY[i] = (float)SY[i];
+  }
+  for (int64_t i = 0; i < n * p; ++i) Sigma_iX[i] = (float)SX[i];
+  for (int64_t i = 0; i < p * p; ++i) cov[i] = (float)cv[i];
+  for (int64_t i = 0; i < p; ++i) alpha[i] = (float)al[i];
+  return SG_OK;
+}
+
+static int trace_common(sg_ctx* c, const float* Sigma_iX, int64_t p, const float* w, const float* tau,
+                        const float* cov, int nrun, int maxiter, float tol, float cutoff, uint64_t seed,
+                        bool quant, float* trace, int32_t* nrun_used) {
+  NEED_GRM(c);
+  if (nrun < 2) return set_err(c, SG_ERR_INVALID, "nrun must be >= 2");
+  SG_TRY(dropin_setup(c, w, tau, 2 * nrun + 4));
+  std::vector<double> SX, cv;
+  f2d(Sigma_iX, c->nn * p, SX);
+  f2d(cov, p * p, cv);
+  TraceOut t;
+  SG_TRY(trace_probes(c, SX, (int)p, cv, nrun, maxiter, tol, cutoff, seed, quant, {}, &t));
+  if (quant) {
+    trace[0] = (float)t.tr0;
+    trace[1] = (float)t.tr1;
+  } else {
+    trace[0] = (float)t.tr1;
+  }
+  if (nrun_used) *nrun_used = t.nrun;
+  return SG_OK;
+}
+
+extern "C" int sg_GetTrace(sg_ctx* c, const float* Sigma_iX, const float* X, int64_t p, const float* w,
+                           const float* tau, const float* cov, int nrun, int maxiter, float tol,
+                           float cutoff, uint64_t seed, float* trace, int32_t* nrun_used) {
+  (void)X;
+  return trace_common(c, Sigma_iX, p, w, tau, cov, nrun, maxiter, tol, cutoff, seed, false, trace, nrun_used);
+}
+extern "C" int sg_GetTrace_q(sg_ctx* c, const float* Sigma_iX, const float* X, int64_t p, const float* w,
+                             const float* tau, const float* cov, int nrun, int maxiter, float tol,
+                             float cutoff, uint64_t seed, float* trace, int32_t* nrun_used) {
+  (void)X;
+  return trace_common(c, Sigma_iX, p, w, tau, cov, nrun, maxiter, tol, cutoff, seed, true, trace, nrun_used);
+}
+
+namespace {
+struct AIOut {
+  double YPAPY = 0, YPA0PY = 0, tr0 = 0, tr1 = 0;
+  double AI[4] = {0, 0, 0, 0};
+  std::vector<double> PY;
+};
+
+// getAIScore / getAIScore_q: K PY rides with the first probe block; the
+// P A PY (and P A0 PY) solves are submitted as soon as K PY is known.
+int ai_score(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* w, const float* tau,
+             const float* Sigma_iY, const float* Sigma_iX, const float* cov_in, int nrun, int maxiter,
+             float tol, float cutoff, uint64_t seed, bool quant, AIOut* o) {
+  NEED_GRM(c);
+  const int64_t n = c->nn;
+  SG_TRY(dropin_setup(c, w, tau, 2 * nrun + 8));
+  std::vector<double> Yd, Xd, SY, SX, cv;
+  f2d(Y, n, Yd);
+  f2d(X, n * p, Xd);
+  f2d(Sigma_iY, n, SY);
+  f2d(Sigma_iX, n * p, SX);
+  if (quant) {
+    std::vector<double> XtSX(p * p);
+    for (int a = 0; a < p; ++a)
+      for (int b = 0; b < p; ++b) XtSX[a + b * p] = dot(n, &Xd[a * n], &SX[b * n]);
+    cv = inv_sympd(XtSX, (int)p);
+  } else {
+    f2d(cov_in, p * p, cv);
+  }
+  o->PY.resize(n);
+  p_apply(n, (int)p, SY.data(), SX.data(), cv.data(), Yd.data(), o->PY.data());
+  int64_t apy_id;
+  SG_TRY(sg_engine_submit(c, 0, 1, o->PY.data(), 1, 1, 0.0, &apy_id));
+  // first probe block + K PY in the same steps
+  const int k = nrun;
+  std::vector<int64_t> pid(k), aid(k);
+  SG_TRY(sg_engine_submit_probes(c, 0, 0, seed, 0, k, maxiter, tol, pid.data()));
+  SG_TRY(sg_engine_submit_probes(c, 0, 1, seed, 0, k, maxiter, tol, aid.data()));
+  SG_TRY(run_until(c, {apy_id}));
+  std::vector<double> APY(n);
+  SG_TRY(fetch(c, apy_id, APY.data(), nullptr));
+  o->YPAPY = dot(n, o->PY.data(), APY.data());
+  o->YPA0PY = dot(n, o->PY.data(), o->PY.data());
+  std::vector<double> rhs(APY);
+  int nsolve = 1;
+  if (quant) {
+    rhs.insert(rhs.end(), o->PY.begin(), o->PY.end());  // A0 PY = PY
+    nsolve = 2;
+  }
+  std::vector<int64_t> sid(nsolve);
+  SG_TRY(sg_engine_submit(c, 0, 0, rhs.data(), nsolve, maxiter, tol, sid.data()));
+  // finish the first probe block (and the solves), then continue GetTrace's CV loop
+  std::vector<int64_t> all(pid);
+  all.insert(all.end(), aid.begin(), aid.end());
+  all.insert(all.end(), sid.begin(), sid.end());
+  SG_TRY(run_until(c, all));
+  std::vector<double> t1, t0, u(n), su(n), au(n), pu(n);
+  for (int j = 0; j < k; ++j) {
+    for (int64_t i = 0; i < n; ++i) u[i] = (hash3(seed, (uint64_t)j, (uint64_t)i) >> 63) ? 1.0 : -1.0;
+    SG_TRY(fetch(c, pid[j], su.data(), nullptr));
+    SG_TRY(fetch(c, aid[j], au.data(), nullptr));
+    p_apply(n, (int)p, su.data(), SX.data(), cv.data(), u.data(), pu.data());
+    t1.push_back(dot(n, au.data(), pu.data()));
+    t0.push_back(dot(n, u.data(), pu.data()));
+  }
+  int start = k, end = k;
+  while (cal_cv(t1) > cutoff || (quant && cal_cv(t0) > cutoff)) {
+    start = end;
+    end = start + 10;
+    std::vector<int64_t> p2(10), a2(10);
+    SG_TRY(sg_engine_submit_probes(c, 0, 0, seed, start, 10, maxiter, tol, p2.data()));
+    SG_TRY(sg_engine_submit_probes(c, 0, 1, seed, start, 10, maxiter, tol, a2.data()));
+    std::vector<int64_t> al(p2);
+    al.insert(al.end(), a2.begin(), a2.end());
+    SG_TRY(run_until(c, al));
+    for (int j = 0; j < 10; ++j) {
+      for (int64_t i = 0; i < n; ++i) u[i] = (hash3(seed, (uint64_t)(start + j), (uint64_t)i) >> 63) ? 1.0 : -1.0;
+      SG_TRY(fetch(c, p2[j], su.data(), nullptr));
+      SG_TRY(fetch(c, a2[j], au.data(), nullptr));
+      p_apply(n, (int)p, su.data(), SX.data(), cv.data(), u.data(), pu.data());
+      t1.push_back(dot(n, au.data(), pu.data()));
+      t0.push_back(dot(n, u.data(), pu.data()));
+    }
+  }
+  double s1 = 0, s0 = 0;
+  for (double v : t1) s1 += v;
+  for (double v : t0) s0 += v;
+  o->tr1 = s1 / t1.size();
+  o->tr0 = s0 / t0.size();
+  std::vector<double> S(n), PAPY(n);
+  SG_TRY(fetch(c, sid[0], S.data(), nullptr));
+  p_apply(n, (int)p, S.data(), SX.data(), cv.data(), APY.data(), PAPY.data());
+  o->AI[3] = dot(n, APY.data(), PAPY.data());
+  if (quant) {
+    std::vector<double> PA0PY(n);
+    SG_TRY(fetch(c, sid[1], S.data(), nullptr));
+    p_apply(n, (int)p, S.data(), SX.data(), cv.data(), o->PY.data(), PA0PY.data());
+    o->AI[0] = dot(n, o->PY.data(), PA0PY.data());
+    o->AI[1] = o->AI[2] = dot(n, o->PY.data(), PAPY.data());
+  }
+  return SG_OK;
+}
+}  // namespace
+
+extern "C" int sg_getAIScore(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* w,
+                             const float* tau, const float* Sigma_iY, const float* Sigma_iX,
+                             const float* cov, int nrun, int maxiter, float tol, float cutoff,
+                             uint64_t seed, float* YPAPY, float* Trace, float* AI, float* PY) {
+  AIOut o;
+  SG_TRY(ai_score(c, Y, X, p, w, tau, Sigma_iY, Sigma_iX, cov, nrun, maxiter, tol, cutoff, seed, false, &o));
+  *YPAPY = (float)o.YPAPY;
+  *Trace = (float)o.tr1;
+  *AI = (float)o.AI[3];
+  if (PY)
+    for (int64_t i = 0; i < c->nn; ++i) PY[i] = (float)o.PY[i];
+  return SG_OK;
+}
+
+extern "C" int sg_getAIScore_q(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* w,
+                               const float* tau, const float* Sigma_iY, const float* Sigma_iX,
+                               const float* cov, int nrun, int maxiter, float tol, float cutoff,
+                               uint64_t seed, float* YPAPY, float* YPA0PY, float* Trace, float* AI,
+                               float* PY) {
+  AIOut o;
+  SG_TRY(ai_score(c, Y, X, p, w, tau, Sigma_iY, Sigma_iX, cov, nrun, maxiter, tol, cutoff, seed, true, &o));
+  *YPAPY = (float)o.YPAPY;
+  *YPA0PY = (float)o.YPA0PY;
+  Trace[0] = (float)o.tr0;
+  Trace[1] = (float)o.tr1;
+  for (int i = 0; i < 4; ++i) AI[i] = (float)o.AI[i];
+  if (PY)
+    for (int64_t i = 0; i < c->nn; ++i) PY[i] = (float)o.PY[i];
+  return SG_OK;
+}
+
+extern "C" int sg_fitglmmaiRPCG(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* w,
+                                float* tau, const float* Sigma_iY, const float* Sigma_iX, const float* cov,
+                                int nrun, int maxiter, float tol_pcg, float tol, float cutoff,
+                                uint64_t seed) {
+  AIOut o;
+  SG_TRY(ai_score(c, Y, X, p, w, tau, Sigma_iY, Sigma_iX, cov, nrun, maxiter, tol_pcg, cutoff, seed, false, &o));
+  // FIT.cpp:3313-3337
+  const double dtau = (o.YPAPY - o.tr1) / o.AI[3];
+  const double t0[2] = {tau[0], tau[1]};
+  double t[2] = {t0[0], t0[1] + dtau};
+  for (double& v : t) if (v < tol) v = 0.0;
+  double step = 1.0;
+  while (t[1] < 0.0) {
+    step *= 0.5;
+    t[1] = t0[1] + step * dtau;
+  }
+  for (double& v : t) if (v < tol) v = 0.0;
+  tau[0] = (float)t[0];
+  tau[1] = (float)t[1];
+  return SG_OK;
+}
+
+extern "C" int sg_fitglmmaiRPCG_q(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* w,
+                                  float* tau, const float* Sigma_iY, const float* Sigma_iX,
+                                  const float* cov, int nrun, int maxiter, float tol_pcg, float tol,
+                                  float cutoff, uint64_t seed) {
+  AIOut o;
+  SG_TRY(ai_score(c, Y, X, p, w, tau, Sigma_iY, Sigma_iX, cov, nrun, maxiter, tol_pcg, cutoff, seed, true, &o));
+  // FIT.cpp:3615-3660: Dtau = solve(AI, score), GMMAT zeroing, step-halving
+  const double s0 = o.YPA0PY - o.tr0, s1 = o.YPAPY - o.tr1;
+  const double det = o.AI[0] * o.AI[3] - o.AI[1] * o.AI[2];
+  if (det == 0.0 || !std::isfinite(det)) return set_err(c, SG_ERR_NUMERIC, "singular AI matrix");
+  const double d0 = (o.AI[3] * s0 - o.AI[2] * s1) / det;
+  const double d1 = (o.AI[0] * s1 - o.AI[1] * s0) / det;
+  const double t0[2] = {tau[0], tau[1]};
+  const bool zero[2] = {t0[0] < tol, t0[1] < tol};
+  double t[2] = {t0[0] + d0, t0[1] + d1};
+  for (int i = 0; i < 2; ++i) if (zero[i] && t[i] < tol) t[i] = 0.0;
+  double step = 1.0;
+  while (t[0] < 0.0 || t[1] < 0.0) {
+    step *= 0.5;
+    t[0] = t0[0] + step * d0;
+    t[1] = t0[1] + step * d1;
+    for (int i = 0; i < 2; ++i) if (zero[i] && t[i] < tol) t[i] = 0.0;
+  }
+  for (double& v : t) if (v < tol) v = 0.0;
+  tau[0] = (float)t[0];
+  tau[1] = (float)t[1];
+  return SG_OK;
+}
+
+// ------------------------------------------------------------------ synthetic cohorts
+extern "C" int sg_synth_bed(sg_ctx* c, uint64_t seed, int64_t n, int64_t m, double miss_rate,
+                            uint8_t** bed_dev, uint64_t* bed_len) {
+  if (!c || n <= 0 || m <= 0 || miss_rate < 0 || miss_rate >= 1) return SG_ERR_INVALID;
+  dev_free_t(c, c->d_synth);
+  const uint64_t len = 3 + (uint64_t)((n + 3) / 4) * (uint64_t)m;
+  SG_TRY(dev_alloc_t(c, &c->d_synth, (size_t)len));
+  const uint8_t magic[3] = {0x6C, 0x1B, 0x01};
+  SG_CUDA(c, cudaMemcpyAsync(c->d_synth, magic, 3, cudaMemcpyHostToDevice, c->stream));
+  const uint32_t thr = (uint32_t)std::llround(miss_rate * 65536.0);
+  launch_synth_bed(seed, n, m, thr, c->d_synth, c->stream);
+  SG_LAUNCHED(c, 1);
+  SG_TRY(sync(c));
+  c->synth_len = len;
+  if (bed_dev) *bed_dev = c->d_synth;
+  if (bed_len) *bed_len = len;
+  return SG_OK;
+}
+
+extern "C" int sg_synth_bed_to_host(sg_ctx* c, uint8_t* host, uint64_t len) {
+  if (!c || !c->d_synth) return SG_ERR_STATE;
+  if (len > c->synth_len) return set_err(c, SG_ERR_INVALID, "length beyond the synthetic image");
+  SG_CUDA(c, cudaMemcpy(host, c->d_synth, len, cudaMemcpyDeviceToHost));
+  return SG_OK;
+}
+
+extern "C" int sg_synth_genetic_value(sg_ctx* c, uint64_t seed, double* out) {
+  NEED_GENO(c);
+  double* d = nullptr;
+  SG_TRY(dev_alloc_t(c, &d, (size_t)c->nn));
+  launch_genetic_value(c->d_packed, c->pitch, c->d_lut, c->m_qc, c->nn, seed, d, c->stream);
+  SG_LAUNCHED(c, 2);
+  SG_CUDA(c, cudaMemcpyAsync(out, d, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
+  SG_TRY(sync(c));
+  dev_free(c, d);
+  return SG_OK;
+}

@@ -1,0 +1,373 @@
+// Genotype kernels: PLINK .bed decode + per-marker QC, re-pack, standardisation,
+// GRM diagonal, and the synthetic-cohort generator.
+//
+// The integer work (allele / missing counts, re-pack) is bit-exact with the
+// reference genoClass (src/SAIGE/src/SAIGE_fitGLMM_fast.cpp, FIT.cpp below);
+// the float work (frequencies, 1/sd, LUT, FP32 diagonal) uses explicitly
+// rounded IEEE intrinsics so it is bit-exact with the reference's float code.
+// These are HBM-bound byte kernels: 16-byte aligned row pitches, 32-bit word
+// loads and popcounts; no tensor cores.
+#include "sg_internal.h"
+#include <cuda_bf16.h>
+#include <math.h>
+
+namespace sg {
+
+// ----------------------------------------------------------------------------
+// Per-marker counts and QC: one warp per marker.
+// 2-bit field f of sample s: b = bit0, a = bit1; 00 -> 2, 01 -> missing,
+// 10 -> 1, 11 -> 0 (FIT.cpp:346-357).  With lo = b bits and hi = a bits of a
+// 32-bit word (16 samples): missing = lo & ~hi; a non-missing sample adds
+// 2 - (a + b) alleles.  ``maskbits`` has bit 2s set for samples with a
+// phenotype (indicatorGenoSamplesWithPheno, FIT.cpp:376-385).
+// ----------------------------------------------------------------------------
+__global__ void marker_qc_kernel(const uint8_t* __restrict__ raw, int64_t pitch, int64_t m,
+                                 int64_t n_fam, const uint32_t* __restrict__ maskbits, int64_t nn,
+                                 float min_maf, float max_miss, const uint8_t* __restrict__ vr_flag,
+                                 float min_mac_vr, int is_var_ratio, MarkerQC* __restrict__ out) {
+  const int64_t marker = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (marker >= m) return;
+  const uint32_t* row = reinterpret_cast<const uint32_t*>(raw + marker * pitch);
+  const int64_t nwords = (n_fam + 15) / 16;
+  int nnon = 0, nmiss = 0, sum_ab = 0;
+  for (int64_t w = lane; w < nwords; w += 32) {
+    const uint32_t x = __ldg(row + w);
+    const uint32_t mk = __ldg(maskbits + w);
+    const uint32_t lo = x & 0x55555555u, hi = (x >> 1) & 0x55555555u;
+    const uint32_t miss = lo & ~hi;
+    const uint32_t non = ~miss & mk;
+    nmiss += __popc(miss & mk);
+    nnon += __popc(non);
+    sum_ab += __popc(hi & non) + __popc(lo & non);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nnon += __shfl_xor_sync(0xffffffffu, nnon, o);
+    nmiss += __shfl_xor_sync(0xffffffffu, nmiss, o);
+    sum_ab += __shfl_xor_sync(0xffffffffu, sum_ab, o);
+  }
+  if (lane != 0) return;
+  int allele = 2 * nnon - sum_ab;
+  // FIT.cpp:436-447: first frequency over non-missing calls, integer fill
+  const float alt0 = __fdiv_rn((float)allele, (float)((nn - nmiss) * 2));
+  const float miss_rate = __fdiv_rn((float)nmiss, (float)nn);
+  int fill = 0;
+  if (isfinite(alt0)) fill = (int)floor((double)__fmul_rn(2.0f, alt0) + 0.5);
+  if (nmiss > 0) allele = allele + fill * nmiss;  // FIT.cpp:449-454
+  const float alt = __fdiv_rn((float)allele, (float)(nn * 2));  // FIT.cpp:484
+  const float maf = fminf(alt, __fsub_rn(1.0f, alt));
+  const int mac = min(allele, (int)(nn * 2) - allele);
+  int pass_qc = (maf >= min_maf && miss_rate <= max_miss) ? 1 : 0;  // FIT.cpp:493-495
+  int pass_vr = 0;
+  if (is_var_ratio && (float)mac >= min_mac_vr && vr_flag[marker]) pass_vr = 1;  // FIT.cpp:521-543
+  if (pass_vr) pass_qc = 0;                                                      // FIT.cpp:545-547
+  // FIT.cpp:916-921: Std = sqrt(2p(1-p)), invStd = 1/Std (0 if Std == 0), in float
+  const float sd = __fsqrt_rn(__fmul_rn(__fmul_rn(2.0f, alt), __fsub_rn(1.0f, alt)));
+  const float inv = (sd == 0.0f) ? 0.0f : __fdiv_rn(1.0f, sd);
+  MarkerQC q;
+  q.allele = allele;
+  q.mac = mac;
+  q.nmiss = nmiss;
+  q.freq = alt;
+  q.invstd = inv;
+  q.fill = fill;
+  q.pass_qc = pass_qc;
+  q.pass_vr = pass_vr;
+  out[marker] = q;
+}
+
+void launch_marker_qc(const uint8_t* raw, int64_t raw_pitch, int64_t m, int64_t n_fam,
+                      const uint32_t* maskbits, int64_t nn, float min_maf, float max_miss,
+                      const uint8_t* vr_flag, float min_mac_vr, int is_var_ratio, MarkerQC* out,
+                      cudaStream_t s) {
+  const int warps = 8;
+  const int64_t blocks = (m + warps - 1) / warps;
+  if (blocks == 0) return;
+  marker_qc_kernel<<<(unsigned)blocks, warps * 32, 0, s>>>(raw, raw_pitch, m, n_fam, maskbits, nn,
+                                                          min_maf, max_miss, vr_flag, min_mac_vr,
+                                                          is_var_ratio, out);
+}
+
+// ----------------------------------------------------------------------------
+// Re-pack (FIT.cpp:551-575): for output marker j (source marker src_marker[j]),
+// sample k takes the source field of sample sub0[k]; a missing field (01)
+// becomes the code of the fill genotype.  The reference's re-pack codes
+// (HOM_ALT=11, HET=10, HOM_REF=00) equal the source fields for non-missing
+// calls, so only missing fields change.  Fields past nn and the row padding
+// are zero.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pack_code_of(int g) { return g == 0 ? 3u : (g == 1 ? 2u : 0u); }
+
+__global__ void repack_gather_kernel(const uint8_t* __restrict__ raw, int64_t raw_pitch,
+                                     const int32_t* __restrict__ src_marker,
+                                     const MarkerQC* __restrict__ qc, const int32_t* __restrict__ sub0,
+                                     int64_t nn, uint8_t* __restrict__ out, int64_t out_pitch) {
+  const int64_t j = blockIdx.y;
+  const int64_t byte = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (byte >= out_pitch) return;
+  const int64_t src = src_marker[j];
+  const uint8_t* row = raw + src * raw_pitch;
+  const uint32_t fcode = pack_code_of(qc[src].fill);
+  uint32_t v = 0;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int64_t k = byte * 4 + t;
+    if (k < nn) {
+      const int64_t si = sub0[k];
+      uint32_t f = (row[si >> 2] >> (2 * (si & 3))) & 3u;
+      if (f == 1u) f = fcode;
+      v |= f << (2 * t);
+    }
+  }
+  out[j * out_pitch + byte] = (uint8_t)v;
+}
+
+// Identity sample order (nn == n_fam, sub0[k] == k): 32-bit word at a time.
+__global__ void repack_identity_kernel(const uint8_t* __restrict__ raw, int64_t raw_pitch,
+                                       const int32_t* __restrict__ src_marker,
+                                       const MarkerQC* __restrict__ qc, int64_t nn,
+                                       uint8_t* __restrict__ out, int64_t out_pitch) {
+  const int64_t j = blockIdx.y;
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nwords = out_pitch / 4;
+  if (w >= nwords) return;
+  const int64_t src = src_marker[j];
+  const uint32_t* row = reinterpret_cast<const uint32_t*>(raw + src * raw_pitch);
+  const uint32_t fcode = pack_code_of(qc[src].fill);
+  uint32_t x = row[w];
+  // valid-sample mask of this word (bits of both halves of each field)
+  const int64_t s0 = w * 16;
+  uint32_t valid;
+  if (s0 + 16 <= nn) valid = 0xffffffffu;
+  else if (s0 >= nn) valid = 0u;
+  else valid = (1u << (2 * (nn - s0))) - 1u;
+  const uint32_t lo = x & 0x55555555u, hi = (x >> 1) & 0x55555555u;
+  const uint32_t miss = lo & ~hi;
+  x = (x & ~(miss * 3u)) | (miss * fcode);
+  reinterpret_cast<uint32_t*>(out + j * out_pitch)[w] = x & valid;
+}
+
+void launch_repack(const uint8_t* raw, int64_t raw_pitch, const int32_t* src_marker,
+                   const MarkerQC* qc, int64_t m_out, const int32_t* sub0, int64_t nn, int identity,
+                   uint8_t* out, int64_t out_pitch, cudaStream_t s) {
+  if (m_out == 0) return;
+  const int threads = 256;
+  for (int64_t j0 = 0; j0 < m_out; j0 += 65535) {
+    const int64_t mj = (m_out - j0) < 65535 ? (m_out - j0) : 65535;
+    if (identity) {
+      dim3 grid((unsigned)((out_pitch / 4 + threads - 1) / threads), (unsigned)mj);
+      repack_identity_kernel<<<grid, threads, 0, s>>>(raw, raw_pitch, src_marker + j0, qc, nn,
+                                                      out + j0 * out_pitch, out_pitch);
+    } else {
+      dim3 grid((unsigned)((out_pitch + threads - 1) / threads), (unsigned)mj);
+      repack_gather_kernel<<<grid, threads, 0, s>>>(raw, raw_pitch, src_marker + j0, qc, sub0, nn,
+                                                    out + j0 * out_pitch, out_pitch);
+    }
+  }
+}
+
+// LUT (g - 2p) * invStd for g = 0,1,2 (setStdGenoLookUpArr FIT.cpp:152-159), in float.
+__global__ void lut_kernel(const MarkerQC* __restrict__ qc, const int32_t* __restrict__ src_marker,
+                           int64_t m_out, float* __restrict__ lut4) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m_out) return;
+  const MarkerQC q = qc[src_marker[j]];
+  const float p2 = __fmul_rn(2.0f, q.freq);
+  lut4[4 * j + 0] = __fmul_rn(__fsub_rn(0.0f, p2), q.invstd);
+  lut4[4 * j + 1] = __fmul_rn(__fsub_rn(1.0f, p2), q.invstd);
+  lut4[4 * j + 2] = __fmul_rn(__fsub_rn(2.0f, p2), q.invstd);
+  lut4[4 * j + 3] = 0.0f;
+}
+
+void launch_lut(const MarkerQC* qc, const int32_t* src_marker, int64_t m_out, float* lut4,
+                cudaStream_t s) {
+  if (m_out == 0) return;
+  lut_kernel<<<(unsigned)((m_out + 255) / 256), 256, 0, s>>>(qc, src_marker, m_out, lut4);
+}
+
+// genotype 0/1/2 of a re-packed field (Get_OneSNP_StdGeno FIT.cpp:620-628: 2 - (a + b))
+__device__ __forceinline__ int field_geno(uint32_t f) { return 2 - (int)((f & 1u) + (f >> 1)); }
+
+// ----------------------------------------------------------------------------
+// Standardised genotypes Z (np x mp): row = sample, markers contiguous, zero
+// padded.  Block = 64 markers x 128 samples staged through shared memory so
+// the transposing writes are coalesced along markers.
+// ----------------------------------------------------------------------------
+template <typename Out>
+__global__ void zbuild_kernel(const uint8_t* __restrict__ packed, int64_t pitch,
+                              const float* __restrict__ lut4, int64_t m_qc, int64_t nn,
+                              int64_t mp, Out* __restrict__ Zhi, Out* __restrict__ Zlo) {
+  __shared__ uint32_t sbytes[64][9];  // 64 markers x 32 bytes (+pad)
+  __shared__ float slut[64][4];
+  const int64_t m0 = (int64_t)blockIdx.x * 64;
+  const int64_t s0 = (int64_t)blockIdx.y * 128;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < 64 * 8; e += blockDim.x) {
+    const int mm = e >> 3, wd = e & 7;
+    const int64_t mk = m0 + mm;
+    const int64_t boff = s0 / 4 + (int64_t)wd * 4;
+    uint32_t v = 0;
+    if (mk < m_qc && boff < pitch) v = *reinterpret_cast<const uint32_t*>(packed + mk * pitch + boff);
+    sbytes[mm][wd] = v;
+  }
+  for (int e = tid; e < 64 * 4; e += blockDim.x) {
+    const int mm = e >> 2;
+    const int64_t mk = m0 + mm;
+    slut[mm][e & 3] = (mk < m_qc) ? lut4[mk * 4 + (e & 3)] : 0.0f;
+  }
+  __syncthreads();
+  const int mm = tid & 63;
+  const int64_t mk = m0 + mm;
+  for (int s = tid >> 6; s < 128; s += (blockDim.x >> 6)) {
+    const int64_t smp = s0 + s;
+    float z = 0.0f;
+    if (mk < m_qc && smp < nn) {
+      const uint32_t f = (sbytes[mm][s >> 4] >> (2 * (s & 15))) & 3u;
+      z = slut[mm][field_geno(f)];
+    }
+    if constexpr (sizeof(Out) == 4) {
+      Zhi[smp * mp + mk] = z;
+    } else {
+      const __nv_bfloat16 h = __float2bfloat16_rn(z);
+      Zhi[smp * mp + mk] = h;
+      if (Zlo) Zlo[smp * mp + mk] = __float2bfloat16_rn(z - __bfloat162float(h));
+    }
+  }
+}
+
+void launch_zbuild_f32(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
+                       int64_t nn, int64_t np, int64_t mp, float* Z, cudaStream_t s) {
+  dim3 grid((unsigned)(mp / 64), (unsigned)(np / 128));
+  zbuild_kernel<float><<<grid, 256, 0, s>>>(packed, pitch, lut4, m_qc, nn, mp, Z, nullptr);
+}
+void launch_zbuild_bf16(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
+                        int64_t nn, int64_t np, int64_t mp, void* Zhi, void* Zlo, cudaStream_t s) {
+  dim3 grid((unsigned)(mp / 64), (unsigned)(np / 128));
+  zbuild_kernel<__nv_bfloat16><<<grid, 256, 0, s>>>(packed, pitch, lut4, m_qc, nn, mp,
+                                                   (__nv_bfloat16*)Zhi, (__nv_bfloat16*)Zlo);
+}
+
+// ----------------------------------------------------------------------------
+// GRM diagonal sum_m z^2 (Get_Diagof_StdGeno FIT.cpp:665-704): one thread per
+// sample, markers in order; FP32 accumulation rounded exactly as the
+// reference's ``m_DiagStd + z % z`` and an FP64 accumulation beside it.
+// ----------------------------------------------------------------------------
+__global__ void diag_kernel(const uint8_t* __restrict__ packed, int64_t pitch,
+                            const float* __restrict__ lut4, int64_t m_qc, int64_t nn,
+                            double* __restrict__ d64, float* __restrict__ d32) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const int64_t byte = i >> 2;
+  const int sh = 2 * (int)(i & 3);
+  float a32 = 0.0f;
+  double a64 = 0.0;
+  for (int64_t m = 0; m < m_qc; ++m) {
+    const uint32_t f = (packed[m * pitch + byte] >> sh) & 3u;
+    const float z = __ldg(lut4 + 4 * m + field_geno(f));
+    a32 = __fadd_rn(a32, __fmul_rn(z, z));
+    a64 = __dadd_rn(a64, __dmul_rn((double)z, (double)z));
+  }
+  d64[i] = a64;
+  d32[i] = a32;
+}
+
+void launch_diag(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc, int64_t nn,
+                 double* diag64, float* diag32, cudaStream_t s) {
+  if (nn == 0) return;
+  diag_kernel<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(packed, pitch, lut4, m_qc, nn, diag64,
+                                                            diag32);
+}
+
+// One marker unpacked to genotypes and standardised values (Get_OneSNP_Geno / _StdGeno).
+__global__ void unpack_marker_kernel(const uint8_t* __restrict__ row, int64_t nn,
+                                     const float* __restrict__ lut4, int32_t* g, float* z) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const uint32_t f = (row[i >> 2] >> (2 * (i & 3))) & 3u;
+  const int gg = field_geno(f);
+  if (g) g[i] = gg;
+  if (z) z[i] = lut4 ? lut4[gg] : 0.0f;
+}
+
+void launch_unpack_marker(const uint8_t* packed_row, int64_t nn, const float* lut4, int32_t* g,
+                          float* z, cudaStream_t s) {
+  if (nn == 0) return;
+  unpack_marker_kernel<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(packed_row, nn, lut4, g, z);
+}
+
+// ----------------------------------------------------------------------------
+// Synthetic cohort (integer recipe, reproduced on the CPU by saigegpu/synth.py):
+//   hm  = hash3(seed, 1, m);  thr_m = 167772 + (((hm >> 40) * 8220835) >> 24)   (p_m in [0.01,0.5))
+//   h   = hash3(seed, 16 + m, i); allele1 = (h >> 40) < thr_m; allele2 = ((h >> 16) & 0xFFFFFF) < thr_m
+//   missing when (h & 0xFFFF) < miss_thr16; genotype g = allele1 + allele2 copies of the counted allele
+//   field: missing 01, g=2 -> 00, g=1 -> 10, g=0 -> 11.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t synth_field(uint64_t seed, int64_t m, int64_t i, uint32_t thr,
+                                                uint32_t miss_thr16) {
+  const uint64_t h = hash3(seed, 16ull + (uint64_t)m, (uint64_t)i);
+  if ((uint32_t)(h & 0xFFFFu) < miss_thr16) return 1u;
+  const int g = (int)((uint32_t)(h >> 40) < thr) + (int)((uint32_t)((h >> 16) & 0xFFFFFFu) < thr);
+  return g == 2 ? 0u : (g == 1 ? 2u : 3u);
+}
+
+__global__ void synth_bed_kernel(uint64_t seed, int64_t n, int64_t m, uint32_t miss_thr16,
+                                 uint8_t* __restrict__ body, int64_t nb) {
+  const int64_t marker = blockIdx.y + (int64_t)blockIdx.z * 65535;
+  const int64_t byte = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (marker >= m || byte >= nb) return;
+  const uint64_t hm = hash3(seed, 1ull, (uint64_t)marker);
+  const uint32_t thr = 167772u + (uint32_t)(((hm >> 40) * 8220835ull) >> 24);
+  uint32_t v = 0;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int64_t i = byte * 4 + t;
+    if (i < n) v |= synth_field(seed, marker, i, thr, miss_thr16) << (2 * t);
+  }
+  body[marker * nb + byte] = (uint8_t)v;
+}
+
+void launch_synth_bed(uint64_t seed, int64_t n, int64_t m, uint32_t miss_thr16, uint8_t* out,
+                      cudaStream_t s) {
+  const int64_t nb = (n + 3) / 4;
+  const int threads = 256;
+  const int64_t gz = (m + 65534) / 65535;
+  dim3 grid((unsigned)((nb + threads - 1) / threads), (unsigned)(m < 65535 ? m : 65535), (unsigned)gz);
+  synth_bed_kernel<<<grid, threads, 0, s>>>(seed, n, m, miss_thr16, out + 3, nb);
+}
+
+// Per-marker effect b_m ~ N(0,1) (Box-Muller on two 53-bit hash uniforms).
+__global__ void effect_kernel(uint64_t seed, int64_t m, float* b) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const double u1 = ((double)(hash3(seed, 2ull, (uint64_t)j) >> 11) + 0.5) * 0x1.0p-53;
+  const double u2 = (double)(hash3(seed, 3ull, (uint64_t)j) >> 11) * 0x1.0p-53;
+  b[j] = (float)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+}
+
+__global__ void genetic_value_kernel(const uint8_t* __restrict__ packed, int64_t pitch,
+                                     const float* __restrict__ lut4, int64_t m_qc, int64_t nn,
+                                     const float* __restrict__ b, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const int64_t byte = i >> 2;
+  const int sh = 2 * (int)(i & 3);
+  double acc = 0.0;
+  for (int64_t m = 0; m < m_qc; ++m) {
+    const uint32_t f = (packed[m * pitch + byte] >> sh) & 3u;
+    acc += (double)__ldg(lut4 + 4 * m + field_geno(f)) * (double)__ldg(b + m);
+  }
+  out[i] = acc / sqrt((double)m_qc);
+}
+
+void launch_genetic_value(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
+                          int64_t nn, uint64_t seed, double* out, cudaStream_t s) {
+  float* b = nullptr;
+  if (cudaMallocAsync(&b, sizeof(float) * (m_qc > 0 ? m_qc : 1), s) != cudaSuccess) return;
+  effect_kernel<<<(unsigned)((m_qc + 255) / 256), 256, 0, s>>>(seed, m_qc, b);
+  genetic_value_kernel<<<(unsigned)((nn + 127) / 128), 128, 0, s>>>(packed, pitch, lut4, m_qc, nn,
+                                                                    b, out);
+  cudaFreeAsync(b, s);
+}
+
+}  // namespace sg

@@ -1,0 +1,340 @@
+// Multi-RHS Jacobi-PCG engine kernels (FP64 vectors and recurrences).
+//
+// Each column c runs the loop of getPCG1ofSigmaAndVector
+// (src/SAIGE/src/SAIGE_fitGLMM_fast.cpp:2593-2809) on its own:
+//     x = 0, r = b, z = M^-1 r, p = z
+//     while (r'r > tol && iter < maxiter):
+//         Ap = tau0 p / W + tau1 K p                      (getCrossprod :2397-2425)
+//         a = r'z / p'Ap;  x += a p;  r1 = r - a Ap;  z1 = M^-1 r1
+//         b = z1'r1 / z'r; p = z1 + b p;  iter++
+// The GRM product K p of all in-flight columns is one GEMM per engine step;
+// the kernels below are the FP64 vector work around it, split at the two
+// reductions.  Reductions are two-level and in a fixed order (block partials,
+// then a sequential sum per column), so a column's arithmetic does not depend
+// on how many other columns share the step.
+//
+// Vectors are RHS-major: column c occupies [c*np, (c+1)*np).  A phenotype
+// slot g contributes winv = 1/W and minv = 1/diag(Sigma) rows, both 0 outside
+// the phenotype's sample subset (which keeps the subset's columns exact).
+#include "sg_internal.h"
+
+namespace sg {
+
+constexpr int kThreads = 256;
+constexpr int kChunk = 2048;  // vector elements per block
+
+int64_t pcg_nblk(int64_t np) { return (np + kChunk - 1) / kChunk; }
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+  }
+  __syncthreads();
+  return s;
+}
+
+// Admit columns cols[0..n): x = 0, r = mask*b, z = minv r, p = z; partial r'z, r'r.
+// Product columns (kind 1) only stage Pf = mask*b.
+__global__ void pcg_init_kernel(int64_t np, const int32_t* __restrict__ cols,
+                                const ColState* __restrict__ st, const double* __restrict__ minv,
+                                const double* __restrict__ B, double* X, double* R, double* Z,
+                                double* P, float* Pf, double* part, int64_t nblk) {
+  __shared__ double sh[kThreads / 32];
+  const int sel = blockIdx.y;
+  const int64_t c = cols[sel];
+  const ColState s = st[c];
+  const double* mv = minv + (int64_t)s.pheno * np;
+  const double* b = B + (int64_t)sel * np;
+  const int64_t base = c * np;
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  double zr = 0.0, rr = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
+    const double m = mv[i];
+    const double bi = (m != 0.0) ? b[i] : 0.0;
+    if (s.kind == 0) {
+      const double z = m * bi;
+      X[base + i] = 0.0;
+      R[base + i] = bi;
+      Z[base + i] = z;
+      P[base + i] = z;
+      Pf[base + i] = (float)z;
+      zr += z * bi;
+      rr += bi * bi;
+    } else {
+      Pf[base + i] = (float)bi;
+      X[base + i] = 0.0;
+    }
+  }
+  zr = block_sum(zr, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    part[(c * nblk + blockIdx.x) * 2 + 0] = zr;
+    part[(c * nblk + blockIdx.x) * 2 + 1] = rr;
+  }
+}
+
+__global__ void pcg_init_finalize_kernel(const int32_t* __restrict__ cols, int64_t ncols_sel,
+                                         ColState* st, const double* __restrict__ part,
+                                         int64_t nblk) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ncols_sel) return;
+  const int64_t c = cols[k];
+  ColState s = st[c];
+  double zr = 0.0, rr = 0.0;
+  for (int64_t b = 0; b < nblk; ++b) {
+    zr += part[(c * nblk + b) * 2 + 0];
+    rr += part[(c * nblk + b) * 2 + 1];
+  }
+  s.iter = 0;
+  s.just_done = 0;
+  s.alpha = 0.0;
+  s.beta = 0.0;
+  if (s.kind == 0) {
+    s.rz = zr;
+    s.r2 = rr;
+    s.active = (rr > s.tol && s.maxiter > 0) ? 1 : 0;
+    if (!s.active) s.just_done = 1;
+  } else {
+    s.active = 1;
+  }
+  st[c] = s;
+}
+
+void launch_pcg_init(int64_t np, int64_t ncols, const int32_t* cols, int64_t ncols_sel,
+                     ColState* st, const PhenoState* ph, const double* minv, const double* B,
+                     double* X, double* R, double* Z, double* P, float* Pf, double* part,
+                     int64_t nblk, cudaStream_t s) {
+  (void)ncols; (void)ph;
+  if (ncols_sel == 0) return;
+  dim3 grid((unsigned)nblk, (unsigned)ncols_sel);
+  pcg_init_kernel<<<grid, kThreads, 0, s>>>(np, cols, st, minv, B, X, R, Z, P, Pf, part, nblk);
+  pcg_init_finalize_kernel<<<(unsigned)((ncols_sel + 127) / 128), 128, 0, s>>>(cols, ncols_sel, st,
+                                                                               part, nblk);
+}
+
+__device__ __forceinline__ double ap_value(double tau0, double tau1, double winv, double m,
+                                           double p, double y) {
+  return (m != 0.0) ? (tau0 * winv * p + tau1 * y) : 0.0;
+}
+
+// partial p'Ap for active PCG columns
+__global__ void pcg_sigma_dot_kernel(int64_t np, const ColState* __restrict__ st,
+                                     const PhenoState* __restrict__ ph,
+                                     const double* __restrict__ winv, const double* __restrict__ minv,
+                                     const double* __restrict__ P, const float* __restrict__ Yf,
+                                     const double* __restrict__ Yd, double* part, int64_t nblk) {
+  __shared__ double sh[kThreads / 32];
+  const int64_t c = blockIdx.y;
+  const ColState s = st[c];
+  if (s.kind != 0 || !s.active) {
+    if (threadIdx.x == 0) part[(c * nblk + blockIdx.x) * 2] = 0.0;
+    return;
+  }
+  const PhenoState g = ph[s.pheno];
+  const double* wv = winv + (int64_t)s.pheno * np;
+  const double* mv = minv + (int64_t)s.pheno * np;
+  const int64_t base = c * np;
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  double acc = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
+    const double p = P[base + i];
+    const double y = Yf ? (double)Yf[base + i] : Yd[base + i];
+    acc += p * ap_value(g.tau0, g.tau1, wv[i], mv[i], p, y);
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) part[(c * nblk + blockIdx.x) * 2] = acc;
+}
+
+void launch_pcg_sigma_dot(int64_t np, int64_t ncols, ColState* st, const PhenoState* ph,
+                          const double* winv, const double* minv, const double* P,
+                          const float* Yf, const double* Yd, double* part, int64_t nblk,
+                          cudaStream_t s) {
+  if (ncols == 0) return;
+  dim3 grid((unsigned)nblk, (unsigned)ncols);
+  pcg_sigma_dot_kernel<<<grid, kThreads, 0, s>>>(np, st, ph, winv, minv, P, Yf, Yd, part, nblk);
+}
+
+__global__ void pcg_alpha_kernel(int64_t ncols, ColState* st, const double* __restrict__ part,
+                                 int64_t nblk) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  ColState s = st[c];
+  if (s.kind != 0 || !s.active) {
+    s.alpha = 0.0;
+  } else {
+    double pap = 0.0;
+    for (int64_t b = 0; b < nblk; ++b) pap += part[(c * nblk + b) * 2];
+    s.alpha = s.rz / pap;
+  }
+  st[c].alpha = s.alpha;
+}
+
+void launch_pcg_alpha(int64_t ncols, ColState* st, const double* part, int64_t nblk,
+                      cudaStream_t s) {
+  if (ncols == 0) return;
+  pcg_alpha_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(ncols, st, part, nblk);
+}
+
+// x += a p; r -= a Ap; z = minv r; partial z'r, r'r.  Product columns copy K b into X.
+__global__ void pcg_update_kernel(int64_t np, const ColState* __restrict__ st,
+                                  const PhenoState* __restrict__ ph, const double* __restrict__ winv,
+                                  const double* __restrict__ minv, double* X, double* R, double* Z,
+                                  const double* __restrict__ P, const float* __restrict__ Yf,
+                                  const double* __restrict__ Yd, double* part, int64_t nblk) {
+  __shared__ double sh[kThreads / 32];
+  const int64_t c = blockIdx.y;
+  const ColState s = st[c];
+  const int64_t base = c * np;
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  if (!s.active) {
+    if (threadIdx.x == 0) {
+      part[(c * nblk + blockIdx.x) * 2 + 0] = 0.0;
+      part[(c * nblk + blockIdx.x) * 2 + 1] = 0.0;
+    }
+    return;
+  }
+  const double* mv = minv + (int64_t)s.pheno * np;
+  if (s.kind == 1) {
+    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
+      const double y = Yf ? (double)Yf[base + i] : Yd[base + i];
+      X[base + i] = (mv[i] != 0.0) ? y : 0.0;
+    }
+    return;
+  }
+  const PhenoState g = ph[s.pheno];
+  const double* wv = winv + (int64_t)s.pheno * np;
+  const double a = s.alpha;
+  double zr = 0.0, rr = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
+    const double p = P[base + i];
+    const double y = Yf ? (double)Yf[base + i] : Yd[base + i];
+    const double m = mv[i];
+    const double ap = ap_value(g.tau0, g.tau1, wv[i], m, p, y);
+    X[base + i] += a * p;
+    const double r = R[base + i] - a * ap;
+    const double z = m * r;
+    R[base + i] = r;
+    Z[base + i] = z;
+    zr += z * r;
+    rr += r * r;
+  }
+  zr = block_sum(zr, sh);
+  rr = block_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    part[(c * nblk + blockIdx.x) * 2 + 0] = zr;
+    part[(c * nblk + blockIdx.x) * 2 + 1] = rr;
+  }
+}
+
+void launch_pcg_update(int64_t np, int64_t ncols, ColState* st, const PhenoState* ph,
+                       const double* winv, const double* minv, double* X, double* R, double* Z,
+                       const double* P, const float* Yf, const double* Yd, double* part,
+                       int64_t nblk, cudaStream_t s) {
+  if (ncols == 0) return;
+  dim3 grid((unsigned)nblk, (unsigned)ncols);
+  pcg_update_kernel<<<grid, kThreads, 0, s>>>(np, st, ph, winv, minv, X, R, Z, P, Yf, Yd, part, nblk);
+}
+
+// beta, iteration count and the stopping rule (sum r^2 <= tol or iter == maxiter)
+__global__ void pcg_beta_kernel(int64_t ncols, ColState* st, const double* __restrict__ part,
+                                int64_t nblk) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  ColState s = st[c];
+  s.just_done = 0;
+  if (s.active) {
+    if (s.kind == 1) {
+      s.active = 0;
+      s.just_done = 1;
+      s.iter = 1;
+    } else {
+      double zr = 0.0, rr = 0.0;
+      for (int64_t b = 0; b < nblk; ++b) {
+        zr += part[(c * nblk + b) * 2 + 0];
+        rr += part[(c * nblk + b) * 2 + 1];
+      }
+      s.beta = zr / s.rz;
+      s.rz = zr;
+      s.r2 = rr;
+      s.iter += 1;
+      if (!(rr > s.tol && s.iter < s.maxiter)) {
+        s.active = 0;
+        s.just_done = 1;
+      }
+    }
+  }
+  st[c] = s;
+}
+
+void launch_pcg_beta(int64_t ncols, ColState* st, const double* part, int64_t nblk,
+                     cudaStream_t s) {
+  if (ncols == 0) return;
+  pcg_beta_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(ncols, st, part, nblk);
+}
+
+// p = z + beta p for columns still iterating; FP32 copy for the next GRM product.
+__global__ void pcg_dir_kernel(int64_t np, const ColState* __restrict__ st, const double* __restrict__ Z,
+                               double* P, float* Pf) {
+  const int64_t c = blockIdx.y;
+  const ColState s = st[c];
+  const int64_t base = c * np;
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  if (s.active && s.kind == 0) {
+    const double b = s.beta;
+    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
+      const double p = Z[base + i] + b * P[base + i];
+      P[base + i] = p;
+      Pf[base + i] = (float)p;
+    }
+  } else if (s.just_done) {
+    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) Pf[base + i] = 0.0f;
+  }
+}
+
+void launch_pcg_dir(int64_t np, int64_t ncols, ColState* st, const double* Z, double* P, float* Pf,
+                    cudaStream_t s) {
+  if (ncols == 0) return;
+  dim3 grid((unsigned)pcg_nblk(np), (unsigned)ncols);
+  pcg_dir_kernel<<<grid, kThreads, 0, s>>>(np, st, Z, P, Pf);
+}
+
+// Rademacher probes of the counter hash (oracle/probes.py): B[j][i] = +-1 for i < nn, 0 after.
+__global__ void probe_fill_kernel(int64_t np, int64_t nn, uint64_t seed, int64_t run0,
+                                  double* B) {
+  const int64_t j = blockIdx.y;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  double v = 0.0;
+  if (i < nn) v = (hash3(seed, (uint64_t)(run0 + j), (uint64_t)i) >> 63) ? 1.0 : -1.0;
+  B[j * np + i] = v;
+}
+
+void launch_probe_fill(int64_t np, int64_t nn, uint64_t seed, int64_t run0, int64_t k, double* B,
+                       cudaStream_t s) {
+  if (k == 0) return;
+  dim3 grid((unsigned)((np + 255) / 256), (unsigned)k);
+  probe_fill_kernel<<<grid, 256, 0, s>>>(np, nn, seed, run0, B);
+}
+
+__global__ void f64_to_f32_kernel(const double* a, float* b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+__global__ void f32_to_f64_kernel(const float* a, double* b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
+}
+void launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s) {
+  if (n) f64_to_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, n);
+}
+void launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s) {
+  if (n) f32_to_f64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, n);
+}
+
+}  // namespace sg

@@ -1,0 +1,122 @@
+// Internal declarations shared by the CUDA translation units of libsaigegpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+
+namespace sg {
+
+// ---- layout helpers
+inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+constexpr int kRowTile = 128;   // GRM rows/cols are padded to a multiple of this
+constexpr int kMarkerTile = 64; // standardised-genotype columns padded to this (128 B of BF16)
+constexpr int kPitchAlign = 16; // byte pitch of packed genotype rows
+
+// ---- counter hash shared with saigegpu/synth.py and the oracle (splitmix64 finaliser x3)
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__host__ __device__ inline uint64_t hash3(uint64_t seed, uint64_t stream, uint64_t idx) {
+  uint64_t h = mix64(seed ^ 0x5851F42D4C957F2Dull);
+  h = mix64(h ^ (stream * 0x9E3779B97F4A7C15ull));
+  return mix64(h ^ (idx * 0xD1B54A32D192ED03ull));
+}
+
+// ---- genotype kernels (k_geno.cu)
+struct MarkerQC {
+  int32_t allele;   // allele count after the integer fill
+  int32_t mac;
+  int32_t nmiss;
+  float freq;       // altFreq over Nnomissing (second estimate)
+  float invstd;
+  int32_t fill;     // int(round(2p)) replacement for missing calls
+  int32_t pass_qc;  // GRM marker
+  int32_t pass_vr;  // variance-ratio marker
+};
+
+void launch_marker_qc(const uint8_t* raw, int64_t raw_pitch, int64_t m, int64_t n_fam,
+                      const uint32_t* maskbits, int64_t nn, float min_maf, float max_miss,
+                      const uint8_t* vr_flag, float min_mac_vr, int is_var_ratio, MarkerQC* out,
+                      cudaStream_t s);
+void launch_repack(const uint8_t* raw, int64_t raw_pitch, const int32_t* src_marker,
+                   const MarkerQC* qc, int64_t m_out, const int32_t* sub0, int64_t nn,
+                   int identity, uint8_t* out, int64_t out_pitch, cudaStream_t s);
+void launch_lut(const MarkerQC* qc, const int32_t* src_marker, int64_t m_out, float* lut4,
+                cudaStream_t s);
+// Z (np x mp, row = sample, markers contiguous) from packed genotypes
+void launch_zbuild_f32(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
+                       int64_t nn, int64_t np, int64_t mp, float* Z, cudaStream_t s);
+void launch_zbuild_bf16(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
+                        int64_t nn, int64_t np, int64_t mp, void* Zhi, void* Zlo, cudaStream_t s);
+void launch_diag(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
+                 int64_t nn, double* diag64, float* diag32, cudaStream_t s);
+void launch_synth_bed(uint64_t seed, int64_t n, int64_t m, uint32_t miss_thr16, uint8_t* out,
+                      cudaStream_t s);
+void launch_genetic_value(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
+                          int64_t nn, uint64_t seed, double* out, cudaStream_t s);
+void launch_unpack_marker(const uint8_t* packed_row, int64_t nn, const float* lut4, int32_t* g,
+                          float* z, cudaStream_t s);
+
+// ---- SIMT GEMM (k_gemm_simt.cu): C = scale * A B^T, A (M x K) and B (N x K) row-major.
+// mode 0: C (M x N) row-major; mode 1: C^T stored (N x M, ldc along M);
+// mode 2: symmetric rank-k update, A == B, only tiles with block j <= block i computed and
+// mirrored.  Requires K % 8 == 0, lda/ldb % 4 == 0, M % 128 == 0, N % BN == 0.
+void launch_gemm_nt_f32(const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
+                        int64_t ldc, int64_t M, int64_t N, int64_t K, float scale, int mode,
+                        cudaStream_t s);
+void launch_gemv_f64(const float* K, int64_t ld, int64_t n, const double* x, double* y,
+                     cudaStream_t s);
+
+// ---- tcgen05 GEMM (k_tc.cu); returns false when the shape is unsupported.
+bool tc_available();
+// K = scale * Z Z^T over lower-triangle tiles, Z bf16 (np x mp), K fp32 (np x np).  With
+// Zlo != nullptr (Z = Zhi + Zlo split) it accumulates Zhi Zhi^T + Zhi Zlo^T + Zlo Zhi^T.
+cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t mp, float* K,
+                         float scale, cudaStream_t s);
+// Y^T (ncols x np) = K (np x np fp32, tf32 MMA) * P^T with P (ncols x np fp32)
+cudaError_t tc_gemm_tf32(const float* K, int64_t np, const float* P, int64_t ncols, float* Y,
+                         cudaStream_t s);
+
+// ---- PCG engine kernels (k_pcg.cu)
+struct ColState {
+  int32_t pheno;    // phenotype slot
+  int32_t kind;     // 0 = PCG, 1 = product only, -1 = free
+  int32_t active;   // 1 while iterating
+  int32_t iter;
+  int32_t maxiter;
+  int32_t just_done;
+  double tol;
+  double rz;        // r'z of the current iterate
+  double r2;        // r'r
+  double alpha, beta;
+};
+struct PhenoState {
+  double tau0, tau1;
+};
+void launch_pcg_init(int64_t np, int64_t ncols, const int32_t* cols, int64_t ncols_sel,
+                     ColState* st, const PhenoState* ph, const double* minv, const double* B,
+                     double* X, double* R, double* Z, double* P, float* Pf, double* part,
+                     int64_t nblk, cudaStream_t s);
+void launch_pcg_sigma_dot(int64_t np, int64_t ncols, ColState* st, const PhenoState* ph,
+                          const double* winv, const double* minv, const double* P,
+                          const float* Yf, const double* Yd, double* part, int64_t nblk,
+                          cudaStream_t s);
+void launch_pcg_alpha(int64_t ncols, ColState* st, const double* part, int64_t nblk,
+                      cudaStream_t s);
+void launch_pcg_update(int64_t np, int64_t ncols, ColState* st, const PhenoState* ph,
+                       const double* winv, const double* minv, double* X, double* R, double* Z,
+                       const double* P, const float* Yf, const double* Yd, double* part,
+                       int64_t nblk, cudaStream_t s);
+void launch_pcg_beta(int64_t ncols, ColState* st, const double* part, int64_t nblk,
+                     cudaStream_t s);
+void launch_pcg_dir(int64_t np, int64_t ncols, ColState* st, const double* Z, double* P,
+                    float* Pf, cudaStream_t s);
+void launch_probe_fill(int64_t np, int64_t nn, uint64_t seed, int64_t run0, int64_t k,
+                       double* B, cudaStream_t s);
+void launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
+void launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s);
+int64_t pcg_nblk(int64_t np);
+
+}  // namespace sg

@@ -1,0 +1,13 @@
+"""saigegpu -- GB300-native SAIGE step-1 hot path (dense GRM + PCG/AI-REML).
+
+The compute lives in ``libsaigegpu.so`` (hand-written sm_103a CUDA behind the
+C ABI of ``include/saigegpu.h``); this package is the host side: the ctypes
+binding, the mirror of the reference's R driver, phenotype preparation, the
+multi-phenotype batching/serving loop and synthetic cohorts.
+"""
+from .context import (Context, GRM_FP32_SIMT, GRM_BF16_TC, GRM_BF16X3_TC, MV_FP32_SIMT,
+                      MV_TF32_TC, MV_FP64_PLAIN)
+from ._lib import SaigeGpuError, load
+
+__all__ = ["Context", "SaigeGpuError", "load", "GRM_FP32_SIMT", "GRM_BF16_TC", "GRM_BF16X3_TC",
+           "MV_FP32_SIMT", "MV_TF32_TC", "MV_FP64_PLAIN"]

@@ -1,0 +1,150 @@
+"""CPU tests of the oracle: pinned against the reference's own fixtures and against direct algebra."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import aireml, plink, probes
+from saigegpu import prep, synth
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_decode_matches_plink_frq(golden_plink):
+    """Known-answer test: A1 MAF of the reference's example .bed equals PLINK's .frq (all 10k markers)."""
+    bed, n, m, _ = golden_plink
+    codes = plink.decode_bed(bed, n, m)
+    ok = codes != 3
+    p = np.where(ok, codes, 0).sum(1) / (2.0 * ok.sum(1))
+    frq = np.load(os.path.join(GOLDEN, "plink_1000x10k_frq.npy"))
+    assert np.array_equal(np.round(np.minimum(p, 1 - p), 4), frq)
+
+
+def test_setgeno_qc_and_imputation():
+    bed, codes = synth.synth_bed(7, 37, 60, 0.05)
+    sub = np.arange(1, 38)[::-1].copy()
+    g = plink.setgeno(bed, 37, 60, sub, np.ones(37, bool), 0.05, 0.15)
+    assert g.codes.shape[1] == 37
+    kept = np.nonzero(g.qc_mask)[0]
+    for row, j in enumerate(kept):
+        c = codes[j][sub - 1]
+        miss = c == 3
+        np.testing.assert_array_equal(g.codes[row][~miss], c[~miss])
+        nm = c[~miss].astype(float)
+        fill = int(np.floor(np.float64(np.float32(2) * np.float32(nm.sum()) / np.float32(2 * len(nm))) + 0.5))
+        assert np.all(g.codes[row][miss] == fill)
+    assert (g.freq >= 0).all() and (g.freq <= 1).all()
+
+
+def test_vr_markers_leave_the_grm():
+    bed, codes = synth.synth_bed(9, 200, 80, 0.0)
+    allm = plink.setgeno(bed, 200, 80, np.arange(1, 201), np.ones(200, bool), 0.01, 0.15)
+    vr = np.array([1, 5, 9, 33, 70])
+    g = plink.setgeno(bed, 200, 80, np.arange(1, 201), np.ones(200, bool), 0.01, 0.15, vr, 20, True)
+    for j in vr:
+        if allm.qc_mask[j] and g.vr_index.size and j in g.vr_index:
+            assert not g.qc_mask[j]
+    assert g.codes.shape[0] + len(g.vr_index) >= allm.codes.shape[0]
+
+
+def test_pack_roundtrip():
+    rng = np.random.default_rng(0)
+    codes = rng.integers(0, 3, size=(5, 13)).astype(np.uint8)
+    packed = plink.pack_codes(codes)
+    fields = np.stack([(packed >> (2 * j)) & 3 for j in range(4)], axis=2).reshape(5, -1)[:, :13]
+    back = 2 - ((fields & 1) + (fields >> 1))
+    np.testing.assert_array_equal(back, codes)
+
+
+def _small_problem(seed=3, n=150, m=400):
+    bed, _ = synth.synth_bed(seed, n, m, 0.01)
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+    return aireml.DenseGRM(g), g
+
+
+def test_oracle_pcg_solves_sigma():
+    grm, _ = _small_problem()
+    n = grm.n
+    rng = np.random.default_rng(1)
+    w = rng.uniform(0.1, 0.3, n)
+    tau = np.array([1.0, 0.4])
+    b = rng.standard_normal((n, 3))
+    x, it = aireml.pcg(grm, w, tau, b, 500, 1e-20, return_iters=True)
+    S = np.diag(tau[0] / w) + tau[1] * grm.K
+    np.testing.assert_allclose(x, np.linalg.solve(S, b), rtol=1e-8, atol=1e-10)
+    for j in range(3):
+        xj, itj = aireml.pcg(grm, w, tau, b[:, j], 500, 1e-20, return_iters=True)
+        assert itj == it[j]
+        np.testing.assert_allclose(xj, x[:, j], rtol=1e-12)
+
+
+def test_oracle_hutchinson_trace_is_unbiased():
+    grm, _ = _small_problem()
+    n = grm.n
+    w = np.full(n, 0.2)
+    tau = np.array([1.0, 0.3])
+    X = np.ones((n, 1))
+    S = np.diag(tau[0] / w) + tau[1] * grm.K
+    Si = np.linalg.inv(S)
+    SX = Si @ X
+    cov = np.linalg.inv(X.T @ SX)
+    P = Si - SX @ cov @ SX.T
+    exact = np.trace(P @ grm.K)
+    est, nr = aireml.get_trace(grm, SX, X, w, tau, cov, 30, 500, 1e-12, 0.0025)
+    assert nr >= 30
+    assert abs(est - exact) / exact < 0.05
+
+
+def test_probes_are_rademacher_and_deterministic():
+    u = probes.rademacher(200, 3, 1000)
+    assert set(np.unique(u)) == {-1.0, 1.0}
+    np.testing.assert_array_equal(u, probes.rademacher(200, 3, 1000))
+    assert abs(u.mean()) < 0.1
+    assert not np.array_equal(u, probes.rademacher(200, 4, 1000))
+    assert np.array_equal(probes.hash3(1, 2, np.arange(5)), synth.hash3(1, 2, np.arange(5)))
+
+
+def test_glm_score_equations():
+    rng = np.random.default_rng(2)
+    n = 500
+    C = rng.standard_normal((n, 2))
+    y = (rng.uniform(size=n) < 1 / (1 + np.exp(-(-1 + C @ [0.5, -0.3])))).astype(float)
+    f0 = prep.make_fit0(y, C, "binary", covariate_offset=False)
+    mu = 1 / (1 + np.exp(-f0["linear_predictors"]))
+    np.testing.assert_allclose(f0["X"].T @ (y - mu), 0, atol=1e-6)
+
+
+def test_golden_theta_monte_carlo_band(golden_plink):
+    """The reference's example fits pin tau only loosely (probes and VR markers come from R's RNG)."""
+    bed, n, m, ph = golden_plink
+    gold = json.load(open(os.path.join(GOLDEN, "golden_fits.json")))
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+    grm = aireml.DenseGRM(g)
+    cov = np.column_stack([ph["x1"], ph["x2"]])
+    fb = prep.make_fit0(ph["y_binary"], cov, "binary", True)
+    rb = aireml.glmmkin_binary(grm, fb)
+    t_gold = gold["example_binary_fullGRM"]["theta"][1]
+    # Monte-Carlo spread of tau1 over probe seeds here is ~0.034 (sd); allow 4 sd
+    assert abs(rb["theta"][1] - t_gold) < 4 * 0.034
+    assert abs(rb["coefficients"][0] - gold["example_binary_fullGRM"]["coefficients"][0]) < 0.05
+    fq = prep.make_fit0(ph["y_quantitative"], cov, "quantitative", True)
+    rq = aireml.glmmkin_quantitative(grm, fq)
+    tq = np.array(gold["example_quantitative_fullGRM"]["theta"])
+    assert np.all(np.abs(rq["theta"] - tq) / tq < 0.25)
+    assert abs(rq["theta"].sum() - tq.sum()) / tq.sum() < 0.05
+
+
+def test_c_restatement_of_reference_cpu_path():
+    from oracle import cpu_ref
+    grm, g = _small_problem(5, 120, 300)
+    cg = cpu_ref.CpuGeno(g)
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(grm.n)
+    np.testing.assert_allclose(cg.crossprod(b), grm.K @ b, rtol=1e-4, atol=1e-4 * np.abs(grm.K @ b).max())
+    w = rng.uniform(0.1, 0.3, grm.n)
+    tau = np.array([1.0, 0.3])
+    x, it = cg.pcg(w, tau, b, 500, 1e-5)
+    xo, ito = aireml.pcg(grm, w, tau, b, 500, 1e-5, return_iters=True)
+    assert abs(it - ito) <= 2
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-3
