@@ -235,7 +235,10 @@ extern "C" int sg_kernel_launches(const sg_ctx* c, uint64_t* count) {
 }
 
 // ------------------------------------------------------------------ genotypes
+static void engine_free(sg_ctx* c);
+
 static void free_geno(sg_ctx* c) {
+  engine_free(c);
   dev_free_t(c, c->d_packed);
   dev_free_t(c, c->d_packed_vr);
   dev_free_t(c, c->d_lut);
@@ -528,6 +531,7 @@ extern "C" int sg_grm_build(sg_ctx* c, int precision) {
     return set_err(c, SG_ERR_INVALID, "tcgen05 SYRK needs an sm_103a device");
   if (c->m_qc == 0) return set_err(c, SG_ERR_STATE, "no marker passed QC");
   dev_free_t(c, c->d_K);
+  engine_free(c);
   c->have_grm = false;
   const int64_t np = round_up(c->nn, kRowTile);
   const int64_t mp = round_up(c->m_qc, kMarkerTile);
@@ -584,6 +588,36 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.Yd); dev_free_t(c, e.Pf); dev_free_t(c, e.Yf); dev_free_t(c, e.d_st);
   dev_free_t(c, e.d_ph); dev_free_t(c, e.d_cols);
   e.cap_cols = e.cap_ph = 0;
+  e.np = 0;
+  e.hi_col = 0;
+  e.n_active = 0;
+  e.queue.clear();
+  e.reqs.clear();
+  e.h_st.clear();
+  e.col_req.clear();
+  e.ph_set.clear();
+}
+
+// Drop every queued and in-flight request (the blocking drop-ins own the engine).
+static int engine_clear(sg_ctx* c) {
+  Engine& e = c->eng;
+  if (e.cap_cols == 0) return SG_OK;
+  bool any = false;
+  for (int64_t col = 0; col < (int64_t)e.col_req.size(); ++col) {
+    if (e.col_req[col] < 0) continue;
+    any = true;
+    e.col_req[col] = -1;
+    e.h_st[col] = ColState{};
+    e.h_st[col].kind = -1;
+    SG_CUDA(c, cudaMemsetAsync(e.Pf + col * e.np, 0, e.np * 4, c->stream));
+  }
+  if (any)
+    SG_CUDA(c, cudaMemcpyAsync(e.d_st, e.h_st.data(), e.cap_cols * sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+  e.hi_col = 0;
+  e.n_active = 0;
+  e.queue.clear();
+  e.reqs.clear();
+  return sync(c);
 }
 
 static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
@@ -965,6 +999,7 @@ int fetch(sg_ctx* c, int64_t id, double* x, int32_t* it) { return sg_engine_fetc
 int dropin_setup(sg_ctx* c, const float* w, const float* tau, int64_t cols) {
   NEED_GRM(c);
   Engine& e = c->eng;
+  SG_TRY(engine_clear(c));
   if (e.cap_cols < cols || e.cap_ph < 1 || e.np != c->np) SG_TRY(engine_reserve(c, std::max<int64_t>(cols, 128), 1));
   std::vector<double> wd(c->nn);
   for (int64_t i = 0; i < c->nn; ++i) wd[i] = w[i];
@@ -1158,8 +1193,7 @@ int trace_probes(sg_ctx* c, const std::vector<double>& SX, int p, const std::vec
 extern "C" int sg_grm_matmul(sg_ctx* c, const double* V, int64_t k, double* out) {
   NEED_GRM(c);
   if (k <= 0 || !V || !out) return set_err(c, SG_ERR_INVALID, "bad arguments");
-  Engine& e = c->eng;
-  if (e.cap_ph < 1 || !e.ph_set[0]) {
+  {
     std::vector<float> w(c->nn, 1.0f);
     const float tau[2] = {1.0f, 0.0f};
     SG_TRY(dropin_setup(c, w.data(), tau, std::min<int64_t>(k, 256)));
@@ -1209,7 +1243,8 @@ extern "C" int sg_pcg_solve(sg_ctx* c, const double* w, const double* tau, const
   NEED_GRM(c);
   if (k <= 0 || !w || !tau || !B || !X) return set_err(c, SG_ERR_INVALID, "bad arguments");
   Engine& e = c->eng;
-  if (e.cap_cols < std::min<int64_t>(k, 256) || e.cap_ph < 1)
+  SG_TRY(engine_clear(c));
+  if (e.cap_cols < std::min<int64_t>(k, 256) || e.cap_ph < 1 || e.np != c->np)
     SG_TRY(engine_reserve(c, std::min<int64_t>(std::max<int64_t>(k, 128), 2048), 1));
   SG_TRY(sg_engine_set_pheno(c, 0, w, tau, nullptr));
   std::vector<int64_t> ids(k);

@@ -1,7 +1,441 @@
-// placeholder replaced by the tcgen05 kernels
+// tcgen05 (5th-generation tensor core) GEMMs of the GRM path, sm_103a.
+//
+//   D[128 x BN] (+)= A[128 x K] * B[BN x K]^T,  A and B K-major in global memory
+//
+// One CTA computes one 128 x BN output tile over the whole reduction:
+//   warp 0 (one lane)  TMA producer: cp.async.bulk.tensor 2D loads of 128-byte
+//                      wide K slices (SWIZZLE_128B) into an S-stage ring,
+//                      completion tracked by mbarrier transaction counts;
+//   warp 1 (one lane)  MMA issuer: tcgen05.mma.cta_group::1 with shared-memory
+//                      descriptors, FP32 accumulator in TMEM (128 lanes x BN
+//                      columns); tcgen05.commit frees each stage and finally
+//                      signals the accumulator;
+//   warp 2             allocates / frees the TMEM columns;
+//   warps 0-3          epilogue: tcgen05.ld 32x32b (each warp its 32 TMEM
+//                      lanes = 32 output rows), scale, store to global.
+// No cluster, no multicast (cta_group::1).  Every mbarrier wait is bounded by
+// a global-timer budget; on expiry the kernel records an error code, skips
+// the remaining work, frees its TMEM and returns.
+//
+// Uses:
+//   * SYRK  K = scale * Z Z^T (Z bf16, kind::f16): lower-triangle tiles only,
+//     each element (r, c <= r) written to K[r][c] and K[c][r].  The split
+//     variant accumulates Zh Zh^T + Zh Zl^T + Zl Zh^T for Z = Zh + Zl.
+//   * GRM.V Y^T = K P^T (K fp32 read as tf32, kind::tf32), output stored
+//     RHS-major so each TMEM column is a coalesced row of Y^T.
 #include "sg_internal.h"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cstdio>
+#include <mutex>
+#include <vector>
+
 namespace sg {
-bool tc_available() { return false; }
-cudaError_t tc_syrk_bf16(const void*, const void*, int64_t, int64_t, float*, float, cudaStream_t) { return cudaErrorNotSupported; }
-cudaError_t tc_gemm_tf32(const float*, int64_t, const float*, int64_t, float*, cudaStream_t) { return cudaErrorNotSupported; }
+
+namespace {
+
+constexpr int kTileM = 128;
+constexpr int kRowBytes = 128;                 // one SWIZZLE_128B atom row
+constexpr int kATileBytes = kTileM * kRowBytes;  // 16 KB
+constexpr unsigned long long kWaitBudgetNs = 4000000000ull;  // 4 s per wait
+
+__device__ int g_tc_error = 0;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: returns false (and records ``code``) when the budget runs out
+// or another thread of this kernel already gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int code,
+                                          volatile int* abort_flag) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255u) == 0u) {
+      if (*abort_flag) return false;
+      if (gtimer() - t0 > kWaitBudgetNs) {
+        *abort_flag = 1;
+        atomicCAS(&g_tc_error, 0, code);
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int32_t x, int32_t y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor, K-major operand in SWIZZLE_128B layout:
+// start address >> 4 (bits 0-13), LBO unused for swizzled K-major (1),
+// SBO = 1024 B between 8-row core-matrix groups (bits 32-45), descriptor
+// version 1 (bits 46-47), layout SWIZZLE_128B = 2 (bits 61-63).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Instruction descriptor: FP32 accumulator, A/B format (1 = BF16 for
+// kind::f16, 2 = TF32 for kind::tf32), both K-major, N >> 3 at bit 17,
+// M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t make_idesc(uint32_t fmt, int n) {
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(kTileM >> 4) << 24);
+}
+
+template <bool kTF32>
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                     uint32_t accumulate) {
+  if constexpr (kTF32) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+  }
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct TileCoord {
+  int32_t bm, bn;  // row block (128 rows) and column block (BN cols)
+};
+
+// kSplit: A = [Ah | Al], B = [Bh | Bl] (second maps); accumulates Ah Bh + Ah Bl + Al Bh.
+template <bool kTF32, int BN, int S, bool kSplit>
+__global__ void __launch_bounds__(128, 1)
+tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+               const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
+               const TileCoord* __restrict__ tiles, int num_kb, float* __restrict__ D, int64_t ldd,
+               float scale, int mode) {
+  constexpr int kBTileBytes = BN * kRowBytes;
+  constexpr int kStageBytes = (kATileBytes + kBTileBytes) * (kSplit ? 2 : 1);
+  constexpr uint32_t kFmt = kTF32 ? 2u : 1u;
+  constexpr int kKSteps = 4;           // 128-byte slice / 32 bytes per MMA K step
+  constexpr uint32_t kTmemCols = BN < 32 ? 32 : BN;
+  constexpr uint32_t kIdesc = make_idesc(kFmt, BN);
+
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * kStageBytes);
+  uint64_t* empty = full + S;
+  uint64_t* accum = empty + S;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const TileCoord tc = tiles[blockIdx.x];
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accum, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 ::"r"(smem_u32(tmem_slot)), "r"(kTmemCols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    const int32_t ya = tc.bm * kTileM, yb = tc.bn * BN;
+    for (int kb = 0; kb < num_kb; ++kb) {
+      const int s = kb % S;
+      const uint32_t ph = (uint32_t)(kb / S) & 1u;
+      if (!mbar_wait(&empty[s], ph ^ 1u, 1, abort_flag)) break;
+      uint8_t* st = smem + s * kStageBytes;
+      mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
+      const int32_t x = kb * (kRowBytes / (kTF32 ? 4 : 2));
+      tma_load_2d(st, &mapA, &full[s], x, ya);
+      tma_load_2d(st + kATileBytes, &mapB, &full[s], x, yb);
+      if constexpr (kSplit) {
+        tma_load_2d(st + kATileBytes + kBTileBytes, &mapA2, &full[s], x, ya);
+        tma_load_2d(st + 2 * kATileBytes + kBTileBytes, &mapB2, &full[s], x, yb);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    for (int kb = 0; kb < num_kb; ++kb) {
+      const int s = kb % S;
+      const uint32_t ph = (uint32_t)(kb / S) & 1u;
+      if (!mbar_wait(&full[s], ph, 2, abort_flag)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = smem_u32(smem + s * kStageBytes);
+      const uint32_t b0 = a0 + kATileBytes;
+#pragma unroll
+      for (int k = 0; k < kKSteps; ++k) {
+        const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
+        umma<kTF32>(tmem_base, smem_desc_sw128(a0 + 32 * k), smem_desc_sw128(b0 + 32 * k), kIdesc, acc);
+        if constexpr (kSplit) {
+          const uint32_t a1 = b0 + kBTileBytes;      // Al
+          const uint32_t b1 = a1 + kATileBytes;      // Bl
+          umma<kTF32>(tmem_base, smem_desc_sw128(a0 + 32 * k), smem_desc_sw128(b1 + 32 * k), kIdesc, 1u);
+          umma<kTF32>(tmem_base, smem_desc_sw128(a1 + 32 * k), smem_desc_sw128(b0 + 32 * k), kIdesc, 1u);
+        }
+      }
+      umma_commit(&empty[s]);  // stage reusable once these MMAs have read it
+    }
+    umma_commit(accum);
+  }
+  __syncwarp();
+
+  // ---------------- epilogue: all four warps
+  int go = mbar_wait(accum, 0u, 3, abort_flag) && !*abort_flag;
+  __syncwarp();
+  go = __shfl_sync(0xffffffffu, go, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (go) {
+    const int64_t r = (int64_t)tc.bm * kTileM + warp * 32 + lane;
+    const uint32_t trow = tmem_base + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t v[32];
+      tmem_ld32(trow + (uint32_t)c0, v);
+      const int64_t cbase = (int64_t)tc.bn * BN + c0;
+      if (mode == 1) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) D[(cbase + j) * ldd + r] = __uint_as_float(v[j]) * scale;
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int64_t c = cbase + j;
+          if (c <= r) {
+            const float f = __uint_as_float(v[j]) * scale;
+            D[r * ldd + c] = f;
+            D[c * ldd + r] = f;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 2) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------- host side
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// 2D K-major map: rows x inner elements, row stride in bytes, box = 128 B x box_rows.
+bool make_map(CUtensorMap* m, const void* base, bool f32, uint64_t inner, uint64_t rows,
+              uint64_t row_bytes, uint32_t box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {inner, rows};
+  const cuuint64_t strides[1] = {row_bytes};
+  const cuuint32_t box[2] = {(cuuint32_t)(kRowBytes / (f32 ? 4 : 2)), box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                  const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+template <bool kTF32, int BN, int S, bool kSplit>
+constexpr size_t smem_bytes() {
+  return (size_t)S * (kATileBytes + BN * kRowBytes) * (kSplit ? 2 : 1) + 1024 + 256;
+}
+
+template <bool kTF32, int BN, int S, bool kSplit>
+cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
+                   const CUtensorMap& b2, const TileCoord* tiles, int ntiles, int num_kb, float* D,
+                   int64_t ldd, float scale, int mode, cudaStream_t s) {
+  auto k = tc_gemm_kernel<kTF32, BN, S, kSplit>;
+  const size_t sm = smem_bytes<kTF32, BN, S, kSplit>();
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k<<<ntiles, 128, sm, s>>>(a, b, a2, b2, tiles, num_kb, D, ldd, scale, mode);
+  return cudaGetLastError();
+}
+
+struct TileCache {
+  std::vector<TileCoord> host;
+  TileCoord* dev = nullptr;
+  size_t cap = 0;
+};
+
+cudaError_t upload_tiles(TileCache& tc, cudaStream_t s) {
+  if (tc.host.size() > tc.cap) {
+    if (tc.dev) cudaFree(tc.dev);
+    tc.cap = tc.host.size();
+    cudaError_t e = cudaMalloc(&tc.dev, tc.cap * sizeof(TileCoord));
+    if (e != cudaSuccess) {
+      tc.dev = nullptr;
+      tc.cap = 0;
+      return e;
+    }
+  }
+  return cudaMemcpyAsync(tc.dev, tc.host.data(), tc.host.size() * sizeof(TileCoord),
+                         cudaMemcpyHostToDevice, s);
+}
+
+cudaError_t check_error_flag(cudaStream_t s) {
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  int h = 0;
+  e = cudaMemcpyFromSymbol(&h, g_tc_error, sizeof(int));
+  if (e != cudaSuccess) return e;
+  if (h != 0) {
+    const int zero = 0;
+    cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(int));
+    return cudaErrorLaunchTimeout;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace
+
+bool tc_available() {
+  int dev = 0, major = 0, minor = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  return major == 10 && minor == 3 && encode_fn() != nullptr;
+}
+
+cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t mp, float* K,
+                         float scale, cudaStream_t s) {
+  constexpr int BN = 256;
+  if (np % kTileM != 0 || mp % 64 != 0) return cudaErrorInvalidValue;
+  CUtensorMap a, b, a2, b2;
+  const uint64_t rb = (uint64_t)mp * 2;
+  if (!make_map(&a, Zhi, false, mp, np, rb, kTileM) || !make_map(&b, Zhi, false, mp, np, rb, BN))
+    return cudaErrorInvalidValue;
+  a2 = a;
+  b2 = b;
+  if (Zlo && (!make_map(&a2, Zlo, false, mp, np, rb, kTileM) || !make_map(&b2, Zlo, false, mp, np, rb, BN)))
+    return cudaErrorInvalidValue;
+  // lower-triangle tiles: column block bn (BN wide) starts at or before the row block's last row;
+  // column blocks past np are not formed (np % BN may be 128: the last block is then half empty,
+  // and its TMA rows past np read zero fill).
+  static TileCache cache;
+  cache.host.clear();
+  const int64_t nbm = np / kTileM;
+  const int64_t nbn = (np + BN - 1) / BN;
+  for (int64_t bm = 0; bm < nbm; ++bm)
+    for (int64_t bn = 0; bn < nbn; ++bn)
+      if (bn * BN <= bm * kTileM + kTileM - 1) cache.host.push_back(TileCoord{(int32_t)bm, (int32_t)bn});
+  cudaError_t e = upload_tiles(cache, s);
+  if (e != cudaSuccess) return e;
+  const int num_kb = (int)(mp / 64);
+  if (Zlo)
+    e = launch<false, BN, 2, true>(a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, K, np, scale, 2, s);
+  else
+    e = launch<false, BN, 4, false>(a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, K, np, scale, 2, s);
+  if (e != cudaSuccess) return e;
+  return check_error_flag(s);
+}
+
+cudaError_t tc_gemm_tf32(const float* K, int64_t np, const float* P, int64_t ncols, float* Y,
+                         cudaStream_t s) {
+  if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0) return cudaErrorInvalidValue;
+  const int BN = ncols % 128 == 0 ? 128 : (ncols % 64 == 0 ? 64 : 32);
+  CUtensorMap a, b;
+  if (!make_map(&a, K, true, np, np, (uint64_t)np * 4, kTileM) ||
+      !make_map(&b, P, true, np, ncols, (uint64_t)np * 4, BN))
+    return cudaErrorInvalidValue;
+  static TileCache cache;
+  cache.host.clear();
+  for (int64_t bm = 0; bm < np / kTileM; ++bm)
+    for (int64_t bn = 0; bn < ncols / BN; ++bn) cache.host.push_back(TileCoord{(int32_t)bm, (int32_t)bn});
+  cudaError_t e = upload_tiles(cache, s);
+  if (e != cudaSuccess) return e;
+  const int num_kb = (int)(np / 32);
+  if (BN == 128)
+    e = launch<true, 128, 4, false>(a, b, a, b, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
+  else if (BN == 64)
+    e = launch<true, 64, 6, false>(a, b, a, b, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
+  else
+    e = launch<true, 32, 8, false>(a, b, a, b, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
+  if (e != cudaSuccess) return e;
+  return check_error_flag(s);
+}
+
+}  // namespace sg
