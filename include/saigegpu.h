@@ -50,8 +50,10 @@ enum sg_grm_precision {
 /* GRM.V product engines used inside the PCG (sg_set_matvec_mode) */
 enum sg_matvec_mode {
   SG_MV_FP32_SIMT = 0,  /* FP32 K, FP32 operands, CUDA cores */
-  SG_MV_TF32_TC = 1,    /* tcgen05 kind::tf32 on the FP32 K, FP64 iterative refinement */
-  SG_MV_FP64_PLAIN = 2  /* plain FP64 GEMV (the single-RHS baseline) */
+  SG_MV_TF32_TC = 1,    /* tcgen05 kind::tf32 on the FP32 K: one product, ~2^-11 relative per term */
+  SG_MV_FP64_PLAIN = 2, /* plain FP64 GEMV (the single-RHS baseline) */
+  SG_MV_TF32X3_TC = 3   /* split-TF32 on tcgen05: K = Khi + Klo, P = Phi + Plo, three products
+                           accumulated in TMEM (FP32-class accuracy at tensor-core rate) */
 };
 
 /* ------------------------------------------------------------ context */
@@ -200,8 +202,16 @@ int sg_engine_run(sg_ctx *ctx, int64_t max_steps, int64_t *n_finished);
 /* Fetch and release a finished column: x[n], iterations.  SG_ERR_STATE if not finished. */
 int sg_engine_fetch(sg_ctx *ctx, int64_t id, double *x, int32_t *iters);
 int sg_engine_cancel(sg_ctx *ctx, int64_t id);
+/* Ids of columns that finished since the previous poll (up to max_ids); *n_out gets the count. */
+int sg_engine_poll(sg_ctx *ctx, int64_t *ids, int64_t max_ids, int64_t *n_out);
 /* counters: [0]=engine steps, [1]=columns retired, [2]=column-iterations, [3]=GRM passes */
 int sg_engine_stats(sg_ctx *ctx, int64_t *stats4);
+/* device timing from CUDA events on the engine stream:
+ * [0]=engine-step device ms, [1]=GRM.V GEMM device ms, [2]=GEMM launches,
+ * [3]=algorithmic GEMM FLOPs over the columns processed (2 n^2 each), [4]=columns processed,
+ * [5]=occupied (useful) columns processed */
+int sg_engine_timing(sg_ctx *ctx, double *t6);
+int sg_engine_reset_timing(sg_ctx *ctx);
 
 /* ------------------------------------------------------------ synthetic cohorts (benchmarks / tests)
  * Writes a SNP-major .bed image (with magic) for n samples x m markers into device memory owned by

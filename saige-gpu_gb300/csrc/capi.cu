@@ -56,6 +56,10 @@ struct Engine {
   int64_t hi_col = 0;
   int64_t n_active = 0;
   int64_t steps = 0, retired = 0, col_iters = 0, grm_passes = 0;
+  std::vector<int64_t> finished;  // ids retired since the last poll
+  float* Pflo = nullptr;          // low TF32 halves of Pf (split-TF32 mode)
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  double t_step_ms = 0, t_gemm_ms = 0, gemm_launches = 0, gemm_flops = 0, gemm_cols = 0, useful_cols = 0;
 };
 
 }  // namespace
@@ -84,6 +88,8 @@ struct sg_ctx {
   bool have_grm = false;
   int64_t np = 0;
   float* d_K = nullptr;
+  float* d_Klo = nullptr;   // K - tf32(K) while the split-TF32 engine is selected (d_K then holds tf32(K))
+  bool k_split = false;
   double* d_diag = nullptr;
   float* d_diag32 = nullptr;
   std::vector<double> diag;
@@ -218,13 +224,22 @@ extern "C" int sg_device_bytes_in_use(const sg_ctx* c, uint64_t* bytes) {
   return SG_OK;
 }
 
+__global__ void add_inplace_kernel(float* a, const float* b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = a[i] + b[i];
+}
+
+static int ensure_k_split(sg_ctx* c, bool want);
+
 extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
   if (!c) return SG_ERR_INVALID;
-  if (mode != SG_MV_FP32_SIMT && mode != SG_MV_TF32_TC && mode != SG_MV_FP64_PLAIN)
+  if (mode != SG_MV_FP32_SIMT && mode != SG_MV_TF32_TC && mode != SG_MV_FP64_PLAIN &&
+      mode != SG_MV_TF32X3_TC)
     return set_err(c, SG_ERR_INVALID, "unknown matvec mode %d", mode);
-  if (mode == SG_MV_TF32_TC && !tc_available())
+  if ((mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC) && !tc_available())
     return set_err(c, SG_ERR_INVALID, "tcgen05 path needs an sm_103a device");
   c->mv_mode = mode;
+  if (c->have_grm) return ensure_k_split(c, mode == SG_MV_TF32X3_TC);
   return SG_OK;
 }
 
@@ -244,6 +259,8 @@ static void free_geno(sg_ctx* c) {
   dev_free_t(c, c->d_lut);
   dev_free_t(c, c->d_lut_vr);
   dev_free_t(c, c->d_K);
+  dev_free_t(c, c->d_Klo);
+  c->k_split = false;
   dev_free_t(c, c->d_diag);
   dev_free_t(c, c->d_diag32);
   c->have_geno = false;
@@ -531,6 +548,8 @@ extern "C" int sg_grm_build(sg_ctx* c, int precision) {
     return set_err(c, SG_ERR_INVALID, "tcgen05 SYRK needs an sm_103a device");
   if (c->m_qc == 0) return set_err(c, SG_ERR_STATE, "no marker passed QC");
   dev_free_t(c, c->d_K);
+  dev_free_t(c, c->d_Klo);
+  c->k_split = false;
   engine_free(c);
   c->have_grm = false;
   const int64_t np = round_up(c->nn, kRowTile);
@@ -564,6 +583,25 @@ extern "C" int sg_grm_build(sg_ctx* c, int precision) {
   return SG_OK;
 }
 
+// Split K = Khi + Klo in place for the split-TF32 engine, or recombine it (exactly) for the others.
+static int ensure_k_split(sg_ctx* c, bool want) {
+  if (!c->have_grm || want == c->k_split) return SG_OK;
+  const int64_t n2 = c->np * c->np;
+  if (want) {
+    SG_TRY(dev_alloc_t(c, &c->d_Klo, (size_t)n2));
+    launch_split_tf32(c->d_K, c->d_K, c->d_Klo, n2, c->stream);
+    SG_LAUNCHED(c, 1);
+    c->k_split = true;
+  } else {
+    add_inplace_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(c->d_K, c->d_Klo, n2);
+    SG_LAUNCHED(c, 1);
+    SG_TRY(sync(c));
+    dev_free_t(c, c->d_Klo);
+    c->k_split = false;
+  }
+  return sync(c);
+}
+
 extern "C" int sg_grm_diag(sg_ctx* c, double* out) {
   NEED_GENO(c);
   std::copy(c->diag.begin(), c->diag.end(), out);
@@ -577,6 +615,11 @@ extern "C" int sg_grm_diag_f32(sg_ctx* c, float* out) {
 extern "C" int sg_grm_get(sg_ctx* c, float* out) {
   NEED_GRM(c);
   SG_CUDA(c, cudaMemcpy2D(out, c->nn * 4, c->d_K, c->np * 4, c->nn * 4, c->nn, cudaMemcpyDeviceToHost));
+  if (c->k_split) {
+    std::vector<float> lo((size_t)(c->nn * c->nn));
+    SG_CUDA(c, cudaMemcpy2D(lo.data(), c->nn * 4, c->d_Klo, c->np * 4, c->nn * 4, c->nn, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < lo.size(); ++i) out[i] += lo[i];
+  }
   return SG_OK;
 }
 
@@ -586,9 +629,10 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.X); dev_free_t(c, e.R); dev_free_t(c, e.Z); dev_free_t(c, e.P);
   dev_free_t(c, e.B); dev_free_t(c, e.part); dev_free_t(c, e.winv); dev_free_t(c, e.minv);
   dev_free_t(c, e.Yd); dev_free_t(c, e.Pf); dev_free_t(c, e.Yf); dev_free_t(c, e.d_st);
-  dev_free_t(c, e.d_ph); dev_free_t(c, e.d_cols);
+  dev_free_t(c, e.d_ph); dev_free_t(c, e.d_cols); dev_free_t(c, e.Pflo);
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
+  e.finished.clear();
   e.hi_col = 0;
   e.n_active = 0;
   e.queue.clear();
@@ -654,6 +698,8 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   SG_CUDA(c, cudaMemsetAsync(e.minv, 0, (size_t)(max_phenos * np) * 8, c->stream));
   e.cap_cols = max_columns;
   e.cap_ph = max_phenos;
+  for (auto& ev : e.ev)
+    if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
   e.h_st.assign(max_columns, ColState{});
   for (auto& s : e.h_st) { s.kind = -1; s.active = 0; }
   SG_CUDA(c, cudaMemcpyAsync(e.d_st, e.h_st.data(), max_columns * sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
@@ -821,8 +867,16 @@ static int engine_gemm(sg_ctx* c, int64_t ncols, bool* used_yf) {
     }
     return SG_OK;
   }
-  if (c->mv_mode == SG_MV_TF32_TC) {
-    cudaError_t err = tc_gemm_tf32(c->d_K, e.np, e.Pf, ncols, e.Yf, c->stream);
+  if (c->mv_mode == SG_MV_TF32_TC || c->mv_mode == SG_MV_TF32X3_TC) {
+    const bool split = c->mv_mode == SG_MV_TF32X3_TC;
+    if (split) {
+      if (!c->k_split) SG_TRY(ensure_k_split(c, true));
+      if (!e.Pflo) SG_TRY(dev_alloc_t(c, &e.Pflo, (size_t)(e.cap_cols * e.np)));
+      launch_split_tf32(e.Pf, e.Pf, e.Pflo, ncols * e.np, c->stream);
+      c->launches += 1;
+    }
+    cudaError_t err = tc_gemm_tf32(c->d_K, split ? c->d_Klo : nullptr, e.np, e.Pf,
+                                   split ? e.Pflo : nullptr, ncols, e.Yf, c->stream);
     if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 GRM.V: %s", cudaGetErrorString(err));
     c->launches += 1;
     return SG_OK;
@@ -836,8 +890,12 @@ static int engine_gemm(sg_ctx* c, int64_t ncols, bool* used_yf) {
 static int engine_step(sg_ctx* c, int64_t* n_finished) {
   Engine& e = c->eng;
   const int64_t ncols = round_up(e.hi_col, 32);
+  int64_t occupied = 0;
+  for (int64_t col = 0; col < e.hi_col; ++col) occupied += e.col_req[col] >= 0 ? 1 : 0;
   bool yf = true;
+  SG_CUDA(c, cudaEventRecord(e.ev[0], c->stream));
   SG_TRY(engine_gemm(c, ncols, &yf));
+  SG_CUDA(c, cudaEventRecord(e.ev[1], c->stream));
   const float* Yf = yf ? e.Yf : nullptr;
   const double* Yd = yf ? nullptr : e.Yd;
   launch_pcg_sigma_dot(e.np, e.hi_col, e.d_st, e.d_ph, e.winv, e.minv, e.P, Yf, Yd, e.part, e.nblk, c->stream);
@@ -847,8 +905,21 @@ static int engine_step(sg_ctx* c, int64_t* n_finished) {
   launch_pcg_beta(e.hi_col, e.d_st, e.part, e.nblk, c->stream);
   launch_pcg_dir(e.np, e.hi_col, e.d_st, e.Z, e.P, e.Pf, c->stream);
   SG_LAUNCHED(c, 5);
+  SG_CUDA(c, cudaEventRecord(e.ev[2], c->stream));
   SG_CUDA(c, cudaMemcpyAsync(e.h_st.data(), e.d_st, e.hi_col * sizeof(ColState), cudaMemcpyDeviceToHost, c->stream));
   SG_TRY(sync(c));
+  {
+    float ms_gemm = 0.f, ms_step = 0.f;
+    cudaEventElapsedTime(&ms_gemm, e.ev[0], e.ev[1]);
+    cudaEventElapsedTime(&ms_step, e.ev[0], e.ev[2]);
+    e.t_gemm_ms += ms_gemm;
+    e.t_step_ms += ms_step;
+    const int64_t launched_cols = c->mv_mode == SG_MV_FP64_PLAIN ? occupied : ncols;
+    e.gemm_launches += c->mv_mode == SG_MV_FP64_PLAIN ? (double)occupied : 1.0;
+    e.gemm_cols += (double)launched_cols;
+    e.useful_cols += (double)occupied;
+    e.gemm_flops += 2.0 * (double)c->nn * (double)c->nn * (double)launched_cols;
+  }
   e.steps += 1;
   e.grm_passes += 1;
   int64_t fin = 0;
@@ -866,6 +937,7 @@ static int engine_step(sg_ctx* c, int64_t* n_finished) {
       r.iters = s.kind == 1 ? 1 : s.iter;
       r.state = 2;
       r.col = -1;
+      e.finished.push_back(id);
     }
     e.col_req[col] = -1;
     s.kind = -1;
@@ -899,6 +971,7 @@ static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
       it->second.iters = 0;
       it->second.state = 2;
       it->second.col = -1;
+      e.finished.push_back(id);
     }
     e.col_req[col] = -1;
     s.kind = -1;
@@ -960,6 +1033,35 @@ extern "C" int sg_engine_cancel(sg_ctx* c, int64_t id) {
     SG_TRY(sync(c));
   }
   e.reqs.erase(it);  // a queued id is skipped at admission
+  return SG_OK;
+}
+
+extern "C" int sg_engine_poll(sg_ctx* c, int64_t* ids, int64_t max_ids, int64_t* n_out) {
+  if (!c || !n_out || (max_ids > 0 && !ids)) return SG_ERR_INVALID;
+  Engine& e = c->eng;
+  const int64_t k = std::min<int64_t>(max_ids, (int64_t)e.finished.size());
+  for (int64_t i = 0; i < k; ++i) ids[i] = e.finished[i];
+  e.finished.erase(e.finished.begin(), e.finished.begin() + k);
+  *n_out = k;
+  return SG_OK;
+}
+
+extern "C" int sg_engine_timing(sg_ctx* c, double* t) {
+  if (!c || !t) return SG_ERR_INVALID;
+  const Engine& e = c->eng;
+  t[0] = e.t_step_ms;
+  t[1] = e.t_gemm_ms;
+  t[2] = e.gemm_launches;
+  t[3] = e.gemm_flops;
+  t[4] = e.gemm_cols;
+  t[5] = e.useful_cols;
+  return SG_OK;
+}
+
+extern "C" int sg_engine_reset_timing(sg_ctx* c) {
+  if (!c) return SG_ERR_INVALID;
+  Engine& e = c->eng;
+  e.t_step_ms = e.t_gemm_ms = e.gemm_launches = e.gemm_flops = e.gemm_cols = e.useful_cols = 0;
   return SG_OK;
 }
 

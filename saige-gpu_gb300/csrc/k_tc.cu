@@ -372,6 +372,26 @@ cudaError_t check_error_flag(cudaStream_t s) {
 
 }  // namespace
 
+__global__ void split_tf32_kernel(const float* __restrict__ x, float* __restrict__ hi,
+                                  float* __restrict__ lo, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float v = x[i];
+  // round to nearest at bit 13 (ties away from zero in magnitude), keep 10 explicit mantissa bits
+  const uint32_t u = __float_as_uint(v);
+  const float h = isfinite(v) ? __uint_as_float((u + 0x1000u) & 0xFFFFE000u) : v;
+  // v - h is exact in FP32: |v - h| <= 2^-11 |v| and both share v's exponent range
+  hi[i] = h;
+  lo[i] = isfinite(v) ? v - h : 0.0f;
+}
+
+
+void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s) {
+  if (n == 0) return;
+  split_tf32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, hi, lo, n);
+}
+
+
 bool tc_available() {
   int dev = 0, major = 0, minor = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
@@ -413,13 +433,19 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
   return check_error_flag(s);
 }
 
-cudaError_t tc_gemm_tf32(const float* K, int64_t np, const float* P, int64_t ncols, float* Y,
-                         cudaStream_t s) {
+cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
+                         const float* Plo, int64_t ncols, float* Y, cudaStream_t s) {
   if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0) return cudaErrorInvalidValue;
-  const int BN = ncols % 128 == 0 ? 128 : (ncols % 64 == 0 ? 64 : 32);
-  CUtensorMap a, b;
+  const bool split = Klo != nullptr && Plo != nullptr;
+  const int BN = split ? (ncols % 64 == 0 ? 64 : 32) : (ncols % 128 == 0 ? 128 : (ncols % 64 == 0 ? 64 : 32));
+  CUtensorMap a, b, a2, b2;
   if (!make_map(&a, K, true, np, np, (uint64_t)np * 4, kTileM) ||
       !make_map(&b, P, true, np, ncols, (uint64_t)np * 4, BN))
+    return cudaErrorInvalidValue;
+  a2 = a;
+  b2 = b;
+  if (split && (!make_map(&a2, Klo, true, np, np, (uint64_t)np * 4, kTileM) ||
+                !make_map(&b2, Plo, true, np, ncols, (uint64_t)np * 4, BN)))
     return cudaErrorInvalidValue;
   static TileCache cache;
   cache.host.clear();
@@ -428,7 +454,11 @@ cudaError_t tc_gemm_tf32(const float* K, int64_t np, const float* P, int64_t nco
   cudaError_t e = upload_tiles(cache, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(np / 32);
-  if (BN == 128)
+  if (split && BN == 64)
+    e = launch<true, 64, 4, true>(a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
+  else if (split)
+    e = launch<true, 32, 5, true>(a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
+  else if (BN == 128)
     e = launch<true, 128, 4, false>(a, b, a, b, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
   else if (BN == 64)
     e = launch<true, 64, 6, false>(a, b, a, b, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);

@@ -75,9 +75,12 @@ bool tc_available();
 // Zlo != nullptr (Z = Zhi + Zlo split) it accumulates Zhi Zhi^T + Zhi Zlo^T + Zlo Zhi^T.
 cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t mp, float* K,
                          float scale, cudaStream_t s);
-// Y^T (ncols x np) = K (np x np fp32, tf32 MMA) * P^T with P (ncols x np fp32)
-cudaError_t tc_gemm_tf32(const float* K, int64_t np, const float* P, int64_t ncols, float* Y,
-                         cudaStream_t s);
+// Y^T (ncols x np) = K (np x np fp32, tf32 MMA) * P^T with P (ncols x np fp32).  With Klo and
+// Plo (split operands) it accumulates K P + K Plo + Klo P (3xTF32).
+cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
+                         const float* Plo, int64_t ncols, float* Y, cudaStream_t s);
+// x = hi + lo with hi rounded to TF32 (low 13 mantissa bits zero) and lo = x - hi (exact)
+void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
 
 // ---- PCG engine kernels (k_pcg.cu)
 struct ColState {

@@ -12,7 +12,7 @@ import numpy as np
 from . import _lib as L
 
 GRM_FP32_SIMT, GRM_BF16_TC, GRM_BF16X3_TC = 0, 1, 2
-MV_FP32_SIMT, MV_TF32_TC, MV_FP64_PLAIN = 0, 1, 2
+MV_FP32_SIMT, MV_TF32_TC, MV_FP64_PLAIN, MV_TF32X3_TC = 0, 1, 2, 3
 
 
 def _f32(a):
@@ -376,6 +376,21 @@ class Context:
 
     def engine_cancel(self, rid):
         self._call("sg_engine_cancel", int(rid))
+
+    def engine_poll(self, max_ids=1 << 16):
+        ids = np.empty(max_ids, np.int64)
+        n = C.c_int64()
+        self._call("sg_engine_poll", _ptr(ids, L.P_i64), int(max_ids), C.byref(n))
+        return ids[:n.value]
+
+    def engine_timing(self):
+        t = np.zeros(6, np.float64)
+        self._call("sg_engine_timing", _ptr(t, L.P_f64))
+        return dict(step_ms=t[0], gemm_ms=t[1], gemm_launches=int(t[2]), gemm_flops=t[3],
+                    gemm_cols=t[4], useful_cols=t[5])
+
+    def engine_reset_timing(self):
+        self._call("sg_engine_reset_timing")
 
     def engine_stats(self):
         s = np.zeros(4, np.int64)
