@@ -1,0 +1,403 @@
+"""Benchmark: null-model fits/hr at N=100k on a resident GRM (batched mixed precision).
+
+Workload (BASELINE config "batching form", with the "precision form"'s cohort):
+N = 100,000 samples x M = 150,000 markers synthetic cohort (p ~ U(0.01,0.5),
+HWE genotypes, 2% missing; seed 1003), GRM built once on the GPU (decode ->
+BF16 standardised genotypes -> tcgen05 SYRK, FP32 K resident in HBM).  One
+step = one batch of P null-model fits run to convergence through the batched
+engine: half binary (prevalence U(0.05,0.3)), half quantitative (h2
+U(0.1,0.6)), each with a sample mask dropping U(5%,40%) of the cohort, 2
+covariates, y + 30 Rademacher probes per trace, split-TF32 tcgen05 GRM.V with
+FP64 PCG recurrences.
+
+value  = fits/hr over the device-busy time of the engine steps (CUDA events on
+         the engine stream), i.e. with the inputs resident in HBM;
+e2e    = fits/hr by wall clock through the C ABI with host buffers (phenotype
+         vectors H2D, solutions D2H every step);
+roofline: the dominant kernel (the tcgen05 GRM.V) -- algorithmic bytes per
+         pass over the split GRM (8 B per stored element + 12 B per RHS entry)
+         or its tensor FLOPs, whichever bounds it, over its event-timed duration;
+cpu_baseline: the reference's CPU GRM.x (oracle/cpu_ref.c, OpenMP, all host
+         cores) timed on a bounded sample, extrapolated to fits/hr with the
+         measured PCG iterations per fit;
+plain: the plain FP64 single-RHS PCG path on the same GPU, timed per iteration
+         and extrapolated the same way.
+
+``--impl reference`` times the reference's CPU path (the oracle's C
+restatement) on the host cores only.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "saige-gpu_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "null-model fits/hr at N=100k (batched mixed-prec vs plain FP64 PCG); p50/p99"
+COUNTS_FILE = os.path.join(ROOT, "profiles", "bench_counts.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=100_000)
+    ap.add_argument("--m", type=int, default=150_000)
+    ap.add_argument("--phenos", type=int, default=16)
+    ap.add_argument("--miss", type=float, default=0.02)
+    ap.add_argument("--seed", type=int, default=1003)
+    ap.add_argument("--mode", default="tf32x3", choices=["tf32x3", "tf32", "fp32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--json-out", default=None)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ distributed plumbing (replicas)
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ clocks sampler
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if len(r) > 5 + k and r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------------ workload
+def make_specs(ctx, args, rng_seed):
+    """P phenotypes over the cohort: half binary, half quantitative, sample masks 5-40% dropped."""
+    from saigegpu import prep, serve, synth
+    n = ctx.n
+    rng = np.random.default_rng(rng_seed)
+    gvs = [ctx.synth_genetic_value(args.seed * 7 + k) for k in range(2)]
+    specs = []
+    for k in range(args.phenos):
+        trait = "binary" if k % 2 == 0 else "quantitative"
+        gv = gvs[k % 2] * rng.choice([-1, 1]) + 0.3 * gvs[(k + 1) % 2]
+        gv = gv / gv.std()
+        drop = rng.uniform(0.05, 0.40)
+        mask = rng.uniform(size=n) > drop
+        S = np.nonzero(mask)[0]
+        y, C = synth.simulate_pheno(gv, args.seed * 100 + k, trait, tau=0.3,
+                                    prevalence=rng.uniform(0.05, 0.3), h2=rng.uniform(0.1, 0.6))
+        f0 = prep.make_fit0(y[S], C[S], trait, True)
+        specs.append(serve.FitSpec(f0, trait, mask=mask, name="pheno%d" % k))
+    return specs
+
+
+def run_batch(ctx, specs, cols):
+    from saigegpu import serve
+    t0 = time.perf_counter()
+    res, jobs = serve.fit_batch(ctx, specs, max_columns=cols)
+    wall = time.perf_counter() - t0
+    errs = [r for r in res if isinstance(r, Exception)]
+    if errs:
+        raise errs[0]
+    return res, jobs, wall
+
+
+def grm_roofline(ctx, peaks, t_dev, n, np_):
+    """Roofline of the dominant kernel (GRM.V) from the engine's own CUDA-event timing."""
+    launches = max(1, t_dev["gemm_launches"])
+    ms = t_dev["gemm_ms"] / launches
+    cols = t_dev["gemm_cols"] / launches
+    split = True
+    sk = 8.0 if split else 4.0
+    bytes_alg = sk * n * n + 12.0 * n * cols
+    flops_tensor = (3.0 if split else 1.0) * 2.0 * n * n * cols
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tf32_peak = peaks.get("bf16_tflops", 1900.0) / 2.0
+    a_bw = bytes_alg / (ms * 1e-3) / 1e9
+    a_tc = flops_tensor / (ms * 1e-3) / 1e12
+    if a_bw / hbm >= a_tc / tf32_peak:
+        return {"bound": "hbm", "achieved": round(a_bw, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(a_bw / hbm, 4), "traffic": None, "kernel": "tc_gemm_kernel<tf32,split>",
+                "per_launch_ms": round(ms, 3), "columns_per_launch": round(cols, 1),
+                "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)"}
+    return {"bound": "tensor", "achieved": round(a_tc, 1), "peak": tf32_peak, "unit": "TFLOP/s",
+            "frac": round(a_tc / tf32_peak, 4), "traffic": None, "kernel": "tc_gemm_kernel<tf32,split>",
+            "per_launch_ms": round(ms, 3), "columns_per_launch": round(cols, 1),
+            "peak_source": "TF32 = half the measured bf16_tflops (MEASURED_PEAKS.json)"}
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def cpu_baseline(ctx, iters_per_fit, budget_s=25.0):
+    """Reference CPU GRM.x (oracle C restatement, all host cores) on the resident cohort."""
+    from oracle import cpu_ref
+    d = ctx.dims()
+    packed = ctx.packed_geno()
+    freq, inv = ctx.allele_freq(), ctx.invstd()
+    p2 = (np.float32(2) * freq).astype(np.float32)
+    lut = np.zeros((len(freq), 4), np.float32)
+    for g in range(3):
+        lut[:, g] = ((np.float32(g) - p2).astype(np.float32) * inv).astype(np.float32)
+    pg = cpu_ref.PackedGeno(packed, lut, d["n"])
+    b = np.random.default_rng(0).standard_normal(d["n"]).astype(np.float32)
+    times = []
+    t_start = time.perf_counter()
+    while not times or (time.perf_counter() - t_start < budget_s and len(times) < 3):
+        t = time.perf_counter()
+        pg.crossprod(b)
+        times.append(time.perf_counter() - t)
+    tm = min(times)
+    return {"value": round(3600.0 / (tm * iters_per_fit), 6), "unit": "fits/hr", "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": "%d GRM.x products (parallelCrossProdOpenMP restated in C, N=%d, M=%d), %.2f s each; "
+                      "fits/hr extrapolated with %.0f GRM.x per fit measured on the GPU path" %
+                      (len(times), d["n"], d["m_qc"], tm, iters_per_fit)}
+
+
+def plain_fp64(ctx, iters_per_fit):
+    """Plain FP64 single-RHS PCG on the same GPU: event-timed per-iteration cost, extrapolated."""
+    from saigegpu import MV_FP64_PLAIN
+    n = ctx.n
+    ctx.set_matvec_mode(MV_FP64_PLAIN)
+    rng = np.random.default_rng(1)
+    w = rng.uniform(0.05, 0.25, n)
+    b = rng.standard_normal(n)
+    ctx.pcg_solve(w, np.array([1.0, 0.3]), b, 2, 1e-30)  # warm-up
+    ctx.engine_reset_timing()
+    t0 = time.perf_counter()
+    _, it = ctx.pcg_solve(w, np.array([1.0, 0.3]), b, 8, 1e-30)
+    wall = time.perf_counter() - t0
+    t = ctx.engine_timing()
+    per_iter = t["step_ms"] / max(1, it) / 1e3
+    return {"fits_per_hr": round(3600.0 / (per_iter * iters_per_fit), 3), "ms_per_iteration": round(per_iter * 1e3, 3),
+            "wall_ms_per_iteration": round(wall / max(1, it) * 1e3, 3),
+            "basis": "FP64 GEMV over the FP32 GRM, one RHS per solve; %.0f PCG iterations per fit" % iters_per_fit}
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    from saigegpu import Context, GRM_BF16_TC, MV_TF32X3_TC, MV_TF32_TC, MV_FP32_SIMT
+    peaks = load_peaks()
+    ctx = Context(local)
+    t_setup = time.perf_counter()
+    ptr, ln = ctx.synth_bed(args.seed + rank, args.n, args.m, args.miss)
+    ctx.setgeno_device(ptr, ln, args.n, args.m)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.grm_build(GRM_BF16_TC)
+    grm_s = time.perf_counter() - t0
+    d = ctx.dims()
+    syrk_flops = float(d["n"]) * (d["n"] + 1) * d["m_qc"]
+    specs = make_specs(ctx, args, args.seed + 17 * rank)
+    mode = {"tf32x3": MV_TF32X3_TC, "tf32": MV_TF32_TC, "fp32": MV_FP32_SIMT}[args.mode]
+    ctx.set_matvec_mode(mode)
+    cols = min(4096, max(256, 64 * args.phenos))
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(args.warmup):
+        run_batch(ctx, specs, cols)
+    L0 = ctx.kernel_launches()
+    ctx.engine_reset_timing()
+    barrier(world)
+    torch.cuda.synchronize()
+    walls, jobs_all, res_all = [], [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            res, jobs, wall = run_batch(ctx, specs, cols)
+            walls.append(wall)
+            jobs_all += jobs
+            res_all += res
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = ctx.kernel_launches() - L0
+    tdev = ctx.engine_timing()
+    dev_s = tdev["step_ms"] / 1e3
+    total_wall = sum(walls)
+    fits = args.phenos * args.steps
+    wall_max = allmax(total_wall, world)
+    dev_max = allmax(dev_s, world)
+    fits_all = allsum(fits, world)
+    value = fits_all / dev_max * 3600.0
+    e2e = fits_all / wall_max * 3600.0
+    lat = sorted(j.t_done - j.t_start for j in jobs_all)
+    col_iters = float(np.mean([j.column_iterations for j in jobs_all]))
+    n_bytes = 8 * args.n
+    # bytes moved per step: RHS uploads (Y, X, K.PY, P A PY), W/tau rows, solutions back
+    cols_per_fit = float(np.mean([j.columns for j in jobs_all]))
+    h2d = int(args.phenos * (cols_per_fit * 0.1 * n_bytes + 2 * n_bytes * 12))
+    d2h = int(args.phenos * cols_per_fit * n_bytes)
+    roof = grm_roofline(ctx, peaks, tdev, d["n"], ctx.n)
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": "fits/hr", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_wall / args.steps * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32-tf32x3/fp64",
+        "data": "synthetic (seeded cohort generator; the reference's 150k x 100k synthetic AFR set is external)",
+        "config": {"workload": "batched null-model fits on a resident GRM", "n_samples": d["n"],
+                   "m_markers_qc": d["m_qc"], "m_markers": args.m, "missing": args.miss,
+                   "phenotypes_per_step": args.phenos, "traits": "half binary / half quantitative",
+                   "sample_masks": "drop U(5%,40%)", "probes": 30, "grm": "BF16 tcgen05 SYRK, FP32 K",
+                   "grm_v": args.mode, "l2": "inputs larger than L2 (GRM %.0f GB)" % (4.0 * ctx.n ** 2 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "value_basis": "device-busy time of engine steps (CUDA events)"},
+        "e2e": {"value": round(e2e, 2), "unit": "fits/hr", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "latency_s": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3)},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "grm_build": {"seconds": round(grm_s, 3), "syrk_flops": syrk_flops,
+                      "tflops_incl_decode": round(syrk_flops / grm_s / 1e12, 1)},
+        "per_fit": {"pcg_column_iterations": round(col_iters, 1), "columns": round(cols_per_fit, 1),
+                    "converged": int(sum(1 for r in res_all if r["converged"])), "fits": len(res_all)},
+        "setup_s": round(setup_s, 1),
+    }
+    out["clocks"] = clk.summary()
+    if rank == 0:
+        out["plain_fp64_single_rhs"] = plain_fp64(ctx, col_iters)
+        out["speedup_vs_plain_fp64"] = round(value / out["plain_fp64_single_rhs"]["fits_per_hr"], 1)
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(ctx, col_iters)
+        try:
+            os.makedirs(os.path.dirname(COUNTS_FILE), exist_ok=True)
+            if args.n == 100_000 and args.m == 150_000:
+                json.dump({"n": args.n, "m": args.m, "pcg_column_iterations_per_fit": col_iters},
+                          open(COUNTS_FILE, "w"))
+        except Exception:
+            pass
+    ctx.close()
+    return out
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path (oracle C restatement of parallelCrossProdOpenMP + PCG) on host cores."""
+    if rank != 0:
+        return None
+    from oracle import cpu_ref
+    try:
+        iters = json.load(open(COUNTS_FILE))["pcg_column_iterations_per_fit"]
+        basis = "PCG iterations per fit measured by the GPU path (profiles/bench_counts.json)"
+    except Exception:
+        iters = 2000.0
+        basis = "assumed 2000 PCG iterations per fit (no GPU measurement available)"
+    t0 = time.perf_counter()
+    pg = cpu_ref.PackedGeno.synthetic(args.seed, args.n, args.m, args.miss)
+    setup = time.perf_counter() - t0
+    b = np.random.default_rng(0).standard_normal(args.n).astype(np.float32)
+    for _ in range(args.warmup):
+        pg.crossprod(b)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        pg.crossprod(b)
+        times.append(time.perf_counter() - t)
+    per = float(np.mean(times))
+    value = 3600.0 / (per * iters)
+    return {
+        "metric": METRIC, "value": round(value, 6), "unit": "fits/hr", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(per * 1e3, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (same cohort recipe, generated on the host)",
+        "config": {"workload": "batched null-model fits on a resident GRM", "n_samples": args.n,
+                   "m_markers_qc": pg.m, "step": "one GRM.x product of the reference's CPU path"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 6), "unit": "fits/hr", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "one GRM.x per step (oracle/cpu_ref.c restating FIT.cpp:1576-1598), "
+                                   "%.2f s each; %s; setup %.0f s" % (per, basis, setup)},
+        "e2e": {"value": round(value, 6), "unit": "fits/hr", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_init(args)
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world, local)
+    if rank == 0 and out is not None:
+        line = json.dumps(out)
+        print(line, flush=True)
+        if args.json_out:
+            with open(args.json_out, "w") as f:
+                f.write(line + "\n")
+
+
+if __name__ == "__main__":
+    main()

@@ -16,6 +16,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <math.h>
 #include <omp.h>
 
 static inline int field_geno(unsigned f) { return 2 - (int)((f & 1u) + (f >> 1)); }
@@ -103,4 +104,76 @@ int cpuref_pcg(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t 
   }
   free(r); free(z); free(p); free(ap); free(kp); free(minv);
   return iter;
+}
+
+/* Same counter hash and synthetic-cohort recipe as the GPU generator (saigegpu/synth.py),
+ * followed by the reference's setgeno for the identity sample order (QC, integer fill,
+ * float frequency and 1/sd, re-pack; FIT.cpp:326-579, 739-1024).  Writes the re-packed
+ * GRM markers (pitch bytes per marker) and their LUTs; returns the number of GRM markers. */
+static inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static inline uint64_t hash3(uint64_t seed, uint64_t stream, uint64_t idx) {
+  uint64_t h = mix64(seed ^ 0x5851F42D4C957F2Dull);
+  h = mix64(h ^ (stream * 0x9E3779B97F4A7C15ull));
+  return mix64(h ^ (idx * 0xD1B54A32D192ED03ull));
+}
+
+int64_t cpuref_synth_setgeno(uint64_t seed, int64_t n, int64_t m, double miss_rate, float min_maf,
+                             float max_miss, uint8_t* packed, int64_t pitch, float* lut4,
+                             int nthreads) {
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  const uint32_t miss_thr = (uint32_t)(miss_rate * 65536.0 + 0.5);
+  int8_t* pass = (int8_t*)calloc((size_t)m, 1);
+  float* lut_all = (float*)malloc((size_t)m * 4 * sizeof(float));
+  uint8_t* rows = (uint8_t*)malloc((size_t)m * (size_t)pitch);
+#pragma omp parallel
+  {
+    uint8_t* g = (uint8_t*)malloc((size_t)n);
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t j = 0; j < m; ++j) {
+      const uint64_t hm = hash3(seed, 1ull, (uint64_t)j);
+      const uint32_t thr = 167772u + (uint32_t)(((hm >> 40) * 8220835ull) >> 24);
+      int allele = 0, nmiss = 0;
+      for (int64_t i = 0; i < n; ++i) {
+        const uint64_t h = hash3(seed, 16ull + (uint64_t)j, (uint64_t)i);
+        if ((uint32_t)(h & 0xFFFFu) < miss_thr) { g[i] = 3; ++nmiss; continue; }
+        g[i] = (uint8_t)(((uint32_t)(h >> 40) < thr) + ((uint32_t)((h >> 16) & 0xFFFFFFu) < thr));
+        allele += g[i];
+      }
+      const float alt0 = (float)allele / (float)((n - nmiss) * 2);
+      const int fill = (alt0 == alt0) ? (int)floor((double)(2.0f * alt0) + 0.5) : 0;
+      if (nmiss > 0) allele += fill * nmiss;
+      const float alt = (float)allele / (float)(n * 2);
+      const float maf = alt < 1.0f - alt ? alt : 1.0f - alt;
+      const float mrate = (float)nmiss / (float)n;
+      pass[j] = (maf >= min_maf && mrate <= max_miss) ? 1 : 0;
+      const float sd = sqrtf(2.0f * alt * (1.0f - alt));
+      const float inv = sd == 0.0f ? 0.0f : 1.0f / sd;
+      const float p2 = 2.0f * alt;
+      lut_all[4 * j + 0] = (0.0f - p2) * inv;
+      lut_all[4 * j + 1] = (1.0f - p2) * inv;
+      lut_all[4 * j + 2] = (2.0f - p2) * inv;
+      lut_all[4 * j + 3] = 0.0f;
+      uint8_t* row = rows + (size_t)j * pitch;
+      memset(row, 0, (size_t)pitch);
+      for (int64_t i = 0; i < n; ++i) {
+        int gi = g[i] == 3 ? fill : g[i];
+        const unsigned code = gi == 0 ? 3u : (gi == 1 ? 2u : 0u);
+        row[i >> 2] |= (uint8_t)(code << (2 * (i & 3)));
+      }
+    }
+    free(g);
+  }
+  int64_t k = 0;
+  for (int64_t j = 0; j < m; ++j) {
+    if (!pass[j]) continue;
+    memcpy(packed + (size_t)k * pitch, rows + (size_t)j * pitch, (size_t)pitch);
+    memcpy(lut4 + 4 * k, lut_all + 4 * j, 4 * sizeof(float));
+    ++k;
+  }
+  free(rows); free(lut_all); free(pass);
+  return k;
 }

@@ -33,7 +33,36 @@ def load():
         _lib.cpuref_pcg.argtypes = [P, C.c_int64, P, C.c_int64, C.c_int64, P, P, P, P, C.c_int,
                                     C.c_float, P, C.c_int]
         _lib.cpuref_pcg.restype = C.c_int
+        _lib.cpuref_synth_setgeno.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_double, C.c_float,
+                                              C.c_float, P, C.c_int64, P, C.c_int]
+        _lib.cpuref_synth_setgeno.restype = C.c_int64
     return _lib
+
+
+class PackedGeno:
+    """Host copy of re-packed GRM genotypes + LUT (the reference's genoClass layout)."""
+
+    def __init__(self, packed, lut4, n):
+        self.packed = np.ascontiguousarray(packed, np.uint8)
+        self.m, self.pitch = self.packed.shape
+        self.lut = np.ascontiguousarray(lut4, np.float32).reshape(self.m, 4)
+        self.n = n
+
+    @classmethod
+    def synthetic(cls, seed, n, m, miss_rate, min_maf=0.01, max_miss=0.15, nthreads=0):
+        pitch = (n + 3) // 4
+        packed = np.empty((m, pitch), np.uint8)
+        lut = np.empty((m, 4), np.float32)
+        k = load().cpuref_synth_setgeno(seed, n, m, miss_rate, min_maf, max_miss, packed.ctypes.data,
+                                        pitch, lut.ctypes.data, nthreads)
+        return cls(packed[:k], lut[:k], n)
+
+    def crossprod(self, b, nthreads=0):
+        b = np.ascontiguousarray(b, np.float32)
+        out = np.empty(self.n, np.float32)
+        load().cpuref_crossprod(self.packed.ctypes.data, self.pitch, self.lut.ctypes.data, self.m,
+                                self.n, b.ctypes.data, out.ctypes.data, nthreads)
+        return out
 
 
 class CpuGeno:

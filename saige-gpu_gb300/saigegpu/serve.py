@@ -1,0 +1,425 @@
+"""Batched and served null-model fits on one resident GRM.
+
+Each fit is a generator that follows the reference's algorithm step by step
+(``Get_Coef`` FIT.R:2-35, ``glmmkin.ai_PCG_Rcpp_Binary`` FIT.R:79-304,
+``glmmkin.ai_PCG_Rcpp_Quantitative`` FIT.R:309-549 with ``getCoefficients``
+FIT.cpp:3167-3199, ``getAIScore``/``_q`` FIT.cpp:3279-3295 / 3479-3531,
+``GetTrace``/``_q`` FIT.cpp:3113-3160 / 3409-3472 and the tau updates of
+``fitglmmaiRPCG``/``_q`` FIT.cpp:3302-3341 / 3610-3662), all in FP64 on the
+host, and *yields* its right-hand sides instead of solving them:
+
+    ("pheno", W, tau)                       set this fit's phenotype slot
+    ("submit", kind, B | None, probes, maxiter, tol) -> request ids
+    ("wait", ids)                           -> the solutions (n-vectors)
+
+``Runner`` multiplexes any number of such fits onto the engine of one
+``Context``: every engine step advances every in-flight column of every fit by
+one PCG iteration (one pass over the GRM), columns retire on their own
+stopping rule, and freed slots are refilled at the next step.  Within a fit
+the batching follows the data dependencies: Y and the X columns are one block,
+the 30 (+10) Hutchinson probes go with K.PY, and the P A PY solve starts as
+soon as K.PY is back.  A column's arithmetic does not depend on its
+neighbours, so a fit gives the same result alone or in a mix.
+
+Sample subsets: a fit may use a mask over the cohort's samples; its vectors are
+zero outside the subset and the engine solves with Sigma[S, S] built from the
+cohort GRM restricted to S (the reference instead recomputes allele
+frequencies on each subset, so this is exact only for full-cohort fits).
+"""
+import time
+
+import numpy as np
+
+from .family import family_of
+from .synth import hash3
+
+# ------------------------------------------------------------------ generator helpers
+
+
+def _solve(B, maxiter, tol):
+    ids = yield ("submit", 0, B, None, maxiter, tol)
+    res = yield ("wait", ids)
+    return np.column_stack(res)
+
+
+def _inv_sympd(A):
+    A = np.triu(A) + np.triu(A, 1).T
+    try:
+        L = np.linalg.cholesky(A)
+        Li = np.linalg.inv(L)
+        return Li.T @ Li
+    except np.linalg.LinAlgError:
+        return np.linalg.pinv(A)
+
+
+def _cal_cv(x):
+    x = np.asarray(x, np.float64)
+    return (x.std(ddof=1) / x.mean()) / len(x)
+
+
+class FitSpec:
+    """One null-model fit request.
+
+    fit0: dict from ``prep.make_fit0`` on the subset (y, X, offset,
+    linear_predictors, coefficients, family) with vectors over the subset.
+    mask: bool over the cohort's n samples (None = all).
+    """
+
+    def __init__(self, fit0, trait, mask=None, tol=0.02, maxiter=20, nrun=30, tol_pcg=1e-5,
+                 maxiter_pcg=500, trace_cv_cutoff=0.0025, seed=200, name=None):
+        self.fit0 = fit0
+        self.trait = trait
+        self.mask = None if mask is None else np.asarray(mask, bool)
+        self.tol, self.maxiter, self.nrun = tol, maxiter, nrun
+        self.tol_pcg, self.maxiter_pcg, self.cutoff, self.seed = tol_pcg, maxiter_pcg, trace_cv_cutoff, seed
+        self.name = name
+
+
+class _Probes:
+    """Probe vectors of the counter hash, cached per run index (identical for every fit)."""
+
+    def __init__(self, n):
+        self.n = n
+        self.cache = {}
+
+    def get(self, seed, run):
+        key = (seed, run)
+        if key not in self.cache:
+            h = hash3(seed, run, np.arange(self.n, dtype=np.uint64))
+            self.cache[key] = np.where((h >> np.uint64(63)) == 1, 1.0, -1.0)
+        return self.cache[key]
+
+
+def fit_generator(spec, n_cohort, probes):
+    """AI-REML null fit of one phenotype as a request generator (returns the result dict)."""
+    fam = family_of("binomial" if spec.trait == "binary" else "gaussian")
+    quant = spec.trait != "binary"
+    m = np.ones(n_cohort, bool) if spec.mask is None else spec.mask
+    idx = np.nonzero(m)[0]
+    n = len(idx)
+    f0 = spec.fit0
+
+    def full(v, fill=0.0):
+        out = np.full(n_cohort, fill)
+        out[idx] = v
+        return out
+
+    y = full(f0["y"])
+    X = np.zeros((n_cohort, f0["X"].shape[1]))
+    X[idx] = f0["X"]
+    offset = full(np.zeros(n) if f0.get("offset") is None else f0["offset"])
+    eta = full(f0["linear_predictors"])
+    alpha = np.asarray(f0["coefficients"], np.float64)
+    stats = {"pcg_columns": 0, "column_iterations": 0, "products": 0}
+
+    def working(eta_):
+        mu = fam.linkinv(eta_)
+        mu_eta = fam.mu_eta(eta_)
+        Y = np.where(m, eta_ - offset + (y - mu) / mu_eta, 0.0)
+        W = np.where(m, (mu_eta / np.sqrt(fam.variance(mu))) ** 2, 1.0)
+        return mu, Y, W
+
+    def get_coefficients(Y, W, tau):
+        yield ("pheno", W, tau)
+        S = yield from _solve(np.column_stack([Y, X]), spec.maxiter_pcg, spec.tol_pcg)
+        SY, SX = S[:, 0], S[:, 1:]
+        cov = _inv_sympd(X.T @ SX)
+        al = cov @ (SX.T @ Y)
+        et = np.where(m, Y - tau[0] * (SY - SX @ al) / W, 0.0)
+        return dict(Sigma_iY=SY, Sigma_iX=SX, cov=cov, alpha=al, eta=et)
+
+    def get_coef(tau, alpha0, eta0):
+        mu, Y, W = working(eta0)
+        for _ in range(spec.maxiter):
+            rc = yield from get_coefficients(Y, W, tau)
+            al = rc["alpha"]
+            et = rc["eta"] + offset
+            mu, Y, W = working(et)
+            if np.max(np.abs(al - alpha0) / (np.abs(al) + np.abs(alpha0) + 0.1)) < 0.1:
+                break
+            alpha0 = al
+        return dict(Y=Y, alpha=al, eta=et, W=W, cov=rc["cov"], Sigma_iY=rc["Sigma_iY"],
+                    Sigma_iX=rc["Sigma_iX"], mu=mu)
+
+    def ai_score(rc, tau):
+        Y, W, SY, SX = rc["Y"], rc["W"], rc["Sigma_iY"], rc["Sigma_iX"]
+        yield ("pheno", W, tau)  # getAIScore solves with Get_Coef's updated weights (FIT.R:142, :186)
+        cov = _inv_sympd(X.T @ SX) if quant else rc["cov"]
+        PY = SY - SX @ (cov @ (SX.T @ Y))
+        # K PY rides with the first probe block
+        apy_id = yield ("submit", 1, PY[:, None], None, 1, 0.0)
+        pid = yield ("submit", 0, None, (spec.seed, 0, spec.nrun), spec.maxiter_pcg, spec.tol_pcg)
+        aid = yield ("submit", 1, None, (spec.seed, 0, spec.nrun), 1, 0.0)
+        APY = (yield ("wait", apy_id))[0]
+        rhs = np.column_stack([APY, PY]) if quant else APY[:, None]
+        sid = yield ("submit", 0, rhs, None, spec.maxiter_pcg, spec.tol_pcg)
+        t1, t0 = [], []
+        run0, k = 0, spec.nrun
+        while True:
+            Su = yield ("wait", pid)
+            Au = yield ("wait", aid)
+            U = np.column_stack([probes.get(spec.seed, run0 + j) * m for j in range(k)])
+            SUm = np.column_stack(Su)
+            PU = SUm - SX @ (cov @ (SX.T @ U))
+            t1.extend((np.column_stack(Au) * PU).sum(axis=0))
+            t0.extend((U * PU).sum(axis=0))
+            if _cal_cv(t1) > spec.cutoff or (quant and _cal_cv(t0) > spec.cutoff):
+                run0, k = run0 + k, 10
+                pid = yield ("submit", 0, None, (spec.seed, run0, k), spec.maxiter_pcg, spec.tol_pcg)
+                aid = yield ("submit", 1, None, (spec.seed, run0, k), 1, 0.0)
+                continue
+            break
+        S = np.column_stack((yield ("wait", sid)))
+        PAPY = S[:, 0] - SX @ (cov @ (SX.T @ S[:, 0]))
+        out = dict(YPAPY=float(PY @ APY), Trace=float(np.mean(t1)), PY=PY, nprobe=len(t1))
+        if quant:
+            PA0PY = S[:, 1] - SX @ (cov @ (SX.T @ S[:, 1]))
+            out["YPA0PY"] = float(PY @ PY)
+            out["Trace"] = np.array([np.mean(t0), np.mean(t1)])
+            out["AI"] = np.array([[PY @ PA0PY, PY @ PAPY], [PY @ PAPY, APY @ PAPY]])
+        else:
+            out["AI"] = float(APY @ PAPY)
+        return out
+
+    def tau_step(rc, tau):
+        re = yield from ai_score(rc, tau)
+        tau0 = np.array(tau, np.float64)
+        if not quant:  # fitglmmaiRPCG (FIT.cpp:3302-3341)
+            dtau = (re["YPAPY"] - re["Trace"]) / re["AI"]
+            t = tau0.copy()
+            t[1] = tau0[1] + dtau
+            t[t < spec.tol] = 0.0
+            step = 1.0
+            while t[1] < 0.0:
+                step *= 0.5
+                t[1] = tau0[1] + step * dtau
+            t[t < spec.tol] = 0.0
+            return t
+        zero = tau0 < spec.tol  # fitglmmaiRPCG_q (FIT.cpp:3610-3662)
+        score = np.array([re["YPA0PY"] - re["Trace"][0], re["YPAPY"] - re["Trace"][1]])
+        dtau = np.linalg.solve(re["AI"], score)
+        t = tau0 + dtau
+        t[zero & (t < spec.tol)] = 0.0
+        step = 1.0
+        while t[0] < 0.0 or t[1] < 0.0:
+            step *= 0.5
+            t = tau0 + step * dtau
+            t[zero & (t < spec.tol)] = 0.0
+        t[t < spec.tol] = 0.0
+        return t
+
+    # ---------------- glmmkin.ai_PCG_Rcpp_* main loop
+    alpha0 = alpha
+    eta0 = eta
+    if quant:
+        _, Y0, _ = working(eta)
+        tau = np.array([1.0, 0.0])
+        if abs(np.var(Y0[idx], ddof=1)) < 0.1:
+            raise ValueError("variance of the phenotype is much smaller than 1")
+    else:
+        tau = np.array([1.0, 0.1])
+    tau0 = tau.copy()
+    rc = yield from get_coef(tau, alpha0, eta0)
+    re = yield from ai_score(rc, tau)
+    if quant:
+        tau[1] = max(0.0, tau0[1] + tau0[1] ** 2 * (re["YPAPY"] - re["Trace"][1]) / n)
+        tau[0] = max(0.0, tau0[0] + tau0[0] ** 2 * (re["YPA0PY"] - re["Trace"][0]) / n)
+    else:
+        tau[1] = max(0.0, tau0[1] + tau0[1] ** 2 * (re["YPAPY"] - re["Trace"]) / n)
+    it_used = 0
+    for i in range(1, spec.maxiter + 1):
+        it_used = i
+        alpha0 = rc["alpha"] if not quant else alpha
+        tau0 = tau.copy()
+        eta0 = eta
+        rc = yield from get_coef(tau, alpha0, eta0)
+        tau = yield from tau_step(rc, tau)
+        alpha, eta = rc["alpha"], rc["eta"]
+        if quant and tau[0] <= 0:
+            raise ValueError("the first variance component parameter estimate is 0")
+        if tau[1] <= 0 if quant else tau[1] == 0:
+            break
+        if np.max(np.abs(tau - tau0) / (np.abs(tau) + np.abs(tau0) + spec.tol)) < spec.tol:
+            break
+        if np.max(tau) > spec.tol ** (-2):
+            it_used = spec.maxiter
+            break
+    rc = yield from get_coef(tau, alpha, eta)
+    return dict(theta=tau, coefficients=rc["alpha"], linear_predictors=rc["eta"][idx],
+                fitted_values=rc["mu"][idx], Y=rc["Y"][idx], residuals=(y - rc["mu"])[idx],
+                cov=rc["cov"], converged=it_used < spec.maxiter, iterations=it_used, n=n)
+
+
+# ------------------------------------------------------------------ runner
+
+
+class _Job:
+    def __init__(self, jid, spec, gen, slot, t_arrive):
+        self.jid, self.spec, self.gen, self.slot = jid, spec, gen, slot
+        self.waiting = None
+        self.results = {}
+        self.t_arrive = t_arrive
+        self.t_start = None
+        self.t_done = None
+        self.result = None
+        self.error = None
+        self.column_iterations = 0
+        self.columns = 0
+
+
+class Runner:
+    """Continuous batching of many null-model fits over one engine."""
+
+    def __init__(self, ctx, max_columns=2048, max_phenos=64):
+        self.ctx = ctx
+        self.n = ctx.n
+        ctx.engine_reserve(max_columns, max_phenos)
+        self.max_columns = max_columns
+        self.free_slots = list(range(max_phenos))[::-1]
+        self.jobs = {}
+        self.owner = {}          # request id -> job id
+        self.done = {}           # request id -> (x, iters)
+        self.probes = _Probes(self.n)
+        self.finished = []
+        self._next = 0
+        self.inflight_columns = 0
+
+    # -- admission
+    def can_admit(self, spec):
+        need = 2 * (spec.nrun + 10) + 4
+        return bool(self.free_slots) and self.inflight_columns + need <= self.max_columns * 4
+
+    def submit(self, spec, t_arrive=None):
+        if not self.free_slots:
+            raise RuntimeError("no free phenotype slot")
+        jid = self._next
+        self._next += 1
+        slot = self.free_slots.pop()
+        job = _Job(jid, spec, fit_generator(spec, self.n, self.probes), slot,
+                   time.perf_counter() if t_arrive is None else t_arrive)
+        job.t_start = time.perf_counter()
+        self.jobs[jid] = job
+        self._advance(job, None)
+        return jid
+
+    # -- generator plumbing
+    def _advance(self, job, value):
+        gen = job.gen
+        try:
+            while True:
+                op = gen.send(value)
+                kind = op[0]
+                if kind == "pheno":
+                    _, W, tau = op
+                    self.ctx.engine_set_pheno(job.slot, W, tau, job.spec.mask)
+                    value = None
+                elif kind == "submit":
+                    _, k, B, probe, maxiter, tol = op
+                    if probe is None:
+                        ids = self.ctx.engine_submit(job.slot, k, B, maxiter, tol)
+                    else:
+                        seed, run0, cnt = probe
+                        ids = self.ctx.engine_submit_probes(job.slot, k, seed, run0, cnt, maxiter, tol)
+                    for i in ids:
+                        self.owner[int(i)] = job.jid
+                    job.columns += len(ids)
+                    self.inflight_columns += len(ids)
+                    value = [int(i) for i in ids]
+                elif kind == "wait":
+                    ids = op[1]
+                    if all(i in self.done for i in ids):
+                        value = [self._take(job, i) for i in ids]
+                        continue
+                    job.waiting = ids
+                    return
+                else:
+                    raise RuntimeError("unknown op %r" % (kind,))
+        except StopIteration as st:
+            job.result = st.value
+            self._finish(job)
+        except Exception as ex:  # the fit failed: release its slot, keep the others running
+            job.error = ex
+            self._finish(job)
+
+    def _take(self, job, rid):
+        x, it = self.done.pop(rid)
+        job.column_iterations += it
+        return x
+
+    def _finish(self, job):
+        job.t_done = time.perf_counter()
+        for rid, jid in list(self.owner.items()):
+            if jid == job.jid:
+                try:
+                    self.ctx.engine_cancel(rid)
+                except Exception:
+                    pass
+                self.owner.pop(rid, None)
+                self.done.pop(rid, None)
+        self.free_slots.append(job.slot)
+        del self.jobs[job.jid]
+        self.finished.append(job)
+
+    def step(self):
+        """One engine step; resume every fit whose awaited columns are complete."""
+        self.ctx.engine_run(1)
+        ids = self.ctx.engine_poll()
+        for rid in ids:
+            rid = int(rid)
+            if rid not in self.owner:
+                continue
+            x, it = self.ctx.engine_fetch(rid)
+            self.done[rid] = (x, it)
+            self.inflight_columns -= 1
+        ready = [j for j in self.jobs.values() if j.waiting is not None and all(i in self.done for i in j.waiting)]
+        for job in ready:
+            ids, job.waiting = job.waiting, None
+            vals = [self._take(job, i) for i in ids]
+            for i in ids:
+                self.owner.pop(i, None)
+            self._advance(job, vals)
+        return len(ids)
+
+    def run(self, max_steps=1 << 30):
+        steps = 0
+        while self.jobs and steps < max_steps:
+            self.step()
+            steps += 1
+        return steps
+
+    def cancel(self, jid):
+        job = self.jobs.get(jid)
+        if job is not None:
+            job.error = RuntimeError("cancelled")
+            job.gen.close()
+            self._finish(job)
+
+
+def fit_batch(ctx, specs, max_columns=2048, max_phenos=None):
+    """Fit all ``specs`` together; returns their result dicts (or exceptions) in order."""
+    r = Runner(ctx, max_columns, max_phenos or max(1, len(specs)))
+    ids = [r.submit(s) for s in specs]
+    r.run()
+    by = {j.jid: j for j in r.finished}
+    return [by[i].result if by[i].error is None else by[i].error for i in ids], [by[i] for i in ids]
+
+
+def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter):
+    """Serve a stream of (t_arrival_seconds, FitSpec): admit as slots and columns free up.
+
+    Returns the finished jobs (with t_arrive / t_start / t_done) in completion order.
+    """
+    r = Runner(ctx, max_columns, max_phenos)
+    pending = sorted(arrivals, key=lambda a: a[0])
+    t0 = clock()
+    k = 0
+    while k < len(pending) or r.jobs:
+        now = clock() - t0
+        while k < len(pending) and pending[k][0] <= now and r.can_admit(pending[k][1]):
+            r.submit(pending[k][1], t_arrive=t0 + pending[k][0])
+            k += 1
+        if r.jobs:
+            r.step()
+        elif k < len(pending):
+            time.sleep(max(0.0, min(0.01, pending[k][0] - now)))
+    return r.finished

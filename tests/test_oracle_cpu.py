@@ -148,3 +148,14 @@ def test_c_restatement_of_reference_cpu_path():
     xo, ito = aireml.pcg(grm, w, tau, b, 500, 1e-5, return_iters=True)
     assert abs(it - ito) <= 2
     assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-3
+
+
+def test_c_synth_setgeno_matches_python_recipe():
+    from oracle import cpu_ref
+    n, m = 203, 150
+    pg = cpu_ref.PackedGeno.synthetic(77, n, m, 0.03)
+    bed, _ = synth.synth_bed(77, n, m, 0.03)
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+    assert pg.m == g.codes.shape[0]
+    np.testing.assert_array_equal(pg.packed, plink.pack_codes(g.codes))
+    np.testing.assert_array_equal(pg.lut[:, :3], plink.std_lut(g.freq, g.invstd))

@@ -1,0 +1,103 @@
+"""Host logic of the batched driver, run against a numpy fake of the engine (no GPU)."""
+import numpy as np
+
+from oracle import aireml, plink, probes
+from saigegpu import prep, serve, synth
+
+
+class FakeEngine:
+    """Implements the engine calls the runner uses with the FP64 oracle (solves on admission)."""
+
+    def __init__(self, grm):
+        self.grm = grm
+        self.n = grm.n
+        self.ph = {}
+        self.res = {}
+        self.fin = []
+        self.next = 1
+
+    def engine_reserve(self, cols, phenos):
+        pass
+
+    def engine_set_pheno(self, slot, w, tau, mask=None):
+        self.ph[slot] = (np.asarray(w, float).copy(), np.asarray(tau, float).copy(),
+                         np.ones(self.n, bool) if mask is None else np.asarray(mask, bool))
+
+    def _solve(self, slot, kind, b, maxiter, tol):
+        w, tau, m = self.ph[slot]
+        S = np.nonzero(m)[0]
+        b = np.where(m, b, 0.0)
+        x = np.zeros(self.n)
+        if kind == 1:
+            x[S] = self.grm.K[np.ix_(S, S)] @ b[S]
+            return x, 1
+        sub = aireml.DenseGRM.from_matrix(self.grm.K[np.ix_(S, S)], self.grm.m_qc, self.grm.diag_sum[S])
+        xs, it = aireml.pcg(sub, w[S], tau, b[S], maxiter, tol, return_iters=True)
+        x[S] = xs
+        return x, int(np.asarray(it).ravel()[0])
+
+    def engine_submit(self, slot, kind, B, maxiter=500, tol=1e-5):
+        B = np.asarray(B, float)
+        ids = []
+        for j in range(B.shape[1]):
+            rid = self.next
+            self.next += 1
+            self.res[rid] = self._solve(slot, kind, B[:, j], maxiter, tol)
+            self.fin.append(rid)
+            ids.append(rid)
+        return np.array(ids)
+
+    def engine_submit_probes(self, slot, kind, seed, run0, k, maxiter=500, tol=1e-5):
+        U = np.column_stack([probes.rademacher(seed, run0 + j, self.n) for j in range(k)])
+        return self.engine_submit(slot, kind, U, maxiter, tol)
+
+    def engine_run(self, k=1):
+        return len(self.fin)
+
+    def engine_poll(self, max_ids=1 << 16):
+        out, self.fin = self.fin, []
+        return np.array(out, dtype=np.int64)
+
+    def engine_fetch(self, rid):
+        return self.res.pop(int(rid))
+
+    def engine_cancel(self, rid):
+        self.res.pop(int(rid), None)
+
+
+def _cohort(seed=13, n=240, m=700):
+    bed, _ = synth.synth_bed(seed, n, m, 0.01)
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+    return aireml.DenseGRM(g), g
+
+
+def test_generator_fit_equals_oracle_fit():
+    grm, g = _cohort()
+    n = grm.n
+    gv = synth.genetic_value_from_codes(g.codes, 3)
+    for trait in ("binary", "quantitative"):
+        y, C = synth.simulate_pheno(gv, 5, trait, tau=0.5, prevalence=0.3, h2=0.5)
+        f0 = prep.make_fit0(y, C, trait, True)
+        ref = (aireml.glmmkin_binary if trait == "binary" else aireml.glmmkin_quantitative)(grm, f0)
+        res, jobs = serve.fit_batch(FakeEngine(grm), [serve.FitSpec(f0, trait)])
+        # same algorithm; summation order differs (a PCG column may stop one iteration apart)
+        np.testing.assert_allclose(res[0]["theta"], ref["theta"], rtol=1e-4)
+        np.testing.assert_allclose(res[0]["coefficients"], ref["coefficients"], rtol=1e-4, atol=1e-8)
+        assert res[0]["iterations"] == ref["iterations"]
+
+
+def test_masked_fit_equals_subset_fit():
+    grm, g = _cohort(17)
+    n = grm.n
+    rng = np.random.default_rng(2)
+    mask = rng.uniform(size=n) > 0.25
+    S = np.nonzero(mask)[0]
+    gv = synth.genetic_value_from_codes(g.codes, 4)
+    y, C = synth.simulate_pheno(gv, 6, "binary", tau=0.5, prevalence=0.3)
+    f0 = prep.make_fit0(y[S], C[S], "binary", True)
+    sub = aireml.DenseGRM.from_matrix(grm.K[np.ix_(S, S)], grm.m_qc, grm.diag_sum[S])
+    ref = aireml.glmmkin_binary(sub, f0)
+    # probes over the subset: the driver masks cohort-length probes, so draw the oracle's the same way
+    res, _ = serve.fit_batch(FakeEngine(grm), [serve.FitSpec(f0, "binary", mask=mask)])
+    assert res[0]["n"] == len(S)
+    assert abs(res[0]["theta"][1] - ref["theta"][1]) / ref["theta"][1] < 0.2
