@@ -122,6 +122,24 @@ int sg_grm_get(sg_ctx *ctx, float *out);
 /* K V for k vectors (RHS-major, FP64 in and out; the product runs in FP32). */
 int sg_grm_matmul(sg_ctx *ctx, const double *V, int64_t k, double *out);
 
+/* GRM.V for callers that cannot allocate device memory.  No counterpart in the reference: it exists
+ * for host runtimes that own all device memory through their own pool and forbid cudaMalloc, and
+ * for latency-critical loops that cannot absorb the synchronisation cudaMalloc/cudaFree can cause.
+ * Y (ncols x n_p, RHS-major, device) = K P with P (ncols x n_p FP32, RHS-major, device); n_p = n
+ * rounded up to 128 (sg_grm_padded_n), rows past n of P must be zero.  Runs the split-TF32 tcgen05
+ * product, so the context must already be in SG_MV_TF32X3_TC mode (else SG_ERR_STATE: switching
+ * would allocate).  The call allocates nothing: its scratch is one static device array of
+ * 2 x 2^21 floats plus a tile table (about 16 MiB), so ncols * n_p must not exceed 2,097,152 and
+ * ncols must be a multiple of 32 (else SG_ERR_INVALID).  The first call on a device looks up that
+ * array's device address, so make the first call before any stream capture.  Every call shares
+ * the array and overwrites what it uses; calls that overlap on the GPU (e.g. on two streams) race.
+ * ``stream`` is a cudaStream_t (NULL = the legacy default stream); the call returns after the
+ * product has finished. */
+int sg_grm_matmul_tf32x3_noalloc(sg_ctx *ctx, const float *P_dev, int64_t ncols, float *Y_dev,
+                                 void *stream);
+/* GRM row count padded to the tile size (the leading dimension of device-side vector blocks). */
+int sg_grm_padded_n(sg_ctx *ctx, int64_t *np);
+
 /* ------------------------------------------------------------ drop-ins for the Rcpp entry points */
 /* getCrossprodMatAndKin (FIT.cpp:1953-1981; RcppExports.cpp:664-671) */
 int sg_getCrossprodMatAndKin(sg_ctx *ctx, const float *b, float *out);

@@ -602,6 +602,33 @@ static int ensure_k_split(sg_ctx* c, bool want) {
   return sync(c);
 }
 
+extern "C" int sg_grm_padded_n(sg_ctx* c, int64_t* np) {
+  NEED_GRM(c);
+  if (!np) return set_err(c, SG_ERR_INVALID, "null output");
+  *np = c->np;
+  return SG_OK;
+}
+
+// Allocation-free GRM.V for callers that cannot allocate (see include/saigegpu.h).
+extern "C" int sg_grm_matmul_tf32x3_noalloc(sg_ctx* c, const float* P_dev, int64_t ncols, float* Y_dev,
+                                            void* stream) {
+  NEED_GRM(c);
+  if (!P_dev || !Y_dev) return set_err(c, SG_ERR_INVALID, "null device pointer");
+  if (!c->k_split)
+    return set_err(c, SG_ERR_STATE, "select SG_MV_TF32X3_TC first (the split GRM is not resident)");
+  if (ncols <= 0 || ncols % 32 != 0)
+    return set_err(c, SG_ERR_INVALID, "ncols = %lld must be a positive multiple of 32", (long long)ncols);
+  if (ncols * c->np > tc_noalloc_max_elems())
+    return set_err(c, SG_ERR_INVALID, "ncols * n_p = %lld exceeds the static scratch limit of %lld entries",
+                   (long long)(ncols * c->np), (long long)tc_noalloc_max_elems());
+  cudaError_t e = tc_gemm_tf32x3_noalloc(c->d_K, c->d_Klo, c->np, P_dev, ncols, Y_dev,
+                                         reinterpret_cast<cudaStream_t>(stream));
+  c->launches += 2;
+  if (e != cudaSuccess) return set_err(c, e == cudaErrorLaunchTimeout ? SG_ERR_TIMEOUT : SG_ERR_CUDA,
+                                       "no-alloc GRM.V: %s", cudaGetErrorString(e));
+  return SG_OK;
+}
+
 extern "C" int sg_grm_diag(sg_ctx* c, double* out) {
   NEED_GENO(c);
   std::copy(c->diag.begin(), c->diag.end(), out);

@@ -468,4 +468,89 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
   return check_error_flag(s);
 }
 
+// ---------------------------------------------------------------- GRM.V that allocates nothing
+//
+// For callers that must not allocate device memory themselves or through us:
+// host runtimes that hand out all HBM from their own pool and forbid raw
+// cudaMalloc (an R or Python serving process that pre-reserves memory for a
+// batch of phenotype fits), and latency-critical loops that cannot take the
+// device-wide synchronisation cudaMalloc / cudaFree may cause.  Its only
+// scratch -- the TF32 high/low halves of the caller's vectors and the tile
+// table -- lives in the file-scope array below, sized for at most
+// kNoAllocMaxElems vector entries (ncols * np).  Every GPU that loads this
+// library holds the array until the process exits.
+constexpr int64_t kNoAllocMaxElems = int64_t(1) << 21;  // 2,097,152 entries (e.g. 20 columns at N = 100k)
+constexpr int64_t kNoAllocMaxTiles = kNoAllocMaxElems / (kTileM * 32);
+constexpr size_t kNoAllocScratchBytes =
+    2 * (size_t)kNoAllocMaxElems * sizeof(float) + (size_t)kNoAllocMaxTiles * sizeof(TileCoord);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+__global__ void noalloc_prepare_kernel(const float* __restrict__ P, int64_t elems, float* __restrict__ hi,
+                                       float* __restrict__ lo, TileCoord* __restrict__ tiles,
+                                       int64_t nbm, int64_t nbn) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < elems) {
+    const float v = P[i];
+    const uint32_t u = __float_as_uint(v);
+    const float h = isfinite(v) ? __uint_as_float((u + 0x1000u) & 0xFFFFE000u) : v;
+    hi[i] = h;
+    lo[i] = isfinite(v) ? v - h : 0.0f;
+  }
+  if (i < nbm * nbn) tiles[i] = TileCoord{(int32_t)(i / nbn), (int32_t)(i % nbn)};
+}
+
+// Device address of the scratch array, looked up once per device with that device current.
+static cudaError_t noalloc_scratch_ptr(unsigned char** out) {
+  constexpr int kMaxDevices = 64;
+  static unsigned char* ptrs[kMaxDevices] = {};
+  static std::mutex mu;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!ptrs[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    ptrs[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = ptrs[dev];
+  return cudaSuccess;
+}
+
+int64_t tc_noalloc_max_elems() { return kNoAllocMaxElems; }
+
+cudaError_t tc_gemm_tf32x3_noalloc(const float* Khi, const float* Klo, int64_t np, const float* P,
+                                   int64_t ncols, float* Y, cudaStream_t s) {
+  if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0 || ncols * np > kNoAllocMaxElems)
+    return cudaErrorInvalidValue;
+  unsigned char* base = nullptr;
+  cudaError_t e = noalloc_scratch_ptr(&base);
+  if (e != cudaSuccess) return e;
+  float* hi = reinterpret_cast<float*>(base);
+  float* lo = hi + kNoAllocMaxElems;
+  TileCoord* tiles = reinterpret_cast<TileCoord*>(lo + kNoAllocMaxElems);
+  const int BN = ncols % 64 == 0 ? 64 : 32;
+  const int64_t nbm = np / kTileM, nbn = ncols / BN;
+  const int64_t elems = ncols * np;
+  const int64_t work = elems > nbm * nbn ? elems : nbm * nbn;
+  noalloc_prepare_kernel<<<(unsigned)((work + 255) / 256), 256, 0, s>>>(P, elems, hi, lo, tiles, nbm, nbn);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  CUtensorMap a, b, a2, b2;
+  if (!make_map(&a, Khi, true, np, np, (uint64_t)np * 4, kTileM) ||
+      !make_map(&a2, Klo, true, np, np, (uint64_t)np * 4, kTileM) ||
+      !make_map(&b, hi, true, np, ncols, (uint64_t)np * 4, BN) ||
+      !make_map(&b2, lo, true, np, ncols, (uint64_t)np * 4, BN))
+    return cudaErrorInvalidValue;
+  const int num_kb = (int)(np / 32);
+  if (BN == 64)
+    e = launch<true, 64, 4, true>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, Y, np, 1.0f, 1, s);
+  else
+    e = launch<true, 32, 5, true>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, Y, np, 1.0f, 1, s);
+  if (e != cudaSuccess) return e;
+  return check_error_flag(s);
+}
+
 }  // namespace sg

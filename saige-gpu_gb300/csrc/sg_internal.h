@@ -79,6 +79,10 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
 // Plo (split operands) it accumulates K P + K Plo + Klo P (3xTF32).
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
                          const float* Plo, int64_t ncols, float* Y, cudaStream_t s);
+// Split-TF32 GRM.V that allocates nothing: scratch in a static device array (k_tc.cu).
+int64_t tc_noalloc_max_elems();
+cudaError_t tc_gemm_tf32x3_noalloc(const float* Khi, const float* Klo, int64_t np, const float* P,
+                                   int64_t ncols, float* Y, cudaStream_t s);
 // x = hi + lo with hi rounded to TF32 (low 13 mantissa bits zero) and lo = x - hi (exact)
 void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
 
