@@ -217,9 +217,19 @@ int sg_engine_submit_probes(sg_ctx *ctx, int64_t slot, int kind, uint64_t seed, 
 /* Run up to max_steps engine steps (admitting queued columns as slots free up).
  * Returns after the step in which at least one column retired, or when idle. */
 int sg_engine_run(sg_ctx *ctx, int64_t max_steps, int64_t *n_finished);
+/* Finished columns keep their result on the device (and their column) until fetched, cancelled or
+ * consumed by sg_engine_probe_dots. */
 /* Fetch and release a finished column: x[n], iterations.  SG_ERR_STATE if not finished. */
 int sg_engine_fetch(sg_ctx *ctx, int64_t id, double *x, int32_t *iters);
 int sg_engine_cancel(sg_ctx *ctx, int64_t id);
+/* Hutchinson trace reductions on the device for k finished probe pairs (ids_pcg[j] = Sigma^-1 u_j,
+ * ids_prod[j] = K u_j, u_j the counter-hash probe of (seed, run0 + j) masked to the slot's samples):
+ * out[j*(2+2p) + ...] = [Au.Su, u.Su, Au.SX_0..p-1, SX_0..p-1.u] with SX (n x p, column-major, host)
+ * = Sigma^-1 X.  Then tr(PK)_j = Au.Su - b' cov c and tr(P)_j = u.Su - c' cov c (GetTrace /
+ * GetTrace_q FIT.cpp:3133-3146, 3427-3446).  Consumes (releases) the 2k results; p <= 16. */
+int sg_engine_probe_dots(sg_ctx *ctx, int64_t slot, const int64_t *ids_pcg, const int64_t *ids_prod,
+                         int64_t k, uint64_t seed, int64_t run0, const double *SX, int64_t p,
+                         double *out, int32_t *iters);
 /* Ids of columns that finished since the previous poll (up to max_ids); *n_out gets the count. */
 int sg_engine_poll(sg_ctx *ctx, int64_t *ids, int64_t max_ids, int64_t *n_out);
 /* counters: [0]=engine steps, [1]=columns retired, [2]=column-iterations, [3]=GRM passes */

@@ -58,6 +58,11 @@ struct Engine {
   int64_t steps = 0, retired = 0, col_iters = 0, grm_passes = 0;
   std::vector<int64_t> finished;  // ids retired since the last poll
   float* Pflo = nullptr;          // low TF32 halves of Pf (split-TF32 mode)
+  double* d_sx = nullptr;         // probe_dots: Sigma^-1 X block
+  double* d_dpart = nullptr;      // probe_dots: block partial sums
+  int32_t* d_dcols = nullptr;     // probe_dots: column indices
+  uint8_t* ptab = nullptr;        // probe table of one admission round (stage_cols x 24 B)
+  size_t dots_cap_sx = 0, dots_cap_part = 0, dots_cap_cols = 0;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   double t_step_ms = 0, t_gemm_ms = 0, gemm_launches = 0, gemm_flops = 0, gemm_cols = 0, useful_cols = 0;
 };
@@ -657,6 +662,8 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.B); dev_free_t(c, e.part); dev_free_t(c, e.winv); dev_free_t(c, e.minv);
   dev_free_t(c, e.Yd); dev_free_t(c, e.Pf); dev_free_t(c, e.Yf); dev_free_t(c, e.d_st);
   dev_free_t(c, e.d_ph); dev_free_t(c, e.d_cols); dev_free_t(c, e.Pflo);
+  dev_free_t(c, e.d_sx); dev_free_t(c, e.d_dpart); dev_free_t(c, e.d_dcols); dev_free_t(c, e.ptab);
+  e.dots_cap_sx = e.dots_cap_part = e.dots_cap_cols = 0;
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
   e.finished.clear();
@@ -695,6 +702,8 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   NEED_GRM(c);
   Engine& e = c->eng;
   max_columns = round_up(std::max<int64_t>(max_columns, 32), 32);
+  if (max_columns > 96) max_columns = round_up(max_columns, 128);
+  if (max_columns > 320) max_columns = round_up(max_columns, 256);
   max_phenos = std::max<int64_t>(max_phenos, 1);
   if (e.cap_cols >= max_columns && e.cap_ph >= max_phenos && e.np == c->np) return SG_OK;
   for (auto& kv : e.reqs)
@@ -714,6 +723,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   SG_TRY(dev_alloc_t(c, &e.Pf, V)); SG_TRY(dev_alloc_t(c, &e.Yf, V));
   SG_TRY(dev_alloc_t(c, &e.B, (size_t)(e.stage_cols * np)));
   SG_TRY(dev_alloc_t(c, &e.part, (size_t)(max_columns * e.nblk * 2)));
+  SG_TRY(dev_alloc_t(c, &e.ptab, (size_t)(e.stage_cols * 24)));
   SG_TRY(dev_alloc_t(c, &e.winv, (size_t)(max_phenos * np)));
   SG_TRY(dev_alloc_t(c, &e.minv, (size_t)(max_phenos * np)));
   SG_TRY(dev_alloc_t(c, &e.d_st, (size_t)max_columns));
@@ -827,6 +837,9 @@ static int engine_admit(sg_ctx* c) {
   while (!e.queue.empty()) {
     std::vector<int32_t> cols;
     std::vector<int64_t> admitted;
+    std::vector<uint64_t> pseeds;
+    std::vector<int64_t> pruns;
+    std::vector<int32_t> psel;
     int64_t col = 0;
     while (!e.queue.empty() && (int64_t)cols.size() < e.stage_cols) {
       while (col < e.cap_cols && e.col_req[col] != -1) ++col;
@@ -838,8 +851,9 @@ static int engine_admit(sg_ctx* c) {
       Req& r = it->second;
       const int64_t sel = (int64_t)cols.size();
       if (r.probe) {
-        launch_probe_fill(e.np, c->nn, r.seed, r.run, 1, e.B + sel * e.np, c->stream);
-        c->launches += 1;
+        pseeds.push_back(r.seed);
+        pruns.push_back(r.run);
+        psel.push_back((int32_t)sel);
       } else {
         SG_CUDA(c, cudaMemcpyAsync(e.B + sel * e.np, r.b.data(), c->nn * 8, cudaMemcpyHostToDevice, c->stream));
         if (e.np > c->nn)
@@ -861,6 +875,19 @@ static int engine_admit(sg_ctx* c) {
       ++col;
     }
     if (cols.empty()) break;
+    if (!psel.empty()) {
+      // one launch for every probe of this admission round; its index table (uint64 seeds |
+      // int64 runs | int32 rows, at most stage_cols entries) lives in e.ptab
+      const size_t kp = psel.size();
+      uint64_t* d_seeds = reinterpret_cast<uint64_t*>(e.ptab);
+      int64_t* d_runs = reinterpret_cast<int64_t*>(d_seeds + kp);
+      int32_t* d_sel = reinterpret_cast<int32_t*>(d_runs + kp);
+      SG_CUDA(c, cudaMemcpyAsync(d_seeds, pseeds.data(), kp * 8, cudaMemcpyHostToDevice, c->stream));
+      SG_CUDA(c, cudaMemcpyAsync(d_runs, pruns.data(), kp * 8, cudaMemcpyHostToDevice, c->stream));
+      SG_CUDA(c, cudaMemcpyAsync(d_sel, psel.data(), kp * 4, cudaMemcpyHostToDevice, c->stream));
+      launch_probe_fill_multi(e.np, c->nn, d_seeds, d_runs, d_sel, (int64_t)kp, e.B, c->stream);
+      c->launches += 1;
+    }
     SG_CUDA(c, cudaMemcpyAsync(e.d_cols, cols.data(), cols.size() * 4, cudaMemcpyHostToDevice, c->stream));
     launch_pcg_init(e.np, e.cap_cols, e.d_cols, (int64_t)cols.size(), e.d_st, e.d_ph, e.minv, e.B,
                     e.X, e.R, e.Z, e.P, e.Pf, e.part, e.nblk, c->stream);
@@ -914,9 +941,22 @@ static int engine_gemm(sg_ctx* c, int64_t ncols, bool* used_yf) {
 }
 
 // One engine step over columns [0, hi_col): GRM product + the FP64 PCG vector work.
+// Columns the GRM.V of one step covers: [0, hi_col) padded to the kernel's column tile (the
+// padding columns are free or finished, their P rows are zero).
+static int64_t engine_gemm_cols(const sg_ctx* c) {
+  const Engine& e = c->eng;
+  int64_t ncols = round_up(e.hi_col, 32);
+  if (c->mv_mode == SG_MV_TF32_TC || c->mv_mode == SG_MV_TF32X3_TC) {
+    const int64_t w = ncols > 320 ? 256 : (ncols > 96 ? 128 : 32);
+    const int64_t padded = std::min(round_up(ncols, w), e.cap_cols);
+    if (padded % w == 0) ncols = padded;
+  }
+  return ncols;
+}
+
 static int engine_step(sg_ctx* c, int64_t* n_finished) {
   Engine& e = c->eng;
-  const int64_t ncols = round_up(e.hi_col, 32);
+  const int64_t ncols = engine_gemm_cols(c);
   int64_t occupied = 0;
   for (int64_t col = 0; col < e.hi_col; ++col) occupied += e.col_req[col] >= 0 ? 1 : 0;
   bool yf = true;
@@ -954,20 +994,18 @@ static int engine_step(sg_ctx* c, int64_t* n_finished) {
     const int64_t id = e.col_req[col];
     if (id < 0) continue;
     ColState& s = e.h_st[col];
+    if (s.kind == -2) continue;  // finished earlier, result held in X[col]
     e.col_iters += 1;
     if (s.active) continue;
     auto it = e.reqs.find(id);
     if (it != e.reqs.end()) {
       Req& r = it->second;
-      r.x.resize(c->nn);
-      SG_CUDA(c, cudaMemcpyAsync(r.x.data(), e.X + col * e.np, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
       r.iters = s.kind == 1 ? 1 : s.iter;
       r.state = 2;
-      r.col = -1;
+      r.col = col;
       e.finished.push_back(id);
     }
-    e.col_req[col] = -1;
-    s.kind = -1;
+    s.kind = -2;
     s.active = 0;
     s.just_done = 0;
     SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
@@ -994,14 +1032,12 @@ static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
     if (s.kind != 0 || s.active || !s.just_done) continue;
     auto it = e.reqs.find(id);
     if (it != e.reqs.end()) {
-      it->second.x.assign(c->nn, 0.0);
       it->second.iters = 0;
       it->second.state = 2;
-      it->second.col = -1;
+      it->second.col = col;  // X[col] was zeroed at admission
       e.finished.push_back(id);
     }
-    e.col_req[col] = -1;
-    s.kind = -1;
+    s.kind = -2;
     s.just_done = 0;
     SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
     e.n_active -= 1;
@@ -1029,14 +1065,35 @@ extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) 
   return SG_OK;
 }
 
+// Free a column (running or holding a result) for the next admission.
+static int release_col(sg_ctx* c, int64_t col) {
+  Engine& e = c->eng;
+  ColState s{};
+  s.kind = -1;
+  s.active = 0;
+  e.h_st[col] = s;
+  SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(c, cudaMemsetAsync(e.Pf + col * e.np, 0, e.np * 4, c->stream));
+  e.col_req[col] = -1;
+  while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
+  return SG_OK;
+}
+
 extern "C" int sg_engine_fetch(sg_ctx* c, int64_t id, double* x, int32_t* iters) {
   if (!c) return SG_ERR_INVALID;
   Engine& e = c->eng;
   auto it = e.reqs.find(id);
   if (it == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
-  if (it->second.state != 2) return set_err(c, SG_ERR_STATE, "request %lld not finished", (long long)id);
-  if (x) std::copy(it->second.x.begin(), it->second.x.end(), x);
-  if (iters) *iters = it->second.iters;
+  Req& r = it->second;
+  if (r.state != 2) return set_err(c, SG_ERR_STATE, "request %lld not finished", (long long)id);
+  if (r.col >= 0) {
+    if (x) SG_CUDA(c, cudaMemcpyAsync(x, e.X + r.col * e.np, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
+    SG_TRY(release_col(c, r.col));
+    SG_TRY(sync(c));
+  } else if (x) {
+    std::copy(r.x.begin(), r.x.end(), x);
+  }
+  if (iters) *iters = r.iters;
   e.reqs.erase(it);
   return SG_OK;
 }
@@ -1047,20 +1104,75 @@ extern "C" int sg_engine_cancel(sg_ctx* c, int64_t id) {
   auto it = e.reqs.find(id);
   if (it == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
   Req& r = it->second;
-  if (r.state == 1 && r.col >= 0) {
-    ColState s{};
-    s.kind = -1;
-    s.active = 0;
-    e.h_st[r.col] = s;
-    SG_CUDA(c, cudaMemcpyAsync(e.d_st + r.col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
-    SG_CUDA(c, cudaMemsetAsync(e.Pf + r.col * e.np, 0, e.np * 4, c->stream));
-    e.col_req[r.col] = -1;
-    e.n_active -= 1;
-    while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
+  if ((r.state == 1 || r.state == 2) && r.col >= 0) {
+    if (r.state == 1) e.n_active -= 1;
+    SG_TRY(release_col(c, r.col));
     SG_TRY(sync(c));
   }
   e.reqs.erase(it);  // a queued id is skipped at admission
   return SG_OK;
+}
+
+// Hutchinson probe reductions on the device (see include/saigegpu.h).
+extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_pcg,
+                                    const int64_t* ids_prod, int64_t k, uint64_t seed, int64_t run0,
+                                    const double* SX, int64_t p, double* out, int32_t* iters) {
+  NEED_GRM(c);
+  Engine& e = c->eng;
+  if (k <= 0 || !ids_pcg || !ids_prod || !out || p < 0 || p > kProbeDotsMaxP || (p > 0 && !SX))
+    return set_err(c, SG_ERR_INVALID, "probe_dots: bad arguments (p <= %d)", kProbeDotsMaxP);
+  if (slot < 0 || slot >= e.cap_ph) return set_err(c, SG_ERR_INVALID, "bad slot");
+  std::vector<int32_t> cols(2 * k);
+  for (int64_t j = 0; j < 2 * k; ++j) {
+    const int64_t id = j < k ? ids_pcg[j] : ids_prod[j - k];
+    auto it = e.reqs.find(id);
+    if (it == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
+    if (it->second.state != 2 || it->second.col < 0)
+      return set_err(c, SG_ERR_STATE, "request %lld has no resident result", (long long)id);
+    cols[j] = (int32_t)it->second.col;
+  }
+  const int64_t nv = 2 + 2 * p;
+  const int64_t nblk = e.nblk;
+  const size_t need_sx = (size_t)std::max<int64_t>(p, 1) * e.np;
+  const size_t need_part = (size_t)(k * nblk * nv);
+  if (e.dots_cap_sx < need_sx) {
+    dev_free_t(c, e.d_sx);
+    SG_TRY(dev_alloc_t(c, &e.d_sx, need_sx));
+    e.dots_cap_sx = need_sx;
+  }
+  if (e.dots_cap_part < need_part || e.dots_cap_cols < (size_t)(2 * k)) {
+    dev_free_t(c, e.d_dpart);
+    dev_free_t(c, e.d_dcols);
+    SG_TRY(dev_alloc_t(c, &e.d_dpart, need_part));
+    SG_TRY(dev_alloc_t(c, &e.d_dcols, (size_t)(2 * k)));
+    e.dots_cap_part = need_part;
+    e.dots_cap_cols = (size_t)(2 * k);
+  }
+  if (p > 0) {
+    SG_CUDA(c, cudaMemsetAsync(e.d_sx, 0, need_sx * 8, c->stream));
+    SG_CUDA(c, cudaMemcpy2DAsync(e.d_sx, e.np * 8, SX, c->nn * 8, c->nn * 8, p, cudaMemcpyHostToDevice, c->stream));
+  }
+  SG_CUDA(c, cudaMemcpyAsync(e.d_dcols, cols.data(), cols.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  launch_probe_dots(e.np, c->nn, e.X, e.d_dcols, k, e.minv + slot * e.np, seed, run0, e.d_sx, p,
+                    e.d_dpart, nblk, c->stream);
+  SG_LAUNCHED(c, 1);
+  std::vector<double> part(need_part);
+  SG_CUDA(c, cudaMemcpyAsync(part.data(), e.d_dpart, need_part * 8, cudaMemcpyDeviceToHost, c->stream));
+  SG_TRY(sync(c));
+  for (int64_t j = 0; j < k; ++j)
+    for (int64_t v = 0; v < nv; ++v) {
+      double acc = 0.0;
+      for (int64_t b = 0; b < nblk; ++b) acc += part[(j * nblk + b) * nv + v];
+      out[j * nv + v] = acc;
+    }
+  for (int64_t j = 0; j < 2 * k; ++j) {
+    const int64_t id = j < k ? ids_pcg[j] : ids_prod[j - k];
+    auto it = e.reqs.find(id);
+    if (iters && j < k) iters[j] = it->second.iters;
+    SG_TRY(release_col(c, it->second.col));
+    e.reqs.erase(it);
+  }
+  return sync(c);
 }
 
 extern "C" int sg_engine_poll(sg_ctx* c, int64_t* ids, int64_t max_ids, int64_t* n_out) {

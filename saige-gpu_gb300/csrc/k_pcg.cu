@@ -322,6 +322,68 @@ void launch_probe_fill(int64_t np, int64_t nn, uint64_t seed, int64_t run0, int6
   probe_fill_kernel<<<grid, 256, 0, s>>>(np, nn, seed, run0, B);
 }
 
+// Probes for a set of staging rows in one launch: row sel[j] of B gets probe (seeds[j], runs[j]).
+__global__ void probe_fill_multi_kernel(int64_t np, int64_t nn, const uint64_t* __restrict__ seeds,
+                                        const int64_t* __restrict__ runs, const int32_t* __restrict__ sel,
+                                        double* B) {
+  const int64_t j = blockIdx.y;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  double v = 0.0;
+  if (i < nn) v = (hash3(seeds[j], (uint64_t)runs[j], (uint64_t)i) >> 63) ? 1.0 : -1.0;
+  B[(int64_t)sel[j] * np + i] = v;
+}
+
+void launch_probe_fill_multi(int64_t np, int64_t nn, const uint64_t* seeds, const int64_t* runs,
+                             const int32_t* sel, int64_t k, double* B, cudaStream_t s) {
+  if (k == 0) return;
+  dim3 grid((unsigned)((np + 255) / 256), (unsigned)k);
+  probe_fill_multi_kernel<<<grid, 256, 0, s>>>(np, nn, seeds, runs, sel, B);
+}
+
+// Hutchinson probe reductions: for probe j the block sums of Au.Su, u.Su, Au.SX_q and SX_q.u.
+__global__ void probe_dots_kernel(int64_t np, int64_t nn, const double* __restrict__ X,
+                                  const int32_t* __restrict__ cols, int64_t k,
+                                  const double* __restrict__ minv, uint64_t seed, int64_t run0,
+                                  const double* __restrict__ SX, int p, double* part, int64_t nblk) {
+  __shared__ double sh[kThreads / 32];
+  const int64_t j = blockIdx.y;
+  const double* su = X + (int64_t)cols[j] * np;
+  const double* au = X + (int64_t)cols[k + j] * np;
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  double v[2 + 2 * kProbeDotsMaxP];
+#pragma unroll
+  for (int q = 0; q < 2 + 2 * kProbeDotsMaxP; ++q) v[q] = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < nn; i += kThreads) {
+    const double a = au[i], s = su[i];
+    const double u = (minv[i] != 0.0) ? ((hash3(seed, (uint64_t)(run0 + j), (uint64_t)i) >> 63) ? 1.0 : -1.0) : 0.0;
+    v[0] += a * s;
+    v[1] += u * s;
+#pragma unroll
+    for (int q = 0; q < kProbeDotsMaxP; ++q) {
+      if (q < p) {
+        const double x = SX[(int64_t)q * np + i];
+        v[2 + q] += a * x;
+        v[2 + kProbeDotsMaxP + q] += x * u;
+      }
+    }
+  }
+  const int nv = 2 + 2 * p;
+  for (int q = 0; q < nv; ++q) {
+    const int src = q < 2 + p ? q : (2 + kProbeDotsMaxP + (q - 2 - p));
+    const double t = block_sum(v[src], sh);
+    if (threadIdx.x == 0) part[(j * nblk + blockIdx.x) * nv + q] = t;
+  }
+}
+
+void launch_probe_dots(int64_t np, int64_t nn, const double* X, const int32_t* cols, int64_t k,
+                       const double* minv_row, uint64_t seed, int64_t run0, const double* SX,
+                       int64_t p, double* part, int64_t nblk, cudaStream_t s) {
+  if (k == 0) return;
+  dim3 grid((unsigned)nblk, (unsigned)k);
+  probe_dots_kernel<<<grid, kThreads, 0, s>>>(np, nn, X, cols, k, minv_row, seed, run0, SX, (int)p, part, nblk);
+}
+
 __global__ void f64_to_f32_kernel(const double* a, float* b, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = (float)a[i];

@@ -433,11 +433,20 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
   return check_error_flag(s);
 }
 
+// Column-tile width for the GRM.V: the widest tile that divides ncols (wider tiles re-read
+// the K strip fewer times; the split variants hold 2x operands per stage).
+int tc_gemm_tile_n(int64_t ncols, bool split) {
+  if (ncols % 256 == 0 && ncols >= 512) return 256;
+  if (ncols % 128 == 0 && ncols >= 128) return 128;
+  if (ncols % 64 == 0) return 64;
+  return 32;
+}
+
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
                          const float* Plo, int64_t ncols, float* Y, cudaStream_t s) {
   if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0) return cudaErrorInvalidValue;
   const bool split = Klo != nullptr && Plo != nullptr;
-  const int BN = split ? (ncols % 64 == 0 ? 64 : 32) : (ncols % 128 == 0 ? 128 : (ncols % 64 == 0 ? 64 : 32));
+  const int BN = tc_gemm_tile_n(ncols, split);
   CUtensorMap a, b, a2, b2;
   if (!make_map(&a, K, true, np, np, (uint64_t)np * 4, kTileM) ||
       !make_map(&b, P, true, np, ncols, (uint64_t)np * 4, BN))
@@ -454,16 +463,22 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
   cudaError_t e = upload_tiles(cache, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(np / 32);
-  if (split && BN == 64)
-    e = launch<true, 64, 4, true>(a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
-  else if (split)
-    e = launch<true, 32, 5, true>(a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
-  else if (BN == 128)
-    e = launch<true, 128, 4, false>(a, b, a, b, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
-  else if (BN == 64)
-    e = launch<true, 64, 6, false>(a, b, a, b, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
-  else
-    e = launch<true, 32, 8, false>(a, b, a, b, cache.dev, (int)cache.host.size(), num_kb, Y, np, 1.0f, 1, s);
+  const int nt = (int)cache.host.size();
+  if (split) {
+    switch (BN) {
+      case 256: e = launch<true, 256, 2, true>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+      case 128: e = launch<true, 128, 3, true>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+      case 64: e = launch<true, 64, 4, true>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+      default: e = launch<true, 32, 5, true>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+    }
+  } else {
+    switch (BN) {
+      case 256: e = launch<true, 256, 3, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+      case 128: e = launch<true, 128, 4, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+      case 64: e = launch<true, 64, 6, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+      default: e = launch<true, 32, 8, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+    }
+  }
   if (e != cudaSuccess) return e;
   return check_error_flag(s);
 }

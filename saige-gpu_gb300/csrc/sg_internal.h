@@ -79,6 +79,8 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
 // Plo (split operands) it accumulates K P + K Plo + Klo P (3xTF32).
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
                          const float* Plo, int64_t ncols, float* Y, cudaStream_t s);
+// Column tile width the GRM.V kernel uses for ncols columns.
+int tc_gemm_tile_n(int64_t ncols, bool split);
 // Split-TF32 GRM.V that allocates nothing: scratch in a static device array (k_tc.cu).
 int64_t tc_noalloc_max_elems();
 cudaError_t tc_gemm_tf32x3_noalloc(const float* Khi, const float* Klo, int64_t np, const float* P,
@@ -122,8 +124,16 @@ void launch_pcg_dir(int64_t np, int64_t ncols, ColState* st, const double* Z, do
                     float* Pf, cudaStream_t s);
 void launch_probe_fill(int64_t np, int64_t nn, uint64_t seed, int64_t run0, int64_t k,
                        double* B, cudaStream_t s);
+void launch_probe_fill_multi(int64_t np, int64_t nn, const uint64_t* seeds, const int64_t* runs,
+                             const int32_t* sel, int64_t k, double* B, cudaStream_t s);
 void launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
 void launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s);
 int64_t pcg_nblk(int64_t np);
+constexpr int kProbeDotsMaxP = 16;
+// Per probe j (columns cols[j] = Sigma^-1 u_j and cols[k+j] = K u_j, u masked by minv != 0):
+// block partials of [Au.Su, u.Su, Au.SX_q (q < p), SX_q.u (q < p)] -> part[(j*nblk + b)*(2+2p) + v]
+void launch_probe_dots(int64_t np, int64_t nn, const double* X, const int32_t* cols, int64_t k,
+                       const double* minv_row, uint64_t seed, int64_t run0, const double* SX,
+                       int64_t p, double* part, int64_t nblk, cudaStream_t s);
 
 }  // namespace sg

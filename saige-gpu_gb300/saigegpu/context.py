@@ -383,6 +383,19 @@ class Context:
         self._call("sg_engine_poll", _ptr(ids, L.P_i64), int(max_ids), C.byref(n))
         return ids[:n.value]
 
+    def engine_probe_dots(self, slot, ids_pcg, ids_prod, seed, run0, SX):
+        """Device-side Hutchinson reductions; returns (dots (k, 2+2p), PCG iterations (k,))."""
+        ip = np.ascontiguousarray(ids_pcg, np.int64)
+        ia = np.ascontiguousarray(ids_prod, np.int64)
+        k = len(ip)
+        SXf, p = _cols(np.asarray(SX, np.float64))
+        SXf = _f64(SXf)
+        out = np.empty(k * (2 + 2 * p), np.float64)
+        it = np.empty(k, np.int32)
+        self._call("sg_engine_probe_dots", int(slot), _ptr(ip, L.P_i64), _ptr(ia, L.P_i64), k, int(seed),
+                   int(run0), _ptr(SXf, L.P_f64), p, _ptr(out, L.P_f64), _ptr(it, L.P_i32))
+        return out.reshape(k, 2 + 2 * p), it
+
     def engine_timing(self):
         t = np.zeros(6, np.float64)
         self._call("sg_engine_timing", _ptr(t, L.P_f64))

@@ -10,7 +10,9 @@ host, and *yields* its right-hand sides instead of solving them:
 
     ("pheno", W, tau)                       set this fit's phenotype slot
     ("submit", kind, B | None, probes, maxiter, tol) -> request ids
-    ("wait", ids)                           -> the solutions (n-vectors)
+    ("wait", ids)                           -> the solutions (n-vectors, copied to the host)
+    ("wait_ids", ids)                       -> None once finished (results stay on the GPU)
+    ("probe_dots", pid, aid, seed, run0, SX) -> per-probe dot products reduced on the GPU
 
 ``Runner`` multiplexes any number of such fits onto the engine of one
 ``Context``: every engine step advances every in-flight column of every fit by
@@ -155,14 +157,14 @@ def fit_generator(spec, n_cohort, probes):
         sid = yield ("submit", 0, rhs, None, spec.maxiter_pcg, spec.tol_pcg)
         t1, t0 = [], []
         run0, k = 0, spec.nrun
+        p = SX.shape[1]
         while True:
-            Su = yield ("wait", pid)
-            Au = yield ("wait", aid)
-            U = np.column_stack([probes.get(spec.seed, run0 + j) * m for j in range(k)])
-            SUm = np.column_stack(Su)
-            PU = SUm - SX @ (cov @ (SX.T @ U))
-            t1.extend((np.column_stack(Au) * PU).sum(axis=0))
-            t0.extend((U * PU).sum(axis=0))
+            yield ("wait_ids", list(pid) + list(aid))
+            # t1 = Au.Pu, t0 = u.Pu with Pu = Su - SX cov SX'u, from device-side dot products
+            D = yield ("probe_dots", pid, aid, spec.seed, run0, SX)
+            b, c = D[:, 2:2 + p], D[:, 2 + p:2 + 2 * p]
+            t1.extend(D[:, 0] - np.einsum("ij,jk,ik->i", b, cov, c))
+            t0.extend(D[:, 1] - np.einsum("ij,jk,ik->i", c, cov, c))
             if _cal_cv(t1) > spec.cutoff or (quant and _cal_cv(t0) > spec.cutoff):
                 run0, k = run0 + k, 10
                 pid = yield ("submit", 0, None, (spec.seed, run0, k), spec.maxiter_pcg, spec.tol_pcg)
@@ -278,7 +280,7 @@ class Runner:
         self.free_slots = list(range(max_phenos))[::-1]
         self.jobs = {}
         self.owner = {}          # request id -> job id
-        self.done = {}           # request id -> (x, iters)
+        self.done = set()        # finished request ids (results resident on the GPU)
         self.probes = _Probes(self.n)
         self.finished = []
         self._next = 0
@@ -325,13 +327,21 @@ class Runner:
                     job.columns += len(ids)
                     self.inflight_columns += len(ids)
                     value = [int(i) for i in ids]
-                elif kind == "wait":
+                elif kind in ("wait", "wait_ids"):
                     ids = op[1]
                     if all(i in self.done for i in ids):
-                        value = [self._take(job, i) for i in ids]
+                        value = self._resolve(job, kind, ids)
                         continue
-                    job.waiting = ids
+                    job.waiting = (kind, ids)
                     return
+                elif kind == "probe_dots":
+                    _, pid, aid, seed, run0, SX = op
+                    D, its = self.ctx.engine_probe_dots(job.slot, pid, aid, seed, run0, SX)
+                    job.column_iterations += int(np.sum(its)) + len(aid)
+                    for i in list(pid) + list(aid):
+                        self.done.discard(i)
+                        self.owner.pop(i, None)
+                    value = D
                 else:
                     raise RuntimeError("unknown op %r" % (kind,))
         except StopIteration as st:
@@ -341,10 +351,17 @@ class Runner:
             job.error = ex
             self._finish(job)
 
-    def _take(self, job, rid):
-        x, it = self.done.pop(rid)
-        job.column_iterations += it
-        return x
+    def _resolve(self, job, kind, ids):
+        if kind == "wait_ids":
+            return None
+        out = []
+        for rid in ids:
+            x, it = self.ctx.engine_fetch(rid)
+            self.done.discard(rid)
+            self.owner.pop(rid, None)
+            job.column_iterations += it
+            out.append(x)
+        return out
 
     def _finish(self, job):
         job.t_done = time.perf_counter()
@@ -355,7 +372,7 @@ class Runner:
                 except Exception:
                     pass
                 self.owner.pop(rid, None)
-                self.done.pop(rid, None)
+                self.done.discard(rid)
         self.free_slots.append(job.slot)
         del self.jobs[job.jid]
         self.finished.append(job)
@@ -368,16 +385,13 @@ class Runner:
             rid = int(rid)
             if rid not in self.owner:
                 continue
-            x, it = self.ctx.engine_fetch(rid)
-            self.done[rid] = (x, it)
+            self.done.add(rid)
             self.inflight_columns -= 1
-        ready = [j for j in self.jobs.values() if j.waiting is not None and all(i in self.done for i in j.waiting)]
+        ready = [j for j in self.jobs.values()
+                 if j.waiting is not None and all(i in self.done for i in j.waiting[1])]
         for job in ready:
-            ids, job.waiting = job.waiting, None
-            vals = [self._take(job, i) for i in ids]
-            for i in ids:
-                self.owner.pop(i, None)
-            self._advance(job, vals)
+            (kind, wids), job.waiting = job.waiting, None
+            self._advance(job, self._resolve(job, kind, wids))
         return len(ids)
 
     def run(self, max_steps=1 << 30):

@@ -61,6 +61,17 @@ class FakeEngine:
     def engine_fetch(self, rid):
         return self.res.pop(int(rid))
 
+    def engine_probe_dots(self, slot, pid, aid, seed, run0, SX):
+        m = self.ph[slot][2]
+        rows, its = [], []
+        for j, (a, b) in enumerate(zip(pid, aid)):
+            su, it = self.res.pop(int(a))
+            au, _ = self.res.pop(int(b))
+            u = probes.rademacher(seed, run0 + j, self.n) * m
+            rows.append(np.concatenate([[au @ su, u @ su], au @ SX, SX.T @ u]))
+            its.append(it)
+        return np.array(rows), np.array(its)
+
     def engine_cancel(self, rid):
         self.res.pop(int(rid), None)
 
