@@ -397,3 +397,56 @@ def glmmkin_quantitative(grm, fit0, tol=0.02, maxiter=20, nrun=30, tol_pcg=1e-5,
     return dict(theta=tau, coefficients=rc["alpha"], linear_predictors=rc["eta"],
                 fitted_values=rc["mu"], Y=rc["Y"], residuals=y - rc["mu"], cov=rc["cov"],
                 converged=it_used < maxiter, iterations=it_used)
+
+
+def score_null_model(mu, mu2, y, X):
+    """ScoreTest_NULL_Model (FIT.R:579-591): XV, XVX, XXVX_inv, ... of the covariate projection."""
+    V = np.asarray(mu2, np.float64)
+    XV = (X * V[:, None]).T
+    XVX = X.T @ (X * V[:, None])
+    XVX_inv = np.linalg.inv(XVX)
+    XXVX_inv = X @ XVX_inv
+    return dict(XV=XV, XVX=XVX, XXVX_inv=XXVX_inv, XVX_inv=XVX_inv, V=V)
+
+
+def variance_ratio(grm, fit, trait, X, vr_geno, order, num_markers=30, ratio_cv_cutoff=0.001,
+                   maxiter=500, tol=1e-5):
+    """extractVarianceRatio (FIT.R:2152-2423), single (non-categorical) ratio, dense GRM.
+
+    ``vr_geno``: (m_vr, n) genotypes 0/1/2 of the variance-ratio markers (missing already filled,
+    ``Get_OneSNP_Geno_forVarRatio``); ``order``: the marker order (the reference draws it with R's
+    ``sample``).  X is the fit's design (``Xorig`` when covariates are offsets).
+    """
+    fam = Binomial() if trait == "binary" else Gaussian()
+    eta = np.asarray(fit["linear_predictors"], np.float64)
+    mu = np.asarray(fit["fitted_values"], np.float64)
+    tau = np.asarray(fit["theta"], np.float64)
+    mu_eta = fam.mu_eta(eta)
+    W = (mu_eta / np.sqrt(fam.variance(mu))) ** 2
+    mu2 = mu * (1 - mu) if trait == "binary" else np.full(len(mu), 1.0 / tau[0])
+    noK = score_null_model(mu, mu2, None, X)
+    SX = pcg(grm, W, tau, X, maxiter, tol)
+    XtSX_inv = np.linalg.inv(X.T @ SX)
+    n = len(mu)
+    ratios = []
+    idx = 0
+    target = num_markers
+    while True:
+        while len(ratios) < target and idx < len(order):
+            G0 = vr_geno[order[idx]].astype(np.float64)
+            idx += 1
+            if G0.sum() / (2 * n) > 0.5:
+                G0 = 2 - G0
+            AC = G0.sum()
+            G = G0 - noK["XXVX_inv"] @ (noK["XV"] @ G0)
+            g = G / np.sqrt(AC)
+            SG = pcg(grm, W, tau, G, maxiter, tol)
+            var1 = (G @ SG - (G @ SX) @ XtSX_inv @ (X.T @ SG)) / AC
+            var2 = float((mu * (1 - mu)) @ (g * g)) if trait == "binary" else float(g @ g)
+            ratios.append(var1 / var2)
+        cv = cal_cv(ratios)
+        if cv > ratio_cv_cutoff and idx < len(order):
+            target += 10
+            continue
+        break
+    return float(np.mean(ratios)), np.array(ratios)

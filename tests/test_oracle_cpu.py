@@ -159,3 +159,34 @@ def test_c_synth_setgeno_matches_python_recipe():
     assert pg.m == g.codes.shape[0]
     np.testing.assert_array_equal(pg.packed, plink.pack_codes(g.codes))
     np.testing.assert_array_equal(pg.lut[:, :3], plink.std_lut(g.freq, g.invstd))
+
+
+def test_variance_ratio_oracle_on_golden(golden_plink):
+    """VR of the reference's example (binary, covariates as offsets) lands near the golden null VR."""
+    bed, n, m, ph = golden_plink
+    rng = np.random.default_rng(5)
+    vr_rand = np.unique(rng.integers(0, m, 1000))
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15, vr_rand, 20, True)
+    grm = aireml.DenseGRM(g)
+    cov = np.column_stack([ph["x1"], ph["x2"]])
+    f0 = prep.make_fit0(ph["y_binary"], cov, "binary", True)
+    fit = aireml.glmmkin_binary(grm, f0)
+    order = rng.permutation(len(g.vr_index))
+    vr, ratios = aireml.variance_ratio(grm, fit, "binary", f0["Xorig"], g.vr_codes, order)
+    assert len(ratios) >= 30
+    gold = json.load(open(os.path.join(GOLDEN, "golden_fits.json")))["variance_ratio_null"]
+    # golden runs differ in tau by up to 30% (R's RNG for probes and markers): loose band
+    assert 0.85 < vr < 1.05, vr
+    assert abs(vr - gold["example_binary"][0]) < 0.1
+
+
+def test_output_writers_roundtrip(tmp_path):
+    from saigegpu import output
+    p = tmp_path / "x.varianceRatio.txt"
+    output.write_variance_ratio(p, [0.9456, 1.01])
+    assert output.read_variance_ratio(p) == [0.9456, 1.01]
+    fit = dict(theta=[1, 0.3], coefficients=[-2.5], linear_predictors=[0.1, 0.2], fitted_values=[0.5, 0.6],
+               Y=[1, 2], residuals=[0.1, 0.1], cov=[[0.01]], converged=True)
+    output.write_model(tmp_path / "m.json", fit, "binary", ["a", "b"])
+    d = output.read_model(tmp_path / "m.json")
+    assert d["theta"].tolist() == [1, 0.3] and d["sampleID"] == ["a", "b"]
