@@ -217,8 +217,12 @@ int sg_engine_submit_probes(sg_ctx *ctx, int64_t slot, int kind, uint64_t seed, 
 /* Run up to max_steps engine steps (admitting queued columns as slots free up).
  * Returns after the step in which at least one column retired, or when idle. */
 int sg_engine_run(sg_ctx *ctx, int64_t max_steps, int64_t *n_finished);
-/* Finished columns keep their result on the device (and their column) until fetched, cancelled or
- * consumed by sg_engine_probe_dots. */
+/* By default a finished column's result is copied to the host and its column freed at once.
+ * With hold != 0 finished results stay on the device (keeping their column) until fetched,
+ * cancelled or consumed by sg_engine_probe_dots; sg_engine_run then fails with SG_ERR_STATE
+ * rather than wait forever when queued columns find every column holding a result.  The blocking
+ * drop-ins switch holding off. */
+int sg_engine_hold_results(sg_ctx *ctx, int hold);
 /* Fetch and release a finished column: x[n], iterations.  SG_ERR_STATE if not finished. */
 int sg_engine_fetch(sg_ctx *ctx, int64_t id, double *x, int32_t *iters);
 int sg_engine_cancel(sg_ctx *ctx, int64_t id);

@@ -57,6 +57,7 @@ struct Engine {
   int64_t n_active = 0;
   int64_t steps = 0, retired = 0, col_iters = 0, grm_passes = 0;
   std::vector<int64_t> finished;  // ids retired since the last poll
+  bool hold = false;              // keep finished results on the device until fetched/consumed
   float* Pflo = nullptr;          // low TF32 halves of Pf (split-TF32 mode)
   double* d_sx = nullptr;         // probe_dots: Sigma^-1 X block
   double* d_dpart = nullptr;      // probe_dots: block partial sums
@@ -676,9 +677,11 @@ static void engine_free(sg_ctx* c) {
   e.ph_set.clear();
 }
 
-// Drop every queued and in-flight request (the blocking drop-ins own the engine).
+// Drop every queued and in-flight request (the blocking drop-ins own the engine); results are
+// copied out at retirement from here on.
 static int engine_clear(sg_ctx* c) {
   Engine& e = c->eng;
+  e.hold = false;
   if (e.cap_cols == 0) return SG_OK;
   bool any = false;
   for (int64_t col = 0; col < (int64_t)e.col_req.size(); ++col) {
@@ -941,6 +944,8 @@ static int engine_gemm(sg_ctx* c, int64_t ncols, bool* used_yf) {
 }
 
 // One engine step over columns [0, hi_col): GRM product + the FP64 PCG vector work.
+static int release_col(sg_ctx* c, int64_t col);
+
 // Columns the GRM.V of one step covers: [0, hi_col) padded to the kernel's column tile (the
 // padding columns are free or finished, their P rows are zero).
 static int64_t engine_gemm_cols(const sg_ctx* c) {
@@ -1004,14 +1009,23 @@ static int engine_step(sg_ctx* c, int64_t* n_finished) {
       r.state = 2;
       r.col = col;
       e.finished.push_back(id);
+      if (!e.hold) {  // copy the result out now and free the column
+        r.x.resize(c->nn);
+        SG_CUDA(c, cudaMemcpyAsync(r.x.data(), e.X + col * e.np, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
+        r.col = -1;
+      }
     }
-    s.kind = -2;
-    s.active = 0;
-    s.just_done = 0;
-    SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
     e.n_active -= 1;
     e.retired += 1;
     ++fin;
+    if (it != e.reqs.end() && it->second.col == col) {
+      s.kind = -2;  // held: result stays in X[col]
+      s.active = 0;
+      s.just_done = 0;
+      SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+    } else {
+      SG_TRY(release_col(c, col));
+    }
   }
   while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
   SG_TRY(sync(c));
@@ -1034,15 +1048,20 @@ static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
     if (it != e.reqs.end()) {
       it->second.iters = 0;
       it->second.state = 2;
-      it->second.col = col;  // X[col] was zeroed at admission
+      it->second.col = e.hold ? col : -1;  // X[col] was zeroed at admission
+      if (!e.hold) it->second.x.assign(c->nn, 0.0);
       e.finished.push_back(id);
     }
-    s.kind = -2;
-    s.just_done = 0;
-    SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
     e.n_active -= 1;
     e.retired += 1;
     *n_finished += 1;
+    if (e.hold && it != e.reqs.end()) {
+      s.kind = -2;
+      s.just_done = 0;
+      SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+    } else {
+      SG_TRY(release_col(c, col));
+    }
   }
   while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
   return sync(c);
@@ -1057,7 +1076,13 @@ extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) 
     SG_TRY(engine_admit(c));
     SG_TRY(engine_retire_immediate(c, &fin));
     if (fin > 0) break;
-    if (e.n_active == 0) break;
+    if (e.n_active == 0) {
+      if (!e.queue.empty())
+        return set_err(c, SG_ERR_STATE,
+                       "engine full: %lld queued columns wait for columns that hold unconsumed results",
+                       (long long)e.queue.size());
+      break;
+    }
     SG_TRY(engine_step(c, &fin));
     if (fin > 0) break;
   }
@@ -1175,6 +1200,12 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
   return sync(c);
 }
 
+extern "C" int sg_engine_hold_results(sg_ctx* c, int hold) {
+  if (!c) return SG_ERR_INVALID;
+  c->eng.hold = hold != 0;
+  return SG_OK;
+}
+
 extern "C" int sg_engine_poll(sg_ctx* c, int64_t* ids, int64_t max_ids, int64_t* n_out) {
   if (!c || !n_out || (max_ids > 0 && !ids)) return SG_ERR_INVALID;
   Engine& e = c->eng;
@@ -1229,8 +1260,8 @@ int run_until(sg_ctx* c, const std::vector<int64_t>& ids) {
     int64_t fin = 0;
     const int64_t before = e.steps;
     SG_TRY(sg_engine_run(c, 1 << 20, &fin));
-    if (fin == 0 && e.steps == before && e.n_active == 0 && e.queue.empty())
-      return set_err(c, SG_ERR_STATE, "engine idle with unfinished requests");
+    if (fin == 0 && e.steps == before)
+      return set_err(c, SG_ERR_STATE, "engine made no progress with unfinished requests");
   }
 }
 

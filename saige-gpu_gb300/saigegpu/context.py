@@ -377,6 +377,9 @@ class Context:
     def engine_cancel(self, rid):
         self._call("sg_engine_cancel", int(rid))
 
+    def engine_hold_results(self, hold=True):
+        self._call("sg_engine_hold_results", int(bool(hold)))
+
     def engine_poll(self, max_ids=1 << 16):
         ids = np.empty(max_ids, np.int64)
         n = C.c_int64()

@@ -272,10 +272,15 @@ class _Job:
 class Runner:
     """Continuous batching of many null-model fits over one engine."""
 
-    def __init__(self, ctx, max_columns=2048, max_phenos=64):
+    def __init__(self, ctx, max_columns=2048, max_phenos=64, min_columns_per_fit=2 * (30 + 10) + 8):
+        if max_columns < min_columns_per_fit:
+            # a fit's trace stage keeps ~2 (nrun + 10) + 4 columns in flight at once
+            raise ValueError("max_columns=%d is below one fit's working set (%d)" % (max_columns, min_columns_per_fit))
         self.ctx = ctx
         self.n = ctx.n
         ctx.engine_reserve(max_columns, max_phenos)
+        if hasattr(ctx, "engine_hold_results"):
+            ctx.engine_hold_results(True)  # probe results are reduced on the device, not copied
         self.max_columns = max_columns
         self.free_slots = list(range(max_phenos))[::-1]
         self.jobs = {}

@@ -26,6 +26,33 @@ def test_grm_fp32_matches_oracle(cohort):
     assert err < 2e-6, err
 
 
+def test_grm_matmul_more_columns_than_the_engine_holds(cohort):
+    ctx, grm = cohort
+    V = np.random.default_rng(1).standard_normal((grm.n, 300))
+    Y = ctx.grm_matmul(V)
+    ref = grm.K @ V
+    assert np.abs(Y - ref).max() / np.abs(ref).max() < 5e-6
+
+
+def test_full_engine_fails_loudly(cohort):
+    """Held results that nobody consumes make the engine report SG_ERR_STATE instead of waiting."""
+    from saigegpu import SaigeGpuError
+    ctx, grm = cohort
+    n = grm.n
+    ctx.engine_reserve(32, 1)
+    ctx.engine_set_pheno(0, np.full(n, 0.2), np.array([1.0, 0.3]))
+    ctx.engine_hold_results(True)
+    try:
+        ids = ctx.engine_submit(0, 1, np.ones((n, 40)), 1, 0.0)
+        with pytest.raises(SaigeGpuError):
+            for _ in range(10):
+                ctx.engine_run(1)
+        for i in ids:
+            ctx.engine_cancel(int(i))
+    finally:
+        ctx.engine_hold_results(False)
+
+
 def test_grm_matmul(cohort):
     ctx, grm = cohort
     rng = np.random.default_rng(0)
