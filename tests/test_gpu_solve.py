@@ -34,23 +34,23 @@ def test_grm_matmul_more_columns_than_the_engine_holds(cohort):
     assert np.abs(Y - ref).max() / np.abs(ref).max() < 5e-6
 
 
-def test_full_engine_fails_loudly(cohort):
+def test_full_engine_fails_loudly():
     """Held results that nobody consumes make the engine report SG_ERR_STATE instead of waiting."""
-    from saigegpu import SaigeGpuError
-    ctx, grm = cohort
-    n = grm.n
-    ctx.engine_reserve(32, 1)
-    ctx.engine_set_pheno(0, np.full(n, 0.2), np.array([1.0, 0.3]))
-    ctx.engine_hold_results(True)
-    try:
+    from saigegpu import Context, SaigeGpuError
+    n, m = 200, 300
+    bed, _ = synth.synth_bed(3, n, m, 0.0)
+    with Context(0) as ctx:
+        ctx.setgeno(bed, n, m)
+        ctx.grm_build(GRM_FP32_SIMT)
+        ctx.engine_reserve(32, 1)
+        ctx.engine_set_pheno(0, np.full(n, 0.2), np.array([1.0, 0.3]))
+        ctx.engine_hold_results(True)
         ids = ctx.engine_submit(0, 1, np.ones((n, 40)), 1, 0.0)
         with pytest.raises(SaigeGpuError):
             for _ in range(10):
                 ctx.engine_run(1)
-        for i in ids:
+        for i in ids[:5]:
             ctx.engine_cancel(int(i))
-    finally:
-        ctx.engine_hold_results(False)
 
 
 def test_grm_matmul(cohort):
