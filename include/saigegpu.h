@@ -140,6 +140,16 @@ int sg_grm_matmul_tf32x3_noalloc(sg_ctx *ctx, const float *P_dev, int64_t ncols,
 /* GRM row count padded to the tile size (the leading dimension of device-side vector blocks). */
 int sg_grm_padded_n(sg_ctx *ctx, int64_t *np);
 
+/* Leave one chromosome out: GRM markers [begin, end] (0-based, inclusive, in GRM-marker order) leave
+ * the GRM for every later product and preconditioner until sg_loco_clear.  Replaces
+ * setStartEndIndex (FIT.cpp:3067-3085) + parallelCrossProd_LOCO (FIT.cpp:1790-1851) +
+ * getDiagOfSigma_LOCO (FIT.cpp:2370-2392): K_-j P = (M K P - Z_j Z_j' P) / (M - M_j) with the
+ * chromosome's standardised genotypes in FP32, and diag minus its sum z^2.  The _LOCO drop-ins of
+ * the reference (getCoefficients_LOCO, getPCG1ofSigmaAndVector_LOCO, ...) are the plain drop-ins
+ * called while a range is set.  Phenotype slots read the diagonal when set, so (re)set them after. */
+int sg_loco_set(sg_ctx *ctx, int64_t begin, int64_t end);
+int sg_loco_clear(sg_ctx *ctx);
+
 /* ------------------------------------------------------------ drop-ins for the Rcpp entry points */
 /* getCrossprodMatAndKin (FIT.cpp:1953-1981; RcppExports.cpp:664-671) */
 int sg_getCrossprodMatAndKin(sg_ctx *ctx, const float *b, float *out);

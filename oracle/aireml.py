@@ -450,3 +450,22 @@ def variance_ratio(grm, fit, trait, X, vr_geno, order, num_markers=30, ratio_cv_
             continue
         break
     return float(np.mean(ratios)), np.array(ratios)
+
+
+def loco_grm(grm, geno, begin, end):
+    """GRM with GRM markers [begin, end] left out (parallelCrossProd_LOCO FIT.cpp:1790-1851 and
+    getDiagOfSigma_LOCO FIT.cpp:2370-2392): (Z'Z - Z_j'Z_j) / (M - M_j), diag minus sum_j z^2."""
+    zj = plink.std_geno(geno)[begin:end + 1].astype(np.float64)
+    mj = zj.shape[0]
+    m = grm.m_qc
+    K = (grm.K * m - zj.T @ zj) / (m - mj)
+    return DenseGRM.from_matrix(K, m - mj, grm.diag_sum - (zj * zj).sum(axis=0), grm.is_diag_one)
+
+
+def get_coef_loco(grm_loco, fit0, fit, trait, maxiter_pcg=500, tol_pcg=1e-5, maxiter=20):
+    """Get_Coef_LOCO (FIT.R:40-73) from the full fit's tau, alpha and eta (FIT.R:254-297)."""
+    fam = Binomial() if trait == "binary" else Gaussian()
+    n = len(fit0["y"])
+    offset = np.zeros(n) if fit0.get("offset") is None else np.asarray(fit0["offset"], np.float64)
+    return get_coef(grm_loco, fit0["y"], fit0["X"], fit["theta"], fam, fit["coefficients"],
+                    fit["linear_predictors"], offset, maxiter_pcg, tol_pcg, maxiter)

@@ -100,6 +100,15 @@ struct sg_ctx {
   float* d_diag32 = nullptr;
   std::vector<double> diag;
   std::vector<float> diag32;
+  // leave-one-chromosome-out state (setStartEndIndex, FIT.cpp:3067-3085)
+  bool loco = false;
+  int64_t loco_begin = 0, loco_end = -1, loco_mj = 0, loco_mjp = 0;
+  float* d_zm = nullptr;   // Z_j marker-major (mjp x np)
+  float* d_zs = nullptr;   // Z_j sample-major (np x mjp)
+  float* d_lu = nullptr;   // Z_j' P  (cap_cols x mjp)
+  float* d_lv = nullptr;   // Z_j Z_j' P (cap_cols x np)
+  float* d_lp = nullptr;   // P in full FP32 for the correction (cap_cols x np)
+  std::vector<double> diag_loco;
   // synthetic bed image
   uint8_t* d_synth = nullptr;
   uint64_t synth_len = 0;
@@ -258,8 +267,11 @@ extern "C" int sg_kernel_launches(const sg_ctx* c, uint64_t* count) {
 // ------------------------------------------------------------------ genotypes
 static void engine_free(sg_ctx* c);
 
+static void loco_free(sg_ctx* c);
+
 static void free_geno(sg_ctx* c) {
   engine_free(c);
+  loco_free(c);
   dev_free_t(c, c->d_packed);
   dev_free_t(c, c->d_packed_vr);
   dev_free_t(c, c->d_lut);
@@ -557,6 +569,7 @@ extern "C" int sg_grm_build(sg_ctx* c, int precision) {
   dev_free_t(c, c->d_Klo);
   c->k_split = false;
   engine_free(c);
+  loco_free(c);
   c->have_grm = false;
   const int64_t np = round_up(c->nn, kRowTile);
   const int64_t mp = round_up(c->m_qc, kMarkerTile);
@@ -668,6 +681,9 @@ static void engine_free(sg_ctx* c) {
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
   e.finished.clear();
+  dev_free_t(c, c->d_lu);
+  dev_free_t(c, c->d_lv);
+  dev_free_t(c, c->d_lp);
   e.hi_col = 0;
   e.n_active = 0;
   e.queue.clear();
@@ -759,11 +775,14 @@ extern "C" int sg_engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phe
   return engine_reserve(c, max_columns, max_phenos);
 }
 
-// getDiagOfSigma in FP64 (FIT.cpp:2322-2365) for the Jacobi preconditioner
+// getDiagOfSigma in FP64 (FIT.cpp:2322-2365) for the Jacobi preconditioner; with a chromosome left
+// out, getDiagOfSigma_LOCO (FIT.cpp:2370-2392): diag minus the chromosome's sum z^2, over M - M_j.
 static void diag_sigma_f64(const sg_ctx* c, const double* w, const double* tau, double* d) {
+  const bool loco = c->loco && !c->is_diag_one;
+  const double m = loco ? (double)(c->m_qc - c->loco_mj) : (double)c->m_qc;
   for (int64_t i = 0; i < c->nn; ++i) {
-    double v = c->is_diag_one ? tau[1] + tau[0] / w[i]
-                              : tau[1] * c->diag[i] / (double)c->m_qc + tau[0] / w[i];
+    const double dk = loco ? c->diag_loco[i] : c->diag[i];
+    double v = c->is_diag_one ? tau[1] + tau[0] / w[i] : tau[1] * dk / m + tau[0] / w[i];
     d[i] = v < 1e-4 ? 1e-4 : v;
   }
 }
@@ -911,7 +930,16 @@ static int engine_admit(sg_ctx* c) {
   return SG_OK;
 }
 
+static int loco_correct(sg_ctx* c, int64_t ncols, bool yf);
+static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf);
+
 static int engine_gemm(sg_ctx* c, int64_t ncols, bool* used_yf) {
+  SG_TRY(engine_gemm_full(c, ncols, used_yf));
+  if (c->loco) SG_TRY(loco_correct(c, ncols, *used_yf));
+  return SG_OK;
+}
+
+static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf) {
   Engine& e = c->eng;
   *used_yf = true;
   if (c->mv_mode == SG_MV_FP64_PLAIN) {
@@ -1241,6 +1269,99 @@ extern "C" int sg_engine_stats(sg_ctx* c, int64_t* s4) {
   s4[1] = c->eng.retired;
   s4[2] = c->eng.col_iters;
   s4[3] = c->eng.grm_passes;
+  return SG_OK;
+}
+
+// ------------------------------------------------------------------ leave one chromosome out
+static void loco_free(sg_ctx* c) {
+  dev_free_t(c, c->d_zm);
+  dev_free_t(c, c->d_zs);
+  dev_free_t(c, c->d_lu);
+  dev_free_t(c, c->d_lv);
+  dev_free_t(c, c->d_lp);
+  c->loco = false;
+  c->loco_mj = c->loco_mjp = 0;
+}
+
+// Y <- (M Y - Z_j (Z_j' P)) / (M - M_j): parallelCrossProd_LOCO (FIT.cpp:1790-1851) on the resident K.
+static int loco_correct(sg_ctx* c, int64_t ncols, bool yf) {
+  Engine& e = c->eng;
+  if (!c->d_lu) SG_TRY(dev_alloc_t(c, &c->d_lu, (size_t)(e.cap_cols * c->loco_mjp)));
+  if (!c->d_lv) SG_TRY(dev_alloc_t(c, &c->d_lv, (size_t)(e.cap_cols * e.np)));
+  const int64_t nc = round_up(ncols, kRowTile);  // the SIMT GEMM's row tile; rows past ncols read zero Pf
+  if (nc > e.cap_cols) return set_err(c, SG_ERR_STATE, "LOCO needs engine capacity in multiples of 128 columns");
+  // the correction needs P in full FP32: the split engine keeps P = Pf (tf32 high) + Pflo, the
+  // plain FP64 engine keeps P in FP64
+  const float* P = e.Pf;
+  if (c->mv_mode == SG_MV_FP64_PLAIN || c->mv_mode == SG_MV_TF32X3_TC) {
+    if (!c->d_lp) {
+      SG_TRY(dev_alloc_t(c, &c->d_lp, (size_t)(e.cap_cols * e.np)));
+      SG_CUDA(c, cudaMemsetAsync(c->d_lp, 0, (size_t)(e.cap_cols * e.np) * 4, c->stream));
+    }
+    if (c->mv_mode == SG_MV_FP64_PLAIN) {
+      launch_f64_to_f32(e.P, c->d_lp, ncols * e.np, c->stream);
+    } else {
+      SG_CUDA(c, cudaMemcpyAsync(c->d_lp, e.Pf, ncols * e.np * 4, cudaMemcpyDeviceToDevice, c->stream));
+      add_inplace_kernel<<<(unsigned)((ncols * e.np + 255) / 256), 256, 0, c->stream>>>(c->d_lp, e.Pflo, ncols * e.np);
+    }
+    c->launches += 1;
+    P = c->d_lp;
+  }
+  // U (nc x mjp) = P Z_j' ; V (ncols x np, stored transposed) = Z_j U'
+  launch_gemm_nt_f32(P, e.np, c->d_zm, e.np, c->d_lu, c->loco_mjp, nc, c->loco_mjp, e.np, 1.0f, 0, c->stream);
+  launch_gemm_nt_f32(c->d_zs, c->loco_mjp, c->d_lu, c->loco_mjp, c->d_lv, e.np, e.np, ncols, c->loco_mjp, 1.0f, 1, c->stream);
+  const double M = (double)c->m_qc;
+  launch_loco_combine(yf ? e.Yf : nullptr, yf ? nullptr : e.Yd, c->d_lv, M, 1.0 / (M - (double)c->loco_mj),
+                      ncols * e.np, c->stream);
+  SG_LAUNCHED(c, 3);
+  return SG_OK;
+}
+
+extern "C" int sg_loco_set(sg_ctx* c, int64_t begin, int64_t end) {
+  NEED_GRM(c);
+  if (begin < 0 || end < begin || end >= c->m_qc)
+    return set_err(c, SG_ERR_INVALID, "LOCO range [%lld, %lld] outside the %lld GRM markers", (long long)begin,
+                   (long long)end, (long long)c->m_qc);
+  if (end - begin + 1 >= c->m_qc) return set_err(c, SG_ERR_INVALID, "LOCO range covers every GRM marker");
+  for (auto& kv : c->eng.reqs)
+    if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");
+  loco_free(c);
+  const int64_t mj = end - begin + 1;
+  const int64_t mjp = round_up(mj, kRowTile);
+  const int64_t np = c->np;
+  SG_TRY(dev_alloc_t(c, &c->d_zm, (size_t)(mjp * np)));
+  SG_TRY(dev_alloc_t(c, &c->d_zs, (size_t)(np * mjp)));
+  const uint8_t* pk = c->d_packed + begin * c->pitch;
+  const float* lut = c->d_lut + 4 * begin;
+  launch_zbuild_marker_major(pk, c->pitch, lut, mj, mjp, c->nn, np, c->d_zm, c->stream);
+  launch_zbuild_f32(pk, c->pitch, lut, mj, c->nn, np, mjp, c->d_zs, c->stream);
+  // the chromosome's diagonal contribution (set_Diagof_StdGeno_LOCO, FIT.cpp:4934-4959)
+  double* dj = nullptr;
+  float* dj32 = nullptr;
+  SG_TRY(dev_alloc_t(c, &dj, (size_t)c->nn));
+  SG_TRY(dev_alloc_t(c, &dj32, (size_t)c->nn));
+  launch_diag(pk, c->pitch, lut, mj, c->nn, dj, dj32, c->stream);
+  SG_LAUNCHED(c, 3);
+  std::vector<double> h(c->nn);
+  SG_CUDA(c, cudaMemcpyAsync(h.data(), dj, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
+  SG_TRY(sync(c));
+  dev_free(c, dj);
+  dev_free(c, dj32);
+  c->diag_loco.resize(c->nn);
+  for (int64_t i = 0; i < c->nn; ++i) c->diag_loco[i] = c->diag[i] - h[i];
+  c->loco_begin = begin;
+  c->loco_end = end;
+  c->loco_mj = mj;
+  c->loco_mjp = mjp;
+  c->loco = true;
+  return SG_OK;
+}
+
+extern "C" int sg_loco_clear(sg_ctx* c) {
+  if (!c) return SG_ERR_INVALID;
+  for (auto& kv : c->eng.reqs)
+    if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");
+  loco_free(c);
   return SG_OK;
 }
 

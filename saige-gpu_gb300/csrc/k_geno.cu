@@ -248,6 +248,45 @@ void launch_zbuild_bf16(const uint8_t* packed, int64_t pitch, const float* lut4,
                                                    (__nv_bfloat16*)Zhi, (__nv_bfloat16*)Zlo);
 }
 
+// Marker-major standardised genotypes Zm (m_rows x np, samples contiguous), zero past nn and for
+// padding rows >= m (LOCO correction operand).
+__global__ void zbuild_marker_major_kernel(const uint8_t* __restrict__ packed, int64_t pitch,
+                                           const float* __restrict__ lut4, int64_t m, int64_t nn,
+                                           int64_t np, float* __restrict__ Zm) {
+  const int64_t row = blockIdx.y;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  float z = 0.0f;
+  if (row < m && i < nn) {
+    const uint32_t f = (packed[row * pitch + (i >> 2)] >> (2 * (i & 3))) & 3u;
+    z = lut4[4 * row + field_geno(f)];
+  }
+  Zm[row * np + i] = z;
+}
+
+void launch_zbuild_marker_major(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m,
+                                int64_t m_rows, int64_t nn, int64_t np, float* Zm, cudaStream_t s) {
+  if (m_rows == 0) return;
+  dim3 grid((unsigned)((np + 255) / 256), (unsigned)m_rows);
+  zbuild_marker_major_kernel<<<grid, 256, 0, s>>>(packed, pitch, lut4, m, nn, np, Zm);
+}
+
+// Y = (a * Y - V) * b elementwise over ncols x np (LOCO: (M K P - Z_j Z_j' P) / (M - M_j))
+__global__ void loco_combine_f32_kernel(float* Y, const float* __restrict__ V, float a, float b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) Y[i] = (a * Y[i] - V[i]) * b;
+}
+__global__ void loco_combine_f64_kernel(double* Y, const float* __restrict__ V, double a, double b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) Y[i] = (a * Y[i] - (double)V[i]) * b;
+}
+void launch_loco_combine(float* Yf, double* Yd, const float* V, double a, double b, int64_t n,
+                         cudaStream_t s) {
+  if (n == 0) return;
+  if (Yf) loco_combine_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(Yf, V, (float)a, (float)b, n);
+  else loco_combine_f64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(Yd, V, a, b, n);
+}
+
 // ----------------------------------------------------------------------------
 // GRM diagonal sum_m z^2 (Get_Diagof_StdGeno FIT.cpp:665-704): one thread per
 // sample, markers in order; FP32 accumulation rounded exactly as the

@@ -56,6 +56,10 @@ void launch_synth_bed(uint64_t seed, int64_t n, int64_t m, uint32_t miss_thr16, 
                       cudaStream_t s);
 void launch_genetic_value(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
                           int64_t nn, uint64_t seed, double* out, cudaStream_t s);
+void launch_zbuild_marker_major(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m,
+                                int64_t m_rows, int64_t nn, int64_t np, float* Zm, cudaStream_t s);
+void launch_loco_combine(float* Yf, double* Yd, const float* V, double a, double b, int64_t n,
+                         cudaStream_t s);
 void launch_unpack_marker(const uint8_t* packed_row, int64_t nn, const float* lut4, int32_t* g,
                           float* z, cudaStream_t s);
 

@@ -200,6 +200,13 @@ class Context:
         out = out.reshape(k, self.n).T
         return out[:, 0] if single else out
 
+    def loco_set(self, begin, end):
+        """Leave GRM markers [begin, end] out (setStartEndIndex); the engine must be idle."""
+        self._call("sg_loco_set", int(begin), int(end))
+
+    def loco_clear(self):
+        self._call("sg_loco_clear")
+
     # ------------------------------------------------------------ Rcpp drop-ins
     def getCrossprodMatAndKin(self, b):
         b = _f32(b)

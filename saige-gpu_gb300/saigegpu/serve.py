@@ -252,6 +252,96 @@ def fit_generator(spec, n_cohort, probes):
                 cov=rc["cov"], converged=it_used < spec.maxiter, iterations=it_used, n=n)
 
 
+def loco_generator(spec, fit, n_cohort):
+    """Get_Coef_LOCO (FIT.R:40-73) for one phenotype while the engine leaves a chromosome out,
+    started from the full fit's tau, alpha and eta (FIT.R:254-297)."""
+    fam = family_of("binomial" if spec.trait == "binary" else "gaussian")
+    m = np.ones(n_cohort, bool) if spec.mask is None else spec.mask
+    idx = np.nonzero(m)[0]
+    f0 = spec.fit0
+
+    def full(v):
+        out = np.zeros(n_cohort)
+        out[idx] = v
+        return out
+
+    y = full(f0["y"])
+    X = np.zeros((n_cohort, f0["X"].shape[1]))
+    X[idx] = f0["X"]
+    offset = full(np.zeros(len(idx)) if f0.get("offset") is None else f0["offset"])
+    tau = np.asarray(fit["theta"], np.float64)
+    alpha0 = np.asarray(fit["coefficients"], np.float64)
+    eta0 = full(fit["linear_predictors"])
+
+    def working(eta_):
+        mu = fam.linkinv(eta_)
+        mu_eta = fam.mu_eta(eta_)
+        Y = np.where(m, eta_ - offset + (y - mu) / mu_eta, 0.0)
+        W = np.where(m, (mu_eta / np.sqrt(fam.variance(mu))) ** 2, 1.0)
+        return mu, Y, W
+
+    mu, Y, W = working(eta0)
+    for _ in range(spec.maxiter):
+        yield ("pheno", W, tau)
+        S = yield from _solve(np.column_stack([Y, X]), spec.maxiter_pcg, spec.tol_pcg)
+        SY, SX = S[:, 0], S[:, 1:]
+        cov = _inv_sympd(X.T @ SX)
+        al = cov @ (SX.T @ Y)
+        et = np.where(m, Y - tau[0] * (SY - SX @ al) / W, 0.0) + offset
+        mu, Y, W = working(et)
+        if np.max(np.abs(al - alpha0) / (np.abs(al) + np.abs(alpha0) + 0.1)) < 0.1:
+            break
+        alpha0 = al
+    return dict(isLOCO=True, coefficients=al, linear_predictors=et[idx], fitted_values=mu[idx],
+                Y=Y[idx], residuals=(y - mu)[idx], cov=cov)
+
+
+def loco_ranges(chrom_of_grm_markers):
+    """Per-autosome [begin, end] of the GRM markers (updateChrStartEndIndexVec, Util.R:29-65);
+    None for chromosomes without markers.  Markers must be ordered by chromosome."""
+    chrom = np.asarray(chrom_of_grm_markers)
+    out = {}
+    last_end = -1
+    for c in range(1, 23):
+        w = np.nonzero(chrom == c)[0]
+        if len(w) == 0:
+            out[c] = None
+            continue
+        b, e = int(w.min()), int(w.max())
+        if b <= last_end:
+            raise ValueError("chromosomes need to be ordered from 1 to 22 in the bim file")
+        last_end = e
+        out[c] = (b, e)
+    return out
+
+
+def fit_loco(ctx, specs, fits, ranges, max_columns=1024):
+    """LOCO results per chromosome for fitted phenotypes: {chrom: [result or None per spec]}."""
+    out = {}
+    for c, rng in ranges.items():
+        if rng is None:
+            out[c] = [dict(isLOCO=False) for _ in specs]
+            continue
+        ctx.loco_set(rng[0], rng[1])
+        try:
+            r = Runner(ctx, max_columns, max(1, len(specs)))
+            ids = []
+            for spec, fit in zip(specs, fits):
+                jid = r._next
+                r._next += 1
+                slot = r.free_slots.pop()
+                job = _Job(jid, spec, loco_generator(spec, fit, r.n), slot, time.perf_counter())
+                r.jobs[jid] = job
+                r._advance(job, None)
+                ids.append(jid)
+            r.run()
+            by = {j.jid: j for j in r.finished}
+            out[c] = [by[i].result if by[i].error is None else by[i].error for i in ids]
+        finally:
+            ctx.loco_clear()
+    return out
+
+
 # ------------------------------------------------------------------ runner
 
 
