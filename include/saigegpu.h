@@ -62,6 +62,10 @@ void sg_ctx_destroy(sg_ctx *ctx);
 const char *sg_last_error(const sg_ctx *ctx);
 int sg_device_bytes_in_use(const sg_ctx *ctx, uint64_t *bytes);
 int sg_set_matvec_mode(sg_ctx *ctx, int mode);
+/* Tuning: how many CTAs (1, 2 or 4) of a thread-block cluster share one B tile through TMA multicast
+ * in the tcgen05 SYRK and split-TF32 GRM.V (process-wide; saigegpu.tune picks them by timing). */
+int sg_set_tc_clusters(sg_ctx *ctx, int syrk, int grmv);
+int sg_get_tc_clusters(sg_ctx *ctx, int *syrk, int *grmv);
 /* GPU kernel launches issued by this context so far (for accounting). */
 int sg_kernel_launches(const sg_ctx *ctx, uint64_t *count);
 

@@ -258,6 +258,18 @@ extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
   return SG_OK;
 }
 
+extern "C" int sg_set_tc_clusters(sg_ctx* c, int syrk, int grmv) {
+  if (!c) return SG_ERR_INVALID;
+  if (!tc_set_clusters(syrk, grmv)) return set_err(c, SG_ERR_INVALID, "cluster sizes must be 1, 2 or 4");
+  return SG_OK;
+}
+
+extern "C" int sg_get_tc_clusters(sg_ctx* c, int* syrk, int* grmv) {
+  if (!c || !syrk || !grmv) return SG_ERR_INVALID;
+  tc_get_clusters(syrk, grmv);
+  return SG_OK;
+}
+
 extern "C" int sg_kernel_launches(const sg_ctx* c, uint64_t* count) {
   if (!c || !count) return SG_ERR_INVALID;
   *count = c->launches;

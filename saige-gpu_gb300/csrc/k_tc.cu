@@ -138,6 +138,35 @@ __device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, ui
   }
 }
 
+// Multicast variant: the box lands at the same shared-memory offset in every CTA of ``mask``
+// and completes transaction bytes on the mbarrier at the same offset in each of them.
+__device__ __forceinline__ void tma_load_2d_mcast(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                                  int32_t x, int32_t y, uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1, {%4, %5}], [%2], %3;"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "h"(mask),
+        "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Arrive once on the mbarrier at this offset in every CTA of ``mask`` when the prior MMAs complete.
+__device__ __forceinline__ void umma_commit_mcast(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+      ::"r"(smem_u32(bar)), "h"(mask) : "memory");
+}
+
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                ::"r"(smem_u32(bar)) : "memory");
@@ -162,12 +191,20 @@ struct TileCoord {
 };
 
 // kSplit: A = [Ah | Al], B = [Bh | Bl] (second maps); accumulates Ah Bh + Ah Bl + Al Bh.
-template <bool kTF32, int BN, int S, bool kSplit>
+// kC > 1: the kC CTAs of a cluster own consecutive row blocks of the same column block and share
+// its B tile -- CTA r loads rows [r*BN/kC, (r+1)*BN/kC) of it and multicasts them to all kC, which
+// cuts the L2->SM operand traffic of B by kC.  Each stage is then refilled only when every CTA of
+// the cluster has consumed it (the empty barrier counts kC multicast MMA commits).
+// Rows >= nrows of a tile (a padding row block that completes the last cluster) are not stored.
+template <bool kTF32, int BN, int S, bool kSplit, int kC>
 __global__ void __launch_bounds__(128, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
                const TileCoord* __restrict__ tiles, int num_kb, float* __restrict__ D, int64_t ldd,
-               float scale, int mode) {
+               float scale, int mode, int64_t nrows) {
+  static_assert(kC == 1 || (BN / kC) % 8 == 0, "B slices must be whole 8-row swizzle atoms");
+  constexpr int kSliceRows = BN / kC;
+  constexpr int kSliceBytes = kSliceRows * kRowBytes;
   constexpr int kBTileBytes = BN * kRowBytes;
   constexpr int kStageBytes = (kATileBytes + kBTileBytes) * (kSplit ? 2 : 1);
   constexpr uint32_t kFmt = kTF32 ? 2u : 1u;
@@ -187,10 +224,12 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   const int lane = threadIdx.x & 31;
   const TileCoord tc = tiles[blockIdx.x];
 
+  const uint32_t crank = kC > 1 ? cluster_rank() : 0u;
+  constexpr uint16_t kMask = (uint16_t)((1u << kC) - 1u);
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], kC);
     }
     mbar_init(accum, 1);
     *abort_flag = 0;
@@ -204,6 +243,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  if constexpr (kC > 1) cluster_sync();  // every CTA's barriers exist before any peer multicasts
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem_base = *tmem_slot;
 
@@ -218,10 +258,20 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
       mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
       const int32_t x = kb * (kRowBytes / (kTF32 ? 4 : 2));
       tma_load_2d(st, &mapA, &full[s], x, ya);
-      tma_load_2d(st + kATileBytes, &mapB, &full[s], x, yb);
+      if constexpr (kC == 1) {
+        tma_load_2d(st + kATileBytes, &mapB, &full[s], x, yb);
+      } else {
+        tma_load_2d_mcast(st + kATileBytes + crank * kSliceBytes, &mapB, &full[s], x,
+                          yb + (int32_t)crank * kSliceRows, kMask);
+      }
       if constexpr (kSplit) {
         tma_load_2d(st + kATileBytes + kBTileBytes, &mapA2, &full[s], x, ya);
-        tma_load_2d(st + 2 * kATileBytes + kBTileBytes, &mapB2, &full[s], x, yb);
+        if constexpr (kC == 1) {
+          tma_load_2d(st + 2 * kATileBytes + kBTileBytes, &mapB2, &full[s], x, yb);
+        } else {
+          tma_load_2d_mcast(st + 2 * kATileBytes + kBTileBytes + crank * kSliceBytes, &mapB2, &full[s], x,
+                            yb + (int32_t)crank * kSliceRows, kMask);
+        }
       }
     }
   } else if (warp == 1 && lane == 0) {
@@ -244,7 +294,9 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
           umma<kTF32>(tmem_base, smem_desc_sw128(a1 + 32 * k), smem_desc_sw128(b0 + 32 * k), kIdesc, 1u);
         }
       }
-      umma_commit(&empty[s]);  // stage reusable once these MMAs have read it
+      // stage reusable once these MMAs have read it (in every CTA of the cluster)
+      if constexpr (kC == 1) umma_commit(&empty[s]);
+      else umma_commit_mcast(&empty[s], kMask);
     }
     umma_commit(accum);
   }
@@ -255,7 +307,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   __syncwarp();
   go = __shfl_sync(0xffffffffu, go, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (go) {
+  if (go && (int64_t)tc.bm * kTileM < nrows) {
     const int64_t r = (int64_t)tc.bm * kTileM + warp * 32 + lane;
     const uint32_t trow = tmem_base + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
@@ -281,6 +333,8 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  // no CTA leaves while a peer may still multicast into its shared memory or arrive on its barriers
+  if constexpr (kC > 1) cluster_sync();
   if (warp == 2) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kTmemCols)
                  : "memory");
@@ -323,15 +377,29 @@ constexpr size_t smem_bytes() {
   return (size_t)S * (kATileBytes + BN * kRowBytes) * (kSplit ? 2 : 1) + 1024 + 256;
 }
 
-template <bool kTF32, int BN, int S, bool kSplit>
+template <bool kTF32, int BN, int S, bool kSplit, int kC = 1>
 cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
                    const CUtensorMap& b2, const TileCoord* tiles, int ntiles, int num_kb, float* D,
-                   int64_t ldd, float scale, int mode, cudaStream_t s) {
-  auto k = tc_gemm_kernel<kTF32, BN, S, kSplit>;
+                   int64_t ldd, float scale, int mode, cudaStream_t s, int64_t nrows) {
+  auto k = tc_gemm_kernel<kTF32, BN, S, kSplit, kC>;
   const size_t sm = smem_bytes<kTF32, BN, S, kSplit>();
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k<<<ntiles, 128, sm, s>>>(a, b, a2, b2, tiles, num_kb, D, ldd, scale, mode);
+  if (ntiles % kC != 0) return cudaErrorInvalidValue;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ntiles);
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kC;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = kC > 1 ? 1 : 0;
+  e = cudaLaunchKernelEx(&cfg, k, a, b, a2, b2, tiles, num_kb, D, ldd, scale, mode, nrows);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
@@ -400,35 +468,66 @@ bool tc_available() {
   return major == 10 && minor == 3 && encode_fn() != nullptr;
 }
 
+// Cluster sizes (CTAs sharing one B tile by TMA multicast) of the SYRK and the split GRM.V.
+static int g_cluster_syrk = 1;
+static int g_cluster_grmv = 1;
+
+bool tc_set_clusters(int syrk, int grmv) {
+  auto ok = [](int c) { return c == 1 || c == 2 || c == 4; };
+  if (!ok(syrk) || !ok(grmv)) return false;
+  g_cluster_syrk = syrk;
+  g_cluster_grmv = grmv;
+  return true;
+}
+void tc_get_clusters(int* syrk, int* grmv) {
+  *syrk = g_cluster_syrk;
+  *grmv = g_cluster_grmv;
+}
+
 cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t mp, float* K,
                          float scale, cudaStream_t s) {
   constexpr int BN = 256;
   if (np % kTileM != 0 || mp % 64 != 0) return cudaErrorInvalidValue;
+  const int C = g_cluster_syrk;
   CUtensorMap a, b, a2, b2;
   const uint64_t rb = (uint64_t)mp * 2;
-  if (!make_map(&a, Zhi, false, mp, np, rb, kTileM) || !make_map(&b, Zhi, false, mp, np, rb, BN))
+  const uint32_t brows = (uint32_t)(BN / C);  // each CTA of a cluster loads its slice of B
+  if (!make_map(&a, Zhi, false, mp, np, rb, kTileM) || !make_map(&b, Zhi, false, mp, np, rb, brows))
     return cudaErrorInvalidValue;
   a2 = a;
   b2 = b;
-  if (Zlo && (!make_map(&a2, Zlo, false, mp, np, rb, kTileM) || !make_map(&b2, Zlo, false, mp, np, rb, BN)))
+  if (Zlo && (!make_map(&a2, Zlo, false, mp, np, rb, kTileM) || !make_map(&b2, Zlo, false, mp, np, rb, brows)))
     return cudaErrorInvalidValue;
-  // lower-triangle tiles: column block bn (BN wide) starts at or before the row block's last row;
-  // column blocks past np are not formed (np % BN may be 128: the last block is then half empty,
-  // and its TMA rows past np read zero fill).
+  // Lower-triangle tiles: column block bn (BN wide) starts at or before the last row of the row
+  // block.  With clusters, C consecutive row blocks share each column block (the union of their
+  // column blocks; tiles fully above a row block's diagonal store nothing), and a trailing group is
+  // padded with row blocks past np (zero-filled loads, nothing stored).
   static TileCache cache;
   cache.host.clear();
   const int64_t nbm = np / kTileM;
-  const int64_t nbn = (np + BN - 1) / BN;
-  for (int64_t bm = 0; bm < nbm; ++bm)
-    for (int64_t bn = 0; bn < nbn; ++bn)
-      if (bn * BN <= bm * kTileM + kTileM - 1) cache.host.push_back(TileCoord{(int32_t)bm, (int32_t)bn});
+  const int64_t ngroups = (nbm + C - 1) / C;
+  for (int64_t gi = 0; gi < ngroups; ++gi) {
+    const int64_t last_row = (gi * C + C - 1) * kTileM + kTileM - 1;
+    for (int64_t bn = 0; bn * BN <= last_row && bn * BN < np; ++bn)
+      for (int r = 0; r < C; ++r) cache.host.push_back(TileCoord{(int32_t)(gi * C + r), (int32_t)bn});
+  }
   cudaError_t e = upload_tiles(cache, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(mp / 64);
-  if (Zlo)
-    e = launch<false, BN, 2, true>(a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, K, np, scale, 2, s);
-  else
-    e = launch<false, BN, 4, false>(a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, K, np, scale, 2, s);
+  const int nt = (int)cache.host.size();
+  if (Zlo) {
+    switch (C) {
+      case 4: e = launch<false, BN, 2, true, 4>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 2: e = launch<false, BN, 2, true, 2>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      default: e = launch<false, BN, 2, true, 1>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+    }
+  } else {
+    switch (C) {
+      case 4: e = launch<false, BN, 4, false, 4>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 2: e = launch<false, BN, 4, false, 2>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      default: e = launch<false, BN, 4, false, 1>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+    }
+  }
   if (e != cudaSuccess) return e;
   return check_error_flag(s);
 }
@@ -436,10 +535,18 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
 // Column-tile width for the GRM.V: the widest tile that divides ncols (wider tiles re-read
 // the K strip fewer times; the split variants hold 2x operands per stage).
 int tc_gemm_tile_n(int64_t ncols, bool split) {
+  (void)split;
   if (ncols % 256 == 0 && ncols >= 512) return 256;
   if (ncols % 128 == 0 && ncols >= 128) return 128;
   if (ncols % 64 == 0) return 64;
   return 32;
+}
+
+template <int BN, int S, int C>
+static cudaError_t launch_grmv_split(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
+                                     const CUtensorMap& b2, const TileCoord* tiles, int nt, int num_kb,
+                                     float* Y, int64_t np, cudaStream_t s) {
+  return launch<true, BN, S, true, C>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f, 1, s, np);
 }
 
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
@@ -447,36 +554,52 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
   if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0) return cudaErrorInvalidValue;
   const bool split = Klo != nullptr && Plo != nullptr;
   const int BN = tc_gemm_tile_n(ncols, split);
+  const int C = split ? g_cluster_grmv : 1;
   CUtensorMap a, b, a2, b2;
+  const uint32_t brows = (uint32_t)(BN / C);
   if (!make_map(&a, K, true, np, np, (uint64_t)np * 4, kTileM) ||
-      !make_map(&b, P, true, np, ncols, (uint64_t)np * 4, BN))
+      !make_map(&b, P, true, np, ncols, (uint64_t)np * 4, brows))
     return cudaErrorInvalidValue;
   a2 = a;
   b2 = b;
   if (split && (!make_map(&a2, Klo, true, np, np, (uint64_t)np * 4, kTileM) ||
-                !make_map(&b2, Plo, true, np, ncols, (uint64_t)np * 4, BN)))
+                !make_map(&b2, Plo, true, np, ncols, (uint64_t)np * 4, brows)))
     return cudaErrorInvalidValue;
+  // row groups of C consecutive row blocks (padded past np), every column block per group
   static TileCache cache;
   cache.host.clear();
-  for (int64_t bm = 0; bm < np / kTileM; ++bm)
-    for (int64_t bn = 0; bn < ncols / BN; ++bn) cache.host.push_back(TileCoord{(int32_t)bm, (int32_t)bn});
+  const int64_t nbm = np / kTileM;
+  for (int64_t gi = 0; gi < (nbm + C - 1) / C; ++gi)
+    for (int64_t bn = 0; bn < ncols / BN; ++bn)
+      for (int r = 0; r < C; ++r) cache.host.push_back(TileCoord{(int32_t)(gi * C + r), (int32_t)bn});
   cudaError_t e = upload_tiles(cache, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(np / 32);
   const int nt = (int)cache.host.size();
   if (split) {
+#define SG_GRMV_CASE(BNv, Sv)                                                                          \
+  case BNv:                                                                                            \
+    e = C == 4 ? launch_grmv_split<BNv, Sv, 4>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s)          \
+      : C == 2 ? launch_grmv_split<BNv, Sv, 2>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s)          \
+               : launch_grmv_split<BNv, Sv, 1>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s);         \
+    break;
     switch (BN) {
-      case 256: e = launch<true, 256, 2, true>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
-      case 128: e = launch<true, 128, 3, true>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
-      case 64: e = launch<true, 64, 4, true>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
-      default: e = launch<true, 32, 5, true>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+      SG_GRMV_CASE(256, 2)
+      SG_GRMV_CASE(128, 3)
+      SG_GRMV_CASE(64, 4)
+      default:
+        e = C == 4 ? launch_grmv_split<32, 5, 4>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s)
+          : C == 2 ? launch_grmv_split<32, 5, 2>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s)
+                   : launch_grmv_split<32, 5, 1>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s);
+        break;
     }
+#undef SG_GRMV_CASE
   } else {
     switch (BN) {
-      case 256: e = launch<true, 256, 3, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
-      case 128: e = launch<true, 128, 4, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
-      case 64: e = launch<true, 64, 6, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
-      default: e = launch<true, 32, 8, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s); break;
+      case 256: e = launch<true, 256, 3, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
+      case 128: e = launch<true, 128, 4, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
+      case 64: e = launch<true, 64, 6, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
+      default: e = launch<true, 32, 8, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
     }
   }
   if (e != cudaSuccess) return e;
@@ -561,9 +684,9 @@ cudaError_t tc_gemm_tf32x3_noalloc(const float* Khi, const float* Klo, int64_t n
     return cudaErrorInvalidValue;
   const int num_kb = (int)(np / 32);
   if (BN == 64)
-    e = launch<true, 64, 4, true>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, Y, np, 1.0f, 1, s);
+    e = launch<true, 64, 4, true>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, Y, np, 1.0f, 1, s, np);
   else
-    e = launch<true, 32, 5, true>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, Y, np, 1.0f, 1, s);
+    e = launch<true, 32, 5, true>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, Y, np, 1.0f, 1, s, np);
   if (e != cudaSuccess) return e;
   return check_error_flag(s);
 }

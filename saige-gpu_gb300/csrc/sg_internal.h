@@ -83,6 +83,9 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
 // Plo (split operands) it accumulates K P + K Plo + Klo P (3xTF32).
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
                          const float* Plo, int64_t ncols, float* Y, cudaStream_t s);
+// Cluster sizes (1, 2 or 4 CTAs sharing one B tile by TMA multicast) of the SYRK and split GRM.V.
+bool tc_set_clusters(int syrk, int grmv);
+void tc_get_clusters(int* syrk, int* grmv);
 // Column tile width the GRM.V kernel uses for ncols columns.
 int tc_gemm_tile_n(int64_t ncols, bool split);
 // Split-TF32 GRM.V that allocates nothing: scratch in a static device array (k_tc.cu).

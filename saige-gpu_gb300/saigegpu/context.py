@@ -83,6 +83,14 @@ class Context:
         self._call("sg_kernel_launches", C.byref(v))
         return v.value
 
+    def set_tc_clusters(self, syrk, grmv):
+        self._call("sg_set_tc_clusters", int(syrk), int(grmv))
+
+    def get_tc_clusters(self):
+        a, b = C.c_int32(), C.c_int32()
+        self._call("sg_get_tc_clusters", C.byref(a), C.byref(b))
+        return a.value, b.value
+
     def set_matvec_mode(self, mode):
         self._call("sg_set_matvec_mode", int(mode))
 

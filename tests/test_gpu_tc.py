@@ -49,3 +49,40 @@ def test_grm_matvec_tf32_tc(cohort):
             assert np.abs(Y - ref).max() / np.abs(ref).max() < 5e-3, k
     finally:
         ctx.set_matvec_mode(MV_FP32_SIMT)
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_syrk_cluster_variants_bit_identical(cohort, split):
+    ctx, grm = cohort
+    prec = GRM_BF16X3_TC if split else GRM_BF16_TC
+    try:
+        ctx.set_tc_clusters(1, 1)
+        ctx.grm_build(prec)
+        K1 = ctx.grm_get()
+        for c in (2, 4):
+            ctx.set_tc_clusters(c, 1)
+            ctx.grm_build(prec)
+            assert np.array_equal(ctx.grm_get(), K1), c
+    finally:
+        ctx.set_tc_clusters(1, 1)
+
+
+def test_grmv_cluster_variants_bit_identical(cohort):
+    from saigegpu import MV_TF32X3_TC
+    ctx, grm = cohort
+    ctx.grm_build(GRM_FP32_SIMT)
+    rng = np.random.default_rng(3)
+    try:
+        ctx.set_matvec_mode(MV_TF32X3_TC)
+        for k in (32, 100, 256):  # column tiles of 32, 128 and 256 (padded)
+            V = rng.standard_normal((grm.n, k))
+            ctx.set_tc_clusters(1, 1)
+            Y1 = ctx.grm_matmul(V)
+            ref = grm.K @ V
+            assert np.abs(Y1 - ref).max() / np.abs(ref).max() < 5e-6
+            for c in (2, 4):
+                ctx.set_tc_clusters(1, c)
+                assert np.array_equal(ctx.grm_matmul(V), Y1), (k, c)
+    finally:
+        ctx.set_tc_clusters(1, 1)
+        ctx.set_matvec_mode(MV_FP32_SIMT)
