@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=1003)
     ap.add_argument("--mode", default="tf32x3", choices=["tf32x3", "tf32", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the cluster-shape autotuner")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
 
@@ -264,9 +265,15 @@ def run_ours(args, rank, world, local):
     ptr, ln = ctx.synth_bed(args.seed + rank, args.n, args.m, args.miss)
     ctx.setgeno_device(ptr, ln, args.n, args.m)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ctx.grm_build(GRM_BF16_TC)
-    grm_s = time.perf_counter() - t0
+    tune_report = None
+    if args.no_tune or args.mode != "tf32x3":
+        t0 = time.perf_counter()
+        ctx.grm_build(GRM_BF16_TC)
+        grm_s = time.perf_counter() - t0
+    else:
+        from saigegpu import tune
+        tune_report = tune.tune(ctx, ncols=(128, 256, 512))
+        grm_s = tune_report["syrk"][tune_report["chosen"][0]]
     d = ctx.dims()
     syrk_flops = float(d["n"]) * (d["n"] + 1) * d["m_qc"]
     specs = make_specs(ctx, args, args.seed + 17 * rank)
@@ -329,6 +336,10 @@ def run_ours(args, rank, world, local):
                     "converged": int(sum(1 for r in res_all if r["converged"])), "fits": len(res_all)},
         "setup_s": round(setup_s, 1),
     }
+    if tune_report is not None:
+        out["tuning"] = {"clusters_syrk_grmv": list(tune_report["chosen"]),
+                         "syrk_s": {str(k): round(v, 4) for k, v in tune_report["syrk"].items()},
+                         "grmv_ms": {"%d@%d" % k: round(v * 1e3, 3) for k, v in tune_report["grmv"].items()}}
     out["clocks"] = clk.summary()
     if rank == 0:
         out["plain_fp64_single_rhs"] = plain_fp64(ctx, col_iters)
