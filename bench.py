@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--mode", default="tf32x3", choices=["tf32x3", "tf32", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster-shape autotuner")
+    ap.add_argument("--serve-requests", type=int, default=32,
+                    help="requests of the serving-form block (Poisson arrivals, 0 = skip)")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
 
@@ -203,6 +205,37 @@ def grm_roofline(ctx, peaks, t_dev, n, np_):
             "peak_source": "TF32 = half the measured bf16_tflops (MEASURED_PEAKS.json)"}
 
 
+def serving_block(ctx, args, cols):
+    """Serving form: Poisson arrivals (mean 2/s) of fits on sample subsets of 20k..N, admitted as
+    slots and columns free up; reports fits/hr over the run and p50/p99 latency from arrival."""
+    from saigegpu import prep, serve, synth
+    n = ctx.n
+    rng = np.random.default_rng(args.seed + 99)
+    gv = ctx.synth_genetic_value(args.seed * 13)
+    gv = gv / gv.std()
+    arrivals, t = [], 0.0
+    for k in range(args.serve_requests):
+        t += rng.exponential(0.5)
+        trait = "binary" if k % 2 == 0 else "quantitative"
+        keep = rng.uniform(min(1.0, 20000 / n), 1.0)
+        mask = rng.uniform(size=n) < keep
+        S = np.nonzero(mask)[0]
+        y, C = synth.simulate_pheno(gv, args.seed * 1000 + k, trait, tau=0.3,
+                                    prevalence=rng.uniform(0.05, 0.3), h2=rng.uniform(0.1, 0.6))
+        f0 = prep.make_fit0(y[S], C[S], trait, True)
+        arrivals.append((t, serve.FitSpec(f0, trait, mask=mask)))
+    t0 = time.perf_counter()
+    done = serve.serve(ctx, arrivals, max_columns=cols, max_phenos=max(4, args.phenos))
+    wall = time.perf_counter() - t0
+    lat = sorted(j.t_done - j.t_arrive for j in done)
+    ok = sum(1 for j in done if j.error is None)
+    return {"requests": len(arrivals), "completed": ok, "arrival_rate_per_s": 2.0,
+            "fits_per_hr": round(ok / wall * 3600.0, 1), "wall_s": round(wall, 1),
+            "latency_s": {"p50": round(float(np.percentile(lat, 50)), 3),
+                          "p99": round(float(np.percentile(lat, 99)), 3)},
+            "subsets": "20k..N samples", "max_concurrent_fits": max(4, args.phenos)}
+
+
 def load_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -341,6 +374,8 @@ def run_ours(args, rank, world, local):
                          "syrk_s": {str(k): round(v, 4) for k, v in tune_report["syrk"].items()},
                          "grmv_ms": {"%d@%d" % k: round(v * 1e3, 3) for k, v in tune_report["grmv"].items()}}
     out["clocks"] = clk.summary()
+    if rank == 0 and args.serve_requests > 0:
+        out["serving"] = serving_block(ctx, args, cols)
     if rank == 0:
         out["plain_fp64_single_rhs"] = plain_fp64(ctx, col_iters)
         out["speedup_vs_plain_fp64"] = round(value / out["plain_fp64_single_rhs"]["fits_per_hr"], 1)

@@ -57,3 +57,24 @@ def test_full_fit_matches_oracle(golden_cohort, trait):
     assert rel.max() < 1e-3, (rg["theta"], ro["theta"])
     assert rg["iterations"] == ro["iterations"]
     np.testing.assert_allclose(rg["coefficients"], ro["coefficients"], rtol=1e-3, atol=1e-6)
+
+
+def test_config1_cpu_runnable_case(gpu_ctx):
+    """The reference's CPU-runnable configuration: N=2,000, M=5,000, binary (prevalence 0.2), tau=0.3."""
+    from saigegpu import synth
+    n, m = 2000, 5000
+    bed, codes = synth.synth_bed(1001, n, m, 0.01)
+    gpu_ctx.setgeno(bed, n, m)
+    gpu_ctx.grm_build(GRM_FP32_SIMT)
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+    grm = aireml.DenseGRM(g)
+    gv = synth.genetic_value_from_codes(g.codes, 1001)
+    y, C = synth.simulate_pheno(gv, 1001, "binary", tau=0.3, prevalence=0.2)
+    fit0 = prep.make_fit0(y, C, "binary", True)
+    ro = aireml.glmmkin_binary(grm, fit0)
+    rg = glmm.glmmkin_binary(gpu_ctx, fit0)
+    assert rg["iterations"] == ro["iterations"]
+    np.testing.assert_allclose(rg["theta"], ro["theta"], rtol=1e-3)
+    from saigegpu import serve
+    rb, _ = serve.fit_batch(gpu_ctx, [serve.FitSpec(fit0, "binary")], max_columns=128)
+    np.testing.assert_allclose(rb[0]["theta"], ro["theta"], rtol=1e-4)
