@@ -76,6 +76,7 @@ struct sg_ctx {
   uint64_t in_use = 0;
   cudaStream_t stream = nullptr;
   std::string err;
+  std::string err_pending;
   uint64_t launches = 0;
   int mv_mode = SG_MV_FP32_SIMT;
   std::unordered_map<void*, size_t> allocs;
@@ -116,6 +117,10 @@ struct sg_ctx {
 };
 
 // ------------------------------------------------------------------ helpers
+extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_pcg,
+                                    const int64_t* ids_prod, int64_t k, uint64_t seed, int64_t run0,
+                                    const double* SX, int64_t p, double* out, int32_t* iters);
+
 static int set_err(sg_ctx* c, int code, const char* fmt, ...) {
   if (!c) return code;
   char buf[512];
@@ -1546,16 +1551,41 @@ struct TraceOut {
   int nrun = 0;
 };
 
+// tr(PK)_j = Au.Su - b' cov c and tr(P)_j = u.Su - c' cov c from the device-side probe dots
+// (b_q = Au.SX_q, c_q = SX_q.u); appends to t1 / t0.  Errors land in c->err_pending.
+void probe_terms(sg_ctx* c, const std::vector<int64_t>& pid, const std::vector<int64_t>& aid,
+                 uint64_t seed, int64_t run0, const std::vector<double>& SX, int p,
+                 const std::vector<double>& cov, std::vector<double>& t1, std::vector<double>& t0) {
+  const int64_t k = (int64_t)pid.size(), nv = 2 + 2 * p;
+  std::vector<double> D(k * nv);
+  c->err_pending.clear();
+  if (sg_engine_probe_dots(c, 0, pid.data(), aid.data(), k, seed, run0, SX.data(), p, D.data(), nullptr) != SG_OK) {
+    c->err_pending = c->err;
+    return;
+  }
+  for (int64_t j = 0; j < k; ++j) {
+    const double* d = &D[j * nv];
+    double bcb = 0.0, ccc = 0.0;
+    for (int a = 0; a < p; ++a)
+      for (int b = 0; b < p; ++b) {
+        bcb += d[2 + a] * cov[a + b * p] * d[2 + p + b];
+        ccc += d[2 + p + a] * cov[a + b * p] * d[2 + p + b];
+      }
+    t1.push_back(d[0] - bcb);
+    t0.push_back(d[1] - ccc);
+  }
+}
+
 // GetTrace / GetTrace_q on the engine: each block of probes is submitted as
 // PCG columns (Sigma^-1 u) and product columns (K u) together.
 int trace_probes(sg_ctx* c, const std::vector<double>& SX, int p, const std::vector<double>& cov,
                  int nrun, int maxiter, double tol, double cutoff, uint64_t seed, bool quant,
                  const std::vector<int64_t>& extra_ids, TraceOut* out) {
-  const int64_t n = c->nn;
+  Engine& e = c->eng;
   std::vector<double> t1, t0;
   int start = 0, end = nrun;
-  std::vector<double> u(n), su(n), au(n), pu(n);
   bool first = true;
+  e.hold = true;  // probe results are reduced on the device (sg_engine_probe_dots)
   for (;;) {
     const int k = end - start;
     std::vector<int64_t> pid(k), aid(k);
@@ -1566,14 +1596,8 @@ int trace_probes(sg_ctx* c, const std::vector<double>& SX, int p, const std::vec
     if (first) all.insert(all.end(), extra_ids.begin(), extra_ids.end());
     first = false;
     SG_TRY(run_until(c, all));
-    for (int j = 0; j < k; ++j) {
-      for (int64_t i = 0; i < n; ++i) u[i] = (hash3(seed, (uint64_t)(start + j), (uint64_t)i) >> 63) ? 1.0 : -1.0;
-      SG_TRY(fetch(c, pid[j], su.data(), nullptr));
-      SG_TRY(fetch(c, aid[j], au.data(), nullptr));
-      p_apply(n, p, su.data(), SX.data(), cov.data(), u.data(), pu.data());
-      t1.push_back(dot(n, au.data(), pu.data()));
-      t0.push_back(dot(n, u.data(), pu.data()));
-    }
+    probe_terms(c, pid, aid, seed, start, SX, p, cov, t1, t0);
+    if (!c->err_pending.empty()) { e.hold = false; return set_err(c, SG_ERR_CUDA, "%s", c->err_pending.c_str()); }
     const double cv1 = cal_cv(t1);
     const double cv0 = quant ? cal_cv(t0) : 0.0;
     if (cv1 > cutoff || (quant && cv0 > cutoff)) {
@@ -1583,6 +1607,7 @@ int trace_probes(sg_ctx* c, const std::vector<double>& SX, int p, const std::vec
     }
     break;
   }
+  e.hold = false;
   double s1 = 0.0, s0 = 0.0;
   for (double v : t1) s1 += v;
   for (double v : t0) s0 += v;
@@ -1786,6 +1811,7 @@ int ai_score(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* 
   }
   o->PY.resize(n);
   p_apply(n, (int)p, SY.data(), SX.data(), cv.data(), Yd.data(), o->PY.data());
+  c->eng.hold = true;  // probe results are reduced on the device
   int64_t apy_id;
   SG_TRY(sg_engine_submit(c, 0, 1, o->PY.data(), 1, 1, 0.0, &apy_id));
   // first probe block + K PY in the same steps
@@ -1811,15 +1837,9 @@ int ai_score(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* 
   all.insert(all.end(), aid.begin(), aid.end());
   all.insert(all.end(), sid.begin(), sid.end());
   SG_TRY(run_until(c, all));
-  std::vector<double> t1, t0, u(n), su(n), au(n), pu(n);
-  for (int j = 0; j < k; ++j) {
-    for (int64_t i = 0; i < n; ++i) u[i] = (hash3(seed, (uint64_t)j, (uint64_t)i) >> 63) ? 1.0 : -1.0;
-    SG_TRY(fetch(c, pid[j], su.data(), nullptr));
-    SG_TRY(fetch(c, aid[j], au.data(), nullptr));
-    p_apply(n, (int)p, su.data(), SX.data(), cv.data(), u.data(), pu.data());
-    t1.push_back(dot(n, au.data(), pu.data()));
-    t0.push_back(dot(n, u.data(), pu.data()));
-  }
+  std::vector<double> t1, t0;
+  probe_terms(c, pid, aid, seed, 0, SX, (int)p, cv, t1, t0);
+  if (!c->err_pending.empty()) { c->eng.hold = false; return set_err(c, SG_ERR_CUDA, "%s", c->err_pending.c_str()); }
   int start = k, end = k;
   while (cal_cv(t1) > cutoff || (quant && cal_cv(t0) > cutoff)) {
     start = end;
@@ -1830,15 +1850,10 @@ int ai_score(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* 
     std::vector<int64_t> al(p2);
     al.insert(al.end(), a2.begin(), a2.end());
     SG_TRY(run_until(c, al));
-    for (int j = 0; j < 10; ++j) {
-      for (int64_t i = 0; i < n; ++i) u[i] = (hash3(seed, (uint64_t)(start + j), (uint64_t)i) >> 63) ? 1.0 : -1.0;
-      SG_TRY(fetch(c, p2[j], su.data(), nullptr));
-      SG_TRY(fetch(c, a2[j], au.data(), nullptr));
-      p_apply(n, (int)p, su.data(), SX.data(), cv.data(), u.data(), pu.data());
-      t1.push_back(dot(n, au.data(), pu.data()));
-      t0.push_back(dot(n, u.data(), pu.data()));
-    }
+    probe_terms(c, p2, a2, seed, start, SX, (int)p, cv, t1, t0);
+    if (!c->err_pending.empty()) { c->eng.hold = false; return set_err(c, SG_ERR_CUDA, "%s", c->err_pending.c_str()); }
   }
+  c->eng.hold = false;
   double s1 = 0, s0 = 0;
   for (double v : t1) s1 += v;
   for (double v : t0) s0 += v;
