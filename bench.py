@@ -320,13 +320,15 @@ def run_ours(args, rank, world, local):
     ctx.engine_reset_timing()
     barrier(world)
     torch.cuda.synchronize()
-    walls, jobs_all, res_all = [], [], []
+    walls, jobs_all, res_all, host_t = [], [], [], {}
     with Clocks(local) as clk:
         for _ in range(args.steps):
             res, jobs, wall = run_batch(ctx, specs, cols)
             walls.append(wall)
             jobs_all += jobs
             res_all += res
+            for k, v in getattr(jobs[0], "host_times", {}).items():
+                host_t[k] = host_t.get(k, 0.0) + v
     torch.cuda.synchronize()
     barrier(world)
     launches = ctx.kernel_launches() - L0
@@ -368,6 +370,7 @@ def run_ours(args, rank, world, local):
         "per_fit": {"pcg_column_iterations": round(col_iters, 1), "columns": round(cols_per_fit, 1),
                     "converged": int(sum(1 for r in res_all if r["converged"])), "fits": len(res_all)},
         "setup_s": round(setup_s, 1),
+        "wall_breakdown_s_per_step": {k: round(v / args.steps, 3) for k, v in host_t.items()},
     }
     if tune_report is not None:
         out["tuning"] = {"clusters_syrk_grmv": list(tune_report["chosen"]),

@@ -380,6 +380,8 @@ class Runner:
         self.finished = []
         self._next = 0
         self.inflight_columns = 0
+        # wall-clock seconds by activity (engine steps incl. their sync, result copies, driver math)
+        self.t = {"engine": 0.0, "fetch": 0.0, "probe_dots": 0.0, "pheno": 0.0, "submit": 0.0, "driver": 0.0}
 
     # -- admission
     def can_admit(self, spec):
@@ -402,14 +404,19 @@ class Runner:
     # -- generator plumbing
     def _advance(self, job, value):
         gen = job.gen
+        clock = time.perf_counter
         try:
             while True:
+                t0 = clock()
                 op = gen.send(value)
+                t1 = clock()
+                self.t["driver"] += t1 - t0
                 kind = op[0]
                 if kind == "pheno":
                     _, W, tau = op
                     self.ctx.engine_set_pheno(job.slot, W, tau, job.spec.mask)
                     value = None
+                    self.t["pheno"] += clock() - t1
                 elif kind == "submit":
                     _, k, B, probe, maxiter, tol = op
                     if probe is None:
@@ -417,6 +424,7 @@ class Runner:
                     else:
                         seed, run0, cnt = probe
                         ids = self.ctx.engine_submit_probes(job.slot, k, seed, run0, cnt, maxiter, tol)
+                    self.t["submit"] += clock() - t1
                     for i in ids:
                         self.owner[int(i)] = job.jid
                     job.columns += len(ids)
@@ -432,6 +440,7 @@ class Runner:
                 elif kind == "probe_dots":
                     _, pid, aid, seed, run0, SX = op
                     D, its = self.ctx.engine_probe_dots(job.slot, pid, aid, seed, run0, SX)
+                    self.t["probe_dots"] += clock() - t1
                     job.column_iterations += int(np.sum(its)) + len(aid)
                     for i in list(pid) + list(aid):
                         self.done.discard(i)
@@ -449,6 +458,7 @@ class Runner:
     def _resolve(self, job, kind, ids):
         if kind == "wait_ids":
             return None
+        t0 = time.perf_counter()
         out = []
         for rid in ids:
             x, it = self.ctx.engine_fetch(rid)
@@ -456,6 +466,7 @@ class Runner:
             self.owner.pop(rid, None)
             job.column_iterations += it
             out.append(x)
+        self.t["fetch"] += time.perf_counter() - t0
         return out
 
     def _finish(self, job):
@@ -474,8 +485,10 @@ class Runner:
 
     def step(self):
         """One engine step; resume every fit whose awaited columns are complete."""
+        t0 = time.perf_counter()
         self.ctx.engine_run(1)
         ids = self.ctx.engine_poll()
+        self.t["engine"] += time.perf_counter() - t0
         for rid in ids:
             rid = int(rid)
             if rid not in self.owner:
@@ -510,7 +523,10 @@ def fit_batch(ctx, specs, max_columns=2048, max_phenos=None):
     ids = [r.submit(s) for s in specs]
     r.run()
     by = {j.jid: j for j in r.finished}
-    return [by[i].result if by[i].error is None else by[i].error for i in ids], [by[i] for i in ids]
+    jobs = [by[i] for i in ids]
+    for j in jobs:
+        j.host_times = r.t
+    return [by[i].result if by[i].error is None else by[i].error for i in ids], jobs
 
 
 def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter):
