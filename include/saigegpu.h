@@ -248,6 +248,12 @@ int sg_engine_cancel(sg_ctx *ctx, int64_t id);
 int sg_engine_probe_dots(sg_ctx *ctx, int64_t slot, const int64_t *ids_pcg, const int64_t *ids_prod,
                          int64_t k, uint64_t seed, int64_t run0, const double *SX, int64_t p,
                          double *out, int32_t *iters);
+/* K u of a slot's probes is kept on the device once computed (the probes and the slot's sample mask
+ * are fixed during a fit): an ids_prod entry of -1 in sg_engine_probe_dots reads the cached K u of
+ * (seed, run0 + j).  Clear a slot's cache when a new phenotype (mask) takes it (slot -1: all). */
+int sg_engine_probe_cache_clear(sg_ctx *ctx, int64_t slot);
+/* 1 if K u of probe (seed, run) is cached for the slot, else 0. */
+int sg_engine_probe_cached(sg_ctx *ctx, int64_t slot, uint64_t seed, int64_t run);
 /* Ids of columns that finished since the previous poll (up to max_ids); *n_out gets the count. */
 int sg_engine_poll(sg_ctx *ctx, int64_t *ids, int64_t max_ids, int64_t *n_out);
 /* counters: [0]=engine steps, [1]=columns retired, [2]=column-iterations, [3]=GRM passes */

@@ -63,6 +63,10 @@ struct Engine {
   double* d_dpart = nullptr;      // probe_dots: block partial sums
   int32_t* d_dcols = nullptr;     // probe_dots: column indices
   uint8_t* ptab = nullptr;        // probe table of one admission round (stage_cols x 24 B)
+  // K u of each slot's probes, kept between AI-REML iterations (the probes and the slot's sample
+  // mask do not change during a fit): kProbeCache vectors per slot, keyed by (seed, run)
+  double* pcache = nullptr;
+  std::vector<std::vector<std::pair<uint64_t, int64_t>>> pcache_key;  // per slot: (seed, run) per entry
   size_t dots_cap_sx = 0, dots_cap_part = 0, dots_cap_cols = 0;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   double t_step_ms = 0, t_gemm_ms = 0, gemm_launches = 0, gemm_flops = 0, gemm_cols = 0, useful_cols = 0;
@@ -694,6 +698,8 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.Yd); dev_free_t(c, e.Pf); dev_free_t(c, e.Yf); dev_free_t(c, e.d_st);
   dev_free_t(c, e.d_ph); dev_free_t(c, e.d_cols); dev_free_t(c, e.Pflo);
   dev_free_t(c, e.d_sx); dev_free_t(c, e.d_dpart); dev_free_t(c, e.d_dcols); dev_free_t(c, e.ptab);
+  dev_free_t(c, e.pcache);
+  e.pcache_key.clear();
   e.dots_cap_sx = e.dots_cap_part = e.dots_cap_cols = 0;
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
@@ -1184,6 +1190,32 @@ extern "C" int sg_engine_cancel(sg_ctx* c, int64_t id) {
 }
 
 // Hutchinson probe reductions on the device (see include/saigegpu.h).
+static constexpr int kProbeCache = 64;
+
+static int pcache_find(const Engine& e, int64_t slot, uint64_t seed, int64_t run) {
+  if (slot >= (int64_t)e.pcache_key.size()) return -1;
+  const auto& v = e.pcache_key[slot];
+  for (size_t i = 0; i < v.size(); ++i)
+    if (v[i].first == seed && v[i].second == run) return (int)i;
+  return -1;
+}
+
+extern "C" int sg_engine_probe_cache_clear(sg_ctx* c, int64_t slot) {
+  if (!c) return SG_ERR_INVALID;
+  Engine& e = c->eng;
+  if (slot < 0) {
+    for (auto& v : e.pcache_key) v.clear();
+  } else if (slot < (int64_t)e.pcache_key.size()) {
+    e.pcache_key[slot].clear();
+  }
+  return SG_OK;
+}
+
+extern "C" int sg_engine_probe_cached(sg_ctx* c, int64_t slot, uint64_t seed, int64_t run) {
+  if (!c) return 0;
+  return pcache_find(c->eng, slot, seed, run) >= 0 ? 1 : 0;
+}
+
 extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_pcg,
                                     const int64_t* ids_prod, int64_t k, uint64_t seed, int64_t run0,
                                     const double* SX, int64_t p, double* out, int32_t* iters) {
@@ -1192,14 +1224,38 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
   if (k <= 0 || !ids_pcg || !ids_prod || !out || p < 0 || p > kProbeDotsMaxP || (p > 0 && !SX))
     return set_err(c, SG_ERR_INVALID, "probe_dots: bad arguments (p <= %d)", kProbeDotsMaxP);
   if (slot < 0 || slot >= e.cap_ph) return set_err(c, SG_ERR_INVALID, "bad slot");
-  std::vector<int32_t> cols(2 * k);
-  for (int64_t j = 0; j < 2 * k; ++j) {
-    const int64_t id = j < k ? ids_pcg[j] : ids_prod[j - k];
-    auto it = e.reqs.find(id);
-    if (it == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
+  if ((int64_t)e.pcache_key.size() < e.cap_ph) e.pcache_key.resize(e.cap_ph);
+  if (!e.pcache) SG_TRY(dev_alloc_t(c, &e.pcache, (size_t)(e.cap_ph * kProbeCache * e.np)));
+  // Su from held engine columns; Au from a held column (then cached) or from the slot's cache
+  std::vector<const double*> su(k), au(k);
+  for (int64_t j = 0; j < k; ++j) {
+    auto it = e.reqs.find(ids_pcg[j]);
+    if (it == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)ids_pcg[j]);
     if (it->second.state != 2 || it->second.col < 0)
-      return set_err(c, SG_ERR_STATE, "request %lld has no resident result", (long long)id);
-    cols[j] = (int32_t)it->second.col;
+      return set_err(c, SG_ERR_STATE, "request %lld has no resident result", (long long)ids_pcg[j]);
+    su[j] = e.X + it->second.col * e.np;
+    if (ids_prod[j] < 0) {
+      const int ci = pcache_find(e, slot, seed, run0 + j);
+      if (ci < 0) return set_err(c, SG_ERR_STATE, "probe %lld of slot %lld is not cached", (long long)(run0 + j), (long long)slot);
+      au[j] = e.pcache + (slot * kProbeCache + ci) * e.np;
+    } else {
+      auto ia = e.reqs.find(ids_prod[j]);
+      if (ia == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)ids_prod[j]);
+      if (ia->second.state != 2 || ia->second.col < 0)
+        return set_err(c, SG_ERR_STATE, "request %lld has no resident result", (long long)ids_prod[j]);
+      au[j] = e.X + ia->second.col * e.np;
+      auto& keys = e.pcache_key[slot];
+      int ci = pcache_find(e, slot, seed, run0 + j);
+      if (ci < 0 && (int)keys.size() < kProbeCache) {
+        keys.emplace_back(seed, run0 + j);
+        ci = (int)keys.size() - 1;
+      }
+      if (ci >= 0) {
+        double* dst = e.pcache + (slot * kProbeCache + ci) * e.np;
+        SG_CUDA(c, cudaMemcpyAsync(dst, au[j], e.np * 8, cudaMemcpyDeviceToDevice, c->stream));
+        au[j] = dst;
+      }
+    }
   }
   const int64_t nv = 2 + 2 * p;
   const int64_t nblk = e.nblk;
@@ -1214,7 +1270,7 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
     dev_free_t(c, e.d_dpart);
     dev_free_t(c, e.d_dcols);
     SG_TRY(dev_alloc_t(c, &e.d_dpart, need_part));
-    SG_TRY(dev_alloc_t(c, &e.d_dcols, (size_t)(2 * k)));
+    SG_TRY(dev_alloc_t(c, &e.d_dcols, (size_t)(2 * k) * 2));  // 2k pointers as int64 pairs
     e.dots_cap_part = need_part;
     e.dots_cap_cols = (size_t)(2 * k);
   }
@@ -1222,9 +1278,11 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
     SG_CUDA(c, cudaMemsetAsync(e.d_sx, 0, need_sx * 8, c->stream));
     SG_CUDA(c, cudaMemcpy2DAsync(e.d_sx, e.np * 8, SX, c->nn * 8, c->nn * 8, p, cudaMemcpyHostToDevice, c->stream));
   }
-  SG_CUDA(c, cudaMemcpyAsync(e.d_dcols, cols.data(), cols.size() * 4, cudaMemcpyHostToDevice, c->stream));
-  launch_probe_dots(e.np, c->nn, e.X, e.d_dcols, k, e.minv + slot * e.np, seed, run0, e.d_sx, p,
-                    e.d_dpart, nblk, c->stream);
+  std::vector<const double*> ptrs(su);
+  ptrs.insert(ptrs.end(), au.begin(), au.end());
+  SG_CUDA(c, cudaMemcpyAsync(e.d_dcols, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice, c->stream));
+  launch_probe_dots(e.np, c->nn, reinterpret_cast<const double* const*>(e.d_dcols), k,
+                    e.minv + slot * e.np, seed, run0, e.d_sx, p, e.d_dpart, nblk, c->stream);
   SG_LAUNCHED(c, 1);
   std::vector<double> part(need_part);
   SG_CUDA(c, cudaMemcpyAsync(part.data(), e.d_dpart, need_part * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -1237,6 +1295,7 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
     }
   for (int64_t j = 0; j < 2 * k; ++j) {
     const int64_t id = j < k ? ids_pcg[j] : ids_prod[j - k];
+    if (id < 0) continue;
     auto it = e.reqs.find(id);
     if (iters && j < k) iters[j] = it->second.iters;
     SG_TRY(release_col(c, it->second.col));

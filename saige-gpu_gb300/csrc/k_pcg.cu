@@ -342,14 +342,13 @@ void launch_probe_fill_multi(int64_t np, int64_t nn, const uint64_t* seeds, cons
 }
 
 // Hutchinson probe reductions: for probe j the block sums of Au.Su, u.Su, Au.SX_q and SX_q.u.
-__global__ void probe_dots_kernel(int64_t np, int64_t nn, const double* __restrict__ X,
-                                  const int32_t* __restrict__ cols, int64_t k,
+__global__ void probe_dots_kernel(int64_t np, int64_t nn, const double* const* __restrict__ vecs, int64_t k,
                                   const double* __restrict__ minv, uint64_t seed, int64_t run0,
                                   const double* __restrict__ SX, int p, double* part, int64_t nblk) {
   __shared__ double sh[kThreads / 32];
   const int64_t j = blockIdx.y;
-  const double* su = X + (int64_t)cols[j] * np;
-  const double* au = X + (int64_t)cols[k + j] * np;
+  const double* su = vecs[j];
+  const double* au = vecs[k + j];
   const int64_t i0 = (int64_t)blockIdx.x * kChunk;
   double v[2 + 2 * kProbeDotsMaxP];
 #pragma unroll
@@ -376,12 +375,12 @@ __global__ void probe_dots_kernel(int64_t np, int64_t nn, const double* __restri
   }
 }
 
-void launch_probe_dots(int64_t np, int64_t nn, const double* X, const int32_t* cols, int64_t k,
+void launch_probe_dots(int64_t np, int64_t nn, const double* const* vecs, int64_t k,
                        const double* minv_row, uint64_t seed, int64_t run0, const double* SX,
                        int64_t p, double* part, int64_t nblk, cudaStream_t s) {
   if (k == 0) return;
   dim3 grid((unsigned)nblk, (unsigned)k);
-  probe_dots_kernel<<<grid, kThreads, 0, s>>>(np, nn, X, cols, k, minv_row, seed, run0, SX, (int)p, part, nblk);
+  probe_dots_kernel<<<grid, kThreads, 0, s>>>(np, nn, vecs, k, minv_row, seed, run0, SX, (int)p, part, nblk);
 }
 
 __global__ void f64_to_f32_kernel(const double* a, float* b, int64_t n) {

@@ -137,9 +137,9 @@ void launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
 void launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s);
 int64_t pcg_nblk(int64_t np);
 constexpr int kProbeDotsMaxP = 16;
-// Per probe j (columns cols[j] = Sigma^-1 u_j and cols[k+j] = K u_j, u masked by minv != 0):
+// Per probe j (vecs[j] = Sigma^-1 u_j and vecs[k+j] = K u_j, u masked by minv != 0):
 // block partials of [Au.Su, u.Su, Au.SX_q (q < p), SX_q.u (q < p)] -> part[(j*nblk + b)*(2+2p) + v]
-void launch_probe_dots(int64_t np, int64_t nn, const double* X, const int32_t* cols, int64_t k,
+void launch_probe_dots(int64_t np, int64_t nn, const double* const* vecs, int64_t k,
                        const double* minv_row, uint64_t seed, int64_t run0, const double* SX,
                        int64_t p, double* part, int64_t nblk, cudaStream_t s);
 

@@ -92,6 +92,8 @@ SIGNATURES = {
     "sg_engine_stats": [c_ctx, P_i64],
     "sg_engine_poll": [c_ctx, P_i64, c_i64, P_i64],
     "sg_engine_hold_results": [c_ctx, C.c_int],
+    "sg_engine_probe_cache_clear": [c_ctx, c_i64],
+    "sg_engine_probe_cached": [c_ctx, c_i64, c_u64, c_i64],
     "sg_engine_probe_dots": [c_ctx, c_i64, P_i64, P_i64, c_i64, c_u64, c_i64, P_f64, c_i64, P_f64,
                              P_i32],
     "sg_engine_timing": [c_ctx, P_f64],

@@ -414,6 +414,12 @@ class Context:
                    int(run0), _ptr(SXf, L.P_f64), p, _ptr(out, L.P_f64), _ptr(it, L.P_i32))
         return out.reshape(k, 2 + 2 * p), it
 
+    def engine_probe_cache_clear(self, slot=-1):
+        self._call("sg_engine_probe_cache_clear", int(slot))
+
+    def engine_probe_cached(self, slot, seed, run):
+        return bool(self._L.sg_engine_probe_cached(self._h, int(slot), int(seed), int(run)))
+
     def engine_timing(self):
         t = np.zeros(6, np.float64)
         self._call("sg_engine_timing", _ptr(t, L.P_f64))

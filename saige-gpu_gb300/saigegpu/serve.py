@@ -151,7 +151,8 @@ def fit_generator(spec, n_cohort, probes):
         # K PY rides with the first probe block
         apy_id = yield ("submit", 1, PY[:, None], None, 1, 0.0)
         pid = yield ("submit", 0, None, (spec.seed, 0, spec.nrun), spec.maxiter_pcg, spec.tol_pcg)
-        aid = yield ("submit", 1, None, (spec.seed, 0, spec.nrun), 1, 0.0)
+        # K u is fixed for the fit (same probes, same sample mask): -1 marks a cached product
+        aid = yield ("probe_products", spec.seed, 0, spec.nrun)
         APY = (yield ("wait", apy_id))[0]
         rhs = np.column_stack([APY, PY]) if quant else APY[:, None]
         sid = yield ("submit", 0, rhs, None, spec.maxiter_pcg, spec.tol_pcg)
@@ -159,7 +160,7 @@ def fit_generator(spec, n_cohort, probes):
         run0, k = 0, spec.nrun
         p = SX.shape[1]
         while True:
-            yield ("wait_ids", list(pid) + list(aid))
+            yield ("wait_ids", list(pid) + [a for a in aid if a >= 0])
             # t1 = Au.Pu, t0 = u.Pu with Pu = Su - SX cov SX'u, from device-side dot products
             D = yield ("probe_dots", pid, aid, spec.seed, run0, SX)
             b, c = D[:, 2:2 + p], D[:, 2 + p:2 + 2 * p]
@@ -168,7 +169,7 @@ def fit_generator(spec, n_cohort, probes):
             if _cal_cv(t1) > spec.cutoff or (quant and _cal_cv(t0) > spec.cutoff):
                 run0, k = run0 + k, 10
                 pid = yield ("submit", 0, None, (spec.seed, run0, k), spec.maxiter_pcg, spec.tol_pcg)
-                aid = yield ("submit", 1, None, (spec.seed, run0, k), 1, 0.0)
+                aid = yield ("probe_products", spec.seed, run0, k)
                 continue
             break
         S = np.column_stack((yield ("wait", sid)))
@@ -394,6 +395,8 @@ class Runner:
         jid = self._next
         self._next += 1
         slot = self.free_slots.pop()
+        if hasattr(self.ctx, "engine_probe_cache_clear"):
+            self.ctx.engine_probe_cache_clear(slot)  # a new sample mask takes this slot
         job = _Job(jid, spec, fit_generator(spec, self.n, self.probes), slot,
                    time.perf_counter() if t_arrive is None else t_arrive)
         job.t_start = time.perf_counter()
@@ -437,12 +440,31 @@ class Runner:
                         continue
                     job.waiting = (kind, ids)
                     return
+                elif kind == "probe_products":
+                    _, seed, run0, cnt = op
+                    value = [-1] * cnt
+                    j = 0
+                    while j < cnt:  # submit maximal runs of uncached probes as blocks
+                        if self.ctx.engine_probe_cached(job.slot, seed, run0 + j):
+                            j += 1
+                            continue
+                        j1 = j
+                        while j1 < cnt and not self.ctx.engine_probe_cached(job.slot, seed, run0 + j1):
+                            j1 += 1
+                        ids = self.ctx.engine_submit_probes(job.slot, 1, seed, run0 + j, j1 - j, 1, 0.0)
+                        for q, i in enumerate(ids):
+                            value[j + q] = int(i)
+                            self.owner[int(i)] = job.jid
+                        job.columns += len(ids)
+                        self.inflight_columns += len(ids)
+                        j = j1
+                    self.t["submit"] += clock() - t1
                 elif kind == "probe_dots":
                     _, pid, aid, seed, run0, SX = op
                     D, its = self.ctx.engine_probe_dots(job.slot, pid, aid, seed, run0, SX)
                     self.t["probe_dots"] += clock() - t1
-                    job.column_iterations += int(np.sum(its)) + len(aid)
-                    for i in list(pid) + list(aid):
+                    job.column_iterations += int(np.sum(its)) + sum(1 for a in aid if a >= 0)
+                    for i in list(pid) + [a for a in aid if a >= 0]:
                         self.done.discard(i)
                         self.owner.pop(i, None)
                     value = D

@@ -9,6 +9,7 @@ class FakeEngine:
     """Implements the engine calls the runner uses with the FP64 oracle (solves on admission)."""
 
     def __init__(self, grm):
+        self.cache = {}
         self.grm = grm
         self.n = grm.n
         self.ph = {}
@@ -61,12 +62,23 @@ class FakeEngine:
     def engine_fetch(self, rid):
         return self.res.pop(int(rid))
 
+    def engine_probe_cached(self, slot, seed, run):
+        return (slot, seed, run) in self.cache
+
+    def engine_probe_cache_clear(self, slot=-1):
+        self.cache = {k: v for k, v in getattr(self, "cache", {}).items() if slot >= 0 and k[0] != slot}
+
     def engine_probe_dots(self, slot, pid, aid, seed, run0, SX):
         m = self.ph[slot][2]
+        self.cache = getattr(self, "cache", {})
         rows, its = [], []
         for j, (a, b) in enumerate(zip(pid, aid)):
             su, it = self.res.pop(int(a))
-            au, _ = self.res.pop(int(b))
+            if int(b) < 0:
+                au = self.cache[(slot, seed, run0 + j)]
+            else:
+                au, _ = self.res.pop(int(b))
+                self.cache[(slot, seed, run0 + j)] = au
             u = probes.rademacher(seed, run0 + j, self.n) * m
             rows.append(np.concatenate([[au @ su, u @ su], au @ SX, SX.T @ u]))
             its.append(it)
