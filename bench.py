@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--m", type=int, default=150_000)
-    ap.add_argument("--phenos", type=int, default=16)
+    ap.add_argument("--phenos", type=int, default=32)
     ap.add_argument("--miss", type=float, default=0.02)
     ap.add_argument("--seed", type=int, default=1003)
     ap.add_argument("--mode", default="tf32x3", choices=["tf32x3", "tf32", "fp32"])
@@ -312,7 +312,8 @@ def run_ours(args, rank, world, local):
     specs = make_specs(ctx, args, args.seed + 17 * rank)
     mode = {"tf32x3": MV_TF32X3_TC, "tf32": MV_TF32_TC, "fp32": MV_FP32_SIMT}[args.mode]
     ctx.set_matvec_mode(mode)
-    cols = min(4096, max(256, 64 * args.phenos))
+    from saigegpu import serve as _serve
+    cols = _serve.columns_for(specs)
     setup_s = time.perf_counter() - t_setup
     for _ in range(args.warmup):
         run_batch(ctx, specs, cols)

@@ -386,8 +386,10 @@ class Runner:
 
     # -- admission
     def can_admit(self, spec):
-        need = 2 * (spec.nrun + 10) + 4
-        return bool(self.free_slots) and self.inflight_columns + need <= self.max_columns * 4
+        """Admit a fit only if its peak working set fits beside the columns already in flight
+        (results stay on the device until consumed, so oversubscribing could stall)."""
+        need = 2 * (spec.nrun + 10) + 8
+        return bool(self.free_slots) and self.inflight_columns + need <= self.max_columns
 
     def submit(self, spec, t_arrive=None):
         if not self.free_slots:
@@ -539,8 +541,16 @@ class Runner:
             self._finish(job)
 
 
-def fit_batch(ctx, specs, max_columns=2048, max_phenos=None):
+def columns_for(specs):
+    """Engine columns that hold every fit's peak working set at once (trace stage: probes,
+    their products, K.PY and the P A PY solves)."""
+    need = sum(2 * (s.nrun + 10) + 8 for s in specs)
+    return int(-(-need // 256) * 256)
+
+
+def fit_batch(ctx, specs, max_columns=None, max_phenos=None):
     """Fit all ``specs`` together; returns their result dicts (or exceptions) in order."""
+    max_columns = max(max_columns or 0, columns_for(specs))
     r = Runner(ctx, max_columns, max_phenos or max(1, len(specs)))
     ids = [r.submit(s) for s in specs]
     r.run()
