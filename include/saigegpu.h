@@ -62,6 +62,10 @@ void sg_ctx_destroy(sg_ctx *ctx);
 const char *sg_last_error(const sg_ctx *ctx);
 int sg_device_bytes_in_use(const sg_ctx *ctx, uint64_t *bytes);
 int sg_set_matvec_mode(sg_ctx *ctx, int mode);
+/* Failure-detection self-test: runs the tcgen05 kernels' bounded mbarrier wait on a barrier that
+ * nothing arrives at, with a budget of budget_ms (<= 2000).  Returns SG_ERR_TIMEOUT (the expected
+ * outcome) through the same device error flag the GEMMs use; the context stays usable. */
+int sg_selftest_wait_timeout(sg_ctx *ctx, double budget_ms);
 /* Tuning: how many CTAs (1, 2 or 4) of a thread-block cluster share one B tile through TMA multicast
  * in the tcgen05 SYRK and split-TF32 GRM.V (process-wide; saigegpu.tune picks them by timing). */
 int sg_set_tc_clusters(sg_ctx *ctx, int syrk, int grmv);

@@ -267,6 +267,18 @@ extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
   return SG_OK;
 }
 
+extern "C" int sg_selftest_wait_timeout(sg_ctx* c, double budget_ms) {
+  if (!c) return SG_ERR_INVALID;
+  if (budget_ms <= 0 || budget_ms > 2000) return set_err(c, SG_ERR_INVALID, "budget must be in (0, 2000] ms");
+  int waited_out = 0;
+  cudaError_t e = tc_wait_selftest(budget_ms, &waited_out, c->stream);
+  c->launches += 1;
+  if (e == cudaErrorLaunchTimeout && waited_out)
+    return set_err(c, SG_ERR_TIMEOUT, "bounded device wait gave up after %.1f ms", budget_ms);
+  if (e != cudaSuccess) return set_err(c, SG_ERR_CUDA, "self-test: %s", cudaGetErrorString(e));
+  return set_err(c, SG_ERR_STATE, "the wait completed although nothing arrived");
+}
+
 extern "C" int sg_set_tc_clusters(sg_ctx* c, int syrk, int grmv) {
   if (!c) return SG_ERR_INVALID;
   if (!tc_set_clusters(syrk, grmv)) return set_err(c, SG_ERR_INVALID, "cluster sizes must be 1, 2 or 4");

@@ -75,21 +75,40 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Bounded wait: returns false (and records ``code``) when the budget runs out
 // or another thread of this kernel already gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int code,
-                                          volatile int* abort_flag) {
+__device__ __forceinline__ bool mbar_wait_budget(uint64_t* bar, uint32_t parity, int code,
+                                                 volatile int* abort_flag, unsigned long long budget_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = gtimer();
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 255u) == 0u) {
       if (*abort_flag) return false;
-      if (gtimer() - t0 > kWaitBudgetNs) {
+      if (gtimer() - t0 > budget_ns) {
         *abort_flag = 1;
         atomicCAS(&g_tc_error, 0, code);
         return false;
       }
     }
   }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int code,
+                                          volatile int* abort_flag) {
+  return mbar_wait_budget(bar, parity, code, abort_flag, kWaitBudgetNs);
+}
+
+// Self-test of the bounded wait: waits on an mbarrier that nothing arrives at, with a short budget,
+// and reports through the same error flag the GEMM kernels use.
+__global__ void wait_selftest_kernel(unsigned long long budget_ns, int* waited_out) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *waited_out = mbar_wait_budget(&bar, 0u, 9, &abort_flag, budget_ns) ? 0 : 1;
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
@@ -459,6 +478,18 @@ void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStre
   split_tf32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, hi, lo, n);
 }
 
+
+cudaError_t tc_wait_selftest(double budget_ms, int* waited_out, cudaStream_t s) {
+  int* d = nullptr;
+  cudaError_t e = cudaMallocAsync(&d, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  wait_selftest_kernel<<<1, 32, 0, s>>>((unsigned long long)(budget_ms * 1e6), d);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(waited_out, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(d, s);
+  if (e != cudaSuccess) return e;
+  return check_error_flag(s);  // cudaErrorLaunchTimeout when the wait ran out (flag then cleared)
+}
 
 bool tc_available() {
   int dev = 0, major = 0, minor = 0;

@@ -83,6 +83,8 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
 // Plo (split operands) it accumulates K P + K Plo + Klo P (3xTF32).
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
                          const float* Plo, int64_t ncols, float* Y, cudaStream_t s);
+// Runs the kernels' bounded mbarrier wait on a barrier nothing arrives at (budget in ms).
+cudaError_t tc_wait_selftest(double budget_ms, int* waited_out, cudaStream_t s);
 // Cluster sizes (1, 2 or 4 CTAs sharing one B tile by TMA multicast) of the SYRK and split GRM.V.
 bool tc_set_clusters(int syrk, int grmv);
 void tc_get_clusters(int* syrk, int* grmv);

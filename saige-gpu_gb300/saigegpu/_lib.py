@@ -34,6 +34,7 @@ SIGNATURES = {
     "sg_set_matvec_mode": [c_ctx, C.c_int],
     "sg_kernel_launches": [c_ctx, P_u64],
     "sg_set_tc_clusters": [c_ctx, C.c_int, C.c_int],
+    "sg_selftest_wait_timeout": [c_ctx, C.c_double],
     "sg_get_tc_clusters": [c_ctx, P_i32, P_i32],
     "sg_setgeno": [c_ctx, P_u8, c_u64, c_i64, c_i64, P_i32, c_i64, P_u8, C.c_float, C.c_float,
                    P_i32, c_i64, C.c_float, C.c_int, C.c_int],
