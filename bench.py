@@ -297,6 +297,7 @@ def run_ours(args, rank, world, local):
     t_setup = time.perf_counter()
     ptr, ln = ctx.synth_bed(args.seed + rank, args.n, args.m, args.miss)
     ctx.setgeno_device(ptr, ln, args.n, args.m)
+    decode_t = ctx.build_timing()
     torch.cuda.synchronize()
     tune_report = None
     if args.no_tune or args.mode != "tf32x3":
@@ -309,6 +310,7 @@ def run_ours(args, rank, world, local):
         grm_s = tune_report["syrk"][tune_report["chosen"][0]]
     d = ctx.dims()
     syrk_flops = float(d["n"]) * (d["n"] + 1) * d["m_qc"]
+    bt = ctx.build_timing()
     specs = make_specs(ctx, args, args.seed + 17 * rank)
     mode = {"tf32x3": MV_TF32X3_TC, "tf32": MV_TF32_TC, "fp32": MV_FP32_SIMT}[args.mode]
     ctx.set_matvec_mode(mode)
@@ -367,7 +369,17 @@ def run_ours(args, rank, world, local):
         "gpu_launches": int(launches),
         "roofline": roof,
         "grm_build": {"seconds": round(grm_s, 3), "syrk_flops": syrk_flops,
-                      "tflops_incl_decode": round(syrk_flops / grm_s / 1e12, 1)},
+                      "tflops_incl_decode": round(syrk_flops / grm_s / 1e12, 1),
+                      "syrk_ms": round(bt["syrk_ms"], 2),
+                      "syrk_tflops": round(syrk_flops / (bt["syrk_ms"] * 1e-3) / 1e12, 1),
+                      "syrk_frac_of_bf16_peak": round(syrk_flops / (bt["syrk_ms"] * 1e-3) / 1e12 / peaks.get("bf16_tflops", 1900.0), 4),
+                      "zbuild_ms": round(bt["zbuild_ms"], 2),
+                      "zbuild_GBps": round((d["m_qc"] * ((d["n"] + 3) // 4) + 2.0 * ctx.n * d["m_qc"]) / (bt["zbuild_ms"] * 1e-3) / 1e9, 1)},
+        "decode": {"qc_ms": round(decode_t["qc_ms"], 2), "repack_ms": round(decode_t["repack_ms"], 2),
+                   "diag_ms": round(decode_t["diag_ms"], 2),
+                   "qc_GBps": round(args.m * ((args.n + 3) // 4) / (decode_t["qc_ms"] * 1e-3) / 1e9, 1),
+                   "repack_GBps": round(2.0 * d["m_qc"] * ((d["n"] + 3) // 4) / (decode_t["repack_ms"] * 1e-3) / 1e9, 1),
+                   "peak_GBps": peaks.get("hbm_gbs")},
         "per_fit": {"pcg_column_iterations": round(col_iters, 1), "columns": round(cols_per_fit, 1),
                     "converged": int(sum(1 for r in res_all if r["converged"])), "fits": len(res_all)},
         "setup_s": round(setup_s, 1),

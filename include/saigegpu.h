@@ -121,6 +121,9 @@ int sg_get_onesnp_stdgeno(sg_ctx *ctx, int64_t marker, float *out);
  * Z_r(Z_r' x) per call, FIT.cpp:1635-1708 and gpuSymMatMult.cu:211-252).
  */
 int sg_grm_build(sg_ctx *ctx, int precision);
+/* Device time (CUDA events) of the last setgeno / grm_build, ms: [0] per-marker QC, [1] re-pack +
+ * LUT, [2] GRM diagonal, [3] standardised-genotype build, [4] SYRK. */
+int sg_build_timing(sg_ctx *ctx, double *t5);
 /* Get_Diagof_StdGeno (FIT.cpp:665-704): sum_m z^2 per sample.  The f32 form is
  * accumulated in marker order in float exactly as the reference does. */
 int sg_grm_diag(sg_ctx *ctx, double *out);

@@ -114,6 +114,10 @@ struct sg_ctx {
   float* d_lv = nullptr;   // Z_j Z_j' P (cap_cols x np)
   float* d_lp = nullptr;   // P in full FP32 for the correction (cap_cols x np)
   std::vector<double> diag_loco;
+  // device time of the last setgeno ([0] QC, [1] re-pack + LUT, [2] diagonal) and grm_build
+  // ([3] Z build, [4] SYRK), in ms, from CUDA events on the context stream
+  double t_build[5] = {0, 0, 0, 0, 0};
+  cudaEvent_t tev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   // synthetic bed image
   uint8_t* d_synth = nullptr;
   uint64_t synth_len = 0;
@@ -124,6 +128,12 @@ struct sg_ctx {
 extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_pcg,
                                     const int64_t* ids_prod, int64_t k, uint64_t seed, int64_t run0,
                                     const double* SX, int64_t p, double* out, int32_t* iters);
+
+static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
 
 static int set_err(sg_ctx* c, int code, const char* fmt, ...) {
   if (!c) return code;
@@ -226,6 +236,7 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
     delete c;
     return SG_ERR_CUDA;
   }
+  for (auto& ev : c->tev) cudaEventCreate(&ev);
   *out = c;
   return SG_OK;
 }
@@ -355,9 +366,11 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
   SG_CUDA(c, cudaMemcpyAsync(d_mask, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, c->stream));
   if (m_bim) SG_CUDA(c, cudaMemcpyAsync(d_vrflag, vrflag.data(), m_bim, cudaMemcpyHostToDevice, c->stream));
   if (nn) SG_CUDA(c, cudaMemcpyAsync(d_sub, sub0.data(), nn * 4, cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
   launch_marker_qc(raw, raw_pitch, m_bim, n_fam, d_mask, nn, min_maf, max_missing, d_vrflag,
                    min_mac_vr, is_var_ratio, d_qc, c->stream);
   SG_LAUNCHED(c, 1);
+  SG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
   std::vector<MarkerQC> qc(m_bim);
   if (m_bim) SG_CUDA(c, cudaMemcpyAsync(qc.data(), d_qc, m_bim * sizeof(MarkerQC), cudaMemcpyDeviceToHost, c->stream));
   SG_TRY(sync(c));
@@ -398,6 +411,7 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
   SG_TRY(dev_alloc_t(c, &c->d_packed_vr, (size_t)std::max<int64_t>(c->m_vr * c->pitch, 16)));
   SG_TRY(dev_alloc_t(c, &c->d_lut, (size_t)std::max<int64_t>(c->m_qc * 4, 4)));
   SG_TRY(dev_alloc_t(c, &c->d_lut_vr, (size_t)std::max<int64_t>(c->m_vr * 4, 4)));
+  SG_CUDA(c, cudaEventRecord(c->tev[2], c->stream));
   launch_repack(raw, raw_pitch, d_src, d_qc, c->m_qc, d_sub, nn, identity ? 1 : 0, c->d_packed,
                 c->pitch, c->stream);
   launch_repack(raw, raw_pitch, d_src + c->m_qc, d_qc, c->m_vr, d_sub, nn, identity ? 1 : 0,
@@ -405,7 +419,10 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
   launch_lut(d_qc, d_src, c->m_qc, c->d_lut, c->stream);
   launch_lut(d_qc, d_src + c->m_qc, c->m_vr, c->d_lut_vr, c->stream);
   SG_LAUNCHED(c, 4);
+  SG_CUDA(c, cudaEventRecord(c->tev[3], c->stream));
   SG_TRY(sync(c));
+  c->t_build[0] = ev_ms(c->tev[0], c->tev[1]);
+  c->t_build[1] = ev_ms(c->tev[2], c->tev[3]);
   dev_free(c, d_src);
   dev_free(c, d_mask);
   dev_free(c, d_vrflag);
@@ -414,8 +431,10 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
   // GRM diagonal from the packed genotypes
   SG_TRY(dev_alloc_t(c, &c->d_diag, (size_t)std::max<int64_t>(nn, 1)));
   SG_TRY(dev_alloc_t(c, &c->d_diag32, (size_t)std::max<int64_t>(nn, 1)));
+  SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
   launch_diag(c->d_packed, c->pitch, c->d_lut, c->m_qc, nn, c->d_diag, c->d_diag32, c->stream);
   SG_LAUNCHED(c, 1);
+  SG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
   c->diag.resize(nn);
   c->diag32.resize(nn);
   if (nn) {
@@ -423,6 +442,7 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
     SG_CUDA(c, cudaMemcpyAsync(c->diag32.data(), c->d_diag32, nn * 4, cudaMemcpyDeviceToHost, c->stream));
   }
   SG_TRY(sync(c));
+  c->t_build[2] = ev_ms(c->tev[0], c->tev[1]);
   c->have_geno = true;
   return SG_OK;
 }
@@ -612,22 +632,32 @@ extern "C" int sg_grm_build(sg_ctx* c, int precision) {
   if (precision == SG_GRM_FP32_SIMT) {
     float* Z = nullptr;
     SG_TRY(dev_alloc_t(c, &Z, (size_t)(np * mp)));
+    SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
     launch_zbuild_f32(c->d_packed, c->pitch, c->d_lut, c->m_qc, c->nn, np, mp, Z, c->stream);
+    SG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
     launch_gemm_nt_f32(Z, mp, Z, mp, c->d_K, np, np, np, mp, scale, 2, c->stream);
     SG_LAUNCHED(c, 2);
+    SG_CUDA(c, cudaEventRecord(c->tev[2], c->stream));
     SG_TRY(sync(c));
+    c->t_build[3] = ev_ms(c->tev[0], c->tev[1]);
+    c->t_build[4] = ev_ms(c->tev[1], c->tev[2]);
     dev_free(c, Z);
   } else {
     void* Zh = nullptr;
     void* Zl = nullptr;
     SG_TRY(dev_alloc(c, &Zh, (size_t)(np * mp * 2)));
     if (precision == SG_GRM_BF16X3_TC) SG_TRY(dev_alloc(c, &Zl, (size_t)(np * mp * 2)));
+    SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
     launch_zbuild_bf16(c->d_packed, c->pitch, c->d_lut, c->m_qc, c->nn, np, mp, Zh, Zl, c->stream);
     SG_LAUNCHED(c, 1);
+    SG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
     cudaError_t e = tc_syrk_bf16(Zh, Zl, np, mp, c->d_K, scale, c->stream);
+    cudaEventRecord(c->tev[2], c->stream);
     if (e != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 SYRK: %s", cudaGetErrorString(e));
     SG_LAUNCHED(c, 1);
     SG_TRY(sync(c));
+    c->t_build[3] = ev_ms(c->tev[0], c->tev[1]);
+    c->t_build[4] = ev_ms(c->tev[1], c->tev[2]);
     dev_free(c, Zh);
     dev_free(c, Zl);
   }
@@ -678,6 +708,12 @@ extern "C" int sg_grm_matmul_tf32x3_noalloc(sg_ctx* c, const float* P_dev, int64
   c->launches += 2;
   if (e != cudaSuccess) return set_err(c, e == cudaErrorLaunchTimeout ? SG_ERR_TIMEOUT : SG_ERR_CUDA,
                                        "no-alloc GRM.V: %s", cudaGetErrorString(e));
+  return SG_OK;
+}
+
+extern "C" int sg_build_timing(sg_ctx* c, double* t5) {
+  if (!c || !t5) return SG_ERR_INVALID;
+  for (int i = 0; i < 5; ++i) t5[i] = c->t_build[i];
   return SG_OK;
 }
 

@@ -54,6 +54,7 @@ SIGNATURES = {
     "sg_get_onesnp_stdgeno": [c_ctx, c_i64, P_f32],
     "sg_grm_build": [c_ctx, C.c_int],
     "sg_grm_diag": [c_ctx, P_f64],
+    "sg_build_timing": [c_ctx, P_f64],
     "sg_grm_diag_f32": [c_ctx, P_f32],
     "sg_grm_get": [c_ctx, P_f32],
     "sg_grm_matmul": [c_ctx, P_f64, c_i64, P_f64],

@@ -182,6 +182,11 @@ class Context:
     def grm_build(self, precision=GRM_FP32_SIMT):
         self._call("sg_grm_build", int(precision))
 
+    def build_timing(self):
+        t = np.zeros(5, np.float64)
+        self._call("sg_build_timing", _ptr(t, L.P_f64))
+        return dict(qc_ms=t[0], repack_ms=t[1], diag_ms=t[2], zbuild_ms=t[3], syrk_ms=t[4])
+
     def grm_diag(self):
         out = np.empty(self.n, np.float64)
         self._call("sg_grm_diag", _ptr(out, L.P_f64))
