@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--mode", default="tf32x3", choices=["tf32x3", "tf32", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster-shape autotuner")
+    ap.add_argument("--blocking-runner", action="store_true",
+                    help="step the engine synchronously instead of overlapping the driver with the next step")
     ap.add_argument("--serve-requests", type=int, default=32,
                     help="requests of the serving-form block (Poisson arrivals, 0 = skip)")
     ap.add_argument("--json-out", default=None)
@@ -170,10 +172,10 @@ def make_specs(ctx, args, rng_seed):
     return specs
 
 
-def run_batch(ctx, specs, cols):
+def run_batch(ctx, specs, cols, pipelined=True):
     from saigegpu import serve
     t0 = time.perf_counter()
-    res, jobs = serve.fit_batch(ctx, specs, max_columns=cols)
+    res, jobs = serve.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined)
     wall = time.perf_counter() - t0
     errs = [r for r in res if isinstance(r, Exception)]
     if errs:
@@ -225,7 +227,8 @@ def serving_block(ctx, args, cols):
         f0 = prep.make_fit0(y[S], C[S], trait, True)
         arrivals.append((t, serve.FitSpec(f0, trait, mask=mask)))
     t0 = time.perf_counter()
-    done = serve.serve(ctx, arrivals, max_columns=cols, max_phenos=max(4, args.phenos))
+    done = serve.serve(ctx, arrivals, max_columns=cols, max_phenos=max(4, args.phenos),
+                       pipelined=not args.blocking_runner)
     wall = time.perf_counter() - t0
     lat = sorted(j.t_done - j.t_arrive for j in done)
     ok = sum(1 for j in done if j.error is None)
@@ -318,7 +321,7 @@ def run_ours(args, rank, world, local):
     cols = _serve.columns_for(specs)
     setup_s = time.perf_counter() - t_setup
     for _ in range(args.warmup):
-        run_batch(ctx, specs, cols)
+        run_batch(ctx, specs, cols, not args.blocking_runner)
     L0 = ctx.kernel_launches()
     ctx.engine_reset_timing()
     barrier(world)
@@ -326,7 +329,7 @@ def run_ours(args, rank, world, local):
     walls, jobs_all, res_all, host_t = [], [], [], {}
     with Clocks(local) as clk:
         for _ in range(args.steps):
-            res, jobs, wall = run_batch(ctx, specs, cols)
+            res, jobs, wall = run_batch(ctx, specs, cols, not args.blocking_runner)
             walls.append(wall)
             jobs_all += jobs
             res_all += res

@@ -238,6 +238,16 @@ int sg_engine_submit_probes(sg_ctx *ctx, int64_t slot, int kind, uint64_t seed, 
 /* Run up to max_steps engine steps (admitting queued columns as slots free up).
  * Returns after the step in which at least one column retired, or when idle. */
 int sg_engine_run(sg_ctx *ctx, int64_t max_steps, int64_t *n_finished);
+/* Asynchronous stepping (no reference counterpart: the reference's PCG loop, FIT.cpp:2593-2680,
+ * blocks on every product).  sg_engine_launch admits queued columns and starts one step without
+ * waiting for it (*launched = 0 when nothing is active; *n_finished counts columns that retired
+ * at admission); sg_engine_finish waits for that step and retires its finished columns.  Between
+ * the two the caller may submit (joins the next launch), poll, fetch or cancel, run
+ * sg_engine_probe_dots and upload weights with sg_engine_set_pheno for slots without running
+ * columns: those calls use a second stream and do not wait for the step.  sg_engine_run finishes
+ * an in-flight step first. */
+int sg_engine_launch(sg_ctx *ctx, int64_t *n_finished, int *launched);
+int sg_engine_finish(sg_ctx *ctx, int64_t *n_finished);
 /* By default a finished column's result is copied to the host and its column freed at once.
  * With hold != 0 finished results stay on the device (keeping their column) until fetched,
  * cancelled or consumed by sg_engine_probe_dots; sg_engine_run then fails with SG_ERR_STATE

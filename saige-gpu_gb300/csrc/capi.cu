@@ -58,6 +58,10 @@ struct Engine {
   int64_t steps = 0, retired = 0, col_iters = 0, grm_passes = 0;
   std::vector<int64_t> finished;  // ids retired since the last poll
   bool hold = false;              // keep finished results on the device until fetched/consumed
+  ColState* h_pin = nullptr;      // pinned mirror for the asynchronous state read-back of a step
+  bool inflight = false;          // a launched step has not been finished yet
+  int64_t inflight_ncols = 0, inflight_occupied = 0, inflight_hi = 0;
+  std::vector<int64_t> pending_release;  // columns freed on the host, reset on the device at the next launch
   float* Pflo = nullptr;          // low TF32 halves of Pf (split-TF32 mode)
   double* d_sx = nullptr;         // probe_dots: Sigma^-1 X block
   double* d_dpart = nullptr;      // probe_dots: block partial sums
@@ -79,6 +83,7 @@ struct sg_ctx {
   uint64_t budget = 0;
   uint64_t in_use = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // result copies, probe reductions and slot uploads overlap a step here
   std::string err;
   std::string err_pending;
   uint64_t launches = 0;
@@ -208,6 +213,11 @@ static int sync(sg_ctx* c) {
   return SG_OK;
 }
 
+static int sync_side(sg_ctx* c) {
+  SG_CUDA(c, cudaStreamSynchronize(c->side));
+  return SG_OK;
+}
+
 static bool all_finite(const float* v, int64_t n) {
   for (int64_t i = 0; i < n; ++i)
     if (!std::isfinite(v[i])) return false;
@@ -237,6 +247,11 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
     return SG_ERR_CUDA;
   }
   for (auto& ev : c->tev) cudaEventCreate(&ev);
+  if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return SG_ERR_CUDA;
+  }
   *out = c;
   return SG_OK;
 }
@@ -245,8 +260,11 @@ extern "C" void sg_ctx_destroy(sg_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  cudaStreamSynchronize(c->side);
+  if (c->eng.h_pin) cudaFreeHost(c->eng.h_pin);
   for (auto& kv : c->allocs) cudaFree(kv.first);
   c->allocs.clear();
+  cudaStreamDestroy(c->side);
   cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -749,6 +767,11 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.pcache);
   e.pcache_key.clear();
   e.dots_cap_sx = e.dots_cap_part = e.dots_cap_cols = 0;
+  if (e.inflight) cudaStreamSynchronize(c->stream);
+  e.inflight = false;
+  e.pending_release.clear();
+  if (e.h_pin) cudaFreeHost(e.h_pin);
+  e.h_pin = nullptr;
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
   e.finished.clear();
@@ -766,10 +789,17 @@ static void engine_free(sg_ctx* c) {
 
 // Drop every queued and in-flight request (the blocking drop-ins own the engine); results are
 // copied out at retirement from here on.
+static int apply_releases(sg_ctx* c);
+
 static int engine_clear(sg_ctx* c) {
   Engine& e = c->eng;
   e.hold = false;
   if (e.cap_cols == 0) return SG_OK;
+  if (e.inflight) {  // an abandoned asynchronous step: let it drain, drop its results
+    e.inflight = false;
+    SG_TRY(sync(c));
+  }
+  SG_TRY(apply_releases(c));
   bool any = false;
   for (int64_t col = 0; col < (int64_t)e.col_req.size(); ++col) {
     if (e.col_req[col] < 0) continue;
@@ -827,6 +857,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   e.cap_ph = max_phenos;
   for (auto& ev : e.ev)
     if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
+  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
   e.h_st.assign(max_columns, ColState{});
   for (auto& s : e.h_st) { s.kind = -1; s.active = 0; }
   SG_CUDA(c, cudaMemcpyAsync(e.d_st, e.h_st.data(), max_columns * sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
@@ -879,12 +910,12 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     winv[i] = 1.0 / w[i];
     minv[i] = 1.0 / d[i];
   }
-  SG_CUDA(c, cudaMemcpyAsync(e.winv + slot * e.np, winv.data(), e.np * 8, cudaMemcpyHostToDevice, c->stream));
-  SG_CUDA(c, cudaMemcpyAsync(e.minv + slot * e.np, minv.data(), e.np * 8, cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(c, cudaMemcpyAsync(e.winv + slot * e.np, winv.data(), e.np * 8, cudaMemcpyHostToDevice, c->side));
+  SG_CUDA(c, cudaMemcpyAsync(e.minv + slot * e.np, minv.data(), e.np * 8, cudaMemcpyHostToDevice, c->side));
   e.h_ph[slot] = PhenoState{tau[0], tau[1]};
-  SG_CUDA(c, cudaMemcpyAsync(e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(c, cudaMemcpyAsync(e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), cudaMemcpyHostToDevice, c->side));
   e.ph_set[slot] = 1;
-  return sync(c);
+  return sync_side(c);
 }
 
 static int engine_submit_common(sg_ctx* c, int64_t slot, int kind, const double* B, bool probe,
@@ -927,6 +958,7 @@ extern "C" int sg_engine_submit_probes(sg_ctx* c, int64_t slot, int kind, uint64
 // Move queued requests into free columns, staged through e.B, and initialise them.
 static int engine_admit(sg_ctx* c) {
   Engine& e = c->eng;
+  SG_TRY(apply_releases(c));
   while (!e.queue.empty()) {
     std::vector<int32_t> cols;
     std::vector<int64_t> admitted;
@@ -1032,7 +1064,7 @@ static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf) {
       c->launches += 1;
     }
     cudaError_t err = tc_gemm_tf32(c->d_K, split ? c->d_Klo : nullptr, e.np, e.Pf,
-                                   split ? e.Pflo : nullptr, ncols, e.Yf, c->stream);
+                                   split ? e.Pflo : nullptr, ncols, e.Yf, c->stream, false);
     if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 GRM.V: %s", cudaGetErrorString(err));
     c->launches += 1;
     return SG_OK;
@@ -1058,7 +1090,10 @@ static int64_t engine_gemm_cols(const sg_ctx* c) {
   return ncols;
 }
 
-static int engine_step(sg_ctx* c, int64_t* n_finished) {
+// First half of a step over columns [0, hi_col): GRM product + the FP64 PCG vector work, the
+// step's timing events and an asynchronous read-back of the column states into pinned memory.
+// Nothing here waits for the device.
+static int step_launch(sg_ctx* c) {
   Engine& e = c->eng;
   const int64_t ncols = engine_gemm_cols(c);
   int64_t occupied = 0;
@@ -1077,8 +1112,25 @@ static int engine_step(sg_ctx* c, int64_t* n_finished) {
   launch_pcg_dir(e.np, e.hi_col, e.d_st, e.Z, e.P, e.Pf, c->stream);
   SG_LAUNCHED(c, 5);
   SG_CUDA(c, cudaEventRecord(e.ev[2], c->stream));
-  SG_CUDA(c, cudaMemcpyAsync(e.h_st.data(), e.d_st, e.hi_col * sizeof(ColState), cudaMemcpyDeviceToHost, c->stream));
+  SG_CUDA(c, cudaMemcpyAsync(e.h_pin, e.d_st, e.hi_col * sizeof(ColState), cudaMemcpyDeviceToHost, c->stream));
+  e.inflight = true;
+  e.inflight_ncols = ncols;
+  e.inflight_occupied = occupied;
+  e.inflight_hi = e.hi_col;
+  return SG_OK;
+}
+
+// Second half: wait for the step, account its time, retire the columns that finished (result
+// held in X[col], or copied out and the column freed).
+static int step_finish(sg_ctx* c, int64_t* n_finished) {
+  Engine& e = c->eng;
+  e.inflight = false;
   SG_TRY(sync(c));
+  if (c->mv_mode == SG_MV_TF32_TC || c->mv_mode == SG_MV_TF32X3_TC) {
+    const cudaError_t err = tc_check_error(c->stream);
+    if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 GRM.V: %s", cudaGetErrorString(err));
+  }
+  const int64_t ncols = e.inflight_ncols, occupied = e.inflight_occupied, hi = e.inflight_hi;
   {
     float ms_gemm = 0.f, ms_step = 0.f;
     cudaEventElapsedTime(&ms_gemm, e.ev[0], e.ev[1]);
@@ -1093,8 +1145,11 @@ static int engine_step(sg_ctx* c, int64_t* n_finished) {
   }
   e.steps += 1;
   e.grm_passes += 1;
+  // columns released while the step ran keep their host state (free); the rest take the device's
+  for (int64_t col = 0; col < hi; ++col)
+    if (e.col_req[col] >= 0) e.h_st[col] = e.h_pin[col];
   int64_t fin = 0;
-  for (int64_t col = 0; col < e.hi_col; ++col) {
+  for (int64_t col = 0; col < hi; ++col) {
     const int64_t id = e.col_req[col];
     if (id < 0) continue;
     ColState& s = e.h_st[col];
@@ -1130,6 +1185,11 @@ static int engine_step(sg_ctx* c, int64_t* n_finished) {
   SG_TRY(sync(c));
   *n_finished += fin;
   return SG_OK;
+}
+
+static int engine_step(sg_ctx* c, int64_t* n_finished) {
+  SG_TRY(step_launch(c));
+  return step_finish(c, n_finished);
 }
 
 // Columns admitted with r'r <= tol retire without a step (iter = 0, x = 0).
@@ -1171,6 +1231,13 @@ extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) 
   Engine& e = c->eng;
   if (e.cap_cols == 0) return set_err(c, SG_ERR_STATE, "engine not reserved");
   int64_t fin = 0;
+  if (e.inflight) {
+    SG_TRY(step_finish(c, &fin));
+    if (fin > 0 || max_steps <= 0) {
+      if (n_finished) *n_finished = fin;
+      return SG_OK;
+    }
+  }
   for (int64_t s = 0; s < max_steps; ++s) {
     SG_TRY(engine_admit(c));
     SG_TRY(engine_retire_immediate(c, &fin));
@@ -1189,17 +1256,69 @@ extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) 
   return SG_OK;
 }
 
-// Free a column (running or holding a result) for the next admission.
+// Asynchronous stepping: sg_engine_launch starts one step and returns at once; sg_engine_finish
+// waits for it and retires its finished columns.  Between the two the caller may fetch held
+// results, run probe reductions, upload weights of idle slots and submit work (it joins the next
+// launch); those calls use the side stream and never wait for the step.
+extern "C" int sg_engine_launch(sg_ctx* c, int64_t* n_finished, int* launched) {
+  NEED_GRM(c);
+  Engine& e = c->eng;
+  if (e.cap_cols == 0) return set_err(c, SG_ERR_STATE, "engine not reserved");
+  if (e.inflight) return set_err(c, SG_ERR_STATE, "a step is in flight: finish it first");
+  int64_t fin = 0;
+  if (launched) *launched = 0;
+  SG_TRY(engine_admit(c));
+  SG_TRY(engine_retire_immediate(c, &fin));
+  if (n_finished) *n_finished = fin;
+  if (e.n_active == 0) {
+    if (!e.queue.empty() && fin == 0)
+      return set_err(c, SG_ERR_STATE,
+                     "engine full: %lld queued columns wait for columns that hold unconsumed results",
+                     (long long)e.queue.size());
+    return SG_OK;
+  }
+  SG_TRY(step_launch(c));
+  if (launched) *launched = 1;
+  return SG_OK;
+}
+
+extern "C" int sg_engine_finish(sg_ctx* c, int64_t* n_finished) {
+  if (!c) return SG_ERR_INVALID;
+  int64_t fin = 0;
+  if (c->eng.inflight) SG_TRY(step_finish(c, &fin));
+  if (n_finished) *n_finished = fin;
+  return SG_OK;
+}
+
+// Free a column (running or holding a result) for the next admission.  The host bookkeeping is
+// immediate; the device-side reset (state, zero P) waits for the next launch, so a release never
+// queues behind a step in flight.
 static int release_col(sg_ctx* c, int64_t col) {
   Engine& e = c->eng;
   ColState s{};
   s.kind = -1;
   s.active = 0;
   e.h_st[col] = s;
-  SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
-  SG_CUDA(c, cudaMemsetAsync(e.Pf + col * e.np, 0, e.np * 4, c->stream));
   e.col_req[col] = -1;
+  e.pending_release.push_back(col);
   while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
+  return SG_OK;
+}
+
+static int apply_releases(sg_ctx* c) {
+  Engine& e = c->eng;
+  if (e.pending_release.empty()) return SG_OK;
+  ColState s{};
+  s.kind = -1;
+  s.active = 0;
+  for (int64_t col : e.pending_release) {
+    if (e.col_req[col] != -1) continue;  // reused since: admission initialises it
+    e.h_st[col] = s;
+    // pageable source: the call returns once the bytes are staged
+    SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+    SG_CUDA(c, cudaMemsetAsync(e.Pf + col * e.np, 0, e.np * 4, c->stream));
+  }
+  e.pending_release.clear();
   return SG_OK;
 }
 
@@ -1211,9 +1330,9 @@ extern "C" int sg_engine_fetch(sg_ctx* c, int64_t id, double* x, int32_t* iters)
   Req& r = it->second;
   if (r.state != 2) return set_err(c, SG_ERR_STATE, "request %lld not finished", (long long)id);
   if (r.col >= 0) {
-    if (x) SG_CUDA(c, cudaMemcpyAsync(x, e.X + r.col * e.np, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (x) SG_CUDA(c, cudaMemcpyAsync(x, e.X + r.col * e.np, c->nn * 8, cudaMemcpyDeviceToHost, c->side));
     SG_TRY(release_col(c, r.col));
-    SG_TRY(sync(c));
+    SG_TRY(sync_side(c));
   } else if (x) {
     std::copy(r.x.begin(), r.x.end(), x);
   }
@@ -1231,7 +1350,6 @@ extern "C" int sg_engine_cancel(sg_ctx* c, int64_t id) {
   if ((r.state == 1 || r.state == 2) && r.col >= 0) {
     if (r.state == 1) e.n_active -= 1;
     SG_TRY(release_col(c, r.col));
-    SG_TRY(sync(c));
   }
   e.reqs.erase(it);  // a queued id is skipped at admission
   return SG_OK;
@@ -1300,7 +1418,7 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
       }
       if (ci >= 0) {
         double* dst = e.pcache + (slot * kProbeCache + ci) * e.np;
-        SG_CUDA(c, cudaMemcpyAsync(dst, au[j], e.np * 8, cudaMemcpyDeviceToDevice, c->stream));
+        SG_CUDA(c, cudaMemcpyAsync(dst, au[j], e.np * 8, cudaMemcpyDeviceToDevice, c->side));
         au[j] = dst;
       }
     }
@@ -1323,18 +1441,18 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
     e.dots_cap_cols = (size_t)(2 * k);
   }
   if (p > 0) {
-    SG_CUDA(c, cudaMemsetAsync(e.d_sx, 0, need_sx * 8, c->stream));
-    SG_CUDA(c, cudaMemcpy2DAsync(e.d_sx, e.np * 8, SX, c->nn * 8, c->nn * 8, p, cudaMemcpyHostToDevice, c->stream));
+    SG_CUDA(c, cudaMemsetAsync(e.d_sx, 0, need_sx * 8, c->side));
+    SG_CUDA(c, cudaMemcpy2DAsync(e.d_sx, e.np * 8, SX, c->nn * 8, c->nn * 8, p, cudaMemcpyHostToDevice, c->side));
   }
   std::vector<const double*> ptrs(su);
   ptrs.insert(ptrs.end(), au.begin(), au.end());
-  SG_CUDA(c, cudaMemcpyAsync(e.d_dcols, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(c, cudaMemcpyAsync(e.d_dcols, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice, c->side));
   launch_probe_dots(e.np, c->nn, reinterpret_cast<const double* const*>(e.d_dcols), k,
-                    e.minv + slot * e.np, seed, run0, e.d_sx, p, e.d_dpart, nblk, c->stream);
+                    e.minv + slot * e.np, seed, run0, e.d_sx, p, e.d_dpart, nblk, c->side);
   SG_LAUNCHED(c, 1);
   std::vector<double> part(need_part);
-  SG_CUDA(c, cudaMemcpyAsync(part.data(), e.d_dpart, need_part * 8, cudaMemcpyDeviceToHost, c->stream));
-  SG_TRY(sync(c));
+  SG_CUDA(c, cudaMemcpyAsync(part.data(), e.d_dpart, need_part * 8, cudaMemcpyDeviceToHost, c->side));
+  SG_TRY(sync_side(c));
   for (int64_t j = 0; j < k; ++j)
     for (int64_t v = 0; v < nv; ++v) {
       double acc = 0.0;
@@ -1349,7 +1467,7 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
     SG_TRY(release_col(c, it->second.col));
     e.reqs.erase(it);
   }
-  return sync(c);
+  return sync_side(c);
 }
 
 extern "C" int sg_engine_hold_results(sg_ctx* c, int hold) {

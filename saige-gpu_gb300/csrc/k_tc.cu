@@ -581,7 +581,7 @@ static cudaError_t launch_grmv_split(const CUtensorMap& a, const CUtensorMap& b,
 }
 
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
-                         const float* Plo, int64_t ncols, float* Y, cudaStream_t s) {
+                         const float* Plo, int64_t ncols, float* Y, cudaStream_t s, bool check) {
   if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0) return cudaErrorInvalidValue;
   const bool split = Klo != nullptr && Plo != nullptr;
   const int BN = tc_gemm_tile_n(ncols, split);
@@ -634,8 +634,10 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
     }
   }
   if (e != cudaSuccess) return e;
-  return check_error_flag(s);
+  return check ? check_error_flag(s) : cudaSuccess;
 }
+
+cudaError_t tc_check_error(cudaStream_t s) { return check_error_flag(s); }
 
 // ---------------------------------------------------------------- GRM.V that allocates nothing
 //

@@ -80,9 +80,14 @@ bool tc_available();
 cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t mp, float* K,
                          float scale, cudaStream_t s);
 // Y^T (ncols x np) = K (np x np fp32, tf32 MMA) * P^T with P (ncols x np fp32).  With Klo and
-// Plo (split operands) it accumulates K P + K Plo + Klo P (3xTF32).
+// Plo (split operands) it accumulates K P + K Plo + Klo P (3xTF32).  With check = false it only
+// launches (no stream synchronisation); the caller then reads the kernels' wait-error flag with
+// tc_check_error after the stream has drained.
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
-                         const float* Plo, int64_t ncols, float* Y, cudaStream_t s);
+                         const float* Plo, int64_t ncols, float* Y, cudaStream_t s, bool check = true);
+// Synchronises s, then reads and clears the flag the tcgen05 kernels set when a bounded wait ran
+// out (cudaErrorLaunchTimeout in that case).
+cudaError_t tc_check_error(cudaStream_t s);
 // Runs the kernels' bounded mbarrier wait on a barrier nothing arrives at (budget in ms).
 cudaError_t tc_wait_selftest(double budget_ms, int* waited_out, cudaStream_t s);
 // Cluster sizes (1, 2 or 4 CTAs sharing one B tile by TMA multicast) of the SYRK and split GRM.V.

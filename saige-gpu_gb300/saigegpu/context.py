@@ -378,6 +378,19 @@ class Context:
         self._call("sg_engine_run", int(max_steps), C.byref(fin))
         return fin.value
 
+    def engine_launch(self):
+        """Start one step without waiting; returns (launched, columns retired at admission)."""
+        fin = C.c_int64()
+        launched = C.c_int32()
+        self._call("sg_engine_launch", C.byref(fin), C.byref(launched))
+        return bool(launched.value), fin.value
+
+    def engine_finish(self):
+        """Wait for the launched step (if any) and retire its columns; returns how many finished."""
+        fin = C.c_int64()
+        self._call("sg_engine_finish", C.byref(fin))
+        return fin.value
+
     def engine_fetch(self, rid, out=None):
         x = np.empty(self.n, np.float64) if out is None else out
         it = C.c_int32()

@@ -363,7 +363,8 @@ class _Job:
 class Runner:
     """Continuous batching of many null-model fits over one engine."""
 
-    def __init__(self, ctx, max_columns=2048, max_phenos=64, min_columns_per_fit=2 * (30 + 10) + 8):
+    def __init__(self, ctx, max_columns=2048, max_phenos=64, min_columns_per_fit=2 * (30 + 10) + 8,
+                 pipelined=False):
         if max_columns < min_columns_per_fit:
             # a fit's trace stage keeps ~2 (nrun + 10) + 4 columns in flight at once
             raise ValueError("max_columns=%d is below one fit's working set (%d)" % (max_columns, min_columns_per_fit))
@@ -381,6 +382,10 @@ class Runner:
         self.finished = []
         self._next = 0
         self.inflight_columns = 0
+        # pipelined: step k+1 runs on the GPU while the fits consume step k's results (their new
+        # columns join step k+2)
+        self.pipelined = bool(pipelined) and hasattr(ctx, "engine_launch")
+        self._launched = False
         # wall-clock seconds by activity (engine steps incl. their sync, result copies, driver math)
         self.t = {"engine": 0.0, "fetch": 0.0, "probe_dots": 0.0, "pheno": 0.0, "submit": 0.0, "driver": 0.0}
 
@@ -510,9 +515,19 @@ class Runner:
     def step(self):
         """One engine step; resume every fit whose awaited columns are complete."""
         t0 = time.perf_counter()
-        self.ctx.engine_run(1)
+        if self.pipelined:
+            if self._launched:
+                self.ctx.engine_finish()
+            self._launched, _ = self.ctx.engine_launch()
+        else:
+            self.ctx.engine_run(1)
         ids = self.ctx.engine_poll()
         self.t["engine"] += time.perf_counter() - t0
+        if self.pipelined and not self._launched and len(ids) == 0:
+            stuck = [j.jid for j in self.jobs.values()
+                     if j.waiting is not None and not all(i in self.done for i in j.waiting[1])]
+            if stuck:
+                raise RuntimeError("engine idle while fits %s wait for columns" % stuck)
         for rid in ids:
             rid = int(rid)
             if rid not in self.owner:
@@ -531,7 +546,18 @@ class Runner:
         while self.jobs and steps < max_steps:
             self.step()
             steps += 1
+        self.drain()
         return steps
+
+    def drain(self):
+        """Wait for a launched step whose columns no fit awaits any more (cancelled or failed fits)."""
+        if self._launched:
+            self.ctx.engine_finish()
+            self._launched = False
+            for rid in self.ctx.engine_poll():
+                if int(rid) in self.owner:
+                    self.done.add(int(rid))
+                    self.inflight_columns -= 1
 
     def cancel(self, jid):
         job = self.jobs.get(jid)
@@ -548,10 +574,10 @@ def columns_for(specs):
     return int(-(-need // 256) * 256)
 
 
-def fit_batch(ctx, specs, max_columns=None, max_phenos=None):
+def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=False):
     """Fit all ``specs`` together; returns their result dicts (or exceptions) in order."""
     max_columns = max(max_columns or 0, columns_for(specs))
-    r = Runner(ctx, max_columns, max_phenos or max(1, len(specs)))
+    r = Runner(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined=pipelined)
     ids = [r.submit(s) for s in specs]
     r.run()
     by = {j.jid: j for j in r.finished}
@@ -561,12 +587,12 @@ def fit_batch(ctx, specs, max_columns=None, max_phenos=None):
     return [by[i].result if by[i].error is None else by[i].error for i in ids], jobs
 
 
-def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter):
+def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter, pipelined=False):
     """Serve a stream of (t_arrival_seconds, FitSpec): admit as slots and columns free up.
 
     Returns the finished jobs (with t_arrive / t_start / t_done) in completion order.
     """
-    r = Runner(ctx, max_columns, max_phenos)
+    r = Runner(ctx, max_columns, max_phenos, pipelined=pipelined)
     pending = sorted(arrivals, key=lambda a: a[0])
     t0 = clock()
     k = 0
@@ -578,5 +604,7 @@ def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counte
         if r.jobs:
             r.step()
         elif k < len(pending):
+            r.drain()
             time.sleep(max(0.0, min(0.01, pending[k][0] - now)))
+    r.drain()
     return r.finished

@@ -71,3 +71,64 @@ def test_serving_stream(cohort):
     assert all(j.error is None for j in done)
     lat = [j.t_done - j.t_arrive for j in done]
     assert min(lat) > 0
+
+
+@pytest.mark.parametrize("mode", [MV_FP32_SIMT, MV_TF32X3_TC])
+def test_pipelined_runner_equals_synchronous(cohort, mode):
+    """Launch/finish stepping (host consumes step k while step k+1 runs) changes when columns
+    start, not what they compute: every fit is bit-identical to the blocking runner's."""
+    ctx, grm, specs, refs = cohort
+    ctx.set_matvec_mode(mode)
+    try:
+        sync, _ = serve.fit_batch(ctx, specs, max_columns=256)
+        pipe, _ = serve.fit_batch(ctx, specs, max_columns=256, pipelined=True)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+    for a, b in zip(pipe, sync):
+        assert not isinstance(a, Exception), a
+        np.testing.assert_array_equal(a["theta"], b["theta"])
+        np.testing.assert_array_equal(a["coefficients"], b["coefficients"])
+        np.testing.assert_array_equal(a["linear_predictors"], b["linear_predictors"])
+
+
+def test_launch_finish_with_host_calls_in_flight(cohort):
+    """Fetch, cancel, submit and weight uploads of an idle slot while a step runs."""
+    ctx, grm, specs, refs = cohort
+    n = ctx.n
+    rng = np.random.default_rng(11)
+    w = rng.uniform(0.5, 2.0, n)
+    tau = np.array([1.0, 0.4])
+    B = rng.standard_normal((n, 6))
+    ctx.engine_reserve(128, 2)
+    ctx.engine_hold_results(True)
+    try:
+        ctx.engine_set_pheno(0, w, tau)
+        ids = ctx.engine_submit(0, 0, B[:, :3], 500, 1e-10)
+        launched, _ = ctx.engine_launch()
+        assert launched
+        with pytest.raises(Exception):
+            ctx.engine_launch()  # one step in flight at a time
+        ctx.engine_set_pheno(1, w * 1.5, tau)  # slot 1 has no columns: allowed in flight
+        more = ctx.engine_submit(1, 0, B[:, 3:5], 500, 1e-10)  # joins the next launch
+        ctx.engine_cancel(int(more[1]))
+        done = {}
+        while len(done) < 4:
+            ctx.engine_finish()
+            for rid in ctx.engine_poll():
+                done[int(rid)] = ctx.engine_fetch(int(rid))[0]
+            ctx.engine_launch()
+        ctx.engine_finish()
+        assert set(done) == set(int(i) for i in ids) | {int(more[0])}
+        # the same solves through the blocking path
+        ctx.engine_hold_results(False)
+        ids2 = ctx.engine_submit(0, 0, B[:, :3], 500, 1e-10)
+        ids3 = ctx.engine_submit(1, 0, B[:, 3:4], 500, 1e-10)
+        got = {}
+        while len(got) < 4:
+            ctx.engine_run(1)
+            for rid in ctx.engine_poll():
+                got[int(rid)] = ctx.engine_fetch(int(rid))[0]
+        for a, b in zip(list(ids) + [more[0]], list(ids2) + [ids3[0]]):
+            np.testing.assert_array_equal(done[int(a)], got[int(b)])
+    finally:
+        ctx.engine_hold_results(False)

@@ -124,3 +124,72 @@ def test_masked_fit_equals_subset_fit():
     res, _ = serve.fit_batch(FakeEngine(grm), [serve.FitSpec(f0, "binary", mask=mask)])
     assert res[0]["n"] == len(S)
     assert abs(res[0]["theta"][1] - ref["theta"][1]) / ref["theta"][1] < 0.2
+
+
+class FakeAsyncEngine(FakeEngine):
+    """FakeEngine with the launch/finish protocol: work submitted before a launch completes at
+    the matching finish, so results reach the driver one step late as in the pipelined engine."""
+
+    def __init__(self, grm):
+        super().__init__(grm)
+        self.queued, self.running = [], []
+        self.launches = 0
+
+    def engine_submit(self, slot, kind, B, maxiter=500, tol=1e-5):
+        ids = super().engine_submit(slot, kind, B, maxiter, tol)
+        done = set(int(i) for i in ids)
+        self.fin = [i for i in self.fin if i not in done]
+        self.queued += [int(i) for i in ids]
+        return ids
+
+    def engine_run(self, k=1):
+        raise AssertionError("the pipelined runner must not call engine_run")
+
+    def engine_launch(self):
+        if self.running:
+            raise RuntimeError("a step is in flight")
+        self.running, self.queued = self.queued, []
+        self.launches += bool(self.running)
+        return bool(self.running), 0
+
+    def engine_finish(self):
+        n = len(self.running)
+        self.fin += self.running
+        self.running = []
+        return n
+
+
+def test_pipelined_runner_matches_synchronous_runner():
+    grm, g = _cohort(19)
+    gv = synth.genetic_value_from_codes(g.codes, 5)
+    specs = []
+    for k, trait in enumerate(("binary", "quantitative", "binary")):
+        y, C = synth.simulate_pheno(gv, 20 + k, trait, tau=0.5, prevalence=0.3, h2=0.5)
+        specs.append(serve.FitSpec(prep.make_fit0(y, C, trait, True), trait))
+    ref, _ = serve.fit_batch(FakeEngine(grm), specs)
+    eng = FakeAsyncEngine(grm)
+    res, jobs = serve.fit_batch(eng, specs, pipelined=True)
+    assert eng.launches > 0 and not eng.running and not eng.queued
+    for a, b in zip(res, ref):
+        assert not isinstance(a, Exception), a
+        np.testing.assert_array_equal(a["theta"], b["theta"])
+        np.testing.assert_array_equal(a["coefficients"], b["coefficients"])
+        assert a["iterations"] == b["iterations"]
+
+
+def test_pipelined_runner_reports_a_stall():
+    grm, g = _cohort(23)
+    gv = synth.genetic_value_from_codes(g.codes, 6)
+    y, C = synth.simulate_pheno(gv, 31, "quantitative", tau=0.5, h2=0.5)
+    spec = serve.FitSpec(prep.make_fit0(y, C, "quantitative", True), "quantitative")
+
+    class Lossy(FakeAsyncEngine):
+        def engine_launch(self):  # drops every queued column: nothing ever finishes
+            self.queued = []
+            return False, 0
+
+    r = serve.Runner(Lossy(grm), 256, 1, pipelined=True)
+    r.submit(spec)
+    import pytest
+    with pytest.raises(RuntimeError, match="engine idle"):
+        r.run()
