@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--phenos", type=int, default=32)
     ap.add_argument("--miss", type=float, default=0.02)
     ap.add_argument("--seed", type=int, default=1003)
-    ap.add_argument("--mode", default="tf32x3", choices=["tf32x3", "tf32", "fp32"])
+    ap.add_argument("--mode", default="tf32x3", choices=["bf16x3", "tf32x3", "tf32", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster-shape autotuner")
     ap.add_argument("--blocking-runner", action="store_true",
@@ -183,28 +183,37 @@ def run_batch(ctx, specs, cols, pipelined=True):
     return res, jobs, wall
 
 
-def grm_roofline(ctx, peaks, t_dev, n, np_):
-    """Roofline of the dominant kernel (GRM.V) from the engine's own CUDA-event timing."""
+def grm_roofline(ctx, peaks, t_dev, n, np_, mode="tf32x3", traffic=None):
+    """Roofline of the dominant kernel (GRM.V) from the engine's own CUDA-event timing.
+
+    Algorithmic bytes per launch: the two halves of K (8 B per entry for TF32 halves, 4 B for BF16
+    halves) + the split P halves read and Y written (FP32); tensor FLOPs: three products of
+    2 N^2 per column.  The tensor peak is the measured BF16 rate (TF32 runs at half of it)."""
     launches = max(1, t_dev["gemm_launches"])
     ms = t_dev["gemm_ms"] / launches
     cols = t_dev["gemm_cols"] / launches
-    split = True
-    sk = 8.0 if split else 4.0
-    bytes_alg = sk * n * n + 12.0 * n * cols
-    flops_tensor = (3.0 if split else 1.0) * 2.0 * n * n * cols
+    bf16 = mode == "bf16x3"
+    split = mode in ("tf32x3", "bf16x3")
+    kb = 4.0 if bf16 else (8.0 if split else 4.0)
+    pb = 4.0 if bf16 else (8.0 if split else 4.0)
+    bytes_alg = kb * np_ * np_ + (pb + 4.0) * np_ * cols
+    flops_tensor = (3.0 if split else 1.0) * 2.0 * np_ * np_ * cols
     hbm = peaks.get("hbm_gbs", 6800.0)
-    tf32_peak = peaks.get("bf16_tflops", 1900.0) / 2.0
+    tc_peak = peaks.get("bf16_tflops", 1900.0) / (1.0 if bf16 else 2.0)
+    kname = "tc_gemm_kernel<%s,split>" % ("bf16" if bf16 else "tf32")
     a_bw = bytes_alg / (ms * 1e-3) / 1e9
     a_tc = flops_tensor / (ms * 1e-3) / 1e12
-    if a_bw / hbm >= a_tc / tf32_peak:
-        return {"bound": "hbm", "achieved": round(a_bw, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(a_bw / hbm, 4), "traffic": None, "kernel": "tc_gemm_kernel<tf32,split>",
-                "per_launch_ms": round(ms, 3), "columns_per_launch": round(cols, 1),
-                "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)"}
-    return {"bound": "tensor", "achieved": round(a_tc, 1), "peak": tf32_peak, "unit": "TFLOP/s",
-            "frac": round(a_tc / tf32_peak, 4), "traffic": None, "kernel": "tc_gemm_kernel<tf32,split>",
-            "per_launch_ms": round(ms, 3), "columns_per_launch": round(cols, 1),
-            "peak_source": "TF32 = half the measured bf16_tflops (MEASURED_PEAKS.json)"}
+    common = {"traffic": traffic, "kernel": kname, "per_launch_ms": round(ms, 3),
+              "columns_per_launch": round(cols, 1), "algorithmic_bytes_per_launch": bytes_alg,
+              "tensor_flops_per_launch": flops_tensor}
+    if a_bw / hbm >= a_tc / tc_peak:
+        return dict({"bound": "hbm", "achieved": round(a_bw, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(a_bw / hbm, 4),
+                     "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)"}, **common)
+    return dict({"bound": "tensor", "achieved": round(a_tc, 1), "peak": tc_peak, "unit": "TFLOP/s",
+                 "frac": round(a_tc / tc_peak, 4),
+                 "peak_source": ("measured bf16_tflops (MEASURED_PEAKS.json)" if bf16 else
+                                 "TF32 = half the measured bf16_tflops (MEASURED_PEAKS.json)")}, **common)
 
 
 def serving_block(ctx, args, cols):
@@ -294,7 +303,7 @@ def plain_fp64(ctx, iters_per_fit):
 
 def run_ours(args, rank, world, local):
     import torch
-    from saigegpu import Context, GRM_BF16_TC, MV_TF32X3_TC, MV_TF32_TC, MV_FP32_SIMT
+    from saigegpu import Context, GRM_BF16_TC, MV_BF16X3_TC, MV_TF32X3_TC, MV_TF32_TC, MV_FP32_SIMT
     peaks = load_peaks()
     ctx = Context(local)
     t_setup = time.perf_counter()
@@ -303,19 +312,20 @@ def run_ours(args, rank, world, local):
     decode_t = ctx.build_timing()
     torch.cuda.synchronize()
     tune_report = None
-    if args.no_tune or args.mode != "tf32x3":
+    if args.no_tune or args.mode not in ("tf32x3", "bf16x3"):
         t0 = time.perf_counter()
         ctx.grm_build(GRM_BF16_TC)
         grm_s = time.perf_counter() - t0
     else:
         from saigegpu import tune
-        tune_report = tune.tune(ctx, ncols=(128, 256, 512))
+        tune_report = tune.tune(ctx, ncols=(128, 256, 512),
+                                mode=MV_BF16X3_TC if args.mode == "bf16x3" else MV_TF32X3_TC)
         grm_s = tune_report["syrk"][tune_report["chosen"][0]]
     d = ctx.dims()
     syrk_flops = float(d["n"]) * (d["n"] + 1) * d["m_qc"]
     bt = ctx.build_timing()
     specs = make_specs(ctx, args, args.seed + 17 * rank)
-    mode = {"tf32x3": MV_TF32X3_TC, "tf32": MV_TF32_TC, "fp32": MV_FP32_SIMT}[args.mode]
+    mode = {"bf16x3": MV_BF16X3_TC, "tf32x3": MV_TF32X3_TC, "tf32": MV_TF32_TC, "fp32": MV_FP32_SIMT}[args.mode]
     ctx.set_matvec_mode(mode)
     from saigegpu import serve as _serve
     cols = _serve.columns_for(specs)
@@ -354,11 +364,11 @@ def run_ours(args, rank, world, local):
     cols_per_fit = float(np.mean([j.columns for j in jobs_all]))
     h2d = int(args.phenos * (cols_per_fit * 0.1 * n_bytes + 2 * n_bytes * 12))
     d2h = int(args.phenos * cols_per_fit * n_bytes)
-    roof = grm_roofline(ctx, peaks, tdev, d["n"], ctx.n)
+    roof = grm_roofline(ctx, peaks, tdev, d["n"], ctx.grm_padded_n(), args.mode)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "fits/hr", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_wall / args.steps * 1e3, 1),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32-tf32x3/fp64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": {"bf16x3": "bf16x3-tc/fp64", "tf32x3": "tf32x3-tc/fp64", "tf32": "tf32-tc/fp64", "fp32": "fp32/fp64"}[args.mode],
         "data": "synthetic (seeded cohort generator; the reference's 150k x 100k synthetic AFR set is external)",
         "config": {"workload": "batched null-model fits on a resident GRM", "n_samples": d["n"],
                    "m_markers_qc": d["m_qc"], "m_markers": args.m, "missing": args.miss,

@@ -52,8 +52,11 @@ enum sg_matvec_mode {
   SG_MV_FP32_SIMT = 0,  /* FP32 K, FP32 operands, CUDA cores */
   SG_MV_TF32_TC = 1,    /* tcgen05 kind::tf32 on the FP32 K: one product, ~2^-11 relative per term */
   SG_MV_FP64_PLAIN = 2, /* plain FP64 GEMV (the single-RHS baseline) */
-  SG_MV_TF32X3_TC = 3   /* split-TF32 on tcgen05: K = Khi + Klo, P = Phi + Plo, three products
+  SG_MV_TF32X3_TC = 3,  /* split-TF32 on tcgen05: K = Khi + Klo, P = Phi + Plo, three products
                            accumulated in TMEM (FP32-class accuracy at tensor-core rate) */
+  SG_MV_BF16X3_TC = 4   /* split-BF16 on tcgen05 (kind::f16): K and P as BF16 high + low halves
+                           (16 significant bits), three products in TMEM; ~1.5e-5 relative per
+                           term, half the bytes and twice the MMA rate of SG_MV_TF32X3_TC */
 };
 
 /* ------------------------------------------------------------ context */

@@ -63,6 +63,7 @@ struct Engine {
   int64_t inflight_ncols = 0, inflight_occupied = 0, inflight_hi = 0;
   std::vector<int64_t> pending_release;  // columns freed on the host, reset on the device at the next launch
   float* Pflo = nullptr;          // low TF32 halves of Pf (split-TF32 mode)
+  void* Pb = nullptr;             // BF16 high (first cap_cols * np) and low halves of Pf (split-BF16 mode)
   double* d_sx = nullptr;         // probe_dots: Sigma^-1 X block
   double* d_dpart = nullptr;      // probe_dots: block partial sums
   int32_t* d_dcols = nullptr;     // probe_dots: column indices
@@ -106,6 +107,7 @@ struct sg_ctx {
   float* d_K = nullptr;
   float* d_Klo = nullptr;   // K - tf32(K) while the split-TF32 engine is selected (d_K then holds tf32(K))
   bool k_split = false;
+  void* d_Kb = nullptr;     // BF16 high (first n_p^2) and low halves of K for SG_MV_BF16X3_TC
   double* d_diag = nullptr;
   float* d_diag32 = nullptr;
   std::vector<double> diag;
@@ -283,17 +285,20 @@ __global__ void add_inplace_kernel(float* a, const float* b, int64_t n) {
 }
 
 static int ensure_k_split(sg_ctx* c, bool want);
+static int ensure_k_bf16(sg_ctx* c, bool want);
 
 extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
   if (!c) return SG_ERR_INVALID;
   if (mode != SG_MV_FP32_SIMT && mode != SG_MV_TF32_TC && mode != SG_MV_FP64_PLAIN &&
-      mode != SG_MV_TF32X3_TC)
+      mode != SG_MV_TF32X3_TC && mode != SG_MV_BF16X3_TC)
     return set_err(c, SG_ERR_INVALID, "unknown matvec mode %d", mode);
-  if ((mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC) && !tc_available())
+  if ((mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC) && !tc_available())
     return set_err(c, SG_ERR_INVALID, "tcgen05 path needs an sm_103a device");
+  if (c->eng.inflight) return set_err(c, SG_ERR_STATE, "a step is in flight: finish it first");
   c->mv_mode = mode;
-  if (c->have_grm) return ensure_k_split(c, mode == SG_MV_TF32X3_TC);
-  return SG_OK;
+  if (!c->have_grm) return SG_OK;
+  SG_TRY(ensure_k_split(c, mode == SG_MV_TF32X3_TC));
+  return ensure_k_bf16(c, mode == SG_MV_BF16X3_TC);
 }
 
 extern "C" int sg_selftest_wait_timeout(sg_ctx* c, double budget_ms) {
@@ -341,6 +346,8 @@ static void free_geno(sg_ctx* c) {
   dev_free_t(c, c->d_K);
   dev_free_t(c, c->d_Klo);
   c->k_split = false;
+  dev_free(c, c->d_Kb);
+  c->d_Kb = nullptr;
   dev_free_t(c, c->d_diag);
   dev_free_t(c, c->d_diag32);
   c->have_geno = false;
@@ -639,6 +646,8 @@ extern "C" int sg_grm_build(sg_ctx* c, int precision) {
   dev_free_t(c, c->d_K);
   dev_free_t(c, c->d_Klo);
   c->k_split = false;
+  dev_free(c, c->d_Kb);
+  c->d_Kb = nullptr;
   engine_free(c);
   loco_free(c);
   c->have_grm = false;
@@ -699,6 +708,24 @@ static int ensure_k_split(sg_ctx* c, bool want) {
     dev_free_t(c, c->d_Klo);
     c->k_split = false;
   }
+  return sync(c);
+}
+
+// BF16 high/low halves of K for the split-BF16 engine (built from the exact FP32 K, which stays
+// resident for the other engines, the diagonal and sg_grm_get); freed when another engine is chosen.
+static int ensure_k_bf16(sg_ctx* c, bool want) {
+  if (!c->have_grm || want == (c->d_Kb != nullptr)) return SG_OK;
+  if (!want) {
+    SG_TRY(sync(c));
+    dev_free(c, c->d_Kb);
+    c->d_Kb = nullptr;
+    return SG_OK;
+  }
+  const int64_t n2 = c->np * c->np;
+  SG_TRY(dev_alloc(c, &c->d_Kb, (size_t)n2 * 4));
+  launch_split_bf16(c->d_K, c->k_split ? c->d_Klo : nullptr, c->d_Kb,
+                    static_cast<uint16_t*>(c->d_Kb) + n2, n2, c->stream);
+  SG_LAUNCHED(c, 1);
   return sync(c);
 }
 
@@ -763,6 +790,8 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.B); dev_free_t(c, e.part); dev_free_t(c, e.winv); dev_free_t(c, e.minv);
   dev_free_t(c, e.Yd); dev_free_t(c, e.Pf); dev_free_t(c, e.Yf); dev_free_t(c, e.d_st);
   dev_free_t(c, e.d_ph); dev_free_t(c, e.d_cols); dev_free_t(c, e.Pflo);
+  dev_free(c, e.Pb);
+  e.Pb = nullptr;
   dev_free_t(c, e.d_sx); dev_free_t(c, e.d_dpart); dev_free_t(c, e.d_dcols); dev_free_t(c, e.ptab);
   dev_free_t(c, e.pcache);
   e.pcache_key.clear();
@@ -1055,6 +1084,19 @@ static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf) {
     }
     return SG_OK;
   }
+  if (c->mv_mode == SG_MV_BF16X3_TC) {
+    if (!c->d_Kb) SG_TRY(ensure_k_bf16(c, true));
+    const size_t half = (size_t)(e.cap_cols * e.np);
+    if (!e.Pb) SG_TRY(dev_alloc(c, &e.Pb, half * 4));
+    uint16_t* ph = static_cast<uint16_t*>(e.Pb);
+    launch_split_bf16(e.Pf, nullptr, ph, ph + half, ncols * e.np, c->stream);
+    c->launches += 1;
+    const uint16_t* kh = static_cast<const uint16_t*>(c->d_Kb);
+    cudaError_t err = tc_gemm_bf16x3(kh, kh + c->np * c->np, e.np, ph, ph + half, ncols, e.Yf, c->stream, false);
+    if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 GRM.V: %s", cudaGetErrorString(err));
+    c->launches += 1;
+    return SG_OK;
+  }
   if (c->mv_mode == SG_MV_TF32_TC || c->mv_mode == SG_MV_TF32X3_TC) {
     const bool split = c->mv_mode == SG_MV_TF32X3_TC;
     if (split) {
@@ -1079,10 +1121,14 @@ static int release_col(sg_ctx* c, int64_t col);
 
 // Columns the GRM.V of one step covers: [0, hi_col) padded to the kernel's column tile (the
 // padding columns are free or finished, their P rows are zero).
+static bool tc_mode(int mode) {
+  return mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC;
+}
+
 static int64_t engine_gemm_cols(const sg_ctx* c) {
   const Engine& e = c->eng;
   int64_t ncols = round_up(e.hi_col, 32);
-  if (c->mv_mode == SG_MV_TF32_TC || c->mv_mode == SG_MV_TF32X3_TC) {
+  if (tc_mode(c->mv_mode)) {
     const int64_t w = ncols > 320 ? 256 : (ncols > 96 ? 128 : 32);
     const int64_t padded = std::min(round_up(ncols, w), e.cap_cols);
     if (padded % w == 0) ncols = padded;
@@ -1126,7 +1172,7 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
   Engine& e = c->eng;
   e.inflight = false;
   SG_TRY(sync(c));
-  if (c->mv_mode == SG_MV_TF32_TC || c->mv_mode == SG_MV_TF32X3_TC) {
+  if (tc_mode(c->mv_mode)) {
     const cudaError_t err = tc_check_error(c->stream);
     if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 GRM.V: %s", cudaGetErrorString(err));
   }

@@ -13,7 +13,8 @@
 //   warp 2             allocates / frees the TMEM columns;
 //   warps 0-3          epilogue: tcgen05.ld 32x32b (each warp its 32 TMEM
 //                      lanes = 32 output rows), scale, store to global.
-// No cluster, no multicast (cta_group::1).  Every mbarrier wait is bounded by
+// Optional thread-block clusters share B tiles by TMA multicast (see the
+// kernel's kC parameter); MMAs stay cta_group::1.  Every mbarrier wait is bounded by
 // a global-timer budget; on expiry the kernel records an error code, skips
 // the remaining work, frees its TMEM and returns.
 //
@@ -22,10 +23,12 @@
 //     each element (r, c <= r) written to K[r][c] and K[c][r].  The split
 //     variant accumulates Zh Zh^T + Zh Zl^T + Zl Zh^T for Z = Zh + Zl.
 //   * GRM.V Y^T = K P^T (K fp32 read as tf32, kind::tf32), output stored
-//     RHS-major so each TMEM column is a coalesced row of Y^T.
+//     RHS-major so each TMEM column is a coalesced row of Y^T; split variants
+//     with TF32 or BF16 high/low halves of K and P (three products).
 #include "sg_internal.h"
 
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 #include <cstdio>
 #include <mutex>
@@ -478,6 +481,39 @@ void launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStre
   split_tf32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, hi, lo, n);
 }
 
+// x (+ x2) = hi + lo with hi = bf16_rn(x), lo = bf16_rn(x - hi): 16 significant bits in all.
+// x - hi is exact in FP32 (|x - hi| <= half a bf16 ulp of x).  Two elements per thread.
+__global__ void split_bf16_kernel(const float* __restrict__ x, const float* __restrict__ x2,
+                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, int64_t n) {
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  if (i >= n) return;
+  float v[2] = {x[i], i + 1 < n ? x[i + 1] : 0.0f};
+  if (x2) {
+    v[0] += x2[i];
+    if (i + 1 < n) v[1] += x2[i + 1];
+  }
+  __nv_bfloat16 h[2], l[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    h[j] = __float2bfloat16_rn(v[j]);
+    l[j] = isfinite(v[j]) ? __float2bfloat16_rn(v[j] - __bfloat162float(h[j])) : __float2bfloat16_rn(0.0f);
+  }
+  if (i + 1 < n) {
+    *reinterpret_cast<__nv_bfloat162*>(hi + i) = __halves2bfloat162(h[0], h[1]);
+    *reinterpret_cast<__nv_bfloat162*>(lo + i) = __halves2bfloat162(l[0], l[1]);
+  } else {
+    hi[i] = h[0];
+    lo[i] = l[0];
+  }
+}
+
+void launch_split_bf16(const float* x, const float* x2, void* hi, void* lo, int64_t n, cudaStream_t s) {
+  if (n == 0) return;
+  const int64_t threads = (n + 1) / 2;
+  split_bf16_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+      x, x2, static_cast<__nv_bfloat16*>(hi), static_cast<__nv_bfloat16*>(lo), n);
+}
+
 
 cudaError_t tc_wait_selftest(double budget_ms, int* waited_out, cudaStream_t s) {
   int* d = nullptr;
@@ -573,11 +609,43 @@ int tc_gemm_tile_n(int64_t ncols, bool split) {
   return 32;
 }
 
-template <int BN, int S, int C>
+template <bool kTF32, int BN, int S, int C>
 static cudaError_t launch_grmv_split(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
                                      const CUtensorMap& b2, const TileCoord* tiles, int nt, int num_kb,
                                      float* Y, int64_t np, cudaStream_t s) {
-  return launch<true, BN, S, true, C>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f, 1, s, np);
+  return launch<kTF32, BN, S, true, C>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f, 1, s, np);
+}
+
+// Split GRM.V over every (BN, cluster) variant.  A stage holds the same bytes for both operand
+// types (128-byte K slices: 32 tf32 or 64 bf16 elements), so the ring depths match.
+template <bool kTF32>
+static cudaError_t grmv_split_dispatch(int BN, int C, const CUtensorMap& a, const CUtensorMap& b,
+                                       const CUtensorMap& a2, const CUtensorMap& b2, const TileCoord* tiles,
+                                       int nt, int num_kb, float* Y, int64_t np, cudaStream_t s) {
+#define SG_GRMV_CASE(BNv, Sv)                                                                             \
+  case BNv:                                                                                               \
+    return C == 4   ? launch_grmv_split<kTF32, BNv, Sv, 4>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s)      \
+           : C == 2 ? launch_grmv_split<kTF32, BNv, Sv, 2>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s)      \
+                    : launch_grmv_split<kTF32, BNv, Sv, 1>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s);
+  switch (BN) {
+    SG_GRMV_CASE(256, 2)
+    SG_GRMV_CASE(128, 3)
+    SG_GRMV_CASE(64, 4)
+    SG_GRMV_CASE(32, 5)
+    default:
+      return cudaErrorInvalidValue;
+  }
+#undef SG_GRMV_CASE
+}
+
+// Row groups of C consecutive row blocks (padded past np), every column block per group.
+static cudaError_t grmv_tiles(TileCache& cache, int64_t np, int64_t ncols, int BN, int C, cudaStream_t s) {
+  cache.host.clear();
+  const int64_t nbm = np / kTileM;
+  for (int64_t gi = 0; gi < (nbm + C - 1) / C; ++gi)
+    for (int64_t bn = 0; bn < ncols / BN; ++bn)
+      for (int r = 0; r < C; ++r) cache.host.push_back(TileCoord{(int32_t)(gi * C + r), (int32_t)bn});
+  return upload_tiles(cache, s);
 }
 
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
@@ -596,35 +664,13 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
   if (split && (!make_map(&a2, Klo, true, np, np, (uint64_t)np * 4, kTileM) ||
                 !make_map(&b2, Plo, true, np, ncols, (uint64_t)np * 4, brows)))
     return cudaErrorInvalidValue;
-  // row groups of C consecutive row blocks (padded past np), every column block per group
   static TileCache cache;
-  cache.host.clear();
-  const int64_t nbm = np / kTileM;
-  for (int64_t gi = 0; gi < (nbm + C - 1) / C; ++gi)
-    for (int64_t bn = 0; bn < ncols / BN; ++bn)
-      for (int r = 0; r < C; ++r) cache.host.push_back(TileCoord{(int32_t)(gi * C + r), (int32_t)bn});
-  cudaError_t e = upload_tiles(cache, s);
+  cudaError_t e = grmv_tiles(cache, np, ncols, BN, C, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(np / 32);
   const int nt = (int)cache.host.size();
   if (split) {
-#define SG_GRMV_CASE(BNv, Sv)                                                                          \
-  case BNv:                                                                                            \
-    e = C == 4 ? launch_grmv_split<BNv, Sv, 4>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s)          \
-      : C == 2 ? launch_grmv_split<BNv, Sv, 2>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s)          \
-               : launch_grmv_split<BNv, Sv, 1>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s);         \
-    break;
-    switch (BN) {
-      SG_GRMV_CASE(256, 2)
-      SG_GRMV_CASE(128, 3)
-      SG_GRMV_CASE(64, 4)
-      default:
-        e = C == 4 ? launch_grmv_split<32, 5, 4>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s)
-          : C == 2 ? launch_grmv_split<32, 5, 2>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s)
-                   : launch_grmv_split<32, 5, 1>(a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s);
-        break;
-    }
-#undef SG_GRMV_CASE
+    e = grmv_split_dispatch<true>(BN, C, a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s);
   } else {
     switch (BN) {
       case 256: e = launch<true, 256, 3, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
@@ -633,6 +679,27 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
       default: e = launch<true, 32, 8, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
     }
   }
+  if (e != cudaSuccess) return e;
+  return check ? check_error_flag(s) : cudaSuccess;
+}
+
+cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const void* Ph, const void* Pl,
+                           int64_t ncols, float* Y, cudaStream_t s, bool check) {
+  if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0 || !Kh || !Kl || !Ph || !Pl)
+    return cudaErrorInvalidValue;
+  const int BN = tc_gemm_tile_n(ncols, true);
+  const int C = g_cluster_grmv;
+  const uint32_t brows = (uint32_t)(BN / C);
+  const uint64_t rb = (uint64_t)np * 2;
+  CUtensorMap a, b, a2, b2;
+  if (!make_map(&a, Kh, false, np, np, rb, kTileM) || !make_map(&b, Ph, false, np, ncols, rb, brows) ||
+      !make_map(&a2, Kl, false, np, np, rb, kTileM) || !make_map(&b2, Pl, false, np, ncols, rb, brows))
+    return cudaErrorInvalidValue;
+  static TileCache cache;
+  cudaError_t e = grmv_tiles(cache, np, ncols, BN, C, s);
+  if (e != cudaSuccess) return e;
+  const int num_kb = (int)(np / 64);
+  e = grmv_split_dispatch<false>(BN, C, a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np, s);
   if (e != cudaSuccess) return e;
   return check ? check_error_flag(s) : cudaSuccess;
 }

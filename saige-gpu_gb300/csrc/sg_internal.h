@@ -85,6 +85,12 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
 // tc_check_error after the stream has drained.
 cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const float* P,
                          const float* Plo, int64_t ncols, float* Y, cudaStream_t s, bool check = true);
+// Y^T = (Kh + Kl)(Ph + Pl)^T without the Kl Pl term, all four BF16 (kind::f16): 16-bit operand
+// significands at the BF16 tensor rate, K in 4 bytes per entry.
+cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const void* Ph, const void* Pl,
+                           int64_t ncols, float* Y, cudaStream_t s, bool check = true);
+// x (+ x2 when not null) = hi + lo, both BF16 (round to nearest even), lo = bf16(x - hi)
+void launch_split_bf16(const float* x, const float* x2, void* hi, void* lo, int64_t n, cudaStream_t s);
 // Synchronises s, then reads and clears the flag the tcgen05 kernels set when a bounded wait ran
 // out (cudaErrorLaunchTimeout in that case).
 cudaError_t tc_check_error(cudaStream_t s);

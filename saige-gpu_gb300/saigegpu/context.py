@@ -12,7 +12,7 @@ import numpy as np
 from . import _lib as L
 
 GRM_FP32_SIMT, GRM_BF16_TC, GRM_BF16X3_TC = 0, 1, 2
-MV_FP32_SIMT, MV_TF32_TC, MV_FP64_PLAIN, MV_TF32X3_TC = 0, 1, 2, 3
+MV_FP32_SIMT, MV_TF32_TC, MV_FP64_PLAIN, MV_TF32X3_TC, MV_BF16X3_TC = 0, 1, 2, 3, 4
 
 
 def _f32(a):
@@ -181,6 +181,12 @@ class Context:
     # ------------------------------------------------------------ GRM
     def grm_build(self, precision=GRM_FP32_SIMT):
         self._call("sg_grm_build", int(precision))
+
+    def grm_padded_n(self):
+        """N rounded up to the 128-row tile: the GRM's leading dimension on the device."""
+        v = C.c_int64()
+        self._call("sg_grm_padded_n", C.byref(v))
+        return v.value
 
     def build_timing(self):
         t = np.zeros(5, np.float64)

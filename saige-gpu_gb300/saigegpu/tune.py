@@ -1,6 +1,6 @@
 """Autotuner for the tcgen05 kernels' cluster shapes.
 
-The SYRK and the split-TF32 GRM.V can run with 1, 2 or 4 CTAs per
+The SYRK and the split GRM.V (TF32 or BF16 halves) can run with 1, 2 or 4 CTAs per
 thread-block cluster sharing each B tile through TMA multicast (fewer
 L2->SM operand bytes per FLOP).  Which size wins depends on N, the number of
 right-hand sides and the tile width, so ``tune`` times every variant on the
@@ -39,8 +39,8 @@ def time_grmv(ctx, cluster, ncols, reps=2, seed=0):
     return best / 1e3
 
 
-def tune(ctx, ncols=(64, 256, 512), tune_syrk=True, clusters=(1, 2, 4)):
-    """Pick the fastest cluster sizes; leaves the GRM built (BF16) and the split-TF32 engine selected."""
+def tune(ctx, ncols=(64, 256, 512), tune_syrk=True, clusters=(1, 2, 4), mode=MV_TF32X3_TC):
+    """Pick the fastest cluster sizes; leaves the GRM built (BF16) and engine ``mode`` selected."""
     report = {"syrk": {}, "grmv": {}}
     if tune_syrk:
         for c in clusters:
@@ -48,7 +48,7 @@ def tune(ctx, ncols=(64, 256, 512), tune_syrk=True, clusters=(1, 2, 4)):
         best_s = min(report["syrk"], key=report["syrk"].get)
         ctx.set_tc_clusters(best_s, ctx.get_tc_clusters()[1])
         ctx.grm_build(GRM_BF16_TC)
-    ctx.set_matvec_mode(MV_TF32X3_TC)
+    ctx.set_matvec_mode(mode)
     totals = {c: 0.0 for c in clusters}
     for k in ncols:
         for c in clusters:

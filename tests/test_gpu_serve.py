@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 from oracle import aireml, plink
-from saigegpu import GRM_FP32_SIMT, MV_FP32_SIMT, MV_TF32X3_TC, prep, serve, synth
+from saigegpu import GRM_FP32_SIMT, MV_BF16X3_TC, MV_FP32_SIMT, MV_TF32X3_TC, prep, serve, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -52,9 +52,10 @@ def test_alone_equals_in_the_mix(cohort):
         np.testing.assert_allclose(alone[0]["linear_predictors"], mix[k]["linear_predictors"], rtol=1e-12, atol=1e-14)
 
 
-def test_split_tf32_engine_matches_oracle(cohort):
+@pytest.mark.parametrize("mode", [MV_TF32X3_TC, MV_BF16X3_TC])
+def test_split_engine_matches_oracle(cohort, mode):
     ctx, grm, specs, refs = cohort
-    ctx.set_matvec_mode(MV_TF32X3_TC)
+    ctx.set_matvec_mode(mode)
     try:
         res, _ = serve.fit_batch(ctx, specs[:2], max_columns=256)
         for r, ref in zip(res, refs[:2]):
@@ -73,7 +74,7 @@ def test_serving_stream(cohort):
     assert min(lat) > 0
 
 
-@pytest.mark.parametrize("mode", [MV_FP32_SIMT, MV_TF32X3_TC])
+@pytest.mark.parametrize("mode", [MV_FP32_SIMT, MV_TF32X3_TC, MV_BF16X3_TC])
 def test_pipelined_runner_equals_synchronous(cohort, mode):
     """Launch/finish stepping (host consumes step k while step k+1 runs) changes when columns
     start, not what they compute: every fit is bit-identical to the blocking runner's."""

@@ -1,4 +1,4 @@
-"""tcgen05 paths: BF16 / split-BF16 SYRK and the TF32 GRM.V against the FP64 oracle."""
+"""tcgen05 paths: BF16 / split-BF16 SYRK and the TF32 / split GRM.V against the FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -67,22 +67,48 @@ def test_syrk_cluster_variants_bit_identical(cohort, split):
         ctx.set_tc_clusters(1, 1)
 
 
-def test_grmv_cluster_variants_bit_identical(cohort):
-    from saigegpu import MV_TF32X3_TC
+@pytest.mark.parametrize("mode", ["tf32x3", "bf16x3"])
+def test_grmv_cluster_variants_bit_identical(cohort, mode):
+    from saigegpu import MV_BF16X3_TC, MV_TF32X3_TC
     ctx, grm = cohort
     ctx.grm_build(GRM_FP32_SIMT)
+    Kg = ctx.grm_get().astype(np.float64)  # the resident FP32 K the split halves come from
     rng = np.random.default_rng(3)
+    # split TF32: 22 significant bits per operand; split BF16: 16 (relative 2^-17 per factor)
+    tol = 5e-6 if mode == "tf32x3" else 6e-5
     try:
-        ctx.set_matvec_mode(MV_TF32X3_TC)
-        for k in (32, 100, 256):  # column tiles of 32, 128 and 256 (padded)
+        ctx.set_matvec_mode(MV_TF32X3_TC if mode == "tf32x3" else MV_BF16X3_TC)
+        for k in (32, 100, 256, 512):  # column tiles of 32, 128, 128 and 256 (padded)
             V = rng.standard_normal((grm.n, k))
             ctx.set_tc_clusters(1, 1)
             Y1 = ctx.grm_matmul(V)
-            ref = grm.K @ V
-            assert np.abs(Y1 - ref).max() / np.abs(ref).max() < 5e-6
+            ref = Kg @ V
+            assert np.abs(Y1 - ref).max() / np.abs(ref).max() < tol, k
             for c in (2, 4):
                 ctx.set_tc_clusters(1, c)
                 assert np.array_equal(ctx.grm_matmul(V), Y1), (k, c)
     finally:
         ctx.set_tc_clusters(1, 1)
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+
+
+def test_grmv_bf16x3_switching_modes_keeps_k_exact(cohort):
+    """Split BF16 halves are built from the exact K; leaving the mode frees them and K is intact."""
+    from saigegpu import MV_BF16X3_TC, MV_TF32X3_TC
+    ctx, grm = cohort
+    ctx.grm_build(GRM_FP32_SIMT)
+    K0 = ctx.grm_get()
+    npad = ctx.grm_padded_n()
+    V = np.random.default_rng(5).standard_normal((grm.n, 40))
+    try:
+        ctx.set_matvec_mode(MV_TF32X3_TC)
+        ctx.set_matvec_mode(MV_BF16X3_TC)  # halves taken from K = Khi + Klo
+        Y_a = ctx.grm_matmul(V)
+        used_bf16 = ctx.bytes_in_use()
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+        assert used_bf16 - ctx.bytes_in_use() >= 4 * npad * npad  # the BF16 halves are released
+        assert np.array_equal(ctx.grm_get(), K0)
+        ctx.set_matvec_mode(MV_BF16X3_TC)  # halves taken from the FP32 K directly
+        assert np.array_equal(ctx.grm_matmul(V), Y_a)
+    finally:
         ctx.set_matvec_mode(MV_FP32_SIMT)
