@@ -348,6 +348,7 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     barrier(world)
     launches = ctx.kernel_launches() - L0
+    io_h2d, io_d2h = ctx.engine_io_bytes()
     tdev = ctx.engine_timing()
     dev_s = tdev["step_ms"] / 1e3
     total_wall = sum(walls)
@@ -359,11 +360,11 @@ def run_ours(args, rank, world, local):
     e2e = fits_all / wall_max * 3600.0
     lat = sorted(j.t_done - j.t_start for j in jobs_all)
     col_iters = float(np.mean([j.column_iterations for j in jobs_all]))
-    n_bytes = 8 * args.n
-    # bytes moved per step: RHS uploads (Y, X, K.PY, P A PY), W/tau rows, solutions back
     cols_per_fit = float(np.mean([j.columns for j in jobs_all]))
-    h2d = int(args.phenos * (cols_per_fit * 0.1 * n_bytes + 2 * n_bytes * 12))
-    d2h = int(args.phenos * cols_per_fit * n_bytes)
+    # bytes the engine API copied per step (counted by the library): right-hand sides, weights,
+    # probe tables, column states, fetched results and probe reductions
+    h2d = int(io_h2d // max(1, args.steps))
+    d2h = int(io_d2h // max(1, args.steps))
     roof = grm_roofline(ctx, peaks, tdev, d["n"], ctx.grm_padded_n(), args.mode)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "fits/hr", "n_gpus": world,

@@ -284,6 +284,10 @@ int sg_engine_stats(sg_ctx *ctx, int64_t *stats4);
  * [5]=occupied (useful) columns processed */
 int sg_engine_timing(sg_ctx *ctx, double *t6);
 int sg_engine_reset_timing(sg_ctx *ctx);
+/* Bytes copied host->device and device->host by the engine calls (right-hand sides, weights,
+ * probe tables, column states, fetched results, probe reductions) since the last
+ * sg_engine_reset_timing.  No reference counterpart (I/O accounting of this engine). */
+int sg_engine_io_bytes(sg_ctx *ctx, uint64_t *h2d_bytes, uint64_t *d2h_bytes);
 
 /* ------------------------------------------------------------ synthetic cohorts (benchmarks / tests)
  * Writes a SNP-major .bed image (with magic) for n samples x m markers into device memory owned by

@@ -58,6 +58,7 @@ struct Engine {
   int64_t steps = 0, retired = 0, col_iters = 0, grm_passes = 0;
   std::vector<int64_t> finished;  // ids retired since the last poll
   bool hold = false;              // keep finished results on the device until fetched/consumed
+  uint64_t io_h2d = 0, io_d2h = 0;  // bytes through the engine API since the last timing reset
   ColState* h_pin = nullptr;      // pinned mirror for the asynchronous state read-back of a step
   bool inflight = false;          // a launched step has not been finished yet
   int64_t inflight_ncols = 0, inflight_occupied = 0, inflight_hi = 0;
@@ -219,6 +220,10 @@ static int sync_side(sg_ctx* c) {
   SG_CUDA(c, cudaStreamSynchronize(c->side));
   return SG_OK;
 }
+
+// Host<->device copies of the engine API, counted for its I/O report (sg_engine_io_bytes).
+static cudaError_t h2d(sg_ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t s);
+static cudaError_t d2h(sg_ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t s);
 
 static bool all_finite(const float* v, int64_t n) {
   for (int64_t i = 0; i < n; ++i)
@@ -784,6 +789,15 @@ extern "C" int sg_grm_get(sg_ctx* c, float* out) {
 }
 
 // ------------------------------------------------------------------ engine
+static cudaError_t h2d(sg_ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  c->eng.io_h2d += bytes;
+  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+}
+static cudaError_t d2h(sg_ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  c->eng.io_d2h += bytes;
+  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+}
+
 static void engine_free(sg_ctx* c) {
   Engine& e = c->eng;
   dev_free_t(c, e.X); dev_free_t(c, e.R); dev_free_t(c, e.Z); dev_free_t(c, e.P);
@@ -939,10 +953,10 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     winv[i] = 1.0 / w[i];
     minv[i] = 1.0 / d[i];
   }
-  SG_CUDA(c, cudaMemcpyAsync(e.winv + slot * e.np, winv.data(), e.np * 8, cudaMemcpyHostToDevice, c->side));
-  SG_CUDA(c, cudaMemcpyAsync(e.minv + slot * e.np, minv.data(), e.np * 8, cudaMemcpyHostToDevice, c->side));
+  SG_CUDA(c, h2d(c, e.winv + slot * e.np, winv.data(), e.np * 8, c->side));
+  SG_CUDA(c, h2d(c, e.minv + slot * e.np, minv.data(), e.np * 8, c->side));
   e.h_ph[slot] = PhenoState{tau[0], tau[1]};
-  SG_CUDA(c, cudaMemcpyAsync(e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), cudaMemcpyHostToDevice, c->side));
+  SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), c->side));
   e.ph_set[slot] = 1;
   return sync_side(c);
 }
@@ -1009,7 +1023,7 @@ static int engine_admit(sg_ctx* c) {
         pruns.push_back(r.run);
         psel.push_back((int32_t)sel);
       } else {
-        SG_CUDA(c, cudaMemcpyAsync(e.B + sel * e.np, r.b.data(), c->nn * 8, cudaMemcpyHostToDevice, c->stream));
+        SG_CUDA(c, h2d(c, e.B + sel * e.np, r.b.data(), c->nn * 8, c->stream));
         if (e.np > c->nn)
           SG_CUDA(c, cudaMemsetAsync(e.B + sel * e.np + c->nn, 0, (e.np - c->nn) * 8, c->stream));
       }
@@ -1019,7 +1033,7 @@ static int engine_admit(sg_ctx* c) {
       s.maxiter = r.maxiter;
       s.tol = r.tol;
       e.h_st[col] = s;
-      SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &e.h_st[col], sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+      SG_CUDA(c, h2d(c, e.d_st + col, &e.h_st[col], sizeof(ColState), c->stream));
       e.col_req[col] = id;
       r.col = col;
       r.state = 1;
@@ -1036,13 +1050,13 @@ static int engine_admit(sg_ctx* c) {
       uint64_t* d_seeds = reinterpret_cast<uint64_t*>(e.ptab);
       int64_t* d_runs = reinterpret_cast<int64_t*>(d_seeds + kp);
       int32_t* d_sel = reinterpret_cast<int32_t*>(d_runs + kp);
-      SG_CUDA(c, cudaMemcpyAsync(d_seeds, pseeds.data(), kp * 8, cudaMemcpyHostToDevice, c->stream));
-      SG_CUDA(c, cudaMemcpyAsync(d_runs, pruns.data(), kp * 8, cudaMemcpyHostToDevice, c->stream));
-      SG_CUDA(c, cudaMemcpyAsync(d_sel, psel.data(), kp * 4, cudaMemcpyHostToDevice, c->stream));
+      SG_CUDA(c, h2d(c, d_seeds, pseeds.data(), kp * 8, c->stream));
+      SG_CUDA(c, h2d(c, d_runs, pruns.data(), kp * 8, c->stream));
+      SG_CUDA(c, h2d(c, d_sel, psel.data(), kp * 4, c->stream));
       launch_probe_fill_multi(e.np, c->nn, d_seeds, d_runs, d_sel, (int64_t)kp, e.B, c->stream);
       c->launches += 1;
     }
-    SG_CUDA(c, cudaMemcpyAsync(e.d_cols, cols.data(), cols.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    SG_CUDA(c, h2d(c, e.d_cols, cols.data(), cols.size() * 4, c->stream));
     launch_pcg_init(e.np, e.cap_cols, e.d_cols, (int64_t)cols.size(), e.d_st, e.d_ph, e.minv, e.B,
                     e.X, e.R, e.Z, e.P, e.Pf, e.part, e.nblk, c->stream);
     SG_LAUNCHED(c, 2);
@@ -1158,7 +1172,7 @@ static int step_launch(sg_ctx* c) {
   launch_pcg_dir(e.np, e.hi_col, e.d_st, e.Z, e.P, e.Pf, c->stream);
   SG_LAUNCHED(c, 5);
   SG_CUDA(c, cudaEventRecord(e.ev[2], c->stream));
-  SG_CUDA(c, cudaMemcpyAsync(e.h_pin, e.d_st, e.hi_col * sizeof(ColState), cudaMemcpyDeviceToHost, c->stream));
+  SG_CUDA(c, d2h(c, e.h_pin, e.d_st, e.hi_col * sizeof(ColState), c->stream));
   e.inflight = true;
   e.inflight_ncols = ncols;
   e.inflight_occupied = occupied;
@@ -1211,7 +1225,7 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
       e.finished.push_back(id);
       if (!e.hold) {  // copy the result out now and free the column
         r.x.resize(c->nn);
-        SG_CUDA(c, cudaMemcpyAsync(r.x.data(), e.X + col * e.np, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
+        SG_CUDA(c, d2h(c, r.x.data(), e.X + col * e.np, c->nn * 8, c->stream));
         r.col = -1;
       }
     }
@@ -1222,7 +1236,7 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
       s.kind = -2;  // held: result stays in X[col]
       s.active = 0;
       s.just_done = 0;
-      SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+      SG_CUDA(c, h2d(c, e.d_st + col, &s, sizeof(ColState), c->stream));
     } else {
       SG_TRY(release_col(c, col));
     }
@@ -1242,7 +1256,7 @@ static int engine_step(sg_ctx* c, int64_t* n_finished) {
 static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
   Engine& e = c->eng;
   if (e.hi_col == 0) return SG_OK;
-  SG_CUDA(c, cudaMemcpyAsync(e.h_st.data(), e.d_st, e.hi_col * sizeof(ColState), cudaMemcpyDeviceToHost, c->stream));
+  SG_CUDA(c, d2h(c, e.h_st.data(), e.d_st, e.hi_col * sizeof(ColState), c->stream));
   SG_TRY(sync(c));
   for (int64_t col = 0; col < e.hi_col; ++col) {
     const int64_t id = e.col_req[col];
@@ -1263,7 +1277,7 @@ static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
     if (e.hold && it != e.reqs.end()) {
       s.kind = -2;
       s.just_done = 0;
-      SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+      SG_CUDA(c, h2d(c, e.d_st + col, &s, sizeof(ColState), c->stream));
     } else {
       SG_TRY(release_col(c, col));
     }
@@ -1361,7 +1375,7 @@ static int apply_releases(sg_ctx* c) {
     if (e.col_req[col] != -1) continue;  // reused since: admission initialises it
     e.h_st[col] = s;
     // pageable source: the call returns once the bytes are staged
-    SG_CUDA(c, cudaMemcpyAsync(e.d_st + col, &s, sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+    SG_CUDA(c, h2d(c, e.d_st + col, &s, sizeof(ColState), c->stream));
     SG_CUDA(c, cudaMemsetAsync(e.Pf + col * e.np, 0, e.np * 4, c->stream));
   }
   e.pending_release.clear();
@@ -1376,7 +1390,7 @@ extern "C" int sg_engine_fetch(sg_ctx* c, int64_t id, double* x, int32_t* iters)
   Req& r = it->second;
   if (r.state != 2) return set_err(c, SG_ERR_STATE, "request %lld not finished", (long long)id);
   if (r.col >= 0) {
-    if (x) SG_CUDA(c, cudaMemcpyAsync(x, e.X + r.col * e.np, c->nn * 8, cudaMemcpyDeviceToHost, c->side));
+    if (x) SG_CUDA(c, d2h(c, x, e.X + r.col * e.np, c->nn * 8, c->side));
     SG_TRY(release_col(c, r.col));
     SG_TRY(sync_side(c));
   } else if (x) {
@@ -1489,15 +1503,16 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
   if (p > 0) {
     SG_CUDA(c, cudaMemsetAsync(e.d_sx, 0, need_sx * 8, c->side));
     SG_CUDA(c, cudaMemcpy2DAsync(e.d_sx, e.np * 8, SX, c->nn * 8, c->nn * 8, p, cudaMemcpyHostToDevice, c->side));
+    e.io_h2d += (uint64_t)(c->nn * 8 * p);
   }
   std::vector<const double*> ptrs(su);
   ptrs.insert(ptrs.end(), au.begin(), au.end());
-  SG_CUDA(c, cudaMemcpyAsync(e.d_dcols, ptrs.data(), ptrs.size() * sizeof(void*), cudaMemcpyHostToDevice, c->side));
+  SG_CUDA(c, h2d(c, e.d_dcols, ptrs.data(), ptrs.size() * sizeof(void*), c->side));
   launch_probe_dots(e.np, c->nn, reinterpret_cast<const double* const*>(e.d_dcols), k,
                     e.minv + slot * e.np, seed, run0, e.d_sx, p, e.d_dpart, nblk, c->side);
   SG_LAUNCHED(c, 1);
   std::vector<double> part(need_part);
-  SG_CUDA(c, cudaMemcpyAsync(part.data(), e.d_dpart, need_part * 8, cudaMemcpyDeviceToHost, c->side));
+  SG_CUDA(c, d2h(c, part.data(), e.d_dpart, need_part * 8, c->side));
   SG_TRY(sync_side(c));
   for (int64_t j = 0; j < k; ++j)
     for (int64_t v = 0; v < nv; ++v) {
@@ -1548,6 +1563,14 @@ extern "C" int sg_engine_reset_timing(sg_ctx* c) {
   if (!c) return SG_ERR_INVALID;
   Engine& e = c->eng;
   e.t_step_ms = e.t_gemm_ms = e.gemm_launches = e.gemm_flops = e.gemm_cols = e.useful_cols = 0;
+  e.io_h2d = e.io_d2h = 0;
+  return SG_OK;
+}
+
+extern "C" int sg_engine_io_bytes(sg_ctx* c, uint64_t* h2d_bytes, uint64_t* d2h_bytes) {
+  if (!c || !h2d_bytes || !d2h_bytes) return SG_ERR_INVALID;
+  *h2d_bytes = c->eng.io_h2d;
+  *d2h_bytes = c->eng.io_d2h;
   return SG_OK;
 }
 

@@ -453,6 +453,12 @@ class Context:
     def engine_reset_timing(self):
         self._call("sg_engine_reset_timing")
 
+    def engine_io_bytes(self):
+        """(host->device, device->host) bytes moved by engine calls since the last timing reset."""
+        a, b = C.c_uint64(), C.c_uint64()
+        self._call("sg_engine_io_bytes", C.byref(a), C.byref(b))
+        return a.value, b.value
+
     def engine_stats(self):
         s = np.zeros(4, np.int64)
         self._call("sg_engine_stats", _ptr(s, L.P_i64))
