@@ -108,6 +108,7 @@ struct sg_ctx {
   float* d_K = nullptr;
   float* d_Klo = nullptr;   // K - tf32(K) while the split-TF32 engine is selected (d_K then holds tf32(K))
   bool k_split = false;
+  int num_sms = 152;
   void* d_Kb = nullptr;     // BF16 high (first n_p^2) and low halves of K for SG_MV_BF16X3_TC
   double* d_diag = nullptr;
   float* d_diag32 = nullptr;
@@ -248,6 +249,8 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
   if (cudaSetDevice(device) != cudaSuccess) return SG_ERR_CUDA;
   sg_ctx* c = new sg_ctx();
   c->device = device;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (c->num_sms <= 0) c->num_sms = 1;
   c->budget = hbm_budget_bytes;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
@@ -1141,13 +1144,9 @@ static bool tc_mode(int mode) {
 
 static int64_t engine_gemm_cols(const sg_ctx* c) {
   const Engine& e = c->eng;
-  int64_t ncols = round_up(e.hi_col, 32);
-  if (tc_mode(c->mv_mode)) {
-    const int64_t w = ncols > 320 ? 256 : (ncols > 96 ? 128 : 32);
-    const int64_t padded = std::min(round_up(ncols, w), e.cap_cols);
-    if (padded % w == 0) ncols = padded;
-  }
-  return ncols;
+  const int64_t ncols = round_up(e.hi_col, 32);
+  if (!tc_mode(c->mv_mode)) return ncols;
+  return tc_grmv_padded_cols(ncols, e.cap_cols, e.np, c->mv_mode != SG_MV_TF32_TC, c->num_sms);
 }
 
 // First half of a step over columns [0, hi_col): GRM product + the FP64 PCG vector work, the

@@ -231,7 +231,8 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   constexpr int kStageBytes = (kATileBytes + kBTileBytes) * (kSplit ? 2 : 1);
   constexpr uint32_t kFmt = kTF32 ? 2u : 1u;
   constexpr int kKSteps = 4;           // 128-byte slice / 32 bytes per MMA K step
-  constexpr uint32_t kTmemCols = BN < 32 ? 32 : BN;
+  // TMEM is allocated in powers of two >= 32 columns
+  constexpr uint32_t kTmemCols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
   constexpr uint32_t kIdesc = make_idesc(kFmt, BN);
 
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -404,7 +405,8 @@ cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap
                    const CUtensorMap& b2, const TileCoord* tiles, int ntiles, int num_kb, float* D,
                    int64_t ldd, float scale, int mode, cudaStream_t s, int64_t nrows) {
   auto k = tc_gemm_kernel<kTF32, BN, S, kSplit, kC>;
-  const size_t sm = smem_bytes<kTF32, BN, S, kSplit>();
+  constexpr size_t sm = smem_bytes<kTF32, BN, S, kSplit>();
+  static_assert(sm <= 232448, "stage ring exceeds the 227 KB of dynamic shared memory per CTA");
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   if (ntiles % kC != 0) return cudaErrorInvalidValue;
@@ -599,14 +601,43 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
   return check_error_flag(s);
 }
 
-// Column-tile width for the GRM.V: the widest tile that divides ncols (wider tiles re-read
-// the K strip fewer times; the split variants hold 2x operands per stage).
+// Column-tile widths of the GRM.V.  The split variants also come in 96..224 so that a column
+// count rarely needs padding to the next power of two.
+static const std::vector<int> kSplitWidths = {256, 224, 192, 160, 128, 96, 64, 32};
+static const std::vector<int> kPlainWidths = {256, 128, 64, 32};
+
+// Column-tile width for ncols columns: the widest tile that divides ncols (wider tiles re-read
+// the K strip fewer times).  A lone 256-wide block is split in two for more CTAs per wave.
 int tc_gemm_tile_n(int64_t ncols, bool split) {
-  (void)split;
-  if (ncols % 256 == 0 && ncols >= 512) return 256;
-  if (ncols % 128 == 0 && ncols >= 128) return 128;
-  if (ncols % 64 == 0) return 64;
+  for (int w : split ? kSplitWidths : kPlainWidths) {
+    if (w == 256 && ncols < 512 && !split) continue;
+    if (ncols % w == 0) return w;
+  }
   return 32;
+}
+
+// Columns one GRM.V launch covers for ncols32 (a multiple of 32) live columns, padded so that the
+// modelled cost is lowest, capped at cap columns.  Cost model (L2->SM bytes of one pass, which
+// bounds these kernels, over the fraction of the last wave of 1-CTA-per-SM tiles that is busy):
+//   padded * (A bytes per stage / BN + B bytes per stage per column) / wave_efficiency.
+int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, bool split, int num_sms) {
+  double best = 1e300;
+  int64_t best_cols = ncols32;
+  const int64_t nbm = np / kTileM;
+  for (int w : split ? kSplitWidths : kPlainWidths) {
+    const int64_t padded = (ncols32 + w - 1) / w * w;
+    if (padded > cap) continue;
+    const int bn = tc_gemm_tile_n(padded, split);
+    const int64_t tiles = nbm * (padded / bn);
+    const int64_t waves = (tiles + num_sms - 1) / num_sms;
+    const double eff = (double)tiles / (double)(waves * num_sms);
+    const double cost = (double)padded * ((double)kATileBytes / bn + (double)kRowBytes) / eff;
+    if (cost < best) {
+      best = cost;
+      best_cols = padded;
+    }
+  }
+  return best_cols;
 }
 
 template <bool kTF32, int BN, int S, int C>
@@ -629,7 +660,11 @@ static cudaError_t grmv_split_dispatch(int BN, int C, const CUtensorMap& a, cons
                     : launch_grmv_split<kTF32, BNv, Sv, 1>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s);
   switch (BN) {
     SG_GRMV_CASE(256, 2)
+    SG_GRMV_CASE(224, 2)
+    SG_GRMV_CASE(192, 2)
+    SG_GRMV_CASE(160, 3)
     SG_GRMV_CASE(128, 3)
+    SG_GRMV_CASE(96, 4)
     SG_GRMV_CASE(64, 4)
     SG_GRMV_CASE(32, 5)
     default:

@@ -101,6 +101,8 @@ bool tc_set_clusters(int syrk, int grmv);
 void tc_get_clusters(int* syrk, int* grmv);
 // Column tile width the GRM.V kernel uses for ncols columns.
 int tc_gemm_tile_n(int64_t ncols, bool split);
+// Columns a GRM.V launch covers for ncols32 live columns (padding chosen by a cost model).
+int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, bool split, int num_sms);
 // Split-TF32 GRM.V that allocates nothing: scratch in a static device array (k_tc.cu).
 int64_t tc_noalloc_max_elems();
 cudaError_t tc_gemm_tf32x3_noalloc(const float* Khi, const float* Klo, int64_t np, const float* P,

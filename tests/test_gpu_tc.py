@@ -78,7 +78,8 @@ def test_grmv_cluster_variants_bit_identical(cohort, mode):
     tol = 5e-6 if mode == "tf32x3" else 6e-5
     try:
         ctx.set_matvec_mode(MV_TF32X3_TC if mode == "tf32x3" else MV_BF16X3_TC)
-        for k in (32, 100, 256, 512):  # column tiles of 32, 128, 128 and 256 (padded)
+        # column tiles 32, 128, 160 (150 padded), 224 (200 padded), 256 and 256 (512)
+        for k in (32, 100, 150, 200, 256, 512):
             V = rng.standard_normal((grm.n, k))
             ctx.set_tc_clusters(1, 1)
             Y1 = ctx.grm_matmul(V)
