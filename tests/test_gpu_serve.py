@@ -113,7 +113,9 @@ def test_launch_finish_with_host_calls_in_flight(cohort):
         more = ctx.engine_submit(1, 0, B[:, 3:5], 500, 1e-10)  # joins the next launch
         ctx.engine_cancel(int(more[1]))
         done = {}
-        while len(done) < 4:
+        for _ in range(2000):  # every column stops within maxiter = 500 steps
+            if len(done) == 4:
+                break
             ctx.engine_finish()
             for rid in ctx.engine_poll():
                 done[int(rid)] = ctx.engine_fetch(int(rid))[0]
@@ -125,7 +127,9 @@ def test_launch_finish_with_host_calls_in_flight(cohort):
         ids2 = ctx.engine_submit(0, 0, B[:, :3], 500, 1e-10)
         ids3 = ctx.engine_submit(1, 0, B[:, 3:4], 500, 1e-10)
         got = {}
-        while len(got) < 4:
+        for _ in range(2000):
+            if len(got) == 4:
+                break
             ctx.engine_run(1)
             for rid in ctx.engine_poll():
                 got[int(rid)] = ctx.engine_fetch(int(rid))[0]
