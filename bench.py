@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--mode", default="tf32x3", choices=["bf16x3", "tf32x3", "tf32", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster-shape autotuner")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip timing the reference's two-SGEMV K.x algorithm on this GPU")
     ap.add_argument("--blocking-runner", action="store_true",
                     help="step the engine synchronously instead of overlapping the driver with the next step")
     ap.add_argument("--serve-requests", type=int, default=32,
@@ -301,6 +303,41 @@ def plain_fp64(ctx, iters_per_fit):
             "basis": "FP64 GEMV over the FP32 GRM, one RHS per solve; %.0f PCG iterations per fit" % iters_per_fit}
 
 
+def reference_gpu_matvec(n, m_qc, iters_per_fit, reps=5):
+    """The reference's own GPU algorithm for K.x, restated with cuBLAS through torch on this GPU:
+    two FP32 SGEMV over the N x M standardised genotype matrix Z per product (y = Z'x, z = Z y),
+    one right-hand side, as gpuSymMatMult::sym_sgemv (gpuSymMatMult.cu:211-252) on a single rank.
+    Z holds seeded random values (SGEMV time does not depend on them).  Extrapolated to fits/hr
+    with the measured PCG iterations per fit; the host PCG vector work is not included."""
+    import torch
+    try:
+        Z = torch.empty((m_qc, n), dtype=torch.float32, device="cuda")  # column-major N x M
+    except RuntimeError as ex:
+        return {"unavailable": "could not hold Z (%d x %d FP32): %s" % (n, m_qc, str(ex).splitlines()[0])}
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    for i in range(0, m_qc, 8192):
+        Z[i:i + 8192].normal_(generator=g)
+    x = torch.randn(n, device="cuda", generator=g)
+    s = torch.cuda.current_stream()
+    for _ in range(2):
+        z = torch.mv(Z.t(), torch.mv(Z, x))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        z = torch.mv(Z.t(), torch.mv(Z, x))
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    del Z, z, x
+    torch.cuda.empty_cache()
+    z_bytes = 4.0 * n * m_qc
+    return {"fits_per_hr": round(3600.0 / (ms * 1e-3 * iters_per_fit), 3), "ms_per_matvec": round(ms, 3),
+            "GBps": round(2 * z_bytes / (ms * 1e-3) / 1e9, 1), "z_gb": round(z_bytes / 1e9, 1),
+            "basis": "2 cuBLAS SGEMV over FP32 Z per K.x, single RHS; %.0f PCG iterations per fit; "
+                     "matvec only (reference's host vector work and MPI allreduce excluded)" % iters_per_fit}
+
+
 def run_ours(args, rank, world, local):
     import torch
     from saigegpu import Context, GRM_BF16_TC, MV_BF16X3_TC, MV_TF32X3_TC, MV_TF32_TC, MV_FP32_SIMT
@@ -409,6 +446,11 @@ def run_ours(args, rank, world, local):
     if rank == 0:
         out["plain_fp64_single_rhs"] = plain_fp64(ctx, col_iters)
         out["speedup_vs_plain_fp64"] = round(value / out["plain_fp64_single_rhs"]["fits_per_hr"], 1)
+        if not args.no_ref_gpu:
+            rg = reference_gpu_matvec(d["n"], d["m_qc"], col_iters)
+            out["reference_gpu_algorithm"] = rg
+            if "fits_per_hr" in rg:
+                out["speedup_vs_reference_gpu_algorithm"] = round(value / rg["fits_per_hr"], 1)
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(ctx, col_iters)
         try:
