@@ -93,6 +93,7 @@ class Context:
 
     def set_matvec_mode(self, mode):
         self._call("sg_set_matvec_mode", int(mode))
+        self._mv_mode = int(mode)
 
     # ------------------------------------------------------------ genotypes (setgeno)
     @staticmethod
@@ -108,6 +109,9 @@ class Context:
                 is_diag_one=False):
         buf = np.frombuffer(bed, dtype=np.uint8) if isinstance(bed, (bytes, bytearray)) else np.ascontiguousarray(bed, np.uint8)
         sub, mask, vr, nvr = self._geno_args(n_fam, sub_1based, pheno_mask, vr_random)
+        self._geno_src = ("setgeno", (buf, n_fam, m_bim), dict(
+            min_maf=min_maf, max_missing=max_missing, vr_random=vr_random, min_mac_vr=min_mac_vr,
+            is_var_ratio=is_var_ratio, is_diag_one=is_diag_one), sub, mask)
         self._call("sg_setgeno", _ptr(buf, L.P_u8), buf.size, n_fam, m_bim, _ptr(sub, L.P_i32), len(sub),
                    _ptr(mask, L.P_u8), min_maf, max_missing, _ptr(vr, L.P_i32), nvr, min_mac_vr,
                    int(is_var_ratio), int(is_diag_one))
@@ -117,6 +121,9 @@ class Context:
                       max_missing=0.15, vr_random=None, min_mac_vr=20.0, is_var_ratio=False,
                       is_diag_one=False):
         sub, mask, vr, nvr = self._geno_args(n_fam, sub_1based, pheno_mask, vr_random)
+        self._geno_src = ("setgeno_files", (bed, bim, fam), dict(
+            min_maf=min_maf, max_missing=max_missing, vr_random=vr_random, min_mac_vr=min_mac_vr,
+            is_var_ratio=is_var_ratio, is_diag_one=is_diag_one), sub, mask, n_fam)
         self._call("sg_setgeno_files", bed.encode(), bim.encode(), fam.encode(), _ptr(sub, L.P_i32),
                    len(sub), _ptr(mask, L.P_u8), min_maf, max_missing, _ptr(vr, L.P_i32), nvr,
                    min_mac_vr, int(is_var_ratio), int(is_diag_one))
@@ -126,6 +133,9 @@ class Context:
                        min_maf=0.01, max_missing=0.15, vr_random=None, min_mac_vr=20.0,
                        is_var_ratio=False, is_diag_one=False):
         sub, mask, vr, nvr = self._geno_args(n_fam, sub_1based, pheno_mask, vr_random)
+        self._geno_src = ("setgeno_device", (ptr, length, n_fam, m_bim), dict(
+            min_maf=min_maf, max_missing=max_missing, vr_random=vr_random, min_mac_vr=min_mac_vr,
+            is_var_ratio=is_var_ratio, is_diag_one=is_diag_one), sub, mask)
         self._call("sg_setgeno_device", C.c_void_p(ptr), length, n_fam, m_bim, _ptr(sub, L.P_i32),
                    len(sub), _ptr(mask, L.P_u8), min_maf, max_missing, _ptr(vr, L.P_i32), nvr,
                    min_mac_vr, int(is_var_ratio), int(is_diag_one))
@@ -181,6 +191,46 @@ class Context:
     # ------------------------------------------------------------ GRM
     def grm_build(self, precision=GRM_FP32_SIMT):
         self._call("sg_grm_build", int(precision))
+        self._grm_prec = int(precision)
+
+    # ------------------------------------------------------------ per-subset cohorts
+    def cohort(self):
+        """The current cohort (1-based .fam indices and .fam phenotype mask) and GRM settings."""
+        src = getattr(self, "_geno_src", None)
+        if src is None:
+            raise RuntimeError("no genotypes loaded")
+        return dict(sub=src[3].copy(), mask=src[4].copy(), grm=getattr(self, "_grm_prec", None),
+                    mode=getattr(self, "_mv_mode", None))
+
+    def set_cohort(self, sub_1based, pheno_mask, grm=None, mode=None):
+        """Reload the same genotypes for another sample list -- allele frequencies, QC, imputation,
+        standardisation and the diagonal are recomputed over it, as setgeno does for the samples
+        of one phenotype (FIT.cpp:739-1024) -- then rebuild the GRM and restore the product mode."""
+        src = getattr(self, "_geno_src", None)
+        if src is None:
+            raise RuntimeError("no genotypes loaded")
+        kind, args, kw = src[0], src[1], src[2]
+        if kind == "setgeno_files":
+            self.setgeno_files(*args, sub_1based, src[5], pheno_mask=pheno_mask, **kw)
+        else:
+            getattr(self, kind)(*args, sub_1based=sub_1based, pheno_mask=pheno_mask, **kw)
+        if grm is not None:
+            self.grm_build(grm)
+        if mode is not None:
+            self.set_matvec_mode(mode)
+
+    def subset_cohort(self, keep):
+        """Restrict the cohort to the samples where ``keep`` (bool over the current cohort) is
+        true and rebuild the GRM with the current settings; returns the previous cohort."""
+        prev = self.cohort()
+        keep = np.asarray(keep, bool)
+        if keep.shape != prev["sub"].shape:
+            raise ValueError("keep must cover the %d cohort samples" % len(prev["sub"]))
+        sub = prev["sub"][keep]
+        fam_mask = np.zeros_like(prev["mask"])
+        fam_mask[sub - 1] = prev["mask"][sub - 1]
+        self.set_cohort(sub, fam_mask, prev["grm"], prev["mode"])
+        return prev
 
     def grm_padded_n(self):
         """N rounded up to the 128-row tile: the GRM's leading dimension on the device."""

@@ -25,8 +25,9 @@ neighbours, so a fit gives the same result alone or in a mix.
 
 Sample subsets: a fit may use a mask over the cohort's samples; its vectors are
 zero outside the subset and the engine solves with Sigma[S, S] built from the
-cohort GRM restricted to S (the reference instead recomputes allele
-frequencies on each subset, so this is exact only for full-cohort fits).
+cohort GRM restricted to S.  The reference instead recomputes allele
+frequencies (and QC, imputation, standardisation) on each subset;
+``fit_batch_exact_subsets`` does that, one GRM build per distinct subset.
 """
 import time
 
@@ -585,6 +586,47 @@ def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=False):
     for j in jobs:
         j.host_times = r.t
     return [by[i].result if by[i].error is None else by[i].error for i in ids], jobs
+
+
+def fit_batch_exact_subsets(ctx, specs, max_columns=None, max_phenos=None, pipelined=False):
+    """Fits whose sample masks differ run on GRMs rebuilt for their own subsets.
+
+    Specs are grouped by mask; each group's samples become the cohort (``Context.subset_cohort``:
+    allele frequencies, QC, imputation, standardisation and K recomputed over the subset, as the
+    reference's setgeno does for a phenotype observed on those samples) and the group is fitted as
+    full-cohort fits; the original cohort and its GRM are restored at the end.  One GRM build per
+    distinct subset.  Returns (results, jobs) in the order of ``specs``."""
+    import copy
+    groups = {}
+    for i, sp in enumerate(specs):
+        key = None if sp.mask is None or bool(np.all(sp.mask)) else np.packbits(sp.mask).tobytes()
+        groups.setdefault(key, []).append(i)
+    results, jobs = [None] * len(specs), [None] * len(specs)
+    order = sorted(groups, key=lambda k: k is not None)  # the resident full cohort first
+    prev = None
+    try:
+        for key in order:
+            idx = groups[key]
+            if key is not None:
+                if prev is None:
+                    prev = ctx.cohort()
+                keep = np.asarray(specs[idx[0]].mask, bool)
+                sub = prev["sub"][keep]
+                fam_mask = np.zeros_like(prev["mask"])
+                fam_mask[sub - 1] = prev["mask"][sub - 1]
+                ctx.set_cohort(sub, fam_mask, prev["grm"], prev["mode"])
+            sub_specs = []
+            for i in idx:
+                sp = copy.copy(specs[i])
+                sp.mask = None
+                sub_specs.append(sp)
+            res, jb = fit_batch(ctx, sub_specs, max_columns, max_phenos, pipelined)
+            for i, r, j in zip(idx, res, jb):
+                results[i], jobs[i] = r, j
+    finally:
+        if prev is not None:
+            ctx.set_cohort(prev["sub"], prev["mask"], prev["grm"], prev["mode"])
+    return results, jobs
 
 
 def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter, pipelined=False):

@@ -137,3 +137,36 @@ def test_launch_finish_with_host_calls_in_flight(cohort):
             np.testing.assert_array_equal(done[int(a)], got[int(b)])
     finally:
         ctx.engine_hold_results(False)
+
+
+def test_exact_subset_fits_match_oracle_on_subset_cohort():
+    """Per-subset exactness: allele frequencies, QC and K recomputed on the phenotype's samples,
+    like the reference's setgeno with that sample list; the oracle does the same on the CPU."""
+    from saigegpu import Context
+    n, m = 520, 1400
+    bed, _ = synth.synth_bed(61, n, m, 0.02)
+    gpu_ctx = Context(0)
+    gpu_ctx.setgeno(bed, n, m)
+    gpu_ctx.grm_build(GRM_FP32_SIMT)
+    gpu_ctx.set_matvec_mode(MV_FP32_SIMT)
+    g_all = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+    gv = synth.genetic_value_from_codes(g_all.codes, 9)
+    rng = np.random.default_rng(8)
+    specs, refs = [], []
+    for k, trait in enumerate(["binary", "quantitative"]):
+        mask = rng.uniform(size=n) > 0.3
+        S = np.nonzero(mask)[0]
+        y, C = synth.simulate_pheno(gv, 70 + k, trait, tau=0.6, prevalence=0.3, h2=0.5)
+        f0 = prep.make_fit0(y[S], C[S], trait, True)
+        specs.append(serve.FitSpec(f0, trait, mask=mask))
+        g_sub = plink.setgeno(bed, n, m, S + 1, mask, 0.01, 0.15)
+        sub = aireml.DenseGRM(g_sub)
+        refs.append((aireml.glmmkin_binary if trait == "binary" else aireml.glmmkin_quantitative)(sub, f0))
+    before = gpu_ctx.dims()
+    res, _ = serve.fit_batch_exact_subsets(gpu_ctx, specs, max_columns=256)
+    assert gpu_ctx.dims() == before  # the full cohort is restored
+    for r, ref in zip(res, refs):
+        assert not isinstance(r, Exception), r
+        np.testing.assert_allclose(r["theta"], ref["theta"], rtol=1e-4)
+        np.testing.assert_allclose(r["coefficients"], ref["coefficients"], rtol=1e-4, atol=1e-8)
+    gpu_ctx.close()

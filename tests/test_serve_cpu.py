@@ -193,3 +193,50 @@ def test_pipelined_runner_reports_a_stall():
     import pytest
     with pytest.raises(RuntimeError, match="engine idle"):
         r.run()
+
+
+class FakeCohortEngine(FakeEngine):
+    """FakeEngine over a cohort that ``set_cohort`` reloads from the bed on the CPU oracle."""
+
+    def __init__(self, bed, n_fam, m_bim):
+        self.bed, self.n_fam, self.m_bim = bed, n_fam, m_bim
+        self.loads = 0
+        self.set_cohort(np.arange(1, n_fam + 1, dtype=np.int32), np.ones(n_fam, np.uint8))
+
+    def cohort(self):
+        return dict(sub=self.sub.copy(), mask=self.fmask.copy(), grm=0, mode=0)
+
+    def set_cohort(self, sub_1based, pheno_mask, grm=None, mode=None):
+        self.sub, self.fmask = np.asarray(sub_1based, np.int32), np.asarray(pheno_mask, np.uint8)
+        g = plink.setgeno(self.bed, self.n_fam, self.m_bim, self.sub, self.fmask.astype(bool), 0.01, 0.15)
+        FakeEngine.__init__(self, aireml.DenseGRM(g))
+        self.loads += 1
+
+    def dims(self):
+        return dict(n=self.n)
+
+
+def test_exact_subset_grouping_and_restore():
+    n, m = 260, 800
+    bed, _ = synth.synth_bed(37, n, m, 0.02)
+    eng = FakeCohortEngine(bed, n, m)
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+    gv = synth.genetic_value_from_codes(g.codes, 2)
+    rng = np.random.default_rng(4)
+    masks = [None, rng.uniform(size=n) > 0.3, None]
+    masks.append(masks[1].copy())  # a second fit on the same subset: one rebuild for both
+    specs, refs = [], []
+    for k, mask in enumerate(masks):
+        trait = "quantitative" if k % 2 else "binary"
+        S = np.arange(n) if mask is None else np.nonzero(mask)[0]
+        y, C = synth.simulate_pheno(gv, 90 + k, trait, tau=0.5, prevalence=0.3, h2=0.5)
+        f0 = prep.make_fit0(y[S], C[S], trait, True)
+        specs.append(serve.FitSpec(f0, trait, mask=mask))
+        gs = plink.setgeno(bed, n, m, S + 1, np.isin(np.arange(n), S), 0.01, 0.15)
+        refs.append((aireml.glmmkin_binary if trait == "binary" else aireml.glmmkin_quantitative)(aireml.DenseGRM(gs), f0))
+    res, _ = serve.fit_batch_exact_subsets(eng, specs)
+    assert eng.loads == 3  # initial load, one subset, the restore
+    assert eng.n == n and np.array_equal(eng.sub, np.arange(1, n + 1))
+    for r, ref in zip(res, refs):
+        assert not isinstance(r, Exception), r
+        np.testing.assert_allclose(r["theta"], ref["theta"], rtol=1e-4)
