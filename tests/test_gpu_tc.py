@@ -74,8 +74,9 @@ def test_grmv_cluster_variants_bit_identical(cohort, mode):
     ctx.grm_build(GRM_FP32_SIMT)
     Kg = ctx.grm_get().astype(np.float64)  # the resident FP32 K the split halves come from
     rng = np.random.default_rng(3)
-    # split TF32: 22 significant bits per operand; split BF16: 16 (relative 2^-17 per factor)
-    tol = 5e-6 if mode == "tf32x3" else 6e-5
+    # split TF32: ~21 significant bits per operand (the MMA reads the low halves at TF32
+    # precision); split BF16: 16.  Both accumulate in the tensor cores' FP32 over n terms.
+    tol = 2e-5 if mode == "tf32x3" else 6e-5
     try:
         ctx.set_matvec_mode(MV_TF32X3_TC if mode == "tf32x3" else MV_BF16X3_TC)
         # column tiles 32, 128, 160 (150 padded), 224 (200 padded), 256 and 256 (512)
