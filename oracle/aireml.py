@@ -173,7 +173,9 @@ def get_ai_score(grm, Y, X, w, tau, Sigma_iY, Sigma_iX, cov, nrun, maxiter, tol,
     S, it = pcg(grm, w, tau, APY, maxiter, tol, return_iters=True)
     if stats is not None:
         stats.append(("papy", 1, it))
-    PAPY = _p_apply(S, Sigma_iX, cov, APY)
+    # the reference projects the solved vector: PAPY_1 - Sigma_iX cov (Sigma_iX' PAPY_1)
+    # (FIT.cpp:3290-3291), not Sigma_iX' APY as P APY would have it
+    PAPY = _p_apply(S, Sigma_iX, cov, S)
     AI = float(APY @ PAPY)
     return dict(YPAPY=YPAPY, Trace=trace, PY=PY, AI=AI, nprobe=nprobe)
 
@@ -192,8 +194,9 @@ def get_ai_score_q(grm, Y, X, w, tau, Sigma_iY, Sigma_iX, cov, nrun, maxiter, to
     S, it = pcg(grm, w, tau, np.column_stack([A0PY, APY]), maxiter, tol, return_iters=True)
     if stats is not None:
         stats.append(("papy", 2, it))
-    PA0PY = _p_apply(S[:, 0], Sigma_iX, cov1, A0PY)
-    PAPY = _p_apply(S[:, 1], Sigma_iX, cov1, APY)
+    # as in getAIScore, the projection acts on the solved vectors (FIT.cpp:3507-3508, 3513-3514)
+    PA0PY = _p_apply(S[:, 0], Sigma_iX, cov1, S[:, 0])
+    PAPY = _p_apply(S[:, 1], Sigma_iX, cov1, S[:, 1])
     AI = np.array([[A0PY @ PA0PY, A0PY @ PAPY], [A0PY @ PAPY, APY @ PAPY]])
     return dict(YPAPY=YPAPY, YPA0PY=YPA0PY, Trace=trace, PY=PY, AI=AI, nprobe=nprobe)
 

@@ -2154,12 +2154,14 @@ int ai_score(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* 
   o->tr0 = s0 / t0.size();
   std::vector<double> S(n), PAPY(n);
   SG_TRY(fetch(c, sid[0], S.data(), nullptr));
-  p_apply(n, (int)p, S.data(), SX.data(), cv.data(), APY.data(), PAPY.data());
+  // the reference projects the solved vector: PAPY_1 - Sigma_iX cov (Sigma_iX' PAPY_1)
+  // (FIT.cpp:3290-3291; 3507-3508 and 3513-3514 in the _q form)
+  p_apply(n, (int)p, S.data(), SX.data(), cv.data(), S.data(), PAPY.data());
   o->AI[3] = dot(n, APY.data(), PAPY.data());
   if (quant) {
     std::vector<double> PA0PY(n);
     SG_TRY(fetch(c, sid[1], S.data(), nullptr));
-    p_apply(n, (int)p, S.data(), SX.data(), cv.data(), o->PY.data(), PA0PY.data());
+    p_apply(n, (int)p, S.data(), SX.data(), cv.data(), S.data(), PA0PY.data());
     o->AI[0] = dot(n, o->PY.data(), PA0PY.data());
     o->AI[1] = o->AI[2] = dot(n, o->PY.data(), PAPY.data());
   }

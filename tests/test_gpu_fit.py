@@ -78,9 +78,7 @@ def test_config1_cpu_runnable_case(gpu_ctx):
     from saigegpu import serve
     from test_serve_cpu import FakeEngine
     rb, _ = serve.fit_batch(gpu_ctx, [serve.FitSpec(fit0, "binary")], max_columns=128)
-    # The batched driver itself, run in FP64 on the CPU (the oracle's PCG per column), differs from
-    # the sequential oracle by ~1.3e-4 here: one PCG column stops an iteration apart when its
-    # absolute sum r^2 crosses tolPCG.  Against that driver the GPU engine agrees far closer.
+    np.testing.assert_allclose(rb[0]["theta"], ro["theta"], rtol=1e-4)
+    # the batched driver run in FP64 on the CPU (the oracle's PCG per column) as a second check
     r64, _ = serve.fit_batch(FakeEngine(grm), [serve.FitSpec(fit0, "binary")])
     np.testing.assert_allclose(rb[0]["theta"], r64[0]["theta"], rtol=1e-5)
-    np.testing.assert_allclose(rb[0]["theta"], ro["theta"], rtol=3e-4)

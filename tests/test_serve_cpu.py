@@ -103,9 +103,9 @@ def test_generator_fit_equals_oracle_fit():
         f0 = prep.make_fit0(y, C, trait, True)
         ref = (aireml.glmmkin_binary if trait == "binary" else aireml.glmmkin_quantitative)(grm, f0)
         res, jobs = serve.fit_batch(FakeEngine(grm), [serve.FitSpec(f0, trait)])
-        # same algorithm; summation order differs (a PCG column may stop one iteration apart)
-        np.testing.assert_allclose(res[0]["theta"], ref["theta"], rtol=1e-4)
-        np.testing.assert_allclose(res[0]["coefficients"], ref["coefficients"], rtol=1e-4, atol=1e-8)
+        # same algorithm in FP64; only the summation order differs
+        np.testing.assert_allclose(res[0]["theta"], ref["theta"], rtol=1e-9)
+        np.testing.assert_allclose(res[0]["coefficients"], ref["coefficients"], rtol=1e-9, atol=1e-12)
         assert res[0]["iterations"] == ref["iterations"]
 
 
@@ -239,4 +239,4 @@ def test_exact_subset_grouping_and_restore():
     assert eng.n == n and np.array_equal(eng.sub, np.arange(1, n + 1))
     for r, ref in zip(res, refs):
         assert not isinstance(r, Exception), r
-        np.testing.assert_allclose(r["theta"], ref["theta"], rtol=1e-4)
+        np.testing.assert_allclose(r["theta"], ref["theta"], rtol=1e-9)
