@@ -257,7 +257,11 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
     return SG_ERR_CUDA;
   }
   for (auto& ev : c->tev) cudaEventCreate(&ev);
-  if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) {
+  // the side stream carries short reductions and copies that the driver waits on while a step's
+  // GEMM fills the GPU: highest priority, so its blocks are dispatched as soon as an SM frees up
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  if (cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
     cudaStreamDestroy(c->stream);
     delete c;
     return SG_ERR_CUDA;

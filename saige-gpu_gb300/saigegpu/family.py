@@ -25,6 +25,17 @@ class Binomial:
     def variance(self, mu):
         return mu * (1.0 - mu)
 
+    def parts(self, eta):
+        """(linkinv, mu_eta, variance) of eta with one exponential; bit-identical to the
+        three separate calls."""
+        eta = np.asarray(eta, np.float64)
+        e = np.exp(np.clip(eta, -30, 30))
+        lo, hi = eta < -30.0, eta > 30.0
+        tmp = np.where(lo, _EPS, np.where(hi, 1.0 / _EPS, e))
+        mu = tmp / (1.0 + tmp)
+        mu_eta = np.where(hi | lo, _EPS, e / ((1.0 + e) * (1.0 + e)))
+        return mu, mu_eta, mu * (1.0 - mu)
+
     def deviance(self, y, mu):
         with np.errstate(divide="ignore", invalid="ignore"):
             a = np.where(y > 0, y * np.log(y / mu), 0.0)
@@ -43,6 +54,11 @@ class Gaussian:
 
     def variance(self, mu):
         return np.ones_like(np.asarray(mu, np.float64))
+
+    def parts(self, eta):
+        mu = np.array(eta, np.float64, copy=True)
+        one = np.ones_like(mu)
+        return mu, one, one
 
     def deviance(self, y, mu):
         return float(np.sum((y - mu) ** 2))

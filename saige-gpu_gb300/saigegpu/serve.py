@@ -116,10 +116,9 @@ def fit_generator(spec, n_cohort, probes):
     stats = {"pcg_columns": 0, "column_iterations": 0, "products": 0}
 
     def working(eta_):
-        mu = fam.linkinv(eta_)
-        mu_eta = fam.mu_eta(eta_)
+        mu, mu_eta, var = fam.parts(eta_)
         Y = np.where(m, eta_ - offset + (y - mu) / mu_eta, 0.0)
-        W = np.where(m, (mu_eta / np.sqrt(fam.variance(mu))) ** 2, 1.0)
+        W = np.where(m, (mu_eta / np.sqrt(var)) ** 2, 1.0) if not quant else np.ones_like(Y)
         return mu, Y, W
 
     def get_coefficients(Y, W, tau):
@@ -276,10 +275,9 @@ def loco_generator(spec, fit, n_cohort):
     eta0 = full(fit["linear_predictors"])
 
     def working(eta_):
-        mu = fam.linkinv(eta_)
-        mu_eta = fam.mu_eta(eta_)
+        mu, mu_eta, var = fam.parts(eta_)
         Y = np.where(m, eta_ - offset + (y - mu) / mu_eta, 0.0)
-        W = np.where(m, (mu_eta / np.sqrt(fam.variance(mu))) ** 2, 1.0)
+        W = np.where(m, (mu_eta / np.sqrt(var)) ** 2, 1.0) if not quant else np.ones_like(Y)
         return mu, Y, W
 
     mu, Y, W = working(eta0)

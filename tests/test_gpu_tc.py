@@ -55,6 +55,7 @@ def test_grm_matvec_tf32_tc(cohort):
 def test_syrk_cluster_variants_bit_identical(cohort, split):
     ctx, grm = cohort
     prec = GRM_BF16X3_TC if split else GRM_BF16_TC
+    prev = ctx.get_tc_clusters()
     try:
         ctx.set_tc_clusters(1, 1)
         ctx.grm_build(prec)
@@ -64,7 +65,7 @@ def test_syrk_cluster_variants_bit_identical(cohort, split):
             ctx.grm_build(prec)
             assert np.array_equal(ctx.grm_get(), K1), c
     finally:
-        ctx.set_tc_clusters(1, 1)
+        ctx.set_tc_clusters(*prev)
 
 
 @pytest.mark.parametrize("mode", ["tf32x3", "bf16x3"])
@@ -77,6 +78,7 @@ def test_grmv_cluster_variants_bit_identical(cohort, mode):
     # split TF32: ~21 significant bits per operand (the MMA reads the low halves at TF32
     # precision); split BF16: 16.  Both accumulate in the tensor cores' FP32 over n terms.
     tol = 2e-5 if mode == "tf32x3" else 6e-5
+    prev = ctx.get_tc_clusters()
     try:
         ctx.set_matvec_mode(MV_TF32X3_TC if mode == "tf32x3" else MV_BF16X3_TC)
         # column tiles 32, 128, 160 (150 padded), 224 (200 padded), 256 and 256 (512)
@@ -90,7 +92,7 @@ def test_grmv_cluster_variants_bit_identical(cohort, mode):
                 ctx.set_tc_clusters(1, c)
                 assert np.array_equal(ctx.grm_matmul(V), Y1), (k, c)
     finally:
-        ctx.set_tc_clusters(1, 1)
+        ctx.set_tc_clusters(*prev)
         ctx.set_matvec_mode(MV_FP32_SIMT)
 
 
