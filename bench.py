@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--phenos", type=int, default=32)
     ap.add_argument("--miss", type=float, default=0.02)
     ap.add_argument("--seed", type=int, default=1003)
-    ap.add_argument("--mode", default="tf32x3", choices=["bf16x3", "tf32x3", "tf32", "fp32"])
+    ap.add_argument("--mode", default="bf16x3", choices=["bf16x3", "tf32x3", "tf32", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster-shape autotuner")
     ap.add_argument("--no-ref-gpu", action="store_true",
