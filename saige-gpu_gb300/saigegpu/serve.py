@@ -363,7 +363,7 @@ class Runner:
     """Continuous batching of many null-model fits over one engine."""
 
     def __init__(self, ctx, max_columns=2048, max_phenos=64, min_columns_per_fit=2 * (30 + 10) + 8,
-                 pipelined=False):
+                 pipelined=True):
         if max_columns < min_columns_per_fit:
             # a fit's trace stage keeps ~2 (nrun + 10) + 4 columns in flight at once
             raise ValueError("max_columns=%d is below one fit's working set (%d)" % (max_columns, min_columns_per_fit))
@@ -573,7 +573,7 @@ def columns_for(specs):
     return int(-(-need // 256) * 256)
 
 
-def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=False):
+def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True):
     """Fit all ``specs`` together; returns their result dicts (or exceptions) in order."""
     max_columns = max(max_columns or 0, columns_for(specs))
     r = Runner(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined=pipelined)
@@ -586,7 +586,7 @@ def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=False):
     return [by[i].result if by[i].error is None else by[i].error for i in ids], jobs
 
 
-def fit_batch_exact_subsets(ctx, specs, max_columns=None, max_phenos=None, pipelined=False):
+def fit_batch_exact_subsets(ctx, specs, max_columns=None, max_phenos=None, pipelined=True):
     """Fits whose sample masks differ run on GRMs rebuilt for their own subsets.
 
     Specs are grouped by mask; each group's samples become the cohort (``Context.subset_cohort``:
@@ -627,7 +627,7 @@ def fit_batch_exact_subsets(ctx, specs, max_columns=None, max_phenos=None, pipel
     return results, jobs
 
 
-def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter, pipelined=False):
+def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter, pipelined=True):
     """Serve a stream of (t_arrival_seconds, FitSpec): admit as slots and columns free up.
 
     Returns the finished jobs (with t_arrive / t_start / t_done) in completion order.

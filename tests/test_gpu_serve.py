@@ -81,7 +81,7 @@ def test_pipelined_runner_equals_synchronous(cohort, mode):
     ctx, grm, specs, refs = cohort
     ctx.set_matvec_mode(mode)
     try:
-        sync, _ = serve.fit_batch(ctx, specs, max_columns=256)
+        sync, _ = serve.fit_batch(ctx, specs, max_columns=256, pipelined=False)
         pipe, _ = serve.fit_batch(ctx, specs, max_columns=256, pipelined=True)
     finally:
         ctx.set_matvec_mode(MV_FP32_SIMT)
