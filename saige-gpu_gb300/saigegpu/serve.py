@@ -357,6 +357,7 @@ class _Job:
         self.error = None
         self.column_iterations = 0
         self.columns = 0
+        self.ready_at = None  # step at which every awaited column was done
 
 
 class Runner:
@@ -385,6 +386,8 @@ class Runner:
         # columns join step k+2)
         self.pipelined = bool(pipelined) and hasattr(ctx, "engine_launch")
         self._launched = False
+        self._steps = 0
+        self._gpu_ms = 0.0
         # wall-clock seconds by activity (engine steps incl. their sync, result copies, driver math)
         self.t = {"engine": 0.0, "fetch": 0.0, "probe_dots": 0.0, "pheno": 0.0, "submit": 0.0, "driver": 0.0}
 
@@ -517,11 +520,19 @@ class Runner:
         if self.pipelined:
             if self._launched:
                 self.ctx.engine_finish()
-            self._launched, _ = self.ctx.engine_launch()
+            try:
+                self._launched, _ = self.ctx.engine_launch()
+            except Exception:
+                # queued columns found every column holding a result: resume every ready fit (they
+                # consume their results) and try once more
+                if not self._resume_all_ready():
+                    raise
+                self._launched, _ = self.ctx.engine_launch()
         else:
             self.ctx.engine_run(1)
         ids = self.ctx.engine_poll()
-        self.t["engine"] += time.perf_counter() - t0
+        t1 = time.perf_counter()
+        self.t["engine"] += t1 - t0
         if self.pipelined and not self._launched and len(ids) == 0:
             stuck = [j.jid for j in self.jobs.values()
                      if j.waiting is not None and not all(i in self.done for i in j.waiting[1])]
@@ -533,12 +544,44 @@ class Runner:
                 continue
             self.done.add(rid)
             self.inflight_columns -= 1
+        self._steps += 1
+        ready = []
+        for j in self.jobs.values():
+            if j.waiting is not None and all(i in self.done for i in j.waiting[1]):
+                if j.ready_at is None:
+                    j.ready_at = self._steps
+                ready.append(j)
+        ready.sort(key=lambda j: (j.ready_at, j.jid))
+        # While a step runs, resume fits for about as long as the previous step took on the GPU and
+        # leave the rest for the next one: fits that started together reach their stage changes
+        # together, and doing all that host work at once would leave the GPU idle.
+        budget = self._host_budget() if (self.pipelined and self._launched) else None
+        for k, job in enumerate(ready):
+            if budget is not None and k > 0 and time.perf_counter() - t1 > budget:
+                break
+            (kind, wids), job.waiting = job.waiting, None
+            job.ready_at = None
+            self._advance(job, self._resolve(job, kind, wids))
+        return len(ids)
+
+    def _resume_all_ready(self):
         ready = [j for j in self.jobs.values()
                  if j.waiting is not None and all(i in self.done for i in j.waiting[1])]
         for job in ready:
             (kind, wids), job.waiting = job.waiting, None
+            job.ready_at = None
             self._advance(job, self._resolve(job, kind, wids))
-        return len(ids)
+        return bool(ready)
+
+    def _host_budget(self):
+        """GPU seconds of the last finished step (None when the engine does not time its steps)."""
+        timing = getattr(self.ctx, "engine_timing", None)
+        if timing is None:
+            return None
+        total = timing()["step_ms"]
+        last = total - self._gpu_ms
+        self._gpu_ms = total
+        return max(last, 0.0) * 1e-3 if last > 0 else None
 
     def run(self, max_steps=1 << 30):
         steps = 0

@@ -177,6 +177,34 @@ def test_pipelined_runner_matches_synchronous_runner():
         assert a["iterations"] == b["iterations"]
 
 
+def test_pipelined_runner_with_a_tiny_host_budget():
+    """A GPU step that takes no time leaves the host a budget of one fit per step: the deferred
+    fits resume on later steps and every result is unchanged."""
+    grm, g = _cohort(29)
+    gv = synth.genetic_value_from_codes(g.codes, 8)
+    specs = []
+    for k, trait in enumerate(("binary", "quantitative", "binary", "quantitative")):
+        y, C = synth.simulate_pheno(gv, 40 + k, trait, tau=0.5, prevalence=0.3, h2=0.5)
+        specs.append(serve.FitSpec(prep.make_fit0(y, C, trait, True), trait))
+    ref, _ = serve.fit_batch(FakeEngine(grm), specs)
+
+    class Timed(FakeAsyncEngine):
+        ms = 0.0
+
+        def engine_finish(self):
+            self.ms += 1e-9
+            return super().engine_finish()
+
+        def engine_timing(self):
+            return {"step_ms": self.ms}
+
+    eng = Timed(grm)
+    res, _ = serve.fit_batch(eng, specs, pipelined=True)
+    for a, b in zip(res, ref):
+        assert not isinstance(a, Exception), a
+        np.testing.assert_array_equal(a["theta"], b["theta"])
+
+
 def test_pipelined_runner_reports_a_stall():
     grm, g = _cohort(23)
     gv = synth.genetic_value_from_codes(g.codes, 6)
