@@ -5,18 +5,22 @@ N = 100,000 samples x M = 150,000 markers synthetic cohort (p ~ U(0.01,0.5),
 HWE genotypes, 2% missing; seed 1003), GRM built once on the GPU (decode ->
 BF16 standardised genotypes -> tcgen05 SYRK, FP32 K resident in HBM).  One
 step = one batch of P null-model fits run to convergence through the batched
-engine: half binary (prevalence U(0.05,0.3)), half quantitative (h2
-U(0.1,0.6)), each with a sample mask dropping U(5%,40%) of the cohort, 2
-covariates, y + 30 Rademacher probes per trace, split-TF32 tcgen05 GRM.V with
-FP64 PCG recurrences.
+engine: P = 64 phenotypes, half binary (prevalence U(0.05,0.3)), half
+quantitative (h2 U(0.1,0.6)), each with a sample mask dropping U(5%,40%) of the
+cohort, 2 covariates, y + 30 Rademacher probes per trace, split-BF16 tcgen05
+GRM.V (--mode) with FP64 PCG recurrences; the driver overlaps its host work with
+the next engine step (--blocking-runner turns that off).
 
 value  = fits/hr over the device-busy time of the engine steps (CUDA events on
          the engine stream), i.e. with the inputs resident in HBM;
 e2e    = fits/hr by wall clock through the C ABI with host buffers (phenotype
          vectors H2D, solutions D2H every step);
 roofline: the dominant kernel (the tcgen05 GRM.V) -- algorithmic bytes per
-         pass over the split GRM (8 B per stored element + 12 B per RHS entry)
-         or its tensor FLOPs, whichever bounds it, over its event-timed duration;
+         pass over the split GRM (4 B per stored element for BF16 halves, 8 B
+         for TF32 halves, + 8-12 B per RHS entry) or its tensor FLOPs (three
+         products), whichever bounds it, over its event-timed duration;
+reference_gpu_algorithm: the reference's K.x (two cuBLAS SGEMV over the FP32
+         N x M genotype matrix, one RHS) timed on the same GPU, extrapolated;
 cpu_baseline: the reference's CPU GRM.x (oracle/cpu_ref.c, OpenMP, all host
          cores) timed on a bounded sample, extrapolated to fits/hr with the
          measured PCG iterations per fit;
@@ -54,7 +58,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=100_000)
     ap.add_argument("--m", type=int, default=150_000)
-    ap.add_argument("--phenos", type=int, default=32)
+    ap.add_argument("--phenos", type=int, default=64)
     ap.add_argument("--miss", type=float, default=0.02)
     ap.add_argument("--seed", type=int, default=1003)
     ap.add_argument("--mode", default="bf16x3", choices=["bf16x3", "tf32x3", "tf32", "fp32"])
