@@ -109,6 +109,7 @@ struct sg_ctx {
   float* d_Klo = nullptr;   // K - tf32(K) while the split-TF32 engine is selected (d_K then holds tf32(K))
   bool k_split = false;
   int num_sms = 152;
+  int diag_frac_bits = 32;  // fixed-point scale of the high-precision diagonal
   void* d_Kb = nullptr;     // BF16 high (first n_p^2) and low halves of K for SG_MV_BF16X3_TC
   double* d_diag = nullptr;
   float* d_diag32 = nullptr;
@@ -366,6 +367,19 @@ static void free_geno(sg_ctx* c) {
   c->have_grm = false;
 }
 
+// Fractional bits of the fixed-point diagonal: the largest F with m_qc * max z^2 * 2^F below
+// 2^64 (a 1% margin), so no sample's sum can overflow.  z = (g - 2p) / sd per the LUT.
+static int diag_frac_bits(const sg_ctx* c) {
+  double zmax2 = 0.0;
+  for (size_t j = 0; j < c->freq.size(); ++j) {
+    const double p2 = 2.0 * (double)c->freq[j], s = (double)c->invstd[j];
+    for (double g : {0.0, 1.0, 2.0}) zmax2 = std::max(zmax2, (g - p2) * (g - p2) * s * s);
+  }
+  const double bound = std::max(1.0, (double)c->freq.size() * zmax2 * 1.01);
+  const int f = (int)std::floor(std::log2(18446744073709551615.0 / bound));
+  return std::max(0, std::min(f, 62));
+}
+
 // raw: device .bed body re-pitched (m_bim rows of raw_pitch bytes, zero padded)
 static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_t n_fam,
                         int64_t m_bim, const int32_t* sub_1based, int64_t n_sub,
@@ -468,9 +482,13 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
   // GRM diagonal from the packed genotypes
   SG_TRY(dev_alloc_t(c, &c->d_diag, (size_t)std::max<int64_t>(nn, 1)));
   SG_TRY(dev_alloc_t(c, &c->d_diag32, (size_t)std::max<int64_t>(nn, 1)));
+  c->diag_frac_bits = diag_frac_bits(c);
+  unsigned long long* lutq = nullptr;
+  SG_TRY(dev_alloc_t(c, &lutq, (size_t)std::max<int64_t>(4 * c->m_qc, 4)));
   SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
-  launch_diag(c->d_packed, c->pitch, c->d_lut, c->m_qc, nn, c->d_diag, c->d_diag32, c->stream);
-  SG_LAUNCHED(c, 1);
+  launch_diag(c->d_packed, c->pitch, c->d_lut, c->m_qc, nn, c->diag_frac_bits, lutq, c->d_diag,
+              c->d_diag32, c->stream);
+  SG_LAUNCHED(c, 2);
   SG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
   c->diag.resize(nn);
   c->diag32.resize(nn);
@@ -479,6 +497,7 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
     SG_CUDA(c, cudaMemcpyAsync(c->diag32.data(), c->d_diag32, nn * 4, cudaMemcpyDeviceToHost, c->stream));
   }
   SG_TRY(sync(c));
+  dev_free(c, lutq);
   c->t_build[2] = ev_ms(c->tev[0], c->tev[1]);
   c->have_geno = true;
   return SG_OK;
@@ -1652,15 +1671,19 @@ extern "C" int sg_loco_set(sg_ctx* c, int64_t begin, int64_t end) {
   // the chromosome's diagonal contribution (set_Diagof_StdGeno_LOCO, FIT.cpp:4934-4959)
   double* dj = nullptr;
   float* dj32 = nullptr;
+  unsigned long long* lutq = nullptr;
   SG_TRY(dev_alloc_t(c, &dj, (size_t)c->nn));
   SG_TRY(dev_alloc_t(c, &dj32, (size_t)c->nn));
-  launch_diag(pk, c->pitch, lut, mj, c->nn, dj, dj32, c->stream);
-  SG_LAUNCHED(c, 3);
+  SG_TRY(dev_alloc_t(c, &lutq, (size_t)(4 * mj)));
+  // the cohort's fractional bits bound this subset's sum too
+  launch_diag(pk, c->pitch, lut, mj, c->nn, c->diag_frac_bits, lutq, dj, dj32, c->stream);
+  SG_LAUNCHED(c, 4);
   std::vector<double> h(c->nn);
   SG_CUDA(c, cudaMemcpyAsync(h.data(), dj, c->nn * 8, cudaMemcpyDeviceToHost, c->stream));
   SG_TRY(sync(c));
   dev_free(c, dj);
   dev_free(c, dj32);
+  dev_free(c, lutq);
   c->diag_loco.resize(c->nn);
   for (int64_t i = 0; i < c->nn; ++i) c->diag_loco[i] = c->diag[i] - h[i];
   c->loco_begin = begin;
