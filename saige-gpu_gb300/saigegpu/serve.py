@@ -257,6 +257,7 @@ def loco_generator(spec, fit, n_cohort):
     """Get_Coef_LOCO (FIT.R:40-73) for one phenotype while the engine leaves a chromosome out,
     started from the full fit's tau, alpha and eta (FIT.R:254-297)."""
     fam = family_of("binomial" if spec.trait == "binary" else "gaussian")
+    quant = spec.trait != "binary"
     m = np.ones(n_cohort, bool) if spec.mask is None else spec.mask
     idx = np.nonzero(m)[0]
     f0 = spec.fit0

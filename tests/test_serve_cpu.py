@@ -268,3 +268,36 @@ def test_exact_subset_grouping_and_restore():
     for r, ref in zip(res, refs):
         assert not isinstance(r, Exception), r
         np.testing.assert_allclose(r["theta"], ref["theta"], rtol=1e-9)
+
+
+class FakeLocoEngine(FakeEngine):
+    """FakeEngine whose loco_set swaps in the oracle's leave-one-chromosome-out GRM."""
+
+    def __init__(self, grm, geno):
+        super().__init__(grm)
+        self.full, self.geno = grm, geno
+
+    def loco_set(self, begin, end):
+        self.grm = aireml.loco_grm(self.full, self.geno, begin, end)
+
+    def loco_clear(self):
+        self.grm = self.full
+
+
+def test_loco_generator_matches_oracle():
+    grm, g = _cohort(43, n=200, m=600)
+    gv = synth.genetic_value_from_codes(g.codes, 5)
+    chrom = np.repeat(np.arange(1, 23), -(-grm.m_qc // 22))[:grm.m_qc]
+    ranges = serve.loco_ranges(chrom)
+    for trait in ("binary", "quantitative"):
+        y, C = synth.simulate_pheno(gv, 8, trait, tau=0.6, prevalence=0.3, h2=0.5)
+        f0 = prep.make_fit0(y, C, trait, True)
+        fit = (aireml.glmmkin_binary if trait == "binary" else aireml.glmmkin_quantitative)(grm, f0)
+        sel = {c: ranges[c] for c in (3, 17)}
+        got = serve.fit_loco(FakeLocoEngine(grm, g), [serve.FitSpec(f0, trait)], [fit], sel)
+        for c, (b, e) in sel.items():
+            ref = aireml.get_coef_loco(aireml.loco_grm(grm, g, b, e), f0, fit, trait)
+            r = got[c][0]
+            assert not isinstance(r, Exception), r
+            np.testing.assert_allclose(r["coefficients"], ref["alpha"], rtol=1e-9)
+            np.testing.assert_allclose(r["linear_predictors"], ref["eta"], rtol=1e-9, atol=1e-12)
