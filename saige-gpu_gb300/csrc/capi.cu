@@ -60,6 +60,8 @@ struct Engine {
   bool hold = false;              // keep finished results on the device until fetched/consumed
   uint64_t io_h2d = 0, io_d2h = 0;  // bytes through the engine API since the last timing reset
   ColState* h_pin = nullptr;      // pinned mirror for the asynchronous state read-back of a step
+  int32_t* h_gcols = nullptr;     // pinned: active columns gathered for the split-BF16 GRM.V
+  int32_t* d_gcols = nullptr;
   bool inflight = false;          // a launched step has not been finished yet
   int64_t inflight_ncols = 0, inflight_occupied = 0, inflight_hi = 0;
   std::vector<int64_t> pending_release;  // columns freed on the host, reset on the device at the next launch
@@ -277,6 +279,7 @@ extern "C" void sg_ctx_destroy(sg_ctx* c) {
   cudaStreamSynchronize(c->stream);
   cudaStreamSynchronize(c->side);
   if (c->eng.h_pin) cudaFreeHost(c->eng.h_pin);
+  if (c->eng.h_gcols) cudaFreeHost(c->eng.h_gcols);
   for (auto& kv : c->allocs) cudaFree(kv.first);
   c->allocs.clear();
   cudaStreamDestroy(c->side);
@@ -841,6 +844,9 @@ static void engine_free(sg_ctx* c) {
   e.pending_release.clear();
   if (e.h_pin) cudaFreeHost(e.h_pin);
   e.h_pin = nullptr;
+  if (e.h_gcols) cudaFreeHost(e.h_gcols);
+  e.h_gcols = nullptr;
+  dev_free_t(c, e.d_gcols);
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
   e.finished.clear();
@@ -927,6 +933,8 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   for (auto& ev : e.ev)
     if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
+  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_gcols), max_columns * sizeof(int32_t), cudaHostAllocDefault));
+  SG_TRY(dev_alloc_t(c, &e.d_gcols, (size_t)max_columns));
   e.h_st.assign(max_columns, ColState{});
   for (auto& s : e.h_st) { s.kind = -1; s.active = 0; }
   SG_CUDA(c, cudaMemcpyAsync(e.d_st, e.h_st.data(), max_columns * sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
@@ -1103,17 +1111,20 @@ static int engine_admit(sg_ctx* c) {
 }
 
 static int loco_correct(sg_ctx* c, int64_t ncols, bool yf);
-static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf);
+static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf, int64_t* launched);
 
-static int engine_gemm(sg_ctx* c, int64_t ncols, bool* used_yf) {
-  SG_TRY(engine_gemm_full(c, ncols, used_yf));
+// GRM product of the step: Y = K P for the columns in [0, ncols); *launched = the columns the
+// tensor-core kernel computed (the active ones, compacted and padded, in the split-BF16 engine).
+static int engine_gemm(sg_ctx* c, int64_t ncols, bool* used_yf, int64_t* launched) {
+  SG_TRY(engine_gemm_full(c, ncols, used_yf, launched));
   if (c->loco) SG_TRY(loco_correct(c, ncols, *used_yf));
   return SG_OK;
 }
 
-static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf) {
+static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf, int64_t* launched) {
   Engine& e = c->eng;
   *used_yf = true;
+  *launched = ncols;
   if (c->mv_mode == SG_MV_FP64_PLAIN) {
     *used_yf = false;
     if (!e.Yd) SG_TRY(dev_alloc_t(c, &e.Yd, (size_t)(e.cap_cols * e.np)));
@@ -1128,11 +1139,25 @@ static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf) {
     if (!c->d_Kb) SG_TRY(ensure_k_bf16(c, true));
     const size_t half = (size_t)(e.cap_cols * e.np);
     if (!e.Pb) SG_TRY(dev_alloc(c, &e.Pb, half * 4));
+    // only the columns still iterating are multiplied: their P is gathered into a compact block
+    // (padded with zero columns to the tile width) and the epilogue scatters Y back by column
+    int64_t nact = 0;
+    for (int64_t col = 0; col < ncols && col < e.cap_cols; ++col)
+      if (e.h_st[col].active) e.h_gcols[nact++] = (int32_t)col;
+    if (nact == 0) {
+      *launched = 0;
+      return SG_OK;
+    }
+    const int64_t npad = tc_grmv_padded_cols(round_up(nact, 32), e.cap_cols, e.np, true, c->num_sms);
+    for (int64_t j = nact; j < npad; ++j) e.h_gcols[j] = -1;
+    SG_CUDA(c, cudaMemcpyAsync(e.d_gcols, e.h_gcols, npad * 4, cudaMemcpyHostToDevice, c->stream));
     uint16_t* ph = static_cast<uint16_t*>(e.Pb);
-    launch_split_bf16(e.Pf, nullptr, ph, ph + half, ncols * e.np, c->stream);
+    launch_split_bf16_gather(e.Pf, e.np, e.d_gcols, npad, ph, ph + half, c->stream);
     c->launches += 1;
+    *launched = npad;
     const uint16_t* kh = static_cast<const uint16_t*>(c->d_Kb);
-    cudaError_t err = tc_gemm_bf16x3(kh, kh + c->np * c->np, e.np, ph, ph + half, ncols, e.Yf, c->stream, false);
+    cudaError_t err = tc_gemm_bf16x3(kh, kh + c->np * c->np, e.np, ph, ph + half, npad, e.Yf, c->stream, false,
+                                     e.d_gcols);
     if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 GRM.V: %s", cudaGetErrorString(err));
     c->launches += 1;
     return SG_OK;
@@ -1177,12 +1202,14 @@ static int64_t engine_gemm_cols(const sg_ctx* c) {
 // Nothing here waits for the device.
 static int step_launch(sg_ctx* c) {
   Engine& e = c->eng;
-  const int64_t ncols = engine_gemm_cols(c);
+  // the split-BF16 engine compacts the active columns itself; the others cover [0, hi_col) padded
+  const int64_t ncols = c->mv_mode == SG_MV_BF16X3_TC ? round_up(e.hi_col, 32) : engine_gemm_cols(c);
   int64_t occupied = 0;
-  for (int64_t col = 0; col < e.hi_col; ++col) occupied += e.col_req[col] >= 0 ? 1 : 0;
+  for (int64_t col = 0; col < e.hi_col; ++col) occupied += e.h_st[col].active ? 1 : 0;
   bool yf = true;
+  int64_t launched = ncols;
   SG_CUDA(c, cudaEventRecord(e.ev[0], c->stream));
-  SG_TRY(engine_gemm(c, ncols, &yf));
+  SG_TRY(engine_gemm(c, ncols, &yf, &launched));
   SG_CUDA(c, cudaEventRecord(e.ev[1], c->stream));
   const float* Yf = yf ? e.Yf : nullptr;
   const double* Yd = yf ? nullptr : e.Yd;
@@ -1196,7 +1223,7 @@ static int step_launch(sg_ctx* c) {
   SG_CUDA(c, cudaEventRecord(e.ev[2], c->stream));
   SG_CUDA(c, d2h(c, e.h_pin, e.d_st, e.hi_col * sizeof(ColState), c->stream));
   e.inflight = true;
-  e.inflight_ncols = ncols;
+  e.inflight_ncols = launched;
   e.inflight_occupied = occupied;
   e.inflight_hi = e.hi_col;
   return SG_OK;

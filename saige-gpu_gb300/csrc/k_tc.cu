@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(128, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
                const TileCoord* __restrict__ tiles, int num_kb, float* __restrict__ D, int64_t ldd,
-               float scale, int mode, int64_t nrows) {
+               float scale, int mode, int64_t nrows, const int32_t* __restrict__ colmap) {
   static_assert(kC == 1 || (BN / kC) % 8 == 0, "B slices must be whole 8-row swizzle atoms");
   constexpr int kSliceRows = BN / kC;
   constexpr int kSliceBytes = kSliceRows * kRowBytes;
@@ -339,8 +339,16 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
       tmem_ld32(trow + (uint32_t)c0, v);
       const int64_t cbase = (int64_t)tc.bn * BN + c0;
       if (mode == 1) {
+        if (colmap) {  // column j of the tile goes to row colmap[j] of D (skipped when negative)
 #pragma unroll
-        for (int j = 0; j < 32; ++j) D[(cbase + j) * ldd + r] = __uint_as_float(v[j]) * scale;
+          for (int j = 0; j < 32; ++j) {
+            const int32_t dc = __ldg(colmap + cbase + j);
+            if (dc >= 0) D[(int64_t)dc * ldd + r] = __uint_as_float(v[j]) * scale;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) D[(cbase + j) * ldd + r] = __uint_as_float(v[j]) * scale;
+        }
       } else {
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
@@ -403,7 +411,8 @@ constexpr size_t smem_bytes() {
 template <bool kTF32, int BN, int S, bool kSplit, int kC = 1>
 cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
                    const CUtensorMap& b2, const TileCoord* tiles, int ntiles, int num_kb, float* D,
-                   int64_t ldd, float scale, int mode, cudaStream_t s, int64_t nrows) {
+                   int64_t ldd, float scale, int mode, cudaStream_t s, int64_t nrows,
+                   const int32_t* colmap = nullptr) {
   auto k = tc_gemm_kernel<kTF32, BN, S, kSplit, kC>;
   constexpr size_t sm = smem_bytes<kTF32, BN, S, kSplit>();
   static_assert(sm <= 232448, "stage ring exceeds the 227 KB of dynamic shared memory per CTA");
@@ -422,7 +431,7 @@ cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = kC > 1 ? 1 : 0;
-  e = cudaLaunchKernelEx(&cfg, k, a, b, a2, b2, tiles, num_kb, D, ldd, scale, mode, nrows);
+  e = cudaLaunchKernelEx(&cfg, k, a, b, a2, b2, tiles, num_kb, D, ldd, scale, mode, nrows, colmap);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
@@ -507,6 +516,39 @@ __global__ void split_bf16_kernel(const float* __restrict__ x, const float* __re
     hi[i] = h[0];
     lo[i] = l[0];
   }
+}
+
+// Compact BF16 halves of selected columns: column j of (hi, lo) is column cols[j] of x (np rows
+// each), or zeros when cols[j] < 0 (padding up to the GRM.V tile width).
+__global__ void split_bf16_gather_kernel(const float* __restrict__ x, int64_t np, const int32_t* __restrict__ cols,
+                                         __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
+  const int64_t j = blockIdx.y;
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  if (i >= np) return;  // np is a multiple of 128
+  const int32_t c = cols[j];
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (c >= 0) v = *reinterpret_cast<const float4*>(x + (int64_t)c * np + i);
+  const float a[4] = {v.x, v.y, v.z, v.w};
+  __nv_bfloat16 h[4], l[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    h[k] = __float2bfloat16_rn(a[k]);
+    l[k] = isfinite(a[k]) ? __float2bfloat16_rn(a[k] - __bfloat162float(h[k])) : __float2bfloat16_rn(0.0f);
+  }
+  __nv_bfloat162* ho = reinterpret_cast<__nv_bfloat162*>(hi + j * np + i);
+  __nv_bfloat162* lw = reinterpret_cast<__nv_bfloat162*>(lo + j * np + i);
+  ho[0] = __halves2bfloat162(h[0], h[1]);
+  ho[1] = __halves2bfloat162(h[2], h[3]);
+  lw[0] = __halves2bfloat162(l[0], l[1]);
+  lw[1] = __halves2bfloat162(l[2], l[3]);
+}
+
+void launch_split_bf16_gather(const float* x, int64_t np, const int32_t* cols, int64_t ncols, void* hi,
+                              void* lo, cudaStream_t s) {
+  if (ncols == 0) return;
+  dim3 grid((unsigned)((np / 4 + 255) / 256), (unsigned)ncols);
+  split_bf16_gather_kernel<<<grid, 256, 0, s>>>(x, np, cols, static_cast<__nv_bfloat16*>(hi),
+                                                static_cast<__nv_bfloat16*>(lo));
 }
 
 void launch_split_bf16(const float* x, const float* x2, void* hi, void* lo, int64_t n, cudaStream_t s) {
@@ -645,8 +687,8 @@ int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, bool split
 template <bool kTF32, int BN, int S, int C>
 static cudaError_t launch_grmv_split(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
                                      const CUtensorMap& b2, const TileCoord* tiles, int nt, int num_kb,
-                                     float* Y, int64_t np, cudaStream_t s) {
-  return launch<kTF32, BN, S, true, C>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f, 1, s, np);
+                                     float* Y, int64_t np, cudaStream_t s, const int32_t* colmap) {
+  return launch<kTF32, BN, S, true, C>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f, 1, s, np, colmap);
 }
 
 // Split GRM.V over every (BN, cluster) variant.  A stage holds the same bytes for both operand
@@ -654,12 +696,13 @@ static cudaError_t launch_grmv_split(const CUtensorMap& a, const CUtensorMap& b,
 template <bool kTF32>
 static cudaError_t grmv_split_dispatch(int BN, int C, const CUtensorMap& a, const CUtensorMap& b,
                                        const CUtensorMap& a2, const CUtensorMap& b2, const TileCoord* tiles,
-                                       int nt, int num_kb, float* Y, int64_t np, cudaStream_t s) {
-#define SG_GRMV_CASE(BNv, Sv)                                                                             \
-  case BNv:                                                                                               \
-    return C == 4   ? launch_grmv_split<kTF32, BNv, Sv, 4>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s)      \
-           : C == 2 ? launch_grmv_split<kTF32, BNv, Sv, 2>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s)      \
-                    : launch_grmv_split<kTF32, BNv, Sv, 1>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s);
+                                       int nt, int num_kb, float* Y, int64_t np, cudaStream_t s,
+                                       const int32_t* colmap = nullptr) {
+#define SG_GRMV_CASE(BNv, Sv)                                                                                 \
+  case BNv:                                                                                                   \
+    return C == 4   ? launch_grmv_split<kTF32, BNv, Sv, 4>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap) \
+           : C == 2 ? launch_grmv_split<kTF32, BNv, Sv, 2>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap) \
+                    : launch_grmv_split<kTF32, BNv, Sv, 1>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap);
   switch (BN) {
     SG_GRMV_CASE(256, 2)
     SG_GRMV_CASE(224, 2)
@@ -721,7 +764,7 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
 }
 
 cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const void* Ph, const void* Pl,
-                           int64_t ncols, float* Y, cudaStream_t s, bool check) {
+                           int64_t ncols, float* Y, cudaStream_t s, bool check, const int32_t* colmap) {
   if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0 || !Kh || !Kl || !Ph || !Pl)
     return cudaErrorInvalidValue;
   const int BN = tc_gemm_tile_n(ncols, true);
@@ -736,7 +779,8 @@ cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const voi
   cudaError_t e = grmv_tiles(cache, np, ncols, BN, C, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(np / 64);
-  e = grmv_split_dispatch<false>(BN, C, a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np, s);
+  e = grmv_split_dispatch<false>(BN, C, a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np, s,
+                                 colmap);
   if (e != cudaSuccess) return e;
   return check ? check_error_flag(s) : cudaSuccess;
 }

@@ -90,8 +90,13 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
                          const float* Plo, int64_t ncols, float* Y, cudaStream_t s, bool check = true);
 // Y^T = (Kh + Kl)(Ph + Pl)^T without the Kl Pl term, all four BF16 (kind::f16): 16-bit operand
 // significands at the BF16 tensor rate, K in 4 bytes per entry.
+// With colmap, tile column j is written to column colmap[j] of Y (skipped when negative).
 cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const void* Ph, const void* Pl,
-                           int64_t ncols, float* Y, cudaStream_t s, bool check = true);
+                           int64_t ncols, float* Y, cudaStream_t s, bool check = true,
+                           const int32_t* colmap = nullptr);
+// (hi, lo) column j = BF16 halves of column cols[j] of x (np rows, np % 128 == 0), zeros if cols[j] < 0
+void launch_split_bf16_gather(const float* x, int64_t np, const int32_t* cols, int64_t ncols, void* hi,
+                              void* lo, cudaStream_t s);
 // x (+ x2 when not null) = hi + lo, both BF16 (round to nearest even), lo = bf16(x - hi)
 void launch_split_bf16(const float* x, const float* x2, void* hi, void* lo, int64_t n, cudaStream_t s);
 // Synchronises s, then reads and clears the flag the tcgen05 kernels set when a bounded wait ran
