@@ -486,8 +486,8 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
   SG_TRY(dev_alloc_t(c, &c->d_diag, (size_t)std::max<int64_t>(nn, 1)));
   SG_TRY(dev_alloc_t(c, &c->d_diag32, (size_t)std::max<int64_t>(nn, 1)));
   c->diag_frac_bits = diag_frac_bits(c);
-  unsigned long long* lutq = nullptr;
-  SG_TRY(dev_alloc_t(c, &lutq, (size_t)std::max<int64_t>(4 * c->m_qc, 4)));
+  void* lutq = nullptr;  // per-marker tables of the diagonal
+  SG_TRY(dev_alloc(c, &lutq, (size_t)std::max<int64_t>(48 * c->m_qc, 48)));
   SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
   launch_diag(c->d_packed, c->pitch, c->d_lut, c->m_qc, nn, c->diag_frac_bits, lutq, c->d_diag,
               c->d_diag32, c->stream);
@@ -1698,10 +1698,10 @@ extern "C" int sg_loco_set(sg_ctx* c, int64_t begin, int64_t end) {
   // the chromosome's diagonal contribution (set_Diagof_StdGeno_LOCO, FIT.cpp:4934-4959)
   double* dj = nullptr;
   float* dj32 = nullptr;
-  unsigned long long* lutq = nullptr;
+  void* lutq = nullptr;
   SG_TRY(dev_alloc_t(c, &dj, (size_t)c->nn));
   SG_TRY(dev_alloc_t(c, &dj32, (size_t)c->nn));
-  SG_TRY(dev_alloc_t(c, &lutq, (size_t)(4 * mj)));
+  SG_TRY(dev_alloc(c, &lutq, (size_t)(48 * mj)));
   // the cohort's fractional bits bound this subset's sum too
   launch_diag(pk, c->pitch, lut, mj, c->nn, c->diag_frac_bits, lutq, dj, dj32, c->stream);
   SG_LAUNCHED(c, 4);

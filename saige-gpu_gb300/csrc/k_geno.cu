@@ -360,56 +360,71 @@ void launch_loco_combine(float* Yf, double* Yd, const float* V, double a, double
 // GRM diagonal sum_m z^2 (Get_Diagof_StdGeno FIT.cpp:665-704).
 //
 // FP32: markers in order per sample, rounded exactly as the reference's
-// ``m_DiagStd + z % z`` (so the chain is sequential in m).  Beside it the
-// high-precision diagonal is accumulated in unsigned 64-bit fixed point:
-// lutq[4m + g] = round(z^2 * 2^F), with F chosen by the host so that the sum
-// over all markers cannot overflow; integer sums are exact and
-// order-independent, and F ~ 39 at M = 150k keeps each term to 2^-40.
+// ``m_DiagStd + z % z`` (z*z rounded to FP32, then added), so each sample's
+// chain is sequential in m.  Beside it the high-precision diagonal is
+// accumulated in unsigned 64-bit fixed point: lutq[4m + g] = round(z^2 2^F)
+// with F chosen by the host so that no sum can overflow; integer sums are
+// exact and order-independent, and F ~ 39 at M = 150k keeps each term to
+// 2^-40.  Both per-marker tables (z*z in FP32 and the fixed-point square) are
+// built once, so the per-sample loop is two table reads and two adds.
 //
-// Layout: a block owns 128 consecutive bytes of every marker row (512
-// samples, 4 per thread) and streams the rows through shared memory in
-// chunks of 128 markers with cp.async double buffering, so each warp-row
-// read is a full 128-byte line and ~32 KB per block is in flight.
+// Layout: one thread per sample; a block owns 128 consecutive bytes of every
+// marker row (512 samples) and streams the rows and the two tables through
+// shared memory in chunks of 128 markers with cp.async double buffering.
 // ----------------------------------------------------------------------------
-__global__ void diag_lutq_kernel(const float* __restrict__ lut4, int64_t m, double scale,
-                                 unsigned long long* __restrict__ lutq) {
+__global__ void diag_tables_kernel(const float* __restrict__ lut4, int64_t m, double scale,
+                                   unsigned long long* __restrict__ lutq, float* __restrict__ lutsq) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= 4 * m) return;
-  const double z = (double)lut4[j];
-  lutq[j] = __double2ull_rn(z * z * scale);  // z*z is exact in FP64, the scale a power of two
+  const float z = lut4[j];
+  lutsq[j] = __fmul_rn(z, z);
+  const double zd = (double)z;
+  lutq[j] = __double2ull_rn(zd * zd * scale);  // zd*zd is exact in FP64, the scale a power of two
 }
 
-constexpr int kDiagCols = 128;   // byte columns per block (one per thread)
-constexpr int kDiagChunk = 128;  // markers per staged chunk
+constexpr int kDiagBytes = 128;                // byte columns per block
+constexpr int kDiagThreads = 4 * kDiagBytes;   // one sample per thread
+constexpr int kDiagChunk = 128;                // markers per staged chunk
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
   const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(gmem), "r"(src_bytes) : "memory");
 }
 
-__global__ void __launch_bounds__(kDiagCols)
-diag_kernel(const uint8_t* __restrict__ packed, int64_t pitch, const float* __restrict__ lut4,
-            const unsigned long long* __restrict__ lutq, int64_t m_qc, int64_t nn, double inv_scale,
+__global__ void __launch_bounds__(kDiagThreads)
+diag_kernel(const uint8_t* __restrict__ packed, int64_t pitch, const unsigned long long* __restrict__ lutq,
+            const float* __restrict__ lutsq, int64_t m_qc, int64_t nn, double inv_scale,
             double* __restrict__ d64, float* __restrict__ d32) {
-  __shared__ __align__(16) uint8_t tile[2][kDiagChunk][kDiagCols];
+  __shared__ __align__(16) uint8_t tile[2][kDiagChunk][kDiagBytes];        // 32 KB
+  __shared__ __align__(16) float ssq[2][kDiagChunk][4];                    // 4 KB
+  __shared__ __align__(16) unsigned long long sq[2][kDiagChunk][4];        // 8 KB
   const int t = threadIdx.x;
-  const int64_t col0 = (int64_t)blockIdx.x * kDiagCols;
-  // 128 rows x 8 sixteen-byte pieces per chunk, 8 pieces per thread; pieces past the row's pitch
-  // or past the last marker are zero-filled without a global read (src-size 0)
+  const int64_t col0 = (int64_t)blockIdx.x * kDiagBytes;
+  // per chunk: 1024 row pieces + 128 FP32-table pieces + 256 fixed-point-table pieces (16 B each);
+  // pieces past the row's pitch or the last marker are zero-filled without a global read
   auto issue = [&](int buf, int64_t m0) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int idx = t + k * kDiagCols;
-      const int r = idx >> 3, q = idx & 7;
-      const int64_t mk = m0 + r;
-      const int64_t col = col0 + q * 16;
-      const bool ok = mk < m_qc && col + 16 <= pitch;
-      cp_async16(&tile[buf][r][q * 16], ok ? packed + mk * pitch + col : packed, ok ? 16 : 0);
+    for (int idx = t; idx < 1024 + 128 + 256; idx += kDiagThreads) {
+      if (idx < 1024) {
+        const int r = idx >> 3, q = idx & 7;
+        const int64_t mk = m0 + r;
+        const int64_t col = col0 + q * 16;
+        const bool ok = mk < m_qc && col + 16 <= pitch;
+        cp_async16(&tile[buf][r][q * 16], ok ? packed + mk * pitch + col : packed, ok ? 16 : 0);
+      } else if (idx < 1024 + 128) {
+        const int r = idx - 1024;
+        const bool ok = m0 + r < m_qc;
+        cp_async16(&ssq[buf][r][0], ok ? lutsq + 4 * (m0 + r) : lutsq, ok ? 16 : 0);
+      } else {
+        const int e = idx - 1024 - 128, r = e >> 1, h = e & 1;
+        const bool ok = m0 + r < m_qc;
+        cp_async16(&sq[buf][r][2 * h], ok ? lutq + 4 * (m0 + r) + 2 * h : lutq, ok ? 16 : 0);
+      }
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
-  float a32[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-  unsigned long long aq[4] = {0ull, 0ull, 0ull, 0ull};
+  const int byte = t >> 2, sh = 2 * (t & 3);
+  float a32 = 0.0f;
+  unsigned long long aq = 0ull;
   const int64_t nchunks = (m_qc + kDiagChunk - 1) / kDiagChunk;
   if (nchunks > 0) issue(0, 0);
   for (int64_t c = 0; c < nchunks; ++c) {
@@ -423,41 +438,32 @@ diag_kernel(const uint8_t* __restrict__ packed, int64_t pitch, const float* __re
     const int buf = (int)(c & 1);
     const int64_t m0 = c * kDiagChunk;
     const int rows = (int)(m_qc - m0 < kDiagChunk ? m_qc - m0 : kDiagChunk);
+#pragma unroll 4
     for (int r = 0; r < rows; ++r) {
-      const uint32_t byte = tile[buf][r][t];
-      const float4 z = __ldg(reinterpret_cast<const float4*>(lut4) + (m0 + r));
-      const ulonglong2 q01 = __ldg(reinterpret_cast<const ulonglong2*>(lutq) + 2 * (m0 + r));
-      const ulonglong2 q23 = __ldg(reinterpret_cast<const ulonglong2*>(lutq) + 2 * (m0 + r) + 1);
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int g = field_geno((byte >> (2 * j)) & 3u);
-        const float zz = g == 0 ? z.x : (g == 1 ? z.y : z.z);
-        const unsigned long long qq = g == 0 ? q01.x : (g == 1 ? q01.y : q23.x);
-        a32[j] = __fadd_rn(a32[j], __fmul_rn(zz, zz));
-        aq[j] += qq;
-      }
+      const int g = field_geno((tile[buf][r][byte] >> sh) & 3u);
+      a32 = __fadd_rn(a32, ssq[buf][r][g]);
+      aq += sq[buf][r][g];
     }
     __syncthreads();  // the buffer is refilled by the next chunk's copies
   }
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const int64_t i = (col0 + t) * 4 + j;
-    if (i < nn) {
-      d32[i] = a32[j];
-      d64[i] = (double)aq[j] * inv_scale;
-    }
+  const int64_t i = col0 * 4 + t;
+  if (i < nn) {
+    d32[i] = a32;
+    d64[i] = (double)aq * inv_scale;
   }
 }
 
 void launch_diag(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc, int64_t nn,
-                 int frac_bits, unsigned long long* lutq, double* diag64, float* diag32, cudaStream_t s) {
+                 int frac_bits, void* scratch, double* diag64, float* diag32, cudaStream_t s) {
   if (nn == 0) return;
   const double scale = ldexp(1.0, frac_bits);
+  unsigned long long* lutq = static_cast<unsigned long long*>(scratch);
+  float* lutsq = reinterpret_cast<float*>(lutq + 4 * m_qc);
   if (m_qc > 0)
-    diag_lutq_kernel<<<(unsigned)((4 * m_qc + 255) / 256), 256, 0, s>>>(lut4, m_qc, scale, lutq);
+    diag_tables_kernel<<<(unsigned)((4 * m_qc + 255) / 256), 256, 0, s>>>(lut4, m_qc, scale, lutq, lutsq);
   const int64_t nbytes = (nn + 3) / 4;
-  diag_kernel<<<(unsigned)((nbytes + kDiagCols - 1) / kDiagCols), kDiagCols, 0, s>>>(
-      packed, pitch, lut4, lutq, m_qc, nn, 1.0 / scale, diag64, diag32);
+  diag_kernel<<<(unsigned)((nbytes + kDiagBytes - 1) / kDiagBytes), kDiagThreads, 0, s>>>(
+      packed, pitch, lutq, lutsq, m_qc, nn, 1.0 / scale, diag64, diag32);
 }
 
 // One marker unpacked to genotypes and standardised values (Get_OneSNP_Geno / _StdGeno).

@@ -51,9 +51,9 @@ void launch_zbuild_f32(const uint8_t* packed, int64_t pitch, const float* lut4, 
 void launch_zbuild_bf16(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
                         int64_t nn, int64_t np, int64_t mp, void* Zhi, void* Zlo, cudaStream_t s);
 // FP32 diagonal in the reference's marker order and a fixed-point (2^-frac_bits) one beside it;
-// lutq is scratch of 4 * m_qc entries.
+// scratch holds 12 * 4 * m_qc bytes (16-byte aligned).
 void launch_diag(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
-                 int64_t nn, int frac_bits, unsigned long long* lutq, double* diag64, float* diag32,
+                 int64_t nn, int frac_bits, void* scratch, double* diag64, float* diag32,
                  cudaStream_t s);
 void launch_synth_bed(uint64_t seed, int64_t n, int64_t m, uint32_t miss_thr16, uint8_t* out,
                       cudaStream_t s);
