@@ -209,7 +209,11 @@ def grm_roofline(ctx, peaks, t_dev, n, np_, mode="tf32x3", traffic=None):
     kname = "tc_gemm_kernel<%s,split>" % ("bf16" if bf16 else "tf32")
     a_bw = bytes_alg / (ms * 1e-3) / 1e9
     a_tc = flops_tensor / (ms * 1e-3) / 1e12
-    common = {"traffic": traffic, "kernel": kname, "per_launch_ms": round(ms, 3),
+    common = {"traffic": None if traffic is None else round(traffic * bytes_alg),
+              "traffic_basis": None if traffic is None else
+              "ncu DRAM bytes of a N=24576 launch / its algorithmic bytes (%.3f), times this launch's "
+              "algorithmic bytes (profiles/grmv_traffic.json)" % traffic,
+              "kernel": kname, "per_launch_ms": round(ms, 3),
               "columns_per_launch": round(cols, 1), "algorithmic_bytes_per_launch": bytes_alg,
               "tensor_flops_per_launch": flops_tensor}
     if a_bw / hbm >= a_tc / tc_peak:
@@ -406,7 +410,14 @@ def run_ours(args, rank, world, local):
     # probe tables, column states, fetched results and probe reductions
     h2d = int(io_h2d // max(1, args.steps))
     d2h = int(io_d2h // max(1, args.steps))
-    roof = grm_roofline(ctx, peaks, tdev, d["n"], ctx.grm_padded_n(), args.mode)
+    traffic = None
+    try:  # DRAM bytes per launch scaled from a committed ncu capture of a smaller case
+        tr = json.load(open(os.path.join(ROOT, "profiles", "grmv_traffic.json")))
+        if args.mode == "bf16x3":
+            traffic = tr["traffic_over_algorithmic"]
+    except Exception:
+        pass
+    roof = grm_roofline(ctx, peaks, tdev, d["n"], ctx.grm_padded_n(), args.mode, traffic)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "fits/hr", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_wall / args.steps * 1e3, 1),
