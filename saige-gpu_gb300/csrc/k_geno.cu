@@ -236,68 +236,6 @@ __global__ void zbuild_kernel(const uint8_t* __restrict__ packed, int64_t pitch,
   }
 }
 
-// BF16 Z (and its low half) for the tcgen05 SYRK: tile = 128 samples x 256 markers.  Phase 1
-// decodes into a shared-memory copy of the output tile (a warp handles 32 consecutive markers of
-// one sample row, so the packed-byte reads and the BF16 writes are bank-conflict free); phase 2
-// streams it out in 16-byte stores, a warp writing 512 contiguous bytes of one row of Z.
-constexpr int kZbSamples = 128;
-constexpr int kZbMarkers = 256;
-
-__global__ void __launch_bounds__(256)
-zbuild_bf16_wide_kernel(const uint8_t* __restrict__ packed, int64_t pitch, const float* __restrict__ lut4,
-                        int64_t m_qc, int64_t nn, int64_t mp, __nv_bfloat16* __restrict__ Zhi,
-                        __nv_bfloat16* __restrict__ Zlo) {
-  __shared__ uint32_t sb[kZbMarkers][9];  // 256 markers x 32 bytes (128 samples), padded row
-  __shared__ float4 sl[kZbMarkers];
-  extern __shared__ __align__(16) __nv_bfloat16 tile[];  // [2][128][256] (low half if Zlo)
-  const int tid = threadIdx.x;
-  const int64_t m0 = (int64_t)blockIdx.x * kZbMarkers;
-  const int64_t s0 = (int64_t)blockIdx.y * kZbSamples;
-  for (int e = tid; e < kZbMarkers * 8; e += 256) {
-    const int mm = e >> 3, wd = e & 7;
-    const int64_t mk = m0 + mm;
-    const int64_t boff = s0 / 4 + (int64_t)wd * 4;
-    sb[mm][wd] = (mk < m_qc && boff < pitch) ? *reinterpret_cast<const uint32_t*>(packed + mk * pitch + boff) : 0u;
-  }
-  {
-    const int64_t mk = m0 + tid;
-    sl[tid] = mk < m_qc ? reinterpret_cast<const float4*>(lut4)[mk] : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  __syncthreads();
-  // phase 1: thread = one marker column (tid), all 128 samples of the tile
-  {
-    const int mm = tid;
-    const bool mok = m0 + mm < m_qc;
-    const float4 l = sl[mm];
-    for (int r = 0; r < kZbSamples; ++r) {
-      float z = 0.0f;
-      if (mok && s0 + r < nn) {
-        const int g = field_geno((sb[mm][r >> 4] >> (2 * (r & 15))) & 3u);
-        z = g == 0 ? l.x : (g == 1 ? l.y : l.z);
-      }
-      const __nv_bfloat16 h = __float2bfloat16_rn(z);
-      tile[r * kZbMarkers + mm] = h;
-      if (Zlo) tile[kZbSamples * kZbMarkers + r * kZbMarkers + mm] = __float2bfloat16_rn(z - __bfloat162float(h));
-    }
-  }
-  __syncthreads();
-  // phase 2: 128 rows x 32 sixteen-byte pieces per half, 16 pieces per thread
-  const int halves = Zlo ? 2 : 1;
-  for (int hf = 0; hf < halves; ++hf) {
-    __nv_bfloat16* dst = hf == 0 ? Zhi : Zlo;
-    const __nv_bfloat16* src = tile + hf * kZbSamples * kZbMarkers;
-#pragma unroll 4
-    for (int k = 0; k < 16; ++k) {
-      const int idx = tid + k * 256;
-      const int r = idx >> 5, q = idx & 31;
-      const int64_t mk = m0 + q * 8;
-      if (mk >= mp) continue;  // mp is a multiple of 64: a piece is wholly inside or outside
-      *reinterpret_cast<uint4*>(dst + (s0 + r) * mp + mk) =
-          *reinterpret_cast<const uint4*>(src + r * kZbMarkers + q * 8);
-    }
-  }
-}
-
 void launch_zbuild_f32(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
                        int64_t nn, int64_t np, int64_t mp, float* Z, cudaStream_t s) {
   dim3 grid((unsigned)(mp / 64), (unsigned)(np / 128));
@@ -305,16 +243,9 @@ void launch_zbuild_f32(const uint8_t* packed, int64_t pitch, const float* lut4, 
 }
 void launch_zbuild_bf16(const uint8_t* packed, int64_t pitch, const float* lut4, int64_t m_qc,
                         int64_t nn, int64_t np, int64_t mp, void* Zhi, void* Zlo, cudaStream_t s) {
-  const size_t smem = (size_t)(Zlo ? 2 : 1) * kZbSamples * kZbMarkers * sizeof(__nv_bfloat16);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(zbuild_bf16_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(2 * kZbSamples * kZbMarkers * sizeof(__nv_bfloat16)));
-    attr_set = true;
-  }
-  dim3 grid((unsigned)((mp + kZbMarkers - 1) / kZbMarkers), (unsigned)(np / kZbSamples));
-  zbuild_bf16_wide_kernel<<<grid, 256, smem, s>>>(packed, pitch, lut4, m_qc, nn, mp, (__nv_bfloat16*)Zhi,
-                                                  (__nv_bfloat16*)Zlo);
+  dim3 grid((unsigned)(mp / 64), (unsigned)(np / 128));
+  zbuild_kernel<__nv_bfloat16><<<grid, 256, 0, s>>>(packed, pitch, lut4, m_qc, nn, mp,
+                                                   (__nv_bfloat16*)Zhi, (__nv_bfloat16*)Zlo);
 }
 
 // Marker-major standardised genotypes Zm (m_rows x np, samples contiguous), zero past nn and for
