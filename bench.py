@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster-shape autotuner")
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="skip timing the reference's two-SGEMV K.x algorithm on this GPU")
+    ap.add_argument("--workers", type=int, default=None,
+                    help="host threads running the fits' driver math (default: half the cores, at most 8)")
     ap.add_argument("--blocking-runner", action="store_true",
                     help="step the engine synchronously instead of overlapping the driver with the next step")
     ap.add_argument("--serve-requests", type=int, default=32,
@@ -178,10 +180,10 @@ def make_specs(ctx, args, rng_seed):
     return specs
 
 
-def run_batch(ctx, specs, cols, pipelined=True):
+def run_batch(ctx, specs, cols, pipelined=True, workers=None):
     from saigegpu import serve
     t0 = time.perf_counter()
-    res, jobs = serve.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined)
+    res, jobs = serve.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined, workers=workers)
     wall = time.perf_counter() - t0
     errs = [r for r in res if isinstance(r, Exception)]
     if errs:
@@ -247,7 +249,7 @@ def serving_block(ctx, args, cols):
         arrivals.append((t, serve.FitSpec(f0, trait, mask=mask)))
     t0 = time.perf_counter()
     done = serve.serve(ctx, arrivals, max_columns=cols, max_phenos=max(4, args.phenos),
-                       pipelined=not args.blocking_runner)
+                       pipelined=not args.blocking_runner, workers=args.workers)
     wall = time.perf_counter() - t0
     lat = sorted(j.t_done - j.t_arrive for j in done)
     ok = sum(1 for j in done if j.error is None)
@@ -376,7 +378,7 @@ def run_ours(args, rank, world, local):
     cols = _serve.columns_for(specs)
     setup_s = time.perf_counter() - t_setup
     for _ in range(args.warmup):
-        run_batch(ctx, specs, cols, not args.blocking_runner)
+        run_batch(ctx, specs, cols, not args.blocking_runner, args.workers)
     L0 = ctx.kernel_launches()
     ctx.engine_reset_timing()
     barrier(world)
@@ -384,7 +386,7 @@ def run_ours(args, rank, world, local):
     walls, jobs_all, res_all, host_t = [], [], [], {}
     with Clocks(local) as clk:
         for _ in range(args.steps):
-            res, jobs, wall = run_batch(ctx, specs, cols, not args.blocking_runner)
+            res, jobs, wall = run_batch(ctx, specs, cols, not args.blocking_runner, args.workers)
             walls.append(wall)
             jobs_all += jobs
             res_all += res
@@ -429,7 +431,9 @@ def run_ours(args, rank, world, local):
                    "sample_masks": "drop U(5%,40%)", "probes": 30, "grm": "BF16 tcgen05 SYRK, FP32 K",
                    "grm_v": args.mode, "l2": "inputs larger than L2 (GRM %.0f GB)" % (4.0 * ctx.n ** 2 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "value_basis": "device-busy time of engine steps (CUDA events)"},
+                   "value_basis": "device-busy time of engine steps (CUDA events)",
+                   "runner": "blocking" if args.blocking_runner else "pipelined",
+                   "driver_threads": args.workers if args.workers is not None else min(8, (os.cpu_count() or 2) // 2)},
         "e2e": {"value": round(e2e, 2), "unit": "fits/hr", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "latency_s": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3)},
         "gpu_launches": int(launches),

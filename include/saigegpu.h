@@ -62,6 +62,10 @@ enum sg_matvec_mode {
 /* ------------------------------------------------------------ context */
 int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx **out);
 void sg_ctx_destroy(sg_ctx *ctx);
+/* Make the context's GPU current on the calling host thread; a caller that drives one context
+ * from several threads (calls serialised by the caller) does this once per thread.  No reference
+ * counterpart (the reference is single-threaded at this boundary). */
+int sg_ctx_make_current(sg_ctx *ctx);
 const char *sg_last_error(const sg_ctx *ctx);
 int sg_device_bytes_in_use(const sg_ctx *ctx, uint64_t *bytes);
 int sg_set_matvec_mode(sg_ctx *ctx, int mode);

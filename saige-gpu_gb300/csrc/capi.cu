@@ -317,6 +317,12 @@ extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
   return ensure_k_bf16(c, mode == SG_MV_BF16X3_TC);
 }
 
+extern "C" int sg_ctx_make_current(sg_ctx* c) {
+  if (!c) return SG_ERR_INVALID;
+  SG_CUDA(c, cudaSetDevice(c->device));
+  return SG_OK;
+}
+
 extern "C" int sg_selftest_wait_timeout(sg_ctx* c, double budget_ms) {
   if (!c) return SG_ERR_INVALID;
   if (budget_ms <= 0 || budget_ms > 2000) return set_err(c, SG_ERR_INVALID, "budget must be in (0, 2000] ms");

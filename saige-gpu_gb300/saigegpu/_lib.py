@@ -33,6 +33,7 @@ SIGNATURES = {
     "sg_device_bytes_in_use": [c_ctx, P_u64],
     "sg_set_matvec_mode": [c_ctx, C.c_int],
     "sg_kernel_launches": [c_ctx, P_u64],
+    "sg_ctx_make_current": [c_ctx],
     "sg_set_tc_clusters": [c_ctx, C.c_int, C.c_int],
     "sg_selftest_wait_timeout": [c_ctx, C.c_double],
     "sg_get_tc_clusters": [c_ctx, P_i32, P_i32],

@@ -83,6 +83,10 @@ class Context:
         self._call("sg_kernel_launches", C.byref(v))
         return v.value
 
+    def make_current(self):
+        """Make this context's GPU current on the calling thread (worker threads of a runner)."""
+        self._call("sg_ctx_make_current")
+
     def set_tc_clusters(self, syrk, grmv):
         self._call("sg_set_tc_clusters", int(syrk), int(grmv))
 

@@ -29,6 +29,9 @@ cohort GRM restricted to S.  The reference instead recomputes allele
 frequencies (and QC, imputation, standardisation) on each subset;
 ``fit_batch_exact_subsets`` does that, one GRM build per distinct subset.
 """
+import concurrent.futures
+import os
+import threading
 import time
 
 import numpy as np
@@ -335,7 +338,10 @@ def fit_loco(ctx, specs, fits, ranges, max_columns=1024):
                 r.jobs[jid] = job
                 r._advance(job, None)
                 ids.append(jid)
-            r.run()
+            try:
+                r.run()
+            finally:
+                r.close()
             by = {j.jid: j for j in r.finished}
             out[c] = [by[i].result if by[i].error is None else by[i].error for i in ids]
         finally:
@@ -365,7 +371,7 @@ class Runner:
     """Continuous batching of many null-model fits over one engine."""
 
     def __init__(self, ctx, max_columns=2048, max_phenos=64, min_columns_per_fit=2 * (30 + 10) + 8,
-                 pipelined=True):
+                 pipelined=True, workers=None):
         if max_columns < min_columns_per_fit:
             # a fit's trace stage keeps ~2 (nrun + 10) + 4 columns in flight at once
             raise ValueError("max_columns=%d is below one fit's working set (%d)" % (max_columns, min_columns_per_fit))
@@ -389,6 +395,13 @@ class Runner:
         self._launched = False
         self._steps = 0
         self._gpu_ms = 0.0
+        self._lock = threading.RLock()
+        # host threads that run the fits' driver math while the main thread steps the engine
+        self.workers = max(1, int(workers if workers is not None else min(8, (os.cpu_count() or 2) // 2)))
+        self._pool = None
+        if self.workers > 1:
+            init = getattr(ctx, "make_current", None)
+            self._pool = concurrent.futures.ThreadPoolExecutor(self.workers, initializer=init)
         # wall-clock seconds by activity (engine steps incl. their sync, result copies, driver math)
         self.t = {"engine": 0.0, "fetch": 0.0, "probe_dots": 0.0, "pheno": 0.0, "submit": 0.0, "driver": 0.0}
 
@@ -416,76 +429,93 @@ class Runner:
 
     # -- generator plumbing
     def _advance(self, job, value):
+        """Run a fit's generator until it waits for columns or ends.  The generator's own numpy
+        work runs outside the lock (worker threads overlap it); every engine call and every
+        change to the runner's bookkeeping happens under it."""
         gen = job.gen
         clock = time.perf_counter
         try:
             while True:
                 t0 = clock()
                 op = gen.send(value)
-                t1 = clock()
-                self.t["driver"] += t1 - t0
-                kind = op[0]
-                if kind == "pheno":
-                    _, W, tau = op
-                    self.ctx.engine_set_pheno(job.slot, W, tau, job.spec.mask)
-                    value = None
-                    self.t["pheno"] += clock() - t1
-                elif kind == "submit":
-                    _, k, B, probe, maxiter, tol = op
-                    if probe is None:
-                        ids = self.ctx.engine_submit(job.slot, k, B, maxiter, tol)
-                    else:
-                        seed, run0, cnt = probe
-                        ids = self.ctx.engine_submit_probes(job.slot, k, seed, run0, cnt, maxiter, tol)
-                    self.t["submit"] += clock() - t1
-                    for i in ids:
-                        self.owner[int(i)] = job.jid
-                    job.columns += len(ids)
-                    self.inflight_columns += len(ids)
-                    value = [int(i) for i in ids]
-                elif kind in ("wait", "wait_ids"):
-                    ids = op[1]
-                    if all(i in self.done for i in ids):
-                        value = self._resolve(job, kind, ids)
-                        continue
-                    job.waiting = (kind, ids)
-                    return
-                elif kind == "probe_products":
-                    _, seed, run0, cnt = op
-                    value = [-1] * cnt
-                    j = 0
-                    while j < cnt:  # submit maximal runs of uncached probes as blocks
-                        if self.ctx.engine_probe_cached(job.slot, seed, run0 + j):
-                            j += 1
-                            continue
-                        j1 = j
-                        while j1 < cnt and not self.ctx.engine_probe_cached(job.slot, seed, run0 + j1):
-                            j1 += 1
-                        ids = self.ctx.engine_submit_probes(job.slot, 1, seed, run0 + j, j1 - j, 1, 0.0)
-                        for q, i in enumerate(ids):
-                            value[j + q] = int(i)
-                            self.owner[int(i)] = job.jid
-                        job.columns += len(ids)
-                        self.inflight_columns += len(ids)
-                        j = j1
-                    self.t["submit"] += clock() - t1
-                elif kind == "probe_dots":
-                    _, pid, aid, seed, run0, SX = op
-                    D, its = self.ctx.engine_probe_dots(job.slot, pid, aid, seed, run0, SX)
-                    self.t["probe_dots"] += clock() - t1
-                    job.column_iterations += int(np.sum(its)) + sum(1 for a in aid if a >= 0)
-                    for i in list(pid) + [a for a in aid if a >= 0]:
-                        self.done.discard(i)
-                        self.owner.pop(i, None)
-                    value = D
-                else:
-                    raise RuntimeError("unknown op %r" % (kind,))
+                with self._lock:
+                    self.t["driver"] += clock() - t0
+                    value, waiting = self._do_op(job, op)
+                    if waiting:
+                        return
         except StopIteration as st:
-            job.result = st.value
-            self._finish(job)
+            with self._lock:
+                job.result = st.value
+                self._finish(job)
         except Exception as ex:  # the fit failed: release its slot, keep the others running
-            job.error = ex
-            self._finish(job)
+            with self._lock:
+                job.error = ex
+                self._finish(job)
+
+    def _do_op(self, job, op):
+        """One engine request of a generator (lock held); returns (value to send, waiting)."""
+        clock = time.perf_counter
+        t1 = clock()
+        kind = op[0]
+        if kind == "pheno":
+            _, W, tau = op
+            self.ctx.engine_set_pheno(job.slot, W, tau, job.spec.mask)
+            self.t["pheno"] += clock() - t1
+            return None, False
+        if kind == "submit":
+            _, k, B, probe, maxiter, tol = op
+            if probe is None:
+                ids = self.ctx.engine_submit(job.slot, k, B, maxiter, tol)
+            else:
+                seed, run0, cnt = probe
+                ids = self.ctx.engine_submit_probes(job.slot, k, seed, run0, cnt, maxiter, tol)
+            self.t["submit"] += clock() - t1
+            for i in ids:
+                self.owner[int(i)] = job.jid
+            job.columns += len(ids)
+            self.inflight_columns += len(ids)
+            return [int(i) for i in ids], False
+        if kind in ("wait", "wait_ids"):
+            ids = op[1]
+            if all(i in self.done for i in ids):
+                return self._resolve(job, kind, ids), False
+            job.waiting = (kind, ids)
+            return None, True
+        if kind == "probe_products":
+            _, seed, run0, cnt = op
+            value = [-1] * cnt
+            j = 0
+            while j < cnt:  # submit maximal runs of uncached probes as blocks
+                if self.ctx.engine_probe_cached(job.slot, seed, run0 + j):
+                    j += 1
+                    continue
+                j1 = j
+                while j1 < cnt and not self.ctx.engine_probe_cached(job.slot, seed, run0 + j1):
+                    j1 += 1
+                ids = self.ctx.engine_submit_probes(job.slot, 1, seed, run0 + j, j1 - j, 1, 0.0)
+                for q, i in enumerate(ids):
+                    value[j + q] = int(i)
+                    self.owner[int(i)] = job.jid
+                job.columns += len(ids)
+                self.inflight_columns += len(ids)
+                j = j1
+            self.t["submit"] += clock() - t1
+            return value, False
+        if kind == "probe_dots":
+            _, pid, aid, seed, run0, SX = op
+            D, its = self.ctx.engine_probe_dots(job.slot, pid, aid, seed, run0, SX)
+            self.t["probe_dots"] += clock() - t1
+            job.column_iterations += int(np.sum(its)) + sum(1 for a in aid if a >= 0)
+            for i in list(pid) + [a for a in aid if a >= 0]:
+                self.done.discard(i)
+                self.owner.pop(i, None)
+            return D, False
+        raise RuntimeError("unknown op %r" % (kind,))
+
+    def _resume(self, job, kind, wids):
+        with self._lock:
+            value = self._resolve(job, kind, wids)
+        self._advance(job, value)
 
     def _resolve(self, job, kind, ids):
         if kind == "wait_ids":
@@ -557,13 +587,35 @@ class Runner:
         # leave the rest for the next one: fits that started together reach their stage changes
         # together, and doing all that host work at once would leave the GPU idle.
         budget = self._host_budget() if (self.pipelined and self._launched) else None
-        for k, job in enumerate(ready):
-            if budget is not None and k > 0 and time.perf_counter() - t1 > budget:
+        if self._pool is None:
+            for k, job in enumerate(ready):
+                if budget is not None and k > 0 and time.perf_counter() - t1 > budget:
+                    break
+                (kind, wids), job.waiting = job.waiting, None
+                job.ready_at = None
+                self._resume(job, kind, wids)
+            return len(ids)
+        # up to `workers` fits at a time; stop starting new ones once the budget is spent
+        pending, running, started = list(ready), set(), 0
+        while pending or running:
+            while pending and len(running) < self.workers and (
+                    budget is None or started == 0 or time.perf_counter() - t1 <= budget):
+                job = pending.pop(0)
+                (kind, wids), job.waiting = job.waiting, None
+                job.ready_at = None
+                running.add(self._pool.submit(self._resume, job, kind, wids))
+                started += 1
+            if not running:
                 break
-            (kind, wids), job.waiting = job.waiting, None
-            job.ready_at = None
-            self._advance(job, self._resolve(job, kind, wids))
+            finished, running = concurrent.futures.wait(running, return_when=concurrent.futures.FIRST_COMPLETED)
+            for f in finished:
+                f.result()
         return len(ids)
+
+    def close(self):
+        if self._pool is not None:
+            self._pool.shutdown(wait=True)
+            self._pool = None
 
     def _resume_all_ready(self):
         ready = [j for j in self.jobs.values()
@@ -571,7 +623,7 @@ class Runner:
         for job in ready:
             (kind, wids), job.waiting = job.waiting, None
             job.ready_at = None
-            self._advance(job, self._resolve(job, kind, wids))
+            self._resume(job, kind, wids)
         return bool(ready)
 
     def _host_budget(self):
@@ -617,12 +669,15 @@ def columns_for(specs):
     return int(-(-need // 256) * 256)
 
 
-def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True):
+def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True, workers=None):
     """Fit all ``specs`` together; returns their result dicts (or exceptions) in order."""
     max_columns = max(max_columns or 0, columns_for(specs))
-    r = Runner(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined=pipelined)
-    ids = [r.submit(s) for s in specs]
-    r.run()
+    r = Runner(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined=pipelined, workers=workers)
+    try:
+        ids = [r.submit(s) for s in specs]
+        r.run()
+    finally:
+        r.close()
     by = {j.jid: j for j in r.finished}
     jobs = [by[i] for i in ids]
     for j in jobs:
@@ -671,12 +726,13 @@ def fit_batch_exact_subsets(ctx, specs, max_columns=None, max_phenos=None, pipel
     return results, jobs
 
 
-def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter, pipelined=True):
+def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter, pipelined=True,
+          workers=None):
     """Serve a stream of (t_arrival_seconds, FitSpec): admit as slots and columns free up.
 
     Returns the finished jobs (with t_arrive / t_start / t_done) in completion order.
     """
-    r = Runner(ctx, max_columns, max_phenos, pipelined=pipelined)
+    r = Runner(ctx, max_columns, max_phenos, pipelined=pipelined, workers=workers)
     pending = sorted(arrivals, key=lambda a: a[0])
     t0 = clock()
     k = 0
@@ -691,4 +747,5 @@ def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counte
             r.drain()
             time.sleep(max(0.0, min(0.01, pending[k][0] - now)))
     r.drain()
+    r.close()
     return r.finished
