@@ -67,7 +67,7 @@ def parse():
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="skip timing the reference's two-SGEMV K.x algorithm on this GPU")
     ap.add_argument("--workers", type=int, default=None,
-                    help="host threads running the fits' driver math (default: half the cores, at most 8)")
+                    help="host threads running the fits' driver math (default 1)")
     ap.add_argument("--blocking-runner", action="store_true",
                     help="step the engine synchronously instead of overlapping the driver with the next step")
     ap.add_argument("--serve-requests", type=int, default=32,
@@ -433,7 +433,7 @@ def run_ours(args, rank, world, local):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "value_basis": "device-busy time of engine steps (CUDA events)",
                    "runner": "blocking" if args.blocking_runner else "pipelined",
-                   "driver_threads": args.workers if args.workers is not None else min(8, (os.cpu_count() or 2) // 2)},
+                   "driver_threads": args.workers if args.workers is not None else 1},
         "e2e": {"value": round(e2e, 2), "unit": "fits/hr", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "latency_s": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3)},
         "gpu_launches": int(launches),
