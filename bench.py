@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="skip the cluster-shape autotuner")
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="skip timing the reference's two-SGEMV K.x algorithm on this GPU")
+    ap.add_argument("--driver", default="native", choices=["native", "python"],
+                    help="fit driver: C++ (sg_fits_*) or the Python generators of saigegpu.serve")
     ap.add_argument("--workers", type=int, default=None,
                     help="host threads running the fits' driver math (default 1)")
     ap.add_argument("--blocking-runner", action="store_true",
@@ -180,10 +182,13 @@ def make_specs(ctx, args, rng_seed):
     return specs
 
 
-def run_batch(ctx, specs, cols, pipelined=True, workers=None):
-    from saigegpu import serve
+def run_batch(ctx, specs, cols, pipelined=True, workers=None, driver="native"):
+    from saigegpu import native, serve
     t0 = time.perf_counter()
-    res, jobs = serve.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined, workers=workers)
+    if driver == "native":
+        res, jobs = native.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined)
+    else:
+        res, jobs = serve.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined, workers=workers)
     wall = time.perf_counter() - t0
     errs = [r for r in res if isinstance(r, Exception)]
     if errs:
@@ -248,8 +253,13 @@ def serving_block(ctx, args, cols):
         f0 = prep.make_fit0(y[S], C[S], trait, True)
         arrivals.append((t, serve.FitSpec(f0, trait, mask=mask)))
     t0 = time.perf_counter()
-    done = serve.serve(ctx, arrivals, max_columns=cols, max_phenos=max(4, args.phenos),
-                       pipelined=not args.blocking_runner, workers=args.workers)
+    if args.driver == "native":
+        from saigegpu import native
+        done = native.serve(ctx, arrivals, max_columns=cols, max_phenos=max(4, args.phenos),
+                            pipelined=not args.blocking_runner)
+    else:
+        done = serve.serve(ctx, arrivals, max_columns=cols, max_phenos=max(4, args.phenos),
+                           pipelined=not args.blocking_runner, workers=args.workers)
     wall = time.perf_counter() - t0
     lat = sorted(j.t_done - j.t_arrive for j in done)
     ok = sum(1 for j in done if j.error is None)
@@ -378,7 +388,7 @@ def run_ours(args, rank, world, local):
     cols = _serve.columns_for(specs)
     setup_s = time.perf_counter() - t_setup
     for _ in range(args.warmup):
-        run_batch(ctx, specs, cols, not args.blocking_runner, args.workers)
+        run_batch(ctx, specs, cols, not args.blocking_runner, args.workers, args.driver)
     L0 = ctx.kernel_launches()
     ctx.engine_reset_timing()
     barrier(world)
@@ -386,7 +396,7 @@ def run_ours(args, rank, world, local):
     walls, jobs_all, res_all, host_t = [], [], [], {}
     with Clocks(local) as clk:
         for _ in range(args.steps):
-            res, jobs, wall = run_batch(ctx, specs, cols, not args.blocking_runner, args.workers)
+            res, jobs, wall = run_batch(ctx, specs, cols, not args.blocking_runner, args.workers, args.driver)
             walls.append(wall)
             jobs_all += jobs
             res_all += res
@@ -433,6 +443,7 @@ def run_ours(args, rank, world, local):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "value_basis": "device-busy time of engine steps (CUDA events)",
                    "runner": "blocking" if args.blocking_runner else "pipelined",
+                   "driver": args.driver,
                    "driver_threads": args.workers if args.workers is not None else 1},
         "e2e": {"value": round(e2e, 2), "unit": "fits/hr", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "latency_s": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3)},

@@ -303,6 +303,37 @@ int sg_synth_bed_to_host(sg_ctx *ctx, uint8_t *host, uint64_t len);
 /* g = Z b / sqrt(M_qc) with b_m ~ N(0,1) from the counter hash (polygenic signal). */
 int sg_synth_genetic_value(sg_ctx *ctx, uint64_t seed, double *out);
 
+/* ------------------------------------------------------------------ native batched fits
+ * The null-model fit driver (glmmkin.ai_PCG_Rcpp_Binary / _Quantitative, FIT.R:79-549, with
+ * Get_Coef, getCoefficients, getAIScore(_q), GetTrace(_q) and the fitglmmaiRPCG(_q) tau updates,
+ * FIT.cpp:3113-3662) for many phenotypes at once over the engine, in native code.  No reference
+ * counterpart as one call: the reference runs one phenotype per R process.
+ *
+ * sg_fits_create reserves the engine (max_columns, max_fits slots) and holds results on the
+ * device; sg_fits_submit queues a fit (admitted when a slot and its columns are free): trait 0
+ * binary (logit), 1 quantitative; mask is cohort-length (NULL = every sample) and y, X (n_sub x p,
+ * column-major), offset (NULL = 0), eta0 and alpha0 are over the n_sub selected samples, as the R
+ * driver's fit0.  sg_fits_run steps the engine until a fit finishes (or max_steps);
+ * sg_fits_poll lists finished fits; sg_fits_result copies one out (theta 2, alpha p, eta / mu /
+ * Y n_sub, cov p x p) and releases it, returning the fit's own error status if it failed
+ * (message in sg_fits_last_error). */
+typedef struct sg_fits sg_fits;
+int sg_fits_create(sg_ctx *ctx, int64_t max_columns, int64_t max_fits, int pipelined, sg_fits **out);
+void sg_fits_destroy(sg_fits *fits);
+const char *sg_fits_last_error(sg_fits *fits);
+int sg_fits_submit(sg_fits *fits, int trait, int64_t n_sub, const uint8_t *mask, const double *y,
+                   const double *X, int p, const double *offset, const double *eta0, const double *alpha0,
+                   double tol, int maxiter, int nrun, double tol_pcg, int maxiter_pcg, double cv_cutoff,
+                   uint64_t seed, int64_t *fit_id);
+int sg_fits_run(sg_fits *fits, int64_t max_steps, int64_t *n_ready);
+int sg_fits_poll(sg_fits *fits, int64_t *ids, int64_t max_ids, int64_t *n_out);
+int sg_fits_counts(sg_fits *fits, int64_t *active, int64_t *pending, int64_t *done);
+/* t3: seconds in engine steps (launch / finish / poll), seconds of driver work, steps */
+int sg_fits_host_times(sg_fits *fits, double *t3);
+int sg_fits_result(sg_fits *fits, int64_t fit_id, double *theta, double *alpha, double *eta, double *mu,
+                   double *Y, double *cov, int32_t *iterations, int32_t *converged,
+                   int64_t *column_iterations);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,895 @@
+// Native batched null-model fits.
+//
+// The AI-REML driver of glmmkin.ai_PCG_Rcpp_Binary / _Quantitative (FIT.R:79-304, 309-549) with
+// Get_Coef (FIT.R:2-35), getCoefficients (FIT.cpp:3167-3199), getAIScore / getAIScore_q
+// (FIT.cpp:3279-3295, 3479-3531), GetTrace / GetTrace_q (FIT.cpp:3113-3160, 3409-3472) and the tau
+// updates of fitglmmaiRPCG / fitglmmaiRPCG_q (FIT.cpp:3302-3341, 3610-3662), run for many
+// phenotypes at once.  Each fit is a state machine that issues right-hand sides to the
+// continuous-batching engine and waits for them; the scheduler steps the engine (launch the next
+// step, then work on the previous step's results) and resumes the fits whose columns are done.
+// All vector arithmetic here is O(n p) per fit and stage, in FP64, fused into single passes.
+//
+// This file is a client of the engine's own C ABI (sg_engine_*): it holds no device state.
+#include "host_math.h"
+#include "../../include/saigegpu.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <exception>
+#include <map>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+namespace {
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+enum Phase { P_INIT_COEF, P_INIT_AI, P_LOOP_COEF, P_LOOP_AI, P_FINAL_COEF, P_DONE };
+enum Stage { S_NONE, S_GC_WAIT, S_AI_WAIT_APY, S_AI_WAIT_PROBES, S_AI_WAIT_SID };
+
+struct FitError {
+  int code;
+  std::string msg;
+};
+
+struct AiScore {
+  double YPAPY = 0, YPA0PY = 0, tr0 = 0, tr1 = 0;
+  double AI[4] = {0, 0, 0, 0};  // column-major 2x2 (quantitative) or AI[0] (binary)
+};
+
+struct Fit {
+  int64_t id = 0, slot = -1;
+  bool quant = false;
+  int64_t n = 0, ns = 0;
+  int p = 0;
+  std::vector<uint8_t> mask;  // cohort-length, 1 = in the fit's sample subset
+  bool has_mask = false;
+  std::vector<int64_t> idx;   // subset position -> cohort position
+  // inputs over the cohort (0 outside the subset)
+  std::vector<double> y, X, offset;
+  std::vector<double> eta, alpha;  // current eta (with offset) and coefficients of the main loop
+  double tol = 0.02, tol_pcg = 1e-5, cutoff = 0.0025;
+  int maxiter = 20, maxiter_pcg = 500, nrun = 30;
+  uint64_t seed = 200;
+  // main loop
+  Phase phase = P_INIT_COEF;
+  Stage stage = S_NONE;
+  double tau[2] = {1.0, 0.0}, tau0[2] = {1.0, 0.0};
+  std::vector<double> alpha0, eta0;
+  int main_iter = 0, it_used = 0;
+  // Get_Coef
+  double gc_tau[2] = {0, 0};
+  int gc_iter = 0;
+  std::vector<double> gc_alpha0, mu, Y, W;
+  // result of the last Get_Coef
+  std::vector<double> rc_alpha, rc_eta, rc_cov, SY, SX;
+  // getAIScore
+  std::vector<double> ai_cov, PY, APY;
+  int64_t apy_id = -1;
+  std::vector<int64_t> pid, aid, sid;
+  int64_t run0 = 0, k = 0;
+  std::vector<double> t1, t0;
+  // waiting
+  std::vector<int64_t> wait_ids;
+  bool wait_fetch = false;
+  std::vector<std::vector<double>> fetched;
+  // bookkeeping
+  int64_t column_iterations = 0, columns = 0;
+  bool failed = false;
+  FitError err;
+  bool converged = false;
+};
+
+}  // namespace
+
+struct sg_fits {
+  sg_ctx* ctx = nullptr;
+  int64_t n = 0, max_columns = 0, max_fits = 0;
+  bool pipelined = true, launched = false;
+  std::vector<int64_t> free_slots;
+  std::map<int64_t, std::unique_ptr<Fit>> active;   // admitted, running
+  std::deque<std::unique_ptr<Fit>> pending;          // waiting for a slot and columns
+  std::map<int64_t, std::unique_ptr<Fit>> done_fits; // finished, not yet collected
+  std::deque<int64_t> finished_order;
+  std::unordered_map<int64_t, int64_t> owner;        // request id -> fit id
+  std::unordered_set<int64_t> done_reqs;
+  std::deque<int64_t> ready;                          // fits whose awaited columns are all done
+  int64_t next_id = 1, inflight_columns = 0;
+  std::string err;
+  double t_engine = 0, t_host = 0;
+  int64_t steps = 0;
+};
+
+namespace {
+
+int fits_err(sg_fits* F, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  F->err = buf;
+  return code;
+}
+
+int64_t need_columns(const Fit& f) { return 2 * (int64_t)(f.nrun + 10) + 8; }
+
+// --------------------------------------------------------------- vector helpers (cohort length)
+// binomial(logit) / gaussian working vector and weights of Get_Coef (FIT.R:4-8); R's logit
+// thresholds: |eta| > 30 clamps mu.eta to DBL_EPSILON and mu to eps / (1 + eps) or its complement.
+void working(Fit& f, const std::vector<double>& et) {
+  const double eps = 2.220446049250313e-16;
+  f.mu.resize(f.n);
+  f.Y.resize(f.n);
+  f.W.resize(f.n);
+  for (int64_t i = 0; i < f.n; ++i) {
+    const double e = et[i];
+    double mu, mu_eta, var;
+    if (f.quant) {
+      mu = e;
+      mu_eta = 1.0;
+      var = 1.0;
+    } else {
+      const double ex = std::exp(std::min(std::max(e, -30.0), 30.0));
+      const double tmp = e < -30.0 ? eps : (e > 30.0 ? 1.0 / eps : ex);
+      mu = tmp / (1.0 + tmp);
+      mu_eta = (e > 30.0 || e < -30.0) ? eps : ex / ((1.0 + ex) * (1.0 + ex));
+      var = mu * (1.0 - mu);
+    }
+    f.mu[i] = mu;
+    const bool in = f.mask[i] != 0;
+    f.Y[i] = in ? e - f.offset[i] + (f.y[i] - mu) / mu_eta : 0.0;
+    if (f.quant) {
+      f.W[i] = 1.0;
+    } else {
+      const double r = mu_eta / std::sqrt(var);
+      f.W[i] = in ? r * r : 1.0;
+    }
+  }
+}
+
+// A' B for column-major n x a and n x b
+void gram(const double* A, int a, const double* B, int b, int64_t n, double* out) {
+  for (int j = 0; j < b; ++j)
+    for (int i = 0; i < a; ++i) {
+      double s = 0.0;
+      const double* x = A + (int64_t)i * n;
+      const double* z = B + (int64_t)j * n;
+      for (int64_t r = 0; r < n; ++r) s += x[r] * z[r];
+      out[i + j * a] = s;
+    }
+}
+
+double dotn(const double* a, const double* b, int64_t n) {
+  double s = 0.0;
+  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+// out = v - SX (cov (SX' w)): the projection P applied as the reference writes it
+void project(const Fit& f, const std::vector<double>& cov, const double* v, const double* w, double* out) {
+  const int p = f.p;
+  std::vector<double> a(p), b(p, 0.0);
+  gram(f.SX.data(), p, w, 1, f.n, a.data());
+  for (int i = 0; i < p; ++i)
+    for (int j = 0; j < p; ++j) b[i] += cov[i + j * p] * a[j];
+  for (int64_t r = 0; r < f.n; ++r) {
+    double s = 0.0;
+    for (int j = 0; j < p; ++j) s += f.SX[r + (int64_t)j * f.n] * b[j];
+    out[r] = v[r] - s;
+  }
+}
+
+double cal_cv(const std::vector<double>& x) {
+  const double nn = (double)x.size();
+  double m = 0.0;
+  for (double v : x) m += v;
+  m /= nn;
+  double ss = 0.0;
+  for (double v : x) ss += (v - m) * (v - m);
+  const double sd = std::sqrt(ss / (nn - 1.0));
+  return (sd / m) / nn;
+}
+
+// --------------------------------------------------------------- engine requests
+void fail(sg_fits* F, Fit& f, int code, const std::string& msg) {
+  if (!f.failed) {
+    f.failed = true;
+    f.err = FitError{code, msg};
+  }
+}
+
+bool eng_ok(sg_fits* F, Fit& f, int rc) {
+  if (rc == SG_OK) return true;
+  const char* m = sg_last_error(F->ctx);
+  fail(F, f, rc, m ? m : "engine error");
+  return false;
+}
+
+void own(sg_fits* F, Fit& f, const std::vector<int64_t>& ids) {
+  for (int64_t id : ids)
+    if (id >= 0) F->owner[id] = f.id;
+  f.columns += (int64_t)ids.size();
+  F->inflight_columns += (int64_t)ids.size();
+}
+
+bool set_pheno(sg_fits* F, Fit& f, const std::vector<double>& W, const double* tau) {
+  return eng_ok(F, f, sg_engine_set_pheno(F->ctx, f.slot, W.data(), tau, f.has_mask ? f.mask.data() : nullptr));
+}
+
+bool submit(sg_fits* F, Fit& f, int kind, const double* B, int64_t k, int maxiter, double tol,
+            std::vector<int64_t>& ids) {
+  ids.assign(k, -1);
+  if (!eng_ok(F, f, sg_engine_submit(F->ctx, f.slot, kind, B, k, maxiter, tol, ids.data()))) return false;
+  own(F, f, ids);
+  return true;
+}
+
+bool submit_probes(sg_fits* F, Fit& f, int64_t run0, int64_t k, std::vector<int64_t>& ids) {
+  ids.assign(k, -1);
+  if (!eng_ok(F, f, sg_engine_submit_probes(F->ctx, f.slot, 0, f.seed, run0, k, f.maxiter_pcg, f.tol_pcg,
+                                            ids.data())))
+    return false;
+  own(F, f, ids);
+  return true;
+}
+
+// K u of the probes: -1 where the slot's cache holds it (same probes and sample mask all fit
+// long), else maximal runs of uncached probes submitted as product blocks
+bool probe_products(sg_fits* F, Fit& f, int64_t run0, int64_t cnt, std::vector<int64_t>& out) {
+  out.assign(cnt, -1);
+  int64_t j = 0;
+  while (j < cnt) {
+    if (sg_engine_probe_cached(F->ctx, f.slot, f.seed, run0 + j)) {
+      ++j;
+      continue;
+    }
+    int64_t j1 = j;
+    while (j1 < cnt && !sg_engine_probe_cached(F->ctx, f.slot, f.seed, run0 + j1)) ++j1;
+    std::vector<int64_t> ids(j1 - j, -1);
+    if (!eng_ok(F, f, sg_engine_submit_probes(F->ctx, f.slot, 1, f.seed, run0 + j, j1 - j, 1, 0.0, ids.data())))
+      return false;
+    own(F, f, ids);
+    for (int64_t q = 0; q < j1 - j; ++q) out[j + q] = ids[q];
+    j = j1;
+  }
+  return true;
+}
+
+void wait_for(Fit& f, Stage st, std::vector<int64_t> ids, bool fetch) {
+  f.stage = st;
+  f.wait_ids.clear();
+  for (int64_t id : ids)
+    if (id >= 0) f.wait_ids.push_back(id);
+  f.wait_fetch = fetch;
+}
+
+// --------------------------------------------------------------- Get_Coef
+bool gc_issue(sg_fits* F, Fit& f) {
+  if (!set_pheno(F, f, f.W, f.gc_tau)) return false;
+  std::vector<double> B((size_t)f.n * (1 + f.p));
+  std::memcpy(B.data(), f.Y.data(), f.n * sizeof(double));
+  std::memcpy(B.data() + f.n, f.X.data(), (size_t)f.n * f.p * sizeof(double));
+  std::vector<int64_t> ids;
+  if (!submit(F, f, 0, B.data(), 1 + f.p, f.maxiter_pcg, f.tol_pcg, ids)) return false;
+  wait_for(f, S_GC_WAIT, ids, true);
+  return true;
+}
+
+bool gc_begin(sg_fits* F, Fit& f, const double* tau, const std::vector<double>& alpha0,
+              const std::vector<double>& eta0) {
+  f.gc_tau[0] = tau[0];
+  f.gc_tau[1] = tau[1];
+  f.gc_alpha0 = alpha0;
+  f.gc_iter = 0;
+  working(f, eta0);
+  return gc_issue(F, f);
+}
+
+// getCoefficients on the solved [Sigma^-1 Y, Sigma^-1 X]; returns true when Get_Coef is done
+bool gc_step(sg_fits* F, Fit& f, bool* done) {
+  const int p = f.p;
+  const int64_t n = f.n;
+  f.SY = std::move(f.fetched[0]);
+  f.SX.assign((size_t)n * p, 0.0);
+  for (int j = 0; j < p; ++j) std::memcpy(f.SX.data() + (int64_t)j * n, f.fetched[1 + j].data(), n * sizeof(double));
+  std::vector<double> XtSX(p * p);
+  gram(f.X.data(), p, f.SX.data(), p, n, XtSX.data());
+  f.rc_cov = sg::inv_sympd(XtSX, p);
+  std::vector<double> sxy(p);
+  gram(f.SX.data(), p, f.Y.data(), 1, n, sxy.data());
+  std::vector<double> al(p, 0.0);
+  for (int i = 0; i < p; ++i)
+    for (int j = 0; j < p; ++j) al[i] += f.rc_cov[i + j * p] * sxy[j];
+  std::vector<double> et(n);
+  for (int64_t r = 0; r < n; ++r) {
+    double s = 0.0;
+    for (int j = 0; j < p; ++j) s += f.SX[r + (int64_t)j * n] * al[j];
+    et[r] = (f.mask[r] ? f.Y[r] - f.gc_tau[0] * (f.SY[r] - s) / f.W[r] : 0.0) + f.offset[r];
+  }
+  working(f, et);
+  ++f.gc_iter;
+  double dmax = 0.0;
+  for (int i = 0; i < p; ++i)
+    dmax = std::max(dmax, std::fabs(al[i] - f.gc_alpha0[i]) / (std::fabs(al[i]) + std::fabs(f.gc_alpha0[i]) + 0.1));
+  f.rc_alpha = al;
+  f.rc_eta = et;
+  if (dmax < 0.1 || f.gc_iter >= f.maxiter) {
+    *done = true;
+    return true;
+  }
+  f.gc_alpha0 = al;
+  *done = false;
+  return gc_issue(F, f);
+}
+
+// --------------------------------------------------------------- getAIScore
+bool ai_begin(sg_fits* F, Fit& f) {
+  const int p = f.p;
+  const int64_t n = f.n;
+  if (!set_pheno(F, f, f.W, f.tau)) return false;
+  if (f.quant) {
+    std::vector<double> XtSX(p * p);
+    gram(f.X.data(), p, f.SX.data(), p, n, XtSX.data());
+    f.ai_cov = sg::inv_sympd(XtSX, p);
+  } else {
+    f.ai_cov = f.rc_cov;
+  }
+  f.PY.resize(n);
+  project(f, f.ai_cov, f.SY.data(), f.Y.data(), f.PY.data());
+  std::vector<int64_t> a;
+  if (!submit(F, f, 1, f.PY.data(), 1, 1, 0.0, a)) return false;
+  f.apy_id = a[0];
+  if (!submit_probes(F, f, 0, f.nrun, f.pid)) return false;
+  if (!probe_products(F, f, 0, f.nrun, f.aid)) return false;
+  f.run0 = 0;
+  f.k = f.nrun;
+  f.t1.clear();
+  f.t0.clear();
+  wait_for(f, S_AI_WAIT_APY, {f.apy_id}, true);
+  return true;
+}
+
+bool ai_after_apy(sg_fits* F, Fit& f) {
+  f.APY = std::move(f.fetched[0]);
+  std::vector<double> rhs(f.APY);
+  if (f.quant) rhs.insert(rhs.end(), f.PY.begin(), f.PY.end());
+  if (!submit(F, f, 0, rhs.data(), f.quant ? 2 : 1, f.maxiter_pcg, f.tol_pcg, f.sid)) return false;
+  std::vector<int64_t> w(f.pid);
+  w.insert(w.end(), f.aid.begin(), f.aid.end());
+  wait_for(f, S_AI_WAIT_PROBES, w, false);
+  return true;
+}
+
+bool ai_after_probes(sg_fits* F, Fit& f) {
+  const int p = f.p;
+  const int64_t nv = 2 + 2 * p, k = (int64_t)f.pid.size();
+  std::vector<double> D(k * nv);
+  std::vector<int32_t> its(k, 0);
+  if (!eng_ok(F, f, sg_engine_probe_dots(F->ctx, f.slot, f.pid.data(), f.aid.data(), k, f.seed, f.run0,
+                                         f.SX.data(), p, D.data(), its.data())))
+    return false;
+  for (int64_t j = 0; j < k; ++j) {
+    f.column_iterations += its[j] + (f.aid[j] >= 0 ? 1 : 0);
+    F->done_reqs.erase(f.pid[j]);
+    F->owner.erase(f.pid[j]);
+    if (f.aid[j] >= 0) {
+      F->done_reqs.erase(f.aid[j]);
+      F->owner.erase(f.aid[j]);
+    }
+  }
+  for (int64_t j = 0; j < k; ++j) {
+    const double* row = D.data() + j * nv;
+    const double* b = row + 2;
+    const double* c = row + 2 + p;
+    double bcc = 0.0, ccc = 0.0;
+    for (int i = 0; i < p; ++i)
+      for (int q = 0; q < p; ++q) {
+        bcc += b[i] * f.ai_cov[i + q * p] * c[q];
+        ccc += c[i] * f.ai_cov[i + q * p] * c[q];
+      }
+    f.t1.push_back(row[0] - bcc);
+    f.t0.push_back(row[1] - ccc);
+  }
+  if (cal_cv(f.t1) > f.cutoff || (f.quant && cal_cv(f.t0) > f.cutoff)) {
+    f.run0 += f.k;
+    f.k = 10;
+    if (!submit_probes(F, f, f.run0, f.k, f.pid)) return false;
+    if (!probe_products(F, f, f.run0, f.k, f.aid)) return false;
+    std::vector<int64_t> w(f.pid);
+    w.insert(w.end(), f.aid.begin(), f.aid.end());
+    wait_for(f, S_AI_WAIT_PROBES, w, false);
+    return true;
+  }
+  wait_for(f, S_AI_WAIT_SID, f.sid, true);
+  return true;
+}
+
+AiScore ai_finish(Fit& f) {
+  const int64_t n = f.n;
+  AiScore re;
+  std::vector<double> PAPY(n);
+  project(f, f.ai_cov, f.fetched[0].data(), f.fetched[0].data(), PAPY.data());
+  re.YPAPY = dotn(f.PY.data(), f.APY.data(), n);
+  double s1 = 0.0, s0 = 0.0;
+  for (double v : f.t1) s1 += v;
+  for (double v : f.t0) s0 += v;
+  re.tr1 = s1 / (double)f.t1.size();
+  re.tr0 = s0 / (double)f.t0.size();
+  if (f.quant) {
+    std::vector<double> PA0PY(n);
+    project(f, f.ai_cov, f.fetched[1].data(), f.fetched[1].data(), PA0PY.data());
+    re.YPA0PY = dotn(f.PY.data(), f.PY.data(), n);
+    re.AI[0] = dotn(f.PY.data(), PA0PY.data(), n);
+    re.AI[1] = re.AI[2] = dotn(f.PY.data(), PAPY.data(), n);
+    re.AI[3] = dotn(f.APY.data(), PAPY.data(), n);
+  } else {
+    re.AI[0] = dotn(f.APY.data(), PAPY.data(), n);
+  }
+  return re;
+}
+
+// --------------------------------------------------------------- tau updates
+void tau_update(Fit& f, const AiScore& re) {
+  const double tol = f.tol;
+  const double t0[2] = {f.tau[0], f.tau[1]};
+  if (!f.quant) {  // fitglmmaiRPCG
+    const double dtau = (re.YPAPY - re.tr1) / re.AI[0];
+    double t[2] = {t0[0], t0[1] + dtau};
+    for (double& v : t)
+      if (v < tol) v = 0.0;
+    double step = 1.0;
+    while (t[1] < 0.0) {
+      step *= 0.5;
+      t[1] = t0[1] + step * dtau;
+    }
+    for (double& v : t)
+      if (v < tol) v = 0.0;
+    f.tau[0] = t[0];
+    f.tau[1] = t[1];
+    return;
+  }
+  // fitglmmaiRPCG_q: dtau = AI^-1 score (2 x 2, partial pivoting)
+  const bool zero[2] = {t0[0] < tol, t0[1] < tol};
+  const double sc[2] = {re.YPA0PY - re.tr0, re.YPAPY - re.tr1};
+  double a = re.AI[0], b = re.AI[2], c = re.AI[1], d = re.AI[3];  // [[a b] [c d]]
+  double r0 = sc[0], r1 = sc[1];
+  double dt[2];
+  if (std::fabs(c) > std::fabs(a)) {
+    std::swap(a, c);
+    std::swap(b, d);
+    std::swap(r0, r1);
+  }
+  const double l = c / a;
+  const double d2 = d - l * b, r2 = r1 - l * r0;
+  dt[1] = r2 / d2;
+  dt[0] = (r0 - b * dt[1]) / a;
+  double t[2] = {t0[0] + dt[0], t0[1] + dt[1]};
+  for (int i = 0; i < 2; ++i)
+    if (zero[i] && t[i] < tol) t[i] = 0.0;
+  double step = 1.0;
+  while (t[0] < 0.0 || t[1] < 0.0) {
+    step *= 0.5;
+    for (int i = 0; i < 2; ++i) {
+      t[i] = t0[i] + step * dt[i];
+      if (zero[i] && t[i] < tol) t[i] = 0.0;
+    }
+  }
+  for (double& v : t)
+    if (v < tol) v = 0.0;
+  f.tau[0] = t[0];
+  f.tau[1] = t[1];
+}
+
+// --------------------------------------------------------------- main loop (glmmkin.ai_PCG_Rcpp_*)
+bool main_start(sg_fits* F, Fit& f) {
+  f.alpha0 = f.alpha;
+  f.eta0 = f.eta;
+  if (f.quant) {
+    working(f, f.eta);
+    double m = 0.0;
+    for (int64_t i : f.idx) m += f.Y[i];
+    m /= (double)f.ns;
+    double ss = 0.0;
+    for (int64_t i : f.idx) ss += (f.Y[i] - m) * (f.Y[i] - m);
+    if (std::fabs(ss / (double)(f.ns - 1)) < 0.1) {
+      fail(F, f, SG_ERR_NUMERIC, "variance of the phenotype is much smaller than 1");
+      return false;
+    }
+    f.tau[0] = 1.0;
+    f.tau[1] = 0.0;
+  } else {
+    f.tau[0] = 1.0;
+    f.tau[1] = 0.1;
+  }
+  f.tau0[0] = f.tau[0];
+  f.tau0[1] = f.tau[1];
+  f.phase = P_INIT_COEF;
+  return gc_begin(F, f, f.tau, f.alpha0, f.eta0);
+}
+
+bool final_coef(sg_fits* F, Fit& f) {
+  f.phase = P_FINAL_COEF;
+  return gc_begin(F, f, f.tau, f.alpha, f.eta);
+}
+
+bool loop_next(sg_fits* F, Fit& f) {
+  if (f.main_iter >= f.maxiter) return final_coef(F, f);
+  f.main_iter += 1;
+  f.it_used = f.main_iter;
+  f.alpha0 = f.quant ? f.alpha : f.rc_alpha;
+  f.tau0[0] = f.tau[0];
+  f.tau0[1] = f.tau[1];
+  f.eta0 = f.eta;
+  f.phase = P_LOOP_COEF;
+  return gc_begin(F, f, f.tau, f.alpha0, f.eta0);
+}
+
+bool coef_done(sg_fits* F, Fit& f) {
+  switch (f.phase) {
+    case P_INIT_COEF:
+      f.phase = P_INIT_AI;
+      return ai_begin(F, f);
+    case P_LOOP_COEF:
+      f.phase = P_LOOP_AI;
+      return ai_begin(F, f);
+    case P_FINAL_COEF:
+      f.phase = P_DONE;
+      f.stage = S_NONE;
+      f.converged = f.it_used < f.maxiter;
+      return true;
+    default:
+      fail(F, f, SG_ERR_STATE, "fit state machine: Get_Coef finished in an unexpected phase");
+      return false;
+  }
+}
+
+bool ai_done(sg_fits* F, Fit& f, const AiScore& re) {
+  const double n = (double)f.ns;
+  if (f.phase == P_INIT_AI) {  // the first, damped step (FIT.R:165, 405-406)
+    if (f.quant) {
+      f.tau[1] = std::max(0.0, f.tau0[1] + f.tau0[1] * f.tau0[1] * (re.YPAPY - re.tr1) / n);
+      f.tau[0] = std::max(0.0, f.tau0[0] + f.tau0[0] * f.tau0[0] * (re.YPA0PY - re.tr0) / n);
+    } else {
+      f.tau[1] = std::max(0.0, f.tau0[1] + f.tau0[1] * f.tau0[1] * (re.YPAPY - re.tr1) / n);
+    }
+    f.main_iter = 0;
+    f.it_used = 0;
+    return loop_next(F, f);
+  }
+  if (f.phase != P_LOOP_AI) {
+    fail(F, f, SG_ERR_STATE, "fit state machine: AI score finished in an unexpected phase");
+    return false;
+  }
+  tau_update(f, re);
+  f.alpha = f.rc_alpha;
+  f.eta = f.rc_eta;
+  if (f.quant && f.tau[0] <= 0.0) {
+    fail(F, f, SG_ERR_NUMERIC, "the first variance component parameter estimate is 0");
+    return false;
+  }
+  if (f.quant ? f.tau[1] <= 0.0 : f.tau[1] == 0.0) return final_coef(F, f);
+  double rel = 0.0;
+  for (int i = 0; i < 2; ++i)
+    rel = std::max(rel, std::fabs(f.tau[i] - f.tau0[i]) / (std::fabs(f.tau[i]) + std::fabs(f.tau0[i]) + f.tol));
+  if (rel < f.tol) return final_coef(F, f);
+  if (std::max(f.tau[0], f.tau[1]) > 1.0 / (f.tol * f.tol)) {
+    f.it_used = f.maxiter;
+    return final_coef(F, f);
+  }
+  return loop_next(F, f);
+}
+
+// Resume a fit whose awaited columns are done: fetch them if asked, then run its next stage.
+bool resume(sg_fits* F, Fit& f) {
+  f.fetched.clear();
+  if (f.wait_fetch) {
+    for (int64_t id : f.wait_ids) {
+      std::vector<double> x(f.n);
+      int32_t it = 0;
+      if (!eng_ok(F, f, sg_engine_fetch(F->ctx, id, x.data(), &it))) return false;
+      f.column_iterations += it;
+      F->done_reqs.erase(id);
+      F->owner.erase(id);
+      f.fetched.push_back(std::move(x));
+    }
+  }
+  const Stage st = f.stage;
+  f.stage = S_NONE;
+  f.wait_ids.clear();
+  switch (st) {
+    case S_GC_WAIT: {
+      bool done = false;
+      if (!gc_step(F, f, &done)) return false;
+      return done ? coef_done(F, f) : true;
+    }
+    case S_AI_WAIT_APY:
+      return ai_after_apy(F, f);
+    case S_AI_WAIT_PROBES:
+      return ai_after_probes(F, f);
+    case S_AI_WAIT_SID:
+      return ai_done(F, f, ai_finish(f));
+    default:
+      fail(F, f, SG_ERR_STATE, "fit state machine: resumed without a pending wait");
+      return false;
+  }
+}
+
+bool is_ready(const sg_fits* F, const Fit& f) {
+  if (f.stage == S_NONE) return false;
+  for (int64_t id : f.wait_ids)
+    if (!F->done_reqs.count(id)) return false;
+  return true;
+}
+
+// A finished or failed fit: cancel its outstanding requests, free its slot, queue it for polling.
+void retire(sg_fits* F, int64_t fid) {
+  auto it = F->active.find(fid);
+  if (it == F->active.end()) return;
+  std::unique_ptr<Fit> f = std::move(it->second);
+  F->active.erase(it);
+  std::vector<int64_t> mine;
+  for (const auto& kv : F->owner)
+    if (kv.second == fid) mine.push_back(kv.first);
+  for (int64_t id : mine) {
+    sg_engine_cancel(F->ctx, id);
+    F->owner.erase(id);
+    if (!F->done_reqs.erase(id)) F->inflight_columns -= 1;
+  }
+  F->free_slots.push_back(f->slot);
+  F->finished_order.push_back(fid);
+  F->done_fits[fid] = std::move(f);
+}
+
+void admit(sg_fits* F) {
+  while (!F->pending.empty() && !F->free_slots.empty() &&
+         F->inflight_columns + need_columns(*F->pending.front()) <= F->max_columns) {
+    std::unique_ptr<Fit> f = std::move(F->pending.front());
+    F->pending.pop_front();
+    f->slot = F->free_slots.back();
+    F->free_slots.pop_back();
+    sg_engine_probe_cache_clear(F->ctx, f->slot);  // a new sample mask takes this slot
+    const int64_t fid = f->id;
+    Fit& ref = *f;
+    F->active[fid] = std::move(f);
+    const double t = now_s();
+    const bool ok = main_start(F, ref);
+    F->t_host += now_s() - t;
+    if (!ok || ref.failed || ref.phase == P_DONE) retire(F, fid);
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" int sg_fits_create(sg_ctx* ctx, int64_t max_columns, int64_t max_fits, int pipelined, sg_fits** out) {
+  if (!ctx || !out || max_fits <= 0 || max_columns <= 0) return SG_ERR_INVALID;
+  int64_t n = 0, mt = 0, mq = 0, mv = 0;
+  int rc = sg_geno_dims(ctx, &n, &mt, &mq, &mv);
+  if (rc != SG_OK) return rc;
+  rc = sg_engine_reserve(ctx, max_columns, max_fits);
+  if (rc != SG_OK) return rc;
+  rc = sg_engine_hold_results(ctx, 1);  // probe results are reduced on the device, not copied
+  if (rc != SG_OK) return rc;
+  sg_fits* F = new sg_fits();
+  F->ctx = ctx;
+  F->n = n;
+  F->max_columns = max_columns;
+  F->max_fits = max_fits;
+  F->pipelined = pipelined != 0;
+  for (int64_t s = max_fits - 1; s >= 0; --s) F->free_slots.push_back(s);
+  *out = F;
+  return SG_OK;
+}
+
+extern "C" void sg_fits_destroy(sg_fits* F) {
+  if (!F) return;
+  if (F->launched) {
+    int64_t fin = 0;
+    sg_engine_finish(F->ctx, &fin);
+  }
+  for (const auto& kv : F->owner) sg_engine_cancel(F->ctx, kv.first);
+  sg_engine_hold_results(F->ctx, 0);
+  delete F;
+}
+
+extern "C" const char* sg_fits_last_error(sg_fits* F) { return F ? F->err.c_str() : "null handle"; }
+
+static int fits_submit_impl(sg_fits* F, int trait, int64_t n_sub, const uint8_t* mask, const double* y,
+                              const double* X, int p, const double* offset, const double* eta0,
+                              const double* alpha0, double tol, int maxiter, int nrun, double tol_pcg,
+                              int maxiter_pcg, double cv_cutoff, uint64_t seed, int64_t* fit_id) {
+  if (!F) return SG_ERR_INVALID;
+  if (!y || !X || !eta0 || !alpha0 || p <= 0 || n_sub <= 1 || nrun < 2 || maxiter < 1 || (trait != 0 && trait != 1))
+    return fits_err(F, SG_ERR_INVALID, "sg_fits_submit: invalid arguments");
+  auto f = std::make_unique<Fit>();
+  f->n = F->n;
+  f->quant = trait == 1;
+  f->p = p;
+  f->mask.assign(F->n, 1);
+  f->has_mask = mask != nullptr;
+  if (mask)
+    for (int64_t i = 0; i < F->n; ++i) f->mask[i] = mask[i] ? 1 : 0;
+  for (int64_t i = 0; i < F->n; ++i)
+    if (f->mask[i]) f->idx.push_back(i);
+  if ((int64_t)f->idx.size() != n_sub)
+    return fits_err(F, SG_ERR_INVALID, "sg_fits_submit: n_sub = %lld but the mask selects %lld samples",
+                    (long long)n_sub, (long long)f->idx.size());
+  f->ns = n_sub;
+  const int64_t n = F->n;
+  f->y.assign(n, 0.0);
+  f->X.assign((size_t)n * p, 0.0);
+  f->offset.assign(n, 0.0);
+  f->eta.assign(n, 0.0);
+  for (int64_t s = 0; s < n_sub; ++s) {
+    const int64_t i = f->idx[s];
+    f->y[i] = y[s];
+    for (int j = 0; j < p; ++j) f->X[i + (int64_t)j * n] = X[s + (int64_t)j * n_sub];
+    f->offset[i] = offset ? offset[s] : 0.0;
+    f->eta[i] = eta0[s];
+  }
+  f->alpha.assign(alpha0, alpha0 + p);
+  f->tol = tol;
+  f->maxiter = maxiter;
+  f->nrun = nrun;
+  f->tol_pcg = tol_pcg;
+  f->maxiter_pcg = maxiter_pcg;
+  f->cutoff = cv_cutoff;
+  f->seed = seed;
+  if (need_columns(*f) > F->max_columns)
+    return fits_err(F, SG_ERR_INVALID, "a fit with %d probes needs %lld engine columns, the engine has %lld", nrun,
+                    (long long)need_columns(*f), (long long)F->max_columns);
+  f->id = F->next_id++;
+  if (fit_id) *fit_id = f->id;
+  F->pending.push_back(std::move(f));
+  admit(F);
+  return SG_OK;
+}
+
+static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
+  if (!F) return SG_ERR_INVALID;
+  const size_t before = F->finished_order.size();
+  for (int64_t s = 0; s < max_steps; ++s) {
+    admit(F);
+    if (F->active.empty() && F->pending.empty()) break;
+    double t = now_s();
+    int64_t fin = 0;
+    int rc;
+    if (F->pipelined) {
+      rc = F->launched ? sg_engine_finish(F->ctx, &fin) : SG_OK;
+      int launched = 0;
+      if (rc == SG_OK) rc = sg_engine_launch(F->ctx, &fin, &launched);
+      F->launched = launched != 0;
+    } else {
+      rc = sg_engine_run(F->ctx, 1, &fin);
+    }
+    if (rc != SG_OK) {
+      const char* m = sg_last_error(F->ctx);
+      return fits_err(F, rc, "engine step: %s", m ? m : "error");
+    }
+    std::vector<int64_t> ids(4096);
+    int64_t got = 0;
+    do {
+      rc = sg_engine_poll(F->ctx, ids.data(), (int64_t)ids.size(), &got);
+      if (rc != SG_OK) return fits_err(F, rc, "engine poll failed");
+      for (int64_t q = 0; q < got; ++q) {
+        if (!F->owner.count(ids[q])) continue;
+        if (F->done_reqs.insert(ids[q]).second) F->inflight_columns -= 1;
+      }
+    } while (got == (int64_t)ids.size());
+    F->t_engine += now_s() - t;
+    F->steps += 1;
+    // resume every fit whose awaited columns are done, oldest first
+    t = now_s();
+    bool progressed = false;
+    std::vector<int64_t> ready;
+    for (auto& kv : F->active)
+      if (is_ready(F, *kv.second)) ready.push_back(kv.first);
+    for (int64_t fid : ready) {
+      auto it = F->active.find(fid);
+      if (it == F->active.end()) continue;
+      Fit& f = *it->second;
+      while (is_ready(F, f)) {
+        progressed = true;
+        if (!resume(F, f) || f.failed || f.phase == P_DONE) break;
+      }
+      if (f.failed || f.phase == P_DONE) retire(F, fid);
+    }
+    F->t_host += now_s() - t;
+    if (!F->launched && !progressed && !F->active.empty()) {
+      bool any_running = false;
+      for (const auto& kv : F->active)
+        if (!is_ready(F, *kv.second)) any_running = true;
+      if (any_running && fin == 0)
+        return fits_err(F, SG_ERR_STATE, "engine idle while %zu fits wait for columns", F->active.size());
+    }
+    if (F->finished_order.size() > before) break;
+  }
+  if (n_ready) *n_ready = (int64_t)F->finished_order.size();
+  return SG_OK;
+}
+
+extern "C" int sg_fits_poll(sg_fits* F, int64_t* ids, int64_t max_ids, int64_t* n_out) {
+  if (!F || !n_out || (max_ids > 0 && !ids)) return SG_ERR_INVALID;
+  int64_t k = 0;
+  while (k < max_ids && !F->finished_order.empty()) {
+    ids[k++] = F->finished_order.front();
+    F->finished_order.pop_front();
+  }
+  *n_out = k;
+  return SG_OK;
+}
+
+extern "C" int sg_fits_counts(sg_fits* F, int64_t* active, int64_t* pending, int64_t* done) {
+  if (!F) return SG_ERR_INVALID;
+  if (active) *active = (int64_t)F->active.size();
+  if (pending) *pending = (int64_t)F->pending.size();
+  if (done) *done = (int64_t)F->done_fits.size();
+  return SG_OK;
+}
+
+extern "C" int sg_fits_host_times(sg_fits* F, double* t3) {
+  if (!F || !t3) return SG_ERR_INVALID;
+  t3[0] = F->t_engine;
+  t3[1] = F->t_host;
+  t3[2] = (double)F->steps;
+  return SG_OK;
+}
+
+extern "C" int sg_fits_result(sg_fits* F, int64_t fit_id, double* theta, double* alpha, double* eta,
+                              double* mu, double* Y, double* cov, int32_t* iterations, int32_t* converged,
+                              int64_t* column_iterations) {
+  if (!F) return SG_ERR_INVALID;
+  auto it = F->done_fits.find(fit_id);
+  if (it == F->done_fits.end()) return fits_err(F, SG_ERR_NOT_FOUND, "fit %lld is not finished", (long long)fit_id);
+  std::unique_ptr<Fit> f = std::move(it->second);
+  F->done_fits.erase(it);
+  if (column_iterations) *column_iterations = f->column_iterations;
+  if (f->failed) return fits_err(F, f->err.code, "%s", f->err.msg.c_str());
+  if (theta) {
+    theta[0] = f->tau[0];
+    theta[1] = f->tau[1];
+  }
+  if (alpha) std::memcpy(alpha, f->rc_alpha.data(), f->p * sizeof(double));
+  for (int64_t s = 0; s < f->ns; ++s) {
+    const int64_t i = f->idx[s];
+    if (eta) eta[s] = f->rc_eta[i];
+    if (mu) mu[s] = f->mu[i];
+    if (Y) Y[s] = f->Y[i];
+  }
+  if (cov) std::memcpy(cov, f->rc_cov.data(), (size_t)f->p * f->p * sizeof(double));
+  if (iterations) *iterations = f->it_used;
+  if (converged) *converged = f->converged ? 1 : 0;
+  return SG_OK;
+}
+
+extern "C" int sg_fits_submit(sg_fits* F, int trait, int64_t n_sub, const uint8_t* mask, const double* y,
+                              const double* X, int p, const double* offset, const double* eta0,
+                              const double* alpha0, double tol, int maxiter, int nrun, double tol_pcg,
+                              int maxiter_pcg, double cv_cutoff, uint64_t seed, int64_t* fit_id) {
+  if (!F) return SG_ERR_INVALID;
+  try {
+    return fits_submit_impl(F, trait, n_sub, mask, y, X, p, offset, eta0, alpha0, tol, maxiter, nrun, tol_pcg,
+                            maxiter_pcg, cv_cutoff, seed, fit_id);
+  } catch (const std::exception& ex) {
+    return fits_err(F, SG_ERR_CUDA, "sg_fits_submit: %s", ex.what());
+  }
+}
+
+extern "C" int sg_fits_run(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
+  if (!F) return SG_ERR_INVALID;
+  try {
+    return fits_run_impl(F, max_steps, n_ready);
+  } catch (const std::exception& ex) {
+    return fits_err(F, SG_ERR_CUDA, "sg_fits_run: %s", ex.what());
+  }
+}

@@ -107,8 +107,19 @@ SIGNATURES = {
     "sg_synth_bed": [c_ctx, c_u64, c_i64, c_i64, C.c_double, C.POINTER(C.c_void_p), P_u64],
     "sg_synth_bed_to_host": [c_ctx, P_u8, c_u64],
     "sg_synth_genetic_value": [c_ctx, c_u64, P_f64],
+    "sg_fits_create": [c_ctx, c_i64, c_i64, C.c_int, C.POINTER(C.c_void_p)],
+    "sg_fits_destroy": [C.c_void_p],
+    "sg_fits_last_error": [C.c_void_p],
+    "sg_fits_submit": [C.c_void_p, C.c_int, c_i64, P_u8, P_f64, P_f64, C.c_int, P_f64, P_f64, P_f64,
+                       C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, c_u64, P_i64],
+    "sg_fits_run": [C.c_void_p, c_i64, P_i64],
+    "sg_fits_poll": [C.c_void_p, P_i64, c_i64, P_i64],
+    "sg_fits_counts": [C.c_void_p, P_i64, P_i64, P_i64],
+    "sg_fits_host_times": [C.c_void_p, P_f64],
+    "sg_fits_result": [C.c_void_p, c_i64, P_f64, P_f64, P_f64, P_f64, P_f64, P_f64, P_i32, P_i32, P_i64],
 }
-_RESTYPE = {"sg_ctx_destroy": None, "sg_last_error": C.c_char_p}
+_RESTYPE = {"sg_ctx_destroy": None, "sg_last_error": C.c_char_p, "sg_fits_destroy": None,
+            "sg_fits_last_error": C.c_char_p}
 
 
 class SaigeGpuError(RuntimeError):

@@ -170,3 +170,43 @@ def test_exact_subset_fits_match_oracle_on_subset_cohort():
         np.testing.assert_allclose(r["theta"], ref["theta"], rtol=1e-4)
         np.testing.assert_allclose(r["coefficients"], ref["coefficients"], rtol=1e-4, atol=1e-8)
     gpu_ctx.close()
+
+
+@pytest.mark.parametrize("mode", [MV_FP32_SIMT, MV_BF16X3_TC])
+def test_native_driver_matches_python_driver_and_oracle(cohort, mode):
+    """The C++ fit driver (sg_fits_*) runs the same algorithm as the Python generators: the same
+    iterations, tau to rounding, and the oracle's tau to 1e-4 (masked fits included)."""
+    from saigegpu import native
+    ctx, grm, specs, refs = cohort
+    ctx.set_matvec_mode(mode)
+    try:
+        py, _ = serve.fit_batch(ctx, specs, max_columns=256)
+        nat, jobs = native.fit_batch(ctx, specs, max_columns=256)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+    for a, b, ref, j in zip(nat, py, refs, jobs):
+        assert not isinstance(a, Exception), a
+        assert a["iterations"] == b["iterations"]
+        np.testing.assert_allclose(a["theta"], b["theta"], rtol=1e-8)
+        np.testing.assert_allclose(a["coefficients"], b["coefficients"], rtol=1e-7, atol=1e-10)
+        np.testing.assert_allclose(a["linear_predictors"], b["linear_predictors"], rtol=1e-7, atol=1e-10)
+        assert j.column_iterations > 0
+        if ref is not None:
+            np.testing.assert_allclose(a["theta"], ref["theta"], rtol=1e-4)
+
+
+def test_native_driver_failing_fit_and_serving(cohort):
+    """A fit that fails (quantitative phenotype with variance << 1) reports its own error; the
+    others finish; served arrivals all complete."""
+    from saigegpu import native
+    ctx, grm, specs, refs = cohort
+    n = ctx.n
+    bad_f0 = dict(specs[1].fit0)
+    bad_f0["y"] = np.full(n, 0.3) + 1e-4 * np.arange(n) / n
+    bad = serve.FitSpec(prep.make_fit0(bad_f0["y"], bad_f0["X"][:, 1:], "quantitative", True), "quantitative")
+    res, _ = native.fit_batch(ctx, [specs[0], bad, specs[1]], max_columns=256)
+    assert isinstance(res[1], Exception) and "variance" in str(res[1])
+    assert not isinstance(res[0], Exception) and not isinstance(res[2], Exception)
+    arrivals = [(0.01 * i, specs[i % len(specs)]) for i in range(5)]
+    done = native.serve(ctx, arrivals, max_columns=256, max_phenos=2)
+    assert len(done) == 5 and all(j.error is None for j in done)
