@@ -201,9 +201,9 @@ def test_native_driver_failing_fit_and_serving(cohort):
     from saigegpu import native
     ctx, grm, specs, refs = cohort
     n = ctx.n
-    bad_f0 = dict(specs[1].fit0)
-    bad_f0["y"] = np.full(n, 0.3) + 1e-4 * np.arange(n) / n
-    bad = serve.FitSpec(prep.make_fit0(bad_f0["y"], bad_f0["X"][:, 1:], "quantitative", True), "quantitative")
+    C = np.random.default_rng(5).standard_normal((n, 2))
+    y_flat = 0.3 + 1e-4 * np.arange(n) / n
+    bad = serve.FitSpec(prep.make_fit0(y_flat, C, "quantitative", True), "quantitative")
     res, _ = native.fit_batch(ctx, [specs[0], bad, specs[1]], max_columns=256)
     assert isinstance(res[1], Exception) and "variance" in str(res[1])
     assert not isinstance(res[0], Exception) and not isinstance(res[2], Exception)
