@@ -328,8 +328,10 @@ int sg_fits_submit(sg_fits *fits, int trait, int64_t n_sub, const uint8_t *mask,
 int sg_fits_run(sg_fits *fits, int64_t max_steps, int64_t *n_ready);
 int sg_fits_poll(sg_fits *fits, int64_t *ids, int64_t max_ids, int64_t *n_out);
 int sg_fits_counts(sg_fits *fits, int64_t *active, int64_t *pending, int64_t *done);
-/* t3: seconds in engine steps (launch / finish / poll), seconds of driver work, steps */
-int sg_fits_host_times(sg_fits *fits, double *t3);
+/* t7: seconds in engine steps (launch / finish / poll), seconds of driver work, steps, and the
+ * parts of the driver work spent in weight uploads, submissions, result copies and probe
+ * reductions */
+int sg_fits_host_times(sg_fits *fits, double *t7);
 int sg_fits_result(sg_fits *fits, int64_t fit_id, double *theta, double *alpha, double *eta, double *mu,
                    double *Y, double *cov, int32_t *iterations, int32_t *converged,
                    int64_t *column_iterations);

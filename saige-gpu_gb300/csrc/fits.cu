@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <deque>
 #include <exception>
@@ -87,6 +88,7 @@ struct Fit {
   bool failed = false;
   FitError err;
   bool converged = false;
+  int64_t ready_at = -1;  // scheduler step at which every awaited column was done
 };
 
 }  // namespace
@@ -102,10 +104,11 @@ struct sg_fits {
   std::deque<int64_t> finished_order;
   std::unordered_map<int64_t, int64_t> owner;        // request id -> fit id
   std::unordered_set<int64_t> done_reqs;
-  std::deque<int64_t> ready;                          // fits whose awaited columns are all done
   int64_t next_id = 1, inflight_columns = 0;
   std::string err;
   double t_engine = 0, t_host = 0;
+  double t_pheno = 0, t_submit = 0, t_fetch = 0, t_dots = 0;  // parts of t_host spent in engine calls
+  double gpu_ms_seen = 0;                                      // engine step time already budgeted
   int64_t steps = 0;
 };
 
@@ -223,13 +226,19 @@ void own(sg_fits* F, Fit& f, const std::vector<int64_t>& ids) {
 }
 
 bool set_pheno(sg_fits* F, Fit& f, const std::vector<double>& W, const double* tau) {
-  return eng_ok(F, f, sg_engine_set_pheno(F->ctx, f.slot, W.data(), tau, f.has_mask ? f.mask.data() : nullptr));
+  const double t = now_s();
+  const int rc = sg_engine_set_pheno(F->ctx, f.slot, W.data(), tau, f.has_mask ? f.mask.data() : nullptr);
+  F->t_pheno += now_s() - t;
+  return eng_ok(F, f, rc);
 }
 
 bool submit(sg_fits* F, Fit& f, int kind, const double* B, int64_t k, int maxiter, double tol,
             std::vector<int64_t>& ids) {
   ids.assign(k, -1);
-  if (!eng_ok(F, f, sg_engine_submit(F->ctx, f.slot, kind, B, k, maxiter, tol, ids.data()))) return false;
+  const double t = now_s();
+  const int rc = sg_engine_submit(F->ctx, f.slot, kind, B, k, maxiter, tol, ids.data());
+  F->t_submit += now_s() - t;
+  if (!eng_ok(F, f, rc)) return false;
   own(F, f, ids);
   return true;
 }
@@ -375,9 +384,11 @@ bool ai_after_probes(sg_fits* F, Fit& f) {
   const int64_t nv = 2 + 2 * p, k = (int64_t)f.pid.size();
   std::vector<double> D(k * nv);
   std::vector<int32_t> its(k, 0);
-  if (!eng_ok(F, f, sg_engine_probe_dots(F->ctx, f.slot, f.pid.data(), f.aid.data(), k, f.seed, f.run0,
-                                         f.SX.data(), p, D.data(), its.data())))
-    return false;
+  const double t = now_s();
+  const int rc = sg_engine_probe_dots(F->ctx, f.slot, f.pid.data(), f.aid.data(), k, f.seed, f.run0, f.SX.data(),
+                                      p, D.data(), its.data());
+  F->t_dots += now_s() - t;
+  if (!eng_ok(F, f, rc)) return false;
   for (int64_t j = 0; j < k; ++j) {
     f.column_iterations += its[j] + (f.aid[j] >= 0 ? 1 : 0);
     F->done_reqs.erase(f.pid[j]);
@@ -596,7 +607,10 @@ bool resume(sg_fits* F, Fit& f) {
     for (int64_t id : f.wait_ids) {
       std::vector<double> x(f.n);
       int32_t it = 0;
-      if (!eng_ok(F, f, sg_engine_fetch(F->ctx, id, x.data(), &it))) return false;
+      const double t = now_s();
+      const int rc = sg_engine_fetch(F->ctx, id, x.data(), &it);
+      F->t_fetch += now_s() - t;
+      if (!eng_ok(F, f, rc)) return false;
       f.column_iterations += it;
       F->done_reqs.erase(id);
       F->owner.erase(id);
@@ -762,16 +776,19 @@ static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
     admit(F);
     if (F->active.empty() && F->pending.empty()) break;
     double t = now_s();
-    int64_t fin = 0;
-    int rc;
-    if (F->pipelined) {
+    int64_t fin = 0, fin2 = 0, st0[4] = {0, 0, 0, 0}, st1[4] = {0, 0, 0, 0};
+    int rc = sg_engine_stats(F->ctx, st0);
+    if (rc == SG_OK && F->pipelined) {
       rc = F->launched ? sg_engine_finish(F->ctx, &fin) : SG_OK;
       int launched = 0;
-      if (rc == SG_OK) rc = sg_engine_launch(F->ctx, &fin, &launched);
+      if (rc == SG_OK) rc = sg_engine_launch(F->ctx, &fin2, &launched);
       F->launched = launched != 0;
-    } else {
+    } else if (rc == SG_OK) {
       rc = sg_engine_run(F->ctx, 1, &fin);
     }
+    if (rc == SG_OK) rc = sg_engine_stats(F->ctx, st1);
+    fin += fin2;
+    const bool stepped = F->pipelined ? F->launched : st1[0] > st0[0];
     if (rc != SG_OK) {
       const char* m = sg_last_error(F->ctx);
       return fits_err(F, rc, "engine step: %s", m ? m : "error");
@@ -788,30 +805,43 @@ static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
     } while (got == (int64_t)ids.size());
     F->t_engine += now_s() - t;
     F->steps += 1;
-    // resume every fit whose awaited columns are done, oldest first
+    // Resume the fits whose awaited columns are done, oldest first.  While a step runs, work for
+    // about as long as the previous step took on the GPU and leave the rest for the next one: fits
+    // that started together reach their stage changes together, and doing all of that host work
+    // at once would leave the GPU idle.
+    double budget = -1.0;
+    if (F->pipelined && F->launched) {
+      double tm[6] = {0, 0, 0, 0, 0, 0};
+      if (sg_engine_timing(F->ctx, tm) == SG_OK) {
+        if (tm[0] >= F->gpu_ms_seen && F->gpu_ms_seen > 0) budget = (tm[0] - F->gpu_ms_seen) * 1e-3;
+        F->gpu_ms_seen = tm[0];
+      }
+    }
     t = now_s();
     bool progressed = false;
-    std::vector<int64_t> ready;
-    for (auto& kv : F->active)
-      if (is_ready(F, *kv.second)) ready.push_back(kv.first);
-    for (int64_t fid : ready) {
-      auto it = F->active.find(fid);
+    std::vector<std::pair<int64_t, int64_t>> ready;  // (ready_at, fit id)
+    for (auto& kv : F->active) {
+      Fit& f = *kv.second;
+      if (!is_ready(F, f)) continue;
+      if (f.ready_at < 0) f.ready_at = F->steps;
+      ready.emplace_back(f.ready_at, kv.first);
+    }
+    std::sort(ready.begin(), ready.end());
+    for (size_t r = 0; r < ready.size(); ++r) {
+      if (budget >= 0.0 && r > 0 && now_s() - t > budget) break;
+      auto it = F->active.find(ready[r].second);
       if (it == F->active.end()) continue;
       Fit& f = *it->second;
       while (is_ready(F, f)) {
         progressed = true;
+        f.ready_at = -1;
         if (!resume(F, f) || f.failed || f.phase == P_DONE) break;
       }
-      if (f.failed || f.phase == P_DONE) retire(F, fid);
+      if (f.failed || f.phase == P_DONE) retire(F, ready[r].second);
     }
     F->t_host += now_s() - t;
-    if (!F->launched && !progressed && !F->active.empty()) {
-      bool any_running = false;
-      for (const auto& kv : F->active)
-        if (!is_ready(F, *kv.second)) any_running = true;
-      if (any_running && fin == 0)
-        return fits_err(F, SG_ERR_STATE, "engine idle while %zu fits wait for columns", F->active.size());
-    }
+    if (!stepped && !progressed && fin == 0 && !F->active.empty())
+      return fits_err(F, SG_ERR_STATE, "engine idle while %zu fits wait for columns", F->active.size());
     if (F->finished_order.size() > before) break;
   }
   if (n_ready) *n_ready = (int64_t)F->finished_order.size();
@@ -837,11 +867,15 @@ extern "C" int sg_fits_counts(sg_fits* F, int64_t* active, int64_t* pending, int
   return SG_OK;
 }
 
-extern "C" int sg_fits_host_times(sg_fits* F, double* t3) {
-  if (!F || !t3) return SG_ERR_INVALID;
-  t3[0] = F->t_engine;
-  t3[1] = F->t_host;
-  t3[2] = (double)F->steps;
+extern "C" int sg_fits_host_times(sg_fits* F, double* t7) {
+  if (!F || !t7) return SG_ERR_INVALID;
+  t7[0] = F->t_engine;
+  t7[1] = F->t_host;
+  t7[2] = (double)F->steps;
+  t7[3] = F->t_pheno;
+  t7[4] = F->t_submit;
+  t7[5] = F->t_fetch;
+  t7[6] = F->t_dots;
   return SG_OK;
 }
 

@@ -81,9 +81,11 @@ class NativeFits:
         return a.value, p.value, d.value
 
     def host_times(self):
-        t = np.zeros(3)
+        """Seconds: engine stepping, driver work (and its pheno / submit / fetch / probe_dots parts)."""
+        t = np.zeros(7)
         self._check(self._L.sg_fits_host_times(self._h, t.ctypes.data_as(L.P_f64)))
-        return {"engine": t[0], "driver": t[1], "steps": int(t[2])}
+        return {"engine": t[0], "driver": t[1], "steps": int(t[2]), "pheno": t[3], "submit": t[4],
+                "fetch": t[5], "probe_dots": t[6]}
 
     def result(self, fid):
         """(result dict, column iterations); the dict has the keys of ``serve.fit_generator``'s."""
