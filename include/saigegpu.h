@@ -326,6 +326,9 @@ int sg_fits_submit(sg_fits *fits, int trait, int64_t n_sub, const uint8_t *mask,
                    double tol, int maxiter, int nrun, double tol_pcg, int maxiter_pcg, double cv_cutoff,
                    uint64_t seed, int64_t *fit_id);
 int sg_fits_run(sg_fits *fits, int64_t max_steps, int64_t *n_ready);
+/* Host threads (the caller's included) for the fits' arithmetic; engine calls stay serialised.
+ * Default: half the hardware threads, at most 8. */
+int sg_fits_set_threads(sg_fits *fits, int threads);
 int sg_fits_poll(sg_fits *fits, int64_t *ids, int64_t max_ids, int64_t *n_out);
 int sg_fits_counts(sg_fits *fits, int64_t *active, int64_t *pending, int64_t *done);
 /* t7: seconds in engine steps (launch / finish / poll), seconds of driver work, steps, and the

@@ -18,7 +18,12 @@
 #include <cstdarg>
 #include <cstdio>
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <deque>
 #include <exception>
 #include <map>
@@ -91,6 +96,79 @@ struct Fit {
   int64_t ready_at = -1;  // scheduler step at which every awaited column was done
 };
 
+// Host threads for the fits' arithmetic: run(count, fn) calls fn(0..count-1) on the pool and the
+// calling thread and returns when every call has returned.  Each worker makes the context's GPU
+// current once (the engine calls it makes run under the driver's lock).
+class Pool {
+ public:
+  Pool(int workers, sg_ctx* ctx) {
+    for (int w = 0; w < workers; ++w)
+      th_.emplace_back([this, ctx] {
+        sg_ctx_make_current(ctx);
+        uint64_t seen = 0;
+        for (;;) {
+          {
+            std::unique_lock<std::mutex> lk(m_);
+            cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+            if (stop_) return;
+            seen = gen_;
+            ++busy_;
+          }
+          work();
+          {
+            std::lock_guard<std::mutex> lk(m_);
+            --busy_;
+          }
+          done_cv_.notify_all();
+        }
+      });
+  }
+  ~Pool() {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  int size() const { return (int)th_.size() + 1; }
+  void run(int64_t count, const std::function<void(int64_t)>& fn) {
+    if (count <= 0) return;
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      fn_ = &fn;
+      count_ = count;
+      next_.store(0);
+      finished_.store(0);
+      ++gen_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(m_);
+    done_cv_.wait(lk, [&] { return finished_.load() == count_ && busy_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  void work() {
+    for (;;) {
+      const int64_t i = next_.fetch_add(1);
+      if (i >= count_) return;
+      (*fn_)(i);
+      if (finished_.fetch_add(1) + 1 == count_) done_cv_.notify_all();
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex m_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int64_t)>* fn_ = nullptr;
+  int64_t count_ = 0;
+  std::atomic<int64_t> next_{0}, finished_{0};
+  uint64_t gen_ = 0;
+  int busy_ = 0;
+  bool stop_ = false;
+};
+
 }  // namespace
 
 struct sg_fits {
@@ -110,6 +188,8 @@ struct sg_fits {
   double t_pheno = 0, t_submit = 0, t_fetch = 0, t_dots = 0;  // parts of t_host spent in engine calls
   double gpu_ms_seen = 0;                                      // engine step time already budgeted
   int64_t steps = 0;
+  std::mutex mu;               // engine calls and the bookkeeping above, from the worker threads
+  std::unique_ptr<Pool> pool;  // null: the fits' arithmetic runs on the calling thread
 };
 
 namespace {
@@ -211,7 +291,13 @@ void fail(sg_fits* F, Fit& f, int code, const std::string& msg) {
   }
 }
 
-bool eng_ok(sg_fits* F, Fit& f, int rc) {
+// One engine call (and whatever bookkeeping fn does with its result) under the driver's lock.
+template <typename Fn>
+bool eng(sg_fits* F, Fit& f, double* timer, Fn fn) {
+  std::lock_guard<std::mutex> g(F->mu);
+  const double t = now_s();
+  const int rc = fn();
+  if (timer) *timer += now_s() - t;
   if (rc == SG_OK) return true;
   const char* m = sg_last_error(F->ctx);
   fail(F, f, rc, m ? m : "engine error");
@@ -226,52 +312,52 @@ void own(sg_fits* F, Fit& f, const std::vector<int64_t>& ids) {
 }
 
 bool set_pheno(sg_fits* F, Fit& f, const std::vector<double>& W, const double* tau) {
-  const double t = now_s();
-  const int rc = sg_engine_set_pheno(F->ctx, f.slot, W.data(), tau, f.has_mask ? f.mask.data() : nullptr);
-  F->t_pheno += now_s() - t;
-  return eng_ok(F, f, rc);
+  return eng(F, f, &F->t_pheno, [&] {
+    return sg_engine_set_pheno(F->ctx, f.slot, W.data(), tau, f.has_mask ? f.mask.data() : nullptr);
+  });
 }
 
 bool submit(sg_fits* F, Fit& f, int kind, const double* B, int64_t k, int maxiter, double tol,
             std::vector<int64_t>& ids) {
   ids.assign(k, -1);
-  const double t = now_s();
-  const int rc = sg_engine_submit(F->ctx, f.slot, kind, B, k, maxiter, tol, ids.data());
-  F->t_submit += now_s() - t;
-  if (!eng_ok(F, f, rc)) return false;
-  own(F, f, ids);
-  return true;
+  return eng(F, f, &F->t_submit, [&] {
+    const int rc = sg_engine_submit(F->ctx, f.slot, kind, B, k, maxiter, tol, ids.data());
+    if (rc == SG_OK) own(F, f, ids);
+    return rc;
+  });
 }
 
 bool submit_probes(sg_fits* F, Fit& f, int64_t run0, int64_t k, std::vector<int64_t>& ids) {
   ids.assign(k, -1);
-  if (!eng_ok(F, f, sg_engine_submit_probes(F->ctx, f.slot, 0, f.seed, run0, k, f.maxiter_pcg, f.tol_pcg,
-                                            ids.data())))
-    return false;
-  own(F, f, ids);
-  return true;
+  return eng(F, f, &F->t_submit, [&] {
+    const int rc = sg_engine_submit_probes(F->ctx, f.slot, 0, f.seed, run0, k, f.maxiter_pcg, f.tol_pcg, ids.data());
+    if (rc == SG_OK) own(F, f, ids);
+    return rc;
+  });
 }
 
 // K u of the probes: -1 where the slot's cache holds it (same probes and sample mask all fit
 // long), else maximal runs of uncached probes submitted as product blocks
 bool probe_products(sg_fits* F, Fit& f, int64_t run0, int64_t cnt, std::vector<int64_t>& out) {
   out.assign(cnt, -1);
-  int64_t j = 0;
-  while (j < cnt) {
-    if (sg_engine_probe_cached(F->ctx, f.slot, f.seed, run0 + j)) {
-      ++j;
-      continue;
+  return eng(F, f, &F->t_submit, [&] {
+    int64_t j = 0;
+    while (j < cnt) {
+      if (sg_engine_probe_cached(F->ctx, f.slot, f.seed, run0 + j)) {
+        ++j;
+        continue;
+      }
+      int64_t j1 = j;
+      while (j1 < cnt && !sg_engine_probe_cached(F->ctx, f.slot, f.seed, run0 + j1)) ++j1;
+      std::vector<int64_t> ids(j1 - j, -1);
+      const int rc = sg_engine_submit_probes(F->ctx, f.slot, 1, f.seed, run0 + j, j1 - j, 1, 0.0, ids.data());
+      if (rc != SG_OK) return rc;
+      own(F, f, ids);
+      for (int64_t q = 0; q < j1 - j; ++q) out[j + q] = ids[q];
+      j = j1;
     }
-    int64_t j1 = j;
-    while (j1 < cnt && !sg_engine_probe_cached(F->ctx, f.slot, f.seed, run0 + j1)) ++j1;
-    std::vector<int64_t> ids(j1 - j, -1);
-    if (!eng_ok(F, f, sg_engine_submit_probes(F->ctx, f.slot, 1, f.seed, run0 + j, j1 - j, 1, 0.0, ids.data())))
-      return false;
-    own(F, f, ids);
-    for (int64_t q = 0; q < j1 - j; ++q) out[j + q] = ids[q];
-    j = j1;
-  }
-  return true;
+    return (int)SG_OK;
+  });
 }
 
 void wait_for(Fit& f, Stage st, std::vector<int64_t> ids, bool fetch) {
@@ -384,20 +470,22 @@ bool ai_after_probes(sg_fits* F, Fit& f) {
   const int64_t nv = 2 + 2 * p, k = (int64_t)f.pid.size();
   std::vector<double> D(k * nv);
   std::vector<int32_t> its(k, 0);
-  const double t = now_s();
-  const int rc = sg_engine_probe_dots(F->ctx, f.slot, f.pid.data(), f.aid.data(), k, f.seed, f.run0, f.SX.data(),
-                                      p, D.data(), its.data());
-  F->t_dots += now_s() - t;
-  if (!eng_ok(F, f, rc)) return false;
-  for (int64_t j = 0; j < k; ++j) {
-    f.column_iterations += its[j] + (f.aid[j] >= 0 ? 1 : 0);
-    F->done_reqs.erase(f.pid[j]);
-    F->owner.erase(f.pid[j]);
-    if (f.aid[j] >= 0) {
-      F->done_reqs.erase(f.aid[j]);
-      F->owner.erase(f.aid[j]);
+  const bool ok = eng(F, f, &F->t_dots, [&] {
+    const int rc = sg_engine_probe_dots(F->ctx, f.slot, f.pid.data(), f.aid.data(), k, f.seed, f.run0, f.SX.data(),
+                                        p, D.data(), its.data());
+    if (rc != SG_OK) return rc;
+    for (int64_t j = 0; j < k; ++j) {
+      F->done_reqs.erase(f.pid[j]);
+      F->owner.erase(f.pid[j]);
+      if (f.aid[j] >= 0) {
+        F->done_reqs.erase(f.aid[j]);
+        F->owner.erase(f.aid[j]);
+      }
     }
-  }
+    return rc;
+  });
+  if (!ok) return false;
+  for (int64_t j = 0; j < k; ++j) f.column_iterations += its[j] + (f.aid[j] >= 0 ? 1 : 0);
   for (int64_t j = 0; j < k; ++j) {
     const double* row = D.data() + j * nv;
     const double* b = row + 2;
@@ -607,13 +695,16 @@ bool resume(sg_fits* F, Fit& f) {
     for (int64_t id : f.wait_ids) {
       std::vector<double> x(f.n);
       int32_t it = 0;
-      const double t = now_s();
-      const int rc = sg_engine_fetch(F->ctx, id, x.data(), &it);
-      F->t_fetch += now_s() - t;
-      if (!eng_ok(F, f, rc)) return false;
+      const bool ok = eng(F, f, &F->t_fetch, [&] {
+        const int rc = sg_engine_fetch(F->ctx, id, x.data(), &it);
+        if (rc == SG_OK) {
+          F->done_reqs.erase(id);
+          F->owner.erase(id);
+        }
+        return rc;
+      });
+      if (!ok) return false;
       f.column_iterations += it;
-      F->done_reqs.erase(id);
-      F->owner.erase(id);
       f.fetched.push_back(std::move(x));
     }
   }
@@ -638,8 +729,9 @@ bool resume(sg_fits* F, Fit& f) {
   }
 }
 
-bool is_ready(const sg_fits* F, const Fit& f) {
+bool is_ready(sg_fits* F, const Fit& f) {
   if (f.stage == S_NONE) return false;
+  std::lock_guard<std::mutex> g(F->mu);
   for (int64_t id : f.wait_ids)
     if (!F->done_reqs.count(id)) return false;
   return true;
@@ -701,7 +793,16 @@ extern "C" int sg_fits_create(sg_ctx* ctx, int64_t max_columns, int64_t max_fits
   F->max_fits = max_fits;
   F->pipelined = pipelined != 0;
   for (int64_t s = max_fits - 1; s >= 0; --s) F->free_slots.push_back(s);
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int workers = (int)std::min<unsigned>(7u, hw > 2 ? hw / 2 - 1 : 0u);
+  if (workers > 0) F->pool.reset(new Pool(workers, ctx));
   *out = F;
+  return SG_OK;
+}
+
+extern "C" int sg_fits_set_threads(sg_fits* F, int threads) {
+  if (!F || threads < 1) return SG_ERR_INVALID;
+  F->pool.reset(threads > 1 ? new Pool(threads - 1, F->ctx) : nullptr);
   return SG_OK;
 }
 
@@ -827,17 +928,31 @@ static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
       ready.emplace_back(f.ready_at, kv.first);
     }
     std::sort(ready.begin(), ready.end());
-    for (size_t r = 0; r < ready.size(); ++r) {
-      if (budget >= 0.0 && r > 0 && now_s() - t > budget) break;
-      auto it = F->active.find(ready[r].second);
-      if (it == F->active.end()) continue;
-      Fit& f = *it->second;
-      while (is_ready(F, f)) {
-        progressed = true;
-        f.ready_at = -1;
-        if (!resume(F, f) || f.failed || f.phase == P_DONE) break;
+    std::vector<Fit*> todo;
+    for (const auto& r : ready) todo.push_back(F->active[r.second].get());
+    std::atomic<bool> any{false};
+    const std::function<void(int64_t)> advance = [&](int64_t r) {
+      if (budget >= 0.0 && r > 0 && now_s() - t > budget) return;  // left for the next step
+      Fit& f = *todo[r];
+      try {
+        while (is_ready(F, f)) {
+          any.store(true);
+          f.ready_at = -1;
+          if (!resume(F, f) || f.failed || f.phase == P_DONE) break;
+        }
+      } catch (const std::exception& ex) {
+        fail(F, f, SG_ERR_NOMEM, std::string("fit driver: ") + ex.what());
       }
-      if (f.failed || f.phase == P_DONE) retire(F, ready[r].second);
+    };
+    if (F->pool && todo.size() > 1) {
+      F->pool->run((int64_t)todo.size(), advance);
+    } else {
+      for (int64_t r = 0; r < (int64_t)todo.size(); ++r) advance(r);
+    }
+    progressed = any.load();
+    for (const auto& r : ready) {
+      auto it = F->active.find(r.second);
+      if (it != F->active.end() && (it->second->failed || it->second->phase == P_DONE)) retire(F, r.second);
     }
     F->t_host += now_s() - t;
     if (!stepped && !progressed && fin == 0 && !F->active.empty())

@@ -113,6 +113,7 @@ SIGNATURES = {
     "sg_fits_submit": [C.c_void_p, C.c_int, c_i64, P_u8, P_f64, P_f64, C.c_int, P_f64, P_f64, P_f64,
                        C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, c_u64, P_i64],
     "sg_fits_run": [C.c_void_p, c_i64, P_i64],
+    "sg_fits_set_threads": [C.c_void_p, C.c_int],
     "sg_fits_poll": [C.c_void_p, P_i64, c_i64, P_i64],
     "sg_fits_counts": [C.c_void_p, P_i64, P_i64, P_i64],
     "sg_fits_host_times": [C.c_void_p, P_f64],
