@@ -62,6 +62,7 @@ struct Engine {
   uint64_t io_h2d = 0, io_d2h = 0;  // bytes through the engine API since the last timing reset
   ColState* h_pin = nullptr;      // pinned mirror for the asynchronous state read-back of a step
   int32_t* h_gcols = nullptr;     // pinned: active columns gathered for the split-BF16 GRM.V
+  double* h_stage = nullptr;      // pinned: 1/W and 1/diag(Sigma) of a slot on their way up
   int32_t* d_gcols = nullptr;
   bool inflight = false;          // a launched step has not been finished yet
   int64_t inflight_ncols = 0, inflight_occupied = 0, inflight_hi = 0;
@@ -281,6 +282,7 @@ extern "C" void sg_ctx_destroy(sg_ctx* c) {
   cudaStreamSynchronize(c->side);
   if (c->eng.h_pin) cudaFreeHost(c->eng.h_pin);
   if (c->eng.h_gcols) cudaFreeHost(c->eng.h_gcols);
+  if (c->eng.h_stage) cudaFreeHost(c->eng.h_stage);
   for (auto& kv : c->allocs) cudaFree(kv.first);
   c->allocs.clear();
   cudaStreamDestroy(c->side);
@@ -853,6 +855,8 @@ static void engine_free(sg_ctx* c) {
   e.h_pin = nullptr;
   if (e.h_gcols) cudaFreeHost(e.h_gcols);
   e.h_gcols = nullptr;
+  if (e.h_stage) cudaFreeHost(e.h_stage);
+  e.h_stage = nullptr;
   dev_free_t(c, e.d_gcols);
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
@@ -941,6 +945,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
     if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_gcols), max_columns * sizeof(int32_t), cudaHostAllocDefault));
+  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_stage), 2 * np * sizeof(double), cudaHostAllocDefault));
   SG_TRY(dev_alloc_t(c, &e.d_gcols, (size_t)max_columns));
   e.h_st.assign(max_columns, ColState{});
   for (auto& s : e.h_st) { s.kind = -1; s.active = 0; }
@@ -961,18 +966,9 @@ extern "C" int sg_engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phe
   return engine_reserve(c, max_columns, max_phenos);
 }
 
-// getDiagOfSigma in FP64 (FIT.cpp:2322-2365) for the Jacobi preconditioner; with a chromosome left
-// out, getDiagOfSigma_LOCO (FIT.cpp:2370-2392): diag minus the chromosome's sum z^2, over M - M_j.
-static void diag_sigma_f64(const sg_ctx* c, const double* w, const double* tau, double* d) {
-  const bool loco = c->loco && !c->is_diag_one;
-  const double m = loco ? (double)(c->m_qc - c->loco_mj) : (double)c->m_qc;
-  for (int64_t i = 0; i < c->nn; ++i) {
-    const double dk = loco ? c->diag_loco[i] : c->diag[i];
-    double v = c->is_diag_one ? tau[1] + tau[0] / w[i] : tau[1] * dk / m + tau[0] / w[i];
-    d[i] = v < 1e-4 ? 1e-4 : v;
-  }
-}
-
+// A slot's weights: 1/W and the Jacobi preconditioner from getDiagOfSigma in FP64
+// (FIT.cpp:2322-2365); with a chromosome left out, getDiagOfSigma_LOCO (FIT.cpp:2370-2392): diag
+// minus the chromosome's sum z^2, over M - M_j.
 extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, const double* tau,
                                    const uint8_t* mask) {
   NEED_GRM(c);
@@ -987,19 +983,31 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
   for (auto& kv : e.reqs)
     if (kv.second.state == 1 && kv.second.slot == slot)
       return set_err(c, SG_ERR_STATE, "phenotype slot %lld has columns in flight", (long long)slot);
-  std::vector<double> d(c->nn), winv(e.np, 0.0), minv(e.np, 0.0);
-  diag_sigma_f64(c, w, tau, d.data());
-  for (int64_t i = 0; i < c->nn; ++i) {
-    if (mask && !mask[i]) continue;
-    winv[i] = 1.0 / w[i];
-    minv[i] = 1.0 / d[i];
+  // 1/W and the Jacobi preconditioner 1/diag(Sigma) (getDiagOfSigma, FIT.cpp:2322-2365), zero
+  // outside the sample subset, staged in pinned memory and copied asynchronously
+  double* winv = e.h_stage;
+  double* minv = e.h_stage + e.np;
+  {
+    const bool loco = c->loco && !c->is_diag_one;
+    const double m = loco ? (double)(c->m_qc - c->loco_mj) : (double)c->m_qc;
+    const double* dg = loco ? c->diag_loco.data() : c->diag.data();
+    for (int64_t i = 0; i < e.np; ++i) {
+      if (i >= c->nn || (mask && !mask[i])) {
+        winv[i] = minv[i] = 0.0;
+        continue;
+      }
+      const double v = c->is_diag_one ? tau[1] + tau[0] / w[i] : tau[1] * dg[i] / m + tau[0] / w[i];
+      winv[i] = 1.0 / w[i];
+      minv[i] = 1.0 / (v < 1e-4 ? 1e-4 : v);
+    }
   }
-  SG_CUDA(c, h2d(c, e.winv + slot * e.np, winv.data(), e.np * 8, c->side));
-  SG_CUDA(c, h2d(c, e.minv + slot * e.np, minv.data(), e.np * 8, c->side));
+  SG_CUDA(c, cudaMemcpyAsync(e.winv + slot * e.np, winv, e.np * 8, cudaMemcpyHostToDevice, c->side));
+  SG_CUDA(c, cudaMemcpyAsync(e.minv + slot * e.np, minv, e.np * 8, cudaMemcpyHostToDevice, c->side));
+  e.io_h2d += (uint64_t)(2 * e.np * 8);
   e.h_ph[slot] = PhenoState{tau[0], tau[1]};
   SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), c->side));
   e.ph_set[slot] = 1;
-  return sync_side(c);
+  return sync_side(c);  // the pinned staging is reused by the next call
 }
 
 static int engine_submit_common(sg_ctx* c, int64_t slot, int kind, const double* B, bool probe,
