@@ -62,7 +62,8 @@ struct Engine {
   uint64_t io_h2d = 0, io_d2h = 0;  // bytes through the engine API since the last timing reset
   ColState* h_pin = nullptr;      // pinned mirror for the asynchronous state read-back of a step
   int32_t* h_gcols = nullptr;     // pinned: active columns gathered for the split-BF16 GRM.V
-  double* h_stage = nullptr;      // pinned: 1/W and 1/diag(Sigma) of a slot on their way up
+  double* h_stage = nullptr;      // pinned: a slot's W and sample mask on their way up
+  double* d_wstage = nullptr;     // their device copy (np doubles + np bytes)
   int32_t* d_gcols = nullptr;
   bool inflight = false;          // a launched step has not been finished yet
   int64_t inflight_ncols = 0, inflight_occupied = 0, inflight_hi = 0;
@@ -128,6 +129,7 @@ struct sg_ctx {
   float* d_lv = nullptr;   // Z_j Z_j' P (cap_cols x np)
   float* d_lp = nullptr;   // P in full FP32 for the correction (cap_cols x np)
   std::vector<double> diag_loco;
+  double* d_diag_loco = nullptr;  // its device copy (slot weights)
   // device time of the last setgeno ([0] QC, [1] re-pack + LUT, [2] diagonal) and grm_build
   // ([3] Z build, [4] SYRK), in ms, from CUDA events on the context stream
   double t_build[5] = {0, 0, 0, 0, 0};
@@ -857,6 +859,7 @@ static void engine_free(sg_ctx* c) {
   e.h_gcols = nullptr;
   if (e.h_stage) cudaFreeHost(e.h_stage);
   e.h_stage = nullptr;
+  dev_free_t(c, e.d_wstage);
   dev_free_t(c, e.d_gcols);
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
@@ -946,6 +949,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_gcols), max_columns * sizeof(int32_t), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_stage), 2 * np * sizeof(double), cudaHostAllocDefault));
+  SG_TRY(dev_alloc_t(c, &e.d_wstage, (size_t)(2 * np)));
   SG_TRY(dev_alloc_t(c, &e.d_gcols, (size_t)max_columns));
   e.h_st.assign(max_columns, ColState{});
   for (auto& s : e.h_st) { s.kind = -1; s.active = 0; }
@@ -983,27 +987,23 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
   for (auto& kv : e.reqs)
     if (kv.second.state == 1 && kv.second.slot == slot)
       return set_err(c, SG_ERR_STATE, "phenotype slot %lld has columns in flight", (long long)slot);
-  // 1/W and the Jacobi preconditioner 1/diag(Sigma) (getDiagOfSigma, FIT.cpp:2322-2365), zero
-  // outside the sample subset, staged in pinned memory and copied asynchronously
-  double* winv = e.h_stage;
-  double* minv = e.h_stage + e.np;
+  // W (and the sample mask) go up through pinned staging; 1/W and the Jacobi preconditioner
+  // 1/diag(Sigma) are formed on the device from the resident FP64 diagonal
   {
+    double* hw = e.h_stage;
+    uint8_t* hm = reinterpret_cast<uint8_t*>(e.h_stage + e.np);
+    std::memcpy(hw, w, c->nn * sizeof(double));
+    if (mask) std::memcpy(hm, mask, c->nn);
     const bool loco = c->loco && !c->is_diag_one;
     const double m = loco ? (double)(c->m_qc - c->loco_mj) : (double)c->m_qc;
-    const double* dg = loco ? c->diag_loco.data() : c->diag.data();
-    for (int64_t i = 0; i < e.np; ++i) {
-      if (i >= c->nn || (mask && !mask[i])) {
-        winv[i] = minv[i] = 0.0;
-        continue;
-      }
-      const double v = c->is_diag_one ? tau[1] + tau[0] / w[i] : tau[1] * dg[i] / m + tau[0] / w[i];
-      winv[i] = 1.0 / w[i];
-      minv[i] = 1.0 / (v < 1e-4 ? 1e-4 : v);
-    }
+    double* dw = e.d_wstage;
+    uint8_t* dm = reinterpret_cast<uint8_t*>(e.d_wstage + e.np);
+    SG_CUDA(c, h2d(c, dw, hw, c->nn * sizeof(double), c->side));
+    if (mask) SG_CUDA(c, h2d(c, dm, hm, c->nn, c->side));
+    launch_slot_weights(e.np, c->nn, dw, mask ? dm : nullptr, loco ? c->d_diag_loco : c->d_diag, m, tau[0], tau[1],
+                        c->is_diag_one ? 1 : 0, e.winv + slot * e.np, e.minv + slot * e.np, c->side);
+    SG_LAUNCHED(c, 1);
   }
-  SG_CUDA(c, cudaMemcpyAsync(e.winv + slot * e.np, winv, e.np * 8, cudaMemcpyHostToDevice, c->side));
-  SG_CUDA(c, cudaMemcpyAsync(e.minv + slot * e.np, minv, e.np * 8, cudaMemcpyHostToDevice, c->side));
-  e.io_h2d += (uint64_t)(2 * e.np * 8);
   e.h_ph[slot] = PhenoState{tau[0], tau[1]};
   SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), c->side));
   e.ph_set[slot] = 1;
@@ -1649,6 +1649,7 @@ extern "C" int sg_engine_stats(sg_ctx* c, int64_t* s4) {
 
 // ------------------------------------------------------------------ leave one chromosome out
 static void loco_free(sg_ctx* c) {
+  dev_free_t(c, c->d_diag_loco);
   dev_free_t(c, c->d_zm);
   dev_free_t(c, c->d_zs);
   dev_free_t(c, c->d_lu);
@@ -1728,6 +1729,8 @@ extern "C" int sg_loco_set(sg_ctx* c, int64_t begin, int64_t end) {
   dev_free(c, lutq);
   c->diag_loco.resize(c->nn);
   for (int64_t i = 0; i < c->nn; ++i) c->diag_loco[i] = c->diag[i] - h[i];
+  SG_TRY(dev_alloc_t(c, &c->d_diag_loco, (size_t)c->nn));
+  SG_CUDA(c, cudaMemcpy(c->d_diag_loco, c->diag_loco.data(), c->nn * 8, cudaMemcpyHostToDevice));
   c->loco_begin = begin;
   c->loco_end = end;
   c->loco_mj = mj;

@@ -399,3 +399,31 @@ void launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s) {
 }
 
 }  // namespace sg
+
+// A phenotype slot's 1/W and Jacobi preconditioner 1/diag(Sigma) (getDiagOfSigma FIT.cpp:2322-2365:
+// tau1 diagK / M + tau0 / W, or tau1 + tau0 / W with isDiagofKinSetAsOne, floored at 1e-4), zero
+// outside the sample subset and past nn; IEEE-rounded operations in the reference's order.
+__global__ void slot_weights_kernel(int64_t np, int64_t nn, const double* __restrict__ w,
+                                    const uint8_t* __restrict__ mask, const double* __restrict__ diag,
+                                    double m, double tau0, double tau1, int diag_one,
+                                    double* __restrict__ winv, double* __restrict__ minv) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  if (i >= nn || (mask && !mask[i])) {
+    winv[i] = 0.0;
+    minv[i] = 0.0;
+    return;
+  }
+  const double wi = w[i];
+  const double t = __ddiv_rn(tau0, wi);
+  const double v = diag_one ? __dadd_rn(tau1, t) : __dadd_rn(__ddiv_rn(__dmul_rn(tau1, diag[i]), m), t);
+  winv[i] = __ddiv_rn(1.0, wi);
+  minv[i] = __ddiv_rn(1.0, v < 1e-4 ? 1e-4 : v);
+}
+
+void launch_slot_weights(int64_t np, int64_t nn, const double* w, const uint8_t* mask, const double* diag,
+                         double m, double tau0, double tau1, int diag_one, double* winv, double* minv,
+                         cudaStream_t s) {
+  slot_weights_kernel<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(np, nn, w, mask, diag, m, tau0, tau1,
+                                                                   diag_one, winv, minv);
+}

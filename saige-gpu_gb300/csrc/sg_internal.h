@@ -157,6 +157,10 @@ void launch_probe_fill(int64_t np, int64_t nn, uint64_t seed, int64_t run0, int6
 void launch_probe_fill_multi(int64_t np, int64_t nn, const uint64_t* seeds, const int64_t* runs,
                              const int32_t* sel, int64_t k, double* B, cudaStream_t s);
 void launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
+// 1/W and 1/diag(Sigma) of a phenotype slot from W on the device (mask: nullptr = every sample)
+void launch_slot_weights(int64_t np, int64_t nn, const double* w, const uint8_t* mask, const double* diag,
+                         double m, double tau0, double tau1, int diag_one, double* winv, double* minv,
+                         cudaStream_t s);
 void launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s);
 int64_t pcg_nblk(int64_t np);
 constexpr int kProbeDotsMaxP = 16;
