@@ -398,7 +398,6 @@ void launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s) {
   if (n) f32_to_f64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, n);
 }
 
-}  // namespace sg
 
 // A phenotype slot's 1/W and Jacobi preconditioner 1/diag(Sigma) (getDiagOfSigma FIT.cpp:2322-2365:
 // tau1 diagK / M + tau0 / W, or tau1 + tau0 / W with isDiagofKinSetAsOne, floored at 1e-4), zero
@@ -427,3 +426,4 @@ void launch_slot_weights(int64_t np, int64_t nn, const double* w, const uint8_t*
   slot_weights_kernel<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(np, nn, w, mask, diag, m, tau0, tau1,
                                                                    diag_one, winv, minv);
 }
+}  // namespace sg

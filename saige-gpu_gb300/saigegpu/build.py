@@ -63,5 +63,6 @@ def build_lib(force=False, verbose=False, extra_flags=()):
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
-        run([nvcc, *ARCH, "-shared", "-o", LIB, *objs])
+        # every symbol must resolve at link time: a missing definition fails the build, not the load
+        run([nvcc, *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", LIB, *objs])
     return LIB
