@@ -32,7 +32,7 @@ struct Req {
   bool probe = false;
   uint64_t seed = 0;
   int64_t run = 0;
-  std::vector<double> b;
+  double* b = nullptr;  // right-hand side in a pinned slab until admission copies it up
   int state = 0;      // 0 queued, 1 running, 2 done
   int64_t col = -1;
   std::vector<double> x;
@@ -62,6 +62,18 @@ struct Engine {
   uint64_t io_h2d = 0, io_d2h = 0;  // bytes through the engine API since the last timing reset
   ColState* h_pin = nullptr;      // pinned mirror for the asynchronous state read-back of a step
   int32_t* h_gcols = nullptr;     // pinned: active columns gathered for the split-BF16 GRM.V
+  // pinned staging: column states for one scatter launch (h_sst / h_scol, n_sst staged), the
+  // admitted columns and probe tables of an admission round, and slabs holding queued
+  // right-hand sides; all copied up asynchronously
+  ColState* h_sst = nullptr;
+  int32_t* h_scol = nullptr;
+  ColState* d_sst = nullptr;
+  int32_t* d_scol = nullptr;
+  int64_t n_sst = 0;
+  int32_t* h_acols = nullptr;
+  unsigned char* h_ptab = nullptr;
+  std::vector<double*> slab_free;
+  std::vector<void*> slab_blocks;
   double* h_stage = nullptr;      // pinned: a slot's W and sample mask on their way up
   double* d_wstage = nullptr;     // their device copy (np doubles + np bytes)
   int32_t* d_gcols = nullptr;
@@ -860,6 +872,17 @@ static void engine_free(sg_ctx* c) {
   if (e.h_stage) cudaFreeHost(e.h_stage);
   e.h_stage = nullptr;
   dev_free_t(c, e.d_wstage);
+  for (void** hp : {reinterpret_cast<void**>(&e.h_sst), reinterpret_cast<void**>(&e.h_scol),
+                    reinterpret_cast<void**>(&e.h_acols), reinterpret_cast<void**>(&e.h_ptab)}) {
+    if (*hp) cudaFreeHost(*hp);
+    *hp = nullptr;
+  }
+  dev_free_t(c, e.d_sst);
+  dev_free_t(c, e.d_scol);
+  e.n_sst = 0;
+  for (void* blk : e.slab_blocks) cudaFreeHost(blk);
+  e.slab_blocks.clear();
+  e.slab_free.clear();
   dev_free_t(c, e.d_gcols);
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
@@ -879,6 +902,8 @@ static void engine_free(sg_ctx* c) {
 // Drop every queued and in-flight request (the blocking drop-ins own the engine); results are
 // copied out at retirement from here on.
 static int apply_releases(sg_ctx* c);
+static void slab_put(Engine& e, Req& r);
+static double* slab_get(sg_ctx* c);
 
 static int engine_clear(sg_ctx* c) {
   Engine& e = c->eng;
@@ -903,6 +928,7 @@ static int engine_clear(sg_ctx* c) {
   e.hi_col = 0;
   e.n_active = 0;
   e.queue.clear();
+  for (auto& kv : e.reqs) slab_put(e, kv.second);
   e.reqs.clear();
   return sync(c);
 }
@@ -949,6 +975,12 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_gcols), max_columns * sizeof(int32_t), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_stage), 2 * np * sizeof(double), cudaHostAllocDefault));
+  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_sst), max_columns * sizeof(ColState), cudaHostAllocDefault));
+  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_scol), max_columns * sizeof(int32_t), cudaHostAllocDefault));
+  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_acols), e.stage_cols * sizeof(int32_t), cudaHostAllocDefault));
+  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_ptab), e.stage_cols * 24, cudaHostAllocDefault));
+  SG_TRY(dev_alloc_t(c, &e.d_sst, (size_t)max_columns));
+  SG_TRY(dev_alloc_t(c, &e.d_scol, (size_t)max_columns));
   SG_TRY(dev_alloc_t(c, &e.d_wstage, (size_t)(2 * np)));
   SG_TRY(dev_alloc_t(c, &e.d_gcols, (size_t)max_columns));
   e.h_st.assign(max_columns, ColState{});
@@ -1030,7 +1062,11 @@ static int engine_submit_common(sg_ctx* c, int64_t slot, int kind, const double*
     r.probe = probe;
     r.seed = seed;
     r.run = run0 + j;
-    if (!probe) r.b.assign(B + j * c->nn, B + (j + 1) * c->nn);
+    if (!probe) {
+      r.b = slab_get(c);
+      if (!r.b) return set_err(c, SG_ERR_NOMEM, "no pinned host memory for a right-hand side");
+      std::memcpy(r.b, B + j * c->nn, c->nn * sizeof(double));
+    }
     if (ids) ids[j] = r.id;
     e.queue.push_back(r.id);
     e.reqs.emplace(r.id, std::move(r));
@@ -1045,6 +1081,50 @@ extern "C" int sg_engine_submit(sg_ctx* c, int64_t slot, int kind, const double*
 extern "C" int sg_engine_submit_probes(sg_ctx* c, int64_t slot, int kind, uint64_t seed, int64_t run0,
                                        int64_t k, int maxiter, double tol, int64_t* ids) {
   return engine_submit_common(c, slot, kind, nullptr, true, seed, run0, k, maxiter, tol, ids);
+}
+
+// Column-state updates go up in one block: stage (col, state) pairs, then flush_states copies them
+// and scatters them into d_st with one launch.  The pinned staging is reused only after the stream
+// has drained past the copy (wait = true, or a later synchronisation on the same stream).
+static void stage_state(Engine& e, int64_t col, const ColState& st) {
+  e.h_sst[e.n_sst] = st;
+  e.h_scol[e.n_sst] = (int32_t)col;
+  ++e.n_sst;
+}
+
+static int flush_states(sg_ctx* c, bool wait) {
+  Engine& e = c->eng;
+  if (e.n_sst == 0) return SG_OK;
+  const int64_t n = e.n_sst;
+  e.n_sst = 0;
+  SG_CUDA(c, cudaMemcpyAsync(e.d_sst, e.h_sst, n * sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(c, cudaMemcpyAsync(e.d_scol, e.h_scol, n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  e.io_h2d += (uint64_t)(n * (sizeof(ColState) + sizeof(int32_t)));
+  launch_scatter_states(e.d_sst, e.d_scol, n, e.d_st, c->stream);
+  SG_LAUNCHED(c, 1);
+  return wait ? sync(c) : SG_OK;
+}
+
+// Pinned slabs of nn doubles for queued right-hand sides (grown 32 at a time, kept until the
+// engine is freed).
+static double* slab_get(sg_ctx* c) {
+  Engine& e = c->eng;
+  if (e.slab_free.empty()) {
+    constexpr int64_t kPer = 32;
+    void* blk = nullptr;
+    if (cudaHostAlloc(&blk, (size_t)(kPer * c->nn) * sizeof(double), cudaHostAllocDefault) != cudaSuccess)
+      return nullptr;
+    e.slab_blocks.push_back(blk);
+    for (int64_t k = 0; k < kPer; ++k) e.slab_free.push_back(static_cast<double*>(blk) + k * c->nn);
+  }
+  double* p = e.slab_free.back();
+  e.slab_free.pop_back();
+  return p;
+}
+
+static void slab_put(Engine& e, Req& r) {
+  if (r.b) e.slab_free.push_back(r.b);
+  r.b = nullptr;
 }
 
 // Move queued requests into free columns, staged through e.B, and initialise them.
@@ -1072,7 +1152,7 @@ static int engine_admit(sg_ctx* c) {
         pruns.push_back(r.run);
         psel.push_back((int32_t)sel);
       } else {
-        SG_CUDA(c, h2d(c, e.B + sel * e.np, r.b.data(), c->nn * 8, c->stream));
+        SG_CUDA(c, h2d(c, e.B + sel * e.np, r.b, c->nn * 8, c->stream));  // pinned: asynchronous
         if (e.np > c->nn)
           SG_CUDA(c, cudaMemsetAsync(e.B + sel * e.np + c->nn, 0, (e.np - c->nn) * 8, c->stream));
       }
@@ -1082,7 +1162,7 @@ static int engine_admit(sg_ctx* c) {
       s.maxiter = r.maxiter;
       s.tol = r.tol;
       e.h_st[col] = s;
-      SG_CUDA(c, h2d(c, e.d_st + col, &e.h_st[col], sizeof(ColState), c->stream));
+      stage_state(e, col, s);
       e.col_req[col] = id;
       r.col = col;
       r.state = 1;
@@ -1092,20 +1172,26 @@ static int engine_admit(sg_ctx* c) {
       ++col;
     }
     if (cols.empty()) break;
+    SG_TRY(flush_states(c, false));  // the round's closing synchronisation frees the staging
     if (!psel.empty()) {
       // one launch for every probe of this admission round; its index table (uint64 seeds |
-      // int64 runs | int32 rows, at most stage_cols entries) lives in e.ptab
+      // int64 runs | int32 rows, at most stage_cols entries) is staged in pinned memory, then e.ptab
       const size_t kp = psel.size();
+      uint64_t* h_seeds = reinterpret_cast<uint64_t*>(e.h_ptab);
+      int64_t* h_runs = reinterpret_cast<int64_t*>(h_seeds + kp);
+      int32_t* h_sel = reinterpret_cast<int32_t*>(h_runs + kp);
+      std::memcpy(h_seeds, pseeds.data(), kp * 8);
+      std::memcpy(h_runs, pruns.data(), kp * 8);
+      std::memcpy(h_sel, psel.data(), kp * 4);
+      SG_CUDA(c, h2d(c, e.ptab, e.h_ptab, kp * 20, c->stream));
       uint64_t* d_seeds = reinterpret_cast<uint64_t*>(e.ptab);
       int64_t* d_runs = reinterpret_cast<int64_t*>(d_seeds + kp);
       int32_t* d_sel = reinterpret_cast<int32_t*>(d_runs + kp);
-      SG_CUDA(c, h2d(c, d_seeds, pseeds.data(), kp * 8, c->stream));
-      SG_CUDA(c, h2d(c, d_runs, pruns.data(), kp * 8, c->stream));
-      SG_CUDA(c, h2d(c, d_sel, psel.data(), kp * 4, c->stream));
       launch_probe_fill_multi(e.np, c->nn, d_seeds, d_runs, d_sel, (int64_t)kp, e.B, c->stream);
       c->launches += 1;
     }
-    SG_CUDA(c, h2d(c, e.d_cols, cols.data(), cols.size() * 4, c->stream));
+    std::memcpy(e.h_acols, cols.data(), cols.size() * 4);
+    SG_CUDA(c, h2d(c, e.d_cols, e.h_acols, cols.size() * 4, c->stream));
     launch_pcg_init(e.np, e.cap_cols, e.d_cols, (int64_t)cols.size(), e.d_st, e.d_ph, e.minv, e.B,
                     e.X, e.R, e.Z, e.P, e.Pf, e.part, e.nblk, c->stream);
     SG_LAUNCHED(c, 2);
@@ -1117,8 +1203,12 @@ static int engine_admit(sg_ctx* c) {
                                      cudaMemcpyDeviceToDevice, c->stream));
       }
     }
-    // staging buffer is reused by the next batch: wait for init to read it
+    // staging buffers are reused by the next batch: wait for init to read them
     SG_TRY(sync(c));
+    for (int64_t id : admitted) {
+      auto it = e.reqs.find(id);
+      if (it != e.reqs.end()) slab_put(e, it->second);
+    }
     e.n_active += (int64_t)cols.size();
     if ((int64_t)cols.size() < e.stage_cols) break;
   }
@@ -1300,12 +1390,13 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
       s.kind = -2;  // held: result stays in X[col]
       s.active = 0;
       s.just_done = 0;
-      SG_CUDA(c, h2d(c, e.d_st + col, &s, sizeof(ColState), c->stream));
+      stage_state(e, col, s);
     } else {
       SG_TRY(release_col(c, col));
     }
   }
   while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
+  SG_TRY(flush_states(c, false));
   SG_TRY(sync(c));
   *n_finished += fin;
   return SG_OK;
@@ -1341,12 +1432,13 @@ static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
     if (e.hold && it != e.reqs.end()) {
       s.kind = -2;
       s.just_done = 0;
-      SG_CUDA(c, h2d(c, e.d_st + col, &s, sizeof(ColState), c->stream));
+      stage_state(e, col, s);
     } else {
       SG_TRY(release_col(c, col));
     }
   }
   while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
+  SG_TRY(flush_states(c, false));
   return sync(c);
 }
 
@@ -1438,12 +1530,11 @@ static int apply_releases(sg_ctx* c) {
   for (int64_t col : e.pending_release) {
     if (e.col_req[col] != -1) continue;  // reused since: admission initialises it
     e.h_st[col] = s;
-    // pageable source: the call returns once the bytes are staged
-    SG_CUDA(c, h2d(c, e.d_st + col, &s, sizeof(ColState), c->stream));
+    stage_state(e, col, s);
     SG_CUDA(c, cudaMemsetAsync(e.Pf + col * e.np, 0, e.np * 4, c->stream));
   }
   e.pending_release.clear();
-  return SG_OK;
+  return flush_states(c, true);  // admission stages into the same buffer next
 }
 
 extern "C" int sg_engine_fetch(sg_ctx* c, int64_t id, double* x, int32_t* iters) {
@@ -1475,6 +1566,7 @@ extern "C" int sg_engine_cancel(sg_ctx* c, int64_t id) {
     if (r.state == 1) e.n_active -= 1;
     SG_TRY(release_col(c, r.col));
   }
+  slab_put(e, r);
   e.reqs.erase(it);  // a queued id is skipped at admission
   return SG_OK;
 }

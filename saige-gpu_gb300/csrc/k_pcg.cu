@@ -426,4 +426,17 @@ void launch_slot_weights(int64_t np, int64_t nn, const double* w, const uint8_t*
   slot_weights_kernel<<<(unsigned)((np + 255) / 256), 256, 0, s>>>(np, nn, w, mask, diag, m, tau0, tau1,
                                                                    diag_one, winv, minv);
 }
+
+// d_st[cols[k]] = src[k]: column states staged by the host in one block
+__global__ void scatter_states_kernel(const ColState* __restrict__ src, const int32_t* __restrict__ cols,
+                                      int64_t n, ColState* __restrict__ dst) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[cols[k]] = src[k];
+}
+
+void launch_scatter_states(const ColState* src, const int32_t* cols, int64_t n, ColState* dst, cudaStream_t s) {
+  if (n <= 0) return;
+  scatter_states_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(src, cols, n, dst);
+}
+
 }  // namespace sg
