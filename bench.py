@@ -69,7 +69,8 @@ def parse():
     ap.add_argument("--driver", default="native", choices=["native", "python"],
                     help="fit driver: C++ (sg_fits_*) or the Python generators of saigegpu.serve")
     ap.add_argument("--workers", type=int, default=None,
-                    help="host threads running the fits' driver math (default 1)")
+                    help="host threads for the fits' driver math (default: native driver half the cores, "
+                         "at most 8; Python driver 1)")
     ap.add_argument("--blocking-runner", action="store_true",
                     help="step the engine synchronously instead of overlapping the driver with the next step")
     ap.add_argument("--serve-requests", type=int, default=32,
@@ -186,7 +187,7 @@ def run_batch(ctx, specs, cols, pipelined=True, workers=None, driver="native"):
     from saigegpu import native, serve
     t0 = time.perf_counter()
     if driver == "native":
-        res, jobs = native.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined)
+        res, jobs = native.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined, threads=workers)
     else:
         res, jobs = serve.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined, workers=workers)
     wall = time.perf_counter() - t0
@@ -256,7 +257,7 @@ def serving_block(ctx, args, cols):
     if args.driver == "native":
         from saigegpu import native
         done = native.serve(ctx, arrivals, max_columns=cols, max_phenos=max(4, args.phenos),
-                            pipelined=not args.blocking_runner)
+                            pipelined=not args.blocking_runner, threads=args.workers)
     else:
         done = serve.serve(ctx, arrivals, max_columns=cols, max_phenos=max(4, args.phenos),
                            pipelined=not args.blocking_runner, workers=args.workers)
@@ -444,7 +445,8 @@ def run_ours(args, rank, world, local):
                    "value_basis": "device-busy time of engine steps (CUDA events)",
                    "runner": "blocking" if args.blocking_runner else "pipelined",
                    "driver": args.driver,
-                   "driver_threads": args.workers if args.workers is not None else 1},
+                   "driver_threads": args.workers if args.workers is not None else (
+                       "half the cores, at most 8" if args.driver == "native" else 1)},
         "e2e": {"value": round(e2e, 2), "unit": "fits/hr", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "latency_s": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3)},
         "gpu_launches": int(launches),

@@ -20,7 +20,8 @@ def _p(a, t):
 class NativeFits:
     """One ``sg_fits`` driver over a context's engine."""
 
-    def __init__(self, ctx, max_columns, max_fits, pipelined=True):
+    def __init__(self, ctx, max_columns, max_fits, pipelined=True, threads=None):
+        """threads: host threads for the fits' arithmetic (None: half the cores, at most 8)."""
         self.ctx = ctx
         self._L = L.load()
         h = C.c_void_p()
@@ -29,6 +30,8 @@ class NativeFits:
             raise L.SaigeGpuError(rc, ctx.last_error())
         self._h = h
         self.specs = {}
+        if threads is not None:
+            self._check(self._L.sg_fits_set_threads(self._h, int(threads)))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -115,11 +118,11 @@ class _Job:
         self.host_times = {}
 
 
-def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True):
+def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True, threads=None):
     """Fit all ``specs`` together in native code; returns (results or exceptions, jobs) in order."""
     from .serve import columns_for
     max_columns = max(max_columns or 0, columns_for(specs))
-    drv = NativeFits(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined)
+    drv = NativeFits(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined, threads)
     try:
         jobs = {}
         for s in specs:
@@ -148,10 +151,11 @@ def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True):
     return out, [jobs[f] for f in order]
 
 
-def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter, pipelined=True):
+def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter, pipelined=True,
+          threads=None):
     """Serve (t_arrival_seconds, FitSpec) requests with the native driver; returns the finished jobs
     (t_arrive / t_start / t_done) in completion order."""
-    drv = NativeFits(ctx, max_columns, max_phenos, pipelined)
+    drv = NativeFits(ctx, max_columns, max_phenos, pipelined, threads)
     pending = sorted(arrivals, key=lambda a: a[0])
     jobs, finished = {}, []
     t0 = clock()
