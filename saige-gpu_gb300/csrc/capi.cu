@@ -32,7 +32,8 @@ struct Req {
   bool probe = false;
   uint64_t seed = 0;
   int64_t run = 0;
-  double* b = nullptr;  // right-hand side in a pinned slab until admission copies it up
+  double* b = nullptr;        // right-hand side in a pinned slab until admission copies it up
+  const double* bd = nullptr; // the slab's device address (mapped pinned memory)
   int state = 0;      // 0 queued, 1 running, 2 done
   int64_t col = -1;
   std::vector<double> x;
@@ -72,7 +73,7 @@ struct Engine {
   int64_t n_sst = 0;
   int32_t* h_acols = nullptr;
   unsigned char* h_ptab = nullptr;
-  std::vector<double*> slab_free;
+  std::vector<std::pair<double*, const double*>> slab_free;  // (host, device) addresses
   std::vector<void*> slab_blocks;
   double* h_stage = nullptr;      // pinned: a slot's W and sample mask on their way up
   double* d_wstage = nullptr;     // their device copy (np doubles + np bytes)
@@ -903,7 +904,7 @@ static void engine_free(sg_ctx* c) {
 // copied out at retirement from here on.
 static int apply_releases(sg_ctx* c);
 static void slab_put(Engine& e, Req& r);
-static double* slab_get(sg_ctx* c);
+static bool slab_get(sg_ctx* c, Req& r);
 
 static int engine_clear(sg_ctx* c) {
   Engine& e = c->eng;
@@ -958,7 +959,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   SG_TRY(dev_alloc_t(c, &e.Pf, V)); SG_TRY(dev_alloc_t(c, &e.Yf, V));
   SG_TRY(dev_alloc_t(c, &e.B, (size_t)(e.stage_cols * np)));
   SG_TRY(dev_alloc_t(c, &e.part, (size_t)(max_columns * e.nblk * 2)));
-  SG_TRY(dev_alloc_t(c, &e.ptab, (size_t)(e.stage_cols * 24)));
+  SG_TRY(dev_alloc_t(c, &e.ptab, (size_t)(e.stage_cols * 36)));  // probe tables | RHS pointers and rows
   SG_TRY(dev_alloc_t(c, &e.winv, (size_t)(max_phenos * np)));
   SG_TRY(dev_alloc_t(c, &e.minv, (size_t)(max_phenos * np)));
   SG_TRY(dev_alloc_t(c, &e.d_st, (size_t)max_columns));
@@ -978,7 +979,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_sst), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_scol), max_columns * sizeof(int32_t), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_acols), e.stage_cols * sizeof(int32_t), cudaHostAllocDefault));
-  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_ptab), e.stage_cols * 24, cudaHostAllocDefault));
+  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_ptab), e.stage_cols * 36, cudaHostAllocDefault));
   SG_TRY(dev_alloc_t(c, &e.d_sst, (size_t)max_columns));
   SG_TRY(dev_alloc_t(c, &e.d_scol, (size_t)max_columns));
   SG_TRY(dev_alloc_t(c, &e.d_wstage, (size_t)(2 * np)));
@@ -1063,8 +1064,7 @@ static int engine_submit_common(sg_ctx* c, int64_t slot, int kind, const double*
     r.seed = seed;
     r.run = run0 + j;
     if (!probe) {
-      r.b = slab_get(c);
-      if (!r.b) return set_err(c, SG_ERR_NOMEM, "no pinned host memory for a right-hand side");
+      if (!slab_get(c, r)) return set_err(c, SG_ERR_NOMEM, "no pinned host memory for a right-hand side");
       std::memcpy(r.b, B + j * c->nn, c->nn * sizeof(double));
     }
     if (ids) ids[j] = r.id;
@@ -1100,31 +1100,39 @@ static int flush_states(sg_ctx* c, bool wait) {
   SG_CUDA(c, cudaMemcpyAsync(e.d_sst, e.h_sst, n * sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
   SG_CUDA(c, cudaMemcpyAsync(e.d_scol, e.h_scol, n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
   e.io_h2d += (uint64_t)(n * (sizeof(ColState) + sizeof(int32_t)));
-  launch_scatter_states(e.d_sst, e.d_scol, n, e.d_st, c->stream);
+  launch_scatter_states(e.d_sst, e.d_scol, n, e.d_st, e.Pf, e.np, c->stream);
   SG_LAUNCHED(c, 1);
   return wait ? sync(c) : SG_OK;
 }
 
-// Pinned slabs of nn doubles for queued right-hand sides (grown 32 at a time, kept until the
-// engine is freed).
-static double* slab_get(sg_ctx* c) {
+// Pinned, device-mapped slabs of nn doubles for queued right-hand sides (grown 32 at a time, kept
+// until the engine is freed); admission's gather kernel reads them through their device address.
+static bool slab_get(sg_ctx* c, Req& r) {
   Engine& e = c->eng;
   if (e.slab_free.empty()) {
     constexpr int64_t kPer = 32;
     void* blk = nullptr;
-    if (cudaHostAlloc(&blk, (size_t)(kPer * c->nn) * sizeof(double), cudaHostAllocDefault) != cudaSuccess)
-      return nullptr;
+    if (cudaHostAlloc(&blk, (size_t)(kPer * c->nn) * sizeof(double), cudaHostAllocMapped) != cudaSuccess)
+      return false;
+    void* dblk = nullptr;
+    if (cudaHostGetDevicePointer(&dblk, blk, 0) != cudaSuccess) {
+      cudaFreeHost(blk);
+      return false;
+    }
     e.slab_blocks.push_back(blk);
-    for (int64_t k = 0; k < kPer; ++k) e.slab_free.push_back(static_cast<double*>(blk) + k * c->nn);
+    for (int64_t k = 0; k < kPer; ++k)
+      e.slab_free.emplace_back(static_cast<double*>(blk) + k * c->nn, static_cast<const double*>(dblk) + k * c->nn);
   }
-  double* p = e.slab_free.back();
+  r.b = e.slab_free.back().first;
+  r.bd = e.slab_free.back().second;
   e.slab_free.pop_back();
-  return p;
+  return true;
 }
 
 static void slab_put(Engine& e, Req& r) {
-  if (r.b) e.slab_free.push_back(r.b);
+  if (r.b) e.slab_free.emplace_back(r.b, r.bd);
   r.b = nullptr;
+  r.bd = nullptr;
 }
 
 // Move queued requests into free columns, staged through e.B, and initialise them.
@@ -1137,6 +1145,8 @@ static int engine_admit(sg_ctx* c) {
     std::vector<uint64_t> pseeds;
     std::vector<int64_t> pruns;
     std::vector<int32_t> psel;
+    std::vector<const double*> rsrc;
+    std::vector<int32_t> rsel;
     int64_t col = 0;
     while (!e.queue.empty() && (int64_t)cols.size() < e.stage_cols) {
       while (col < e.cap_cols && e.col_req[col] != -1) ++col;
@@ -1152,9 +1162,8 @@ static int engine_admit(sg_ctx* c) {
         pruns.push_back(r.run);
         psel.push_back((int32_t)sel);
       } else {
-        SG_CUDA(c, h2d(c, e.B + sel * e.np, r.b, c->nn * 8, c->stream));  // pinned: asynchronous
-        if (e.np > c->nn)
-          SG_CUDA(c, cudaMemsetAsync(e.B + sel * e.np + c->nn, 0, (e.np - c->nn) * 8, c->stream));
+        rsrc.push_back(r.bd);  // read by the gather kernel straight from mapped pinned host memory
+        rsel.push_back((int32_t)sel);
       }
       ColState s{};
       s.pheno = (int32_t)r.slot;
@@ -1173,6 +1182,19 @@ static int engine_admit(sg_ctx* c) {
     }
     if (cols.empty()) break;
     SG_TRY(flush_states(c, false));  // the round's closing synchronisation frees the staging
+    if (!rsrc.empty()) {
+      // explicit right-hand sides: pointer and row tables staged behind the probe tables
+      const size_t kr = rsrc.size();
+      unsigned char* hb = e.h_ptab + e.stage_cols * 24;
+      std::memcpy(hb, rsrc.data(), kr * sizeof(void*));
+      std::memcpy(hb + kr * sizeof(void*), rsel.data(), kr * 4);
+      unsigned char* db = reinterpret_cast<unsigned char*>(e.ptab) + e.stage_cols * 24;
+      SG_CUDA(c, h2d(c, db, hb, kr * (sizeof(void*) + 4), c->stream));
+      launch_gather_rhs(reinterpret_cast<const double* const*>(db), reinterpret_cast<const int32_t*>(db + kr * sizeof(void*)),
+                        (int64_t)kr, c->nn, e.np, e.B, c->stream);
+      SG_LAUNCHED(c, 1);
+      e.io_h2d += (uint64_t)(kr * c->nn * 8);
+    }
     if (!psel.empty()) {
       // one launch for every probe of this admission round; its index table (uint64 seeds |
       // int64 runs | int32 rows, at most stage_cols entries) is staged in pinned memory, then e.ptab
@@ -1530,8 +1552,7 @@ static int apply_releases(sg_ctx* c) {
   for (int64_t col : e.pending_release) {
     if (e.col_req[col] != -1) continue;  // reused since: admission initialises it
     e.h_st[col] = s;
-    stage_state(e, col, s);
-    SG_CUDA(c, cudaMemsetAsync(e.Pf + col * e.np, 0, e.np * 4, c->stream));
+    stage_state(e, col, s);  // the scatter also zeroes the column's P
   }
   e.pending_release.clear();
   return flush_states(c, true);  // admission stages into the same buffer next

@@ -427,16 +427,41 @@ void launch_slot_weights(int64_t np, int64_t nn, const double* w, const uint8_t*
                                                                    diag_one, winv, minv);
 }
 
-// d_st[cols[k]] = src[k]: column states staged by the host in one block
+// d_st[cols[k]] = src[k]: column states staged by the host in one block; a column set free
+// (kind -1) also gets a zero FP32 direction, so padding columns of a GRM.V pass contribute nothing.
+// One block per staged column.
 __global__ void scatter_states_kernel(const ColState* __restrict__ src, const int32_t* __restrict__ cols,
-                                      int64_t n, ColState* __restrict__ dst) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) dst[cols[k]] = src[k];
+                                      int64_t n, ColState* __restrict__ dst, float* __restrict__ Pf, int64_t np) {
+  const int64_t k = blockIdx.x;
+  if (k >= n) return;
+  const ColState st = src[k];
+  const int64_t c = cols[k];
+  if (threadIdx.x == 0) dst[c] = st;
+  if (Pf && st.kind == -1)
+    for (int64_t i = threadIdx.x; i < np; i += blockDim.x) Pf[c * np + i] = 0.0f;
 }
 
-void launch_scatter_states(const ColState* src, const int32_t* cols, int64_t n, ColState* dst, cudaStream_t s) {
+void launch_scatter_states(const ColState* src, const int32_t* cols, int64_t n, ColState* dst, float* Pf,
+                           int64_t np, cudaStream_t s) {
   if (n <= 0) return;
-  scatter_states_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(src, cols, n, dst);
+  scatter_states_kernel<<<(unsigned)n, 256, 0, s>>>(src, cols, n, dst, Pf, np);
+}
+
+// Right-hand sides of an admission round: column sel[k] of B (np rows) = the nn values at host
+// address src[k] (pinned and mapped), zero past nn.  One block per column.
+__global__ void gather_rhs_kernel(const double* const* __restrict__ src, const int32_t* __restrict__ sel,
+                                  int64_t n, int64_t nn, int64_t np, double* __restrict__ B) {
+  const int64_t k = blockIdx.x;
+  if (k >= n) return;
+  const double* x = src[k];
+  double* b = B + (int64_t)sel[k] * np;
+  for (int64_t i = threadIdx.x; i < np; i += blockDim.x) b[i] = i < nn ? x[i] : 0.0;
+}
+
+void launch_gather_rhs(const double* const* src, const int32_t* sel, int64_t n, int64_t nn, int64_t np, double* B,
+                       cudaStream_t s) {
+  if (n <= 0) return;
+  gather_rhs_kernel<<<(unsigned)n, 256, 0, s>>>(src, sel, n, nn, np, B);
 }
 
 }  // namespace sg

@@ -157,8 +157,12 @@ void launch_probe_fill(int64_t np, int64_t nn, uint64_t seed, int64_t run0, int6
 void launch_probe_fill_multi(int64_t np, int64_t nn, const uint64_t* seeds, const int64_t* runs,
                              const int32_t* sel, int64_t k, double* B, cudaStream_t s);
 void launch_f64_to_f32(const double* a, float* b, int64_t n, cudaStream_t s);
-// d_st[cols[k]] = src[k] for k < n
-void launch_scatter_states(const ColState* src, const int32_t* cols, int64_t n, ColState* dst, cudaStream_t s);
+// d_st[cols[k]] = src[k] for k < n; with Pf, columns set free (kind -1) also get P = 0
+void launch_scatter_states(const ColState* src, const int32_t* cols, int64_t n, ColState* dst, float* Pf,
+                           int64_t np, cudaStream_t s);
+// B[:, sel[k]] = the nn doubles at mapped pinned host address src[k], zero-padded to np
+void launch_gather_rhs(const double* const* src, const int32_t* sel, int64_t n, int64_t nn, int64_t np, double* B,
+                       cudaStream_t s);
 // 1/W and 1/diag(Sigma) of a phenotype slot from W on the device (mask: nullptr = every sample)
 void launch_slot_weights(int64_t np, int64_t nn, const double* w, const uint8_t* mask, const double* diag,
                          double m, double tau0, double tau1, int diag_one, double* winv, double* minv,
