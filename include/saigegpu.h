@@ -287,6 +287,10 @@ int sg_engine_stats(sg_ctx *ctx, int64_t *stats4);
  * [3]=algorithmic GEMM FLOPs over the columns processed (2 n^2 each), [4]=columns processed,
  * [5]=occupied (useful) columns processed */
 int sg_engine_timing(sg_ctx *ctx, double *t6);
+/* Device time between the end of one engine step and the start of the next (CUDA events), summed
+ * since the last sg_engine_reset_timing: the GPU idling while the host admits, retires and
+ * prepares work.  No reference counterpart. */
+int sg_engine_idle_ms(sg_ctx *ctx, double *ms);
 int sg_engine_reset_timing(sg_ctx *ctx);
 /* Bytes copied host->device and device->host by the engine calls (right-hand sides, weights,
  * probe tables, column states, fetched results, probe reductions) since the last
@@ -331,10 +335,10 @@ int sg_fits_run(sg_fits *fits, int64_t max_steps, int64_t *n_ready);
 int sg_fits_set_threads(sg_fits *fits, int threads);
 int sg_fits_poll(sg_fits *fits, int64_t *ids, int64_t max_ids, int64_t *n_out);
 int sg_fits_counts(sg_fits *fits, int64_t *active, int64_t *pending, int64_t *done);
-/* t7: seconds in engine steps (launch / finish / poll), seconds of driver work, steps, and the
- * parts of the driver work spent in weight uploads, submissions, result copies and probe
- * reductions */
-int sg_fits_host_times(sg_fits *fits, double *t7);
+/* t8: seconds in engine steps (launch / finish / poll), seconds of driver work, steps, the parts of
+ * the driver work spent in weight uploads, submissions, result copies and probe reductions, and
+ * the part of the engine time spent launching steps */
+int sg_fits_host_times(sg_fits *fits, double *t8);
 int sg_fits_result(sg_fits *fits, int64_t fit_id, double *theta, double *alpha, double *eta, double *mu,
                    double *Y, double *cov, int32_t *iterations, int32_t *converged,
                    int64_t *column_iterations);

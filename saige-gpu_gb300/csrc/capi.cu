@@ -93,6 +93,9 @@ struct Engine {
   std::vector<std::vector<std::pair<uint64_t, int64_t>>> pcache_key;  // per slot: (seed, run) per entry
   size_t dots_cap_sx = 0, dots_cap_part = 0, dots_cap_cols = 0;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_prev[3] = {nullptr, nullptr, nullptr};  // the previous step's (swapped per launch)
+  bool have_prev = false;  // ev_prev holds a finished step whose end the idle time counts from
+  double t_idle_ms = 0.0;  // device idle time between consecutive steps
   double t_step_ms = 0, t_gemm_ms = 0, gemm_launches = 0, gemm_flops = 0, gemm_cols = 0, useful_cols = 0;
 };
 
@@ -973,6 +976,9 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   e.cap_ph = max_phenos;
   for (auto& ev : e.ev)
     if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
+  for (auto& ev : e.ev_prev)
+    if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
+  e.have_prev = false;
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_gcols), max_columns * sizeof(int32_t), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_stage), 2 * np * sizeof(double), cudaHostAllocDefault));
@@ -1335,6 +1341,7 @@ static int step_launch(sg_ctx* c) {
   for (int64_t col = 0; col < e.hi_col; ++col) occupied += e.h_st[col].active ? 1 : 0;
   bool yf = true;
   int64_t launched = ncols;
+  std::swap(e.ev, e.ev_prev);  // keep the last step's events for the idle time before this one
   SG_CUDA(c, cudaEventRecord(e.ev[0], c->stream));
   SG_TRY(engine_gemm(c, ncols, &yf, &launched));
   SG_CUDA(c, cudaEventRecord(e.ev[1], c->stream));
@@ -1368,9 +1375,12 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
   }
   const int64_t ncols = e.inflight_ncols, occupied = e.inflight_occupied, hi = e.inflight_hi;
   {
-    float ms_gemm = 0.f, ms_step = 0.f;
+    float ms_gemm = 0.f, ms_step = 0.f, ms_idle = 0.f;
     cudaEventElapsedTime(&ms_gemm, e.ev[0], e.ev[1]);
     cudaEventElapsedTime(&ms_step, e.ev[0], e.ev[2]);
+    if (e.have_prev && cudaEventElapsedTime(&ms_idle, e.ev_prev[2], e.ev[0]) == cudaSuccess && ms_idle > 0.f)
+      e.t_idle_ms += ms_idle;
+    e.have_prev = true;
     e.t_gemm_ms += ms_gemm;
     e.t_step_ms += ms_step;
     const int64_t launched_cols = c->mv_mode == SG_MV_FP64_PLAIN ? occupied : ncols;
@@ -1736,9 +1746,17 @@ extern "C" int sg_engine_timing(sg_ctx* c, double* t) {
   return SG_OK;
 }
 
+extern "C" int sg_engine_idle_ms(sg_ctx* c, double* ms) {
+  if (!c || !ms) return SG_ERR_INVALID;
+  *ms = c->eng.t_idle_ms;
+  return SG_OK;
+}
+
 extern "C" int sg_engine_reset_timing(sg_ctx* c) {
   if (!c) return SG_ERR_INVALID;
   Engine& e = c->eng;
+  e.t_idle_ms = 0.0;
+  e.have_prev = false;
   e.t_step_ms = e.t_gemm_ms = e.gemm_launches = e.gemm_flops = e.gemm_cols = e.useful_cols = 0;
   e.io_h2d = e.io_d2h = 0;
   return SG_OK;

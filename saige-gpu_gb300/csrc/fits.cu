@@ -186,6 +186,7 @@ struct sg_fits {
   std::string err;
   double t_engine = 0, t_host = 0;
   double t_pheno = 0, t_submit = 0, t_fetch = 0, t_dots = 0;  // parts of t_host spent in engine calls
+  double t_launch = 0;                                          // part of t_engine spent launching
   double gpu_ms_seen = 0;                                      // engine step time already budgeted
   int64_t steps = 0;
   std::mutex mu;               // engine calls and the bookkeeping above, from the worker threads
@@ -882,7 +883,9 @@ static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
     if (rc == SG_OK && F->pipelined) {
       rc = F->launched ? sg_engine_finish(F->ctx, &fin) : SG_OK;
       int launched = 0;
+      const double tl = now_s();
       if (rc == SG_OK) rc = sg_engine_launch(F->ctx, &fin2, &launched);
+      F->t_launch += now_s() - tl;
       F->launched = launched != 0;
     } else if (rc == SG_OK) {
       rc = sg_engine_run(F->ctx, 1, &fin);
@@ -982,15 +985,16 @@ extern "C" int sg_fits_counts(sg_fits* F, int64_t* active, int64_t* pending, int
   return SG_OK;
 }
 
-extern "C" int sg_fits_host_times(sg_fits* F, double* t7) {
-  if (!F || !t7) return SG_ERR_INVALID;
-  t7[0] = F->t_engine;
-  t7[1] = F->t_host;
-  t7[2] = (double)F->steps;
-  t7[3] = F->t_pheno;
-  t7[4] = F->t_submit;
-  t7[5] = F->t_fetch;
-  t7[6] = F->t_dots;
+extern "C" int sg_fits_host_times(sg_fits* F, double* t8) {
+  if (!F || !t8) return SG_ERR_INVALID;
+  t8[0] = F->t_engine;
+  t8[1] = F->t_host;
+  t8[2] = (double)F->steps;
+  t8[3] = F->t_pheno;
+  t8[4] = F->t_submit;
+  t8[5] = F->t_fetch;
+  t8[6] = F->t_dots;
+  t8[7] = F->t_launch;
   return SG_OK;
 }
 

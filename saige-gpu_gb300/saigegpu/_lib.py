@@ -103,6 +103,7 @@ SIGNATURES = {
                              P_i32],
     "sg_engine_timing": [c_ctx, P_f64],
     "sg_engine_io_bytes": [c_ctx, P_u64, P_u64],
+    "sg_engine_idle_ms": [c_ctx, P_f64],
     "sg_engine_reset_timing": [c_ctx],
     "sg_synth_bed": [c_ctx, c_u64, c_i64, c_i64, C.c_double, C.POINTER(C.c_void_p), P_u64],
     "sg_synth_bed_to_host": [c_ctx, P_u8, c_u64],

@@ -507,6 +507,12 @@ class Context:
     def engine_reset_timing(self):
         self._call("sg_engine_reset_timing")
 
+    def engine_idle_ms(self):
+        """Device idle milliseconds between consecutive engine steps since the last timing reset."""
+        v = C.c_double()
+        self._call("sg_engine_idle_ms", C.byref(v))
+        return v.value
+
     def engine_io_bytes(self):
         """(host->device, device->host) bytes moved by engine calls since the last timing reset."""
         a, b = C.c_uint64(), C.c_uint64()

@@ -85,10 +85,10 @@ class NativeFits:
 
     def host_times(self):
         """Seconds: engine stepping, driver work (and its pheno / submit / fetch / probe_dots parts)."""
-        t = np.zeros(7)
+        t = np.zeros(8)
         self._check(self._L.sg_fits_host_times(self._h, t.ctypes.data_as(L.P_f64)))
         return {"engine": t[0], "driver": t[1], "steps": int(t[2]), "pheno": t[3], "submit": t[4],
-                "fetch": t[5], "probe_dots": t[6]}
+                "fetch": t[5], "probe_dots": t[6], "launch": t[7]}
 
     def result(self, fid):
         """(result dict, column iterations); the dict has the keys of ``serve.fit_generator``'s."""
