@@ -71,6 +71,8 @@ struct Engine {
   ColState* d_sst = nullptr;
   int32_t* d_scol = nullptr;
   int64_t n_sst = 0;
+  std::vector<int32_t> stage_idx;  // column -> its entry in the current staging batch, or -1
+  std::vector<int64_t> slab_pending;  // admitted requests whose slabs return once the stream drains
   int32_t* h_acols = nullptr;
   unsigned char* h_ptab = nullptr;
   std::vector<std::pair<double*, const double*>> slab_free;  // (host, device) addresses
@@ -987,6 +989,8 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_acols), e.stage_cols * sizeof(int32_t), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_ptab), e.stage_cols * 36, cudaHostAllocDefault));
   SG_TRY(dev_alloc_t(c, &e.d_sst, (size_t)max_columns));
+  e.stage_idx.assign(max_columns, -1);
+  e.slab_pending.clear();
   SG_TRY(dev_alloc_t(c, &e.d_scol, (size_t)max_columns));
   SG_TRY(dev_alloc_t(c, &e.d_wstage, (size_t)(2 * np)));
   SG_TRY(dev_alloc_t(c, &e.d_gcols, (size_t)max_columns));
@@ -1093,6 +1097,12 @@ extern "C" int sg_engine_submit_probes(sg_ctx* c, int64_t slot, int kind, uint64
 // and scatters them into d_st with one launch.  The pinned staging is reused only after the stream
 // has drained past the copy (wait = true, or a later synchronisation on the same stream).
 static void stage_state(Engine& e, int64_t col, const ColState& st) {
+  int32_t& at = e.stage_idx[col];
+  if (at >= 0) {  // staged earlier in this batch (released, then admitted again): the last state wins
+    e.h_sst[at] = st;
+    return;
+  }
+  at = (int32_t)e.n_sst;
   e.h_sst[e.n_sst] = st;
   e.h_scol[e.n_sst] = (int32_t)col;
   ++e.n_sst;
@@ -1103,6 +1113,7 @@ static int flush_states(sg_ctx* c, bool wait) {
   if (e.n_sst == 0) return SG_OK;
   const int64_t n = e.n_sst;
   e.n_sst = 0;
+  for (int64_t k = 0; k < n; ++k) e.stage_idx[e.h_scol[k]] = -1;
   SG_CUDA(c, cudaMemcpyAsync(e.d_sst, e.h_sst, n * sizeof(ColState), cudaMemcpyHostToDevice, c->stream));
   SG_CUDA(c, cudaMemcpyAsync(e.d_scol, e.h_scol, n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
   e.io_h2d += (uint64_t)(n * (sizeof(ColState) + sizeof(int32_t)));
@@ -1144,8 +1155,24 @@ static void slab_put(Engine& e, Req& r) {
 // Move queued requests into free columns, staged through e.B, and initialise them.
 static int engine_admit(sg_ctx* c) {
   Engine& e = c->eng;
+  // the previous admission's copies have run (the stream drained at the last finish / sync)
+  for (int64_t id : e.slab_pending) {
+    auto it = e.reqs.find(id);
+    if (it != e.reqs.end()) slab_put(e, it->second);
+  }
+  e.slab_pending.clear();
   SG_TRY(apply_releases(c));
+  bool synced_round = false;
   while (!e.queue.empty()) {
+    if (synced_round) {  // a second round reuses the staging buffers and e.B: wait for the first
+      SG_TRY(sync(c));
+      for (int64_t id : e.slab_pending) {
+        auto it = e.reqs.find(id);
+        if (it != e.reqs.end()) slab_put(e, it->second);
+      }
+      e.slab_pending.clear();
+    }
+    synced_round = true;
     std::vector<int32_t> cols;
     std::vector<int64_t> admitted;
     std::vector<uint64_t> pseeds;
@@ -1176,8 +1203,12 @@ static int engine_admit(sg_ctx* c) {
       s.kind = r.kind;
       s.maxiter = r.maxiter;
       s.tol = r.tol;
-      e.h_st[col] = s;
       stage_state(e, col, s);
+      // the device decides at init whether the column iterates; until the step's states come back
+      // the host counts it as active (the GRM.V then includes it; a column that converged at init
+      // is skipped by the vector kernels and retired when the step finishes)
+      e.h_st[col] = s;
+      e.h_st[col].active = 1;
       e.col_req[col] = id;
       r.col = col;
       r.state = 1;
@@ -1231,16 +1262,12 @@ static int engine_admit(sg_ctx* c) {
                                      cudaMemcpyDeviceToDevice, c->stream));
       }
     }
-    // staging buffers are reused by the next batch: wait for init to read them
-    SG_TRY(sync(c));
-    for (int64_t id : admitted) {
-      auto it = e.reqs.find(id);
-      if (it != e.reqs.end()) slab_put(e, it->second);
-    }
+    // the staging buffers and slabs are reused only after the stream has drained past init
+    e.slab_pending.insert(e.slab_pending.end(), admitted.begin(), admitted.end());
     e.n_active += (int64_t)cols.size();
     if ((int64_t)cols.size() < e.stage_cols) break;
   }
-  return SG_OK;
+  return flush_states(c, false);  // releases with no admission round after them
 }
 
 static int loco_correct(sg_ctx* c, int64_t ncols, bool yf);
@@ -1400,7 +1427,7 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
     if (id < 0) continue;
     ColState& s = e.h_st[col];
     if (s.kind == -2) continue;  // finished earlier, result held in X[col]
-    e.col_iters += 1;
+    if (s.active || s.iter > 0 || s.kind == 1) e.col_iters += 1;  // not the ones that converged at init
     if (s.active) continue;
     auto it = e.reqs.find(id);
     if (it != e.reqs.end()) {
@@ -1516,7 +1543,8 @@ extern "C" int sg_engine_launch(sg_ctx* c, int64_t* n_finished, int* launched) {
   int64_t fin = 0;
   if (launched) *launched = 0;
   SG_TRY(engine_admit(c));
-  SG_TRY(engine_retire_immediate(c, &fin));
+  // no read-back of the fresh columns here: ones that converged at init retire when this step
+  // finishes, so the launch path never waits for the device
   if (n_finished) *n_finished = fin;
   if (e.n_active == 0) {
     if (!e.queue.empty() && fin == 0)
@@ -1562,10 +1590,10 @@ static int apply_releases(sg_ctx* c) {
   for (int64_t col : e.pending_release) {
     if (e.col_req[col] != -1) continue;  // reused since: admission initialises it
     e.h_st[col] = s;
-    stage_state(e, col, s);  // the scatter also zeroes the column's P
+    stage_state(e, col, s);  // the scatter also zeroes the column's P; admission flushes the batch
   }
   e.pending_release.clear();
-  return flush_states(c, true);  // admission stages into the same buffer next
+  return SG_OK;
 }
 
 extern "C" int sg_engine_fetch(sg_ctx* c, int64_t id, double* x, int32_t* iters) {

@@ -31,6 +31,7 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -436,25 +437,35 @@ cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap
   return cudaGetLastError();
 }
 
+// Tile table of one GEMM call site: built on the host, staged in pinned memory and copied up
+// asynchronously (the launching stream drains before the table is rebuilt: every caller
+// synchronises on its result before the next call).
 struct TileCache {
   std::vector<TileCoord> host;
   TileCoord* dev = nullptr;
+  TileCoord* pinned = nullptr;
   size_t cap = 0;
 };
 
 cudaError_t upload_tiles(TileCache& tc, cudaStream_t s) {
   if (tc.host.size() > tc.cap) {
     if (tc.dev) cudaFree(tc.dev);
-    tc.cap = tc.host.size();
-    cudaError_t e = cudaMalloc(&tc.dev, tc.cap * sizeof(TileCoord));
+    if (tc.pinned) cudaFreeHost(tc.pinned);
+    tc.dev = nullptr;
+    tc.pinned = nullptr;
+    tc.cap = 0;
+    cudaError_t e = cudaMalloc(&tc.dev, tc.host.size() * sizeof(TileCoord));
+    if (e == cudaSuccess) e = cudaHostAlloc(&tc.pinned, tc.host.size() * sizeof(TileCoord), cudaHostAllocDefault);
     if (e != cudaSuccess) {
+      if (tc.dev) cudaFree(tc.dev);
       tc.dev = nullptr;
-      tc.cap = 0;
+      tc.pinned = nullptr;
       return e;
     }
+    tc.cap = tc.host.size();
   }
-  return cudaMemcpyAsync(tc.dev, tc.host.data(), tc.host.size() * sizeof(TileCoord),
-                         cudaMemcpyHostToDevice, s);
+  std::memcpy(tc.pinned, tc.host.data(), tc.host.size() * sizeof(TileCoord));
+  return cudaMemcpyAsync(tc.dev, tc.pinned, tc.host.size() * sizeof(TileCoord), cudaMemcpyHostToDevice, s);
 }
 
 cudaError_t check_error_flag(cudaStream_t s) {
