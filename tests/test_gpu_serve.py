@@ -210,3 +210,44 @@ def test_native_driver_failing_fit_and_serving(cohort):
     arrivals = [(0.01 * i, specs[i % len(specs)]) for i in range(5)]
     done = native.serve(ctx, arrivals, max_columns=256, max_phenos=2)
     assert len(done) == 5 and all(j.error is None for j in done)
+
+
+def test_launch_finish_retires_columns_that_converge_at_init(cohort):
+    """With asynchronous stepping a zero right-hand side (r'r = 0 at init) is retired when the step
+    it rode along finishes: zero iterations, zero solution; the other columns are unaffected."""
+    ctx, grm, specs, refs = cohort
+    n = ctx.n
+    rng = np.random.default_rng(12)
+    w = rng.uniform(0.5, 2.0, n)
+    tau = np.array([1.0, 0.4])
+    B = rng.standard_normal((n, 3))
+    B[:, 1] = 0.0
+    ctx.engine_reserve(128, 2)
+    ctx.engine_hold_results(True)
+    try:
+        ctx.engine_set_pheno(0, w, tau)
+        ids = [int(i) for i in ctx.engine_submit(0, 0, B, 500, 1e-10)]
+        got = {}
+        for _ in range(2000):
+            if len(got) == 3:
+                break
+            ctx.engine_launch()
+            ctx.engine_finish()
+            for rid in ctx.engine_poll():
+                got[int(rid)] = ctx.engine_fetch(int(rid))
+        assert set(got) == set(ids)
+        x0, it0 = got[ids[1]]
+        assert it0 == 0 and not np.any(x0)
+        ctx.engine_hold_results(False)
+        ref = {}
+        ids2 = [int(i) for i in ctx.engine_submit(0, 0, B[:, [0, 2]], 500, 1e-10)]
+        for _ in range(2000):
+            if len(ref) == 2:
+                break
+            ctx.engine_run(1)
+            for rid in ctx.engine_poll():
+                ref[int(rid)] = ctx.engine_fetch(int(rid))[0]
+        np.testing.assert_array_equal(got[ids[0]][0], ref[ids2[0]])
+        np.testing.assert_array_equal(got[ids[2]][0], ref[ids2[1]])
+    finally:
+        ctx.engine_hold_results(False)
