@@ -917,7 +917,9 @@ static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
     if (F->pipelined && F->launched) {
       double tm[6] = {0, 0, 0, 0, 0, 0};
       if (sg_engine_timing(F->ctx, tm) == SG_OK) {
-        if (tm[0] >= F->gpu_ms_seen && F->gpu_ms_seen > 0) budget = (tm[0] - F->gpu_ms_seen) * 1e-3;
+        // 70%: fits already started finish past the deadline, and the next finish should not
+        // find the GPU idle
+        if (tm[0] >= F->gpu_ms_seen && F->gpu_ms_seen > 0) budget = 0.7 * (tm[0] - F->gpu_ms_seen) * 1e-3;
         F->gpu_ms_seen = tm[0];
       }
     }
