@@ -1,6 +1,6 @@
 """Benchmark: null-model fits/hr at N=100k on a resident GRM (batched mixed precision).
 
-Workload (BASELINE config "batching form", with the "precision form"'s cohort):
+Workload (the batching form of the metric, on the precision form's cohort):
 N = 100,000 samples x M = 150,000 markers synthetic cohort (p ~ U(0.01,0.5),
 HWE genotypes, 2% missing; seed 1003), GRM built once on the GPU (decode ->
 BF16 standardised genotypes -> tcgen05 SYRK, FP32 K resident in HBM).  One

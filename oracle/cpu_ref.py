@@ -1,6 +1,6 @@
 """Build and call oracle/cpu_ref.c: the reference's CPU GRM.x and FP32 PCG restated in C.
 
-TEST / BASELINE INFRASTRUCTURE ONLY (the ``cpu_baseline`` and ``--impl
+TEST / CPU-BASELINE INFRASTRUCTURE ONLY (the ``cpu_baseline`` and ``--impl
 reference`` legs of bench.py).  Built with gcc -O3 -fopenmp into
 oracle/_build/; portable C (no -march flags), so it builds on x86 and Arm.
 """

@@ -98,7 +98,7 @@ struct Fit {
 
 // Host threads for the fits' arithmetic: run(count, fn) calls fn(0..count-1) on the pool and the
 // calling thread and returns when every call has returned.  Each worker makes the context's GPU
-// current once (the engine calls it makes run under the driver's lock).
+// current once (the engine calls it makes run under the fit driver's lock).
 class Pool {
  public:
   Pool(int workers, sg_ctx* ctx) {
@@ -292,7 +292,7 @@ void fail(sg_fits* F, Fit& f, int code, const std::string& msg) {
   }
 }
 
-// One engine call (and whatever bookkeeping fn does with its result) under the driver's lock.
+// One engine call (and whatever bookkeeping fn does with its result) under the fit driver's lock.
 template <typename Fn>
 bool eng(sg_fits* F, Fit& f, double* timer, Fn fn) {
   std::lock_guard<std::mutex> g(F->mu);
