@@ -407,7 +407,7 @@ def run_ours(args, rank, world, local):
     barrier(world)
     launches = ctx.kernel_launches() - L0
     io_h2d, io_d2h = ctx.engine_io_bytes()
-    idle_s = ctx.engine_idle_ms() / 1e3
+    idle_ms, admit_ms = ctx.engine_idle_ms()
     tdev = ctx.engine_timing()
     dev_s = tdev["step_ms"] / 1e3
     total_wall = sum(walls)
@@ -468,7 +468,8 @@ def run_ours(args, rank, world, local):
                     "converged": int(sum(1 for r in res_all if r["converged"])), "fits": len(res_all)},
         "setup_s": round(setup_s, 1),
         "wall_breakdown_s_per_step": {k: round(v / args.steps, 3) for k, v in host_t.items()},
-        "device_idle_between_steps_s_per_step": round(idle_s / args.steps, 3),
+        "between_steps_s_per_step": {"total": round(idle_ms / 1e3 / args.steps, 3),
+                                     "launch_admission": round(admit_ms / 1e3 / args.steps, 3)},
     }
     if tune_report is not None:
         out["tuning"] = {"clusters_syrk_grmv": list(tune_report["chosen"]),

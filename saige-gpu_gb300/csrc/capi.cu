@@ -97,7 +97,10 @@ struct Engine {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t ev_prev[3] = {nullptr, nullptr, nullptr};  // the previous step's (swapped per launch)
   bool have_prev = false;  // ev_prev holds a finished step whose end the idle time counts from
-  double t_idle_ms = 0.0;  // device idle time between consecutive steps
+  double t_idle_ms = 0.0;  // device time between consecutive steps
+  double t_admit_ms = 0.0; // of which: admission work queued at the launch (state scatter, RHS gather, init)
+  cudaEvent_t ev_adm = nullptr;
+  bool adm_recorded = false;
   double t_step_ms = 0, t_gemm_ms = 0, gemm_launches = 0, gemm_flops = 0, gemm_cols = 0, useful_cols = 0;
 };
 
@@ -980,6 +983,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
     if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
   for (auto& ev : e.ev_prev)
     if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
+  if (!e.ev_adm) SG_CUDA(c, cudaEventCreate(&e.ev_adm));
   e.have_prev = false;
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_gcols), max_columns * sizeof(int32_t), cudaHostAllocDefault));
@@ -1407,6 +1411,10 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
     cudaEventElapsedTime(&ms_step, e.ev[0], e.ev[2]);
     if (e.have_prev && cudaEventElapsedTime(&ms_idle, e.ev_prev[2], e.ev[0]) == cudaSuccess && ms_idle > 0.f)
       e.t_idle_ms += ms_idle;
+    float ms_adm = 0.f;
+    if (e.adm_recorded && cudaEventElapsedTime(&ms_adm, e.ev_adm, e.ev[0]) == cudaSuccess && ms_adm > 0.f)
+      e.t_admit_ms += ms_adm;
+    e.adm_recorded = false;
     e.have_prev = true;
     e.t_gemm_ms += ms_gemm;
     e.t_step_ms += ms_step;
@@ -1542,6 +1550,8 @@ extern "C" int sg_engine_launch(sg_ctx* c, int64_t* n_finished, int* launched) {
   if (e.inflight) return set_err(c, SG_ERR_STATE, "a step is in flight: finish it first");
   int64_t fin = 0;
   if (launched) *launched = 0;
+  SG_CUDA(c, cudaEventRecord(e.ev_adm, c->stream));
+  e.adm_recorded = true;
   SG_TRY(engine_admit(c));
   // no read-back of the fresh columns here: ones that converged at init retire when this step
   // finishes, so the launch path never waits for the device
@@ -1776,7 +1786,8 @@ extern "C" int sg_engine_timing(sg_ctx* c, double* t) {
 
 extern "C" int sg_engine_idle_ms(sg_ctx* c, double* ms) {
   if (!c || !ms) return SG_ERR_INVALID;
-  *ms = c->eng.t_idle_ms;
+  ms[0] = c->eng.t_idle_ms;
+  ms[1] = c->eng.t_admit_ms;
   return SG_OK;
 }
 
@@ -1784,6 +1795,7 @@ extern "C" int sg_engine_reset_timing(sg_ctx* c) {
   if (!c) return SG_ERR_INVALID;
   Engine& e = c->eng;
   e.t_idle_ms = 0.0;
+  e.t_admit_ms = 0.0;
   e.have_prev = false;
   e.t_step_ms = e.t_gemm_ms = e.gemm_launches = e.gemm_flops = e.gemm_cols = e.useful_cols = 0;
   e.io_h2d = e.io_d2h = 0;
