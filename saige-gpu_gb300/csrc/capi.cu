@@ -62,7 +62,8 @@ struct Engine {
   bool hold = false;              // keep finished results on the device until fetched/consumed
   uint64_t io_h2d = 0, io_d2h = 0;  // bytes through the engine API since the last timing reset
   ColState* h_pin = nullptr;      // pinned mirror for the asynchronous state read-back of a step
-  int32_t* h_gcols = nullptr;     // pinned: active columns gathered for the split-BF16 GRM.V
+  int32_t* h_gcols = nullptr;     // pinned: the step's active columns (GRM.V compaction, vector kernels)
+  int64_t nact = 0;
   // pinned staging: column states for one scatter launch (h_sst / h_scol, n_sst staged), the
   // admitted columns and probe tables of an admission round, and slabs holding queued
   // right-hand sides; all copied up asynchronously
@@ -949,6 +950,8 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   if (max_columns > 96) max_columns = round_up(max_columns, 128);
   if (max_columns > 320) max_columns = round_up(max_columns, 256);
   max_phenos = std::max<int64_t>(max_phenos, 1);
+  if (max_columns > 65535)  // one grid row per column in the vector kernels
+    return set_err(c, SG_ERR_INVALID, "at most 65535 engine columns (asked for %lld)", (long long)max_columns);
   if (e.cap_cols >= max_columns && e.cap_ph >= max_phenos && e.np == c->np) return SG_OK;
   for (auto& kv : e.reqs)
     if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "engine busy: cannot grow while columns run");
@@ -1305,9 +1308,7 @@ static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf, int64_t* la
     if (!e.Pb) SG_TRY(dev_alloc(c, &e.Pb, half * 4));
     // only the columns still iterating are multiplied: their P is gathered into a compact block
     // (padded with zero columns to the tile width) and the epilogue scatters Y back by column
-    int64_t nact = 0;
-    for (int64_t col = 0; col < ncols && col < e.cap_cols; ++col)
-      if (e.h_st[col].active) e.h_gcols[nact++] = (int32_t)col;
+    const int64_t nact = e.nact;  // built by step_launch
     if (nact == 0) {
       *launched = 0;
       return SG_OK;
@@ -1366,6 +1367,11 @@ static int64_t engine_gemm_cols(const sg_ctx* c) {
 // Nothing here waits for the device.
 static int step_launch(sg_ctx* c) {
   Engine& e = c->eng;
+  // the step's active columns (host view: admitted columns count as active until their state comes
+  // back); the GRM.V compaction and the vector kernels work on this list only
+  e.nact = 0;
+  for (int64_t col = 0; col < e.hi_col; ++col)
+    if (e.h_st[col].active) e.h_gcols[e.nact++] = (int32_t)col;
   // the split-BF16 engine compacts the active columns itself; the others cover [0, hi_col) padded
   const int64_t ncols = c->mv_mode == SG_MV_BF16X3_TC ? round_up(e.hi_col, 32) : engine_gemm_cols(c);
   int64_t occupied = 0;
@@ -1378,12 +1384,15 @@ static int step_launch(sg_ctx* c) {
   SG_CUDA(c, cudaEventRecord(e.ev[1], c->stream));
   const float* Yf = yf ? e.Yf : nullptr;
   const double* Yd = yf ? nullptr : e.Yd;
-  launch_pcg_sigma_dot(e.np, e.hi_col, e.d_st, e.d_ph, e.winv, e.minv, e.P, Yf, Yd, e.part, e.nblk, c->stream);
-  launch_pcg_alpha(e.hi_col, e.d_st, e.part, e.nblk, c->stream);
-  launch_pcg_update(e.np, e.hi_col, e.d_st, e.d_ph, e.winv, e.minv, e.X, e.R, e.Z, e.P, Yf, Yd,
-                    e.part, e.nblk, c->stream);
-  launch_pcg_beta(e.hi_col, e.d_st, e.part, e.nblk, c->stream);
-  launch_pcg_dir(e.np, e.hi_col, e.d_st, e.Z, e.P, e.Pf, c->stream);
+  if (c->mv_mode != SG_MV_BF16X3_TC && e.nact > 0)  // the split-BF16 GRM.V uploaded the list already
+    SG_CUDA(c, cudaMemcpyAsync(e.d_gcols, e.h_gcols, e.nact * 4, cudaMemcpyHostToDevice, c->stream));
+  launch_pcg_sigma_dot(e.np, e.nact, e.d_st, e.d_ph, e.winv, e.minv, e.P, Yf, Yd, e.part, e.nblk, e.d_gcols,
+                       c->stream);
+  launch_pcg_alpha(e.nact, e.d_st, e.part, e.nblk, e.d_gcols, c->stream);
+  launch_pcg_update(e.np, e.nact, e.d_st, e.d_ph, e.winv, e.minv, e.X, e.R, e.Z, e.P, Yf, Yd,
+                    e.part, e.nblk, e.d_gcols, c->stream);
+  launch_pcg_beta(e.nact, e.d_st, e.part, e.nblk, e.d_gcols, c->stream);
+  launch_pcg_dir(e.np, e.nact, e.d_st, e.Z, e.P, e.Pf, e.d_gcols, c->stream);
   SG_LAUNCHED(c, 5);
   SG_CUDA(c, cudaEventRecord(e.ev[2], c->stream));
   SG_CUDA(c, d2h(c, e.h_pin, e.d_st, e.hi_col * sizeof(ColState), c->stream));

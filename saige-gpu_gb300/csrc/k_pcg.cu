@@ -128,9 +128,10 @@ __global__ void pcg_sigma_dot_kernel(int64_t np, const ColState* __restrict__ st
                                      const PhenoState* __restrict__ ph,
                                      const double* __restrict__ winv, const double* __restrict__ minv,
                                      const double* __restrict__ P, const float* __restrict__ Yf,
-                                     const double* __restrict__ Yd, double* part, int64_t nblk) {
+                                     const double* __restrict__ Yd, double* part, int64_t nblk,
+                                     const int32_t* __restrict__ cols) {
   __shared__ double sh[kThreads / 32];
-  const int64_t c = blockIdx.y;
+  const int64_t c = cols ? cols[blockIdx.y] : blockIdx.y;
   const ColState s = st[c];
   if (s.kind != 0 || !s.active) {
     if (threadIdx.x == 0) part[(c * nblk + blockIdx.x) * 2] = 0.0;
@@ -154,16 +155,17 @@ __global__ void pcg_sigma_dot_kernel(int64_t np, const ColState* __restrict__ st
 void launch_pcg_sigma_dot(int64_t np, int64_t ncols, ColState* st, const PhenoState* ph,
                           const double* winv, const double* minv, const double* P,
                           const float* Yf, const double* Yd, double* part, int64_t nblk,
-                          cudaStream_t s) {
+                          const int32_t* cols, cudaStream_t s) {
   if (ncols == 0) return;
   dim3 grid((unsigned)nblk, (unsigned)ncols);
-  pcg_sigma_dot_kernel<<<grid, kThreads, 0, s>>>(np, st, ph, winv, minv, P, Yf, Yd, part, nblk);
+  pcg_sigma_dot_kernel<<<grid, kThreads, 0, s>>>(np, st, ph, winv, minv, P, Yf, Yd, part, nblk, cols);
 }
 
 __global__ void pcg_alpha_kernel(int64_t ncols, ColState* st, const double* __restrict__ part,
-                                 int64_t nblk) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncols) return;
+                                 int64_t nblk, const int32_t* __restrict__ cols) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ncols) return;
+  const int64_t c = cols ? cols[j] : j;
   ColState s = st[c];
   if (s.kind != 0 || !s.active) {
     s.alpha = 0.0;
@@ -176,9 +178,9 @@ __global__ void pcg_alpha_kernel(int64_t ncols, ColState* st, const double* __re
 }
 
 void launch_pcg_alpha(int64_t ncols, ColState* st, const double* part, int64_t nblk,
-                      cudaStream_t s) {
+                      const int32_t* cols, cudaStream_t s) {
   if (ncols == 0) return;
-  pcg_alpha_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(ncols, st, part, nblk);
+  pcg_alpha_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(ncols, st, part, nblk, cols);
 }
 
 // x += a p; r -= a Ap; z = minv r; partial z'r, r'r.  Product columns copy K b into X.
@@ -186,9 +188,10 @@ __global__ void pcg_update_kernel(int64_t np, const ColState* __restrict__ st,
                                   const PhenoState* __restrict__ ph, const double* __restrict__ winv,
                                   const double* __restrict__ minv, double* X, double* R, double* Z,
                                   const double* __restrict__ P, const float* __restrict__ Yf,
-                                  const double* __restrict__ Yd, double* part, int64_t nblk) {
+                                  const double* __restrict__ Yd, double* part, int64_t nblk,
+                                  const int32_t* __restrict__ cols) {
   __shared__ double sh[kThreads / 32];
-  const int64_t c = blockIdx.y;
+  const int64_t c = cols ? cols[blockIdx.y] : blockIdx.y;
   const ColState s = st[c];
   const int64_t base = c * np;
   const int64_t i0 = (int64_t)blockIdx.x * kChunk;
@@ -235,17 +238,18 @@ __global__ void pcg_update_kernel(int64_t np, const ColState* __restrict__ st,
 void launch_pcg_update(int64_t np, int64_t ncols, ColState* st, const PhenoState* ph,
                        const double* winv, const double* minv, double* X, double* R, double* Z,
                        const double* P, const float* Yf, const double* Yd, double* part,
-                       int64_t nblk, cudaStream_t s) {
+                       int64_t nblk, const int32_t* cols, cudaStream_t s) {
   if (ncols == 0) return;
   dim3 grid((unsigned)nblk, (unsigned)ncols);
-  pcg_update_kernel<<<grid, kThreads, 0, s>>>(np, st, ph, winv, minv, X, R, Z, P, Yf, Yd, part, nblk);
+  pcg_update_kernel<<<grid, kThreads, 0, s>>>(np, st, ph, winv, minv, X, R, Z, P, Yf, Yd, part, nblk, cols);
 }
 
 // beta, iteration count and the stopping rule (sum r^2 <= tol or iter == maxiter)
 __global__ void pcg_beta_kernel(int64_t ncols, ColState* st, const double* __restrict__ part,
-                                int64_t nblk) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncols) return;
+                                int64_t nblk, const int32_t* __restrict__ cols) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ncols) return;
+  const int64_t c = cols ? cols[j] : j;
   ColState s = st[c];
   s.just_done = 0;
   if (s.active) {
@@ -273,15 +277,15 @@ __global__ void pcg_beta_kernel(int64_t ncols, ColState* st, const double* __res
 }
 
 void launch_pcg_beta(int64_t ncols, ColState* st, const double* part, int64_t nblk,
-                     cudaStream_t s) {
+                     const int32_t* cols, cudaStream_t s) {
   if (ncols == 0) return;
-  pcg_beta_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(ncols, st, part, nblk);
+  pcg_beta_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(ncols, st, part, nblk, cols);
 }
 
 // p = z + beta p for columns still iterating; FP32 copy for the next GRM product.
 __global__ void pcg_dir_kernel(int64_t np, const ColState* __restrict__ st, const double* __restrict__ Z,
-                               double* P, float* Pf) {
-  const int64_t c = blockIdx.y;
+                               double* P, float* Pf, const int32_t* __restrict__ cols) {
+  const int64_t c = cols ? cols[blockIdx.y] : blockIdx.y;
   const ColState s = st[c];
   const int64_t base = c * np;
   const int64_t i0 = (int64_t)blockIdx.x * kChunk;
@@ -298,10 +302,10 @@ __global__ void pcg_dir_kernel(int64_t np, const ColState* __restrict__ st, cons
 }
 
 void launch_pcg_dir(int64_t np, int64_t ncols, ColState* st, const double* Z, double* P, float* Pf,
-                    cudaStream_t s) {
+                    const int32_t* cols, cudaStream_t s) {
   if (ncols == 0) return;
   dim3 grid((unsigned)pcg_nblk(np), (unsigned)ncols);
-  pcg_dir_kernel<<<grid, kThreads, 0, s>>>(np, st, Z, P, Pf);
+  pcg_dir_kernel<<<grid, kThreads, 0, s>>>(np, st, Z, P, Pf, cols);
 }
 
 // Rademacher probes of the counter hash (oracle/probes.py): B[j][i] = +-1 for i < nn, 0 after.

@@ -138,20 +138,22 @@ void launch_pcg_init(int64_t np, int64_t ncols, const int32_t* cols, int64_t nco
                      ColState* st, const PhenoState* ph, const double* minv, const double* B,
                      double* X, double* R, double* Z, double* P, float* Pf, double* part,
                      int64_t nblk, cudaStream_t s);
+// The step kernels act on ncols columns: cols[0..ncols) when cols is not null (the active list),
+// else columns 0..ncols-1.
 void launch_pcg_sigma_dot(int64_t np, int64_t ncols, ColState* st, const PhenoState* ph,
                           const double* winv, const double* minv, const double* P,
                           const float* Yf, const double* Yd, double* part, int64_t nblk,
-                          cudaStream_t s);
+                          const int32_t* cols, cudaStream_t s);
 void launch_pcg_alpha(int64_t ncols, ColState* st, const double* part, int64_t nblk,
-                      cudaStream_t s);
+                      const int32_t* cols, cudaStream_t s);
 void launch_pcg_update(int64_t np, int64_t ncols, ColState* st, const PhenoState* ph,
                        const double* winv, const double* minv, double* X, double* R, double* Z,
                        const double* P, const float* Yf, const double* Yd, double* part,
-                       int64_t nblk, cudaStream_t s);
+                       int64_t nblk, const int32_t* cols, cudaStream_t s);
 void launch_pcg_beta(int64_t ncols, ColState* st, const double* part, int64_t nblk,
-                     cudaStream_t s);
+                     const int32_t* cols, cudaStream_t s);
 void launch_pcg_dir(int64_t np, int64_t ncols, ColState* st, const double* Z, double* P,
-                    float* Pf, cudaStream_t s);
+                    float* Pf, const int32_t* cols, cudaStream_t s);
 void launch_probe_fill(int64_t np, int64_t nn, uint64_t seed, int64_t run0, int64_t k,
                        double* B, cudaStream_t s);
 void launch_probe_fill_multi(int64_t np, int64_t nn, const uint64_t* seeds, const int64_t* runs,
