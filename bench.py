@@ -407,7 +407,7 @@ def run_ours(args, rank, world, local):
     barrier(world)
     launches = ctx.kernel_launches() - L0
     io_h2d, io_d2h = ctx.engine_io_bytes()
-    idle_ms, admit_ms = ctx.engine_idle_ms()
+    idle_ms, admit_ms, finish_ms = ctx.engine_idle_ms()
     tdev = ctx.engine_timing()
     dev_s = tdev["step_ms"] / 1e3
     total_wall = sum(walls)
@@ -469,7 +469,8 @@ def run_ours(args, rank, world, local):
         "setup_s": round(setup_s, 1),
         "wall_breakdown_s_per_step": {k: round(v / args.steps, 3) for k, v in host_t.items()},
         "between_steps_s_per_step": {"total": round(idle_ms / 1e3 / args.steps, 3),
-                                     "launch_admission": round(admit_ms / 1e3 / args.steps, 3)},
+                                     "launch_admission": round(admit_ms / 1e3 / args.steps, 3),
+                                     "finish_host": round(finish_ms / 1e3 / args.steps, 3)},
     }
     if tune_report is not None:
         out["tuning"] = {"clusters_syrk_grmv": list(tune_report["chosen"]),

@@ -287,11 +287,11 @@ int sg_engine_stats(sg_ctx *ctx, int64_t *stats4);
  * [3]=algorithmic GEMM FLOPs over the columns processed (2 n^2 each), [4]=columns processed,
  * [5]=occupied (useful) columns processed */
 int sg_engine_timing(sg_ctx *ctx, double *t6);
-/* ms2[0]: device time between the end of one engine step and the start of the next (CUDA events),
- * summed since the last sg_engine_reset_timing; ms2[1]: the part of it from the start of an
+/* ms3[0]: device time between the end of one engine step and the start of the next (CUDA events),
+ * summed since the last sg_engine_reset_timing; ms3[1]: the part of it from the start of an
  * asynchronous launch's admission work (state scatter, right-hand-side gather, column init) to its
- * step.  No reference counterpart. */
-int sg_engine_idle_ms(sg_ctx *ctx, double *ms2);
+ * step; ms3[2]: host time finishes spent after their step had drained.  No reference counterpart. */
+int sg_engine_idle_ms(sg_ctx *ctx, double *ms3);
 int sg_engine_reset_timing(sg_ctx *ctx);
 /* Bytes copied host->device and device->host by the engine calls (right-hand sides, weights,
  * probe tables, column states, fetched results, probe reductions) since the last

@@ -9,6 +9,7 @@
 #include "../../include/saigegpu.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -100,6 +101,7 @@ struct Engine {
   bool have_prev = false;  // ev_prev holds a finished step whose end the idle time counts from
   double t_idle_ms = 0.0;  // device time between consecutive steps
   double t_admit_ms = 0.0; // of which: admission work queued at the launch (state scatter, RHS gather, init)
+  double t_finish_host_ms = 0.0;  // host time a finish spends after the step has drained
   cudaEvent_t ev_adm = nullptr;
   bool adm_recorded = false;
   double t_step_ms = 0, t_gemm_ms = 0, gemm_launches = 0, gemm_flops = 0, gemm_cols = 0, useful_cols = 0;
@@ -1409,6 +1411,7 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
   Engine& e = c->eng;
   e.inflight = false;
   SG_TRY(sync(c));
+  const auto th0 = std::chrono::steady_clock::now();
   if (tc_mode(c->mv_mode)) {
     const cudaError_t err = tc_check_error(c->stream);
     if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 GRM.V: %s", cudaGetErrorString(err));
@@ -1475,6 +1478,7 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
   SG_TRY(flush_states(c, false));
   SG_TRY(sync(c));
   *n_finished += fin;
+  e.t_finish_host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count();
   return SG_OK;
 }
 
@@ -1797,6 +1801,7 @@ extern "C" int sg_engine_idle_ms(sg_ctx* c, double* ms) {
   if (!c || !ms) return SG_ERR_INVALID;
   ms[0] = c->eng.t_idle_ms;
   ms[1] = c->eng.t_admit_ms;
+  ms[2] = c->eng.t_finish_host_ms;
   return SG_OK;
 }
 
@@ -1805,6 +1810,7 @@ extern "C" int sg_engine_reset_timing(sg_ctx* c) {
   Engine& e = c->eng;
   e.t_idle_ms = 0.0;
   e.t_admit_ms = 0.0;
+  e.t_finish_host_ms = 0.0;
   e.have_prev = false;
   e.t_step_ms = e.t_gemm_ms = e.gemm_launches = e.gemm_flops = e.gemm_cols = e.useful_cols = 0;
   e.io_h2d = e.io_d2h = 0;

@@ -508,11 +508,11 @@ class Context:
         self._call("sg_engine_reset_timing")
 
     def engine_idle_ms(self):
-        """(ms between consecutive engine steps, ms of it from launch admission to the step) since
-        the last timing reset."""
-        v = np.zeros(2)
+        """(ms between consecutive engine steps, ms of it from launch admission to the step, host ms
+        of finishes after their step drained) since the last timing reset."""
+        v = np.zeros(3)
         self._call("sg_engine_idle_ms", _ptr(v, L.P_f64))
-        return float(v[0]), float(v[1])
+        return float(v[0]), float(v[1]), float(v[2])
 
     def engine_io_bytes(self):
         """(host->device, device->host) bytes moved by engine calls since the last timing reset."""
