@@ -255,6 +255,10 @@ int sg_engine_run(sg_ctx *ctx, int64_t max_steps, int64_t *n_finished);
  * an in-flight step first. */
 int sg_engine_launch(sg_ctx *ctx, int64_t *n_finished, int *launched);
 int sg_engine_finish(sg_ctx *ctx, int64_t *n_finished);
+/* Block until the launched step has run on the device without finishing it.  Unlike every other
+ * engine call it need not be serialised with the calls other threads make (the thread that
+ * launches and finishes steps calls it); a device error is reported by the next sg_engine_finish. */
+int sg_engine_wait(sg_ctx *ctx);
 /* By default a finished column's result is copied to the host and its column freed at once.
  * With hold != 0 finished results stay on the device (keeping their column) until fetched,
  * cancelled or consumed by sg_engine_probe_dots; sg_engine_run then fails with SG_ERR_STATE
@@ -331,14 +335,18 @@ int sg_fits_submit(sg_fits *fits, int trait, int64_t n_sub, const uint8_t *mask,
                    double tol, int maxiter, int nrun, double tol_pcg, int maxiter_pcg, double cv_cutoff,
                    uint64_t seed, int64_t *fit_id);
 int sg_fits_run(sg_fits *fits, int64_t max_steps, int64_t *n_ready);
-/* Host threads (the caller's included) for the fits' arithmetic; engine calls stay serialised.
- * Default: half the hardware threads, at most 8. */
+/* Host threads for the fits' arithmetic; engine calls stay serialised.  threads > 1 (pipelined
+ * drivers): threads - 1 workers resume fits while the calling thread steps the engine, launching
+ * each step as soon as the last one has run, and sg_fits_run may return with workers still
+ * resuming fits.  threads = 1: the calling thread alternates stepping and resuming.  Default: half
+ * the hardware threads, at most 8. */
 int sg_fits_set_threads(sg_fits *fits, int threads);
 int sg_fits_poll(sg_fits *fits, int64_t *ids, int64_t max_ids, int64_t *n_out);
 int sg_fits_counts(sg_fits *fits, int64_t *active, int64_t *pending, int64_t *done);
-/* t8: seconds in engine steps (launch / finish / poll), seconds of driver work, steps, the parts of
- * the driver work spent in weight uploads, submissions, result copies and probe reductions, and
- * the part of the engine time spent launching steps */
+/* t8: seconds in engine steps (launch / finish / poll, and with worker threads the wait for the
+ * step), seconds of driver work (summed over the worker threads when there are any), steps, the
+ * parts of the driver work spent in weight uploads, submissions, result copies and probe
+ * reductions, and the part of the engine time spent launching steps */
 int sg_fits_host_times(sg_fits *fits, double *t8);
 int sg_fits_result(sg_fits *fits, int64_t fit_id, double *theta, double *alpha, double *eta, double *mu,
                    double *Y, double *cov, int32_t *iterations, int32_t *converged,

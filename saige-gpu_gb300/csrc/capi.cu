@@ -1589,6 +1589,16 @@ extern "C" int sg_engine_finish(sg_ctx* c, int64_t* n_finished) {
   return SG_OK;
 }
 
+// Block until the step in flight has run on the device, without finishing it.  It reads only the
+// in-flight flag (written by launch and finish) and records no error, so the thread that launches
+// and finishes steps may wait here while other threads make engine calls; a device error surfaces
+// in the sg_engine_finish that follows.
+extern "C" int sg_engine_wait(sg_ctx* c) {
+  if (!c) return SG_ERR_INVALID;
+  if (c->eng.inflight) (void)cudaStreamSynchronize(c->stream);
+  return SG_OK;
+}
+
 // Free a column (running or holding a result) for the next admission.  The host bookkeeping is
 // immediate; the device-side reset (state, zero P) waits for the next launch, so a release never
 // queues behind a step in flight.

@@ -94,36 +94,45 @@ struct Fit {
   FitError err;
   bool converged = false;
   int64_t ready_at = -1;  // scheduler step at which every awaited column was done
+  bool started = false;   // main_start has run
+  bool busy = false;      // handed to a worker thread (only the stepping thread reads or writes it)
+  int64_t reserved = 0;   // engine columns set aside at admission until main_start has submitted
 };
 
-// Host threads for the fits' arithmetic: run(count, fn) calls fn(0..count-1) on the pool and the
-// calling thread and returns when every call has returned.  Each worker makes the context's GPU
-// current once (the engine calls it makes run under the fit driver's lock).
-class Pool {
+// Host threads that resume fits.  The thread that steps the engine hands a fit over (push) and
+// takes it back once the fit waits for columns again (take_done): a fit is in the hands of one
+// thread at a time.  Each worker makes the context's GPU current once (the engine calls it makes
+// run under the fit driver's lock).
+class Workers {
  public:
-  Pool(int workers, sg_ctx* ctx) {
+  Workers(int workers, sg_ctx* ctx, std::function<void(Fit&)> fn) : fn_(std::move(fn)) {
     for (int w = 0; w < workers; ++w)
       th_.emplace_back([this, ctx] {
         sg_ctx_make_current(ctx);
-        uint64_t seen = 0;
         for (;;) {
+          Fit* f = nullptr;
           {
             std::unique_lock<std::mutex> lk(m_);
-            cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+            cv_.wait(lk, [&] { return stop_ || !q_.empty(); });
             if (stop_) return;
-            seen = gen_;
-            ++busy_;
+            f = q_.front();
+            q_.pop_front();
+            ++running_;
           }
-          work();
+          const double t = now_s();
+          fn_(*f);
           {
             std::lock_guard<std::mutex> lk(m_);
-            --busy_;
+            --running_;
+            busy_s_ += now_s() - t;
+            done_.push_back(f);
           }
           done_cv_.notify_all();
         }
       });
   }
-  ~Pool() {
+  // Fits still queued are dropped; call wait_idle first to keep them.
+  ~Workers() {
     {
       std::lock_guard<std::mutex> lk(m_);
       stop_ = true;
@@ -131,41 +140,38 @@ class Pool {
     cv_.notify_all();
     for (auto& t : th_) t.join();
   }
-  int size() const { return (int)th_.size() + 1; }
-  void run(int64_t count, const std::function<void(int64_t)>& fn) {
-    if (count <= 0) return;
+  void push(const std::vector<Fit*>& fits) {
+    if (fits.empty()) return;
     {
       std::lock_guard<std::mutex> lk(m_);
-      fn_ = &fn;
-      count_ = count;
-      next_.store(0);
-      finished_.store(0);
-      ++gen_;
+      q_.insert(q_.end(), fits.begin(), fits.end());
     }
     cv_.notify_all();
-    work();
+  }
+  // Appends the fits resumed since the last call.
+  void take_done(std::vector<Fit*>& out) {
+    std::lock_guard<std::mutex> lk(m_);
+    out.insert(out.end(), done_.begin(), done_.end());
+    done_.clear();
+  }
+  void wait_idle() {
     std::unique_lock<std::mutex> lk(m_);
-    done_cv_.wait(lk, [&] { return finished_.load() == count_ && busy_ == 0; });
-    fn_ = nullptr;
+    done_cv_.wait(lk, [&] { return q_.empty() && running_ == 0; });
+  }
+  double busy_seconds() {
+    std::lock_guard<std::mutex> lk(m_);
+    return busy_s_;
   }
 
  private:
-  void work() {
-    for (;;) {
-      const int64_t i = next_.fetch_add(1);
-      if (i >= count_) return;
-      (*fn_)(i);
-      if (finished_.fetch_add(1) + 1 == count_) done_cv_.notify_all();
-    }
-  }
+  std::function<void(Fit&)> fn_;
   std::vector<std::thread> th_;
   std::mutex m_;
   std::condition_variable cv_, done_cv_;
-  const std::function<void(int64_t)>* fn_ = nullptr;
-  int64_t count_ = 0;
-  std::atomic<int64_t> next_{0}, finished_{0};
-  uint64_t gen_ = 0;
-  int busy_ = 0;
+  std::deque<Fit*> q_;
+  std::vector<Fit*> done_;
+  int running_ = 0;
+  double busy_s_ = 0.0;
   bool stop_ = false;
 };
 
@@ -183,14 +189,15 @@ struct sg_fits {
   std::unordered_map<int64_t, int64_t> owner;        // request id -> fit id
   std::unordered_set<int64_t> done_reqs;
   int64_t next_id = 1, inflight_columns = 0;
+  int64_t reserved_columns = 0;  // sum of Fit::reserved
   std::string err;
   double t_engine = 0, t_host = 0;
   double t_pheno = 0, t_submit = 0, t_fetch = 0, t_dots = 0;  // parts of t_host spent in engine calls
   double t_launch = 0;                                          // part of t_engine spent launching
   double gpu_ms_seen = 0;                                      // engine step time already budgeted
   int64_t steps = 0;
-  std::mutex mu;               // engine calls and the bookkeeping above, from the worker threads
-  std::unique_ptr<Pool> pool;  // null: the fits' arithmetic runs on the calling thread
+  std::mutex mu;                  // engine calls and the bookkeeping above, from the worker threads
+  std::unique_ptr<Workers> pool;  // null: the fits' arithmetic runs on the calling thread
 };
 
 namespace {
@@ -730,12 +737,35 @@ bool resume(sg_fits* F, Fit& f) {
   }
 }
 
-bool is_ready(sg_fits* F, const Fit& f) {
+// Every awaited column is done (the caller holds F->mu).
+bool ready_locked(sg_fits* F, const Fit& f) {
   if (f.stage == S_NONE) return false;
-  std::lock_guard<std::mutex> g(F->mu);
   for (int64_t id : f.wait_ids)
     if (!F->done_reqs.count(id)) return false;
   return true;
+}
+
+bool is_ready(sg_fits* F, const Fit& f) {
+  if (f.stage == S_NONE) return false;
+  std::lock_guard<std::mutex> g(F->mu);
+  return ready_locked(F, f);
+}
+
+// Start the fit if it has not started, then resume it until it waits for columns still running
+// (or finishes, or fails).  On a worker thread or the calling thread; the fit is this thread's.
+void advance(sg_fits* F, Fit& f) {
+  try {
+    if (!f.started) {
+      f.started = true;
+      if (!main_start(F, f) || f.failed || f.phase == P_DONE) return;
+    }
+    while (is_ready(F, f)) {
+      f.ready_at = -1;
+      if (!resume(F, f) || f.failed || f.phase == P_DONE) break;
+    }
+  } catch (const std::exception& ex) {
+    fail(F, f, SG_ERR_NOMEM, std::string("fit driver: ") + ex.what());
+  }
 }
 
 // A finished or failed fit: cancel its outstanding requests, free its slot, queue it for polling.
@@ -744,35 +774,97 @@ void retire(sg_fits* F, int64_t fid) {
   if (it == F->active.end()) return;
   std::unique_ptr<Fit> f = std::move(it->second);
   F->active.erase(it);
-  std::vector<int64_t> mine;
-  for (const auto& kv : F->owner)
-    if (kv.second == fid) mine.push_back(kv.first);
-  for (int64_t id : mine) {
-    sg_engine_cancel(F->ctx, id);
-    F->owner.erase(id);
-    if (!F->done_reqs.erase(id)) F->inflight_columns -= 1;
+  {
+    std::lock_guard<std::mutex> g(F->mu);
+    std::vector<int64_t> mine;
+    for (const auto& kv : F->owner)
+      if (kv.second == fid) mine.push_back(kv.first);
+    for (int64_t id : mine) {
+      sg_engine_cancel(F->ctx, id);
+      F->owner.erase(id);
+      if (!F->done_reqs.erase(id)) F->inflight_columns -= 1;
+    }
   }
+  F->reserved_columns -= f->reserved;
+  f->reserved = 0;
   F->free_slots.push_back(f->slot);
   F->finished_order.push_back(fid);
   F->done_fits[fid] = std::move(f);
 }
 
+// Retire the fits no worker holds that finished or failed; returns how many.
+int64_t retire_finished(sg_fits* F) {
+  std::vector<int64_t> out;
+  for (const auto& kv : F->active) {
+    const Fit& f = *kv.second;
+    if (!f.busy && (f.failed || f.phase == P_DONE)) out.push_back(kv.first);
+  }
+  for (int64_t fid : out) retire(F, fid);
+  return (int64_t)out.size();
+}
+
+// Take back the fits the workers are done with.
+void take_back(sg_fits* F) {
+  if (!F->pool) return;
+  std::vector<Fit*> back;
+  F->pool->take_done(back);
+  for (Fit* f : back) {
+    f->busy = false;
+    F->reserved_columns -= f->reserved;
+    f->reserved = 0;
+  }
+}
+
+// Admit queued fits while slots and engine columns last.  With workers the fits start there (their
+// columns are reserved until they have submitted); without, here.
 void admit(sg_fits* F) {
-  while (!F->pending.empty() && !F->free_slots.empty() &&
-         F->inflight_columns + need_columns(*F->pending.front()) <= F->max_columns) {
+  std::vector<Fit*> starts;
+  while (!F->pending.empty() && !F->free_slots.empty()) {
+    int64_t inflight;
+    {
+      std::lock_guard<std::mutex> g(F->mu);
+      inflight = F->inflight_columns;
+    }
+    if (inflight + F->reserved_columns + need_columns(*F->pending.front()) > F->max_columns) break;
     std::unique_ptr<Fit> f = std::move(F->pending.front());
     F->pending.pop_front();
     f->slot = F->free_slots.back();
     F->free_slots.pop_back();
-    sg_engine_probe_cache_clear(F->ctx, f->slot);  // a new sample mask takes this slot
+    {
+      std::lock_guard<std::mutex> g(F->mu);
+      sg_engine_probe_cache_clear(F->ctx, f->slot);  // a new sample mask takes this slot
+    }
     const int64_t fid = f->id;
     Fit& ref = *f;
     F->active[fid] = std::move(f);
+    if (F->pool) {
+      ref.reserved = need_columns(ref);
+      F->reserved_columns += ref.reserved;
+      ref.busy = true;
+      starts.push_back(&ref);
+      continue;
+    }
     const double t = now_s();
-    const bool ok = main_start(F, ref);
+    advance(F, ref);
     F->t_host += now_s() - t;
-    if (!ok || ref.failed || ref.phase == P_DONE) retire(F, fid);
+    if (ref.failed || ref.phase == P_DONE) retire(F, fid);
   }
+  if (F->pool) F->pool->push(starts);
+}
+
+// Mark the requests the engine finished as done (the caller holds F->mu or runs alone).
+int poll_done(sg_fits* F) {
+  int64_t ids[1024];
+  int64_t got = 0;
+  do {
+    const int rc = sg_engine_poll(F->ctx, ids, 1024, &got);
+    if (rc != SG_OK) return rc;
+    for (int64_t q = 0; q < got; ++q) {
+      if (!F->owner.count(ids[q])) continue;
+      if (F->done_reqs.insert(ids[q]).second) F->inflight_columns -= 1;
+    }
+  } while (got == 1024);
+  return SG_OK;
 }
 
 }  // namespace
@@ -796,19 +888,28 @@ extern "C" int sg_fits_create(sg_ctx* ctx, int64_t max_columns, int64_t max_fits
   for (int64_t s = max_fits - 1; s >= 0; --s) F->free_slots.push_back(s);
   const unsigned hw = std::thread::hardware_concurrency();
   const int workers = (int)std::min<unsigned>(7u, hw > 2 ? hw / 2 - 1 : 0u);
-  if (workers > 0) F->pool.reset(new Pool(workers, ctx));
+  if (workers > 0) F->pool.reset(new Workers(workers, ctx, [F](Fit& f) { advance(F, f); }));
   *out = F;
   return SG_OK;
 }
 
 extern "C" int sg_fits_set_threads(sg_fits* F, int threads) {
   if (!F || threads < 1) return SG_ERR_INVALID;
-  F->pool.reset(threads > 1 ? new Pool(threads - 1, F->ctx) : nullptr);
+  if (F->pool) {  // let the current workers finish what they hold
+    F->pool->wait_idle();
+    take_back(F);
+    F->t_host += F->pool->busy_seconds();
+  }
+  F->pool.reset(threads > 1 ? new Workers(threads - 1, F->ctx, [F](Fit& f) { advance(F, f); }) : nullptr);
   return SG_OK;
 }
 
 extern "C" void sg_fits_destroy(sg_fits* F) {
   if (!F) return;
+  if (F->pool) {
+    F->pool->wait_idle();
+    F->pool.reset();
+  }
   if (F->launched) {
     int64_t fin = 0;
     sg_engine_finish(F->ctx, &fin);
@@ -871,11 +972,22 @@ static int fits_submit_impl(sg_fits* F, int trait, int64_t n_sub, const uint8_t*
   return SG_OK;
 }
 
-static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
-  if (!F) return SG_ERR_INVALID;
-  const size_t before = F->finished_order.size();
+static int engine_error(sg_fits* F, int rc) {
+  const char* m = sg_last_error(F->ctx);
+  return fits_err(F, rc, "engine step: %s", m ? m : "error");
+}
+
+// The calling thread alternates: step the engine (launch the next step, then work on the last
+// one's results, or one blocking step), then resume the fits whose columns are done -- on the
+// workers when there are any, waiting for them.
+static int run_sync(sg_fits* F, int64_t max_steps, size_t before) {
   for (int64_t s = 0; s < max_steps; ++s) {
     admit(F);
+    if (F->pool) {
+      F->pool->wait_idle();
+      take_back(F);
+      retire_finished(F);
+    }
     if (F->active.empty() && F->pending.empty()) break;
     double t = now_s();
     int64_t fin = 0, fin2 = 0, st0[4] = {0, 0, 0, 0}, st1[4] = {0, 0, 0, 0};
@@ -891,40 +1003,27 @@ static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
       rc = sg_engine_run(F->ctx, 1, &fin);
     }
     if (rc == SG_OK) rc = sg_engine_stats(F->ctx, st1);
+    if (rc == SG_OK) rc = poll_done(F);
+    if (rc != SG_OK) return engine_error(F, rc);
     fin += fin2;
     const bool stepped = F->pipelined ? F->launched : st1[0] > st0[0];
-    if (rc != SG_OK) {
-      const char* m = sg_last_error(F->ctx);
-      return fits_err(F, rc, "engine step: %s", m ? m : "error");
-    }
-    std::vector<int64_t> ids(4096);
-    int64_t got = 0;
-    do {
-      rc = sg_engine_poll(F->ctx, ids.data(), (int64_t)ids.size(), &got);
-      if (rc != SG_OK) return fits_err(F, rc, "engine poll failed");
-      for (int64_t q = 0; q < got; ++q) {
-        if (!F->owner.count(ids[q])) continue;
-        if (F->done_reqs.insert(ids[q]).second) F->inflight_columns -= 1;
-      }
-    } while (got == (int64_t)ids.size());
     F->t_engine += now_s() - t;
     F->steps += 1;
-    // Resume the fits whose awaited columns are done, oldest first.  While a step runs, work for
-    // about as long as the previous step took on the GPU and leave the rest for the next one: fits
-    // that started together reach their stage changes together, and doing all of that host work
-    // at once would leave the GPU idle.
+    // Resume the fits whose awaited columns are done, oldest first.  Alone, while a step runs,
+    // work for about as long as the previous step took on the GPU and leave the rest for the next
+    // one: fits that started together reach their stage changes together, and doing all of that
+    // host work at once would leave the GPU idle.
     double budget = -1.0;
-    if (F->pipelined && F->launched) {
+    if (F->pipelined && F->launched && !F->pool) {
       double tm[6] = {0, 0, 0, 0, 0, 0};
       if (sg_engine_timing(F->ctx, tm) == SG_OK) {
-        // 70%: fits already started finish past the deadline, and the next finish should not
+        // 70%: a fit already started finishes past the deadline, and the next finish should not
         // find the GPU idle
         if (tm[0] >= F->gpu_ms_seen && F->gpu_ms_seen > 0) budget = 0.7 * (tm[0] - F->gpu_ms_seen) * 1e-3;
         F->gpu_ms_seen = tm[0];
       }
     }
     t = now_s();
-    bool progressed = false;
     std::vector<std::pair<int64_t, int64_t>> ready;  // (ready_at, fit id)
     for (auto& kv : F->active) {
       Fit& f = *kv.second;
@@ -933,37 +1032,96 @@ static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
       ready.emplace_back(f.ready_at, kv.first);
     }
     std::sort(ready.begin(), ready.end());
-    std::vector<Fit*> todo;
-    for (const auto& r : ready) todo.push_back(F->active[r.second].get());
-    std::atomic<bool> any{false};
-    const std::function<void(int64_t)> advance = [&](int64_t r) {
-      if (budget >= 0.0 && r > 0 && now_s() - t > budget) return;  // left for the next step
-      Fit& f = *todo[r];
-      try {
-        while (is_ready(F, f)) {
-          any.store(true);
-          f.ready_at = -1;
-          if (!resume(F, f) || f.failed || f.phase == P_DONE) break;
-        }
-      } catch (const std::exception& ex) {
-        fail(F, f, SG_ERR_NOMEM, std::string("fit driver: ") + ex.what());
+    bool progressed = false;
+    if (F->pool) {
+      std::vector<Fit*> todo;
+      for (const auto& r : ready) {
+        Fit* f = F->active[r.second].get();
+        f->busy = true;
+        todo.push_back(f);
       }
-    };
-    if (F->pool && todo.size() > 1) {
-      F->pool->run((int64_t)todo.size(), advance);
+      F->pool->push(todo);
+      F->pool->wait_idle();
+      take_back(F);
+      progressed = !todo.empty();
     } else {
-      for (int64_t r = 0; r < (int64_t)todo.size(); ++r) advance(r);
+      for (size_t r = 0; r < ready.size(); ++r) {
+        if (budget >= 0.0 && r > 0 && now_s() - t > budget) break;  // left for the next step
+        advance(F, *F->active[ready[r].second]);
+        progressed = true;
+      }
+      F->t_host += now_s() - t;
     }
-    progressed = any.load();
-    for (const auto& r : ready) {
-      auto it = F->active.find(r.second);
-      if (it != F->active.end() && (it->second->failed || it->second->phase == P_DONE)) retire(F, r.second);
-    }
-    F->t_host += now_s() - t;
+    retire_finished(F);
     if (!stepped && !progressed && fin == 0 && !F->active.empty())
       return fits_err(F, SG_ERR_STATE, "engine idle while %zu fits wait for columns", F->active.size());
     if (F->finished_order.size() > before) break;
   }
+  return SG_OK;
+}
+
+// Pipelined with workers: the calling thread only steps the engine.  It waits for the step in
+// flight without the driver's lock, finishes it and launches the next one at once, then hands the
+// fits whose columns are done to the workers, which resume them meanwhile; what they submit joins
+// the next launch.  The GPU never waits for the fits' host arithmetic, only for the engine calls
+// of the few fits it was in the middle of.
+static int run_async(sg_fits* F, int64_t max_steps, size_t before) {
+  for (int64_t s = 0; s < max_steps; ++s) {
+    take_back(F);
+    int64_t retired = retire_finished(F);
+    admit(F);
+    if (F->active.empty() && F->pending.empty()) break;
+    const double t = now_s();
+    if (F->launched) sg_engine_wait(F->ctx);
+    int rc = SG_OK;
+    {
+      std::lock_guard<std::mutex> g(F->mu);
+      int64_t fin = 0, fin2 = 0;
+      if (F->launched) rc = sg_engine_finish(F->ctx, &fin);
+      int launched = 0;
+      const double tl = now_s();
+      if (rc == SG_OK) rc = sg_engine_launch(F->ctx, &fin2, &launched);
+      F->t_launch += now_s() - tl;
+      F->launched = launched != 0;
+      if (rc == SG_OK) rc = poll_done(F);
+    }
+    if (rc != SG_OK) return engine_error(F, rc);
+    F->t_engine += now_s() - t;
+    F->steps += 1;
+    take_back(F);
+    std::vector<Fit*> todo;
+    bool busy = false;
+    {
+      std::lock_guard<std::mutex> g(F->mu);
+      for (auto& kv : F->active) {
+        Fit& f = *kv.second;
+        if (!f.busy && !f.failed && f.phase != P_DONE && ready_locked(F, f)) {
+          f.busy = true;
+          todo.push_back(&f);
+        }
+        busy = busy || f.busy;
+      }
+    }
+    F->pool->push(todo);
+    retired += retire_finished(F);
+    if (!F->launched) {
+      // nothing on the GPU: wait for the fits being resumed to submit
+      if (busy) {
+        F->pool->wait_idle();
+      } else if (retired == 0 && !F->active.empty()) {
+        return fits_err(F, SG_ERR_STATE, "engine idle while %zu fits wait for columns", F->active.size());
+      }
+    }
+    if (F->finished_order.size() > before) break;
+  }
+  return SG_OK;
+}
+
+static int fits_run_impl(sg_fits* F, int64_t max_steps, int64_t* n_ready) {
+  if (!F) return SG_ERR_INVALID;
+  const size_t before = F->finished_order.size();
+  const int rc = F->pool && F->pipelined ? run_async(F, max_steps, before) : run_sync(F, max_steps, before);
+  if (rc != SG_OK) return rc;
   if (n_ready) *n_ready = (int64_t)F->finished_order.size();
   return SG_OK;
 }
@@ -989,8 +1147,9 @@ extern "C" int sg_fits_counts(sg_fits* F, int64_t* active, int64_t* pending, int
 
 extern "C" int sg_fits_host_times(sg_fits* F, double* t8) {
   if (!F || !t8) return SG_ERR_INVALID;
+  std::lock_guard<std::mutex> g(F->mu);
   t8[0] = F->t_engine;
-  t8[1] = F->t_host;
+  t8[1] = F->t_host + (F->pool ? F->pool->busy_seconds() : 0.0);
   t8[2] = (double)F->steps;
   t8[3] = F->t_pheno;
   t8[4] = F->t_submit;

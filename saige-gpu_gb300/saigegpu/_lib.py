@@ -92,6 +92,7 @@ SIGNATURES = {
     "sg_engine_run": [c_ctx, c_i64, P_i64],
     "sg_engine_launch": [c_ctx, P_i64, P_i32],
     "sg_engine_finish": [c_ctx, P_i64],
+    "sg_engine_wait": [c_ctx],
     "sg_engine_fetch": [c_ctx, c_i64, P_f64, P_i32],
     "sg_engine_cancel": [c_ctx, c_i64],
     "sg_engine_stats": [c_ctx, P_i64],
@@ -143,9 +144,18 @@ def load():
     if not os.path.exists(path):
         raise ImportError("libsaigegpu.so not built (%s); run __graft_entry__.build()" % path)
     lib = C.CDLL(path)
+    bind(lib, strict=True)
+    _lib = lib
+    return lib
+
+
+def bind(lib, strict=False):
+    """Give ``lib``'s entry points of this ABI their argument and result types (strict: every
+    one must be present); returns ``lib``."""
     for name, argtypes in SIGNATURES.items():
+        if not strict and not hasattr(lib, name):
+            continue
         f = getattr(lib, name)
         f.argtypes = argtypes
         f.restype = _RESTYPE.get(name, C.c_int)
-    _lib = lib
     return lib

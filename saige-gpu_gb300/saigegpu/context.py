@@ -451,6 +451,10 @@ class Context:
         self._call("sg_engine_finish", C.byref(fin))
         return fin.value
 
+    def engine_wait(self):
+        """Block until the launched step has run on the device, without finishing it."""
+        self._call("sg_engine_wait")
+
     def engine_fetch(self, rid, out=None):
         x = np.empty(self.n, np.float64) if out is None else out
         it = C.c_int32()
