@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--workers", type=int, default=None,
                     help="host threads for the fits' driver math (default: native driver half the cores, "
                          "at most 8; Python driver 1)")
+    ap.add_argument("--launch-wait-ms", type=float, default=None,
+                    help="native driver: how long a launch may wait for the fits the last step made ready "
+                         "(default: the library's)")
     ap.add_argument("--blocking-runner", action="store_true",
                     help="step the engine synchronously instead of overlapping the driver with the next step")
     ap.add_argument("--serve-requests", type=int, default=32,
@@ -183,11 +186,12 @@ def make_specs(ctx, args, rng_seed):
     return specs
 
 
-def run_batch(ctx, specs, cols, pipelined=True, workers=None, driver="native"):
+def run_batch(ctx, specs, cols, pipelined=True, workers=None, driver="native", launch_wait_ms=None):
     from saigegpu import native, serve
     t0 = time.perf_counter()
     if driver == "native":
-        res, jobs = native.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined, threads=workers)
+        res, jobs = native.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined, threads=workers,
+                                     launch_wait_ms=launch_wait_ms)
     else:
         res, jobs = serve.fit_batch(ctx, specs, max_columns=cols, pipelined=pipelined, workers=workers)
     wall = time.perf_counter() - t0
@@ -232,6 +236,19 @@ def grm_roofline(ctx, peaks, t_dev, n, np_, mode="tf32x3", traffic=None):
                  "frac": round(a_tc / tc_peak, 4),
                  "peak_source": ("measured bf16_tflops (MEASURED_PEAKS.json)" if bf16 else
                                  "TF32 = half the measured bf16_tflops (MEASURED_PEAKS.json)")}, **common)
+
+
+def step_width_summary(trace):
+    """How wide the engine steps were (GRM.V columns per launch) and where the GRM.V time went."""
+    if len(trace) == 0:
+        return None
+    cols, occ, gemm = trace[:, 0], trace[:, 1], trace[:, 2]
+    narrow = cols <= 128  # K-streaming bound: the K halves' read sets the time
+    return {"steps": int(len(trace)),
+            "columns_p10_p50_p90": [float(np.percentile(cols, q)) for q in (10, 50, 90)],
+            "occupied_mean": round(float(occ.mean()), 1),
+            "grmv_ms_share_steps_le_128_columns": round(float(gemm[narrow].sum() / max(gemm.sum(), 1e-9)), 3),
+            "steps_le_128_columns": int(narrow.sum())}
 
 
 def serving_block(ctx, args, cols):
@@ -389,7 +406,7 @@ def run_ours(args, rank, world, local):
     cols = _serve.columns_for(specs)
     setup_s = time.perf_counter() - t_setup
     for _ in range(args.warmup):
-        run_batch(ctx, specs, cols, not args.blocking_runner, args.workers, args.driver)
+        run_batch(ctx, specs, cols, not args.blocking_runner, args.workers, args.driver, args.launch_wait_ms)
     L0 = ctx.kernel_launches()
     ctx.engine_reset_timing()
     barrier(world)
@@ -397,7 +414,8 @@ def run_ours(args, rank, world, local):
     walls, jobs_all, res_all, host_t = [], [], [], {}
     with Clocks(local) as clk:
         for _ in range(args.steps):
-            res, jobs, wall = run_batch(ctx, specs, cols, not args.blocking_runner, args.workers, args.driver)
+            res, jobs, wall = run_batch(ctx, specs, cols, not args.blocking_runner, args.workers, args.driver,
+                                        args.launch_wait_ms)
             walls.append(wall)
             jobs_all += jobs
             res_all += res
@@ -408,6 +426,7 @@ def run_ours(args, rank, world, local):
     launches = ctx.kernel_launches() - L0
     io_h2d, io_d2h = ctx.engine_io_bytes()
     idle_ms, admit_ms, finish_ms = ctx.engine_idle_ms()
+    trace = ctx.engine_step_trace()
     tdev = ctx.engine_timing()
     dev_s = tdev["step_ms"] / 1e3
     total_wall = sum(walls)
@@ -447,7 +466,8 @@ def run_ours(args, rank, world, local):
                    "runner": "blocking" if args.blocking_runner else "pipelined",
                    "driver": args.driver,
                    "driver_threads": args.workers if args.workers is not None else (
-                       "half the cores, at most 8" if args.driver == "native" else 1)},
+                       "half the cores, at most 8" if args.driver == "native" else 1),
+                   "launch_wait_ms": args.launch_wait_ms if args.launch_wait_ms is not None else "library default"},
         "e2e": {"value": round(e2e, 2), "unit": "fits/hr", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "latency_s": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3)},
         "gpu_launches": int(launches),
@@ -471,6 +491,7 @@ def run_ours(args, rank, world, local):
         "between_steps_s_per_step": {"total": round(idle_ms / 1e3 / args.steps, 3),
                                      "launch_admission": round(admit_ms / 1e3 / args.steps, 3),
                                      "finish_host": round(finish_ms / 1e3 / args.steps, 3)},
+        "step_widths": step_width_summary(trace),
     }
     if tune_report is not None:
         out["tuning"] = {"clusters_syrk_grmv": list(tune_report["chosen"]),

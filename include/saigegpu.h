@@ -297,6 +297,11 @@ int sg_engine_timing(sg_ctx *ctx, double *t6);
  * step; ms3[2]: host time finishes spent after their step had drained.  No reference counterpart. */
 int sg_engine_idle_ms(sg_ctx *ctx, double *ms3);
 int sg_engine_reset_timing(sg_ctx *ctx);
+/* Per-step records since the last sg_engine_reset_timing (at most 65536 steps), five doubles each:
+ * columns the GRM.V computed (active columns padded to its tile width), occupied columns, GRM.V
+ * device ms, step device ms, device idle ms before the step (-1 for the first).  Up to max_steps
+ * records into out[5 * max_steps]; *n_out gets the count.  No reference counterpart. */
+int sg_engine_step_trace(sg_ctx *ctx, double *out, int64_t max_steps, int64_t *n_out);
 /* Bytes copied host->device and device->host by the engine calls (right-hand sides, weights,
  * probe tables, column states, fetched results, probe reductions) since the last
  * sg_engine_reset_timing.  No reference counterpart (I/O accounting of this engine). */
@@ -341,6 +346,10 @@ int sg_fits_run(sg_fits *fits, int64_t max_steps, int64_t *n_ready);
  * resuming fits.  threads = 1: the calling thread alternates stepping and resuming.  Default: half
  * the hardware threads, at most 8. */
 int sg_fits_set_threads(sg_fits *fits, int threads);
+/* With worker threads: after a step finishes, the next launch waits up to ms (0..1000, default 0)
+ * for the workers to resume the fits that step made ready, so that their new columns ride the
+ * next step instead of the one after it (fewer steps per fit, at the cost of device idle time). */
+int sg_fits_set_launch_wait(sg_fits *fits, double ms);
 int sg_fits_poll(sg_fits *fits, int64_t *ids, int64_t max_ids, int64_t *n_out);
 int sg_fits_counts(sg_fits *fits, int64_t *active, int64_t *pending, int64_t *done);
 /* t8: seconds in engine steps (launch / finish / poll, and with worker threads the wait for the

@@ -105,7 +105,12 @@ struct Engine {
   cudaEvent_t ev_adm = nullptr;
   bool adm_recorded = false;
   double t_step_ms = 0, t_gemm_ms = 0, gemm_launches = 0, gemm_flops = 0, gemm_cols = 0, useful_cols = 0;
+  // per-step records since the last timing reset (the first kStepTrace steps):
+  // [columns the GRM.V computed, occupied columns, GRM.V ms, step ms, idle ms before the step]
+  std::vector<double> trace;
 };
+constexpr int64_t kStepTrace = 65536;
+constexpr int kTraceFields = 5;
 
 }  // namespace
 
@@ -1427,7 +1432,13 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
     if (e.adm_recorded && cudaEventElapsedTime(&ms_adm, e.ev_adm, e.ev[0]) == cudaSuccess && ms_adm > 0.f)
       e.t_admit_ms += ms_adm;
     e.adm_recorded = false;
+    const bool had_prev = e.have_prev;
     e.have_prev = true;
+    if ((int64_t)e.trace.size() < kStepTrace * kTraceFields) {
+      const double rec[kTraceFields] = {(double)(c->mv_mode == SG_MV_FP64_PLAIN ? occupied : ncols),
+                                        (double)occupied, ms_gemm, ms_step, had_prev ? (double)ms_idle : -1.0};
+      e.trace.insert(e.trace.end(), rec, rec + kTraceFields);
+    }
     e.t_gemm_ms += ms_gemm;
     e.t_step_ms += ms_step;
     const int64_t launched_cols = c->mv_mode == SG_MV_FP64_PLAIN ? occupied : ncols;
@@ -1824,6 +1835,16 @@ extern "C" int sg_engine_reset_timing(sg_ctx* c) {
   e.have_prev = false;
   e.t_step_ms = e.t_gemm_ms = e.gemm_launches = e.gemm_flops = e.gemm_cols = e.useful_cols = 0;
   e.io_h2d = e.io_d2h = 0;
+  e.trace.clear();
+  return SG_OK;
+}
+
+extern "C" int sg_engine_step_trace(sg_ctx* c, double* out, int64_t max_steps, int64_t* n_out) {
+  if (!c || !n_out || (max_steps > 0 && !out)) return SG_ERR_INVALID;
+  const std::vector<double>& t = c->eng.trace;
+  const int64_t n = std::min<int64_t>(max_steps, (int64_t)t.size() / kTraceFields);
+  std::copy(t.begin(), t.begin() + n * kTraceFields, out);
+  *n_out = n;
   return SG_OK;
 }
 

@@ -158,6 +158,12 @@ class Workers {
     std::unique_lock<std::mutex> lk(m_);
     done_cv_.wait(lk, [&] { return q_.empty() && running_ == 0; });
   }
+  // wait_idle for at most `seconds`; true if idle
+  bool wait_idle_for(double seconds) {
+    std::unique_lock<std::mutex> lk(m_);
+    return done_cv_.wait_for(lk, std::chrono::duration<double>(seconds),
+                             [&] { return q_.empty() && running_ == 0; });
+  }
   double busy_seconds() {
     std::lock_guard<std::mutex> lk(m_);
     return busy_s_;
@@ -195,6 +201,7 @@ struct sg_fits {
   double t_pheno = 0, t_submit = 0, t_fetch = 0, t_dots = 0;  // parts of t_host spent in engine calls
   double t_launch = 0;                                          // part of t_engine spent launching
   double gpu_ms_seen = 0;                                      // engine step time already budgeted
+  double launch_wait_s = 0.0;  // with workers: how long a launch may wait for the fits just made ready
   int64_t steps = 0;
   std::mutex mu;                  // engine calls and the bookkeeping above, from the worker threads
   std::unique_ptr<Workers> pool;  // null: the fits' arithmetic runs on the calling thread
@@ -248,22 +255,62 @@ void working(Fit& f, const std::vector<double>& et) {
   }
 }
 
-// A' B for column-major n x a and n x b
-void gram(const double* A, int a, const double* B, int b, int64_t n, double* out) {
-  for (int j = 0; j < b; ++j)
-    for (int i = 0; i < a; ++i) {
-      double s = 0.0;
-      const double* x = A + (int64_t)i * n;
-      const double* z = B + (int64_t)j * n;
-      for (int64_t r = 0; r < n; ++r) s += x[r] * z[r];
-      out[i + j * a] = s;
+// A' B for column-major n x a and n x b.  Every entry is summed in row order, as one dot product
+// at a time would sum it, but the entries advance together in one pass over the rows: the loop is
+// bound by throughput instead of by the latency of a single chain of additions (sizes up to 8 x 8
+// get their accumulators in registers).
+template <int NA, int NB>
+void gram_fixed(const double* A, const double* B, int64_t n, double* out) {
+  double acc[NA * NB] = {};
+  for (int64_t r = 0; r < n; ++r) {
+    double x[NA];
+    for (int i = 0; i < NA; ++i) x[i] = A[(int64_t)i * n + r];
+    for (int j = 0; j < NB; ++j) {
+      const double z = B[(int64_t)j * n + r];
+      for (int i = 0; i < NA; ++i) acc[i + j * NA] += x[i] * z;
     }
+  }
+  for (int k = 0; k < NA * NB; ++k) out[k] = acc[k];
 }
 
-double dotn(const double* a, const double* b, int64_t n) {
-  double s = 0.0;
-  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
-  return s;
+template <int NA>
+bool gram_dispatch_b(const double* A, const double* B, int b, int64_t n, double* out) {
+  if (b == 1) gram_fixed<NA, 1>(A, B, n, out);
+  else if (b == NA) gram_fixed<NA, NA>(A, B, n, out);
+  else return false;
+  return true;
+}
+
+void gram(const double* A, int a, const double* B, int b, int64_t n, double* out) {
+  bool done = false;
+  switch (a) {
+    case 1: done = gram_dispatch_b<1>(A, B, b, n, out); break;
+    case 2: done = gram_dispatch_b<2>(A, B, b, n, out); break;
+    case 3: done = gram_dispatch_b<3>(A, B, b, n, out); break;
+    case 4: done = gram_dispatch_b<4>(A, B, b, n, out); break;
+    case 5: done = gram_dispatch_b<5>(A, B, b, n, out); break;
+    case 6: done = gram_dispatch_b<6>(A, B, b, n, out); break;
+    case 7: done = gram_dispatch_b<7>(A, B, b, n, out); break;
+    case 8: done = gram_dispatch_b<8>(A, B, b, n, out); break;
+    default: break;
+  }
+  if (done) return;
+  std::vector<double> acc((size_t)a * b, 0.0);
+  for (int64_t r = 0; r < n; ++r)
+    for (int j = 0; j < b; ++j) {
+      const double z = B[(int64_t)j * n + r];
+      for (int i = 0; i < a; ++i) acc[i + j * a] += A[(int64_t)i * n + r] * z;
+    }
+  std::copy(acc.begin(), acc.end(), out);
+}
+
+// k dot products a_q . b_q of length n in one pass (each summed in index order)
+template <int K>
+void dots(const double* const* a, const double* const* b, int64_t n, double* out) {
+  double acc[K] = {};
+  for (int64_t i = 0; i < n; ++i)
+    for (int q = 0; q < K; ++q) acc[q] += a[q][i] * b[q][i];
+  for (int q = 0; q < K; ++q) out[q] = acc[q];
 }
 
 // out = v - SX (cov (SX' w)): the projection P applied as the reference writes it
@@ -526,21 +573,32 @@ AiScore ai_finish(Fit& f) {
   AiScore re;
   std::vector<double> PAPY(n);
   project(f, f.ai_cov, f.fetched[0].data(), f.fetched[0].data(), PAPY.data());
-  re.YPAPY = dotn(f.PY.data(), f.APY.data(), n);
   double s1 = 0.0, s0 = 0.0;
   for (double v : f.t1) s1 += v;
   for (double v : f.t0) s0 += v;
   re.tr1 = s1 / (double)f.t1.size();
   re.tr0 = s0 / (double)f.t0.size();
+  const double* py = f.PY.data();
+  const double* apy = f.APY.data();
   if (f.quant) {
     std::vector<double> PA0PY(n);
     project(f, f.ai_cov, f.fetched[1].data(), f.fetched[1].data(), PA0PY.data());
-    re.YPA0PY = dotn(f.PY.data(), f.PY.data(), n);
-    re.AI[0] = dotn(f.PY.data(), PA0PY.data(), n);
-    re.AI[1] = re.AI[2] = dotn(f.PY.data(), PAPY.data(), n);
-    re.AI[3] = dotn(f.APY.data(), PAPY.data(), n);
+    const double* a[5] = {py, py, py, py, apy};
+    const double* b[5] = {apy, py, PA0PY.data(), PAPY.data(), PAPY.data()};
+    double d[5];
+    dots<5>(a, b, n, d);
+    re.YPAPY = d[0];
+    re.YPA0PY = d[1];
+    re.AI[0] = d[2];
+    re.AI[1] = re.AI[2] = d[3];
+    re.AI[3] = d[4];
   } else {
-    re.AI[0] = dotn(f.APY.data(), PAPY.data(), n);
+    const double* a[2] = {py, apy};
+    const double* b[2] = {apy, PAPY.data()};
+    double d[2];
+    dots<2>(a, b, n, d);
+    re.YPAPY = d[0];
+    re.AI[0] = d[1];
   }
   return re;
 }
@@ -904,6 +962,12 @@ extern "C" int sg_fits_set_threads(sg_fits* F, int threads) {
   return SG_OK;
 }
 
+extern "C" int sg_fits_set_launch_wait(sg_fits* F, double ms) {
+  if (!F || !(ms >= 0.0) || ms > 1000.0) return SG_ERR_INVALID;
+  F->launch_wait_s = ms * 1e-3;
+  return SG_OK;
+}
+
 extern "C" void sg_fits_destroy(sg_fits* F) {
   if (!F) return;
   if (F->pool) {
@@ -1071,26 +1135,22 @@ static int run_async(sg_fits* F, int64_t max_steps, size_t before) {
     int64_t retired = retire_finished(F);
     admit(F);
     if (F->active.empty() && F->pending.empty()) break;
-    const double t = now_s();
+    double t = now_s();
     if (F->launched) sg_engine_wait(F->ctx);
     int rc = SG_OK;
     {
       std::lock_guard<std::mutex> g(F->mu);
-      int64_t fin = 0, fin2 = 0;
+      int64_t fin = 0;
       if (F->launched) rc = sg_engine_finish(F->ctx, &fin);
-      int launched = 0;
-      const double tl = now_s();
-      if (rc == SG_OK) rc = sg_engine_launch(F->ctx, &fin2, &launched);
-      F->t_launch += now_s() - tl;
-      F->launched = launched != 0;
+      F->launched = false;
       if (rc == SG_OK) rc = poll_done(F);
     }
     if (rc != SG_OK) return engine_error(F, rc);
     F->t_engine += now_s() - t;
-    F->steps += 1;
+    // hand the fits whose columns are done to the workers; optionally give them a moment, so that
+    // what they submit rides the next step instead of the one after
     take_back(F);
     std::vector<Fit*> todo;
-    bool busy = false;
     {
       std::lock_guard<std::mutex> g(F->mu);
       for (auto& kv : F->active) {
@@ -1099,12 +1159,27 @@ static int run_async(sg_fits* F, int64_t max_steps, size_t before) {
           f.busy = true;
           todo.push_back(&f);
         }
-        busy = busy || f.busy;
       }
     }
     F->pool->push(todo);
+    if (F->launch_wait_s > 0.0 && !todo.empty()) F->pool->wait_idle_for(F->launch_wait_s);
+    t = now_s();
+    {
+      std::lock_guard<std::mutex> g(F->mu);
+      int64_t fin2 = 0;
+      int launched = 0;
+      rc = sg_engine_launch(F->ctx, &fin2, &launched);
+      F->launched = launched != 0;
+      F->t_launch += now_s() - t;
+    }
+    if (rc != SG_OK) return engine_error(F, rc);
+    F->t_engine += now_s() - t;
+    F->steps += 1;
+    take_back(F);
     retired += retire_finished(F);
     if (!F->launched) {
+      bool busy = false;
+      for (const auto& kv : F->active) busy = busy || kv.second->busy;
       // nothing on the GPU: wait for the fits being resumed to submit
       if (busy) {
         F->pool->wait_idle();

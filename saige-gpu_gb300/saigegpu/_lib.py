@@ -93,6 +93,7 @@ SIGNATURES = {
     "sg_engine_launch": [c_ctx, P_i64, P_i32],
     "sg_engine_finish": [c_ctx, P_i64],
     "sg_engine_wait": [c_ctx],
+    "sg_engine_step_trace": [c_ctx, P_f64, c_i64, P_i64],
     "sg_engine_fetch": [c_ctx, c_i64, P_f64, P_i32],
     "sg_engine_cancel": [c_ctx, c_i64],
     "sg_engine_stats": [c_ctx, P_i64],
@@ -116,6 +117,7 @@ SIGNATURES = {
                        C.c_double, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, c_u64, P_i64],
     "sg_fits_run": [C.c_void_p, c_i64, P_i64],
     "sg_fits_set_threads": [C.c_void_p, C.c_int],
+    "sg_fits_set_launch_wait": [C.c_void_p, C.c_double],
     "sg_fits_poll": [C.c_void_p, P_i64, c_i64, P_i64],
     "sg_fits_counts": [C.c_void_p, P_i64, P_i64, P_i64],
     "sg_fits_host_times": [C.c_void_p, P_f64],

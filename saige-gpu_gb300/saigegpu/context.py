@@ -518,6 +518,14 @@ class Context:
         self._call("sg_engine_idle_ms", _ptr(v, L.P_f64))
         return float(v[0]), float(v[1]), float(v[2])
 
+    def engine_step_trace(self, max_steps=65536):
+        """Per-step records since the last timing reset, shape (steps, 5): GRM.V columns, occupied
+        columns, GRM.V ms, step ms, idle ms before the step (-1 for the first)."""
+        out = np.zeros((max_steps, 5))
+        n = C.c_int64()
+        self._call("sg_engine_step_trace", _ptr(out, L.P_f64), int(max_steps), C.byref(n))
+        return out[:n.value].copy()
+
     def engine_io_bytes(self):
         """(host->device, device->host) bytes moved by engine calls since the last timing reset."""
         a, b = C.c_uint64(), C.c_uint64()

@@ -20,10 +20,11 @@ def _p(a, t):
 class NativeFits:
     """One ``sg_fits`` driver over a context's engine."""
 
-    def __init__(self, ctx, max_columns, max_fits, pipelined=True, threads=None, lib=None):
+    def __init__(self, ctx, max_columns, max_fits, pipelined=True, threads=None, lib=None, launch_wait_ms=None):
         """threads: host threads for the fits' arithmetic (None: half the cores, at most 8).
         lib: a library exporting the sg_fits_* ABI other than libsaigegpu (bound with
-        ``_lib.bind``); ctx then only needs ``_h`` and ``last_error()``."""
+        ``_lib.bind``); ctx then only needs ``_h`` and ``last_error()``.
+        launch_wait_ms: see ``sg_fits_set_launch_wait`` (None: the library default)."""
         self.ctx = ctx
         self._L = L.load() if lib is None else lib
         h = C.c_void_p()
@@ -34,6 +35,8 @@ class NativeFits:
         self.specs = {}
         if threads is not None:
             self._check(self._L.sg_fits_set_threads(self._h, int(threads)))
+        if launch_wait_ms is not None:
+            self._check(self._L.sg_fits_set_launch_wait(self._h, float(launch_wait_ms)))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -120,11 +123,12 @@ class _Job:
         self.host_times = {}
 
 
-def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True, threads=None, lib=None):
+def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True, threads=None, lib=None,
+              launch_wait_ms=None):
     """Fit all ``specs`` together in native code; returns (results or exceptions, jobs) in order."""
     from .serve import columns_for
     max_columns = max(max_columns or 0, columns_for(specs))
-    drv = NativeFits(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined, threads, lib)
+    drv = NativeFits(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined, threads, lib, launch_wait_ms)
     try:
         jobs = {}
         for s in specs:
@@ -154,10 +158,10 @@ def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True, thr
 
 
 def serve(ctx, arrivals, max_columns=2048, max_phenos=64, clock=time.perf_counter, pipelined=True,
-          threads=None, lib=None):
+          threads=None, lib=None, launch_wait_ms=None):
     """Serve (t_arrival_seconds, FitSpec) requests with the native driver; returns the finished jobs
     (t_arrive / t_start / t_done) in completion order."""
-    drv = NativeFits(ctx, max_columns, max_phenos, pipelined, threads, lib)
+    drv = NativeFits(ctx, max_columns, max_phenos, pipelined, threads, lib, launch_wait_ms)
     pending = sorted(arrivals, key=lambda a: a[0])
     jobs, finished = {}, []
     t0 = clock()

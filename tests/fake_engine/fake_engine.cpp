@@ -54,7 +54,7 @@ struct Slot {
 
 struct sg_ctx {
   int64_t n = 0;
-  std::vector<double> K, diag;  // n x n (symmetric), diag(Sigma) term of K
+  std::vector<double> K, diag;  // n x n (symmetric; empty: K = diag(diag)), diag(Sigma) term of K
   int64_t cap_cols = 0, running_or_held = 0;
   std::vector<Slot> slots;
   std::map<int64_t, Req> reqs;
@@ -81,6 +81,10 @@ void kprod(const sg_ctx* c, const Slot& s, const std::vector<double>& v, std::ve
   out.assign(n, 0.0);
   for (int64_t i = 0; i < n; ++i) {
     if (!s.mask[i]) continue;
+    if (c->K.empty()) {  // K = diag(diag): large cohorts at O(n) per product
+      out[i] = c->diag[i] * v[i];
+      continue;
+    }
     const double* row = c->K.data() + i * n;
     double acc = 0.0;
     for (int64_t j = 0; j < n; ++j) acc += row[j] * v[j];
@@ -167,11 +171,12 @@ void wait_device(sg_ctx* c) {
 
 extern "C" {
 
+// K NULL: K = diag(diag)
 int fake_ctx_create(int64_t n, const double* K, const double* diag, double step_ms, sg_ctx** out) {
-  if (n <= 0 || !K || !diag || !out) return SG_ERR_INVALID;
+  if (n <= 0 || !diag || !out) return SG_ERR_INVALID;
   sg_ctx* c = new sg_ctx();
   c->n = n;
-  c->K.assign(K, K + n * n);
+  if (K) c->K.assign(K, K + n * n);
   c->diag.assign(diag, diag + n);
   c->step_ms = step_ms;
   *out = c;

@@ -118,11 +118,12 @@ def test_native_driver_matches_oracle(fake_lib, cohort):
     assert all(j.column_iterations > 0 for j in jobs)
 
 
-@pytest.mark.parametrize("mode", [dict(threads=1), dict(threads=4, pipelined=False), dict(threads=3, step_ms=0.3)])
+@pytest.mark.parametrize("mode", [dict(threads=1), dict(threads=4, pipelined=False), dict(threads=3, step_ms=0.3),
+                                  dict(threads=4, step_ms=0.3, launch_wait_ms=2.0)])
 def test_native_driver_schedules_agree(fake_lib, cohort, mode):
-    """The calling thread alone, blocking steps with workers, and workers under an emulated step
-    time give bit-identical fits to the default schedule: a fit's columns never depend on what
-    shared their steps."""
+    """The calling thread alone, blocking steps with workers, workers under an emulated step time,
+    and launches that wait for the workers give bit-identical fits to the default schedule: a fit's
+    columns never depend on what shared their steps."""
     grm, specs, _ = cohort
     base, bj = _run(fake_lib, grm, specs, threads=4)
     mode = dict(mode)
