@@ -61,7 +61,10 @@ struct Fit {
   bool has_mask = false;
   std::vector<int64_t> idx;   // subset position -> cohort position
   // inputs over the cohort (0 outside the subset)
-  std::vector<double> y, X, offset;
+  std::vector<double> y, offset;
+  // [Y | X]: Get_Coef's working vector, then the covariates (n x (1 + p), column-major), so that
+  // Get_Coef's right-hand sides go to the engine as they are
+  std::vector<double> YX;
   std::vector<double> eta, alpha;  // current eta (with offset) and coefficients of the main loop
   double tol = 0.02, tol_pcg = 1e-5, cutoff = 0.0025;
   int maxiter = 20, maxiter_pcg = 500, nrun = 30;
@@ -75,7 +78,7 @@ struct Fit {
   // Get_Coef
   double gc_tau[2] = {0, 0};
   int gc_iter = 0;
-  std::vector<double> gc_alpha0, mu, Y, W;
+  std::vector<double> gc_alpha0, mu, W;
   // result of the last Get_Coef
   std::vector<double> rc_alpha, rc_eta, rc_cov, SY, SX;
   // getAIScore
@@ -87,7 +90,8 @@ struct Fit {
   // waiting
   std::vector<int64_t> wait_ids;
   bool wait_fetch = false;
-  std::vector<std::vector<double>> fetched;
+  std::vector<std::vector<double>> fetched;  // kept between stages (their buffers are reused)
+  std::vector<double> rhs;                     // reused staging for two-column submissions
   // bookkeeping
   int64_t column_iterations = 0, columns = 0;
   bool failed = false;
@@ -227,7 +231,6 @@ int64_t need_columns(const Fit& f) { return 2 * (int64_t)(f.nrun + 10) + 8; }
 void working(Fit& f, const std::vector<double>& et) {
   const double eps = 2.220446049250313e-16;
   f.mu.resize(f.n);
-  f.Y.resize(f.n);
   f.W.resize(f.n);
   for (int64_t i = 0; i < f.n; ++i) {
     const double e = et[i];
@@ -245,7 +248,7 @@ void working(Fit& f, const std::vector<double>& et) {
     }
     f.mu[i] = mu;
     const bool in = f.mask[i] != 0;
-    f.Y[i] = in ? e - f.offset[i] + (f.y[i] - mu) / mu_eta : 0.0;
+    f.YX[i] = in ? e - f.offset[i] + (f.y[i] - mu) / mu_eta : 0.0;
     if (f.quant) {
       f.W[i] = 1.0;
     } else {
@@ -426,11 +429,8 @@ void wait_for(Fit& f, Stage st, std::vector<int64_t> ids, bool fetch) {
 // --------------------------------------------------------------- Get_Coef
 bool gc_issue(sg_fits* F, Fit& f) {
   if (!set_pheno(F, f, f.W, f.gc_tau)) return false;
-  std::vector<double> B((size_t)f.n * (1 + f.p));
-  std::memcpy(B.data(), f.Y.data(), f.n * sizeof(double));
-  std::memcpy(B.data() + f.n, f.X.data(), (size_t)f.n * f.p * sizeof(double));
   std::vector<int64_t> ids;
-  if (!submit(F, f, 0, B.data(), 1 + f.p, f.maxiter_pcg, f.tol_pcg, ids)) return false;
+  if (!submit(F, f, 0, f.YX.data(), 1 + f.p, f.maxiter_pcg, f.tol_pcg, ids)) return false;
   wait_for(f, S_GC_WAIT, ids, true);
   return true;
 }
@@ -445,18 +445,17 @@ bool gc_begin(sg_fits* F, Fit& f, const double* tau, const std::vector<double>& 
   return gc_issue(F, f);
 }
 
-// getCoefficients on the solved [Sigma^-1 Y, Sigma^-1 X]; returns true when Get_Coef is done
+// getCoefficients on the solved [Sigma^-1 Y, Sigma^-1 X] (Sigma^-1 X fetched into SX by resume);
+// returns true when Get_Coef is done
 bool gc_step(sg_fits* F, Fit& f, bool* done) {
   const int p = f.p;
   const int64_t n = f.n;
-  f.SY = std::move(f.fetched[0]);
-  f.SX.assign((size_t)n * p, 0.0);
-  for (int j = 0; j < p; ++j) std::memcpy(f.SX.data() + (int64_t)j * n, f.fetched[1 + j].data(), n * sizeof(double));
+  f.SY.swap(f.fetched[0]);
   std::vector<double> XtSX(p * p);
-  gram(f.X.data(), p, f.SX.data(), p, n, XtSX.data());
+  gram(f.YX.data() + n, p, f.SX.data(), p, n, XtSX.data());
   f.rc_cov = sg::inv_sympd(XtSX, p);
   std::vector<double> sxy(p);
-  gram(f.SX.data(), p, f.Y.data(), 1, n, sxy.data());
+  gram(f.SX.data(), p, f.YX.data(), 1, n, sxy.data());
   std::vector<double> al(p, 0.0);
   for (int i = 0; i < p; ++i)
     for (int j = 0; j < p; ++j) al[i] += f.rc_cov[i + j * p] * sxy[j];
@@ -464,7 +463,7 @@ bool gc_step(sg_fits* F, Fit& f, bool* done) {
   for (int64_t r = 0; r < n; ++r) {
     double s = 0.0;
     for (int j = 0; j < p; ++j) s += f.SX[r + (int64_t)j * n] * al[j];
-    et[r] = (f.mask[r] ? f.Y[r] - f.gc_tau[0] * (f.SY[r] - s) / f.W[r] : 0.0) + f.offset[r];
+    et[r] = (f.mask[r] ? f.YX[r] - f.gc_tau[0] * (f.SY[r] - s) / f.W[r] : 0.0) + f.offset[r];
   }
   working(f, et);
   ++f.gc_iter;
@@ -489,13 +488,13 @@ bool ai_begin(sg_fits* F, Fit& f) {
   if (!set_pheno(F, f, f.W, f.tau)) return false;
   if (f.quant) {
     std::vector<double> XtSX(p * p);
-    gram(f.X.data(), p, f.SX.data(), p, n, XtSX.data());
+    gram(f.YX.data() + n, p, f.SX.data(), p, n, XtSX.data());
     f.ai_cov = sg::inv_sympd(XtSX, p);
   } else {
     f.ai_cov = f.rc_cov;
   }
   f.PY.resize(n);
-  project(f, f.ai_cov, f.SY.data(), f.Y.data(), f.PY.data());
+  project(f, f.ai_cov, f.SY.data(), f.YX.data(), f.PY.data());
   std::vector<int64_t> a;
   if (!submit(F, f, 1, f.PY.data(), 1, 1, 0.0, a)) return false;
   f.apy_id = a[0];
@@ -510,10 +509,15 @@ bool ai_begin(sg_fits* F, Fit& f) {
 }
 
 bool ai_after_apy(sg_fits* F, Fit& f) {
-  f.APY = std::move(f.fetched[0]);
-  std::vector<double> rhs(f.APY);
-  if (f.quant) rhs.insert(rhs.end(), f.PY.begin(), f.PY.end());
-  if (!submit(F, f, 0, rhs.data(), f.quant ? 2 : 1, f.maxiter_pcg, f.tol_pcg, f.sid)) return false;
+  f.APY.swap(f.fetched[0]);
+  const double* rhs = f.APY.data();
+  if (f.quant) {  // [APY | PY]
+    f.rhs.resize(2 * (size_t)f.n);
+    std::copy(f.APY.begin(), f.APY.end(), f.rhs.begin());
+    std::copy(f.PY.begin(), f.PY.end(), f.rhs.begin() + f.n);
+    rhs = f.rhs.data();
+  }
+  if (!submit(F, f, 0, rhs, f.quant ? 2 : 1, f.maxiter_pcg, f.tol_pcg, f.sid)) return false;
   std::vector<int64_t> w(f.pid);
   w.insert(w.end(), f.aid.begin(), f.aid.end());
   wait_for(f, S_AI_WAIT_PROBES, w, false);
@@ -662,10 +666,10 @@ bool main_start(sg_fits* F, Fit& f) {
   if (f.quant) {
     working(f, f.eta);
     double m = 0.0;
-    for (int64_t i : f.idx) m += f.Y[i];
+    for (int64_t i : f.idx) m += f.YX[i];
     m /= (double)f.ns;
     double ss = 0.0;
-    for (int64_t i : f.idx) ss += (f.Y[i] - m) * (f.Y[i] - m);
+    for (int64_t i : f.idx) ss += (f.YX[i] - m) * (f.YX[i] - m);
     if (std::fabs(ss / (double)(f.ns - 1)) < 0.1) {
       fail(F, f, SG_ERR_NUMERIC, "variance of the phenotype is much smaller than 1");
       return false;
@@ -754,15 +758,26 @@ bool ai_done(sg_fits* F, Fit& f, const AiScore& re) {
   return loop_next(F, f);
 }
 
-// Resume a fit whose awaited columns are done: fetch them if asked, then run its next stage.
+// Resume a fit whose awaited columns are done: fetch them if asked (Get_Coef's Sigma^-1 X straight
+// into SX, the others into the fit's reused buffers), then run its next stage.
 bool resume(sg_fits* F, Fit& f) {
-  f.fetched.clear();
   if (f.wait_fetch) {
-    for (int64_t id : f.wait_ids) {
-      std::vector<double> x(f.n);
+    const size_t nw = f.wait_ids.size();
+    const bool gc = f.stage == S_GC_WAIT;
+    if (f.fetched.size() < nw) f.fetched.resize(nw);
+    if (gc) f.SX.resize((size_t)f.n * f.p);
+    for (size_t q = 0; q < nw; ++q) {
+      const int64_t id = f.wait_ids[q];
+      double* x;
+      if (gc && q > 0) {
+        x = f.SX.data() + (q - 1) * (size_t)f.n;
+      } else {
+        f.fetched[q].resize(f.n);
+        x = f.fetched[q].data();
+      }
       int32_t it = 0;
       const bool ok = eng(F, f, &F->t_fetch, [&] {
-        const int rc = sg_engine_fetch(F->ctx, id, x.data(), &it);
+        const int rc = sg_engine_fetch(F->ctx, id, x, &it);
         if (rc == SG_OK) {
           F->done_reqs.erase(id);
           F->owner.erase(id);
@@ -771,7 +786,6 @@ bool resume(sg_fits* F, Fit& f) {
       });
       if (!ok) return false;
       f.column_iterations += it;
-      f.fetched.push_back(std::move(x));
     }
   }
   const Stage st = f.stage;
@@ -1008,13 +1022,13 @@ static int fits_submit_impl(sg_fits* F, int trait, int64_t n_sub, const uint8_t*
   f->ns = n_sub;
   const int64_t n = F->n;
   f->y.assign(n, 0.0);
-  f->X.assign((size_t)n * p, 0.0);
+  f->YX.assign((size_t)n * (1 + p), 0.0);
   f->offset.assign(n, 0.0);
   f->eta.assign(n, 0.0);
   for (int64_t s = 0; s < n_sub; ++s) {
     const int64_t i = f->idx[s];
     f->y[i] = y[s];
-    for (int j = 0; j < p; ++j) f->X[i + (int64_t)j * n] = X[s + (int64_t)j * n_sub];
+    for (int j = 0; j < p; ++j) f->YX[(int64_t)(1 + j) * n + i] = X[s + (int64_t)j * n_sub];
     f->offset[i] = offset ? offset[s] : 0.0;
     f->eta[i] = eta0[s];
   }
@@ -1253,7 +1267,7 @@ extern "C" int sg_fits_result(sg_fits* F, int64_t fit_id, double* theta, double*
     const int64_t i = f->idx[s];
     if (eta) eta[s] = f->rc_eta[i];
     if (mu) mu[s] = f->mu[i];
-    if (Y) Y[s] = f->Y[i];
+    if (Y) Y[s] = f->YX[i];
   }
   if (cov) std::memcpy(cov, f->rc_cov.data(), (size_t)f->p * f->p * sizeof(double));
   if (iterations) *iterations = f->it_used;
