@@ -1320,7 +1320,7 @@ static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf, int64_t* la
       *launched = 0;
       return SG_OK;
     }
-    const int64_t npad = tc_grmv_padded_cols(round_up(nact, 32), e.cap_cols, e.np, true, c->num_sms);
+    const int64_t npad = tc_grmv_padded_cols(round_up(nact, 16), e.cap_cols, e.np, kTilesSplitBF16, c->num_sms);
     for (int64_t j = nact; j < npad; ++j) e.h_gcols[j] = -1;
     SG_CUDA(c, cudaMemcpyAsync(e.d_gcols, e.h_gcols, npad * 4, cudaMemcpyHostToDevice, c->stream));
     uint16_t* ph = static_cast<uint16_t*>(e.Pb);
@@ -1366,7 +1366,8 @@ static int64_t engine_gemm_cols(const sg_ctx* c) {
   const Engine& e = c->eng;
   const int64_t ncols = round_up(e.hi_col, 32);
   if (!tc_mode(c->mv_mode)) return ncols;
-  return tc_grmv_padded_cols(ncols, e.cap_cols, e.np, c->mv_mode != SG_MV_TF32_TC, c->num_sms);
+  return tc_grmv_padded_cols(ncols, e.cap_cols, e.np, c->mv_mode == SG_MV_TF32_TC ? kTilesPlain : kTilesSplitTF32,
+                             c->num_sms);
 }
 
 // First half of a step over columns [0, hi_col): GRM product + the FP64 PCG vector work, the

@@ -337,18 +337,21 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 32) {
       uint32_t v[32];
-      tmem_ld32(trow + (uint32_t)c0, v);
+      tmem_ld32(trow + (uint32_t)c0, v);  // within the allocation (kTmemCols >= BN rounded up to 32)
       const int64_t cbase = (int64_t)tc.bn * BN + c0;
+      const int lim = BN - c0 < 32 ? BN - c0 : 32;  // a tile width of 16 (mod 32) ends on half a chunk
       if (mode == 1) {
         if (colmap) {  // column j of the tile goes to row colmap[j] of D (skipped when negative)
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
+            if (j >= lim) break;
             const int32_t dc = __ldg(colmap + cbase + j);
             if (dc >= 0) D[(int64_t)dc * ldd + r] = __uint_as_float(v[j]) * scale;
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) D[(cbase + j) * ldd + r] = __uint_as_float(v[j]) * scale;
+          for (int j = 0; j < 32; ++j)
+            if (j < lim) D[(cbase + j) * ldd + r] = __uint_as_float(v[j]) * scale;
         }
       } else {
 #pragma unroll
@@ -659,30 +662,36 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
 // Column-tile widths of the GRM.V.  The split variants also come in 96..224 so that a column
 // count rarely needs padding to the next power of two.
 static const std::vector<int> kSplitWidths = {256, 224, 192, 160, 128, 96, 64, 32};
+// split-BF16 also has the widths that are odd multiples of 16 (clusters of at most 2 CTAs)
+static const std::vector<int> kBf16Widths = {256, 224, 208, 192, 176, 160, 144, 128, 112, 96, 80, 64, 48, 32};
 static const std::vector<int> kPlainWidths = {256, 128, 64, 32};
+
+static const std::vector<int>& tile_widths(int set) {
+  return set == kTilesSplitBF16 ? kBf16Widths : set == kTilesSplitTF32 ? kSplitWidths : kPlainWidths;
+}
 
 // Column-tile width for ncols columns: the widest tile that divides ncols (wider tiles re-read
 // the K strip fewer times).  A lone 256-wide block is split in two for more CTAs per wave.
-int tc_gemm_tile_n(int64_t ncols, bool split) {
-  for (int w : split ? kSplitWidths : kPlainWidths) {
-    if (w == 256 && ncols < 512 && !split) continue;
+int tc_gemm_tile_n(int64_t ncols, int set) {
+  for (int w : tile_widths(set)) {
+    if (w == 256 && ncols < 512 && set == kTilesPlain) continue;
     if (ncols % w == 0) return w;
   }
-  return 32;
+  return set == kTilesSplitBF16 ? 16 : 32;
 }
 
 // Columns one GRM.V launch covers for ncols32 (a multiple of 32) live columns, padded so that the
 // modelled cost is lowest, capped at cap columns.  Cost model (L2->SM bytes of one pass, which
 // bounds these kernels, over the fraction of the last wave of 1-CTA-per-SM tiles that is busy):
 //   padded * (A bytes per stage / BN + B bytes per stage per column) / wave_efficiency.
-int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, bool split, int num_sms) {
+int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, int set, int num_sms) {
   double best = 1e300;
   int64_t best_cols = ncols32;
   const int64_t nbm = np / kTileM;
-  for (int w : split ? kSplitWidths : kPlainWidths) {
+  for (int w : tile_widths(set)) {
     const int64_t padded = (ncols32 + w - 1) / w * w;
     if (padded > cap) continue;
-    const int bn = tc_gemm_tile_n(padded, split);
+    const int bn = tc_gemm_tile_n(padded, set);
     const int64_t tiles = nbm * (padded / bn);
     const int64_t waves = (tiles + num_sms - 1) / num_sms;
     const double eff = (double)tiles / (double)(waves * num_sms);
@@ -714,6 +723,23 @@ static cudaError_t grmv_split_dispatch(int BN, int C, const CUtensorMap& a, cons
     return C == 4   ? launch_grmv_split<kTF32, BNv, Sv, 4>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap) \
            : C == 2 ? launch_grmv_split<kTF32, BNv, Sv, 2>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap) \
                     : launch_grmv_split<kTF32, BNv, Sv, 1>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap);
+  // odd multiples of 16 (split-BF16 only): a 4-CTA slice would not be whole 8-row swizzle atoms
+#define SG_GRMV_CASE16(BNv, Sv)                                                                               \
+  case BNv:                                                                                                   \
+    return C >= 2 ? launch_grmv_split<kTF32, BNv, Sv, 2>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap)   \
+                  : launch_grmv_split<kTF32, BNv, Sv, 1>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap);
+  if constexpr (!kTF32) {
+    switch (BN) {
+      SG_GRMV_CASE16(208, 2)
+      SG_GRMV_CASE16(176, 2)
+      SG_GRMV_CASE16(144, 3)
+      SG_GRMV_CASE16(112, 3)
+      SG_GRMV_CASE16(80, 4)
+      SG_GRMV_CASE16(48, 5)
+      default:
+        break;
+    }
+  }
   switch (BN) {
     SG_GRMV_CASE(256, 2)
     SG_GRMV_CASE(224, 2)
@@ -727,6 +753,7 @@ static cudaError_t grmv_split_dispatch(int BN, int C, const CUtensorMap& a, cons
       return cudaErrorInvalidValue;
   }
 #undef SG_GRMV_CASE
+#undef SG_GRMV_CASE16
 }
 
 // Row groups of C consecutive row blocks (padded past np), every column block per group.
@@ -743,7 +770,7 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
                          const float* Plo, int64_t ncols, float* Y, cudaStream_t s, bool check) {
   if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0) return cudaErrorInvalidValue;
   const bool split = Klo != nullptr && Plo != nullptr;
-  const int BN = tc_gemm_tile_n(ncols, split);
+  const int BN = tc_gemm_tile_n(ncols, split ? kTilesSplitTF32 : kTilesPlain);
   const int C = split ? g_cluster_grmv : 1;
   CUtensorMap a, b, a2, b2;
   const uint32_t brows = (uint32_t)(BN / C);
@@ -776,10 +803,10 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
 
 cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const void* Ph, const void* Pl,
                            int64_t ncols, float* Y, cudaStream_t s, bool check, const int32_t* colmap) {
-  if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0 || !Kh || !Kl || !Ph || !Pl)
+  if (np % kTileM != 0 || ncols % 16 != 0 || ncols <= 0 || !Kh || !Kl || !Ph || !Pl)
     return cudaErrorInvalidValue;
-  const int BN = tc_gemm_tile_n(ncols, true);
-  const int C = g_cluster_grmv;
+  const int BN = tc_gemm_tile_n(ncols, kTilesSplitBF16);
+  const int C = BN % 32 != 0 && g_cluster_grmv > 2 ? 2 : g_cluster_grmv;
   const uint32_t brows = (uint32_t)(BN / C);
   const uint64_t rb = (uint64_t)np * 2;
   CUtensorMap a, b, a2, b2;

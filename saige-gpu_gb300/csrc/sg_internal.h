@@ -107,10 +107,13 @@ cudaError_t tc_wait_selftest(double budget_ms, int* waited_out, cudaStream_t s);
 // Cluster sizes (1, 2 or 4 CTAs sharing one B tile by TMA multicast) of the SYRK and split GRM.V.
 bool tc_set_clusters(int syrk, int grmv);
 void tc_get_clusters(int* syrk, int* grmv);
+// GRM.V column-tile width sets: plain TF32 / FP32, split-TF32, split-BF16 (multiples of 16)
+enum { kTilesPlain = 0, kTilesSplitTF32 = 1, kTilesSplitBF16 = 2 };
 // Column tile width the GRM.V kernel uses for ncols columns.
-int tc_gemm_tile_n(int64_t ncols, bool split);
-// Columns a GRM.V launch covers for ncols32 live columns (padding chosen by a cost model).
-int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, bool split, int num_sms);
+int tc_gemm_tile_n(int64_t ncols, int set);
+// Columns a GRM.V launch covers for ncols live columns (a multiple of 32, or of 16 for split-BF16),
+// padded to the width a cost model picks, at most cap.
+int64_t tc_grmv_padded_cols(int64_t ncols, int64_t cap, int64_t np, int set, int num_sms);
 // Split-TF32 GRM.V that allocates nothing: scratch in a static device array (k_tc.cu).
 int64_t tc_noalloc_max_elems();
 cudaError_t tc_gemm_tf32x3_noalloc(const float* Khi, const float* Klo, int64_t np, const float* P,

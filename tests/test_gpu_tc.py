@@ -81,8 +81,10 @@ def test_grmv_cluster_variants_bit_identical(cohort, mode):
     prev = ctx.get_tc_clusters()
     try:
         ctx.set_matvec_mode(MV_TF32X3_TC if mode == "tf32x3" else MV_BF16X3_TC)
-        # column tiles 32, 128, 160 (150 padded), 224 (200 padded), 256 and 256 (512)
-        for k in (32, 100, 150, 200, 256, 512):
+        # every tile width: split-TF32 pads to multiples of 32; split-BF16 to multiples of 16 (32, 48,
+        # 80, 112, 144, 160, 176, 208, 256, 256 here), where the odd multiples of 16 end on half a
+        # 32-column epilogue chunk and run clusters of at most 2
+        for k in (32, 40, 70, 100, 140, 150, 170, 200, 256, 512):
             V = rng.standard_normal((grm.n, k))
             ctx.set_tc_clusters(1, 1)
             Y1 = ctx.grm_matmul(V)
