@@ -206,8 +206,10 @@ struct sg_fits {
   double t_launch = 0;                                          // part of t_engine spent launching
   double gpu_ms_seen = 0;                                      // engine step time already budgeted
   double launch_wait_s = 0.0;  // with workers: how long a launch may wait for the fits just made ready
+  int idle_passes = 0;         // consecutive stepping passes in which nothing could run
   int64_t steps = 0;
   std::mutex mu;                  // engine calls and the bookkeeping above, from the worker threads
+  std::atomic<bool> step_wants{false};  // the stepping thread is waiting for mu: workers hold back
   std::unique_ptr<Workers> pool;  // null: the fits' arithmetic runs on the calling thread
 };
 
@@ -349,10 +351,27 @@ void fail(sg_fits* F, Fit& f, int code, const std::string& msg) {
   }
 }
 
+// The driver's lock as a worker takes it: after the stepping thread, which is waiting to turn a
+// finished step around (StepLock), so that it waits for at most the engine call in progress.
+std::unique_lock<std::mutex> worker_lock(sg_fits* F) {
+  while (F->step_wants.load(std::memory_order_acquire)) std::this_thread::yield();
+  return std::unique_lock<std::mutex>(F->mu);
+}
+
+struct StepLock {
+  sg_fits* F;
+  explicit StepLock(sg_fits* f) : F(f) {
+    F->step_wants.store(true, std::memory_order_release);
+    F->mu.lock();
+    F->step_wants.store(false, std::memory_order_release);
+  }
+  ~StepLock() { F->mu.unlock(); }
+};
+
 // One engine call (and whatever bookkeeping fn does with its result) under the fit driver's lock.
 template <typename Fn>
 bool eng(sg_fits* F, Fit& f, double* timer, Fn fn) {
-  std::lock_guard<std::mutex> g(F->mu);
+  const auto g = worker_lock(F);
   const double t = now_s();
   const int rc = fn();
   if (timer) *timer += now_s() - t;
@@ -819,7 +838,7 @@ bool ready_locked(sg_fits* F, const Fit& f) {
 
 bool is_ready(sg_fits* F, const Fit& f) {
   if (f.stage == S_NONE) return false;
-  std::lock_guard<std::mutex> g(F->mu);
+  const auto g = worker_lock(F);
   return ready_locked(F, f);
 }
 
@@ -1050,6 +1069,17 @@ static int fits_submit_impl(sg_fits* F, int trait, int64_t n_sub, const uint8_t*
   return SG_OK;
 }
 
+// Launch the next engine step (the caller holds F->mu).
+static int launch_step(sg_fits* F) {
+  const double t = now_s();
+  int64_t fin = 0;
+  int launched = 0;
+  const int rc = sg_engine_launch(F->ctx, &fin, &launched);
+  F->launched = rc == SG_OK && launched != 0;
+  F->t_launch += now_s() - t;
+  return rc;
+}
+
 static int engine_error(sg_fits* F, int rc) {
   const char* m = sg_last_error(F->ctx);
   return fits_err(F, rc, "engine step: %s", m ? m : "error");
@@ -1151,42 +1181,39 @@ static int run_async(sg_fits* F, int64_t max_steps, size_t before) {
     if (F->active.empty() && F->pending.empty()) break;
     double t = now_s();
     if (F->launched) sg_engine_wait(F->ctx);
+    // under one hold of the lock: finish the step, mark its columns done, collect the fits they
+    // make ready and (without a launch wait) launch the next step
     int rc = SG_OK;
+    std::vector<Fit*> todo;
+    bool launch_now = F->launch_wait_s <= 0.0;
     {
-      std::lock_guard<std::mutex> g(F->mu);
+      StepLock g(F);
       int64_t fin = 0;
       if (F->launched) rc = sg_engine_finish(F->ctx, &fin);
       F->launched = false;
       if (rc == SG_OK) rc = poll_done(F);
-    }
-    if (rc != SG_OK) return engine_error(F, rc);
-    F->t_engine += now_s() - t;
-    // hand the fits whose columns are done to the workers; optionally give them a moment, so that
-    // what they submit rides the next step instead of the one after
-    take_back(F);
-    std::vector<Fit*> todo;
-    {
-      std::lock_guard<std::mutex> g(F->mu);
-      for (auto& kv : F->active) {
-        Fit& f = *kv.second;
-        if (!f.busy && !f.failed && f.phase != P_DONE && ready_locked(F, f)) {
-          f.busy = true;
-          todo.push_back(&f);
+      if (rc == SG_OK) {
+        take_back(F);
+        for (auto& kv : F->active) {
+          Fit& f = *kv.second;
+          if (!f.busy && !f.failed && f.phase != P_DONE && ready_locked(F, f)) {
+            f.busy = true;
+            todo.push_back(&f);
+          }
         }
+        launch_now = launch_now || todo.empty();
+        if (launch_now) rc = launch_step(F);
       }
     }
-    F->pool->push(todo);
-    if (F->launch_wait_s > 0.0 && !todo.empty()) F->pool->wait_idle_for(F->launch_wait_s);
-    t = now_s();
-    {
-      std::lock_guard<std::mutex> g(F->mu);
-      int64_t fin2 = 0;
-      int launched = 0;
-      rc = sg_engine_launch(F->ctx, &fin2, &launched);
-      F->launched = launched != 0;
-      F->t_launch += now_s() - t;
-    }
     if (rc != SG_OK) return engine_error(F, rc);
+    F->pool->push(todo);
+    if (!launch_now) {
+      // give the workers a moment, so that what they submit rides this step instead of the next
+      F->pool->wait_idle_for(F->launch_wait_s);
+      StepLock g(F);
+      rc = launch_step(F);
+      if (rc != SG_OK) return engine_error(F, rc);
+    }
     F->t_engine += now_s() - t;
     F->steps += 1;
     take_back(F);
@@ -1194,12 +1221,19 @@ static int run_async(sg_fits* F, int64_t max_steps, size_t before) {
     if (!F->launched) {
       bool busy = false;
       for (const auto& kv : F->active) busy = busy || kv.second->busy;
-      // nothing on the GPU: wait for the fits being resumed to submit
       if (busy) {
+        // nothing on the GPU: wait for the fits being resumed to submit
         F->pool->wait_idle();
-      } else if (retired == 0 && !F->active.empty()) {
+        F->idle_passes = 0;
+      } else if (retired > 0 || !todo.empty() || F->active.empty()) {
+        F->idle_passes = 0;
+      } else if (++F->idle_passes >= 2) {
+        // twice in a row nothing ran, nothing was resumed and no worker held a fit (once could be a
+        // worker that submitted, or whose columns finished, after this pass launched and scanned)
         return fits_err(F, SG_ERR_STATE, "engine idle while %zu fits wait for columns", F->active.size());
       }
+    } else {
+      F->idle_passes = 0;
     }
     if (F->finished_order.size() > before) break;
   }

@@ -167,3 +167,23 @@ def test_native_driver_failing_fit_and_serving(fake_lib, cohort):
     finally:
         ctx.close()
     assert len(done) == 7 and all(j.error is None for j in done)
+
+
+@pytest.mark.parametrize("rep", range(3))
+def test_native_driver_serving_stress(fake_lib, cohort, rep):
+    """Many short arrivals into few slots, with steps of 50 us: fits start, submit and finish while
+    the calling thread steps, so every ordering of a worker's submission against a launch and a
+    stall check occurs; every fit completes with its result alone."""
+    grm, specs, _ = cohort
+    alone, _ = _run(fake_lib, grm, specs, threads=1)
+    ctx = _ctx(fake_lib, grm, 0.05)
+    try:
+        arrivals = [(0.0005 * i, specs[(i + rep) % len(specs)]) for i in range(18)]
+        done = native.serve(ctx, arrivals, max_columns=256, max_phenos=3, threads=4, lib=fake_lib)
+        assert ctx.requests() == 0
+    finally:
+        ctx.close()
+    assert len(done) == 18 and all(j.error is None for j in done)
+    for j in done:
+        k = specs.index(j.spec)
+        assert np.array_equal(j.result["theta"], alone[k]["theta"])
