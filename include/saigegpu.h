@@ -242,6 +242,13 @@ int sg_engine_submit(sg_ctx *ctx, int64_t slot, int kind, const double *B, int64
 /* Submit Rademacher probes (counter hash of seed, run0+j, sample) as PCG (kind 0) or product (kind 1) columns. */
 int sg_engine_submit_probes(sg_ctx *ctx, int64_t slot, int kind, uint64_t seed, int64_t run0,
                             int64_t k, int maxiter, double tol, int64_t *ids);
+/* Queue k PCG solves whose right-hand sides are the results of requests src_ids[k] (e.g. a K b
+ * product, solved as Sigma x = K b without a round trip through the host).  Each is admitted at the
+ * first launch after its source has finished; if the source is fetched, cancelled or reduced first,
+ * its result is copied to the solve's own right-hand side (a source cancelled before it finished
+ * cancels the solve).  Needs held results (sg_engine_hold_results).  No reference counterpart. */
+int sg_engine_submit_chained(sg_ctx *ctx, int64_t slot, const int64_t *src_ids, int64_t k, int maxiter,
+                             double tol, int64_t *ids);
 /* Run up to max_steps engine steps (admitting queued columns as slots free up).
  * Returns after the step in which at least one column retired, or when idle. */
 int sg_engine_run(sg_ctx *ctx, int64_t max_steps, int64_t *n_finished);

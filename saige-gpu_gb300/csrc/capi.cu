@@ -39,6 +39,7 @@ struct Req {
   int64_t col = -1;
   std::vector<double> x;
   int32_t iters = 0;
+  int64_t src = -1;   // chained: the right-hand side is this request's result (admitted once it is done)
 };
 
 struct Engine {
@@ -55,6 +56,7 @@ struct Engine {
   std::vector<char> ph_set;
   std::deque<int64_t> queue;
   std::unordered_map<int64_t, Req> reqs;
+  std::unordered_multimap<int64_t, int64_t> deps;  // source request -> chained requests still queued
   int64_t next_id = 1;
   int64_t hi_col = 0;
   int64_t n_active = 0;
@@ -104,6 +106,10 @@ struct Engine {
   double t_finish_host_ms = 0.0;  // host time a finish spends after the step has drained
   cudaEvent_t ev_adm = nullptr;
   bool adm_recorded = false;
+  // set_pheno uploads without waiting: the next set_pheno reuses the staging buffer after ev_pheno,
+  // and the next launch's work on the main stream waits for it
+  cudaEvent_t ev_pheno = nullptr;
+  bool pheno_stage_busy = false, pheno_main_wait = false;
   double t_step_ms = 0, t_gemm_ms = 0, gemm_launches = 0, gemm_flops = 0, gemm_cols = 0, useful_cols = 0;
   // per-step records since the last timing reset (the first kStepTrace steps):
   // [columns the GRM.V computed, occupied columns, GRM.V ms, step ms, idle ms before the step]
@@ -869,6 +875,8 @@ static cudaError_t d2h(sg_ctx* c, void* dst, const void* src, size_t bytes, cuda
 
 static void engine_free(sg_ctx* c) {
   Engine& e = c->eng;
+  cudaStreamSynchronize(c->side);  // a weight upload may still read the staging buffer
+  e.pheno_stage_busy = e.pheno_main_wait = false;
   dev_free_t(c, e.X); dev_free_t(c, e.R); dev_free_t(c, e.Z); dev_free_t(c, e.P);
   dev_free_t(c, e.B); dev_free_t(c, e.part); dev_free_t(c, e.winv); dev_free_t(c, e.minv);
   dev_free_t(c, e.Yd); dev_free_t(c, e.Pf); dev_free_t(c, e.Yf); dev_free_t(c, e.d_st);
@@ -911,6 +919,7 @@ static void engine_free(sg_ctx* c) {
   e.n_active = 0;
   e.queue.clear();
   e.reqs.clear();
+  e.deps.clear();
   e.h_st.clear();
   e.col_req.clear();
   e.ph_set.clear();
@@ -947,6 +956,7 @@ static int engine_clear(sg_ctx* c) {
   e.queue.clear();
   for (auto& kv : e.reqs) slab_put(e, kv.second);
   e.reqs.clear();
+  e.deps.clear();
   return sync(c);
 }
 
@@ -994,6 +1004,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   for (auto& ev : e.ev_prev)
     if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
   if (!e.ev_adm) SG_CUDA(c, cudaEventCreate(&e.ev_adm));
+  if (!e.ev_pheno) SG_CUDA(c, cudaEventCreateWithFlags(&e.ev_pheno, cudaEventDisableTiming));
   e.have_prev = false;
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_gcols), max_columns * sizeof(int32_t), cudaHostAllocDefault));
@@ -1018,6 +1029,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   e.n_active = 0;
   e.queue.clear();
   e.reqs.clear();
+  e.deps.clear();
   SG_TRY(sync(c));
   (void)old_ph; (void)old_set;
   return SG_OK;
@@ -1046,6 +1058,10 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
       return set_err(c, SG_ERR_STATE, "phenotype slot %lld has columns in flight", (long long)slot);
   // W (and the sample mask) go up through pinned staging; 1/W and the Jacobi preconditioner
   // 1/diag(Sigma) are formed on the device from the resident FP64 diagonal
+  if (e.pheno_stage_busy) {  // the previous upload has left the staging buffer (long since, as a rule)
+    SG_CUDA(c, cudaEventSynchronize(e.ev_pheno));
+    e.pheno_stage_busy = false;
+  }
   {
     double* hw = e.h_stage;
     uint8_t* hm = reinterpret_cast<uint8_t*>(e.h_stage + e.np);
@@ -1064,7 +1080,9 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
   e.h_ph[slot] = PhenoState{tau[0], tau[1]};
   SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), c->side));
   e.ph_set[slot] = 1;
-  return sync_side(c);  // the pinned staging is reused by the next call
+  SG_CUDA(c, cudaEventRecord(e.ev_pheno, c->side));
+  e.pheno_stage_busy = e.pheno_main_wait = true;
+  return SG_OK;
 }
 
 static int engine_submit_common(sg_ctx* c, int64_t slot, int kind, const double* B, bool probe,
@@ -1105,6 +1123,35 @@ extern "C" int sg_engine_submit(sg_ctx* c, int64_t slot, int kind, const double*
 extern "C" int sg_engine_submit_probes(sg_ctx* c, int64_t slot, int kind, uint64_t seed, int64_t run0,
                                        int64_t k, int maxiter, double tol, int64_t* ids) {
   return engine_submit_common(c, slot, kind, nullptr, true, seed, run0, k, maxiter, tol, ids);
+}
+
+extern "C" int sg_engine_submit_chained(sg_ctx* c, int64_t slot, const int64_t* src_ids, int64_t k, int maxiter,
+                                        double tol, int64_t* ids) {
+  NEED_GRM(c);
+  Engine& e = c->eng;
+  if (!e.hold) return set_err(c, SG_ERR_STATE, "chained solves need held results (sg_engine_hold_results)");
+  if (slot < 0 || slot >= e.cap_ph || !e.ph_set[slot])
+    return set_err(c, SG_ERR_STATE, "phenotype slot %lld not set", (long long)slot);
+  if (k < 0 || (k > 0 && !src_ids)) return set_err(c, SG_ERR_INVALID, "bad source list");
+  for (int64_t j = 0; j < k; ++j)
+    if (!e.reqs.count(src_ids[j]))
+      return set_err(c, SG_ERR_NOT_FOUND, "unknown source request %lld", (long long)src_ids[j]);
+  for (int64_t j = 0; j < k; ++j) {
+    Req r;
+    r.id = e.next_id++;
+    r.slot = slot;
+    r.kind = 0;
+    r.maxiter = maxiter;
+    r.tol = tol;
+    r.src = src_ids[j];
+    // a slab for the source's result, should the source be fetched before this one is admitted
+    if (!slab_get(c, r)) return set_err(c, SG_ERR_NOMEM, "no pinned host memory for a right-hand side");
+    if (ids) ids[j] = r.id;
+    e.deps.emplace(r.src, r.id);
+    e.queue.push_back(r.id);
+    e.reqs.emplace(r.id, std::move(r));
+  }
+  return SG_OK;
 }
 
 // Column-state updates go up in one block: stage (col, state) pairs, then flush_states copies them
@@ -1167,8 +1214,48 @@ static void slab_put(Engine& e, Req& r) {
 }
 
 // Move queued requests into free columns, staged through e.B, and initialise them.
+static void unlink_dep(Engine& e, int64_t src, int64_t dep) {
+  auto range = e.deps.equal_range(src);
+  for (auto it = range.first; it != range.second; ++it)
+    if (it->second == dep) {
+      e.deps.erase(it);
+      return;
+    }
+}
+
+// Before a finished request's column is released: the chained requests still queued on it get its
+// result in their own right-hand-side slabs.  Before an unfinished one is cancelled: they are
+// cancelled with it (their right-hand side will never exist).
+static int detach_dependents(sg_ctx* c, Req& src) {
+  Engine& e = c->eng;
+  auto range = e.deps.equal_range(src.id);
+  if (range.first == range.second) return SG_OK;
+  std::vector<int64_t> ds;
+  for (auto it = range.first; it != range.second; ++it) ds.push_back(it->second);
+  e.deps.erase(src.id);
+  bool copied = false;
+  for (int64_t d : ds) {
+    auto it = e.reqs.find(d);
+    if (it == e.reqs.end()) continue;
+    Req& r = it->second;
+    if (src.state == 2 && src.col >= 0 && r.b) {
+      SG_CUDA(c, d2h(c, r.b, e.X + src.col * e.np, c->nn * 8, c->side));
+      r.src = -1;
+      copied = true;
+    } else {
+      slab_put(e, r);
+      e.reqs.erase(it);  // its queue entry is skipped at admission
+    }
+  }
+  return copied ? sync_side(c) : SG_OK;
+}
+
 static int engine_admit(sg_ctx* c) {
   Engine& e = c->eng;
+  if (e.pheno_main_wait) {  // slot weights uploaded since the last launch: the step reads them
+    SG_CUDA(c, cudaStreamWaitEvent(c->stream, e.ev_pheno, 0));
+    e.pheno_main_wait = false;
+  }
   // the previous admission's copies have run (the stream drained at the last finish / sync)
   for (int64_t id : e.slab_pending) {
     auto it = e.reqs.find(id);
@@ -1195,6 +1282,7 @@ static int engine_admit(sg_ctx* c) {
     std::vector<const double*> rsrc;
     std::vector<int32_t> rsel;
     int64_t col = 0;
+    std::vector<int64_t> later;  // chained requests whose source has not finished: stay queued, in order
     while (!e.queue.empty() && (int64_t)cols.size() < e.stage_cols) {
       while (col < e.cap_cols && e.col_req[col] != -1) ++col;
       if (col >= e.cap_cols) break;
@@ -1204,7 +1292,17 @@ static int engine_admit(sg_ctx* c) {
       if (it == e.reqs.end()) continue;  // cancelled
       Req& r = it->second;
       const int64_t sel = (int64_t)cols.size();
-      if (r.probe) {
+      if (r.src >= 0) {
+        auto is = e.reqs.find(r.src);
+        if (is == e.reqs.end() || is->second.state != 2 || is->second.col < 0) {
+          later.push_back(id);
+          continue;
+        }
+        rsrc.push_back(e.X + is->second.col * e.np);  // the source's result, still in its column
+        rsel.push_back((int32_t)sel);
+        unlink_dep(e, r.src, id);
+        r.src = -1;
+      } else if (r.probe) {
         pseeds.push_back(r.seed);
         pruns.push_back(r.run);
         psel.push_back((int32_t)sel);
@@ -1231,6 +1329,7 @@ static int engine_admit(sg_ctx* c) {
       e.hi_col = std::max(e.hi_col, col + 1);
       ++col;
     }
+    e.queue.insert(e.queue.begin(), later.begin(), later.end());
     if (cols.empty()) break;
     SG_TRY(flush_states(c, false));  // the round's closing synchronisation frees the staging
     if (!rsrc.empty()) {
@@ -1648,6 +1747,7 @@ extern "C" int sg_engine_fetch(sg_ctx* c, int64_t id, double* x, int32_t* iters)
   if (it == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
   Req& r = it->second;
   if (r.state != 2) return set_err(c, SG_ERR_STATE, "request %lld not finished", (long long)id);
+  SG_TRY(detach_dependents(c, r));
   if (r.col >= 0) {
     if (x) SG_CUDA(c, d2h(c, x, e.X + r.col * e.np, c->nn * 8, c->side));
     SG_TRY(release_col(c, r.col));
@@ -1666,6 +1766,8 @@ extern "C" int sg_engine_cancel(sg_ctx* c, int64_t id) {
   auto it = e.reqs.find(id);
   if (it == e.reqs.end()) return set_err(c, SG_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
   Req& r = it->second;
+  SG_TRY(detach_dependents(c, r));
+  if (r.src >= 0) unlink_dep(e, r.src, r.id);
   if ((r.state == 1 || r.state == 2) && r.col >= 0) {
     if (r.state == 1) e.n_active -= 1;
     SG_TRY(release_col(c, r.col));
@@ -1785,6 +1887,7 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
     if (id < 0) continue;
     auto it = e.reqs.find(id);
     if (iters && j < k) iters[j] = it->second.iters;
+    SG_TRY(detach_dependents(c, it->second));
     SG_TRY(release_col(c, it->second.col));
     e.reqs.erase(it);
   }

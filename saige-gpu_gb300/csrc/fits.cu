@@ -40,7 +40,7 @@ double now_s() {
 }
 
 enum Phase { P_INIT_COEF, P_INIT_AI, P_LOOP_COEF, P_LOOP_AI, P_FINAL_COEF, P_DONE };
-enum Stage { S_NONE, S_GC_WAIT, S_AI_WAIT_APY, S_AI_WAIT_PROBES, S_AI_WAIT_SID };
+enum Stage { S_NONE, S_GC_WAIT, S_AI_WAIT_PROBES, S_AI_WAIT_SID };
 
 struct FitError {
   int code;
@@ -91,7 +91,6 @@ struct Fit {
   std::vector<int64_t> wait_ids;
   bool wait_fetch = false;
   std::vector<std::vector<double>> fetched;  // kept between stages (their buffers are reused)
-  std::vector<double> rhs;                     // reused staging for two-column submissions
   // bookkeeping
   int64_t column_iterations = 0, columns = 0;
   bool failed = false;
@@ -404,6 +403,16 @@ bool submit(sg_fits* F, Fit& f, int kind, const double* B, int64_t k, int maxite
   });
 }
 
+// one PCG solve of Sigma x = (result of request src), chained on the engine
+bool submit_chained(sg_fits* F, Fit& f, int64_t src, std::vector<int64_t>& ids) {
+  ids.assign(1, -1);
+  return eng(F, f, &F->t_submit, [&] {
+    const int rc = sg_engine_submit_chained(F->ctx, f.slot, &src, 1, f.maxiter_pcg, f.tol_pcg, ids.data());
+    if (rc == SG_OK) own(F, f, ids);
+    return rc;
+  });
+}
+
 bool submit_probes(sg_fits* F, Fit& f, int64_t run0, int64_t k, std::vector<int64_t>& ids) {
   ids.assign(k, -1);
   return eng(F, f, &F->t_submit, [&] {
@@ -514,29 +523,23 @@ bool ai_begin(sg_fits* F, Fit& f) {
   }
   f.PY.resize(n);
   project(f, f.ai_cov, f.SY.data(), f.YX.data(), f.PY.data());
+  // APY = K PY, then Sigma^-1 APY chained to it on the engine (admitted as soon as the product is
+  // done, no trip through the host) and, quantitative, Sigma^-1 PY; APY itself is fetched with them
   std::vector<int64_t> a;
   if (!submit(F, f, 1, f.PY.data(), 1, 1, 0.0, a)) return false;
   f.apy_id = a[0];
+  if (!submit_chained(F, f, f.apy_id, f.sid)) return false;
+  if (f.quant) {
+    std::vector<int64_t> q;
+    if (!submit(F, f, 0, f.PY.data(), 1, f.maxiter_pcg, f.tol_pcg, q)) return false;
+    f.sid.push_back(q[0]);
+  }
   if (!submit_probes(F, f, 0, f.nrun, f.pid)) return false;
   if (!probe_products(F, f, 0, f.nrun, f.aid)) return false;
   f.run0 = 0;
   f.k = f.nrun;
   f.t1.clear();
   f.t0.clear();
-  wait_for(f, S_AI_WAIT_APY, {f.apy_id}, true);
-  return true;
-}
-
-bool ai_after_apy(sg_fits* F, Fit& f) {
-  f.APY.swap(f.fetched[0]);
-  const double* rhs = f.APY.data();
-  if (f.quant) {  // [APY | PY]
-    f.rhs.resize(2 * (size_t)f.n);
-    std::copy(f.APY.begin(), f.APY.end(), f.rhs.begin());
-    std::copy(f.PY.begin(), f.PY.end(), f.rhs.begin() + f.n);
-    rhs = f.rhs.data();
-  }
-  if (!submit(F, f, 0, rhs, f.quant ? 2 : 1, f.maxiter_pcg, f.tol_pcg, f.sid)) return false;
   std::vector<int64_t> w(f.pid);
   w.insert(w.end(), f.aid.begin(), f.aid.end());
   wait_for(f, S_AI_WAIT_PROBES, w, false);
@@ -587,7 +590,9 @@ bool ai_after_probes(sg_fits* F, Fit& f) {
     wait_for(f, S_AI_WAIT_PROBES, w, false);
     return true;
   }
-  wait_for(f, S_AI_WAIT_SID, f.sid, true);
+  std::vector<int64_t> w{f.apy_id};
+  w.insert(w.end(), f.sid.begin(), f.sid.end());
+  wait_for(f, S_AI_WAIT_SID, w, true);
   return true;
 }
 
@@ -595,7 +600,8 @@ AiScore ai_finish(Fit& f) {
   const int64_t n = f.n;
   AiScore re;
   std::vector<double> PAPY(n);
-  project(f, f.ai_cov, f.fetched[0].data(), f.fetched[0].data(), PAPY.data());
+  f.APY.swap(f.fetched[0]);
+  project(f, f.ai_cov, f.fetched[1].data(), f.fetched[1].data(), PAPY.data());
   double s1 = 0.0, s0 = 0.0;
   for (double v : f.t1) s1 += v;
   for (double v : f.t0) s0 += v;
@@ -605,7 +611,7 @@ AiScore ai_finish(Fit& f) {
   const double* apy = f.APY.data();
   if (f.quant) {
     std::vector<double> PA0PY(n);
-    project(f, f.ai_cov, f.fetched[1].data(), f.fetched[1].data(), PA0PY.data());
+    project(f, f.ai_cov, f.fetched[2].data(), f.fetched[2].data(), PA0PY.data());
     const double* a[5] = {py, py, py, py, apy};
     const double* b[5] = {apy, py, PA0PY.data(), PAPY.data(), PAPY.data()};
     double d[5];
@@ -816,8 +822,6 @@ bool resume(sg_fits* F, Fit& f) {
       if (!gc_step(F, f, &done)) return false;
       return done ? coef_done(F, f) : true;
     }
-    case S_AI_WAIT_APY:
-      return ai_after_apy(F, f);
     case S_AI_WAIT_PROBES:
       return ai_after_probes(F, f);
     case S_AI_WAIT_SID:

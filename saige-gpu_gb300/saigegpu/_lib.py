@@ -89,6 +89,7 @@ SIGNATURES = {
     "sg_engine_submit": [c_ctx, c_i64, C.c_int, P_f64, c_i64, C.c_int, C.c_double, P_i64],
     "sg_engine_submit_probes": [c_ctx, c_i64, C.c_int, c_u64, c_i64, c_i64, C.c_int, C.c_double,
                                 P_i64],
+    "sg_engine_submit_chained": [c_ctx, c_i64, P_i64, c_i64, C.c_int, C.c_double, P_i64],
     "sg_engine_run": [c_ctx, c_i64, P_i64],
     "sg_engine_launch": [c_ctx, P_i64, P_i32],
     "sg_engine_finish": [c_ctx, P_i64],

@@ -433,6 +433,14 @@ class Context:
                    int(maxiter), float(tol), _ptr(ids, L.P_i64))
         return ids
 
+    def engine_submit_chained(self, slot, src_ids, maxiter=500, tol=1e-5):
+        """PCG solves whose right-hand sides are the results of the requests src_ids."""
+        src = np.ascontiguousarray(src_ids, np.int64)
+        ids = np.empty(len(src), np.int64)
+        self._call("sg_engine_submit_chained", int(slot), _ptr(src, L.P_i64), len(src), int(maxiter), float(tol),
+                   _ptr(ids, L.P_i64))
+        return ids
+
     def engine_run(self, max_steps=1 << 30):
         fin = C.c_int64()
         self._call("sg_engine_run", int(max_steps), C.byref(fin))

@@ -39,6 +39,7 @@ struct Req {
   int kind = 0, maxiter = 0, iters = 0, state = Q_QUEUED;
   double tol = 0.0, rz = 0.0, sumr2 = 0.0;
   bool stop = false;  // the launched step ended this column
+  int64_t src = -1;   // chained: the right-hand side is this request's result
   std::vector<double> b, x, r, z, p;
 };
 
@@ -99,12 +100,22 @@ double dot(const std::vector<double>& a, const std::vector<double>& b) {
 }
 
 void admit(sg_ctx* c) {
+  std::deque<int64_t> later;  // chained requests whose source has not finished, in order
   while (!c->queue.empty() && c->running_or_held < c->cap_cols) {
     const int64_t id = c->queue.front();
     c->queue.pop_front();
     auto it = c->reqs.find(id);
     if (it == c->reqs.end()) continue;  // cancelled while queued
     Req& q = it->second;
+    if (q.src >= 0) {
+      auto is = c->reqs.find(q.src);
+      if (is == c->reqs.end() || is->second.state != Q_DONE) {
+        later.push_back(id);
+        continue;
+      }
+      q.b = is->second.x;
+      q.src = -1;
+    }
     const Slot& s = c->slots[q.slot];
     const int64_t n = c->n;
     q.state = Q_RUNNING;
@@ -120,6 +131,26 @@ void admit(sg_ctx* c) {
     q.iters = 0;
     q.stop = q.kind == 0 && !(q.sumr2 > q.tol && q.iters < q.maxiter);
   }
+  c->queue.insert(c->queue.begin(), later.begin(), later.end());
+}
+
+// Before request id leaves: chained requests queued on it take its result, or are cancelled with
+// it when it has none.
+void detach(sg_ctx* c, int64_t id) {
+  auto is = c->reqs.find(id);
+  if (is == c->reqs.end()) return;
+  std::vector<int64_t> gone;
+  for (auto& kv : c->reqs) {
+    Req& q = kv.second;
+    if (q.src != id) continue;
+    if (is->second.state == Q_DONE) {
+      q.b = is->second.x;
+      q.src = -1;
+    } else {
+      gone.push_back(kv.first);
+    }
+  }
+  for (int64_t g : gone) c->reqs.erase(g);
 }
 
 // One PCG iteration (or the product) of a running column.
@@ -281,6 +312,29 @@ int sg_engine_submit_probes(sg_ctx* c, int64_t slot, int kind, uint64_t seed, in
   return submit_common(c, slot, kind, nullptr, true, seed, run0, k, maxiter, tol, ids);
 }
 
+int sg_engine_submit_chained(sg_ctx* c, int64_t slot, const int64_t* src_ids, int64_t k, int maxiter, double tol,
+                             int64_t* ids) {
+  if (!c || k < 0 || (k > 0 && !src_ids)) return SG_ERR_INVALID;
+  if (!c->hold) return fail(c, SG_ERR_STATE, "chained solves need held results");
+  if (slot < 0 || slot >= (int64_t)c->slots.size() || !c->slots[slot].set)
+    return fail(c, SG_ERR_STATE, "phenotype slot not set");
+  for (int64_t j = 0; j < k; ++j)
+    if (!c->reqs.count(src_ids[j])) return fail(c, SG_ERR_NOT_FOUND, "unknown source request");
+  for (int64_t j = 0; j < k; ++j) {
+    Req q;
+    q.slot = slot;
+    q.kind = 0;
+    q.maxiter = maxiter;
+    q.tol = tol;
+    q.src = src_ids[j];
+    const int64_t id = c->next_id++;
+    if (ids) ids[j] = id;
+    c->reqs.emplace(id, std::move(q));
+    c->queue.push_back(id);
+  }
+  return SG_OK;
+}
+
 int sg_engine_launch(sg_ctx* c, int64_t* n_finished, int* launched) {
   if (!c) return SG_ERR_INVALID;
   if (c->inflight) return fail(c, SG_ERR_STATE, "a step is in flight: finish it first");
@@ -348,6 +402,7 @@ int sg_engine_fetch(sg_ctx* c, int64_t id, double* x, int32_t* iters) {
   auto it = c->reqs.find(id);
   if (it == c->reqs.end()) return fail(c, SG_ERR_NOT_FOUND, "unknown request");
   if (it->second.state != Q_DONE) return fail(c, SG_ERR_STATE, "request not finished");
+  detach(c, id);
   if (x) std::memcpy(x, it->second.x.data(), c->n * sizeof(double));
   if (iters) *iters = it->second.iters;
   c->running_or_held -= 1;
@@ -359,6 +414,8 @@ int sg_engine_cancel(sg_ctx* c, int64_t id) {
   if (!c) return SG_ERR_INVALID;
   auto it = c->reqs.find(id);
   if (it == c->reqs.end()) return fail(c, SG_ERR_NOT_FOUND, "unknown request");
+  detach(c, id);
+  it = c->reqs.find(id);
   if (it->second.state != Q_QUEUED) c->running_or_held -= 1;
   c->reqs.erase(it);
   return SG_OK;
@@ -446,6 +503,7 @@ int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_pcg, const 
   for (int64_t j = 0; j < 2 * k; ++j) {
     const int64_t id = j < k ? ids_pcg[j] : ids_prod[j - k];
     if (id < 0) continue;
+    detach(c, id);
     c->reqs.erase(id);
     c->running_or_held -= 1;
   }

@@ -212,6 +212,64 @@ def test_native_driver_failing_fit_and_serving(cohort):
     assert len(done) == 5 and all(j.error is None for j in done)
 
 
+def test_chained_solve_equals_solve_of_fetched_product(cohort):
+    """A solve chained to a product (Sigma x = K b on the engine) equals the solve of the fetched
+    product bit for bit: admitted after the product finished, after the product was fetched first
+    (its result handed to the solve's own right-hand side), and cancelled with an unfinished source."""
+    from saigegpu import _lib as L
+    ctx, grm, specs, refs = cohort
+    n = ctx.n
+    rng = np.random.default_rng(21)
+    w = rng.uniform(0.5, 2.0, n)
+    tau = np.array([1.0, 0.4])
+    b = rng.standard_normal((n, 3))
+    ctx.engine_reserve(128, 2)
+    ctx.engine_hold_results(True)
+
+    def drive(want):
+        done = set()
+        for _ in range(3000):
+            if want <= done:
+                return
+            ctx.engine_launch()
+            ctx.engine_finish()
+            done.update(int(r) for r in ctx.engine_poll())
+        raise AssertionError("engine did not finish %s" % sorted(want - done))
+
+    def solve_direct(rhs):
+        d = int(ctx.engine_submit(0, 0, rhs, 500, 1e-10)[0])
+        drive({d})
+        return ctx.engine_fetch(d)[0]
+
+    try:
+        ctx.engine_set_pheno(0, w, tau)
+        # admitted once the product is done
+        p0 = int(ctx.engine_submit(0, 1, b[:, 0], 1, 0.0)[0])
+        c0 = int(ctx.engine_submit_chained(0, [p0], 500, 1e-10)[0])
+        drive({p0, c0})
+        x0, it0 = ctx.engine_fetch(c0)
+        kb0 = ctx.engine_fetch(p0)[0]
+        assert it0 > 0
+        np.testing.assert_array_equal(x0, solve_direct(kb0))
+        # the product fetched before the chained solve was admitted
+        p1 = int(ctx.engine_submit(0, 1, b[:, 1], 1, 0.0)[0])
+        c1 = int(ctx.engine_submit_chained(0, [p1], 500, 1e-10)[0])
+        drive({p1})
+        kb1 = ctx.engine_fetch(p1)[0]
+        drive({c1})
+        np.testing.assert_array_equal(ctx.engine_fetch(c1)[0], solve_direct(kb1))
+        # a source cancelled before it ran takes its chained solve with it
+        p2 = int(ctx.engine_submit(0, 1, b[:, 2], 1, 0.0)[0])
+        c2 = int(ctx.engine_submit_chained(0, [p2], 500, 1e-10)[0])
+        ctx.engine_cancel(p2)
+        with pytest.raises(L.SaigeGpuError):
+            ctx.engine_fetch(c2)
+        launched, _ = ctx.engine_launch()
+        assert not launched
+    finally:
+        ctx.engine_hold_results(False)
+
+
 def test_launch_finish_retires_columns_that_converge_at_init(cohort):
     """With asynchronous stepping a zero right-hand side (r'r = 0 at init) is retired when the step
     it rode along finishes: zero iterations, zero solution; the other columns are unaffected."""
