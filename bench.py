@@ -393,7 +393,7 @@ def run_ours(args, rank, world, local):
         grm_s = time.perf_counter() - t0
     else:
         from saigegpu import tune
-        tune_report = tune.tune(ctx, ncols=(128, 256, 512),
+        tune_report = tune.tune(ctx, ncols=(128, 384, 1024),
                                 mode=MV_BF16X3_TC if args.mode == "bf16x3" else MV_TF32X3_TC)
         grm_s = tune_report["syrk"][tune_report["chosen"][0]]
     d = ctx.dims()

@@ -137,6 +137,23 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
   return d;
 }
 
+// The same for K slices of RB bytes per row: SWIZZLE_128B (RB = 128) as above, or SWIZZLE_64B
+// (RB = 64: SBO = 512 B between 8-row groups, layout code 4).
+template <int RB>
+__device__ __forceinline__ uint64_t smem_desc_kmajor(uint32_t addr) {
+  if constexpr (RB == 128) {
+    return smem_desc_sw128(addr);
+  } else {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)((8 * RB) >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)4 << 61;
+    return d;
+  }
+}
+
 // Instruction descriptor: FP32 accumulator, A/B format (1 = BF16 for
 // kind::f16, 2 = TF32 for kind::tf32), both K-major, N >> 3 at bit 17,
 // M >> 4 at bit 24.
@@ -219,19 +236,25 @@ struct TileCoord {
 // cuts the L2->SM operand traffic of B by kC.  Each stage is then refilled only when every CTA of
 // the cluster has consumed it (the empty barrier counts kC multicast MMA commits).
 // Rows >= nrows of a tile (a padding row block that completes the last cluster) are not stored.
-template <bool kTF32, int BN, int S, bool kSplit, int kC>
+// RB: bytes of one operand row's K slice per pipeline stage -- 128 (SWIZZLE_128B, the TF32
+// kernels and the SYRK) or 64 (SWIZZLE_64B: half the bytes per stage, twice the stages in the
+// same shared memory, for the split-BF16 GRM.V, whose four operand tiles per stage left it with
+// only two stages of 128-byte slices).
+template <bool kTF32, int BN, int S, bool kSplit, int kC, int RB = 128>
 __global__ void __launch_bounds__(128, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
                const TileCoord* __restrict__ tiles, int num_kb, float* __restrict__ D, int64_t ldd,
                float scale, int mode, int64_t nrows, const int32_t* __restrict__ colmap) {
+  static_assert(RB == 128 || RB == 64, "K slices of 128 or 64 bytes");
   static_assert(kC == 1 || (BN / kC) % 8 == 0, "B slices must be whole 8-row swizzle atoms");
+  constexpr int kATile = kTileM * RB;
   constexpr int kSliceRows = BN / kC;
-  constexpr int kSliceBytes = kSliceRows * kRowBytes;
-  constexpr int kBTileBytes = BN * kRowBytes;
-  constexpr int kStageBytes = (kATileBytes + kBTileBytes) * (kSplit ? 2 : 1);
+  constexpr int kSliceBytes = kSliceRows * RB;
+  constexpr int kBTileBytes = BN * RB;
+  constexpr int kStageBytes = (kATile + kBTileBytes) * (kSplit ? 2 : 1);
   constexpr uint32_t kFmt = kTF32 ? 2u : 1u;
-  constexpr int kKSteps = 4;           // 128-byte slice / 32 bytes per MMA K step
+  constexpr int kKSteps = RB / 32;     // 32 bytes of K per MMA
   // TMEM is allocated in powers of two >= 32 columns
   constexpr uint32_t kTmemCols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
   constexpr uint32_t kIdesc = make_idesc(kFmt, BN);
@@ -280,20 +303,20 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
       if (!mbar_wait(&empty[s], ph ^ 1u, 1, abort_flag)) break;
       uint8_t* st = smem + s * kStageBytes;
       mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
-      const int32_t x = kb * (kRowBytes / (kTF32 ? 4 : 2));
+      const int32_t x = kb * (RB / (kTF32 ? 4 : 2));
       tma_load_2d(st, &mapA, &full[s], x, ya);
       if constexpr (kC == 1) {
-        tma_load_2d(st + kATileBytes, &mapB, &full[s], x, yb);
+        tma_load_2d(st + kATile, &mapB, &full[s], x, yb);
       } else {
-        tma_load_2d_mcast(st + kATileBytes + crank * kSliceBytes, &mapB, &full[s], x,
+        tma_load_2d_mcast(st + kATile + crank * kSliceBytes, &mapB, &full[s], x,
                           yb + (int32_t)crank * kSliceRows, kMask);
       }
       if constexpr (kSplit) {
-        tma_load_2d(st + kATileBytes + kBTileBytes, &mapA2, &full[s], x, ya);
+        tma_load_2d(st + kATile + kBTileBytes, &mapA2, &full[s], x, ya);
         if constexpr (kC == 1) {
-          tma_load_2d(st + 2 * kATileBytes + kBTileBytes, &mapB2, &full[s], x, yb);
+          tma_load_2d(st + 2 * kATile + kBTileBytes, &mapB2, &full[s], x, yb);
         } else {
-          tma_load_2d_mcast(st + 2 * kATileBytes + kBTileBytes + crank * kSliceBytes, &mapB2, &full[s], x,
+          tma_load_2d_mcast(st + 2 * kATile + kBTileBytes + crank * kSliceBytes, &mapB2, &full[s], x,
                             yb + (int32_t)crank * kSliceRows, kMask);
         }
       }
@@ -306,16 +329,16 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
       if (!mbar_wait(&full[s], ph, 2, abort_flag)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t a0 = smem_u32(smem + s * kStageBytes);
-      const uint32_t b0 = a0 + kATileBytes;
+      const uint32_t b0 = a0 + kATile;
 #pragma unroll
       for (int k = 0; k < kKSteps; ++k) {
         const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
-        umma<kTF32>(tmem_base, smem_desc_sw128(a0 + 32 * k), smem_desc_sw128(b0 + 32 * k), kIdesc, acc);
+        umma<kTF32>(tmem_base, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, acc);
         if constexpr (kSplit) {
           const uint32_t a1 = b0 + kBTileBytes;      // Al
-          const uint32_t b1 = a1 + kATileBytes;      // Bl
-          umma<kTF32>(tmem_base, smem_desc_sw128(a0 + 32 * k), smem_desc_sw128(b1 + 32 * k), kIdesc, 1u);
-          umma<kTF32>(tmem_base, smem_desc_sw128(a1 + 32 * k), smem_desc_sw128(b0 + 32 * k), kIdesc, 1u);
+          const uint32_t b1 = a1 + kATile;           // Bl
+          umma<kTF32>(tmem_base, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
+          umma<kTF32>(tmem_base, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, 1u);
         }
       }
       // stage reusable once these MMAs have read it (in every CTA of the cluster)
@@ -391,34 +414,35 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2D K-major map: rows x inner elements, row stride in bytes, box = 128 B x box_rows.
+// 2D K-major map: rows x inner elements, row stride in bytes, box = slice_bytes (128: SWIZZLE_128B,
+// 64: SWIZZLE_64B) x box_rows.
 bool make_map(CUtensorMap* m, const void* base, bool f32, uint64_t inner, uint64_t rows,
-              uint64_t row_bytes, uint32_t box_rows) {
+              uint64_t row_bytes, uint32_t box_rows, int slice_bytes = kRowBytes) {
   auto fn = encode_fn();
   if (!fn) return false;
   const cuuint64_t dims[2] = {inner, rows};
   const cuuint64_t strides[1] = {row_bytes};
-  const cuuint32_t box[2] = {(cuuint32_t)(kRowBytes / (f32 ? 4 : 2)), box_rows};
+  const cuuint32_t box[2] = {(cuuint32_t)(slice_bytes / (f32 ? 4 : 2)), box_rows};
   const cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                   const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                  slice_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
-template <bool kTF32, int BN, int S, bool kSplit>
+template <bool kTF32, int BN, int S, bool kSplit, int RB = kRowBytes>
 constexpr size_t smem_bytes() {
-  return (size_t)S * (kATileBytes + BN * kRowBytes) * (kSplit ? 2 : 1) + 1024 + 256;
+  return (size_t)S * (kTileM * RB + BN * RB) * (kSplit ? 2 : 1) + 1024 + 256;
 }
 
-template <bool kTF32, int BN, int S, bool kSplit, int kC = 1>
+template <bool kTF32, int BN, int S, bool kSplit, int kC = 1, int RB = kRowBytes>
 cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
                    const CUtensorMap& b2, const TileCoord* tiles, int ntiles, int num_kb, float* D,
                    int64_t ldd, float scale, int mode, cudaStream_t s, int64_t nrows,
                    const int32_t* colmap = nullptr) {
-  auto k = tc_gemm_kernel<kTF32, BN, S, kSplit, kC>;
-  constexpr size_t sm = smem_bytes<kTF32, BN, S, kSplit>();
+  auto k = tc_gemm_kernel<kTF32, BN, S, kSplit, kC, RB>;
+  constexpr size_t sm = smem_bytes<kTF32, BN, S, kSplit, RB>();
   static_assert(sm <= 232448, "stage ring exceeds the 227 KB of dynamic shared memory per CTA");
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
@@ -704,15 +728,23 @@ int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, int set, i
   return best_cols;
 }
 
+// K slice bytes of the split GRM.V: 128 for split-TF32; for split-BF16, 64 (more stages: measured
+// 8-12% faster from 256 columns up) except on tiles of at most 64 columns, which stream K and do
+// better with half as many, larger stages (measured 3-4% faster at 32-64 columns)
+constexpr int grmv_slice_bytes(bool tf32, int bn) {
+  return tf32 || bn <= 64 ? 128 : 64;
+}
+
 template <bool kTF32, int BN, int S, int C>
 static cudaError_t launch_grmv_split(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
                                      const CUtensorMap& b2, const TileCoord* tiles, int nt, int num_kb,
                                      float* Y, int64_t np, cudaStream_t s, const int32_t* colmap) {
-  return launch<kTF32, BN, S, true, C>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f, 1, s, np, colmap);
+  return launch<kTF32, BN, S, true, C, grmv_slice_bytes(kTF32, BN)>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f,
+                                                                    1, s, np, colmap);
 }
 
-// Split GRM.V over every (BN, cluster) variant.  A stage holds the same bytes for both operand
-// types (128-byte K slices: 32 tf32 or 64 bf16 elements), so the ring depths match.
+// Split GRM.V over every (BN, cluster) variant, with as many pipeline stages as the 227 KB of
+// shared memory hold at that width.
 template <bool kTF32>
 static cudaError_t grmv_split_dispatch(int BN, int C, const CUtensorMap& a, const CUtensorMap& b,
                                        const CUtensorMap& a2, const CUtensorMap& b2, const TileCoord* tiles,
@@ -729,28 +761,40 @@ static cudaError_t grmv_split_dispatch(int BN, int C, const CUtensorMap& a, cons
     return C >= 2 ? launch_grmv_split<kTF32, BNv, Sv, 2>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap)   \
                   : launch_grmv_split<kTF32, BNv, Sv, 1>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap);
   if constexpr (!kTF32) {
+    // from 80 columns: 64-byte K slices, (8 KB + BN x 64 B) x 2 halves per stage, as many stages as
+    // fit; up to 64: 128-byte slices, (16 KB + BN x 128 B) x 2
     switch (BN) {
-      SG_GRMV_CASE16(208, 2)
-      SG_GRMV_CASE16(176, 2)
-      SG_GRMV_CASE16(144, 3)
-      SG_GRMV_CASE16(112, 3)
-      SG_GRMV_CASE16(80, 4)
+      SG_GRMV_CASE(256, 4)
+      SG_GRMV_CASE(224, 5)
+      SG_GRMV_CASE16(208, 5)
+      SG_GRMV_CASE(192, 5)
+      SG_GRMV_CASE16(176, 5)
+      SG_GRMV_CASE(160, 6)
+      SG_GRMV_CASE16(144, 6)
+      SG_GRMV_CASE(128, 7)
+      SG_GRMV_CASE16(112, 7)
+      SG_GRMV_CASE(96, 8)
+      SG_GRMV_CASE16(80, 8)
+      SG_GRMV_CASE(64, 4)
       SG_GRMV_CASE16(48, 5)
+      SG_GRMV_CASE(32, 5)
       default:
-        break;
+        return cudaErrorInvalidValue;
     }
-  }
-  switch (BN) {
-    SG_GRMV_CASE(256, 2)
-    SG_GRMV_CASE(224, 2)
-    SG_GRMV_CASE(192, 2)
-    SG_GRMV_CASE(160, 3)
-    SG_GRMV_CASE(128, 3)
-    SG_GRMV_CASE(96, 4)
-    SG_GRMV_CASE(64, 4)
-    SG_GRMV_CASE(32, 5)
-    default:
-      return cudaErrorInvalidValue;
+  } else {
+    // 128-byte K slices: (16 KB + BN x 128 B) x 2 halves per stage
+    switch (BN) {
+      SG_GRMV_CASE(256, 2)
+      SG_GRMV_CASE(224, 2)
+      SG_GRMV_CASE(192, 2)
+      SG_GRMV_CASE(160, 3)
+      SG_GRMV_CASE(128, 3)
+      SG_GRMV_CASE(96, 4)
+      SG_GRMV_CASE(64, 4)
+      SG_GRMV_CASE(32, 5)
+      default:
+        return cudaErrorInvalidValue;
+    }
   }
 #undef SG_GRMV_CASE
 #undef SG_GRMV_CASE16
@@ -809,14 +853,15 @@ cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const voi
   const int C = BN % 32 != 0 && g_cluster_grmv > 2 ? 2 : g_cluster_grmv;
   const uint32_t brows = (uint32_t)(BN / C);
   const uint64_t rb = (uint64_t)np * 2;
+  const int kSlice = grmv_slice_bytes(false, BN);
   CUtensorMap a, b, a2, b2;
-  if (!make_map(&a, Kh, false, np, np, rb, kTileM) || !make_map(&b, Ph, false, np, ncols, rb, brows) ||
-      !make_map(&a2, Kl, false, np, np, rb, kTileM) || !make_map(&b2, Pl, false, np, ncols, rb, brows))
+  if (!make_map(&a, Kh, false, np, np, rb, kTileM, kSlice) || !make_map(&b, Ph, false, np, ncols, rb, brows, kSlice) ||
+      !make_map(&a2, Kl, false, np, np, rb, kTileM, kSlice) || !make_map(&b2, Pl, false, np, ncols, rb, brows, kSlice))
     return cudaErrorInvalidValue;
   static TileCache cache;
   cudaError_t e = grmv_tiles(cache, np, ncols, BN, C, s);
   if (e != cudaSuccess) return e;
-  const int num_kb = (int)(np / 64);
+  const int num_kb = (int)(np / (kSlice / 2));
   e = grmv_split_dispatch<false>(BN, C, a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np, s,
                                  colmap);
   if (e != cudaSuccess) return e;

@@ -53,9 +53,12 @@ def _pick(times, clusters):
     return best
 
 
-def tune(ctx, ncols=(64, 256, 512), tune_syrk=True, clusters=(1, 2, 4), mode=MV_TF32X3_TC):
-    """Pick the cluster sizes (the smallest one within 2% of the fastest); leaves the GRM built
-    (BF16) and engine ``mode`` selected."""
+def tune(ctx, ncols=(128, 384, 1024), tune_syrk=True, clusters=(1, 2, 4), mode=MV_TF32X3_TC):
+    """Pick the cluster sizes; leaves the GRM built (BF16) and engine ``mode`` selected.
+
+    The SYRK: the smallest cluster within 2% of the fastest.  The GRM.V: each width's times relative
+    to the fastest cluster at that width, summed over the widths (each launched as one pass), the
+    smallest cluster within 2% of the lowest sum."""
     report = {"syrk": {}, "grmv": {}}
     if tune_syrk:
         for c in clusters:
@@ -64,12 +67,13 @@ def tune(ctx, ncols=(64, 256, 512), tune_syrk=True, clusters=(1, 2, 4), mode=MV_
         ctx.set_tc_clusters(best_s, ctx.get_tc_clusters()[1])
         ctx.grm_build(GRM_BF16_TC)
     ctx.set_matvec_mode(mode)
+    ctx.engine_reserve(max(ncols), 1)  # every width in one launch
     totals = {c: 0.0 for c in clusters}
     for k in ncols:
+        times = {c: time_grmv(ctx, c, k) for c in clusters}
         for c in clusters:
-            t = time_grmv(ctx, c, k)
-            report["grmv"][(c, k)] = t
-            totals[c] += t
+            report["grmv"][(c, k)] = times[c]
+            totals[c] += times[c] / min(times.values())
     best_g = _pick(totals, clusters)
     ctx.set_tc_clusters(ctx.get_tc_clusters()[0], best_g)
     report["chosen"] = ctx.get_tc_clusters()
