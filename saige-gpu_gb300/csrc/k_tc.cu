@@ -640,14 +640,17 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
   constexpr int BN = 256;
   if (np % kTileM != 0 || mp % 64 != 0) return cudaErrorInvalidValue;
   const int C = g_cluster_syrk;
+  // 64-byte K slices (SWIZZLE_64B): 9 stages of 24 KB instead of 4 of 48 KB (4 instead of 2 for
+  // the split build), as for the split-BF16 GRM.V
+  constexpr int RB = 64;
   CUtensorMap a, b, a2, b2;
   const uint64_t rb = (uint64_t)mp * 2;
   const uint32_t brows = (uint32_t)(BN / C);  // each CTA of a cluster loads its slice of B
-  if (!make_map(&a, Zhi, false, mp, np, rb, kTileM) || !make_map(&b, Zhi, false, mp, np, rb, brows))
+  if (!make_map(&a, Zhi, false, mp, np, rb, kTileM, RB) || !make_map(&b, Zhi, false, mp, np, rb, brows, RB))
     return cudaErrorInvalidValue;
   a2 = a;
   b2 = b;
-  if (Zlo && (!make_map(&a2, Zlo, false, mp, np, rb, kTileM) || !make_map(&b2, Zlo, false, mp, np, rb, brows)))
+  if (Zlo && (!make_map(&a2, Zlo, false, mp, np, rb, kTileM, RB) || !make_map(&b2, Zlo, false, mp, np, rb, brows, RB)))
     return cudaErrorInvalidValue;
   // Lower-triangle tiles: column block bn (BN wide) starts at or before the last row of the row
   // block.  With clusters, C consecutive row blocks share each column block (the union of their
@@ -664,19 +667,19 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
   }
   cudaError_t e = upload_tiles(cache, s);
   if (e != cudaSuccess) return e;
-  const int num_kb = (int)(mp / 64);
+  const int num_kb = (int)(mp / (RB / 2));
   const int nt = (int)cache.host.size();
   if (Zlo) {
     switch (C) {
-      case 4: e = launch<false, BN, 2, true, 4>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      case 2: e = launch<false, BN, 2, true, 2>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      default: e = launch<false, BN, 2, true, 1>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 4: e = launch<false, BN, 4, true, 4, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 2: e = launch<false, BN, 4, true, 2, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      default: e = launch<false, BN, 4, true, 1, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
     }
   } else {
     switch (C) {
-      case 4: e = launch<false, BN, 4, false, 4>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      case 2: e = launch<false, BN, 4, false, 2>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      default: e = launch<false, BN, 4, false, 1>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 4: e = launch<false, BN, 9, false, 4, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 2: e = launch<false, BN, 9, false, 2, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      default: e = launch<false, BN, 9, false, 1, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
     }
   }
   if (e != cudaSuccess) return e;
@@ -728,76 +731,93 @@ int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, int set, i
   return best_cols;
 }
 
-// K slice bytes of the split GRM.V: 128 for split-TF32; for split-BF16, 64 (more stages: measured
-// 8-12% faster from 256 columns up) except on tiles of at most 64 columns, which stream K and do
-// better with half as many, larger stages (measured 3-4% faster at 32-64 columns)
-constexpr int grmv_slice_bytes(bool tf32, int bn) {
-  return tf32 || bn <= 64 ? 128 : 64;
+// K slice bytes of a split GRM.V launch over ncols columns: 128 for split-TF32; for split-BF16, 64
+// (twice the stages: measured 10% faster at 256 columns, 8-12% from there up) once the launch is
+// bound by the tensor pipe, and 128 while it streams K from HBM (at most 160 columns: half as many,
+// larger stages, measured 3% faster at 128 columns)
+static int grmv_slice_bytes(bool tf32, int64_t ncols) {
+  return tf32 || ncols <= 160 ? 128 : 64;
 }
 
-template <bool kTF32, int BN, int S, int C>
+template <bool kTF32, int BN, int S, int C, int RB>
 static cudaError_t launch_grmv_split(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
                                      const CUtensorMap& b2, const TileCoord* tiles, int nt, int num_kb,
                                      float* Y, int64_t np, cudaStream_t s, const int32_t* colmap) {
-  return launch<kTF32, BN, S, true, C, grmv_slice_bytes(kTF32, BN)>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f,
-                                                                    1, s, np, colmap);
+  return launch<kTF32, BN, S, true, C, RB>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f, 1, s, np, colmap);
 }
 
 // Split GRM.V over every (BN, cluster) variant, with as many pipeline stages as the 227 KB of
 // shared memory hold at that width.
 template <bool kTF32>
-static cudaError_t grmv_split_dispatch(int BN, int C, const CUtensorMap& a, const CUtensorMap& b,
+static cudaError_t grmv_split_dispatch(int BN, int C, int RB, const CUtensorMap& a, const CUtensorMap& b,
                                        const CUtensorMap& a2, const CUtensorMap& b2, const TileCoord* tiles,
                                        int nt, int num_kb, float* Y, int64_t np, cudaStream_t s,
                                        const int32_t* colmap = nullptr) {
-#define SG_GRMV_CASE(BNv, Sv)                                                                                 \
-  case BNv:                                                                                                   \
-    return C == 4   ? launch_grmv_split<kTF32, BNv, Sv, 4>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap) \
-           : C == 2 ? launch_grmv_split<kTF32, BNv, Sv, 2>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap) \
-                    : launch_grmv_split<kTF32, BNv, Sv, 1>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap);
+#define SG_GRMV_ARGS a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap
+#define SG_GRMV_CASE(BNv, Sv, RBv)                                                 \
+  case BNv:                                                                        \
+    return C == 4   ? launch_grmv_split<kTF32, BNv, Sv, 4, RBv>(SG_GRMV_ARGS)      \
+           : C == 2 ? launch_grmv_split<kTF32, BNv, Sv, 2, RBv>(SG_GRMV_ARGS)      \
+                    : launch_grmv_split<kTF32, BNv, Sv, 1, RBv>(SG_GRMV_ARGS);
   // odd multiples of 16 (split-BF16 only): a 4-CTA slice would not be whole 8-row swizzle atoms
-#define SG_GRMV_CASE16(BNv, Sv)                                                                               \
-  case BNv:                                                                                                   \
-    return C >= 2 ? launch_grmv_split<kTF32, BNv, Sv, 2>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap)   \
-                  : launch_grmv_split<kTF32, BNv, Sv, 1>(a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap);
+#define SG_GRMV_CASE16(BNv, Sv, RBv)                                               \
+  case BNv:                                                                        \
+    return C >= 2 ? launch_grmv_split<kTF32, BNv, Sv, 2, RBv>(SG_GRMV_ARGS)        \
+                  : launch_grmv_split<kTF32, BNv, Sv, 1, RBv>(SG_GRMV_ARGS);
   if constexpr (!kTF32) {
-    // from 80 columns: 64-byte K slices, (8 KB + BN x 64 B) x 2 halves per stage, as many stages as
-    // fit; up to 64: 128-byte slices, (16 KB + BN x 128 B) x 2
+    if (RB == 64) {
+      // (8 KB + BN x 64 B) x 2 halves per stage, as many stages as fit
+      switch (BN) {
+        SG_GRMV_CASE(256, 4, 64)
+        SG_GRMV_CASE(224, 5, 64)
+        SG_GRMV_CASE16(208, 5, 64)
+        SG_GRMV_CASE(192, 5, 64)
+        SG_GRMV_CASE16(176, 5, 64)
+        SG_GRMV_CASE(160, 6, 64)
+        SG_GRMV_CASE16(144, 6, 64)
+        SG_GRMV_CASE(128, 7, 64)
+        SG_GRMV_CASE16(112, 7, 64)
+        SG_GRMV_CASE(96, 8, 64)
+        SG_GRMV_CASE16(80, 8, 64)
+        SG_GRMV_CASE(64, 9, 64)
+        SG_GRMV_CASE16(48, 10, 64)
+        SG_GRMV_CASE(32, 11, 64)
+        default:
+          return cudaErrorInvalidValue;
+      }
+    }
+    // (16 KB + BN x 128 B) x 2 halves per stage; launches of at most 160 columns
     switch (BN) {
-      SG_GRMV_CASE(256, 4)
-      SG_GRMV_CASE(224, 5)
-      SG_GRMV_CASE16(208, 5)
-      SG_GRMV_CASE(192, 5)
-      SG_GRMV_CASE16(176, 5)
-      SG_GRMV_CASE(160, 6)
-      SG_GRMV_CASE16(144, 6)
-      SG_GRMV_CASE(128, 7)
-      SG_GRMV_CASE16(112, 7)
-      SG_GRMV_CASE(96, 8)
-      SG_GRMV_CASE16(80, 8)
-      SG_GRMV_CASE(64, 4)
-      SG_GRMV_CASE16(48, 5)
-      SG_GRMV_CASE(32, 5)
+      SG_GRMV_CASE(160, 3, 128)
+      SG_GRMV_CASE16(144, 3, 128)
+      SG_GRMV_CASE(128, 3, 128)
+      SG_GRMV_CASE16(112, 3, 128)
+      SG_GRMV_CASE(96, 4, 128)
+      SG_GRMV_CASE16(80, 4, 128)
+      SG_GRMV_CASE(64, 4, 128)
+      SG_GRMV_CASE16(48, 5, 128)
+      SG_GRMV_CASE(32, 5, 128)
       default:
         return cudaErrorInvalidValue;
     }
   } else {
-    // 128-byte K slices: (16 KB + BN x 128 B) x 2 halves per stage
+    // (16 KB + BN x 128 B) x 2 halves per stage
     switch (BN) {
-      SG_GRMV_CASE(256, 2)
-      SG_GRMV_CASE(224, 2)
-      SG_GRMV_CASE(192, 2)
-      SG_GRMV_CASE(160, 3)
-      SG_GRMV_CASE(128, 3)
-      SG_GRMV_CASE(96, 4)
-      SG_GRMV_CASE(64, 4)
-      SG_GRMV_CASE(32, 5)
+      SG_GRMV_CASE(256, 2, 128)
+      SG_GRMV_CASE(224, 2, 128)
+      SG_GRMV_CASE(192, 2, 128)
+      SG_GRMV_CASE(160, 3, 128)
+      SG_GRMV_CASE(128, 3, 128)
+      SG_GRMV_CASE(96, 4, 128)
+      SG_GRMV_CASE(64, 4, 128)
+      SG_GRMV_CASE(32, 5, 128)
       default:
         return cudaErrorInvalidValue;
     }
   }
 #undef SG_GRMV_CASE
 #undef SG_GRMV_CASE16
+#undef SG_GRMV_ARGS
 }
 
 // Row groups of C consecutive row blocks (padded past np), every column block per group.
@@ -832,7 +852,7 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
   const int num_kb = (int)(np / 32);
   const int nt = (int)cache.host.size();
   if (split) {
-    e = grmv_split_dispatch<true>(BN, C, a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s);
+    e = grmv_split_dispatch<true>(BN, C, 128, a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s);
   } else {
     switch (BN) {
       case 256: e = launch<true, 256, 3, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
@@ -853,7 +873,7 @@ cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const voi
   const int C = BN % 32 != 0 && g_cluster_grmv > 2 ? 2 : g_cluster_grmv;
   const uint32_t brows = (uint32_t)(BN / C);
   const uint64_t rb = (uint64_t)np * 2;
-  const int kSlice = grmv_slice_bytes(false, BN);
+  const int kSlice = grmv_slice_bytes(false, ncols);
   CUtensorMap a, b, a2, b2;
   if (!make_map(&a, Kh, false, np, np, rb, kTileM, kSlice) || !make_map(&b, Ph, false, np, ncols, rb, brows, kSlice) ||
       !make_map(&a2, Kl, false, np, np, rb, kTileM, kSlice) || !make_map(&b2, Pl, false, np, ncols, rb, brows, kSlice))
@@ -862,8 +882,8 @@ cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const voi
   cudaError_t e = grmv_tiles(cache, np, ncols, BN, C, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(np / (kSlice / 2));
-  e = grmv_split_dispatch<false>(BN, C, a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np, s,
-                                 colmap);
+  e = grmv_split_dispatch<false>(BN, C, kSlice, a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np,
+                                 s, colmap);
   if (e != cudaSuccess) return e;
   return check ? check_error_flag(s) : cudaSuccess;
 }
