@@ -487,6 +487,8 @@ def run_ours(args, rank, world, local):
         "per_fit": {"pcg_column_iterations": round(col_iters, 1), "columns": round(cols_per_fit, 1),
                     "converged": int(sum(1 for r in res_all if r["converged"])), "fits": len(res_all)},
         "setup_s": round(setup_s, 1),
+        # engine: the stepping thread's seconds (waits for the device included); driver: the fits'
+        # host arithmetic, summed over the driver's worker threads; the rest are engine calls within it
         "wall_breakdown_s_per_step": {k: round(v / args.steps, 3) for k, v in host_t.items()},
         "between_steps_s_per_step": {"total": round(idle_ms / 1e3 / args.steps, 3),
                                      "launch_admission": round(admit_ms / 1e3 / args.steps, 3),
