@@ -640,9 +640,11 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
   constexpr int BN = 256;
   if (np % kTileM != 0 || mp % 64 != 0) return cudaErrorInvalidValue;
   const int C = g_cluster_syrk;
-  // 64-byte K slices (SWIZZLE_64B): 9 stages of 24 KB instead of 4 of 48 KB (4 instead of 2 for
-  // the split build), as for the split-BF16 GRM.V
-  constexpr int RB = 64;
+  // 128-byte K slices, 4 stages of 48 KB (2 for the split build).  64-byte slices with twice the
+  // stages measured slower here (1.25 s against 1.06-1.09 s at N = 100k; tensor pipe 49% against
+  // 56% busy in ncu): each stage is one MMA pass shared by a 4-CTA cluster, and halving it doubles
+  // the cluster-wide barrier round trips per FLOP.
+  constexpr int RB = 128;
   CUtensorMap a, b, a2, b2;
   const uint64_t rb = (uint64_t)mp * 2;
   const uint32_t brows = (uint32_t)(BN / C);  // each CTA of a cluster loads its slice of B
@@ -671,15 +673,15 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
   const int nt = (int)cache.host.size();
   if (Zlo) {
     switch (C) {
-      case 4: e = launch<false, BN, 4, true, 4, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      case 2: e = launch<false, BN, 4, true, 2, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      default: e = launch<false, BN, 4, true, 1, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 4: e = launch<false, BN, 2, true, 4, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 2: e = launch<false, BN, 2, true, 2, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      default: e = launch<false, BN, 2, true, 1, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
     }
   } else {
     switch (C) {
-      case 4: e = launch<false, BN, 9, false, 4, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      case 2: e = launch<false, BN, 9, false, 2, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      default: e = launch<false, BN, 9, false, 1, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 4: e = launch<false, BN, 4, false, 4, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 2: e = launch<false, BN, 4, false, 2, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      default: e = launch<false, BN, 4, false, 1, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
     }
   }
   if (e != cudaSuccess) return e;
