@@ -22,6 +22,25 @@ namespace sg {
 
 constexpr int kThreads = 256;
 constexpr int kChunk = 2048;  // vector elements per block
+// The vector kernels move two consecutive elements per thread and iteration (16-byte FP64 and
+// 8-byte FP32 accesses; np is even, so every column starts 16-byte aligned), four iterations per
+// block, unrolled so that their loads are in flight together.
+constexpr int kVecIters = kChunk / (2 * kThreads);
+
+__device__ __forceinline__ double2 ld2(const double* p) { return *reinterpret_cast<const double2*>(p); }
+__device__ __forceinline__ void st2(double* p, double a, double b) {
+  *reinterpret_cast<double2*>(p) = make_double2(a, b);
+}
+__device__ __forceinline__ void st2f(float* p, float a, float b) {
+  *reinterpret_cast<float2*>(p) = make_float2(a, b);
+}
+__device__ __forceinline__ double2 ld2y(const float* Yf, const double* Yd, int64_t i) {
+  if (Yf) {
+    const float2 v = *reinterpret_cast<const float2*>(Yf + i);
+    return make_double2((double)v.x, (double)v.y);
+  }
+  return ld2(Yd + i);
+}
 
 int64_t pcg_nblk(int64_t np) { return (np + kChunk - 1) / kChunk; }
 
@@ -54,21 +73,25 @@ __global__ void pcg_init_kernel(int64_t np, const int32_t* __restrict__ cols,
   const int64_t base = c * np;
   const int64_t i0 = (int64_t)blockIdx.x * kChunk;
   double zr = 0.0, rr = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
-    const double m = mv[i];
-    const double bi = (m != 0.0) ? b[i] : 0.0;
+#pragma unroll
+  for (int it = 0; it < kVecIters; ++it) {
+    const int64_t i = i0 + 2 * (it * kThreads + threadIdx.x);
+    if (i >= np) break;
+    const double2 m = ld2(mv + i), bb = ld2(b + i);
+    const double b0 = (m.x != 0.0) ? bb.x : 0.0, b1 = (m.y != 0.0) ? bb.y : 0.0;
+    st2(X + base + i, 0.0, 0.0);
     if (s.kind == 0) {
-      const double z = m * bi;
-      X[base + i] = 0.0;
-      R[base + i] = bi;
-      Z[base + i] = z;
-      P[base + i] = z;
-      Pf[base + i] = (float)z;
-      zr += z * bi;
-      rr += bi * bi;
+      const double z0 = m.x * b0, z1 = m.y * b1;
+      st2(R + base + i, b0, b1);
+      st2(Z + base + i, z0, z1);
+      st2(P + base + i, z0, z1);
+      st2f(Pf + base + i, (float)z0, (float)z1);
+      zr += z0 * b0;
+      zr += z1 * b1;
+      rr += b0 * b0;
+      rr += b1 * b1;
     } else {
-      Pf[base + i] = (float)bi;
-      X[base + i] = 0.0;
+      st2f(Pf + base + i, (float)b0, (float)b1);
     }
   }
   zr = block_sum(zr, sh);
@@ -143,10 +166,13 @@ __global__ void pcg_sigma_dot_kernel(int64_t np, const ColState* __restrict__ st
   const int64_t base = c * np;
   const int64_t i0 = (int64_t)blockIdx.x * kChunk;
   double acc = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
-    const double p = P[base + i];
-    const double y = Yf ? (double)Yf[base + i] : Yd[base + i];
-    acc += p * ap_value(g.tau0, g.tau1, wv[i], mv[i], p, y);
+#pragma unroll
+  for (int it = 0; it < kVecIters; ++it) {
+    const int64_t i = i0 + 2 * (it * kThreads + threadIdx.x);
+    if (i >= np) break;
+    const double2 p = ld2(P + base + i), y = ld2y(Yf, Yd, base + i), w = ld2(wv + i), m = ld2(mv + i);
+    acc += p.x * ap_value(g.tau0, g.tau1, w.x, m.x, p.x, y.x);
+    acc += p.y * ap_value(g.tau0, g.tau1, w.y, m.y, p.y, y.y);
   }
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) part[(c * nblk + blockIdx.x) * 2] = acc;
@@ -204,9 +230,12 @@ __global__ void pcg_update_kernel(int64_t np, const ColState* __restrict__ st,
   }
   const double* mv = minv + (int64_t)s.pheno * np;
   if (s.kind == 1) {
-    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
-      const double y = Yf ? (double)Yf[base + i] : Yd[base + i];
-      X[base + i] = (mv[i] != 0.0) ? y : 0.0;
+#pragma unroll
+    for (int it = 0; it < kVecIters; ++it) {
+      const int64_t i = i0 + 2 * (it * kThreads + threadIdx.x);
+      if (i >= np) break;
+      const double2 y = ld2y(Yf, Yd, base + i), m = ld2(mv + i);
+      st2(X + base + i, (m.x != 0.0) ? y.x : 0.0, (m.y != 0.0) ? y.y : 0.0);
     }
     return;
   }
@@ -214,18 +243,23 @@ __global__ void pcg_update_kernel(int64_t np, const ColState* __restrict__ st,
   const double* wv = winv + (int64_t)s.pheno * np;
   const double a = s.alpha;
   double zr = 0.0, rr = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
-    const double p = P[base + i];
-    const double y = Yf ? (double)Yf[base + i] : Yd[base + i];
-    const double m = mv[i];
-    const double ap = ap_value(g.tau0, g.tau1, wv[i], m, p, y);
-    X[base + i] += a * p;
-    const double r = R[base + i] - a * ap;
-    const double z = m * r;
-    R[base + i] = r;
-    Z[base + i] = z;
-    zr += z * r;
-    rr += r * r;
+#pragma unroll
+  for (int it = 0; it < kVecIters; ++it) {
+    const int64_t i = i0 + 2 * (it * kThreads + threadIdx.x);
+    if (i >= np) break;
+    const double2 p = ld2(P + base + i), y = ld2y(Yf, Yd, base + i), m = ld2(mv + i), w = ld2(wv + i);
+    const double2 x = ld2(X + base + i), r0 = ld2(R + base + i);
+    const double ap0 = ap_value(g.tau0, g.tau1, w.x, m.x, p.x, y.x);
+    const double ap1 = ap_value(g.tau0, g.tau1, w.y, m.y, p.y, y.y);
+    st2(X + base + i, x.x + a * p.x, x.y + a * p.y);
+    const double ra = r0.x - a * ap0, rb = r0.y - a * ap1;
+    const double za = m.x * ra, zb = m.y * rb;
+    st2(R + base + i, ra, rb);
+    st2(Z + base + i, za, zb);
+    zr += za * ra;
+    zr += zb * rb;
+    rr += ra * ra;
+    rr += rb * rb;
   }
   zr = block_sum(zr, sh);
   rr = block_sum(rr, sh);
@@ -291,13 +325,22 @@ __global__ void pcg_dir_kernel(int64_t np, const ColState* __restrict__ st, cons
   const int64_t i0 = (int64_t)blockIdx.x * kChunk;
   if (s.active && s.kind == 0) {
     const double b = s.beta;
-    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
-      const double p = Z[base + i] + b * P[base + i];
-      P[base + i] = p;
-      Pf[base + i] = (float)p;
+#pragma unroll
+    for (int it = 0; it < kVecIters; ++it) {
+      const int64_t i = i0 + 2 * (it * kThreads + threadIdx.x);
+      if (i >= np) break;
+      const double2 z = ld2(Z + base + i), p = ld2(P + base + i);
+      const double pa = z.x + b * p.x, pb = z.y + b * p.y;
+      st2(P + base + i, pa, pb);
+      st2f(Pf + base + i, (float)pa, (float)pb);
     }
   } else if (s.just_done) {
-    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) Pf[base + i] = 0.0f;
+#pragma unroll
+    for (int it = 0; it < kVecIters; ++it) {
+      const int64_t i = i0 + 2 * (it * kThreads + threadIdx.x);
+      if (i >= np) break;
+      st2f(Pf + base + i, 0.0f, 0.0f);
+    }
   }
 }
 
