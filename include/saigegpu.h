@@ -44,7 +44,7 @@ enum sg_status {
 enum sg_grm_precision {
   SG_GRM_FP32_SIMT = 0, /* FP32 standardised genotypes, FP32 CUDA-core SYRK */
   SG_GRM_BF16_TC = 1,   /* BF16 genotypes, tcgen05 SYRK, FP32 accumulation in TMEM */
-  SG_GRM_BF16X3_TC = 2  /* split-BF16 (hi+lo, 3 products) tcgen05 SYRK: near-FP32 accuracy */
+  SG_GRM_BF16X3_TC = 2  /* split-BF16 (hi+lo, 4 products) tcgen05 SYRK: 16-bit genotypes, near-FP64 K */
 };
 
 /* GRM.V product engines used inside the PCG (sg_set_matvec_mode) */

@@ -3,16 +3,28 @@
 //   D[128 x BN] (+)= A[128 x K] * B[BN x K]^T,  A and B K-major in global memory
 //
 // One CTA computes one 128 x BN output tile over the whole reduction:
-//   warp 0 (one lane)  TMA producer: cp.async.bulk.tensor 2D loads of 128-byte
+//   warp 8 (one lane)  TMA producer: cp.async.bulk.tensor 2D loads of 128-byte
 //                      wide K slices (SWIZZLE_128B) into an S-stage ring,
 //                      completion tracked by mbarrier transaction counts;
-//   warp 1 (one lane)  MMA issuer: tcgen05.mma.cta_group::1 with shared-memory
-//                      descriptors, FP32 accumulator in TMEM (128 lanes x BN
-//                      columns); tcgen05.commit frees each stage and finally
-//                      signals the accumulator;
-//   warp 2             allocates / frees the TMEM columns;
-//   warps 0-3          epilogue: tcgen05.ld 32x32b (each warp its 32 TMEM
-//                      lanes = 32 output rows), scale, store to global.
+//   warp 9 (one lane)  MMA issuer: tcgen05.mma.cta_group::1 with shared-memory
+//                      descriptors into one of two FP32 accumulators in TMEM
+//                      (128 lanes x BN columns each); tcgen05.commit frees each
+//                      stage and hands over each finished accumulator;
+//                      warp 9 also allocates / frees the TMEM columns;
+//   warps 0-7          drain: tcgen05.ld 32x32b of each finished accumulator
+//                      (warp w: TMEM lanes 32 (w % 4).. = 32 output rows, every
+//                      other 32-column group), added into FP32 registers, then
+//                      scale and store to global after the last one.
+// Drained accumulation: the tensor core rounds each accumulation into TMEM
+// toward zero, so a sum over the whole reduction (tens of thousands of MMAs at
+// N = 100k) shrinks by ~1e-4 relative -- a bias that grows with the reduction
+// length.  Here an accumulator covers only 512 bytes of K per row (16 MMA K
+// steps per product) before it is added, round-to-nearest, into registers,
+// while the MMAs fill the other accumulator.  Measured at N = 100k against an
+// FP64 GEMV on the same K, the split-BF16 GRM.V's bias went from -1e-4..-3e-4
+// to -3e-7..-8e-7 relative, and a binary fit's tau from 1.1% off to 2e-5; the
+// launches are 3% (1024 columns) to 13% (384 columns) slower, the SYRK 8%.
+// (256-byte chunks: bias below 4.3e-7, launches 8-19% slower.)
 // Optional thread-block clusters share B tiles by TMA multicast (see the
 // kernel's kC parameter); MMAs stay cta_group::1.  Every mbarrier wait is bounded by
 // a global-timer budget; on expiry the kernel records an error code, skips
@@ -21,7 +33,7 @@
 // Uses:
 //   * SYRK  K = scale * Z Z^T (Z bf16, kind::f16): lower-triangle tiles only,
 //     each element (r, c <= r) written to K[r][c] and K[c][r].  The split
-//     variant accumulates Zh Zh^T + Zh Zl^T + Zl Zh^T for Z = Zh + Zl.
+//     variant accumulates all four products of Z = Zh + Zl.
 //   * GRM.V Y^T = K P^T (K fp32 read as tf32, kind::tf32), output stored
 //     RHS-major so each TMEM column is a coalesced row of Y^T; split variants
 //     with TF32 or BF16 high/low halves of K and P (three products).
@@ -43,6 +55,16 @@ constexpr int kTileM = 128;
 constexpr int kRowBytes = 128;                 // one SWIZZLE_128B atom row
 constexpr int kATileBytes = kTileM * kRowBytes;  // 16 KB
 constexpr unsigned long long kWaitBudgetNs = 4000000000ull;  // 4 s per wait
+// warp roles of the GEMM kernel: 8 drain/epilogue warps, the TMA producer, the MMA issuer
+constexpr int kDrainWarps = 8;
+constexpr int kProducerWarp = 8;
+constexpr int kMmaWarp = 9;
+constexpr int kGemmThreads = 320;
+// bytes of K per row that one TMEM accumulator takes before it is drained into registers
+#ifndef SG_DRAIN_BYTES
+#define SG_DRAIN_BYTES 512
+#endif
+constexpr int kDrainBytes = SG_DRAIN_BYTES;
 
 __device__ int g_tc_error = 0;
 
@@ -63,6 +85,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
@@ -99,6 +125,26 @@ __device__ __forceinline__ bool mbar_wait_budget(uint64_t* bar, uint32_t parity,
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int code,
                                           volatile int* abort_flag) {
   return mbar_wait_budget(bar, parity, code, abort_flag, kWaitBudgetNs);
+}
+
+// Bounded wait with a sleeping back-off between polls, for waits that last a whole chunk of MMAs:
+// the drain warps share the SM's schedulers with the single-lane TMA and MMA loops.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, int code,
+                                                volatile int* abort_flag) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  unsigned ns = 32;
+  for (;;) {
+    __nanosleep(ns);
+    if (mbar_try_wait(bar, parity)) return true;
+    if (ns < 256) ns <<= 1;
+    if (*abort_flag) return false;
+    if (gtimer() - t0 > kWaitBudgetNs) {
+      *abort_flag = 1;
+      atomicCAS(&g_tc_error, 0, code);
+      return false;
+    }
+  }
 }
 
 // Self-test of the bounded wait: waits on an mbarrier that nothing arrives at, with a short budget,
@@ -230,7 +276,7 @@ struct TileCoord {
   int32_t bm, bn;  // row block (128 rows) and column block (BN cols)
 };
 
-// kSplit: A = [Ah | Al], B = [Bh | Bl] (second maps); accumulates Ah Bh + Ah Bl + Al Bh.
+// kSplit: A = [Ah | Al], B = [Bh | Bl] (second maps); accumulates Ah Bh + Ah Bl + Al Bh (+ Al Bl with kLoLo).
 // kC > 1: the kC CTAs of a cluster own consecutive row blocks of the same column block and share
 // its B tile -- CTA r loads rows [r*BN/kC, (r+1)*BN/kC) of it and multicasts them to all kC, which
 // cuts the L2->SM operand traffic of B by kC.  Each stage is then refilled only when every CTA of
@@ -240,8 +286,8 @@ struct TileCoord {
 // kernels and the SYRK) or 64 (SWIZZLE_64B: half the bytes per stage, twice the stages in the
 // same shared memory, for the split-BF16 GRM.V, whose four operand tiles per stage left it with
 // only two stages of 128-byte slices).
-template <bool kTF32, int BN, int S, bool kSplit, int kC, int RB = 128>
-__global__ void __launch_bounds__(128, 1)
+template <bool kTF32, int BN, int S, bool kSplit, int kC, int RB = 128, bool kLoLo = false>
+__global__ void __launch_bounds__(kGemmThreads, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
                const TileCoord* __restrict__ tiles, int num_kb, float* __restrict__ D, int64_t ldd,
@@ -255,16 +301,21 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   constexpr int kStageBytes = (kATile + kBTileBytes) * (kSplit ? 2 : 1);
   constexpr uint32_t kFmt = kTF32 ? 2u : 1u;
   constexpr int kKSteps = RB / 32;     // 32 bytes of K per MMA
-  // TMEM is allocated in powers of two >= 32 columns
-  constexpr uint32_t kTmemCols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+  // two accumulators, each a power of two >= 32 columns wide
+  constexpr uint32_t kAccCols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+  constexpr uint32_t kTmemCols = 2 * kAccCols;
   constexpr uint32_t kIdesc = make_idesc(kFmt, BN);
+  constexpr int kDrainKB = kDrainBytes / RB;  // pipeline stages per accumulator
+  constexpr int kGroups = (BN + 31) / 32;     // 32-column groups of the tile
+  constexpr int kHalfGroups = (kGroups + 1) / 2;
 
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * kStageBytes);
   uint64_t* empty = full + S;
-  uint64_t* accum = empty + S;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  uint64_t* acc_full = empty + S;     // [2] the MMAs of an accumulator's chunk completed
+  uint64_t* acc_empty = acc_full + 2;  // [2] the drain warps read the accumulator
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
@@ -278,12 +329,15 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kC);
     }
-    mbar_init(accum, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], kDrainWarps);
+    }
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  if (warp == 2) {
+  if (warp == kMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                  ::"r"(smem_u32(tmem_slot)), "r"(kTmemCols) : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
@@ -293,107 +347,149 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   if constexpr (kC > 1) cluster_sync();  // every CTA's barriers exist before any peer multicasts
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem_base = *tmem_slot;
+  const int nchunks = (num_kb + kDrainKB - 1) / kDrainKB;
 
-  if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer
-    const int32_t ya = tc.bm * kTileM, yb = tc.bn * BN;
-    for (int kb = 0; kb < num_kb; ++kb) {
-      const int s = kb % S;
-      const uint32_t ph = (uint32_t)(kb / S) & 1u;
-      if (!mbar_wait(&empty[s], ph ^ 1u, 1, abort_flag)) break;
-      uint8_t* st = smem + s * kStageBytes;
-      mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
-      const int32_t x = kb * (RB / (kTF32 ? 4 : 2));
-      tma_load_2d(st, &mapA, &full[s], x, ya);
-      if constexpr (kC == 1) {
-        tma_load_2d(st + kATile, &mapB, &full[s], x, yb);
-      } else {
-        tma_load_2d_mcast(st + kATile + crank * kSliceBytes, &mapB, &full[s], x,
-                          yb + (int32_t)crank * kSliceRows, kMask);
-      }
-      if constexpr (kSplit) {
-        tma_load_2d(st + kATile + kBTileBytes, &mapA2, &full[s], x, ya);
+  if (warp == kProducerWarp) {
+    if (lane == 0) {
+      // ---------------- TMA producer
+      const int32_t ya = tc.bm * kTileM, yb = tc.bn * BN;
+      for (int kb = 0; kb < num_kb; ++kb) {
+        const int s = kb % S;
+        const uint32_t ph = (uint32_t)(kb / S) & 1u;
+        if (!mbar_wait(&empty[s], ph ^ 1u, 1, abort_flag)) break;
+        uint8_t* st = smem + s * kStageBytes;
+        mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
+        const int32_t x = kb * (RB / (kTF32 ? 4 : 2));
+        tma_load_2d(st, &mapA, &full[s], x, ya);
         if constexpr (kC == 1) {
-          tma_load_2d(st + 2 * kATile + kBTileBytes, &mapB2, &full[s], x, yb);
+          tma_load_2d(st + kATile, &mapB, &full[s], x, yb);
         } else {
-          tma_load_2d_mcast(st + 2 * kATile + kBTileBytes + crank * kSliceBytes, &mapB2, &full[s], x,
+          tma_load_2d_mcast(st + kATile + crank * kSliceBytes, &mapB, &full[s], x,
                             yb + (int32_t)crank * kSliceRows, kMask);
         }
-      }
-    }
-  } else if (warp == 1 && lane == 0) {
-    // ---------------- MMA issuer
-    for (int kb = 0; kb < num_kb; ++kb) {
-      const int s = kb % S;
-      const uint32_t ph = (uint32_t)(kb / S) & 1u;
-      if (!mbar_wait(&full[s], ph, 2, abort_flag)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a0 = smem_u32(smem + s * kStageBytes);
-      const uint32_t b0 = a0 + kATile;
-#pragma unroll
-      for (int k = 0; k < kKSteps; ++k) {
-        const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
-        umma<kTF32>(tmem_base, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, acc);
         if constexpr (kSplit) {
-          const uint32_t a1 = b0 + kBTileBytes;      // Al
-          const uint32_t b1 = a1 + kATile;           // Bl
-          umma<kTF32>(tmem_base, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
-          umma<kTF32>(tmem_base, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, 1u);
+          tma_load_2d(st + kATile + kBTileBytes, &mapA2, &full[s], x, ya);
+          if constexpr (kC == 1) {
+            tma_load_2d(st + 2 * kATile + kBTileBytes, &mapB2, &full[s], x, yb);
+          } else {
+            tma_load_2d_mcast(st + 2 * kATile + kBTileBytes + crank * kSliceBytes, &mapB2, &full[s], x,
+                              yb + (int32_t)crank * kSliceRows, kMask);
+          }
         }
       }
-      // stage reusable once these MMAs have read it (in every CTA of the cluster)
-      if constexpr (kC == 1) umma_commit(&empty[s]);
-      else umma_commit_mcast(&empty[s], kMask);
     }
-    umma_commit(accum);
-  }
-  __syncwarp();
-
-  // ---------------- epilogue: all four warps
-  int go = mbar_wait(accum, 0u, 3, abort_flag) && !*abort_flag;
-  __syncwarp();
-  go = __shfl_sync(0xffffffffu, go, 0);  // warp-uniform: tcgen05.ld is .sync.aligned
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (go && (int64_t)tc.bm * kTileM < nrows) {
-    const int64_t r = (int64_t)tc.bm * kTileM + warp * 32 + lane;
-    const uint32_t trow = tmem_base + ((uint32_t)(warp * 32) << 16);
-#pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-      uint32_t v[32];
-      tmem_ld32(trow + (uint32_t)c0, v);  // within the allocation (kTmemCols >= BN rounded up to 32)
-      const int64_t cbase = (int64_t)tc.bn * BN + c0;
-      const int lim = BN - c0 < 32 ? BN - c0 : 32;  // a tile width of 16 (mod 32) ends on half a chunk
-      if (mode == 1) {
-        if (colmap) {  // column j of the tile goes to row colmap[j] of D (skipped when negative)
+  } else if (warp == kMmaWarp) {
+    if (lane == 0) {
+      // ---------------- MMA issuer: chunk ch of kDrainKB stages goes to accumulator ch % 2, which is
+      // reused once the drain warps have read it (two chunks earlier)
+      for (int kb = 0; kb < num_kb; ++kb) {
+        const int ch = kb / kDrainKB;
+        const int kin = kb - ch * kDrainKB;
+        const int ab = ch & 1;
+        if (kin == 0) {
+          if (!mbar_wait(&acc_empty[ab], ((uint32_t)(ch >> 1) & 1u) ^ 1u, 5, abort_flag)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
+        const int s = kb % S;
+        const uint32_t ph = (uint32_t)(kb / S) & 1u;
+        if (!mbar_wait(&full[s], ph, 2, abort_flag)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dacc = tmem_base + (uint32_t)ab * kAccCols;
+        const uint32_t a0 = smem_u32(smem + s * kStageBytes);
+        const uint32_t b0 = a0 + kATile;
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            if (j >= lim) break;
-            const int32_t dc = __ldg(colmap + cbase + j);
-            if (dc >= 0) D[(int64_t)dc * ldd + r] = __uint_as_float(v[j]) * scale;
+        for (int k = 0; k < kKSteps; ++k) {
+          const uint32_t acc = (kin > 0 || k > 0) ? 1u : 0u;
+          umma<kTF32>(dacc, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, acc);
+          if constexpr (kSplit) {
+            const uint32_t a1 = b0 + kBTileBytes;      // Al
+            const uint32_t b1 = a1 + kATile;           // Bl
+            umma<kTF32>(dacc, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
+            umma<kTF32>(dacc, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, 1u);
+            if constexpr (kLoLo)
+              umma<kTF32>(dacc, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
+          }
+        }
+        // stage reusable once these MMAs have read it (in every CTA of the cluster)
+        if constexpr (kC == 1) umma_commit(&empty[s]);
+        else umma_commit_mcast(&empty[s], kMask);
+        if (kin == kDrainKB - 1 || kb == num_kb - 1) umma_commit(&acc_full[ab]);
+      }
+    }
+  } else {
+    // ---------------- drain warps 0-7, then the epilogue
+    const int quad = warp & 3, half = warp >> 2;
+    const uint32_t tlane = (uint32_t)(quad * 32) << 16;
+    float sum[kHalfGroups][32];
+#pragma unroll
+    for (int g = 0; g < kHalfGroups; ++g)
+#pragma unroll
+      for (int j = 0; j < 32; ++j) sum[g][j] = 0.0f;
+    int go = 1;
+    for (int ch = 0; ch < nchunks; ++ch) {
+      const int ab = ch & 1;
+      // one lane polls; the others wait in the shuffle (warp-uniform: tcgen05.ld is .sync.aligned)
+      if (lane == 0) go = mbar_wait_sleep(&acc_full[ab], (uint32_t)(ch >> 1) & 1u, 3, abort_flag) && !*abort_flag;
+      go = __shfl_sync(0xffffffffu, go, 0);
+      __syncwarp();
+      if (!go) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t taddr = tmem_base + tlane + (uint32_t)ab * kAccCols;
+#pragma unroll
+      for (int g = 0; g < kHalfGroups; ++g) {
+        const int grp = 2 * g + half;
+        if (grp < kGroups) {  // within the allocation: kAccCols >= BN rounded up to 32
+          uint32_t v[32];
+          tmem_ld32(taddr + (uint32_t)(grp * 32), v);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) sum[g][j] += __uint_as_float(v[j]);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[ab]);
+    }
+    if (go && (int64_t)tc.bm * kTileM < nrows) {
+      const int64_t r = (int64_t)tc.bm * kTileM + quad * 32 + lane;
+#pragma unroll
+      for (int g = 0; g < kHalfGroups; ++g) {
+        const int grp = 2 * g + half;
+        if (grp >= kGroups) continue;
+        const int64_t cbase = (int64_t)tc.bn * BN + grp * 32;
+        const int lim = BN - grp * 32 < 32 ? BN - grp * 32 : 32;  // a width of 16 (mod 32) ends on half a group
+        if (mode == 1) {
+          if (colmap) {  // column j of the tile goes to row colmap[j] of D (skipped when negative)
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              if (j >= lim) break;
+              const int32_t dc = __ldg(colmap + cbase + j);
+              if (dc >= 0) D[(int64_t)dc * ldd + r] = sum[g][j] * scale;
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (j < lim) D[(cbase + j) * ldd + r] = sum[g][j] * scale;
           }
         } else {
 #pragma unroll
-          for (int j = 0; j < 32; ++j)
-            if (j < lim) D[(cbase + j) * ldd + r] = __uint_as_float(v[j]) * scale;
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int64_t c = cbase + j;
-          if (c <= r) {
-            const float f = __uint_as_float(v[j]) * scale;
-            D[r * ldd + c] = f;
-            D[c * ldd + r] = f;
+          for (int j = 0; j < 32; ++j) {
+            const int64_t c = cbase + j;
+            if (c <= r) {
+              const float f = sum[g][j] * scale;
+              D[r * ldd + c] = f;
+              D[c * ldd + r] = f;
+            }
           }
         }
       }
     }
   }
+  __syncwarp();  // the producer and MMA warps reconverge after their single-lane loops
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   // no CTA leaves while a peer may still multicast into its shared memory or arrive on its barriers
   if constexpr (kC > 1) cluster_sync();
-  if (warp == 2) {
+  if (warp == kMmaWarp) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kTmemCols)
                  : "memory");
   }
@@ -436,12 +532,12 @@ constexpr size_t smem_bytes() {
   return (size_t)S * (kTileM * RB + BN * RB) * (kSplit ? 2 : 1) + 1024 + 256;
 }
 
-template <bool kTF32, int BN, int S, bool kSplit, int kC = 1, int RB = kRowBytes>
+template <bool kTF32, int BN, int S, bool kSplit, int kC = 1, int RB = kRowBytes, bool kLoLo = false>
 cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
                    const CUtensorMap& b2, const TileCoord* tiles, int ntiles, int num_kb, float* D,
                    int64_t ldd, float scale, int mode, cudaStream_t s, int64_t nrows,
                    const int32_t* colmap = nullptr) {
-  auto k = tc_gemm_kernel<kTF32, BN, S, kSplit, kC, RB>;
+  auto k = tc_gemm_kernel<kTF32, BN, S, kSplit, kC, RB, kLoLo>;
   constexpr size_t sm = smem_bytes<kTF32, BN, S, kSplit, RB>();
   static_assert(sm <= 232448, "stage ring exceeds the 227 KB of dynamic shared memory per CTA");
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -449,7 +545,7 @@ cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap
   if (ntiles % kC != 0) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)ntiles);
-  cfg.blockDim = dim3(128);
+  cfg.blockDim = dim3(kGemmThreads);
   cfg.dynamicSmemBytes = sm;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -672,10 +768,13 @@ cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t m
   const int num_kb = (int)(mp / (RB / 2));
   const int nt = (int)cache.host.size();
   if (Zlo) {
+    // all four products: the residuals Zl of a marker take only three values (one per genotype),
+    // so the Zl Zl' term does not average out over markers (dropping it left the off-diagonal
+    // entries ~7e-7 off at M = 150k, against ~2e-9 with it)
     switch (C) {
-      case 4: e = launch<false, BN, 2, true, 4, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      case 2: e = launch<false, BN, 2, true, 2, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      default: e = launch<false, BN, 2, true, 1, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 4: e = launch<false, BN, 2, true, 4, RB, true>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      case 2: e = launch<false, BN, 2, true, 2, RB, true>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
+      default: e = launch<false, BN, 2, true, 1, RB, true>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
     }
   } else {
     switch (C) {
