@@ -118,3 +118,58 @@ def test_grmv_bf16x3_switching_modes_keeps_k_exact(cohort):
         assert np.array_equal(ctx.grm_matmul(V), Y_a)
     finally:
         ctx.set_matvec_mode(MV_FP32_SIMT)
+
+
+# ---------------------------------------------------------------- accumulation bias
+# The tensor core rounds each accumulation into TMEM toward zero.  Summed over a whole reduction
+# that shrank every product: at N = 20k, M = 30k the split GRM.V products by 2e-5 to 6e-5 relative
+# (split TF32 twice that) and the BF16 SYRK's diagonal by ~2e-4, growing linearly with the reduction.
+# The kernels drain their accumulators into FP32 registers every 512 bytes of K, which leaves a
+# few 1e-7 here (measured: profiles/precision_n100k_m150k.md for the full-size case).
+
+@pytest.fixture(scope="module")
+def cohort20k(gpu_ctx):
+    n, m = 20000, 30000
+    ptr, ln = gpu_ctx.synth_bed(1003, n, m, 0.02)
+    gpu_ctx.setgeno_device(ptr, ln, n, m)
+    return gpu_ctx
+
+
+@pytest.mark.parametrize("mode", ["bf16x3", "tf32x3"])
+def test_grmv_products_carry_no_accumulation_bias(cohort20k, mode):
+    from saigegpu import MV_BF16X3_TC, MV_FP64_PLAIN, MV_TF32X3_TC
+    ctx = cohort20k
+    ctx.grm_build(GRM_BF16_TC)
+    n = ctx.n
+    rng = np.random.default_rng(3)
+    V = np.column_stack([rng.choice([-1.0, 1.0], size=(n, 4)), rng.standard_normal((n, 4)), np.ones(n),
+                         rng.uniform(0, 1, n)])
+    try:
+        ctx.set_matvec_mode(MV_FP64_PLAIN)
+        Y64 = ctx.grm_matmul(V)
+        ctx.set_matvec_mode(MV_BF16X3_TC if mode == "bf16x3" else MV_TF32X3_TC)
+        Y = ctx.grm_matmul(V)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+    bias = ((Y - Y64) * Y64).sum(axis=0) / (Y64 * Y64).sum(axis=0)  # error along each product
+    assert np.abs(bias).max() < 2e-6, bias
+    rel = np.linalg.norm(Y - Y64, axis=0) / np.linalg.norm(Y64, axis=0)
+    assert rel.max() < 5e-5, rel
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_syrk_diagonal_carries_no_accumulation_bias(cohort20k, split):
+    ctx = cohort20k
+    ctx.grm_build(GRM_BF16X3_TC if split else GRM_BF16_TC)
+    S = np.arange(0, ctx.n, 79)[:256]
+    E = np.zeros((ctx.n, len(S)))
+    E[S, np.arange(len(S))] = 1.0
+    ctx.set_matvec_mode(MV_FP32_SIMT)
+    Kss = ctx.grm_matmul(E)[S, np.arange(len(S))]  # K[s, s], read exactly through unit vectors
+    ref = ctx.grm_diag()[S] / ctx.dims()["m_qc"]  # exact sum of z^2 over the GRM markers
+    rel = Kss / ref - 1.0
+    # BF16 operands round to nearest, once per marker and genotype: every sample sees the same
+    # roundings, so their mean error does not average out over samples (~1e-5 at M = 30k); without
+    # the drains the mean was ~2e-4 low
+    assert abs(rel.mean()) < (5e-5 if not split else 5e-6), rel.mean()
+    assert np.abs(rel).max() < (4e-4 if not split else 2e-5), np.abs(rel).max()
