@@ -60,7 +60,8 @@ constexpr int kDrainWarps = 8;
 constexpr int kProducerWarp = 8;
 constexpr int kMmaWarp = 9;
 constexpr int kGemmThreads = 320;
-// bytes of K per row that one TMEM accumulator takes before it is drained into registers
+// bytes of K per row that one TMEM accumulator takes before it is drained into registers (a
+// multiple of 128; the bias left by the toward-zero TMEM rounding grows linearly with it)
 #ifndef SG_DRAIN_BYTES
 #define SG_DRAIN_BYTES 512
 #endif
@@ -305,9 +306,13 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   constexpr uint32_t kAccCols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
   constexpr uint32_t kTmemCols = 2 * kAccCols;
   constexpr uint32_t kIdesc = make_idesc(kFmt, BN);
+  static_assert(kDrainBytes % RB == 0 && kDrainBytes >= RB, "an accumulator covers whole pipeline stages");
   constexpr int kDrainKB = kDrainBytes / RB;  // pipeline stages per accumulator
   constexpr int kGroups = (BN + 31) / 32;     // 32-column groups of the tile
   constexpr int kHalfGroups = (kGroups + 1) / 2;
+  static_assert(kDrainWarps == 8 && kGemmThreads == 32 * (kDrainWarps + 2),
+                "two drain warps per TMEM lane quadrant, then the producer and MMA warps");
+  static_assert(kTmemCols <= 512, "two accumulators of at most 256 columns");
 
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
