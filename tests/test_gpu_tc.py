@@ -125,7 +125,7 @@ def test_grmv_bf16x3_switching_modes_keeps_k_exact(cohort):
 # that shrank every product: at N = 20k, M = 30k the split GRM.V products by 2e-5 to 6e-5 relative
 # (split TF32 twice that) and the BF16 SYRK's diagonal by ~2e-4, growing linearly with the reduction.
 # The kernels drain their accumulators into FP32 registers every 512 bytes of K, which leaves a
-# few 1e-7 here (measured: profiles/precision_n100k_m150k.md for the full-size case).
+# few 1e-7 here (test_gpu_precision_fullsize.py holds the full-size case to FP64).
 
 @pytest.fixture(scope="module")
 def cohort20k(gpu_ctx):
