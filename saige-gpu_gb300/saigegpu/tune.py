@@ -54,7 +54,9 @@ def _pick(times, clusters):
 
 
 def tune(ctx, ncols=(128, 384, 1024), tune_syrk=True, clusters=(1, 2, 4), mode=MV_TF32X3_TC):
-    """Pick the cluster sizes; leaves the GRM built (BF16) and engine ``mode`` selected.
+    """Pick the cluster sizes; leaves the GRM built from 8-bit (BF16) genotypes and engine ``mode``
+    selected.  For fits, rebuild it with GRM_BF16X3_TC (16-bit genotypes): at N = 100k the 8-bit
+    GRM moved binary variance components by up to 1.1e-3 against FP64.
 
     The SYRK: the smallest cluster within 2% of the fastest.  The GRM.V: each width's times relative
     to the fastest cluster at that width, summed over the widths (each launched as one pass), the
