@@ -27,6 +27,13 @@ def test_syrk_bf16_tc(cohort):
     assert np.abs(np.diag(K) - np.diag(grm.K)).max() < 2e-3
 
 
+def _bf16(x):
+    """float32 -> bfloat16 (round to nearest, ties to even), returned as float32."""
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
 def test_syrk_split_bf16_tc(cohort):
     ctx, grm = cohort
     ctx.grm_build(GRM_BF16X3_TC)
@@ -34,6 +41,20 @@ def test_syrk_split_bf16_tc(cohort):
     assert np.array_equal(K, K.T)
     err = np.abs(K - grm.K).max() / np.abs(grm.K).max()
     assert err < 2e-5, err
+    # all four products of Z = Zh + Zl: a marker's Zl takes one value per genotype, so dropping
+    # Zl Zl' would shift every off-diagonal entry the same way (~8e-7 RMS here); the kernel's sum
+    # must sit on the four-product one, up to its FP32 accumulation (~2e-9)
+    bed, _ = synth.synth_bed(31, grm.n, 1900, 0.01)
+    g = plink.setgeno(bed, grm.n, 1900, np.arange(1, grm.n + 1), np.ones(grm.n, bool), 0.01, 0.15)
+    Z = plink.std_geno(g)
+    Zh = _bf16(Z)
+    Zl = _bf16(Z - Zh).astype(np.float64)
+    Zh = Zh.astype(np.float64)
+    K4 = (Zh + Zl).T @ (Zh + Zl) / Z.shape[0]
+    lolo = Zl.T @ Zl / Z.shape[0]
+    off = ~np.eye(grm.n, dtype=bool)
+    rms = lambda a: float(np.sqrt(np.mean(a[off] ** 2)))  # noqa: E731
+    assert rms(K - K4) < 0.1 * rms(lolo), (rms(K - K4), rms(lolo))
 
 
 def test_grm_matvec_tf32_tc(cohort):
