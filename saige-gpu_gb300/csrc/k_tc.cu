@@ -18,9 +18,10 @@
 // Drained accumulation: accumulating into TMEM loses magnitude -- measured, a
 // sum over the whole reduction (tens of thousands of MMAs at N = 100k) came out
 // 1e-4 to 3e-4 smaller than the FP64 value, a bias that grows linearly with the
-// reduction length, as rounding each accumulation toward zero would give.  Here an accumulator covers only 512 bytes of K per row (16 MMA K
-// steps per product) before it is added, round-to-nearest, into registers,
-// while the MMAs fill the other accumulator.  Measured at N = 100k against an
+// reduction length, as rounding each accumulation toward zero would give.
+// Here an accumulator covers only 512 bytes of K per row (16 MMA K steps per
+// product) before it is added, round-to-nearest, into registers, while the
+// MMAs fill the other accumulator.  Measured at N = 100k against an
 // FP64 GEMV on the same K, the split-BF16 GRM.V's bias went from -1e-4..-3e-4
 // to -3e-7..-8e-7 relative, and a binary fit's tau from 1.1% off to 3e-5; the
 // launches are 3% (1024 columns) to 13% (384 columns) slower, the SYRK 8%.
