@@ -47,7 +47,10 @@ for _p in (ROOT, os.path.join(ROOT, "saige-gpu_gb300")):
 import numpy as np  # noqa: E402
 
 METRIC = "null-model fits/hr at N=100k (batched mixed-prec vs plain FP64 PCG); p50/p99"
-COUNTS_FILE = os.path.join(ROOT, "profiles", "bench_counts.json")
+# PCG column-iterations per fit of this workload (N = 100k, M = 150k, 64 phenotypes), measured by the
+# GPU arm (its line reports the value of each run under per_fit); the reference arm extrapolates its
+# per-product CPU time with this fixed count
+PCG_COLUMN_ITERATIONS_PER_FIT = 513.9
 
 
 def parse():
@@ -61,11 +64,15 @@ def parse():
     ap.add_argument("--phenos", type=int, default=64)
     ap.add_argument("--miss", type=float, default=0.02)
     ap.add_argument("--seed", type=int, default=1003)
-    ap.add_argument("--mode", default="bf16x3", choices=["bf16x3", "tf32x3", "tf32", "fp32"])
+    ap.add_argument("--mode", default="subset", choices=["subset", "bf16x3", "tf32x3", "tf32", "fp32"],
+                    help="GRM.V engine: subset = each phenotype's GRM from its own samples (the reference's "
+                         "setgeno per phenotype; genotype GEMMs), the others restrict the cohort GRM to the "
+                         "phenotype's samples (an approximation for masked phenotypes)")
     ap.add_argument("--grm", default="bf16x3", choices=["bf16x3", "bf16"],
-                    help="GRM build: split-BF16 standardised genotypes (four products) or BF16 (one)")
+                    help="GRM build of the cohort-GRM engines: split-BF16 standardised genotypes (four "
+                         "products) or BF16 (one)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-tune", action="store_true", help="skip the cluster-shape autotuner")
+    ap.add_argument("--no-tune", action="store_true", help="skip the tcgen05 shape autotuner")
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="skip timing the reference's two-SGEMV K.x algorithm on this GPU")
     ap.add_argument("--driver", default="native", choices=["native", "python"],
@@ -203,12 +210,58 @@ def run_batch(ctx, specs, cols, pipelined=True, workers=None, driver="native", l
     return res, jobs, wall
 
 
-def grm_roofline(ctx, peaks, t_dev, n, np_, mode="tf32x3", traffic=None):
-    """Roofline of the dominant kernel (GRM.V) from the engine's own CUDA-event timing.
+# DRAM traffic of the split-BF16 GRM.V over its algorithmic bytes, from ncu on a smaller case
+# (dram__bytes_read.sum + dram__bytes_write.sum; profiles/grmv_bf16x3_n24576_and_n100k.md)
+GRMV_TRAFFIC_RATIO = 1.023
+GRMV_TRAFFIC_BASIS = ("ncu DRAM bytes of two N=24576 launches (224 and 512 columns) over their algorithmic bytes "
+                      "(1.008, 1.037; mean 1.023), times this launch's algorithmic bytes "
+                      "(profiles/grmv_bf16x3_n24576_and_n100k.md)")
 
-    Algorithmic bytes per launch: the two halves of K (8 B per entry for TF32 halves, 4 B for BF16
-    halves) + the split P halves read and Y written (FP32); tensor FLOPs: three products of
-    2 N^2 per column.  The tensor peak is the measured BF16 rate (TF32 runs at half of it)."""
+
+def subset_roofline(peaks, t_dev, np_, mg):
+    """Roofline of the subset-exact engine's GRM.V (two genotype GEMMs and the small kernels around
+    them, timed together by the engine's CUDA events).  Algorithmic work per launch over C columns:
+    bytes = the genotype matrix read by both GEMMs (2 B per sample and marker each) + the centred
+    vector halves and T' halves read (4 B each per entry) + T and U written (4 B); FLOPs = two
+    GEMMs of 2 N_p M_g per column (one product each, as the reference's two SGEMVs per K.x,
+    gpuSymMatMult.cu:211-252).  ``executed``: two BF16 products per GEMM."""
+    launches = max(1, t_dev["gemm_launches"])
+    ms = t_dev["gemm_ms"] / launches
+    cols = t_dev["gemm_cols"] / launches
+    bytes_alg = 2.0 * 2.0 * np_ * mg + 8.0 * (np_ + mg) * cols
+    flops_alg = 2.0 * 2.0 * np_ * mg * cols
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tc_peak = peaks.get("bf16_tflops_sustained", 1700.0)
+    t = ms * 1e-3
+    a_bw = bytes_alg / t / 1e9
+    a_tc = flops_alg / t / 1e12
+    common = {"traffic": None, "kernel": "tc_gemm_kernel<bf16, kSplitB> x 2 (G'V, G T') + subset kernels",
+              "per_launch_ms": round(ms, 3), "columns_per_launch": round(cols, 1),
+              "algorithmic_bytes_per_launch": bytes_alg, "algorithmic_flops_per_launch": flops_alg,
+              "algorithmic_basis": "bytes: G read by both GEMMs + vector halves read + T and U written; "
+                                   "FLOPs: 2 GEMMs x 2 N_p M_g per column",
+              "executed": {"products": 2.0, "tensor_flops_per_launch": 2.0 * flops_alg,
+                           "tflops": round(2.0 * a_tc, 1), "peak": tc_peak,
+                           "frac": round(2.0 * a_tc / tc_peak, 4),
+                           "peak_source": "measured bf16_tflops_sustained (MEASURED_PEAKS.json)"}}
+    if a_bw / hbm >= a_tc / tc_peak:
+        return dict({"bound": "hbm", "achieved": round(a_bw, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(a_bw / hbm, 4), "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)"},
+                    **common)
+    return dict({"bound": "tensor", "achieved": round(a_tc, 1), "peak": tc_peak, "unit": "TFLOP/s",
+                 "frac": round(a_tc / tc_peak, 4),
+                 "peak_source": "measured bf16_tflops_sustained (MEASURED_PEAKS.json)"}, **common)
+
+
+def grm_roofline(ctx, peaks, t_dev, n, np_, mode="bf16x3", traffic=None):
+    """Roofline of the dominant kernel (the GRM.V) from the engine's own CUDA-event timing.
+
+    Algorithmic work per launch, whatever the precision form executes: bytes = the stored K (4 B
+    per entry for the two BF16 halves, 8 B for TF32 halves, 4 B for one FP32 K) + the P halves
+    read and Y written per column; FLOPs = 2 N_p^2 per column (one product).  The binding roof is
+    the one on which this work takes longer; frac = achieved / peak on it.  The tensor peak is the
+    measured sustained BF16 rate (the kernel runs inside seconds-long steps; TF32 at half of it).
+    ``executed`` adds the tensor work the kernel issues (three products for the split forms)."""
     launches = max(1, t_dev["gemm_launches"])
     ms = t_dev["gemm_ms"] / launches
     cols = t_dev["gemm_cols"] / launches
@@ -217,27 +270,34 @@ def grm_roofline(ctx, peaks, t_dev, n, np_, mode="tf32x3", traffic=None):
     kb = 4.0 if bf16 else (8.0 if split else 4.0)
     pb = 4.0 if bf16 else (8.0 if split else 4.0)
     bytes_alg = kb * np_ * np_ + (pb + 4.0) * np_ * cols
-    flops_tensor = (3.0 if split else 1.0) * 2.0 * np_ * np_ * cols
+    flops_alg = 2.0 * np_ * np_ * cols
+    products = 3.0 if split else 1.0
     hbm = peaks.get("hbm_gbs", 6800.0)
-    tc_peak = peaks.get("bf16_tflops", 1900.0) / (1.0 if bf16 else 2.0)
+    tc_peak = peaks.get("bf16_tflops_sustained", 1700.0) / (1.0 if bf16 else 2.0)
     kname = "tc_gemm_kernel<%s,split>" % ("bf16" if bf16 else "tf32")
-    a_bw = bytes_alg / (ms * 1e-3) / 1e9
-    a_tc = flops_tensor / (ms * 1e-3) / 1e12
+    t = ms * 1e-3
+    a_bw = bytes_alg / t / 1e9
+    a_tc = flops_alg / t / 1e12
     common = {"traffic": None if traffic is None else round(traffic * bytes_alg),
-              "traffic_basis": None if traffic is None else
-              "ncu DRAM bytes of a N=24576 launch / its algorithmic bytes (%.3f), times this launch's "
-              "algorithmic bytes (profiles/grmv_traffic.json)" % traffic,
+              "traffic_basis": None if traffic is None else GRMV_TRAFFIC_BASIS,
               "kernel": kname, "per_launch_ms": round(ms, 3),
               "columns_per_launch": round(cols, 1), "algorithmic_bytes_per_launch": bytes_alg,
-              "tensor_flops_per_launch": flops_tensor}
+              "algorithmic_flops_per_launch": flops_alg,
+              "algorithmic_basis": "bytes: stored K + P read + Y written; FLOPs: 2 N_p^2 per column",
+              "executed": {"products": products, "tensor_flops_per_launch": products * flops_alg,
+                           "tflops": round(products * a_tc, 1), "peak": tc_peak,
+                           "frac": round(products * a_tc / tc_peak, 4),
+                           "peak_source": "measured bf16_tflops_sustained (MEASURED_PEAKS.json)"
+                                          + ("" if bf16 else ", TF32 at half of it")}}
     if a_bw / hbm >= a_tc / tc_peak:
         return dict({"bound": "hbm", "achieved": round(a_bw, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(a_bw / hbm, 4),
                      "peak_source": "measured hbm_gbs (MEASURED_PEAKS.json)"}, **common)
     return dict({"bound": "tensor", "achieved": round(a_tc, 1), "peak": tc_peak, "unit": "TFLOP/s",
                  "frac": round(a_tc / tc_peak, 4),
-                 "peak_source": ("measured bf16_tflops (MEASURED_PEAKS.json)" if bf16 else
-                                 "TF32 = half the measured bf16_tflops (MEASURED_PEAKS.json)")}, **common)
+                 "peak_source": ("measured bf16_tflops_sustained (MEASURED_PEAKS.json)" if bf16 else
+                                 "TF32 = half the measured bf16_tflops_sustained (MEASURED_PEAKS.json)")},
+                **common)
 
 
 def step_width_summary(trace):
@@ -381,7 +441,8 @@ def reference_gpu_matvec(n, m_qc, iters_per_fit, reps=5):
 def run_ours(args, rank, world, local):
     import torch
     from saigegpu import (Context, GRM_BF16_TC, GRM_BF16X3_TC, MV_BF16X3_TC, MV_TF32X3_TC, MV_TF32_TC,
-                          MV_FP32_SIMT)
+                          MV_FP32_SIMT, MV_SUBSET_EXACT)
+    exact = args.mode == "subset"
     peaks = load_peaks()
     ctx = Context(local)
     t_setup = time.perf_counter()
@@ -392,29 +453,32 @@ def run_ours(args, rank, world, local):
     tune_report = None
     d = ctx.dims()
     syrk_flops = float(d["n"]) * (d["n"] + 1) * d["m_qc"]
-    bt1 = None
-    if not args.no_tune and args.mode in ("tf32x3", "bf16x3"):
-        # cluster shapes; leaves the single-product BF16 GRM built, whose SYRK is the roofline line
+    syrk1_ms = None  # the single-product BF16 SYRK (the tuner's chosen shape)
+    if not args.no_tune and args.mode in ("subset", "bf16x3"):
+        # SYRK shape (and for the cohort-GRM engine the per-width GRM.V plan) from measured times;
+        # leaves the single-product BF16 GRM built
         from saigegpu import tune
-        tune_report = tune.tune(ctx, ncols=(128, 384, 1024),
-                                mode=MV_BF16X3_TC if args.mode == "bf16x3" else MV_TF32X3_TC)
-        bt1 = ctx.build_timing()
-    # the GRM the fits use: split-BF16 standardised genotypes (16 significant bits, four products)
-    # by default, so that tau lands within 1e-4 of FP64 arithmetic
+        tune_report = tune.tune(ctx, mode=MV_BF16X3_TC, grmv=not exact)
+        syrk1_ms = tune_report["syrk"]["times_ms"][tune_report["syrk"]["chosen"]]
+    # the cohort GRM: split-BF16 standardised genotypes (16 significant bits, four products) for the
+    # cohort-GRM engines, so that tau lands within 1e-4 of FP64 arithmetic; the subset-exact engine
+    # needs none (the plain FP64 comparator keeps the tuner's BF16 GRM, or builds one)
     grm_prec = GRM_BF16X3_TC if args.grm == "bf16x3" else GRM_BF16_TC
-    if bt1 is None or grm_prec != GRM_BF16_TC:
-        t0 = time.perf_counter()
+    if exact:
+        grm_prec = GRM_BF16_TC
+    t0 = time.perf_counter()
+    if not (exact and tune_report is not None):
         ctx.grm_build(grm_prec)
-        grm_s = time.perf_counter() - t0
-    else:
-        grm_s = tune_report["syrk"][tune_report["chosen"][0]]
+    grm_s = time.perf_counter() - t0
     bt = ctx.build_timing()
-    if bt1 is None and grm_prec == GRM_BF16_TC:
-        bt1 = bt
+    if syrk1_ms is None and grm_prec == GRM_BF16_TC:
+        syrk1_ms = bt["syrk_ms"]
     build_products = 4 if grm_prec == GRM_BF16X3_TC else 1
     specs = make_specs(ctx, args, args.seed + 17 * rank)
-    mode = {"bf16x3": MV_BF16X3_TC, "tf32x3": MV_TF32X3_TC, "tf32": MV_TF32_TC, "fp32": MV_FP32_SIMT}[args.mode]
+    mode = {"subset": MV_SUBSET_EXACT, "bf16x3": MV_BF16X3_TC, "tf32x3": MV_TF32X3_TC, "tf32": MV_TF32_TC,
+            "fp32": MV_FP32_SIMT}[args.mode]
     ctx.set_matvec_mode(mode)
+    g_ms = ctx.build_timing()["zbuild_ms"] if exact else None  # the genotype matrix build
     from saigegpu import serve as _serve
     cols = _serve.columns_for(specs)
     setup_s = time.perf_counter() - t_setup
@@ -456,24 +520,36 @@ def run_ours(args, rank, world, local):
     # probe tables, column states, fetched results and probe reductions
     h2d = int(io_h2d // max(1, args.steps))
     d2h = int(io_d2h // max(1, args.steps))
-    traffic = None
-    try:  # DRAM bytes per launch scaled from a committed ncu capture of a smaller case
-        tr = json.load(open(os.path.join(ROOT, "profiles", "grmv_traffic.json")))
-        if args.mode == "bf16x3":
-            traffic = tr["traffic_over_algorithmic"]
-    except Exception:
-        pass
-    roof = grm_roofline(ctx, peaks, tdev, d["n"], ctx.grm_padded_n(), args.mode, traffic)
+    # DRAM bytes per launch scaled from an ncu capture of a smaller case
+    traffic = GRMV_TRAFFIC_RATIO if args.mode == "bf16x3" else None
+    npad_n = ctx.grm_padded_n()
+    mg = (args.m + 127) // 128 * 128
+    if exact:
+        roof = subset_roofline(peaks, tdev, npad_n, mg)
+    else:
+        roof = grm_roofline(ctx, peaks, tdev, d["n"], npad_n, args.mode, traffic)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "fits/hr", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_wall / args.steps * 1e3, 1),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": {"bf16x3": "bf16x3-tc/fp64", "tf32x3": "tf32x3-tc/fp64", "tf32": "tf32-tc/fp64", "fp32": "fp32/fp64"}[args.mode],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"subset": "bf16x2-tc/fp64", "bf16x3": "bf16x3-tc/fp64", "tf32x3": "tf32x3-tc/fp64",
+                  "tf32": "tf32-tc/fp64", "fp32": "fp32/fp64"}[args.mode],
         "data": "synthetic (seeded cohort generator; the reference's 150k x 100k synthetic AFR set is external)",
         "config": {"workload": "batched null-model fits on a resident GRM", "n_samples": d["n"],
                    "m_markers_qc": d["m_qc"], "m_markers": args.m, "missing": args.miss,
                    "phenotypes_per_step": args.phenos, "traits": "half binary / half quantitative",
-                   "sample_masks": "drop U(5%,40%)", "probes": 30, "grm": "BF16 tcgen05 SYRK, FP32 K",
-                   "grm_v": args.mode, "l2": "inputs larger than L2 (GRM %.0f GB)" % (4.0 * ctx.n ** 2 / 1e9),
+                   "sample_masks": "drop U(5%,40%)", "probes": 30,
+                   "semantics": ("exact per phenotype: each phenotype's GRM from its own samples' allele "
+                                 "frequencies, fill, QC and 1/sd (setgeno per phenotype, FIT.cpp:376-385, 436-495)"
+                                 if exact else
+                                 "masked approximation: the cohort GRM restricted to each phenotype's samples"),
+                   "grm": ("genotype matrix (0/1/2, BF16) in both layouts, K_S applied as G'V then G T' with "
+                           "per-phenotype weights; no K" if exact else
+                           "split-BF16 tcgen05 SYRK (four products), FP32 K" if args.grm == "bf16x3"
+                           else "BF16 tcgen05 SYRK, FP32 K"),
+                   "grm_v": args.mode,
+                   "l2": ("inputs larger than L2 (genotype matrix %.0f GB per GEMM)" % (2.0 * npad_n * mg / 1e9)
+                          if exact else "inputs larger than L2 (GRM %.0f GB)" % (4.0 * ctx.n ** 2 / 1e9)),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "value_basis": "device-busy time of engine steps (CUDA events)",
                    "runner": "blocking" if args.blocking_runner else "pipelined",
@@ -485,11 +561,18 @@ def run_ours(args, rank, world, local):
         "latency_s": {"p50": round(float(np.percentile(lat, 50)), 3), "p99": round(float(np.percentile(lat, 99)), 3)},
         "gpu_launches": int(launches),
         "roofline": roof,
-        "grm_build": {"grm": args.grm, "seconds": round(grm_s, 3), "syrk_products": build_products,
-                      "syrk_flops": build_products * syrk_flops,
+        "grm_build": {"grm": "bf16 (plain FP64 comparator only)" if exact else args.grm,
+                      "seconds": round(grm_s, 3), "syrk_products": build_products,
+                      "syrk_algorithmic_flops": syrk_flops,
+                      "syrk_executed_flops": build_products * syrk_flops,
                       "syrk_ms": round(bt["syrk_ms"], 2),
-                      "syrk_tflops": round(build_products * syrk_flops / (bt["syrk_ms"] * 1e-3) / 1e12, 1),
-                      "syrk_frac_of_bf16_peak": round(build_products * syrk_flops / (bt["syrk_ms"] * 1e-3) / 1e12 / peaks.get("bf16_tflops", 1900.0), 4),
+                      "syrk_algorithmic_tflops": round(syrk_flops / (bt["syrk_ms"] * 1e-3) / 1e12, 1),
+                      "syrk_algorithmic_frac_of_bf16_sustained": round(
+                          syrk_flops / (bt["syrk_ms"] * 1e-3) / 1e12 / peaks.get("bf16_tflops_sustained", 1700.0), 4),
+                      "syrk_executed_tflops": round(build_products * syrk_flops / (bt["syrk_ms"] * 1e-3) / 1e12, 1),
+                      "syrk_executed_frac_of_bf16_sustained": round(
+                          build_products * syrk_flops / (bt["syrk_ms"] * 1e-3) / 1e12
+                          / peaks.get("bf16_tflops_sustained", 1700.0), 4),
                       "zbuild_ms": round(bt["zbuild_ms"], 2),
                       # packed genotypes read + Z written (BF16, both halves for the split build)
                       "zbuild_GBps": round((d["m_qc"] * ((d["n"] + 3) // 4)
@@ -511,15 +594,18 @@ def run_ours(args, rank, world, local):
                                      "finish_host": round(finish_ms / 1e3 / args.steps, 3)},
         "step_widths": step_width_summary(trace),
     }
-    if bt1 is not None:  # the single-product BF16 SYRK (N(N+1)M FLOP), timed by the library's events
-        out["syrk_bf16"] = {"syrk_ms": round(bt1["syrk_ms"], 2), "flops": syrk_flops,
-                            "tflops": round(syrk_flops / (bt1["syrk_ms"] * 1e-3) / 1e12, 1),
-                            "frac_of_bf16_peak": round(syrk_flops / (bt1["syrk_ms"] * 1e-3) / 1e12
-                                                       / peaks.get("bf16_tflops", 1900.0), 4)}
+    if exact:
+        gb = 2.0 * 2.0 * npad_n * mg + mg * ((args.n + 3) // 4)  # both layouts written + codes read
+        out["genotype_matrix_build"] = {"ms": round(g_ms, 2), "GB": round(gb / 1e9, 2),
+                                        "GBps": round(gb / (g_ms * 1e-3) / 1e9, 1)}
+    if syrk1_ms is not None:  # the single-product BF16 SYRK (N(N+1)M FLOP), timed by the library's events
+        tf = syrk_flops / (syrk1_ms * 1e-3) / 1e12
+        out["syrk_bf16"] = {"syrk_ms": round(syrk1_ms, 2), "flops": syrk_flops, "tflops": round(tf, 1),
+                            "frac_of_bf16_peak": round(tf / peaks.get("bf16_tflops", 1900.0), 4),
+                            "frac_of_bf16_sustained": round(tf / peaks.get("bf16_tflops_sustained", 1700.0), 4)}
     if tune_report is not None:
-        out["tuning"] = {"clusters_syrk_grmv": list(tune_report["chosen"]),
-                         "syrk_s": {str(k): round(v, 4) for k, v in tune_report["syrk"].items()},
-                         "grmv_ms": {"%d@%d" % k: round(v * 1e3, 3) for k, v in tune_report["grmv"].items()}}
+        from saigegpu import tune
+        out["tuning"] = tune.report_json(tune_report)
     out["clocks"] = clk.summary()
     if rank == 0 and args.serve_requests > 0:
         out["serving"] = serving_block(ctx, args, cols)
@@ -533,28 +619,67 @@ def run_ours(args, rank, world, local):
                 out["speedup_vs_reference_gpu_algorithm"] = round(value / rg["fits_per_hr"], 1)
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(ctx, col_iters)
-        try:
-            os.makedirs(os.path.dirname(COUNTS_FILE), exist_ok=True)
-            if args.n == 100_000 and args.m == 150_000:
-                json.dump({"n": args.n, "m": args.m, "pcg_column_iterations_per_fit": col_iters},
-                          open(COUNTS_FILE, "w"))
-        except Exception:
-            pass
     ctx.close()
     return out
 
 
+def c1_full_fit(seed=1001, n=2000, m=5000, miss=0.01):
+    """One full binary null-model fit at N = 2,000, M = 5,000 on the host cores: the oracle's AI-REML
+    driver over the C restatement of the reference's CPU GRM.x (parallelCrossProdOpenMP,
+    FIT.cpp:1576-1598; OpenMP over all cores).  Returns the measured fit time and what the
+    per-product extrapolation used at N = 100k predicts for the same fit."""
+    from oracle import aireml, cpu_ref, plink
+    from saigegpu import prep, synth
+    bed, codes = synth.synth_bed(seed, n, m, miss)
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+    cg = cpu_ref.CpuGeno(g)
+
+    class CpuRefGRM:
+        """GRM.x through the reference's CPU algorithm, one column at a time."""
+        def __init__(self):
+            self.n, self.m_qc, self.is_diag_one = n, g.freq.shape[0], False
+            self.diag_sum = plink.diag_std_geno(g)
+            self.products = 0
+
+        def matvec(self, B):
+            B = np.asarray(B)
+            if B.ndim == 1:
+                self.products += 1
+                return cg.crossprod(B).astype(np.float64)
+            self.products += B.shape[1]
+            return np.column_stack([cg.crossprod(B[:, j]).astype(np.float64) for j in range(B.shape[1])])
+
+    grm = CpuRefGRM()
+    gv = synth.genetic_value_from_codes(g.codes, 3)
+    y, C = synth.simulate_pheno(gv, seed, "binary", tau=0.3, prevalence=0.2)
+    f0 = prep.make_fit0(y, C, "binary", True)
+    t0 = time.perf_counter()
+    fit = aireml.glmmkin_binary(grm, f0)
+    fit_s = time.perf_counter() - t0
+    b = np.random.default_rng(0).standard_normal(n).astype(np.float32)
+    cg.crossprod(b)
+    reps = 20
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        cg.crossprod(b)
+    per = (time.perf_counter() - t0) / reps
+    return {"n": n, "m_qc": int(grm.m_qc), "seconds": round(fit_s, 3), "fits_per_hr": round(3600.0 / fit_s, 2),
+            "grm_products": int(grm.products), "product_ms": round(per * 1e3, 3),
+            "products_share_of_fit": round(grm.products * per / fit_s, 3),
+            "tau": [float(x) for x in fit["theta"]],
+            "basis": "oracle AI-REML driver (numpy) over the C restatement of the reference's CPU GRM.x; "
+                     "products_share_of_fit = the part of the fit the per-product extrapolation counts"}
+
+
 def run_reference(args, rank, world):
-    """The reference's CPU path (oracle C restatement of parallelCrossProdOpenMP + PCG) on host cores."""
+    """The reference's CPU path (oracle C restatement of parallelCrossProdOpenMP) on the host cores:
+    each step times one GRM.x product at the workload's N and M, extrapolated to fits/hr with the
+    workload's PCG column-iterations per fit; one full fit at N = 2,000 is timed beside it."""
     if rank != 0:
         return None
     from oracle import cpu_ref
-    try:
-        iters = json.load(open(COUNTS_FILE))["pcg_column_iterations_per_fit"]
-        basis = "PCG iterations per fit measured by the GPU path (profiles/bench_counts.json)"
-    except Exception:
-        iters = 2000.0
-        basis = "assumed 2000 PCG iterations per fit (no GPU measurement available)"
+    iters = PCG_COLUMN_ITERATIONS_PER_FIT
+    basis = "%.1f PCG column-iterations per fit (measured by the GPU arm on this workload)" % iters
     t0 = time.perf_counter()
     pg = cpu_ref.PackedGeno.synthetic(args.seed, args.n, args.m, args.miss)
     setup = time.perf_counter() - t0
@@ -568,6 +693,11 @@ def run_reference(args, rank, world):
         times.append(time.perf_counter() - t)
     per = float(np.mean(times))
     value = 3600.0 / (per * iters)
+    c1 = None
+    try:
+        c1 = c1_full_fit()
+    except Exception as ex:  # the C1 fit is a companion figure; the line stands without it
+        c1 = {"unavailable": str(ex).splitlines()[0][:200]}
     return {
         "metric": METRIC, "value": round(value, 6), "unit": "fits/hr", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(per * 1e3, 1), "higher_is_better": True, "scaling": "weak",
@@ -577,7 +707,8 @@ def run_reference(args, rank, world):
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 6), "unit": "fits/hr", "cores": os.cpu_count(), "kind": "port",
                          "sample": "one GRM.x per step (oracle/cpu_ref.c restating FIT.cpp:1576-1598), "
-                                   "%.2f s each; %s; setup %.0f s" % (per, basis, setup)},
+                                   "%.2f s each; extrapolated with %s; setup %.0f s" % (per, basis, setup)},
+        "c1_full_fit": c1,
         "e2e": {"value": round(value, 6), "unit": "fits/hr", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

@@ -54,9 +54,15 @@ enum sg_matvec_mode {
   SG_MV_FP64_PLAIN = 2, /* plain FP64 GEMV (the single-RHS baseline) */
   SG_MV_TF32X3_TC = 3,  /* split-TF32 on tcgen05: K = Khi + Klo, P = Phi + Plo, three products
                            accumulated in TMEM (FP32-class accuracy at tensor-core rate) */
-  SG_MV_BF16X3_TC = 4   /* split-BF16 on tcgen05 (kind::f16): K and P as BF16 high + low halves
+  SG_MV_BF16X3_TC = 4,  /* split-BF16 on tcgen05 (kind::f16): K and P as BF16 high + low halves
                            (16 significant bits), three products in TMEM; ~1.5e-5 relative per
                            term, half the bytes and twice the MMA rate of SG_MV_TF32X3_TC */
+  SG_MV_SUBSET_EXACT = 5 /* subset-exact: each phenotype slot's product is K_S P with K_S the GRM
+                            of the slot's own sample subset (its allele frequencies, fill, QC and
+                            1/sd, as setgeno over that subset computes them, FIT.cpp:376-385,
+                            436-495), applied through the genotype matrix (0/1/2 in BF16, exact)
+                            with two tcgen05 GEMMs of two BF16 products each; needs no sg_grm_build.
+                            The other engines restrict the cohort GRM to the subset instead */
 };
 
 /* ------------------------------------------------------------ context */
@@ -73,10 +79,30 @@ int sg_set_matvec_mode(sg_ctx *ctx, int mode);
  * nothing arrives at, with a budget of budget_ms (<= 2000).  Returns SG_ERR_TIMEOUT (the expected
  * outcome) through the same device error flag the GEMMs use; the context stays usable. */
 int sg_selftest_wait_timeout(sg_ctx *ctx, double budget_ms);
-/* Tuning: how many CTAs (1, 2 or 4) of a thread-block cluster share one B tile through TMA multicast
- * in the tcgen05 SYRK and split-TF32 GRM.V (process-wide; saigegpu.tune picks them by timing). */
-int sg_set_tc_clusters(sg_ctx *ctx, int syrk, int grmv);
-int sg_get_tc_clusters(sg_ctx *ctx, int *syrk, int *grmv);
+/* Shape options of the tcgen05 GEMMs (process-wide; saigegpu.tune picks them by timing).  No
+ * reference counterpart (the reference's GRM.x is two cuBLAS SGEMV calls, gpuSymMatMult.cu:211-252).
+ * Every choice gives the same products up to the drain length: the accumulation order within a
+ * drain chunk and across chunks does not depend on the others. */
+enum sg_tc_option {
+  SG_TC_SYRK_PAIR = 0,   /* 1: SYRK tiles of 256 x 256 on CTA pairs (tcgen05 cta_group::2); default 0 */
+  SG_TC_GRMV_PAIR = 1,   /* 1: split-BF16 GRM.V tiles of 256 rows on CTA pairs; default 0 */
+  SG_TC_DRAIN_BYTES = 2, /* bytes of K per row one TMEM accumulator takes before it is added into
+                            registers: 128..4096, a multiple of 128; default 512 */
+  SG_TC_SYRK_GROUP = 3,  /* row tiles per raster group of the SYRK (1..4096); default 16 */
+  SG_TC_GRMV_SLICE = 4,  /* K slice bytes per pipeline stage of the split-BF16 GRM.V: 0 = by
+                            width (128 up to 160 columns, else 64), 64 or 128; default 0 */
+  SG_TC_SUBSET_PAIR = 5  /* 1: the subset-exact engine's genotype GEMMs on CTA pairs; default 0 */
+};
+int sg_set_tc_option(sg_ctx *ctx, int option, int value);
+int sg_get_tc_option(sg_ctx *ctx, int option, int *value);
+/* Per-width plan of the split-BF16 GRM.V (the tuner's choice table; process-wide): a launch over
+ * ncols columns takes pair[i] (SG_TC_GRMV_PAIR) and slice[i] (SG_TC_GRMV_SLICE) of the first
+ * bucket i with ncols <= max_cols[i] (max_cols increasing; at most 64 buckets); wider launches use
+ * the options.  n = 0 clears the plan.  sg_get_grmv_plan copies up to cap buckets and sets *n to
+ * the plan's length.  No reference counterpart. */
+int sg_set_grmv_plan(sg_ctx *ctx, int n, const int32_t *max_cols, const int32_t *pair,
+                     const int32_t *slice);
+int sg_get_grmv_plan(sg_ctx *ctx, int cap, int32_t *max_cols, int32_t *pair, int32_t *slice, int *n);
 /* GPU kernel launches issued by this context so far (for accounting). */
 int sg_kernel_launches(const sg_ctx *ctx, uint64_t *count);
 
@@ -95,6 +121,12 @@ int sg_setgeno(sg_ctx *ctx, const uint8_t *bed, uint64_t bed_len, int64_t n_fam,
                const int32_t *sub_1based, int64_t n_sub, const uint8_t *pheno_mask,
                float min_maf, float max_missing, const int32_t *vr_random_markers,
                int64_t n_vr_random, float min_mac_vr, int is_var_ratio, int is_diag_one);
+/* Categorical variance ratios for the next setgeno: the upper MAC bound g_maxMACVarRatio of
+ * setminMAC_VarianceRatio (FIT.cpp:4969-4973; the lower bound is setgeno's min_mac_vr).  With
+ * max_mac != -1, every marker with min_mac_vr <= MAC < max_mac becomes a variance-ratio marker and
+ * leaves the GRM, and from max_mac up only the random draw's markers do (FIT.cpp:497-518).
+ * -1 (the default) keeps the single-ratio selection. */
+int sg_set_vr_max_mac(sg_ctx *ctx, float max_mac);
 /* Same, reading the files; n_fam / m_bim are the line counts of .fam / .bim (FIT.cpp:760-787). */
 int sg_setgeno_files(sg_ctx *ctx, const char *bed_path, const char *bim_path, const char *fam_path,
                      const int32_t *sub_1based, int64_t n_sub, const uint8_t *pheno_mask,
@@ -151,6 +183,9 @@ int sg_grm_matmul(sg_ctx *ctx, const double *V, int64_t k, double *out);
  * ncols must be a multiple of 32 (else SG_ERR_INVALID).  The first call on a device looks up that
  * array's device address, so make the first call before any stream capture.  Every call shares
  * the array and overwrites what it uses; calls that overlap on the GPU (e.g. on two streams) race.
+ * A bounded device wait that gives up in any tcgen05 GEMM of the process sets one process-wide
+ * flag, which the next call that checks it reads and clears: a call that overlaps another tcgen05
+ * product on another stream may report that product's timeout, or leave its own to that product.
  * ``stream`` is a cudaStream_t (NULL = the legacy default stream); the call returns after the
  * product has finished. */
 int sg_grm_matmul_tf32x3_noalloc(sg_ctx *ctx, const float *P_dev, int64_t ncols, float *Y_dev,

@@ -119,7 +119,8 @@ def get_trace(grm, Sigma_iX, X, w, tau, cov, nrun, maxiter, tol, cutoff, seed=20
     t1, t0 = [], []
     start, end = 0, nrun
     while True:
-        U = np.stack([rademacher(seed, i, n) for i in range(start, end)], axis=1)
+        U = np.stack([rademacher(seed, i, n, getattr(grm, "probe_index", None)) for i in range(start, end)],
+                     axis=1)
         Su, it = pcg(grm, w, tau, U, maxiter, tol, return_iters=True)
         if stats is not None:
             stats.append(("trace", U.shape[1], it))
@@ -453,6 +454,18 @@ def variance_ratio(grm, fit, trait, X, vr_geno, order, num_markers=30, ratio_cv_
             continue
         break
     return float(np.mean(ratios)), np.array(ratios)
+
+
+def categorical_variance_ratio(grm, fit, trait, X, vr_geno, orders, num_markers=30, ratio_cv_cutoff=0.001,
+                               maxiter=500, tol=1e-5):
+    """extractVarianceRatio with isCateVarianceRatio (FIT.R:2245-2410): the single-ratio estimate
+    run once per MAC category over that category's markers, in ``orders[k]``."""
+    out = []
+    for order in orders:
+        if len(order) < num_markers:
+            raise ValueError("a MAC category has fewer than %d variance-ratio markers" % num_markers)
+        out.append(variance_ratio(grm, fit, trait, X, vr_geno, order, num_markers, ratio_cv_cutoff, maxiter, tol)[0])
+    return out
 
 
 def loco_grm(grm, geno, begin, end):

@@ -59,8 +59,11 @@ class GenoResult:
 
 
 def setgeno(bed, n_fam, m_bim, sub_1based, pheno_mask, min_maf=0.01, max_miss=0.15,
-            vr_random_set=None, min_mac_vr=20.0, is_var_ratio=False):
+            vr_random_set=None, min_mac_vr=20.0, is_var_ratio=False, max_mac_vr=-1.0):
     """Restatement of ``genoClass::setGenoObj`` (FIT.cpp:739-1024).
+
+    ``max_mac_vr`` != -1: categorical variance-ratio markers (g_maxMACVarRatio, FIT.cpp:497-518):
+    every marker with min_mac_vr <= MAC < max_mac_vr, and the random set's markers from max_mac_vr up.
 
     Returns a ``GenoResult`` with: ``codes`` (m_qc, nn) genotype 0/1/2 of the
     GRM markers in sub-sample order (missing already filled), ``freq``,
@@ -92,7 +95,12 @@ def setgeno(bed, n_fam, m_bim, sub_1based, pheno_mask, min_maf=0.01, max_miss=0.
         mac = min(allele, nn * 2 - allele)
         pass_qc = bool(maf >= f32(min_maf) and miss_rate <= f32(max_miss))
         pass_vr = False
-        if is_var_ratio and mac >= min_mac_vr:
+        if is_var_ratio and max_mac_vr != -1.0:
+            if min_mac_vr <= mac < max_mac_vr:
+                pass_vr = True
+            elif mac >= max_mac_vr:
+                pass_vr = i in vr_set
+        elif is_var_ratio and mac >= min_mac_vr:
             pass_vr = i in vr_set
         if pass_vr:
             pass_qc = False

@@ -44,9 +44,13 @@ def hash3(seed, stream, idx):
     return h
 
 
-def rademacher(seed, run, n):
-    """Probe vector u (length n, float64 in {-1,+1}) for probe number ``run``."""
-    h = hash3(seed, np.uint64(run), np.arange(n, dtype=np.uint64))
+def rademacher(seed, run, n, index=None):
+    """Probe vector u (length n, float64 in {-1,+1}) for probe number ``run``.
+
+    ``index``: the sample numbers the hash takes (default 0..n-1).  A phenotype whose samples are a
+    subset S of a cohort hashes the cohort positions S, as the engine masks the cohort's probes."""
+    idx = np.arange(n, dtype=np.uint64) if index is None else np.asarray(index, dtype=np.uint64)
+    h = hash3(seed, np.uint64(run), idx)
     return np.where((h >> np.uint64(63)) == 1, 1.0, -1.0)
 
 

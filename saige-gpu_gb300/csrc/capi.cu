@@ -114,6 +114,31 @@ struct Engine {
   // per-step records since the last timing reset (the first kStepTrace steps):
   // [columns the GRM.V computed, occupied columns, GRM.V ms, step ms, idle ms before the step]
   std::vector<double> trace;
+  // subset-exact engine: per slot, the state of its sample subset (kept while the mask is the same)
+  struct SlotSub {
+    bool valid = false;
+    bool all = false;             // built for "every sample" (no mask)
+    std::vector<uint8_t> mask;    // the mask it was built for
+    float* dp = nullptr;          // mg: d' = 1/sd'^2 (0 off the subset's GRM markers)
+    float* p2 = nullptr;          // mg: 2p'
+    float* lut = nullptr;         // mg x 4: d' (g - 2p')^2 per packed code (diagonal)
+    int32_t* flips = nullptr;     // fill-changed markers
+    float* dfill = nullptr;
+    int64_t flip_cap = 0;
+    uint32_t* bits = nullptr;     // np x W bit map
+    int64_t bits_cap = 0;
+    double* diag = nullptr;       // np: sum of z'^2 (the preconditioner's diagonal)
+    SubsetSlot dev;               // what d_slots[slot] holds
+    double m_prime = 0.0;
+  };
+  std::vector<SlotSub> sub;
+  SubsetSlot* d_slots = nullptr;
+  int max_w = 0;
+  void* Vb = nullptr;             // centred P halves: cap_cols x np BF16, high then low
+  float* Tm = nullptr;            // T = G^T v_c: cap_cols x mg
+  void* Tb = nullptr;             // T' halves: cap_cols x mg BF16, high then low
+  float* Um = nullptr;            // U = G T': cap_cols x np
+  double* spart = nullptr;        // column partials: cap_cols x max(blocks over np, over mg)
 };
 constexpr int64_t kStepTrace = 65536;
 constexpr int kTraceFields = 5;
@@ -169,6 +194,20 @@ struct sg_ctx {
   // ([3] Z build, [4] SYRK), in ms, from CUDA events on the context stream
   double t_build[5] = {0, 0, 0, 0, 0};
   cudaEvent_t tev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // every .bim marker in cohort order with missing calls kept, the cohort fill and the
+  // variance-ratio candidates per .bim marker, and setgeno's thresholds: what the subset-exact
+  // engine recomputes a phenotype subset's QC from
+  uint8_t* d_codes = nullptr;
+  uint8_t* d_vrflag_all = nullptr;
+  std::vector<int32_t> fill_all;
+  float qc_min_maf = 0.01f, qc_max_missing = 0.15f, qc_min_mac_vr = 20.0f, qc_max_mac_vr = -1.0f;
+  // upper MAC bound of categorical variance ratios for the next setgeno (-1: a single ratio)
+  float vr_max_mac = -1.0f;
+  int qc_is_var_ratio = 0;
+  // subset-exact engine: genotype values 0/1/2 (cohort fill in missing calls) in BF16, marker-major
+  // (mg x np) then sample-major (np x mg), mg = .bim markers rounded up to 128
+  void* d_G = nullptr;
+  int64_t mg = 0;
   // synthetic bed image
   uint8_t* d_synth = nullptr;
   uint64_t synth_len = 0;
@@ -342,19 +381,72 @@ __global__ void add_inplace_kernel(float* a, const float* b, int64_t n) {
 
 static int ensure_k_split(sg_ctx* c, bool want);
 static int ensure_k_bf16(sg_ctx* c, bool want);
+static void engine_free(sg_ctx* c);
+
+static int ensure_g(sg_ctx* c);
 
 extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
   if (!c) return SG_ERR_INVALID;
   if (mode != SG_MV_FP32_SIMT && mode != SG_MV_TF32_TC && mode != SG_MV_FP64_PLAIN &&
-      mode != SG_MV_TF32X3_TC && mode != SG_MV_BF16X3_TC)
+      mode != SG_MV_TF32X3_TC && mode != SG_MV_BF16X3_TC && mode != SG_MV_SUBSET_EXACT)
     return set_err(c, SG_ERR_INVALID, "unknown matvec mode %d", mode);
-  if ((mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC) && !tc_available())
+  if ((mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC || mode == SG_MV_SUBSET_EXACT) &&
+      !tc_available())
     return set_err(c, SG_ERR_INVALID, "tcgen05 path needs an sm_103a device");
   if (c->eng.inflight) return set_err(c, SG_ERR_STATE, "a step is in flight: finish it first");
+  if (mode == SG_MV_SUBSET_EXACT) {
+    if (!c->have_geno) return set_err(c, SG_ERR_STATE, "setgeno has not run");
+    if (c->loco) return set_err(c, SG_ERR_STATE, "clear the LOCO range first (sg_loco_clear)");
+    for (auto& kv : c->eng.reqs)
+      if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");
+  }
+  const bool was_exact = c->mv_mode == SG_MV_SUBSET_EXACT;
   c->mv_mode = mode;
+  // a slot's subset state and preconditioner belong to the engine they were set for: entering or
+  // leaving the subset-exact engine asks for every slot to be set again
+  if (was_exact != (mode == SG_MV_SUBSET_EXACT)) {
+    for (auto& ss : c->eng.sub) ss.valid = false;
+    std::fill(c->eng.ph_set.begin(), c->eng.ph_set.end(), 0);
+  }
+  if (mode == SG_MV_SUBSET_EXACT) {
+    SG_TRY(ensure_k_split(c, false));
+    SG_TRY(ensure_k_bf16(c, false));
+    return ensure_g(c);
+  }
+  if (was_exact) {  // the genotype matrix (2 bytes per sample and marker, twice) leaves HBM
+    SG_TRY(sync(c));
+    dev_free(c, c->d_G);
+    c->d_G = nullptr;
+  }
   if (!c->have_grm) return SG_OK;
   SG_TRY(ensure_k_split(c, mode == SG_MV_TF32X3_TC));
   return ensure_k_bf16(c, mode == SG_MV_BF16X3_TC);
+}
+
+// Genotype values of every .bim marker for the subset-exact engine, in BF16 (exact), both layouts.
+static int ensure_g(sg_ctx* c) {
+  if (c->d_G) return SG_OK;
+  const int64_t np = round_up(c->nn, kRowTile), mg = round_up(std::max<int64_t>(c->m_bim, 1), kRowTile);
+  if (c->have_grm && c->np != np) return set_err(c, SG_ERR_STATE, "GRM row padding differs");
+  if (!c->have_grm) {
+    engine_free(c);
+    c->np = np;
+  }
+  int32_t* d_fill = nullptr;
+  SG_TRY(dev_alloc_t(c, &d_fill, (size_t)std::max<int64_t>(c->m_bim, 1)));
+  SG_TRY(dev_alloc(c, &c->d_G, (size_t)(2 * mg * np * 2)));
+  if (c->m_bim)
+    SG_CUDA(c, cudaMemcpyAsync(d_fill, c->fill_all.data(), c->m_bim * 4, cudaMemcpyHostToDevice, c->stream));
+  SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
+  launch_gbuild(c->d_codes, c->pitch, d_fill, c->m_bim, c->nn, mg, np, c->d_G,
+                static_cast<uint16_t*>(c->d_G) + mg * np, c->stream);
+  SG_LAUNCHED(c, 1);
+  SG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
+  SG_TRY(sync(c));
+  c->t_build[3] = ev_ms(c->tev[0], c->tev[1]);
+  dev_free(c, d_fill);
+  c->mg = mg;
+  return SG_OK;
 }
 
 extern "C" int sg_ctx_make_current(sg_ctx* c) {
@@ -375,15 +467,40 @@ extern "C" int sg_selftest_wait_timeout(sg_ctx* c, double budget_ms) {
   return set_err(c, SG_ERR_STATE, "the wait completed although nothing arrived");
 }
 
-extern "C" int sg_set_tc_clusters(sg_ctx* c, int syrk, int grmv) {
+extern "C" int sg_set_tc_option(sg_ctx* c, int option, int value) {
   if (!c) return SG_ERR_INVALID;
-  if (!tc_set_clusters(syrk, grmv)) return set_err(c, SG_ERR_INVALID, "cluster sizes must be 1, 2 or 4");
+  if (!tc_set_option(option, value))
+    return set_err(c, SG_ERR_INVALID, "tcgen05 option %d cannot take the value %d", option, value);
   return SG_OK;
 }
 
-extern "C" int sg_get_tc_clusters(sg_ctx* c, int* syrk, int* grmv) {
-  if (!c || !syrk || !grmv) return SG_ERR_INVALID;
-  tc_get_clusters(syrk, grmv);
+extern "C" int sg_get_tc_option(sg_ctx* c, int option, int* value) {
+  if (!c || !value) return SG_ERR_INVALID;
+  const int v = tc_get_option(option);
+  if (v < 0) return set_err(c, SG_ERR_INVALID, "unknown tcgen05 option %d", option);
+  *value = v;
+  return SG_OK;
+}
+
+extern "C" int sg_set_grmv_plan(sg_ctx* c, int n, const int32_t* max_cols, const int32_t* pair,
+                                const int32_t* slice) {
+  if (!c || n < 0 || n > 64 || (n > 0 && (!max_cols || !pair || !slice))) return SG_ERR_INVALID;
+  if (!tc_set_grmv_plan(max_cols, pair, slice, n))
+    return set_err(c, SG_ERR_INVALID, "plan buckets need increasing max_cols, pair 0/1 and slice 0/64/128");
+  return SG_OK;
+}
+
+extern "C" int sg_get_grmv_plan(sg_ctx* c, int cap, int32_t* max_cols, int32_t* pair, int32_t* slice,
+                                int* n) {
+  if (!c || !n || cap < 0 || (cap > 0 && (!max_cols || !pair || !slice))) return SG_ERR_INVALID;
+  *n = tc_get_grmv_plan(max_cols, pair, slice, cap);
+  return SG_OK;
+}
+
+extern "C" int sg_set_vr_max_mac(sg_ctx* c, float max_mac) {
+  if (!c) return SG_ERR_INVALID;
+  if (max_mac != -1.0f && !(max_mac > 0.0f)) return set_err(c, SG_ERR_INVALID, "max MAC must be -1 or positive");
+  c->vr_max_mac = max_mac;
   return SG_OK;
 }
 
@@ -412,6 +529,11 @@ static void free_geno(sg_ctx* c) {
   c->d_Kb = nullptr;
   dev_free_t(c, c->d_diag);
   dev_free_t(c, c->d_diag32);
+  dev_free_t(c, c->d_codes);
+  dev_free_t(c, c->d_vrflag_all);
+  dev_free(c, c->d_G);
+  c->d_G = nullptr;
+  c->fill_all.clear();
   c->have_geno = false;
   c->have_grm = false;
 }
@@ -468,7 +590,7 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
   if (nn) SG_CUDA(c, cudaMemcpyAsync(d_sub, sub0.data(), nn * 4, cudaMemcpyHostToDevice, c->stream));
   SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
   launch_marker_qc(raw, raw_pitch, m_bim, n_fam, d_mask, nn, min_maf, max_missing, d_vrflag,
-                   min_mac_vr, is_var_ratio, d_qc, c->stream);
+                   min_mac_vr, c->vr_max_mac, is_var_ratio, d_qc, c->stream);
   SG_LAUNCHED(c, 1);
   SG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
   std::vector<MarkerQC> qc(m_bim);
@@ -493,6 +615,13 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
       c->vr_index.push_back((int32_t)i);
     }
   }
+  c->fill_all.resize(m_bim);
+  for (int64_t i = 0; i < m_bim; ++i) c->fill_all[i] = qc[i].fill;
+  c->qc_min_maf = min_maf;
+  c->qc_max_missing = max_missing;
+  c->qc_min_mac_vr = min_mac_vr;
+  c->qc_max_mac_vr = c->vr_max_mac;
+  c->qc_is_var_ratio = is_var_ratio;
   c->nn = nn;
   c->n_fam = n_fam;
   c->m_bim = m_bim;
@@ -520,12 +649,26 @@ static int setgeno_core(sg_ctx* c, const uint8_t* raw, int64_t raw_pitch, int64_
   launch_lut(d_qc, d_src + c->m_qc, c->m_vr, c->d_lut_vr, c->stream);
   SG_LAUNCHED(c, 4);
   SG_CUDA(c, cudaEventRecord(c->tev[3], c->stream));
+  // every marker in cohort order with missing calls kept (the subset-exact engine's source)
+  {
+    std::vector<int32_t> all(m_bim);
+    for (int64_t i = 0; i < m_bim; ++i) all[i] = (int32_t)i;
+    int32_t* d_all = nullptr;
+    SG_TRY(dev_alloc_t(c, &d_all, (size_t)std::max<int64_t>(m_bim, 1)));
+    SG_TRY(dev_alloc_t(c, &c->d_codes, (size_t)std::max<int64_t>(m_bim * c->pitch, 16)));
+    if (m_bim) SG_CUDA(c, cudaMemcpyAsync(d_all, all.data(), m_bim * 4, cudaMemcpyHostToDevice, c->stream));
+    launch_repack(raw, raw_pitch, d_all, nullptr, m_bim, d_sub, nn, identity ? 1 : 0, c->d_codes, c->pitch,
+                  c->stream);
+    SG_LAUNCHED(c, 1);
+    SG_TRY(sync(c));
+    dev_free(c, d_all);
+  }
   SG_TRY(sync(c));
   c->t_build[0] = ev_ms(c->tev[0], c->tev[1]);
   c->t_build[1] = ev_ms(c->tev[2], c->tev[3]);
   dev_free(c, d_src);
   dev_free(c, d_mask);
-  dev_free(c, d_vrflag);
+  c->d_vrflag_all = d_vrflag;  // kept for the subset-exact engine's per-subset QC
   dev_free(c, d_qc);
   dev_free(c, d_sub);
   // GRM diagonal from the packed genotypes
@@ -641,6 +784,13 @@ extern "C" int sg_setgeno_files(sg_ctx* c, const char* bed_path, const char* bim
   do { if (!(c)) return SG_ERR_INVALID; if (!(c)->have_geno) return set_err((c), SG_ERR_STATE, "setgeno has not run"); } while (0)
 #define NEED_GRM(c) \
   do { NEED_GENO(c); if (!(c)->have_grm) return set_err((c), SG_ERR_STATE, "sg_grm_build has not run"); } while (0)
+// the engine's operator: the resident K, or (subset-exact engine) the genotype matrix
+#define NEED_OPERATOR(c)                                                                               \
+  do {                                                                                                 \
+    NEED_GENO(c);                                                                                      \
+    if (!(c)->have_grm && !((c)->mv_mode == SG_MV_SUBSET_EXACT && (c)->d_G))                            \
+      return set_err((c), SG_ERR_STATE, "sg_grm_build has not run (or select SG_MV_SUBSET_EXACT)");    \
+  } while (0)
 
 extern "C" int sg_geno_dims(sg_ctx* c, int64_t* n, int64_t* m_total, int64_t* m_qc, int64_t* m_vr) {
   NEED_GENO(c);
@@ -810,7 +960,7 @@ static int ensure_k_bf16(sg_ctx* c, bool want) {
 }
 
 extern "C" int sg_grm_padded_n(sg_ctx* c, int64_t* np) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   if (!np) return set_err(c, SG_ERR_INVALID, "null output");
   *np = c->np;
   return SG_OK;
@@ -821,6 +971,8 @@ extern "C" int sg_grm_matmul_tf32x3_noalloc(sg_ctx* c, const float* P_dev, int64
                                             void* stream) {
   NEED_GRM(c);
   if (!P_dev || !Y_dev) return set_err(c, SG_ERR_INVALID, "null device pointer");
+  // the scratch address is looked up per device, for the device that is current
+  SG_CUDA(c, cudaSetDevice(c->device));
   if (!c->k_split)
     return set_err(c, SG_ERR_STATE, "select SG_MV_TF32X3_TC first (the split GRM is not resident)");
   if (ncols <= 0 || ncols % 32 != 0)
@@ -886,6 +1038,20 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.d_sx); dev_free_t(c, e.d_dpart); dev_free_t(c, e.d_dcols); dev_free_t(c, e.ptab);
   dev_free_t(c, e.pcache);
   e.pcache_key.clear();
+  for (auto& ss : e.sub) {
+    dev_free_t(c, ss.dp); dev_free_t(c, ss.p2); dev_free_t(c, ss.lut); dev_free_t(c, ss.flips);
+    dev_free_t(c, ss.dfill); dev_free_t(c, ss.bits); dev_free_t(c, ss.diag);
+  }
+  e.sub.clear();
+  e.max_w = 0;
+  dev_free_t(c, e.d_slots);
+  dev_free(c, e.Vb);
+  e.Vb = nullptr;
+  dev_free_t(c, e.Tm);
+  dev_free(c, e.Tb);
+  e.Tb = nullptr;
+  dev_free_t(c, e.Um);
+  dev_free_t(c, e.spart);
   e.dots_cap_sx = e.dots_cap_part = e.dots_cap_cols = 0;
   if (e.inflight) cudaStreamSynchronize(c->stream);
   e.inflight = false;
@@ -961,7 +1127,7 @@ static int engine_clear(sg_ctx* c) {
 }
 
 static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   Engine& e = c->eng;
   max_columns = round_up(std::max<int64_t>(max_columns, 32), 32);
   if (max_columns > 96) max_columns = round_up(max_columns, 128);
@@ -1025,6 +1191,9 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   e.col_req.assign(max_columns, -1);
   e.h_ph.assign(max_phenos, PhenoState{0.0, 0.0});
   e.ph_set.assign(max_phenos, 0);
+  e.sub.assign(max_phenos, Engine::SlotSub{});
+  SG_TRY(dev_alloc_t(c, &e.d_slots, (size_t)max_phenos));
+  SG_CUDA(c, cudaMemsetAsync(e.d_slots, 0, max_phenos * sizeof(SubsetSlot), c->stream));
   e.hi_col = 0;
   e.n_active = 0;
   e.queue.clear();
@@ -1039,12 +1208,116 @@ extern "C" int sg_engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phe
   return engine_reserve(c, max_columns, max_phenos);
 }
 
+// Subset-exact engine: the state of slot ``slot``'s sample subset, rebuilt only when its mask
+// changes.  The subset's per-marker counts, fill, QC, frequency and 1/sd come from the same kernel
+// setgeno uses (genoClass::setGenoObj over the subset, FIT.cpp:376-385, 436-495, 916-921), run on
+// the cohort's codes of every .bim marker with the subset as the phenotype mask; the host turns them
+// into d' = 1/sd'^2 (GRM markers), 2p', the fill-changed markers and the diagonal table.  dmask: the
+// mask bytes already on the device (side stream), or nullptr for every sample.
+static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint8_t* dmask) {
+  Engine& e = c->eng;
+  Engine::SlotSub& ss = e.sub[slot];
+  const int64_t nn = c->nn, np = e.np, mg = c->mg, m = c->m_bim;
+  if (ss.valid && ((!mask && ss.all) || (mask && !ss.all && std::memcmp(ss.mask.data(), mask, nn) == 0)))
+    return SG_OK;
+  const int64_t nwords = (nn + 15) / 16;
+  std::vector<uint32_t> maskbits(nwords + 1, 0u);
+  int64_t ns = 0;
+  for (int64_t i = 0; i < nn; ++i)
+    if (!mask || mask[i]) {
+      maskbits[i / 16] |= 1u << (2 * (i % 16));
+      ++ns;
+    }
+  if (ns == 0) return set_err(c, SG_ERR_INVALID, "phenotype slot %lld: empty sample subset", (long long)slot);
+  uint32_t* d_mb = nullptr;
+  MarkerQC* d_qc = nullptr;
+  SG_TRY(dev_alloc_t(c, &d_mb, maskbits.size()));
+  SG_TRY(dev_alloc_t(c, &d_qc, (size_t)std::max<int64_t>(m, 1)));
+  SG_CUDA(c, cudaMemcpyAsync(d_mb, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, c->side));
+  launch_marker_qc(c->d_codes, c->pitch, m, nn, d_mb, ns, c->qc_min_maf, c->qc_max_missing, c->d_vrflag_all,
+                   c->qc_min_mac_vr, c->qc_max_mac_vr, c->qc_is_var_ratio, d_qc, c->side);
+  SG_LAUNCHED(c, 1);
+  std::vector<MarkerQC> qc(m);
+  if (m) SG_CUDA(c, cudaMemcpyAsync(qc.data(), d_qc, m * sizeof(MarkerQC), cudaMemcpyDeviceToHost, c->side));
+  SG_TRY(sync_side(c));
+  dev_free(c, d_mb);
+  dev_free(c, d_qc);
+  std::vector<float> dp(mg, 0.0f), p2(mg, 0.0f), lut(4 * mg, 0.0f), dfill;
+  std::vector<int32_t> flips;
+  int64_t mprime = 0;
+  for (int64_t k = 0; k < m; ++k) {
+    const MarkerQC& q = qc[k];
+    if (!q.pass_qc) continue;
+    ++mprime;
+    const double d = (double)q.invstd * (double)q.invstd;
+    const float two_p = 2.0f * q.freq;  // exact: the LUT's 2p (setStdGenoLookUpArr FIT.cpp:152-159)
+    dp[k] = (float)d;
+    p2[k] = two_p;
+    // packed codes 00 -> 2, 01 -> missing (the subset fill), 10 -> 1, 11 -> 0
+    const double g[4] = {2.0, (double)q.fill, 1.0, 0.0};
+    for (int t = 0; t < 4; ++t) lut[4 * k + t] = (float)(d * (g[t] - two_p) * (g[t] - two_p));
+    if (q.fill != c->fill_all[k]) {
+      flips.push_back((int32_t)k);
+      dfill.push_back((float)(q.fill - c->fill_all[k]));
+    }
+  }
+  if (mprime == 0) return set_err(c, SG_ERR_STATE, "phenotype slot %lld: no marker passes QC in its subset", (long long)slot);
+  const int nflip = (int)flips.size();
+  const int W = (nflip + 31) / 32;
+  if (!ss.dp) SG_TRY(dev_alloc_t(c, &ss.dp, (size_t)mg));
+  if (!ss.p2) SG_TRY(dev_alloc_t(c, &ss.p2, (size_t)mg));
+  if (!ss.lut) SG_TRY(dev_alloc_t(c, &ss.lut, (size_t)(4 * mg)));
+  if (!ss.diag) SG_TRY(dev_alloc_t(c, &ss.diag, (size_t)np));
+  if (nflip > ss.flip_cap) {
+    dev_free_t(c, ss.flips);
+    dev_free_t(c, ss.dfill);
+    SG_TRY(dev_alloc_t(c, &ss.flips, (size_t)nflip));
+    SG_TRY(dev_alloc_t(c, &ss.dfill, (size_t)nflip));
+    ss.flip_cap = nflip;
+  }
+  if ((int64_t)W * np > ss.bits_cap) {
+    dev_free_t(c, ss.bits);
+    SG_TRY(dev_alloc_t(c, &ss.bits, (size_t)(W * np)));
+    ss.bits_cap = (int64_t)W * np;
+  }
+  SG_CUDA(c, cudaMemcpyAsync(ss.dp, dp.data(), mg * 4, cudaMemcpyHostToDevice, c->side));
+  SG_CUDA(c, cudaMemcpyAsync(ss.p2, p2.data(), mg * 4, cudaMemcpyHostToDevice, c->side));
+  SG_CUDA(c, cudaMemcpyAsync(ss.lut, lut.data(), 4 * mg * 4, cudaMemcpyHostToDevice, c->side));
+  if (nflip) {
+    SG_CUDA(c, cudaMemcpyAsync(ss.flips, flips.data(), nflip * 4, cudaMemcpyHostToDevice, c->side));
+    SG_CUDA(c, cudaMemcpyAsync(ss.dfill, dfill.data(), nflip * 4, cudaMemcpyHostToDevice, c->side));
+  }
+  launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, nflip, W, dmask, nn, np, ss.bits, c->side);
+  launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, ss.diag, c->side);
+  SG_LAUNCHED(c, W > 0 ? 2 : 1);
+  ss.dev.dprime = ss.dp;
+  ss.dev.p2 = ss.p2;
+  ss.dev.flips = ss.flips;
+  ss.dev.dfill = ss.dfill;
+  ss.dev.bits = ss.bits;
+  ss.dev.nflip = nflip;
+  ss.dev.W = W;
+  ss.dev.inv_m = 1.0 / (double)mprime;
+  ss.dev.ns = (double)ns;
+  SG_CUDA(c, cudaMemcpyAsync(e.d_slots + slot, &ss.dev, sizeof(SubsetSlot), cudaMemcpyHostToDevice, c->side));
+  SG_TRY(sync_side(c));  // the host vectors above must outlive their copies
+  ss.m_prime = (double)mprime;
+  ss.all = mask == nullptr;
+  if (mask) ss.mask.assign(mask, mask + nn);
+  else ss.mask.clear();
+  ss.valid = true;
+  e.max_w = 0;
+  for (const auto& x : e.sub)
+    if (x.valid) e.max_w = std::max(e.max_w, (int)x.dev.W);
+  return SG_OK;
+}
+
 // A slot's weights: 1/W and the Jacobi preconditioner from getDiagOfSigma in FP64
 // (FIT.cpp:2322-2365); with a chromosome left out, getDiagOfSigma_LOCO (FIT.cpp:2370-2392): diag
 // minus the chromosome's sum z^2, over M - M_j.
 extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, const double* tau,
                                    const uint8_t* mask) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   Engine& e = c->eng;
   if (e.cap_ph == 0) SG_TRY(engine_reserve(c, 128, std::max<int64_t>(slot + 1, 1)));
   if (slot < 0 || slot >= e.cap_ph) return set_err(c, SG_ERR_INVALID, "phenotype slot %lld out of range", (long long)slot);
@@ -1073,7 +1346,14 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     uint8_t* dm = reinterpret_cast<uint8_t*>(e.d_wstage + e.np);
     SG_CUDA(c, h2d(c, dw, hw, c->nn * sizeof(double), c->side));
     if (mask) SG_CUDA(c, h2d(c, dm, hm, c->nn, c->side));
-    launch_slot_weights(e.np, c->nn, dw, mask ? dm : nullptr, loco ? c->d_diag_loco : c->d_diag, m, tau[0], tau[1],
+    const double* diag = loco ? c->d_diag_loco : c->d_diag;
+    double mm = m;
+    if (c->mv_mode == SG_MV_SUBSET_EXACT) {  // the subset's own diagonal and GRM marker count
+      SG_TRY(subset_setup(c, slot, mask, mask ? dm : nullptr));
+      diag = e.sub[slot].diag;
+      mm = e.sub[slot].m_prime;
+    }
+    launch_slot_weights(e.np, c->nn, dw, mask ? dm : nullptr, diag, mm, tau[0], tau[1],
                         c->is_diag_one ? 1 : 0, e.winv + slot * e.np, e.minv + slot * e.np, c->side);
     SG_LAUNCHED(c, 1);
   }
@@ -1088,7 +1368,7 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
 static int engine_submit_common(sg_ctx* c, int64_t slot, int kind, const double* B, bool probe,
                                 uint64_t seed, int64_t run0, int64_t k, int maxiter, double tol,
                                 int64_t* ids) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   Engine& e = c->eng;
   if (slot < 0 || slot >= e.cap_ph || !e.ph_set[slot])
     return set_err(c, SG_ERR_STATE, "phenotype slot %lld not set", (long long)slot);
@@ -1127,7 +1407,7 @@ extern "C" int sg_engine_submit_probes(sg_ctx* c, int64_t slot, int kind, uint64
 
 extern "C" int sg_engine_submit_chained(sg_ctx* c, int64_t slot, const int64_t* src_ids, int64_t k, int maxiter,
                                         double tol, int64_t* ids) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   Engine& e = c->eng;
   if (!e.hold) return set_err(c, SG_ERR_STATE, "chained solves need held results (sg_engine_hold_results)");
   if (slot < 0 || slot >= e.cap_ph || !e.ph_set[slot])
@@ -1433,6 +1713,45 @@ static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf, int64_t* la
     c->launches += 1;
     return SG_OK;
   }
+  if (c->mv_mode == SG_MV_SUBSET_EXACT) {
+    // K_S P per column's own sample subset, through the genotype matrix (k_subset.cu)
+    const int64_t nact = e.nact;
+    if (nact == 0) {
+      *launched = 0;
+      return SG_OK;
+    }
+    const int64_t np = e.np, mg = c->mg;
+    const int64_t npad = tc_grmv_padded_cols(round_up(nact, 32), e.cap_cols, np, kTilesSplitB, c->num_sms);
+    for (int64_t j = nact; j < npad; ++j) e.h_gcols[j] = -1;
+    SG_CUDA(c, cudaMemcpyAsync(e.d_gcols, e.h_gcols, npad * 4, cudaMemcpyHostToDevice, c->stream));
+    const size_t cap = (size_t)e.cap_cols;
+    if (!e.Vb) SG_TRY(dev_alloc(c, &e.Vb, cap * np * 4));
+    if (!e.Tm) SG_TRY(dev_alloc_t(c, &e.Tm, cap * mg));
+    if (!e.Tb) SG_TRY(dev_alloc(c, &e.Tb, cap * mg * 4));
+    if (!e.Um) SG_TRY(dev_alloc_t(c, &e.Um, cap * np));
+    if (!e.spart) SG_TRY(dev_alloc_t(c, &e.spart, cap * (size_t)std::max(subset_nblk(np), subset_nblk(mg))));
+    uint16_t* vh = static_cast<uint16_t*>(e.Vb);
+    uint16_t* vl = vh + cap * np;
+    uint16_t* th = static_cast<uint16_t*>(e.Tb);
+    uint16_t* tl = th + cap * mg;
+    const uint16_t* Gmm = static_cast<const uint16_t*>(c->d_G);
+    const uint16_t* Gsm = Gmm + mg * np;
+    launch_subset_prepare(e.Pf, np, e.d_gcols, npad, e.d_st, e.d_slots, e.winv, e.spart, vh, vl, c->stream);
+    c->launches += 2;
+    cudaError_t err = tc_gemm_splitb(Gmm, mg, np, vh, vl, npad, e.Tm, mg, c->stream, false, 0);
+    if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 genotype GEMM (G'V): %s", cudaGetErrorString(err));
+    launch_subset_scale(vh, vl, np, c->nn, e.d_gcols, npad, e.d_st, e.d_slots, e.max_w, e.Tm, mg, th, tl, e.spart,
+                        c->stream);
+    c->launches += e.max_w > 0 ? 3 : 2;
+    err = tc_gemm_splitb(Gsm, np, mg, th, tl, npad, e.Um, np, c->stream, false, 1);
+    if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 genotype GEMM (G T'): %s", cudaGetErrorString(err));
+    launch_subset_finalize(e.Um, np, c->nn, e.d_gcols, npad, e.d_st, e.d_slots, th, tl, mg, e.spart, e.winv, e.Yf,
+                           c->stream);
+    c->launches += 2;
+    SG_LAUNCHED(c, 0);
+    *launched = npad;
+    return SG_OK;
+  }
   if (c->mv_mode == SG_MV_TF32_TC || c->mv_mode == SG_MV_TF32X3_TC) {
     const bool split = c->mv_mode == SG_MV_TF32X3_TC;
     if (split) {
@@ -1458,8 +1777,10 @@ static int release_col(sg_ctx* c, int64_t col);
 // Columns the GRM.V of one step covers: [0, hi_col) padded to the kernel's column tile (the
 // padding columns are free or finished, their P rows are zero).
 static bool tc_mode(int mode) {
-  return mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC;
+  return mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC || mode == SG_MV_SUBSET_EXACT;
 }
+// engines that gather the step's active columns into a compact block themselves
+static bool compact_mode(int mode) { return mode == SG_MV_BF16X3_TC || mode == SG_MV_SUBSET_EXACT; }
 
 static int64_t engine_gemm_cols(const sg_ctx* c) {
   const Engine& e = c->eng;
@@ -1480,7 +1801,7 @@ static int step_launch(sg_ctx* c) {
   for (int64_t col = 0; col < e.hi_col; ++col)
     if (e.h_st[col].active) e.h_gcols[e.nact++] = (int32_t)col;
   // the split-BF16 engine compacts the active columns itself; the others cover [0, hi_col) padded
-  const int64_t ncols = c->mv_mode == SG_MV_BF16X3_TC ? round_up(e.hi_col, 32) : engine_gemm_cols(c);
+  const int64_t ncols = compact_mode(c->mv_mode) ? round_up(e.hi_col, 32) : engine_gemm_cols(c);
   int64_t occupied = 0;
   for (int64_t col = 0; col < e.hi_col; ++col) occupied += e.h_st[col].active ? 1 : 0;
   bool yf = true;
@@ -1491,7 +1812,7 @@ static int step_launch(sg_ctx* c) {
   SG_CUDA(c, cudaEventRecord(e.ev[1], c->stream));
   const float* Yf = yf ? e.Yf : nullptr;
   const double* Yd = yf ? nullptr : e.Yd;
-  if (c->mv_mode != SG_MV_BF16X3_TC && e.nact > 0)  // the split-BF16 GRM.V uploaded the list already
+  if (!compact_mode(c->mv_mode) && e.nact > 0)  // the compacting engines uploaded the list already
     SG_CUDA(c, cudaMemcpyAsync(e.d_gcols, e.h_gcols, e.nact * 4, cudaMemcpyHostToDevice, c->stream));
   launch_pcg_sigma_dot(e.np, e.nact, e.d_st, e.d_ph, e.winv, e.minv, e.P, Yf, Yd, e.part, e.nblk, e.d_gcols,
                        c->stream);
@@ -1634,7 +1955,7 @@ static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
 }
 
 extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   Engine& e = c->eng;
   if (e.cap_cols == 0) return set_err(c, SG_ERR_STATE, "engine not reserved");
   int64_t fin = 0;
@@ -1668,7 +1989,7 @@ extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) 
 // results, run probe reductions, upload weights of idle slots and submit work (it joins the next
 // launch); those calls use the side stream and never wait for the step.
 extern "C" int sg_engine_launch(sg_ctx* c, int64_t* n_finished, int* launched) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   Engine& e = c->eng;
   if (e.cap_cols == 0) return set_err(c, SG_ERR_STATE, "engine not reserved");
   if (e.inflight) return set_err(c, SG_ERR_STATE, "a step is in flight: finish it first");
@@ -1807,7 +2128,7 @@ extern "C" int sg_engine_probe_cached(sg_ctx* c, int64_t slot, uint64_t seed, in
 extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_pcg,
                                     const int64_t* ids_prod, int64_t k, uint64_t seed, int64_t run0,
                                     const double* SX, int64_t p, double* out, int32_t* iters) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   Engine& e = c->eng;
   if (k <= 0 || !ids_pcg || !ids_prod || !out || p < 0 || p > kProbeDotsMaxP || (p > 0 && !SX))
     return set_err(c, SG_ERR_INVALID, "probe_dots: bad arguments (p <= %d)", kProbeDotsMaxP);
@@ -2020,6 +2341,8 @@ extern "C" int sg_loco_set(sg_ctx* c, int64_t begin, int64_t end) {
     return set_err(c, SG_ERR_INVALID, "LOCO range [%lld, %lld] outside the %lld GRM markers", (long long)begin,
                    (long long)end, (long long)c->m_qc);
   if (end - begin + 1 >= c->m_qc) return set_err(c, SG_ERR_INVALID, "LOCO range covers every GRM marker");
+  if (c->mv_mode == SG_MV_SUBSET_EXACT)
+    return set_err(c, SG_ERR_STATE, "LOCO runs on the resident GRM: select another engine first");
   for (auto& kv : c->eng.reqs)
     if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");
   loco_free(c);
@@ -2093,7 +2416,7 @@ int fetch(sg_ctx* c, int64_t id, double* x, int32_t* it) { return sg_engine_fetc
 
 // Drop-ins run on phenotype slot 0 with capacity for one probe block.
 int dropin_setup(sg_ctx* c, const float* w, const float* tau, int64_t cols) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   Engine& e = c->eng;
   SG_TRY(engine_clear(c));
   if (e.cap_cols < cols || e.cap_ph < 1 || e.np != c->np) SG_TRY(engine_reserve(c, std::max<int64_t>(cols, 128), 1));
@@ -2222,7 +2545,7 @@ int trace_probes(sg_ctx* c, const std::vector<double>& SX, int p, const std::vec
 
 // ------------------------------------------------------------------ drop-ins
 extern "C" int sg_grm_matmul(sg_ctx* c, const double* V, int64_t k, double* out) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   if (k <= 0 || !V || !out) return set_err(c, SG_ERR_INVALID, "bad arguments");
   {
     std::vector<float> w(c->nn, 1.0f);
@@ -2237,7 +2560,7 @@ extern "C" int sg_grm_matmul(sg_ctx* c, const double* V, int64_t k, double* out)
 }
 
 extern "C" int sg_getCrossprodMatAndKin(sg_ctx* c, const float* b, float* out) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   std::vector<double> bd, od(c->nn);
   f2d(b, c->nn, bd);
   SG_TRY(sg_grm_matmul(c, bd.data(), 1, od.data()));
@@ -2257,7 +2580,7 @@ extern "C" int sg_getDiagOfSigma(sg_ctx* c, const float* w, const float* tau, fl
 }
 
 extern "C" int sg_getCrossprod(sg_ctx* c, const float* b, const float* w, const float* tau, float* out) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   const int64_t n = c->nn;
   if (tau[1] == 0.0f) {
     for (int64_t i = 0; i < n; ++i) out[i] = tau[0] * (b[i] * (1.0f / w[i]));
@@ -2271,7 +2594,7 @@ extern "C" int sg_getCrossprod(sg_ctx* c, const float* b, const float* w, const 
 
 extern "C" int sg_pcg_solve(sg_ctx* c, const double* w, const double* tau, const double* B, int64_t k,
                             int maxiter, double tol, double* X, int32_t* iters) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   if (k <= 0 || !w || !tau || !B || !X) return set_err(c, SG_ERR_INVALID, "bad arguments");
   Engine& e = c->eng;
   SG_TRY(engine_clear(c));
@@ -2287,7 +2610,7 @@ extern "C" int sg_pcg_solve(sg_ctx* c, const double* w, const double* tau, const
 
 static int solve_f32(sg_ctx* c, const float* w, const float* tau, const float* B, int64_t k, int maxiter,
                      float tol, float* out, int32_t* iters) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   const int64_t n = c->nn;
   if (!all_finite(w, n) || !all_finite(tau, 2)) return set_err(c, SG_ERR_NUMERIC, "W or tau not finite");
   std::vector<double> wd, bd, xd(n * k);
@@ -2315,7 +2638,7 @@ extern "C" int sg_getSigma_G(sg_ctx* c, const float* w, const float* tau, const 
 extern "C" int sg_getCoefficients(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* w,
                                   const float* tau, int maxiter, float tol, float* Sigma_iY,
                                   float* Sigma_iX, float* cov, float* alpha, float* eta) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   const int64_t n = c->nn;
   if (p <= 0) return set_err(c, SG_ERR_INVALID, "p must be positive");
   std::vector<float> B(n * (p + 1));
@@ -2351,7 +2674,7 @@ extern "C" int sg_getCoefficients(sg_ctx* c, const float* Y, const float* X, int
 static int trace_common(sg_ctx* c, const float* Sigma_iX, int64_t p, const float* w, const float* tau,
                         const float* cov, int nrun, int maxiter, float tol, float cutoff, uint64_t seed,
                         bool quant, float* trace, int32_t* nrun_used) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   if (nrun < 2) return set_err(c, SG_ERR_INVALID, "nrun must be >= 2");
   SG_TRY(dropin_setup(c, w, tau, 2 * nrun + 4));
   std::vector<double> SX, cv;
@@ -2394,7 +2717,7 @@ struct AIOut {
 int ai_score(sg_ctx* c, const float* Y, const float* X, int64_t p, const float* w, const float* tau,
              const float* Sigma_iY, const float* Sigma_iX, const float* cov_in, int nrun, int maxiter,
              float tol, float cutoff, uint64_t seed, bool quant, AIOut* o) {
-  NEED_GRM(c);
+  NEED_OPERATOR(c);
   const int64_t n = c->nn;
   SG_TRY(dropin_setup(c, w, tau, 2 * nrun + 8));
   std::vector<double> Yd, Xd, SY, SX, cv;

@@ -24,7 +24,8 @@ namespace sg {
 __global__ void marker_qc_kernel(const uint8_t* __restrict__ raw, int64_t pitch, int64_t m,
                                  int64_t n_fam, const uint32_t* __restrict__ maskbits, int64_t nn,
                                  float min_maf, float max_miss, const uint8_t* __restrict__ vr_flag,
-                                 float min_mac_vr, int is_var_ratio, MarkerQC* __restrict__ out) {
+                                 float min_mac_vr, float max_mac_vr, int is_var_ratio,
+                                 MarkerQC* __restrict__ out) {
   const int64_t marker = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (marker >= m) return;
@@ -60,7 +61,16 @@ __global__ void marker_qc_kernel(const uint8_t* __restrict__ raw, int64_t pitch,
   const int mac = min(allele, (int)(nn * 2) - allele);
   int pass_qc = (maf >= min_maf && miss_rate <= max_miss) ? 1 : 0;  // FIT.cpp:493-495
   int pass_vr = 0;
-  if (is_var_ratio && (float)mac >= min_mac_vr && vr_flag[marker]) pass_vr = 1;  // FIT.cpp:521-543
+  if (is_var_ratio) {
+    if (max_mac_vr != -1.0f) {
+      // categorical variance ratios (FIT.cpp:497-518): every marker with min <= MAC < max, and the
+      // random draw's markers from max up
+      if ((float)mac >= min_mac_vr && (float)mac < max_mac_vr) pass_vr = 1;
+      else if ((float)mac >= max_mac_vr && vr_flag[marker]) pass_vr = 1;
+    } else if ((float)mac >= min_mac_vr && vr_flag[marker]) {
+      pass_vr = 1;  // FIT.cpp:521-543
+    }
+  }
   if (pass_vr) pass_qc = 0;                                                      // FIT.cpp:545-547
   // FIT.cpp:916-921: Std = sqrt(2p(1-p)), invStd = 1/Std (0 if Std == 0), in float
   const float sd = __fsqrt_rn(__fmul_rn(__fmul_rn(2.0f, alt), __fsub_rn(1.0f, alt)));
@@ -79,14 +89,14 @@ __global__ void marker_qc_kernel(const uint8_t* __restrict__ raw, int64_t pitch,
 
 void launch_marker_qc(const uint8_t* raw, int64_t raw_pitch, int64_t m, int64_t n_fam,
                       const uint32_t* maskbits, int64_t nn, float min_maf, float max_miss,
-                      const uint8_t* vr_flag, float min_mac_vr, int is_var_ratio, MarkerQC* out,
-                      cudaStream_t s) {
+                      const uint8_t* vr_flag, float min_mac_vr, float max_mac_vr, int is_var_ratio,
+                      MarkerQC* out, cudaStream_t s) {
   const int warps = 8;
   const int64_t blocks = (m + warps - 1) / warps;
   if (blocks == 0) return;
   marker_qc_kernel<<<(unsigned)blocks, warps * 32, 0, s>>>(raw, raw_pitch, m, n_fam, maskbits, nn,
                                                           min_maf, max_miss, vr_flag, min_mac_vr,
-                                                          is_var_ratio, out);
+                                                          max_mac_vr, is_var_ratio, out);
 }
 
 // ----------------------------------------------------------------------------
@@ -108,7 +118,7 @@ __global__ void repack_gather_kernel(const uint8_t* __restrict__ raw, int64_t ra
   if (byte >= out_pitch) return;
   const int64_t src = src_marker[j];
   const uint8_t* row = raw + src * raw_pitch;
-  const uint32_t fcode = pack_code_of(qc[src].fill);
+  const uint32_t fcode = qc ? pack_code_of(qc[src].fill) : 1u;  // no qc: missing calls stay 01
   uint32_t v = 0;
 #pragma unroll
   for (int t = 0; t < 4; ++t) {
@@ -134,7 +144,7 @@ __global__ void repack_identity_kernel(const uint8_t* __restrict__ raw, int64_t 
   if (w >= nwords) return;
   const int64_t src = src_marker[j];
   const uint32_t* row = reinterpret_cast<const uint32_t*>(raw + src * raw_pitch);
-  const uint32_t fcode = pack_code_of(qc[src].fill);
+  const uint32_t fcode = qc ? pack_code_of(qc[src].fill) : 1u;  // no qc: missing calls stay 01
   uint32_t x = row[w];
   // valid-sample mask of this word (bits of both halves of each field)
   const int64_t s0 = w * 16;

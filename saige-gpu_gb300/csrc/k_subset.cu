@@ -1,0 +1,341 @@
+// Subset-exact GRM.V: K_S v for a phenotype whose sample subset S has its own allele frequencies.
+//
+// The reference rebuilds the genotype object for every phenotype's samples (setgeno over
+// subSampleInGeno / indicatorGenoSamplesWithPheno, src/SAIGE/src/SAIGE_fitGLMM_fast.cpp:376-385,
+// 436-495 -- "FIT.cpp" below): allele frequency p', integer fill round(2 p'_nonmissing), QC and
+// 1/sd' are those of S, so K_S = Z'_S Z'_S^T / M' with z'_im = (g'_im - 2p'_m) / sd'_m is not the
+// cohort GRM restricted to S.  This engine applies K_S without forming it, through the cohort's
+// genotype values G (0/1/2, the cohort fill in missing calls), stored twice in BF16 (exact):
+//
+//   v_c = v - mean_S(v)                 (K_S 1_S = 0, so centring changes nothing but rounding)
+//   T   = G^T v_c                       (GEMM 1, marker-major G, two BF16 products of v_c's halves)
+//   T  += dF^T v_c                      (missing calls of markers whose subset fill differs)
+//   T'  = d' .* T,  d'_m = 1/sd'_m^2 for S's GRM markers, 0 otherwise
+//   U   = G T'                          (GEMM 2, sample-major G, two BF16 products of T''s halves)
+//   K_S v = (U + dF T' - (2p')^T T') / M'   on S
+//
+// Every kernel below reduces in a fixed order, so a column's product does not depend on which
+// other columns share the step.
+#include "sg_internal.h"
+#include <cuda_bf16.h>
+
+namespace sg {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kChunk = 2048;  // vector elements per block of the column reductions
+
+__device__ __forceinline__ int field_geno(uint32_t f) { return 2 - (int)((f & 1u) + (f >> 1)); }
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+  __syncthreads();
+  return s;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------------- set-up
+// G in both layouts from the cohort's packed codes (missing calls kept as 01): block = 64 markers x
+// 128 samples staged through shared memory, written coalesced along samples (marker-major G_mm,
+// mg x np) and along markers (sample-major G_sm, np x mg).  Missing calls take the cohort fill;
+// rows and columns past m and nn are zero.
+__global__ void gbuild_kernel(const uint8_t* __restrict__ codes, int64_t pitch, const int32_t* __restrict__ fill,
+                              int64_t m, int64_t nn, int64_t mg, int64_t np, __nv_bfloat16* __restrict__ Gmm,
+                              __nv_bfloat16* __restrict__ Gsm) {
+  __shared__ uint8_t sval[64][128 + 2];
+  const int64_t m0 = (int64_t)blockIdx.x * 64;
+  const int64_t s0 = (int64_t)blockIdx.y * 128;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < 64 * 128; e += blockDim.x) {
+    const int mm = e >> 7, s = e & 127;
+    const int64_t mk = m0 + mm, smp = s0 + s;
+    uint8_t g = 0;
+    if (mk < m && smp < nn) {
+      const uint32_t f = (codes[mk * pitch + (smp >> 2)] >> (2 * (smp & 3))) & 3u;
+      g = (uint8_t)(f == 1u ? fill[mk] : field_geno(f));
+    }
+    sval[mm][s] = g;
+    Gmm[mk * np + smp] = __float2bfloat16_rn((float)g);
+  }
+  __syncthreads();
+  for (int e = tid; e < 64 * 128; e += blockDim.x) {
+    const int mm = e & 63, s = e >> 6;
+    Gsm[(s0 + s) * mg + m0 + mm] = __float2bfloat16_rn((float)sval[mm][s]);
+  }
+}
+
+void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int64_t m, int64_t nn,
+                   int64_t mg, int64_t np, void* Gmm, void* Gsm, cudaStream_t s) {
+  dim3 grid((unsigned)(mg / 64), (unsigned)(np / 128));
+  gbuild_kernel<<<grid, kThreads, 0, s>>>(codes, pitch, fill, m, nn, mg, np, static_cast<__nv_bfloat16*>(Gmm),
+                                          static_cast<__nv_bfloat16*>(Gsm));
+}
+
+// Bit map of a slot's fill-changed markers: word w of sample i has bit b set when marker
+// flips[32 w + b] is missing at sample i and i is in the subset (mask).
+__global__ void subset_bitmap_kernel(const uint8_t* __restrict__ codes, int64_t pitch,
+                                     const int32_t* __restrict__ flips, int nflip, int W,
+                                     const uint8_t* __restrict__ mask, int64_t nn, int64_t np,
+                                     uint32_t* __restrict__ bits) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int w = blockIdx.y;
+  if (i >= np) return;
+  uint32_t word = 0;
+  if (i < nn && (!mask || mask[i])) {
+    for (int b = 0; b < 32; ++b) {
+      const int k = 32 * w + b;
+      if (k >= nflip) break;
+      const int64_t mk = flips[k];
+      const uint32_t f = (codes[mk * pitch + (i >> 2)] >> (2 * (i & 3))) & 3u;
+      if (f == 1u) word |= 1u << b;
+    }
+  }
+  bits[i * W + w] = word;
+}
+
+void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* flips, int nflip, int W,
+                          const uint8_t* mask, int64_t nn, int64_t np, uint32_t* bits, cudaStream_t s) {
+  if (W == 0) return;
+  dim3 grid((unsigned)((np + kThreads - 1) / kThreads), (unsigned)W);
+  subset_bitmap_kernel<<<grid, kThreads, 0, s>>>(codes, pitch, flips, nflip, W, mask, nn, np, bits);
+}
+
+// Diagonal of M' K_S (sum over the subset's GRM markers of z'^2, the Jacobi preconditioner's
+// Get_Diagof_StdGeno, FIT.cpp:665-704): one thread per sample, lut4[4 m + code] = d'_m (g - 2p'_m)^2
+// per packed code (the missing code carries the subset fill); FP32 over 256 markers, then FP64.
+__global__ void subset_diag_kernel(const uint8_t* __restrict__ codes, int64_t pitch, const float4* __restrict__ lut4,
+                                   int64_t m, int64_t nn, int64_t np, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  if (i >= nn) {
+    out[i] = 0.0;
+    return;
+  }
+  const int64_t byte = i >> 2;
+  const int sh = 2 * (int)(i & 3);
+  double tot = 0.0;
+  for (int64_t m0 = 0; m0 < m; m0 += 256) {
+    const int64_t m1 = m0 + 256 < m ? m0 + 256 : m;
+    float acc = 0.0f;
+    for (int64_t mk = m0; mk < m1; ++mk) {
+      const uint32_t f = (__ldg(codes + mk * pitch + byte) >> sh) & 3u;
+      const float4 l = __ldg(lut4 + mk);
+      acc += f == 0u ? l.x : f == 1u ? l.y : f == 2u ? l.z : l.w;
+    }
+    tot += (double)acc;
+  }
+  out[i] = tot;
+}
+
+void launch_subset_diag(const uint8_t* codes, int64_t pitch, const float* lut4, int64_t m, int64_t nn, int64_t np,
+                        double* out, cudaStream_t s) {
+  subset_diag_kernel<<<(unsigned)((np + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+      codes, pitch, reinterpret_cast<const float4*>(lut4), m, nn, np, out);
+}
+
+// ----------------------------------------------------------------------------------- per step
+// Column sums over the subset (rows outside S are zero in P): block partials, kChunk rows each.
+__global__ void subset_colsum_kernel(const float* __restrict__ Pf, int64_t np, const int32_t* __restrict__ cols,
+                                     double* __restrict__ part, int nblk) {
+  __shared__ double sh[kThreads / 32];
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  double v = 0.0;
+  if (col >= 0) {
+    const float* p = Pf + (int64_t)col * np;
+    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) v += (double)p[i];
+  }
+  v = block_sum(v, sh);
+  if (threadIdx.x == 0) part[j * nblk + blockIdx.x] = v;
+}
+
+// v_c = P - mean_S(P) on the subset (0 elsewhere and for padding columns), as BF16 high + low
+// halves of the compact block (column j at row j * np).
+__global__ void subset_center_split_kernel(const float* __restrict__ Pf, int64_t np, const int32_t* __restrict__ cols,
+                                           const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
+                                           const double* __restrict__ winv, const double* __restrict__ part,
+                                           int nblk, __nv_bfloat16* __restrict__ Vh, __nv_bfloat16* __restrict__ Vl) {
+  __shared__ float s_mu;
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  int slot = 0;
+  if (col >= 0) slot = st[col].pheno;
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    if (col >= 0)
+      for (int b = 0; b < nblk; ++b) sum += part[j * nblk + b];
+    s_mu = col >= 0 ? (float)(sum / slots[slot].ns) : 0.0f;
+  }
+  __syncthreads();
+  const float mu = s_mu;
+  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
+    float v = 0.0f;
+    if (col >= 0 && winv[(int64_t)slot * np + i] != 0.0) v = Pf[(int64_t)col * np + i] - mu;
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    Vh[j * np + i] = h;
+    Vl[j * np + i] = __float2bfloat16_rn(v - __bfloat162float(h));
+  }
+}
+
+// T[j, flips[k]] += dfill[k] * sum over the subset samples missing at that marker of v_c[j, i]:
+// block (j, w) scans every sample's bit-map word w and accumulates the (at most 32) markers of that
+// word in registers, then reduces them over the block in a fixed order.
+__global__ void subset_flip_t_kernel(const __nv_bfloat16* __restrict__ Vh, const __nv_bfloat16* __restrict__ Vl,
+                                     int64_t np, int64_t nn, const int32_t* __restrict__ cols,
+                                     const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
+                                     float* __restrict__ T, int64_t mg) {
+  __shared__ float red[kThreads / 32][32];
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  if (col < 0) return;
+  const SubsetSlot sl = slots[st[col].pheno];
+  const int w = blockIdx.x;
+  if (w >= sl.W) return;
+  float acc[32];
+#pragma unroll
+  for (int b = 0; b < 32; ++b) acc[b] = 0.0f;
+  for (int64_t i = threadIdx.x; i < nn; i += kThreads) {
+    const uint32_t word = sl.bits[i * sl.W + w];
+    if (word == 0u) continue;
+    const float v = __bfloat162float(Vh[j * np + i]) + __bfloat162float(Vl[j * np + i]);
+#pragma unroll
+    for (int b = 0; b < 32; ++b)
+      if ((word >> b) & 1u) acc[b] += v;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int b = 0; b < 32; ++b) {
+    float x = acc[b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == b) red[warp][b] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int b = threadIdx.x;
+    const int k = 32 * w + b;
+    if (k < sl.nflip) {
+      float s = 0.0f;
+      for (int q = 0; q < kThreads / 32; ++q) s += red[q][b];
+      T[j * mg + sl.flips[k]] += sl.dfill[k] * s;
+    }
+  }
+}
+
+// T' = d' .* T as BF16 high + low halves (compact block, column j at row j * mg), and the block
+// partials of (2p')^T T' in FP64 (from the halves GEMM 2 multiplies).  Padding columns get zeros.
+__global__ void subset_scale_split_kernel(const float* __restrict__ T, int64_t mg, const int32_t* __restrict__ cols,
+                                          const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
+                                          __nv_bfloat16* __restrict__ Th, __nv_bfloat16* __restrict__ Tl,
+                                          double* __restrict__ part, int nblk) {
+  __shared__ double sh[kThreads / 32];
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  const int64_t m0 = (int64_t)blockIdx.x * kChunk;
+  const SubsetSlot* sl = col >= 0 ? &slots[st[col].pheno] : nullptr;
+  double c = 0.0;
+  for (int64_t mk = m0 + threadIdx.x; mk < m0 + kChunk && mk < mg; mk += kThreads) {
+    float t = 0.0f;
+    if (sl) t = sl->dprime[mk] * T[j * mg + mk];
+    const __nv_bfloat16 h = __float2bfloat16_rn(t);
+    const __nv_bfloat16 l = __float2bfloat16_rn(t - __bfloat162float(h));
+    Th[j * mg + mk] = h;
+    Tl[j * mg + mk] = l;
+    if (sl) c += (double)sl->p2[mk] * ((double)__bfloat162float(h) + (double)__bfloat162float(l));
+  }
+  c = block_sum(c, sh);
+  if (threadIdx.x == 0) part[j * nblk + blockIdx.x] = c;
+}
+
+// K_S v on the subset: (U + dF T' - (2p')^T T') / M', written to column cols[j] of Y (zero outside
+// the subset); padding columns are skipped.
+__global__ void subset_finalize_kernel(const float* __restrict__ U, int64_t np, int64_t nn,
+                                       const int32_t* __restrict__ cols, const ColState* __restrict__ st,
+                                       const SubsetSlot* __restrict__ slots, const __nv_bfloat16* __restrict__ Th,
+                                       const __nv_bfloat16* __restrict__ Tl, int64_t mg,
+                                       const double* __restrict__ part, int nblk, const double* __restrict__ winv,
+                                       float* __restrict__ Yf) {
+  __shared__ double s_c;
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  if (col < 0) return;
+  const int slot = st[col].pheno;
+  const SubsetSlot sl = slots[slot];
+  if (threadIdx.x == 0) {
+    double c = 0.0;
+    for (int b = 0; b < nblk; ++b) c += part[j * nblk + b];
+    s_c = c;
+  }
+  __syncthreads();
+  const double c = s_c;
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
+    float y = 0.0f;
+    if (i < nn && winv[(int64_t)slot * np + i] != 0.0) {
+      double du = 0.0;
+      for (int w = 0; w < sl.W; ++w) {
+        uint32_t word = sl.bits[i * sl.W + w];
+        while (word) {
+          const int b = __ffs(word) - 1;
+          word &= word - 1u;
+          const int k = 32 * w + b;
+          const int64_t mk = sl.flips[k];
+          du += (double)sl.dfill[k] *
+                ((double)__bfloat162float(Th[j * mg + mk]) + (double)__bfloat162float(Tl[j * mg + mk]));
+        }
+      }
+      y = (float)(((double)U[j * np + i] - c + du) * sl.inv_m);
+    }
+    Yf[(int64_t)col * np + i] = y;
+  }
+}
+
+int subset_nblk(int64_t n) { return (int)((n + kChunk - 1) / kChunk); }
+
+void launch_subset_prepare(const float* Pf, int64_t np, const int32_t* cols, int64_t ncols, const ColState* st,
+                           const SubsetSlot* slots, const double* winv, double* part, void* Vh, void* Vl,
+                           cudaStream_t s) {
+  const int nblk = subset_nblk(np);
+  dim3 grid((unsigned)nblk, (unsigned)ncols);
+  subset_colsum_kernel<<<grid, kThreads, 0, s>>>(Pf, np, cols, part, nblk);
+  subset_center_split_kernel<<<grid, kThreads, 0, s>>>(Pf, np, cols, st, slots, winv, part, nblk,
+                                                       static_cast<__nv_bfloat16*>(Vh),
+                                                       static_cast<__nv_bfloat16*>(Vl));
+}
+
+void launch_subset_scale(const void* Vh, const void* Vl, int64_t np, int64_t nn, const int32_t* cols, int64_t ncols,
+                         const ColState* st, const SubsetSlot* slots, int max_w, float* T, int64_t mg, void* Th,
+                         void* Tl, double* part, cudaStream_t s) {
+  if (max_w > 0) {
+    dim3 g1((unsigned)max_w, (unsigned)ncols);
+    subset_flip_t_kernel<<<g1, kThreads, 0, s>>>(static_cast<const __nv_bfloat16*>(Vh),
+                                                 static_cast<const __nv_bfloat16*>(Vl), np, nn, cols, st, slots, T,
+                                                 mg);
+  }
+  const int nblk = subset_nblk(mg);
+  dim3 g2((unsigned)nblk, (unsigned)ncols);
+  subset_scale_split_kernel<<<g2, kThreads, 0, s>>>(T, mg, cols, st, slots, static_cast<__nv_bfloat16*>(Th),
+                                                    static_cast<__nv_bfloat16*>(Tl), part, nblk);
+}
+
+void launch_subset_finalize(const float* U, int64_t np, int64_t nn, const int32_t* cols, int64_t ncols,
+                            const ColState* st, const SubsetSlot* slots, const void* Th, const void* Tl, int64_t mg,
+                            const double* part, const double* winv, float* Yf, cudaStream_t s) {
+  dim3 grid((unsigned)subset_nblk(np), (unsigned)ncols);
+  subset_finalize_kernel<<<grid, kThreads, 0, s>>>(U, np, nn, cols, st, slots, static_cast<const __nv_bfloat16*>(Th),
+                                                   static_cast<const __nv_bfloat16*>(Tl), mg, part, subset_nblk(mg),
+                                                   winv, Yf);
+}
+
+}  // namespace sg

@@ -26,10 +26,12 @@
 // to -3e-7..-8e-7 relative, and a binary fit's tau from 1.1% off to 3e-5; the
 // launches are 3% (1024 columns) to 13% (384 columns) slower, the SYRK 8%.
 // (256-byte chunks: bias below 4.3e-7, launches 8-19% slower.)
-// Optional thread-block clusters share B tiles by TMA multicast (see the
-// kernel's kC parameter); MMAs stay cta_group::1.  Every mbarrier wait is bounded by
-// a global-timer budget; on expiry the kernel records an error code, skips
-// the remaining work, frees its TMEM and returns.
+// Optional CTA pairs (2-CTA clusters, tcgen05 cta_group::2) compute 256-row tiles: each CTA loads
+// its own operand rows with plain TMA loads, so a pair reads half the B bytes per SM (see the
+// kernel's kPair parameter).  The drain length is a launch argument (option SG_TC_DRAIN_BYTES,
+// 512 bytes by default).  Every mbarrier wait is bounded by a global-timer budget; on expiry the
+// kernel records an error code, skips the remaining work, waits for the MMAs it issued, frees its
+// TMEM and returns.
 //
 // Uses:
 //   * SYRK  K = scale * Z Z^T (Z bf16, kind::f16): lower-triangle tiles only,
@@ -53,6 +55,8 @@ namespace sg {
 namespace {
 
 constexpr int kTileM = 128;
+// products per K step of the GEMM kernel (see tc_gemm_kernel)
+constexpr int kOne = 0, kSplitB = 1, kSplit3 = 2, kSplit4 = 3;
 constexpr int kRowBytes = 128;                 // one SWIZZLE_128B atom row
 constexpr int kATileBytes = kTileM * kRowBytes;  // 16 KB
 constexpr unsigned long long kWaitBudgetNs = 4000000000ull;  // 4 s per wait
@@ -61,12 +65,6 @@ constexpr int kDrainWarps = 8;
 constexpr int kProducerWarp = 8;
 constexpr int kMmaWarp = 9;
 constexpr int kGemmThreads = 320;
-// bytes of K per row that one TMEM accumulator takes before it is drained into registers (a
-// multiple of 128; the bias left by the toward-zero TMEM rounding grows linearly with it)
-#ifndef SG_DRAIN_BYTES
-#define SG_DRAIN_BYTES 512
-#endif
-constexpr int kDrainBytes = SG_DRAIN_BYTES;
 
 __device__ int g_tc_error = 0;
 
@@ -149,6 +147,15 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, 
   }
 }
 
+// Bounded wait at teardown: the MMAs a CTA issued complete within microseconds once issued (their
+// operands are already in shared memory), so this wait ignores the abort flag and gives up after
+// 1 s without recording anything.
+__device__ __forceinline__ void mbar_wait_teardown(uint64_t* bar, uint32_t parity) {
+  const unsigned long long t0 = gtimer();
+  while (!mbar_try_wait(bar, parity))
+    if (gtimer() - t0 > 1000000000ull) return;
+}
+
 // Self-test of the bounded wait: waits on an mbarrier that nothing arrives at, with a short budget,
 // and reports through the same error flag the GEMM kernels use.
 __global__ void wait_selftest_kernel(unsigned long long budget_ns, int* waited_out) {
@@ -204,19 +211,29 @@ __device__ __forceinline__ uint64_t smem_desc_kmajor(uint32_t addr) {
 
 // Instruction descriptor: FP32 accumulator, A/B format (1 = BF16 for
 // kind::f16, 2 = TF32 for kind::tf32), both K-major, N >> 3 at bit 17,
-// M >> 4 at bit 24.
-__host__ __device__ constexpr uint32_t make_idesc(uint32_t fmt, int n) {
+// M >> 4 at bit 24 (M = 128 for one CTA, 256 for a CTA pair).
+__host__ __device__ constexpr uint32_t make_idesc(uint32_t fmt, int m, int n) {
   return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(n >> 3) << 17) |
-         ((uint32_t)(kTileM >> 4) << 24);
+         ((uint32_t)(m >> 4) << 24);
 }
 
-template <bool kTF32>
+template <bool kTF32, bool kPair>
 __device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
                                      uint32_t accumulate) {
-  if constexpr (kTF32) {
+  if constexpr (kTF32 && kPair) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+  } else if constexpr (kTF32) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+  } else if constexpr (kPair) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}"
         ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
   } else {
     asm volatile(
@@ -224,18 +241,6 @@ __device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, ui
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
         ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
   }
-}
-
-// Multicast variant: the box lands at the same shared-memory offset in every CTA of ``mask``
-// and completes transaction bytes on the mbarrier at the same offset in each of them.
-__device__ __forceinline__ void tma_load_2d_mcast(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                                  int32_t x, int32_t y, uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-      " [%0], [%1, {%4, %5}], [%2], %3;"
-      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "h"(mask),
-        "r"(x), "r"(y)
-      : "memory");
 }
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -248,16 +253,37 @@ __device__ __forceinline__ void cluster_sync() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-// Arrive once on the mbarrier at this offset in every CTA of ``mask`` when the prior MMAs complete.
-__device__ __forceinline__ void umma_commit_mcast(uint64_t* bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
-      ::"r"(smem_u32(bar)), "h"(mask) : "memory");
+// Address of the same shared-memory location in CTA ``rank`` of the cluster.
+__device__ __forceinline__ uint32_t cluster_addr(const void* p, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
 }
 
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-               ::"r"(smem_u32(bar)) : "memory");
+// Arrive once on an mbarrier given by its cluster address (this CTA's or the peer's).
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
+}
+
+// CTA-pair load: the box lands in this CTA's shared memory and completes its transaction bytes on
+// the mbarrier at cluster address ``bar_cluster``, which may sit in the pair's other CTA.
+__device__ __forceinline__ void tma_load_2d_pair(void* dst, const CUtensorMap* map, uint32_t bar_cluster,
+                                                 int32_t x, int32_t y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar_cluster), "r"(x), "r"(y)
+      : "memory");
+}
+
+template <bool kPair>
+__device__ __forceinline__ void umma_commit(uint32_t bar_cluster) {
+  if constexpr (kPair)
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(bar_cluster) : "memory");
+  else
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(bar_cluster) : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
@@ -275,40 +301,46 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 }
 
 struct TileCoord {
-  int32_t bm, bn;  // row block (128 rows) and column block (BN cols)
+  int32_t bm, bn;  // row block (128 rows; the first of two for a CTA pair) and column block (BN cols)
 };
 
-// kSplit: A = [Ah | Al], B = [Bh | Bl] (second maps); accumulates Ah Bh + Ah Bl + Al Bh (+ Al Bl with kLoLo).
-// kC > 1: the kC CTAs of a cluster own consecutive row blocks of the same column block and share
-// its B tile -- CTA r loads rows [r*BN/kC, (r+1)*BN/kC) of it and multicasts them to all kC, which
-// cuts the L2->SM operand traffic of B by kC.  Each stage is then refilled only when every CTA of
-// the cluster has consumed it (the empty barrier counts kC multicast MMA commits).
-// Rows >= nrows of a tile (a padding row block that completes the last cluster) are not stored.
-// RB: bytes of one operand row's K slice per pipeline stage -- 128 (SWIZZLE_128B, the TF32
-// kernels and the SYRK) or 64 (SWIZZLE_64B: half the bytes per stage, twice the stages in the
-// same shared memory, for the split-BF16 GRM.V, whose four operand tiles per stage left it with
-// only two stages of 128-byte slices).
-template <bool kTF32, int BN, int S, bool kSplit, int kC, int RB = 128, bool kLoLo = false>
+// kForm: the products accumulated per K step (operand halves come from the second maps):
+//   kOne    A B                          (A and B loaded)
+//   kSplitB A Bh + A Bl                  (A exact in the operand type, B as high + low halves)
+//   kSplit3 Ah Bh + Ah Bl + Al Bh        (both as halves, the low x low term dropped)
+//   kSplit4 Ah Bh + Ah Bl + Al Bh + Al Bl
+// kPair: two CTAs of a 2-CTA cluster compute one 256 x BN tile with tcgen05.mma.cta_group::2, issued
+// by the even CTA (the leader).  Each CTA loads its own 128 rows of A and half of the B tile
+// (BN / 2 rows) into the same shared-memory offsets with plain TMA loads; the loads of both signal
+// the leader's full barrier (cta_group::2 form of the load), the leader's MMA commits arrive on the
+// empty and accumulator barriers of each CTA (one commit addressed to each CTA), and each CTA drains
+// its own 128 accumulator rows from its own TMEM.  Per SM this halves the B operand bytes read from
+// L2 for the same tensor work.
+// drain_kb: pipeline stages per TMEM accumulator chunk (the drain length is drain_kb * RB bytes of
+// K per row).  Rows >= nrows of a tile (a padding row block) are not stored.
+// RB: bytes of one operand row's K slice per pipeline stage -- 128 (SWIZZLE_128B) or 64
+// (SWIZZLE_64B: half the bytes per stage, twice the stages in the same shared memory, for the
+// split-BF16 GRM.V, whose four operand tiles per stage left it with only two stages of 128-byte slices).
+template <bool kTF32, int BN, int S, int kForm, bool kPair, int RB = 128>
 __global__ void __launch_bounds__(kGemmThreads, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
-               const TileCoord* __restrict__ tiles, int num_kb, float* __restrict__ D, int64_t ldd,
-               float scale, int mode, int64_t nrows, const int32_t* __restrict__ colmap) {
+               const TileCoord* __restrict__ tiles, int num_kb, int drain_kb, float* __restrict__ D,
+               int64_t ldd, float scale, int mode, int64_t nrows, const int32_t* __restrict__ colmap) {
   static_assert(RB == 128 || RB == 64, "K slices of 128 or 64 bytes");
-  static_assert(kC == 1 || (BN / kC) % 8 == 0, "B slices must be whole 8-row swizzle atoms");
+  static_assert(!kPair || (BN / 2) % 8 == 0, "a CTA's half of the B tile is whole 8-row swizzle atoms");
   constexpr int kATile = kTileM * RB;
-  constexpr int kSliceRows = BN / kC;
-  constexpr int kSliceBytes = kSliceRows * RB;
-  constexpr int kBTileBytes = BN * RB;
-  constexpr int kStageBytes = (kATile + kBTileBytes) * (kSplit ? 2 : 1);
+  constexpr int kBRows = kPair ? BN / 2 : BN;  // rows of the B tile this CTA loads
+  constexpr int kBTileBytes = kBRows * RB;
+  constexpr int kStageBytes = kATile * (kForm >= kSplit3 ? 2 : 1) + kBTileBytes * (kForm >= kSplitB ? 2 : 1);
+  // stage layout: [A][B], then [B2] (kSplitB) or [A2][B2] (kSplit3, kSplit4)
+  constexpr int kOffB2 = kForm == kSplitB ? kATile + kBTileBytes : 2 * kATile + kBTileBytes;
   constexpr uint32_t kFmt = kTF32 ? 2u : 1u;
   constexpr int kKSteps = RB / 32;     // 32 bytes of K per MMA
   // two accumulators, each a power of two >= 32 columns wide
   constexpr uint32_t kAccCols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
   constexpr uint32_t kTmemCols = 2 * kAccCols;
-  constexpr uint32_t kIdesc = make_idesc(kFmt, BN);
-  static_assert(kDrainBytes % RB == 0 && kDrainBytes >= RB, "an accumulator covers whole pipeline stages");
-  constexpr int kDrainKB = kDrainBytes / RB;  // pipeline stages per accumulator
+  constexpr uint32_t kIdesc = make_idesc(kFmt, kPair ? 2 * kTileM : kTileM, BN);
   constexpr int kGroups = (BN + 31) / 32;     // 32-column groups of the tile
   constexpr int kHalfGroups = (kGroups + 1) / 2;
   static_assert(kDrainWarps == 8 && kGemmThreads == 32 * (kDrainWarps + 2),
@@ -320,77 +352,90 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * kStageBytes);
   uint64_t* empty = full + S;
   uint64_t* acc_full = empty + S;     // [2] the MMAs of an accumulator's chunk completed
-  uint64_t* acc_empty = acc_full + 2;  // [2] the drain warps read the accumulator
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  uint64_t* acc_empty = acc_full + 2;  // [2] the drain warps (of both CTAs of a pair) read the accumulator
+  uint64_t* mma_done = acc_empty + 2;  // every MMA this CTA issued has completed (teardown)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const TileCoord tc = tiles[blockIdx.x];
+  const uint32_t crank = kPair ? cluster_rank() : 0u;
+  const bool leader = crank == 0;
+  const TileCoord tc = tiles[kPair ? (blockIdx.x >> 1) : blockIdx.x];
+  const int32_t row_block = tc.bm + (int32_t)crank;  // this CTA's 128 rows
 
-  const uint32_t crank = kC > 1 ? cluster_rank() : 0u;
-  constexpr uint16_t kMask = (uint16_t)((1u << kC) - 1u);
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], kC);
+      mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], kDrainWarps);
+      mbar_init(&acc_empty[b], kDrainWarps * (kPair ? 2 : 1));
     }
+    mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if (warp == kMmaWarp) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 ::"r"(smem_u32(tmem_slot)), "r"(kTmemCols) : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    // a pair allocates collectively: one warp of each CTA, same columns, same address in both
+    if constexpr (kPair) {
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;"
+                   ::"r"(smem_u32(tmem_slot)), "r"(kTmemCols) : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+    } else {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                   ::"r"(smem_u32(tmem_slot)), "r"(kTmemCols) : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if constexpr (kC > 1) cluster_sync();  // every CTA's barriers exist before any peer multicasts
+  if constexpr (kPair) cluster_sync();  // both CTAs' barriers exist before either signals the other
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem_base = *tmem_slot;
-  const int nchunks = (num_kb + kDrainKB - 1) / kDrainKB;
+  const int nchunks = (num_kb + drain_kb - 1) / drain_kb;
 
   if (warp == kProducerWarp) {
     if (lane == 0) {
-      // ---------------- TMA producer
-      const int32_t ya = tc.bm * kTileM, yb = tc.bn * BN;
+      // ---------------- TMA producer (each CTA of a pair loads its own operand rows)
+      const int32_t ya = row_block * kTileM, yb = tc.bn * BN + (int32_t)crank * kBRows;
       for (int kb = 0; kb < num_kb; ++kb) {
         const int s = kb % S;
         const uint32_t ph = (uint32_t)(kb / S) & 1u;
         if (!mbar_wait(&empty[s], ph ^ 1u, 1, abort_flag)) break;
         uint8_t* st = smem + s * kStageBytes;
-        mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
         const int32_t x = kb * (RB / (kTF32 ? 4 : 2));
-        tma_load_2d(st, &mapA, &full[s], x, ya);
-        if constexpr (kC == 1) {
-          tma_load_2d(st + kATile, &mapB, &full[s], x, yb);
+        if constexpr (kPair) {
+          // the leader's full barrier counts both CTAs' bytes; only the leader arrives on it
+          const uint32_t fb = cluster_addr(&full[s], 0);
+          if (leader) mbar_expect_tx(&full[s], 2u * (uint32_t)kStageBytes);
+          tma_load_2d_pair(st, &mapA, fb, x, ya);
+          tma_load_2d_pair(st + kATile, &mapB, fb, x, yb);
+          if constexpr (kForm >= kSplit3) tma_load_2d_pair(st + kATile + kBTileBytes, &mapA2, fb, x, ya);
+          if constexpr (kForm >= kSplitB) tma_load_2d_pair(st + kOffB2, &mapB2, fb, x, yb);
         } else {
-          tma_load_2d_mcast(st + kATile + crank * kSliceBytes, &mapB, &full[s], x,
-                            yb + (int32_t)crank * kSliceRows, kMask);
-        }
-        if constexpr (kSplit) {
-          tma_load_2d(st + kATile + kBTileBytes, &mapA2, &full[s], x, ya);
-          if constexpr (kC == 1) {
-            tma_load_2d(st + 2 * kATile + kBTileBytes, &mapB2, &full[s], x, yb);
-          } else {
-            tma_load_2d_mcast(st + 2 * kATile + kBTileBytes + crank * kSliceBytes, &mapB2, &full[s], x,
-                              yb + (int32_t)crank * kSliceRows, kMask);
-          }
+          mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
+          tma_load_2d(st, &mapA, &full[s], x, ya);
+          tma_load_2d(st + kATile, &mapB, &full[s], x, yb);
+          if constexpr (kForm >= kSplit3) tma_load_2d(st + kATile + kBTileBytes, &mapA2, &full[s], x, ya);
+          if constexpr (kForm >= kSplitB) tma_load_2d(st + kOffB2, &mapB2, &full[s], x, yb);
         }
       }
     }
   } else if (warp == kMmaWarp) {
-    if (lane == 0) {
-      // ---------------- MMA issuer: chunk ch of kDrainKB stages goes to accumulator ch % 2, which is
+    if (lane == 0 && leader) {
+      // ---------------- MMA issuer: chunk ch of drain_kb stages goes to accumulator ch % 2, which is
       // reused once the drain warps have read it (two chunks earlier)
+      uint32_t empty_peer = 0, accf_peer = 0;
+      if constexpr (kPair) {
+        empty_peer = cluster_addr(empty, 1);
+        accf_peer = cluster_addr(acc_full, 1);
+      }
       for (int kb = 0; kb < num_kb; ++kb) {
-        const int ch = kb / kDrainKB;
-        const int kin = kb - ch * kDrainKB;
+        const int ch = kb / drain_kb;
+        const int kin = kb - ch * drain_kb;
         const int ab = ch & 1;
         if (kin == 0) {
           if (!mbar_wait(&acc_empty[ab], ((uint32_t)(ch >> 1) & 1u) ^ 1u, 5, abort_flag)) break;
@@ -406,26 +451,37 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 #pragma unroll
         for (int k = 0; k < kKSteps; ++k) {
           const uint32_t acc = (kin > 0 || k > 0) ? 1u : 0u;
-          umma<kTF32>(dacc, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, acc);
-          if constexpr (kSplit) {
-            const uint32_t a1 = b0 + kBTileBytes;      // Al
-            const uint32_t b1 = a1 + kATile;           // Bl
-            umma<kTF32>(dacc, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
-            umma<kTF32>(dacc, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, 1u);
-            if constexpr (kLoLo)
-              umma<kTF32>(dacc, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
+          umma<kTF32, kPair>(dacc, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, acc);
+          if constexpr (kForm >= kSplitB) {
+            const uint32_t b1 = a0 + kOffB2;            // Bl
+            umma<kTF32, kPair>(dacc, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
+            if constexpr (kForm >= kSplit3) {
+              const uint32_t a1 = b0 + kBTileBytes;     // Al
+              umma<kTF32, kPair>(dacc, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, 1u);
+              if constexpr (kForm == kSplit4)
+                umma<kTF32, kPair>(dacc, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
+            }
           }
         }
-        // stage reusable once these MMAs have read it (in every CTA of the cluster)
-        if constexpr (kC == 1) umma_commit(&empty[s]);
-        else umma_commit_mcast(&empty[s], kMask);
-        if (kin == kDrainKB - 1 || kb == num_kb - 1) umma_commit(&acc_full[ab]);
+        // the stage is reusable once these MMAs have read it (in both CTAs of a pair)
+        umma_commit<kPair>(smem_u32(&empty[s]));
+        if constexpr (kPair) umma_commit<kPair>(empty_peer + (uint32_t)s * 8u);
+        if (kin == drain_kb - 1 || kb == num_kb - 1) {
+          umma_commit<kPair>(smem_u32(&acc_full[ab]));
+          if constexpr (kPair) umma_commit<kPair>(accf_peer + (uint32_t)ab * 8u);
+        }
       }
+      // every MMA issued above has completed before the TMEM (and a pair's shared memory) is
+      // released, also when a wait gave up and the loop stopped early
+      umma_commit<kPair>(smem_u32(mma_done));
+      mbar_wait_teardown(mma_done, 0u);
     }
   } else {
     // ---------------- drain warps 0-7, then the epilogue
     const int quad = warp & 3, half = warp >> 2;
     const uint32_t tlane = (uint32_t)(quad * 32) << 16;
+    uint32_t acce_leader = 0;
+    if constexpr (kPair) acce_leader = cluster_addr(acc_empty, 0);
     float sum[kHalfGroups][32];
 #pragma unroll
     for (int g = 0; g < kHalfGroups; ++g)
@@ -453,10 +509,13 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[ab]);
+      if (lane == 0) {
+        if constexpr (kPair) mbar_arrive_cluster(acce_leader + (uint32_t)ab * 8u);
+        else mbar_arrive(&acc_empty[ab]);
+      }
     }
-    if (go && (int64_t)tc.bm * kTileM < nrows) {
-      const int64_t r = (int64_t)tc.bm * kTileM + quad * 32 + lane;
+    if (go && (int64_t)row_block * kTileM < nrows) {
+      const int64_t r = (int64_t)row_block * kTileM + quad * 32 + lane;
 #pragma unroll
       for (int g = 0; g < kHalfGroups; ++g) {
         const int grp = 2 * g + half;
@@ -493,11 +552,17 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   __syncwarp();  // the producer and MMA warps reconverge after their single-lane loops
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  // no CTA leaves while a peer may still multicast into its shared memory or arrive on its barriers
-  if constexpr (kC > 1) cluster_sync();
+  // a pair: neither CTA leaves while the leader's MMAs may still read the other's shared memory or
+  // either may still arrive on the other's barriers
+  if constexpr (kPair) cluster_sync();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == kMmaWarp) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kTmemCols)
-                 : "memory");
+    if constexpr (kPair)
+      asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kTmemCols)
+                   : "memory");
+    else
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kTmemCols)
+                   : "memory");
   }
 }
 
@@ -533,35 +598,39 @@ bool make_map(CUtensorMap* m, const void* base, bool f32, uint64_t inner, uint64
   return r == CUDA_SUCCESS;
 }
 
-template <bool kTF32, int BN, int S, bool kSplit, int RB = kRowBytes>
+template <int BN, int S, int kForm, bool kPair, int RB = kRowBytes>
 constexpr size_t smem_bytes() {
-  return (size_t)S * (kTileM * RB + BN * RB) * (kSplit ? 2 : 1) + 1024 + 256;
+  return (size_t)S * ((size_t)kTileM * RB * (kForm >= kSplit3 ? 2 : 1) +
+                      (size_t)(kPair ? BN / 2 : BN) * RB * (kForm >= kSplitB ? 2 : 1)) +
+         1024 + 256;
 }
 
-template <bool kTF32, int BN, int S, bool kSplit, int kC = 1, int RB = kRowBytes, bool kLoLo = false>
+// Launches ntiles output tiles (ntiles CTAs, or ntiles 2-CTA clusters for a CTA pair).
+template <bool kTF32, int BN, int S, int kForm, bool kPair = false, int RB = kRowBytes>
 cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
-                   const CUtensorMap& b2, const TileCoord* tiles, int ntiles, int num_kb, float* D,
-                   int64_t ldd, float scale, int mode, cudaStream_t s, int64_t nrows,
+                   const CUtensorMap& b2, const TileCoord* tiles, int ntiles, int num_kb, int drain_kb,
+                   float* D, int64_t ldd, float scale, int mode, cudaStream_t s, int64_t nrows,
                    const int32_t* colmap = nullptr) {
-  auto k = tc_gemm_kernel<kTF32, BN, S, kSplit, kC, RB, kLoLo>;
-  constexpr size_t sm = smem_bytes<kTF32, BN, S, kSplit, RB>();
+  auto k = tc_gemm_kernel<kTF32, BN, S, kForm, kPair, RB>;
+  constexpr size_t sm = smem_bytes<BN, S, kForm, kPair, RB>();
   static_assert(sm <= 232448, "stage ring exceeds the 227 KB of dynamic shared memory per CTA");
+  static_assert(2 * S + 5 <= 31, "barriers, TMEM slot and abort flag fit the 256-byte tail");
+  if (drain_kb < 1) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  if (ntiles % kC != 0) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)ntiles);
+  cfg.gridDim = dim3((unsigned)ntiles * (kPair ? 2u : 1u));
   cfg.blockDim = dim3(kGemmThreads);
   cfg.dynamicSmemBytes = sm;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kC;
+  attr[0].val.clusterDim.x = 2;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = kC > 1 ? 1 : 0;
-  e = cudaLaunchKernelEx(&cfg, k, a, b, a2, b2, tiles, num_kb, D, ldd, scale, mode, nrows, colmap);
+  cfg.numAttrs = kPair ? 1 : 0;
+  e = cudaLaunchKernelEx(&cfg, k, a, b, a2, b2, tiles, num_kb, drain_kb, D, ldd, scale, mode, nrows, colmap);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
@@ -719,75 +788,138 @@ bool tc_available() {
   return major == 10 && minor == 3 && encode_fn() != nullptr;
 }
 
-// Cluster sizes (CTAs sharing one B tile by TMA multicast) of the SYRK and the split GRM.V.
-// Defaults from the cluster sweep at N = 100k, M = 150k (SYRK 1.96 s with 1 CTA, 1.20 s with 2,
-// 1.11 s with 4; GRM.V fastest with 2 at 256-1024 columns); the tuner can change them.
-static int g_cluster_syrk = 4;
-static int g_cluster_grmv = 2;
+// Shape options of the tcgen05 GEMMs (process-wide; saigegpu.tune sets them from timings).
+static int g_opt[kTcOptions] = {
+    0,    // kTcSyrkPair: SYRK tiles on CTA pairs (cta_group::2, 256 x 256)
+    0,    // kTcGrmvPair: split GRM.V tiles on CTA pairs (256 x BN)
+    512,  // kTcDrainBytes: bytes of K per row one TMEM accumulator takes before it is drained
+    16,   // kTcSyrkGroup: row tiles per raster group of the SYRK
+    0,    // kTcGrmvSlice: K slice bytes of the split-BF16 GRM.V (0: by width, 64 or 128)
+    0,    // kTcSubsetPair: subset-exact genotype GEMMs on CTA pairs
+};
 
-bool tc_set_clusters(int syrk, int grmv) {
-  auto ok = [](int c) { return c == 1 || c == 2 || c == 4; };
-  if (!ok(syrk) || !ok(grmv)) return false;
-  g_cluster_syrk = syrk;
-  g_cluster_grmv = grmv;
+bool tc_set_option(int opt, int value) {
+  if (opt < 0 || opt >= kTcOptions) return false;
+  switch (opt) {
+    case kTcSyrkPair:
+    case kTcGrmvPair:
+    case kTcSubsetPair:
+      if (value != 0 && value != 1) return false;
+      break;
+    case kTcDrainBytes:  // whole 128-byte stages, at most 4 KB (the bias grows with the length)
+      if (value < 128 || value > 4096 || value % 128 != 0) return false;
+      break;
+    case kTcSyrkGroup:
+      if (value < 1 || value > 4096) return false;
+      break;
+    case kTcGrmvSlice:
+      if (value != 0 && value != 64 && value != 128) return false;
+      break;
+  }
+  g_opt[opt] = value;
   return true;
 }
-void tc_get_clusters(int* syrk, int* grmv) {
-  *syrk = g_cluster_syrk;
-  *grmv = g_cluster_grmv;
+
+int tc_get_option(int opt) { return opt >= 0 && opt < kTcOptions ? g_opt[opt] : -1; }
+
+// Per-launch-width choices of the split-BF16 GRM.V (the tuner's table): the first bucket whose
+// max_cols covers a launch's columns gives its CTA-pair and K-slice choice; wider launches, or no
+// table, use the process-wide options.
+struct GrmvChoice {
+  int64_t max_cols;
+  int pair, slice;
+};
+static std::vector<GrmvChoice> g_plan;
+
+bool tc_set_grmv_plan(const int32_t* max_cols, const int32_t* pair, const int32_t* slice, int n) {
+  std::vector<GrmvChoice> plan;
+  for (int i = 0; i < n; ++i) {
+    if (max_cols[i] <= 0 || (i > 0 && max_cols[i] <= max_cols[i - 1])) return false;
+    if ((pair[i] != 0 && pair[i] != 1) || (slice[i] != 0 && slice[i] != 64 && slice[i] != 128)) return false;
+    plan.push_back(GrmvChoice{max_cols[i], pair[i], slice[i]});
+  }
+  g_plan.swap(plan);
+  return true;
+}
+
+int tc_get_grmv_plan(int32_t* max_cols, int32_t* pair, int32_t* slice, int cap) {
+  const int n = (int)g_plan.size();
+  for (int i = 0; i < n && i < cap; ++i) {
+    max_cols[i] = (int32_t)g_plan[i].max_cols;
+    pair[i] = g_plan[i].pair;
+    slice[i] = g_plan[i].slice;
+  }
+  return n;
+}
+
+static GrmvChoice grmv_choice(int64_t ncols) {
+  for (const GrmvChoice& b : g_plan)
+    if (ncols <= b.max_cols) return b;
+  return GrmvChoice{0, g_opt[kTcGrmvPair], g_opt[kTcGrmvSlice]};
+}
+
+static int drain_stages(int rb) { return g_opt[kTcDrainBytes] / rb > 0 ? g_opt[kTcDrainBytes] / rb : 1; }
+
+// Lower-triangle tiles of the SYRK in raster groups: ``group`` consecutive row tiles (of ``unit``
+// 128-row blocks each) sweep the column blocks together, column block by column block, so that the
+// tiles resident at one time share a few row panels and a few column panels of Z in L2 instead of
+// one row panel and a whole row of column panels.  Column block bn (BN wide) of a row tile is
+// kept when it starts at or before the tile's last row; tiles above a row block's diagonal store
+// nothing, and a trailing row block past np loads zeros and stores nothing.
+static void syrk_tiles(std::vector<TileCoord>& out, int64_t np, int BN, int unit, int group) {
+  out.clear();
+  const int64_t nbm = np / kTileM;
+  const int64_t nrt = (nbm + unit - 1) / unit;
+  for (int64_t g0 = 0; g0 < nrt; g0 += group) {
+    const int64_t g1 = g0 + group < nrt ? g0 + group : nrt;
+    for (int64_t bn = 0;; ++bn) {
+      if (bn * BN >= np) break;
+      bool any = false;
+      for (int64_t rt = g0; rt < g1; ++rt) {
+        const int64_t last_row = (rt * unit + unit) * kTileM - 1;
+        if (bn * BN <= last_row) {
+          out.push_back(TileCoord{(int32_t)(rt * unit), (int32_t)bn});
+          any = true;
+        }
+      }
+      if (!any) break;
+    }
+  }
 }
 
 cudaError_t tc_syrk_bf16(const void* Zhi, const void* Zlo, int64_t np, int64_t mp, float* K,
                          float scale, cudaStream_t s) {
   constexpr int BN = 256;
   if (np % kTileM != 0 || mp % 64 != 0) return cudaErrorInvalidValue;
-  const int C = g_cluster_syrk;
-  // 128-byte K slices, 4 stages of 48 KB (2 for the split build).  64-byte slices with twice the
-  // stages measured slower here (1.25 s against 1.06-1.09 s at N = 100k; tensor pipe 49% against
-  // 56% busy in ncu): each stage is one MMA pass shared by a 4-CTA cluster, and halving it doubles
-  // the cluster-wide barrier round trips per FLOP.
+  const bool pair = g_opt[kTcSyrkPair] != 0;
+  // 128-byte K slices: 4 stages of 48 KB per CTA (2 for the split build), or on a CTA pair 6
+  // stages of 32 KB (3 for the split build)
   constexpr int RB = 128;
   CUtensorMap a, b, a2, b2;
   const uint64_t rb = (uint64_t)mp * 2;
-  const uint32_t brows = (uint32_t)(BN / C);  // each CTA of a cluster loads its slice of B
+  const uint32_t brows = (uint32_t)(pair ? BN / 2 : BN);  // a pair's CTAs load half of B each
   if (!make_map(&a, Zhi, false, mp, np, rb, kTileM, RB) || !make_map(&b, Zhi, false, mp, np, rb, brows, RB))
     return cudaErrorInvalidValue;
   a2 = a;
   b2 = b;
   if (Zlo && (!make_map(&a2, Zlo, false, mp, np, rb, kTileM, RB) || !make_map(&b2, Zlo, false, mp, np, rb, brows, RB)))
     return cudaErrorInvalidValue;
-  // Lower-triangle tiles: column block bn (BN wide) starts at or before the last row of the row
-  // block.  With clusters, C consecutive row blocks share each column block (the union of their
-  // column blocks; tiles fully above a row block's diagonal store nothing), and a trailing group is
-  // padded with row blocks past np (zero-filled loads, nothing stored).
   static TileCache cache;
-  cache.host.clear();
-  const int64_t nbm = np / kTileM;
-  const int64_t ngroups = (nbm + C - 1) / C;
-  for (int64_t gi = 0; gi < ngroups; ++gi) {
-    const int64_t last_row = (gi * C + C - 1) * kTileM + kTileM - 1;
-    for (int64_t bn = 0; bn * BN <= last_row && bn * BN < np; ++bn)
-      for (int r = 0; r < C; ++r) cache.host.push_back(TileCoord{(int32_t)(gi * C + r), (int32_t)bn});
-  }
+  syrk_tiles(cache.host, np, BN, pair ? 2 : 1, g_opt[kTcSyrkGroup]);
   cudaError_t e = upload_tiles(cache, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(mp / (RB / 2));
   const int nt = (int)cache.host.size();
+  const int dk = drain_stages(RB);
   if (Zlo) {
     // all four products: the residuals Zl of a marker take only three values (one per genotype),
     // so the Zl Zl' term does not average out over markers (dropping it left the off-diagonal
     // entries ~7e-7 off at M = 150k, against ~2e-9 with it)
-    switch (C) {
-      case 4: e = launch<false, BN, 2, true, 4, RB, true>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      case 2: e = launch<false, BN, 2, true, 2, RB, true>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      default: e = launch<false, BN, 2, true, 1, RB, true>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-    }
+    e = pair ? launch<false, BN, 3, kSplit4, true, RB>(a, b, a2, b2, cache.dev, nt, num_kb, dk, K, np, scale, 2, s, np)
+             : launch<false, BN, 2, kSplit4, false, RB>(a, b, a2, b2, cache.dev, nt, num_kb, dk, K, np, scale, 2, s, np);
   } else {
-    switch (C) {
-      case 4: e = launch<false, BN, 4, false, 4, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      case 2: e = launch<false, BN, 4, false, 2, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-      default: e = launch<false, BN, 4, false, 1, RB>(a, b, a2, b2, cache.dev, nt, num_kb, K, np, scale, 2, s, np); break;
-    }
+    e = pair ? launch<false, BN, 6, kOne, true, RB>(a, b, a2, b2, cache.dev, nt, num_kb, dk, K, np, scale, 2, s, np)
+             : launch<false, BN, 4, kOne, false, RB>(a, b, a2, b2, cache.dev, nt, num_kb, dk, K, np, scale, 2, s, np);
   }
   if (e != cudaSuccess) return e;
   return check_error_flag(s);
@@ -801,7 +933,9 @@ static const std::vector<int> kBf16Widths = {256, 224, 208, 192, 176, 160, 144, 
 static const std::vector<int> kPlainWidths = {256, 128, 64, 32};
 
 static const std::vector<int>& tile_widths(int set) {
-  return set == kTilesSplitBF16 ? kBf16Widths : set == kTilesSplitTF32 ? kSplitWidths : kPlainWidths;
+  return set == kTilesSplitBF16 ? kBf16Widths
+         : (set == kTilesSplitTF32 || set == kTilesSplitB) ? kSplitWidths
+                                                           : kPlainWidths;
 }
 
 // Column-tile width for ncols columns: the widest tile that divides ncols (wider tiles re-read
@@ -814,22 +948,26 @@ int tc_gemm_tile_n(int64_t ncols, int set) {
   return set == kTilesSplitBF16 ? 16 : 32;
 }
 
-// Columns one GRM.V launch covers for ncols32 (a multiple of 32) live columns, padded so that the
+// Columns one GRM.V launch covers for ncols32 (a multiple of 16) live columns, padded so that the
 // modelled cost is lowest, capped at cap columns.  Cost model (L2->SM bytes of one pass, which
-// bounds these kernels, over the fraction of the last wave of 1-CTA-per-SM tiles that is busy):
-//   padded * (A bytes per stage / BN + B bytes per stage per column) / wave_efficiency.
+// bounds these kernels, over the fraction of the last wave of 1-tile-per-SM(-pair) tiles that is
+// busy): padded * (A bytes per stage / BN + B bytes per stage per column) / wave_efficiency; a CTA
+// pair loads half of the B tile per SM and fills num_sms / 2 tile slots per wave.
 int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, int set, int num_sms) {
   double best = 1e300;
   int64_t best_cols = ncols32;
-  const int64_t nbm = np / kTileM;
   for (int w : tile_widths(set)) {
     const int64_t padded = (ncols32 + w - 1) / w * w;
     if (padded > cap) continue;
+    const bool pair = (set == kTilesSplitBF16 && grmv_choice(padded).pair != 0) ||
+                      (set == kTilesSplitB && g_opt[kTcSubsetPair] != 0);
+    const int64_t nrt = pair ? (np / kTileM + 1) / 2 : np / kTileM;
+    const int64_t slots = pair ? num_sms / 2 : num_sms;
     const int bn = tc_gemm_tile_n(padded, set);
-    const int64_t tiles = nbm * (padded / bn);
-    const int64_t waves = (tiles + num_sms - 1) / num_sms;
-    const double eff = (double)tiles / (double)(waves * num_sms);
-    const double cost = (double)padded * ((double)kATileBytes / bn + (double)kRowBytes) / eff;
+    const int64_t tiles = nrt * (padded / bn);
+    const int64_t waves = (tiles + slots - 1) / slots;
+    const double eff = (double)tiles / (double)(waves * slots);
+    const double cost = (double)padded * ((double)kATileBytes / bn + (double)kRowBytes / (pair ? 2 : 1)) / eff;
     if (cost < best) {
       best = cost;
       best_cols = padded;
@@ -841,73 +979,119 @@ int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, int set, i
 // K slice bytes of a split GRM.V launch over ncols columns: 128 for split-TF32; for split-BF16, 64
 // (twice the stages: measured 10% faster at 256 columns, 8-12% from there up) once the launch is
 // bound by the tensor pipe, and 128 while it streams K from HBM (at most 160 columns: half as many,
-// larger stages, measured 3% faster at 128 columns)
+// larger stages, measured 3% faster at 128 columns); kTcGrmvSlice overrides the split-BF16 choice.
 static int grmv_slice_bytes(bool tf32, int64_t ncols) {
-  return tf32 || ncols <= 160 ? 128 : 64;
+  if (tf32) return 128;
+  const int slice = grmv_choice(ncols).slice;
+  if (slice != 0) return slice;
+  return ncols <= 160 ? 128 : 64;
 }
 
-template <bool kTF32, int BN, int S, int C, int RB>
+template <bool kTF32, int BN, int S, bool kPair, int RB>
 static cudaError_t launch_grmv_split(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& a2,
                                      const CUtensorMap& b2, const TileCoord* tiles, int nt, int num_kb,
                                      float* Y, int64_t np, cudaStream_t s, const int32_t* colmap) {
-  return launch<kTF32, BN, S, true, C, RB>(a, b, a2, b2, tiles, nt, num_kb, Y, np, 1.0f, 1, s, np, colmap);
+  return launch<kTF32, BN, S, kSplit3, kPair, RB>(a, b, a2, b2, tiles, nt, num_kb, drain_stages(RB), Y, np, 1.0f,
+                                               1, s, np, colmap);
 }
 
-// Split GRM.V over every (BN, cluster) variant, with as many pipeline stages as the 227 KB of
-// shared memory hold at that width.
+// Split GRM.V over every tile width, with as many pipeline stages as the 227 KB of shared memory
+// hold at that width (per CTA: two halves of 128 K rows plus BN -- or BN / 2 on a CTA pair -- P rows).
 template <bool kTF32>
-static cudaError_t grmv_split_dispatch(int BN, int C, int RB, const CUtensorMap& a, const CUtensorMap& b,
+static cudaError_t grmv_split_dispatch(int BN, bool pair, int RB, const CUtensorMap& a, const CUtensorMap& b,
                                        const CUtensorMap& a2, const CUtensorMap& b2, const TileCoord* tiles,
                                        int nt, int num_kb, float* Y, int64_t np, cudaStream_t s,
                                        const int32_t* colmap = nullptr) {
 #define SG_GRMV_ARGS a, b, a2, b2, tiles, nt, num_kb, Y, np, s, colmap
-#define SG_GRMV_CASE(BNv, Sv, RBv)                                                 \
-  case BNv:                                                                        \
-    return C == 4   ? launch_grmv_split<kTF32, BNv, Sv, 4, RBv>(SG_GRMV_ARGS)      \
-           : C == 2 ? launch_grmv_split<kTF32, BNv, Sv, 2, RBv>(SG_GRMV_ARGS)      \
-                    : launch_grmv_split<kTF32, BNv, Sv, 1, RBv>(SG_GRMV_ARGS);
-  // odd multiples of 16 (split-BF16 only): a 4-CTA slice would not be whole 8-row swizzle atoms
-#define SG_GRMV_CASE16(BNv, Sv, RBv)                                               \
-  case BNv:                                                                        \
-    return C >= 2 ? launch_grmv_split<kTF32, BNv, Sv, 2, RBv>(SG_GRMV_ARGS)        \
-                  : launch_grmv_split<kTF32, BNv, Sv, 1, RBv>(SG_GRMV_ARGS);
+#define SG_GRMV_CASE(BNv, Sv, RBv) \
+  case BNv:                        \
+    return launch_grmv_split<kTF32, BNv, Sv, false, RBv>(SG_GRMV_ARGS);
+#define SG_GRMV_PAIR(BNv, Sv, RBv) \
+  case BNv:                        \
+    return launch_grmv_split<kTF32, BNv, Sv, true, RBv>(SG_GRMV_ARGS);
   if constexpr (!kTF32) {
+    if (pair && RB == 64) {
+      switch (BN) {
+        SG_GRMV_PAIR(256, 7, 64)
+        SG_GRMV_PAIR(224, 7, 64)
+        SG_GRMV_PAIR(208, 7, 64)
+        SG_GRMV_PAIR(192, 8, 64)
+        SG_GRMV_PAIR(176, 8, 64)
+        SG_GRMV_PAIR(160, 8, 64)
+        SG_GRMV_PAIR(144, 9, 64)
+        SG_GRMV_PAIR(128, 9, 64)
+        SG_GRMV_PAIR(112, 9, 64)
+        SG_GRMV_PAIR(96, 10, 64)
+        SG_GRMV_PAIR(80, 10, 64)
+        SG_GRMV_PAIR(64, 11, 64)
+        SG_GRMV_PAIR(48, 11, 64)
+        SG_GRMV_PAIR(32, 12, 64)
+        default:
+          return cudaErrorInvalidValue;
+      }
+    }
+    if (pair) {
+      switch (BN) {
+        SG_GRMV_PAIR(256, 3, 128)
+        SG_GRMV_PAIR(224, 3, 128)
+        SG_GRMV_PAIR(208, 3, 128)
+        SG_GRMV_PAIR(192, 4, 128)
+        SG_GRMV_PAIR(176, 4, 128)
+        SG_GRMV_PAIR(160, 4, 128)
+        SG_GRMV_PAIR(144, 4, 128)
+        SG_GRMV_PAIR(128, 4, 128)
+        SG_GRMV_PAIR(112, 4, 128)
+        SG_GRMV_PAIR(96, 5, 128)
+        SG_GRMV_PAIR(80, 5, 128)
+        SG_GRMV_PAIR(64, 5, 128)
+        SG_GRMV_PAIR(48, 5, 128)
+        SG_GRMV_PAIR(32, 6, 128)
+        default:
+          return cudaErrorInvalidValue;
+      }
+    }
     if (RB == 64) {
       // (8 KB + BN x 64 B) x 2 halves per stage, as many stages as fit
       switch (BN) {
         SG_GRMV_CASE(256, 4, 64)
         SG_GRMV_CASE(224, 5, 64)
-        SG_GRMV_CASE16(208, 5, 64)
+        SG_GRMV_CASE(208, 5, 64)
         SG_GRMV_CASE(192, 5, 64)
-        SG_GRMV_CASE16(176, 5, 64)
+        SG_GRMV_CASE(176, 5, 64)
         SG_GRMV_CASE(160, 6, 64)
-        SG_GRMV_CASE16(144, 6, 64)
+        SG_GRMV_CASE(144, 6, 64)
         SG_GRMV_CASE(128, 7, 64)
-        SG_GRMV_CASE16(112, 7, 64)
+        SG_GRMV_CASE(112, 7, 64)
         SG_GRMV_CASE(96, 8, 64)
-        SG_GRMV_CASE16(80, 8, 64)
+        SG_GRMV_CASE(80, 8, 64)
         SG_GRMV_CASE(64, 9, 64)
-        SG_GRMV_CASE16(48, 10, 64)
+        SG_GRMV_CASE(48, 10, 64)
         SG_GRMV_CASE(32, 11, 64)
         default:
           return cudaErrorInvalidValue;
       }
     }
-    // (16 KB + BN x 128 B) x 2 halves per stage; launches of at most 160 columns
+    // (16 KB + BN x 128 B) x 2 halves per stage
     switch (BN) {
+      SG_GRMV_CASE(256, 2, 128)
+      SG_GRMV_CASE(224, 2, 128)
+      SG_GRMV_CASE(208, 2, 128)
+      SG_GRMV_CASE(192, 2, 128)
+      SG_GRMV_CASE(176, 2, 128)
       SG_GRMV_CASE(160, 3, 128)
-      SG_GRMV_CASE16(144, 3, 128)
+      SG_GRMV_CASE(144, 3, 128)
       SG_GRMV_CASE(128, 3, 128)
-      SG_GRMV_CASE16(112, 3, 128)
+      SG_GRMV_CASE(112, 3, 128)
       SG_GRMV_CASE(96, 4, 128)
-      SG_GRMV_CASE16(80, 4, 128)
+      SG_GRMV_CASE(80, 4, 128)
       SG_GRMV_CASE(64, 4, 128)
-      SG_GRMV_CASE16(48, 5, 128)
+      SG_GRMV_CASE(48, 5, 128)
       SG_GRMV_CASE(32, 5, 128)
       default:
         return cudaErrorInvalidValue;
     }
   } else {
+    (void)pair;
     // (16 KB + BN x 128 B) x 2 halves per stage
     switch (BN) {
       SG_GRMV_CASE(256, 2, 128)
@@ -923,17 +1107,19 @@ static cudaError_t grmv_split_dispatch(int BN, int C, int RB, const CUtensorMap&
     }
   }
 #undef SG_GRMV_CASE
-#undef SG_GRMV_CASE16
+#undef SG_GRMV_PAIR
 #undef SG_GRMV_ARGS
 }
 
-// Row groups of C consecutive row blocks (padded past np), every column block per group.
-static cudaError_t grmv_tiles(TileCache& cache, int64_t np, int64_t ncols, int BN, int C, cudaStream_t s) {
+// Row tiles (one 128-row block, or two for a CTA pair; a trailing block past np loads zeros and
+// stores nothing) times column blocks, column blocks fastest so that the tiles of one K row strip
+// run together.
+static cudaError_t grmv_tiles(TileCache& cache, int64_t np, int64_t ncols, int BN, bool pair, cudaStream_t s) {
   cache.host.clear();
   const int64_t nbm = np / kTileM;
-  for (int64_t gi = 0; gi < (nbm + C - 1) / C; ++gi)
-    for (int64_t bn = 0; bn < ncols / BN; ++bn)
-      for (int r = 0; r < C; ++r) cache.host.push_back(TileCoord{(int32_t)(gi * C + r), (int32_t)bn});
+  const int unit = pair ? 2 : 1;
+  for (int64_t rt = 0; rt < (nbm + unit - 1) / unit; ++rt)
+    for (int64_t bn = 0; bn < ncols / BN; ++bn) cache.host.push_back(TileCoord{(int32_t)(rt * unit), (int32_t)bn});
   return upload_tiles(cache, s);
 }
 
@@ -942,30 +1128,29 @@ cudaError_t tc_gemm_tf32(const float* K, const float* Klo, int64_t np, const flo
   if (np % kTileM != 0 || ncols % 32 != 0 || ncols <= 0) return cudaErrorInvalidValue;
   const bool split = Klo != nullptr && Plo != nullptr;
   const int BN = tc_gemm_tile_n(ncols, split ? kTilesSplitTF32 : kTilesPlain);
-  const int C = split ? g_cluster_grmv : 1;
   CUtensorMap a, b, a2, b2;
-  const uint32_t brows = (uint32_t)(BN / C);
   if (!make_map(&a, K, true, np, np, (uint64_t)np * 4, kTileM) ||
-      !make_map(&b, P, true, np, ncols, (uint64_t)np * 4, brows))
+      !make_map(&b, P, true, np, ncols, (uint64_t)np * 4, BN))
     return cudaErrorInvalidValue;
   a2 = a;
   b2 = b;
   if (split && (!make_map(&a2, Klo, true, np, np, (uint64_t)np * 4, kTileM) ||
-                !make_map(&b2, Plo, true, np, ncols, (uint64_t)np * 4, brows)))
+                !make_map(&b2, Plo, true, np, ncols, (uint64_t)np * 4, BN)))
     return cudaErrorInvalidValue;
   static TileCache cache;
-  cudaError_t e = grmv_tiles(cache, np, ncols, BN, C, s);
+  cudaError_t e = grmv_tiles(cache, np, ncols, BN, false, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(np / 32);
   const int nt = (int)cache.host.size();
+  const int dk = drain_stages(128);
   if (split) {
-    e = grmv_split_dispatch<true>(BN, C, 128, a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s);
+    e = grmv_split_dispatch<true>(BN, false, 128, a, b, a2, b2, cache.dev, nt, num_kb, Y, np, s);
   } else {
     switch (BN) {
-      case 256: e = launch<true, 256, 3, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
-      case 128: e = launch<true, 128, 4, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
-      case 64: e = launch<true, 64, 6, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
-      default: e = launch<true, 32, 8, false>(a, b, a, b, cache.dev, nt, num_kb, Y, np, 1.0f, 1, s, np); break;
+      case 256: e = launch<true, 256, 3, kOne>(a, b, a, b, cache.dev, nt, num_kb, dk, Y, np, 1.0f, 1, s, np); break;
+      case 128: e = launch<true, 128, 4, kOne>(a, b, a, b, cache.dev, nt, num_kb, dk, Y, np, 1.0f, 1, s, np); break;
+      case 64: e = launch<true, 64, 6, kOne>(a, b, a, b, cache.dev, nt, num_kb, dk, Y, np, 1.0f, 1, s, np); break;
+      default: e = launch<true, 32, 8, kOne>(a, b, a, b, cache.dev, nt, num_kb, dk, Y, np, 1.0f, 1, s, np); break;
     }
   }
   if (e != cudaSuccess) return e;
@@ -977,8 +1162,8 @@ cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const voi
   if (np % kTileM != 0 || ncols % 16 != 0 || ncols <= 0 || !Kh || !Kl || !Ph || !Pl)
     return cudaErrorInvalidValue;
   const int BN = tc_gemm_tile_n(ncols, kTilesSplitBF16);
-  const int C = BN % 32 != 0 && g_cluster_grmv > 2 ? 2 : g_cluster_grmv;
-  const uint32_t brows = (uint32_t)(BN / C);
+  const bool pair = grmv_choice(ncols).pair != 0;
+  const uint32_t brows = (uint32_t)(pair ? BN / 2 : BN);
   const uint64_t rb = (uint64_t)np * 2;
   const int kSlice = grmv_slice_bytes(false, ncols);
   CUtensorMap a, b, a2, b2;
@@ -986,11 +1171,74 @@ cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const voi
       !make_map(&a2, Kl, false, np, np, rb, kTileM, kSlice) || !make_map(&b2, Pl, false, np, ncols, rb, brows, kSlice))
     return cudaErrorInvalidValue;
   static TileCache cache;
-  cudaError_t e = grmv_tiles(cache, np, ncols, BN, C, s);
+  cudaError_t e = grmv_tiles(cache, np, ncols, BN, pair, s);
   if (e != cudaSuccess) return e;
   const int num_kb = (int)(np / (kSlice / 2));
-  e = grmv_split_dispatch<false>(BN, C, kSlice, a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y, np,
-                                 s, colmap);
+  e = grmv_split_dispatch<false>(BN, pair, kSlice, a, b, a2, b2, cache.dev, (int)cache.host.size(), num_kb, Y,
+                                 np, s, colmap);
+  if (e != cudaSuccess) return e;
+  return check ? check_error_flag(s) : cudaSuccess;
+}
+
+// D = A (Bh + Bl)^T: A (rows x kdim) exact in BF16 (genotype values), B as BF16 high + low halves
+// (ncols x kdim), two products per K step into the drained TMEM accumulators; D RHS-major (column j
+// of the product is row j of D, leading dimension ldd).  64-byte K slices, as many stages as fit.
+cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void* Bh, const void* Bl,
+                           int64_t ncols, float* D, int64_t ldd, cudaStream_t s, bool check, int site) {
+  if (rows % kTileM != 0 || kdim % 32 != 0 || ncols % 32 != 0 || ncols <= 0 || !A || !Bh || !Bl || site < 0 ||
+      site > 1)
+    return cudaErrorInvalidValue;
+  const int BN = tc_gemm_tile_n(ncols, kTilesSplitB);
+  const bool pair = g_opt[kTcSubsetPair] != 0;
+  constexpr int RB = 64;
+  const uint64_t rb = (uint64_t)kdim * 2;
+  CUtensorMap a, b, b2;
+  if (!make_map(&a, A, false, kdim, rows, rb, kTileM, RB) ||
+      !make_map(&b, Bh, false, kdim, ncols, rb, pair ? BN / 2 : BN, RB) ||
+      !make_map(&b2, Bl, false, kdim, ncols, rb, pair ? BN / 2 : BN, RB))
+    return cudaErrorInvalidValue;
+  // one tile table per call site: the two GEMMs of an engine step are queued back to back, so the
+  // second must not restage the table the first one's upload may still be reading
+  static TileCache caches[2];
+  TileCache& cache = caches[site];
+  cudaError_t e = grmv_tiles(cache, rows, ncols, BN, pair, s);
+  if (e != cudaSuccess) return e;
+  const int num_kb = (int)(kdim / (RB / 2));
+  const int nt = (int)cache.host.size();
+  const int dk = drain_stages(RB);
+#define SG_SB(BNv, Sv, Pv)                                                                                  \
+  case BNv:                                                                                                 \
+    e = launch<false, BNv, Sv, kSplitB, Pv, RB>(a, b, a, b2, cache.dev, nt, num_kb, dk, D, ldd, 1.0f, 1, s, \
+                                                 rows);                                                    \
+    break;
+  if (pair) {
+    switch (BN) {
+      SG_SB(256, 9, true)
+      SG_SB(224, 10, true)
+      SG_SB(192, 11, true)
+      SG_SB(160, 12, true)
+      SG_SB(128, 12, true)
+      SG_SB(96, 12, true)
+      SG_SB(64, 12, true)
+      SG_SB(32, 12, true)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else {
+    switch (BN) {
+      SG_SB(256, 5, false)
+      SG_SB(224, 6, false)
+      SG_SB(192, 7, false)
+      SG_SB(160, 8, false)
+      SG_SB(128, 9, false)
+      SG_SB(96, 11, false)
+      SG_SB(64, 12, false)
+      SG_SB(32, 12, false)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  }
+#undef SG_SB
   if (e != cudaSuccess) return e;
   return check ? check_error_flag(s) : cudaSuccess;
 }
@@ -1075,9 +1323,11 @@ cudaError_t tc_gemm_tf32x3_noalloc(const float* Khi, const float* Klo, int64_t n
     return cudaErrorInvalidValue;
   const int num_kb = (int)(np / 32);
   if (BN == 64)
-    e = launch<true, 64, 4, true>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, Y, np, 1.0f, 1, s, np);
+    e = launch<true, 64, 4, kSplit3>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, drain_stages(128), Y, np, 1.0f,
+                                  1, s, np);
   else
-    e = launch<true, 32, 5, true>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, Y, np, 1.0f, 1, s, np);
+    e = launch<true, 32, 5, kSplit3>(a, b, a2, b2, tiles, (int)(nbm * nbn), num_kb, drain_stages(128), Y, np, 1.0f,
+                                  1, s, np);
   if (e != cudaSuccess) return e;
   return check_error_flag(s);
 }

@@ -36,10 +36,12 @@ struct MarkerQC {
   int32_t pass_vr;  // variance-ratio marker
 };
 
+// max_mac_vr != -1 selects categorical variance-ratio markers (every marker with min <= MAC < max)
 void launch_marker_qc(const uint8_t* raw, int64_t raw_pitch, int64_t m, int64_t n_fam,
                       const uint32_t* maskbits, int64_t nn, float min_maf, float max_miss,
-                      const uint8_t* vr_flag, float min_mac_vr, int is_var_ratio, MarkerQC* out,
-                      cudaStream_t s);
+                      const uint8_t* vr_flag, float min_mac_vr, float max_mac_vr, int is_var_ratio,
+                      MarkerQC* out, cudaStream_t s);
+// qc == nullptr keeps missing calls (code 01) instead of writing the fill genotype's code
 void launch_repack(const uint8_t* raw, int64_t raw_pitch, const int32_t* src_marker,
                    const MarkerQC* qc, int64_t m_out, const int32_t* sub0, int64_t nn,
                    int identity, uint8_t* out, int64_t out_pitch, cudaStream_t s);
@@ -104,11 +106,24 @@ void launch_split_bf16(const float* x, const float* x2, void* hi, void* lo, int6
 cudaError_t tc_check_error(cudaStream_t s);
 // Runs the kernels' bounded mbarrier wait on a barrier nothing arrives at (budget in ms).
 cudaError_t tc_wait_selftest(double budget_ms, int* waited_out, cudaStream_t s);
-// Cluster sizes (1, 2 or 4 CTAs sharing one B tile by TMA multicast) of the SYRK and split GRM.V.
-bool tc_set_clusters(int syrk, int grmv);
-void tc_get_clusters(int* syrk, int* grmv);
-// GRM.V column-tile width sets: plain TF32 / FP32, split-TF32, split-BF16 (multiples of 16)
-enum { kTilesPlain = 0, kTilesSplitTF32 = 1, kTilesSplitBF16 = 2 };
+// Shape options of the tcgen05 GEMMs (process-wide), in the order of sg_tc_option (saigegpu.h):
+// SYRK on CTA pairs, split-BF16 GRM.V on CTA pairs, drain length (bytes of K per row per TMEM
+// accumulator chunk), SYRK raster group (row tiles), split-BF16 GRM.V K slice bytes (0 = by width).
+// The last one: the subset-exact genotype GEMMs on CTA pairs.
+enum { kTcSyrkPair = 0, kTcGrmvPair = 1, kTcDrainBytes = 2, kTcSyrkGroup = 3, kTcGrmvSlice = 4, kTcSubsetPair = 5,
+       kTcOptions = 6 };
+bool tc_set_option(int opt, int value);
+int tc_get_option(int opt);
+// Split-BF16 GRM.V choices per launch width (n buckets, max_cols increasing; n = 0 clears).
+bool tc_set_grmv_plan(const int32_t* max_cols, const int32_t* pair, const int32_t* slice, int n);
+int tc_get_grmv_plan(int32_t* max_cols, int32_t* pair, int32_t* slice, int cap);
+// GRM.V column-tile width sets: plain TF32 / FP32, split-TF32, split-BF16 (multiples of 16), and
+// the subset-exact genotype GEMMs (multiples of 32)
+enum { kTilesPlain = 0, kTilesSplitTF32 = 1, kTilesSplitBF16 = 2, kTilesSplitB = 3 };
+// D (ncols x ldd, RHS-major) = A (rows x kdim, exact BF16) (Bh + Bl)^T (ncols x kdim BF16 halves).
+// site (0 or 1): which of two call sites queued back to back on one stream (own tile tables).
+cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void* Bh, const void* Bl,
+                           int64_t ncols, float* D, int64_t ldd, cudaStream_t s, bool check, int site);
 // Column tile width the GRM.V kernel uses for ncols columns.
 int tc_gemm_tile_n(int64_t ncols, int set);
 // Columns a GRM.V launch covers for ncols live columns (a multiple of 32, or of 16 for split-BF16),
@@ -174,6 +189,37 @@ void launch_slot_weights(int64_t np, int64_t nn, const double* w, const uint8_t*
                          cudaStream_t s);
 void launch_f32_to_f64(const float* a, double* b, int64_t n, cudaStream_t s);
 int64_t pcg_nblk(int64_t np);
+
+// ---- subset-exact GRM.V (k_subset.cu): per-slot state of a phenotype's sample subset
+struct SubsetSlot {
+  const float* dprime;    // mg: 1/sd'^2 of the subset's GRM markers, 0 for the others
+  const float* p2;        // mg: 2 p' (the subset's allele frequency, FP32 as the reference's LUT)
+  const int32_t* flips;   // nflip markers whose subset fill differs from the cohort fill in G
+  const float* dfill;     // nflip: subset fill - cohort fill
+  const uint32_t* bits;   // np x W: bit b of word w = sample misses marker flips[32 w + b] (in S)
+  int32_t nflip = 0, W = 0;
+  double inv_m = 0.0;     // 1 / M' (the subset's GRM marker count)
+  double ns = 1.0;        // subset size
+};
+void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int64_t m, int64_t nn, int64_t mg,
+                   int64_t np, void* Gmm, void* Gsm, cudaStream_t s);
+void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* flips, int nflip, int W,
+                          const uint8_t* mask, int64_t nn, int64_t np, uint32_t* bits, cudaStream_t s);
+void launch_subset_diag(const uint8_t* codes, int64_t pitch, const float* lut4, int64_t m, int64_t nn, int64_t np,
+                        double* out, cudaStream_t s);
+int subset_nblk(int64_t n);
+// per step: column sums over the subset, then the centred BF16 halves (compact block of ncols)
+void launch_subset_prepare(const float* Pf, int64_t np, const int32_t* cols, int64_t ncols, const ColState* st,
+                           const SubsetSlot* slots, const double* winv, double* part, void* Vh, void* Vl,
+                           cudaStream_t s);
+// after GEMM 1: fill corrections into T, then T' = d' .* T as halves and the (2p')^T T' partials
+void launch_subset_scale(const void* Vh, const void* Vl, int64_t np, int64_t nn, const int32_t* cols, int64_t ncols,
+                         const ColState* st, const SubsetSlot* slots, int max_w, float* T, int64_t mg, void* Th,
+                         void* Tl, double* part, cudaStream_t s);
+// after GEMM 2: Y[cols[j]] = (U + dF T' - (2p')^T T') / M' on the subset
+void launch_subset_finalize(const float* U, int64_t np, int64_t nn, const int32_t* cols, int64_t ncols,
+                            const ColState* st, const SubsetSlot* slots, const void* Th, const void* Tl, int64_t mg,
+                            const double* part, const double* winv, float* Yf, cudaStream_t s);
 constexpr int kProbeDotsMaxP = 16;
 // Per probe j (vecs[j] = Sigma^-1 u_j and vecs[k+j] = K u_j, u masked by minv != 0):
 // block partials of [Au.Su, u.Su, Au.SX_q (q < p), SX_q.u (q < p)] -> part[(j*nblk + b)*(2+2p) + v]

@@ -12,7 +12,11 @@ import numpy as np
 from . import _lib as L
 
 GRM_FP32_SIMT, GRM_BF16_TC, GRM_BF16X3_TC = 0, 1, 2
-MV_FP32_SIMT, MV_TF32_TC, MV_FP64_PLAIN, MV_TF32X3_TC, MV_BF16X3_TC = 0, 1, 2, 3, 4
+MV_FP32_SIMT, MV_TF32_TC, MV_FP64_PLAIN, MV_TF32X3_TC, MV_BF16X3_TC, MV_SUBSET_EXACT = 0, 1, 2, 3, 4, 5
+# tcgen05 GEMM shape options (enum sg_tc_option)
+TC_SYRK_PAIR, TC_GRMV_PAIR, TC_DRAIN_BYTES, TC_SYRK_GROUP, TC_GRMV_SLICE, TC_SUBSET_PAIR = 0, 1, 2, 3, 4, 5
+TC_OPTIONS = {"syrk_pair": TC_SYRK_PAIR, "grmv_pair": TC_GRMV_PAIR, "drain_bytes": TC_DRAIN_BYTES,
+              "syrk_group": TC_SYRK_GROUP, "grmv_slice": TC_GRMV_SLICE, "subset_pair": TC_SUBSET_PAIR}
 
 
 def _f32(a):
@@ -87,13 +91,41 @@ class Context:
         """Make this context's GPU current on the calling thread (worker threads of a runner)."""
         self._call("sg_ctx_make_current")
 
-    def set_tc_clusters(self, syrk, grmv):
-        self._call("sg_set_tc_clusters", int(syrk), int(grmv))
+    def set_tc_option(self, option, value):
+        """Shape option of the tcgen05 GEMMs (TC_* constants; process-wide)."""
+        self._call("sg_set_tc_option", int(option), int(value))
 
-    def get_tc_clusters(self):
-        a, b = C.c_int32(), C.c_int32()
-        self._call("sg_get_tc_clusters", C.byref(a), C.byref(b))
-        return a.value, b.value
+    def get_tc_option(self, option):
+        v = C.c_int32()
+        self._call("sg_get_tc_option", int(option), C.byref(v))
+        return v.value
+
+    def tc_options(self):
+        """All tcgen05 shape options as a dict name -> value."""
+        return {name: self.get_tc_option(opt) for name, opt in TC_OPTIONS.items()}
+
+    def set_grmv_plan(self, plan):
+        """Per-width split-BF16 GRM.V choices: a list of (max_cols, pair, slice) with increasing
+        max_cols ([] clears)."""
+        plan = sorted(plan)
+        mc = np.array([p[0] for p in plan], np.int32)
+        pr = np.array([p[1] for p in plan], np.int32)
+        sl = np.array([p[2] for p in plan], np.int32)
+        P = C.POINTER(C.c_int32)
+        self._call("sg_set_grmv_plan", len(plan), _ptr(mc, P), _ptr(pr, P), _ptr(sl, P))
+
+    def grmv_plan(self):
+        cap = 64
+        mc, pr, sl = (np.zeros(cap, np.int32) for _ in range(3))
+        n = C.c_int()
+        P = C.POINTER(C.c_int32)
+        self._call("sg_get_grmv_plan", cap, _ptr(mc, P), _ptr(pr, P), _ptr(sl, P), C.byref(n))
+        return [(int(mc[i]), int(pr[i]), int(sl[i])) for i in range(n.value)]
+
+    def set_tc_options(self, opts):
+        """Set options from a dict name -> value (as returned by ``tc_options``)."""
+        for name, v in opts.items():
+            self.set_tc_option(TC_OPTIONS[name], v)
 
     def set_matvec_mode(self, mode):
         self._call("sg_set_matvec_mode", int(mode))
@@ -107,6 +139,11 @@ class Context:
         vr = np.zeros(1, np.int32) if vr_random is None else np.ascontiguousarray(vr_random, np.int32)
         nvr = 0 if vr_random is None else len(vr)
         return sub, mask, vr, nvr
+
+    def set_vr_max_mac(self, max_mac):
+        """Categorical variance ratios for the next setgeno (g_maxMACVarRatio; -1 = single ratio)."""
+        self._call("sg_set_vr_max_mac", float(max_mac))
+        self._vr_max_mac = float(max_mac)
 
     def setgeno(self, bed, n_fam, m_bim, sub_1based=None, pheno_mask=None, min_maf=0.01,
                 max_missing=0.15, vr_random=None, min_mac_vr=20.0, is_var_ratio=False,

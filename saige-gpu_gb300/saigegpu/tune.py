@@ -1,11 +1,16 @@
-"""Autotuner for the tcgen05 kernels' cluster shapes.
+"""Autotuner for the tcgen05 kernels' shapes, from measured times on the resident cohort.
 
-The SYRK and the split GRM.V (TF32 or BF16 halves) can run with 1, 2 or 4 CTAs per
-thread-block cluster sharing each B tile through TMA multicast (fewer
-L2->SM operand bytes per FLOP).  Which size wins depends on N, the number of
-right-hand sides and the tile width, so ``tune`` times every variant on the
-resident cohort with the library's CUDA-event timers and keeps the fastest.
-All variants produce bit-identical results (same accumulation order).
+SYRK: single CTAs (128 x 256 tiles) or CTA pairs (tcgen05 cta_group::2, 256 x 256 tiles), and the
+raster group (how many row tiles sweep the column blocks together, which sets how many Z panels the
+resident tiles share in L2).
+
+Split-BF16 GRM.V: per launch-width bucket, single CTAs or CTA pairs and the K slice per pipeline
+stage (64 bytes: twice the stages; 128: half the barrier round trips).  The chosen table goes into
+the library (``Context.set_grmv_plan``), which applies it to every later launch.
+
+Every choice gives bit-identical products (same MMA order, same drain length), so tuning never
+changes a fit.  The drain length is not tuned: it sets the accumulation bias (the tensor core's
+accumulation into TMEM loses magnitude over long chunks), so it stays at the library's 512 bytes.
 """
 import argparse
 import json
@@ -13,24 +18,42 @@ import time
 
 import numpy as np
 
-from .context import GRM_BF16_TC, MV_BF16X3_TC, MV_TF32X3_TC
+from .context import GRM_BF16_TC, MV_BF16X3_TC, TC_SYRK_GROUP, TC_SYRK_PAIR
+
+# launch widths the GRM.V table covers (columns after padding to a tile width)
+GRMV_BUCKETS = (32, 64, 96, 128, 160, 224, 320, 448, 640, 1024)
+GRMV_VARIANTS = ((0, 128), (0, 64), (1, 128), (1, 64))  # (CTA pair, K slice bytes)
+SYRK_VARIANTS = ((0, 16), (1, 8), (1, 16), (1, 32))     # (CTA pair, raster group)
+
+# a variant other than the first is kept only when it is faster by more than the spread of
+# repeated timings
+MARGIN = 0.02
 
 
-def time_syrk(ctx, cluster, precision=GRM_BF16_TC, reps=1):
-    _, g = ctx.get_tc_clusters()
-    ctx.set_tc_clusters(cluster, g)
-    best = float("inf")
-    for _ in range(reps):
-        t = time.perf_counter()
-        ctx.grm_build(precision)  # synchronous: returns when the SYRK has finished
-        best = min(best, time.perf_counter() - t)
+def _pick(times, variants):
+    best = variants[0]
+    for v in variants[1:]:
+        if times[v] < times[best] * (1.0 - MARGIN):
+            best = v
     return best
 
 
-def time_grmv(ctx, cluster, ncols, reps=2, seed=0):
-    s, _ = ctx.get_tc_clusters()
-    ctx.set_tc_clusters(s, cluster)
-    V = np.random.default_rng(seed).standard_normal((ctx.n, ncols))
+def time_syrk(ctx, pair, group, precision=GRM_BF16_TC, reps=1):
+    """Event-timed SYRK of the resident cohort (ms), best of reps."""
+    ctx.set_tc_option(TC_SYRK_PAIR, pair)
+    ctx.set_tc_option(TC_SYRK_GROUP, group)
+    best = float("inf")
+    for _ in range(reps):
+        ctx.grm_build(precision)
+        best = min(best, ctx.build_timing()["syrk_ms"])
+    return best
+
+
+def time_grmv(ctx, ncols, pair, slice_bytes, reps=2, seed=0, V=None):
+    """Event-timed split GRM.V launch over ncols columns (ms per launch), best of reps."""
+    ctx.set_grmv_plan([(1 << 30, pair, slice_bytes)])  # whatever width the launch pads to
+    if V is None:
+        V = np.random.default_rng(seed).standard_normal((ctx.n, ncols))
     ctx.grm_matmul(V)
     best = float("inf")
     for _ in range(reps):
@@ -38,94 +61,64 @@ def time_grmv(ctx, cluster, ncols, reps=2, seed=0):
         ctx.grm_matmul(V)
         t = ctx.engine_timing()
         best = min(best, t["gemm_ms"] / max(1, t["gemm_launches"]))
-    return best / 1e3
-
-
-# a larger cluster is kept only when it is faster by more than the spread of repeated timings
-MARGIN = 0.02
-
-
-def _pick(times, clusters):
-    best = clusters[0]
-    for c in clusters[1:]:
-        if times[c] < times[best] * (1.0 - MARGIN):
-            best = c
     return best
 
 
-def tune(ctx, ncols=(128, 384, 1024), tune_syrk=True, clusters=(1, 2, 4), mode=MV_TF32X3_TC):
-    """Pick the cluster sizes; leaves the GRM built from 8-bit (BF16) genotypes and engine ``mode``
-    selected.  For fits, rebuild it with GRM_BF16X3_TC (16-bit genotypes): at N = 100k the 8-bit
-    GRM moved binary variance components by up to 1.1e-3 against FP64.
+def tune_syrk(ctx, variants=SYRK_VARIANTS):
+    """Times the single-product BF16 SYRK per variant and keeps the choice; leaves that GRM built
+    (every variant builds the same K)."""
+    times = {v: time_syrk(ctx, *v) for v in variants}
+    best = _pick(times, variants)
+    ctx.set_tc_option(TC_SYRK_PAIR, best[0])
+    ctx.set_tc_option(TC_SYRK_GROUP, best[1])
+    return {"times_ms": times, "chosen": best}
 
-    The SYRK: the smallest cluster within 2% of the fastest.  The GRM.V: each width's times relative
-    to the fastest cluster at that width, summed over the widths (each launched as one pass), the
-    smallest cluster within 2% of the lowest sum."""
-    report = {"syrk": {}, "grmv": {}}
-    if tune_syrk:
-        for c in clusters:
-            report["syrk"][c] = time_syrk(ctx, c)
-        best_s = _pick(report["syrk"], clusters)
-        ctx.set_tc_clusters(best_s, ctx.get_tc_clusters()[1])
-        ctx.grm_build(GRM_BF16_TC)
+
+def tune_grmv(ctx, buckets=GRMV_BUCKETS, variants=GRMV_VARIANTS, mode=MV_BF16X3_TC):
+    """Times every variant at every bucket width and installs the per-width plan."""
     ctx.set_matvec_mode(mode)
-    ctx.engine_reserve(max(ncols), 1)  # every width in one launch
-    totals = {c: 0.0 for c in clusters}
-    for k in ncols:
-        times = {c: time_grmv(ctx, c, k) for c in clusters}
-        for c in clusters:
-            report["grmv"][(c, k)] = times[c]
-            totals[c] += times[c] / min(times.values())
-    best_g = _pick(totals, clusters)
-    ctx.set_tc_clusters(ctx.get_tc_clusters()[0], best_g)
-    report["chosen"] = ctx.get_tc_clusters()
+    ctx.engine_reserve(max(buckets), 1)  # every width in one launch
+    table = {}
+    plan = []
+    rng = np.random.default_rng(0)
+    for w in buckets:
+        V = rng.standard_normal((ctx.n, w))
+        times = {v: time_grmv(ctx, w, *v, V=V) for v in variants}
+        best = _pick(times, variants)
+        table[w] = {"times_ms": times, "chosen": best}
+        plan.append((w, best[0], best[1]))
+    ctx.set_grmv_plan(plan)
+    return table
+
+
+def tune(ctx, tune_syrk_too=True, mode=MV_BF16X3_TC, grmv=True):
+    """SYRK and GRM.V choices from measured times; leaves the single-product BF16 GRM built (rebuild
+    it with GRM_BF16X3_TC for fits: at N = 100k the 8-bit GRM moved binary variance components by
+    up to 1.1e-3 against FP64) and, when the GRM.V is tuned, the engine in ``mode``."""
+    report = {"grmv": {}}
+    if tune_syrk_too:
+        report["syrk"] = tune_syrk(ctx)
+    if grmv:
+        report["grmv"] = tune_grmv(ctx, mode=mode)
+    report["plan"] = ctx.grmv_plan()
     return report
 
 
-def sweep(ctx, ncols=(32, 64, 128, 256, 512, 1024), clusters=(1, 2, 4),
-          modes=((MV_BF16X3_TC, "bf16x3"), (MV_TF32X3_TC, "tf32x3"))):
-    """Event-timed SYRK and split GRM.V over cluster sizes, tile widths and column counts on the
-    resident cohort; yields one dict per measurement (per-launch milliseconds, TFLOP/s, GB/s)."""
-    d = ctx.dims()
-    n, mq = d["n"], d["m_qc"]
-    prev = ctx.get_tc_clusters()
-    try:
-        for c in clusters:
-            ctx.set_tc_clusters(c, prev[1])
-            ms = []
-            for _ in range(2):
-                ctx.grm_build(GRM_BF16_TC)
-                ms.append(ctx.build_timing()["syrk_ms"])
-            yield {"kernel": "syrk_bf16", "cluster": c, "syrk_ms": [round(x, 2) for x in ms],
-                   "tflops": round(n * (n + 1.0) * mq / (min(ms) * 1e-3) / 1e12, 1)}
-        ctx.set_tc_clusters(prev[0], prev[1])
-        ctx.grm_build(GRM_BF16_TC)
-        npad = ctx.grm_padded_n()
-        rng = np.random.default_rng(0)
-        for mode, name in modes:
-            ctx.set_matvec_mode(mode)
-            ctx.engine_reserve(max(ncols), 1)
-            kbytes = 4.0 if name == "bf16x3" else 8.0
-            for k in ncols:
-                V = rng.standard_normal((n, k))
-                for c in clusters:
-                    ctx.set_tc_clusters(prev[0], c)
-                    ctx.grm_matmul(V)
-                    ctx.engine_reset_timing()
-                    ctx.grm_matmul(V)
-                    t = ctx.engine_timing()
-                    launches = max(1, t["gemm_launches"])
-                    ms = t["gemm_ms"] / launches
-                    cols = t["gemm_cols"] / launches
-                    yield {"kernel": "grmv_" + name, "k": k, "cluster": c, "cols": cols, "ms": round(ms, 3),
-                           "GBps": round((kbytes * npad * npad + 12.0 * npad * cols) / (ms * 1e-3) / 1e9, 1),
-                           "tflops": round(3 * 2.0 * npad * npad * cols / (ms * 1e-3) / 1e12, 1)}
-    finally:
-        ctx.set_tc_clusters(*prev)
+def report_json(report):
+    """The tuner's report with string keys (JSON)."""
+    out = {}
+    if "syrk" in report:
+        out["syrk"] = {"times_ms": {"pair%d_group%d" % k: round(v, 2) for k, v in report["syrk"]["times_ms"].items()},
+                       "chosen": {"pair": report["syrk"]["chosen"][0], "group": report["syrk"]["chosen"][1]}}
+    out["grmv"] = {str(w): {"times_ms": {"pair%d_slice%d" % k: round(v, 3) for k, v in r["times_ms"].items()},
+                            "chosen": {"pair": r["chosen"][0], "slice": r["chosen"][1]}}
+                   for w, r in report["grmv"].items()}
+    out["plan"] = [list(p) for p in report["plan"]]
+    return out
 
 
 def main(argv=None):
-    """python -m saigegpu.tune [--n N --m M]: the sweep above on a synthetic cohort, JSON lines."""
+    """python -m saigegpu.tune [--n N --m M]: the tuner on a synthetic cohort; one JSON report."""
     from .context import Context
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=100_000)
@@ -136,8 +129,12 @@ def main(argv=None):
     ctx = Context(0)
     ptr, ln = ctx.synth_bed(args.seed, args.n, args.m, args.miss)
     ctx.setgeno_device(ptr, ln, args.n, args.m)
-    for row in sweep(ctx):
-        print(json.dumps(row), flush=True)
+    t0 = time.perf_counter()
+    rep = tune(ctx)
+    out = report_json(rep)
+    out["seconds"] = round(time.perf_counter() - t0, 1)
+    out["n"], out["m"] = args.n, args.m
+    print(json.dumps(out), flush=True)
 
 
 if __name__ == "__main__":

@@ -11,7 +11,10 @@ multi-RHS solve on the GPU engine; the per-marker algebra is the reference's:
     var2 = sum mu(1-mu) g^2 (binary) or sum g^2 (quantitative), g = G / sqrt(AC)
     ratio = var1 / var2;  VR = mean(ratios)
 
-Single-ratio (non-categorical) estimate over the cohort's full sample set.
+Single ratio (``variance_ratio``) or one per MAC category (``categorical_variance_ratio``,
+isCateVarianceRatio: FIT.R:2245-2280 builds the categories, the loop at :2290-2410 runs the same
+estimate per category).  For categories, setgeno selects the markers with
+``Context.set_vr_max_mac(max(max_incl))`` and ``min_mac_vr = min(min_excl)`` (FIT.R:1082-1085).
 """
 import numpy as np
 
@@ -75,3 +78,39 @@ def variance_ratio(ctx, fit, trait, X, order, num_markers=30, ratio_cv_cutoff=0.
             continue
         break
     return float(np.mean(ratios)), np.array(ratios)
+
+
+# default MAC categories of fitNULLGLMM (FIT.R:683-684): 10 < MAC <= 20.5 and MAC > 20.5
+CATE_MIN_EXCL = (10.0, 20.5)
+CATE_MAX_INCL = (20.5,)
+
+
+def category_markers(mac, min_excl=CATE_MIN_EXCL, max_incl=CATE_MAX_INCL):
+    """Indices of the variance-ratio markers in each MAC category (FIT.R:2245-2260): category i
+    holds min_excl[i] < MAC <= max_incl[i]; the last one MAC > min_excl[-1] (and <= max_incl[-1]
+    when max_incl has as many entries as there are categories)."""
+    mac = np.asarray(mac, np.float64)
+    k = len(min_excl)
+    cats = []
+    for i in range(k - 1):
+        cats.append(np.nonzero((mac > min_excl[i]) & (mac <= max_incl[i]))[0])
+    if len(max_incl) == k - 1:
+        cats.append(np.nonzero(mac > min_excl[k - 1])[0])
+    else:
+        cats.append(np.nonzero((mac > min_excl[k - 1]) & (mac <= max_incl[k - 1]))[0])
+    return cats
+
+
+def categorical_variance_ratio(ctx, fit, trait, X, orders, num_markers=30, ratio_cv_cutoff=0.001, maxiter=500,
+                               tol=1e-5, vr_geno=None):
+    """One variance ratio per MAC category; ``orders[k]``: indices into the variance-ratio markers of
+    category k in test order (the reference shuffles each category with R's ``sample``).  A category
+    with fewer than num_markers markers is an error, as in the reference (FIT.R:2262-2278)."""
+    out = []
+    for k, order in enumerate(orders):
+        if len(order) < num_markers:
+            raise ValueError("MAC category %d has %d variance-ratio markers, fewer than %d" % (k + 1, len(order),
+                                                                                            num_markers))
+        v, _ = variance_ratio(ctx, fit, trait, X, order, num_markers, ratio_cv_cutoff, maxiter, tol, vr_geno)
+        out.append(v)
+    return out

@@ -1,9 +1,8 @@
 """Generate the golden fixtures under tests/golden/ from the reference project's example data.
 
-Run in a container where the reference checkout is mounted (read-only) at
-``/root/reference``:
+Run with the path of a (read-only) checkout of the reference project:
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py <reference checkout>
 
 It writes (all derived from ``src/SAIGE/extdata``):
 
@@ -197,4 +196,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout>")
+    main(sys.argv[1])

@@ -53,6 +53,7 @@ def test_full_fit_matches_oracle(golden_cohort, trait):
         ro = aireml.glmmkin_quantitative(grm, fit0)
         rg = glmm.glmmkin_quantitative(ctx, fit0)
     rel = np.abs(rg["theta"] - ro["theta"]) / np.abs(ro["theta"])
+    print("%s drop-in fit: tau %s oracle %s rel %s" % (trait, rg["theta"], ro["theta"], rel))
     # the drop-ins carry float32 vectors across the boundary, like Rcpp does
     assert rel.max() < 1e-3, (rg["theta"], ro["theta"])
     assert rg["iterations"] == ro["iterations"]

@@ -108,7 +108,6 @@ def test_fullsize_precision_against_fp64():
     rep = {"n": N, "m": M, "missing": MISS, "seed": SEED, "sampled_samples": N_SAMPLED}
     ctx = Context(0)
     try:
-        ctx.set_tc_clusters(4, 2)
         ptr, ln = ctx.synth_bed(SEED, N, M, MISS)
         vr_rand = np.unique(np.random.default_rng(5).integers(0, M, 1000)).astype(np.int32)
         ctx.setgeno_device(ptr, ln, N, M, vr_random=vr_rand, min_mac_vr=20.0, is_var_ratio=True)

@@ -1,0 +1,148 @@
+"""Subset-exact engine: each phenotype's GRM from its own sample subset, as the reference builds it.
+
+The reference runs setgeno over every phenotype's samples (FIT.cpp:376-385, 436-495), so allele
+frequencies, the integer fill, QC and 1/sd are the subset's; the cohort GRM restricted to the
+subset (the masked engines) is a different matrix.  Here the subset-exact engine is held to the
+FP64 oracle built over the subset (oracle.plink.setgeno with that subset), with the same probes,
+and the masked approximation's error is measured against it.
+"""
+import numpy as np
+import pytest
+
+from oracle import aireml, plink
+from saigegpu import MV_FP32_SIMT, MV_SUBSET_EXACT, TC_SUBSET_PAIR, native, prep, serve, synth
+
+pytestmark = pytest.mark.gpu
+
+N, M = 1800, 4000
+DROPS = (0.05, 0.2, 0.4, 0.3)
+
+
+def _subset_grm(bed, mask):
+    S = np.nonzero(mask)[0]
+    g = plink.setgeno(bed, N, M, S + 1, mask, 0.01, 0.15)
+    grm = aireml.DenseGRM(g)
+    grm.probe_index = S  # the engine hashes the cohort positions of the subset's samples
+    return grm
+
+
+def _run_products(ctx, ids):
+    """Steps the engine until every request in ids has finished; returns their results by id."""
+    pending = [int(i) for i in ids]
+    out = {}
+    for _ in range(1000):
+        if not pending:
+            break
+        ctx.engine_run()
+        for i in list(pending):
+            r = ctx.engine_try_fetch(i)
+            if r is not None:
+                out[i] = r[0]
+                pending.remove(i)
+    assert not pending, pending
+    return out
+
+
+@pytest.fixture(scope="module")
+def exact_cohort(gpu_ctx):
+    bed, _ = synth.synth_bed(77, N, M, 0.02)
+    gpu_ctx.set_matvec_mode(MV_FP32_SIMT)
+    gpu_ctx.setgeno(bed, N, M)
+    g = plink.setgeno(bed, N, M, np.arange(1, N + 1), np.ones(N, bool), 0.01, 0.15)
+    gv = synth.genetic_value_from_codes(g.codes, 9)
+    gv = gv / gv.std()
+    rng = np.random.default_rng(12)
+    cases = []
+    for k, drop in enumerate(DROPS):
+        trait = "binary" if k % 2 == 0 else "quantitative"
+        mask = rng.uniform(size=N) > drop
+        S = np.nonzero(mask)[0]
+        y, C = synth.simulate_pheno(gv, 300 + k, trait, tau=0.5, prevalence=0.25, h2=0.5)
+        f0 = prep.make_fit0(y[S], C[S], trait, True)
+        cases.append((trait, mask, f0))
+    return gpu_ctx, bed, g, cases
+
+
+def test_subset_exact_products_match_oracle(exact_cohort):
+    """Engine products K_S v (kind 1 columns) against the FP64 GRM built over each subset."""
+    ctx, bed, _, cases = exact_cohort
+    rng = np.random.default_rng(5)
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    try:
+        for pair in (0, 1):
+            ctx.set_tc_option(TC_SUBSET_PAIR, pair)
+            ctx.engine_reserve(128, len(cases))
+            ids = []
+            Vs = []
+            for slot, (_, mask, _) in enumerate(cases):
+                ctx.engine_set_pheno(slot, np.ones(N), np.array([1.0, 0.5]), mask)
+                V = rng.standard_normal((N, 7)) + 0.5  # a nonzero mean exercises the centring
+                V[~mask] = 0.0
+                Vs.append(V)
+                ids.append(ctx.engine_submit(slot, 1, V))
+            got = _run_products(ctx, np.concatenate(ids))
+            for (trait, mask, _), V, idk in zip(cases, Vs, ids):
+                S = np.nonzero(mask)[0]
+                grm = _subset_grm(bed, mask)
+                ref = grm.K @ V[S]
+                Y = np.column_stack([got[int(i)] for i in idk])[S]
+                err = np.abs(Y - ref).max() / np.abs(ref).max()
+                assert err < 6e-5, (pair, trait, err)
+    finally:
+        ctx.set_tc_option(TC_SUBSET_PAIR, 0)
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+
+
+def test_subset_exact_fits_match_oracle_and_masked_error_is_bounded(exact_cohort):
+    """Native batched fits on the subset-exact engine: tau within 1e-4 of the FP64 oracle on the
+    subset-built GRM (same probes).  The masked approximation (cohort GRM restricted to S) is
+    measured against the same exact answer: at this N it is off by percent, far beyond 1e-4."""
+    ctx, bed, g, cases = exact_cohort
+    specs = [serve.FitSpec(f0, trait, mask=mask) for trait, mask, f0 in cases]
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    try:
+        res, _ = native.fit_batch(ctx, specs, max_columns=256)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+    Kc = aireml.DenseGRM(g)
+    masked_err = []
+    for (trait, mask, f0), r in zip(cases, res):
+        assert not isinstance(r, Exception), r
+        S = np.nonzero(mask)[0]
+        fit = aireml.glmmkin_binary if trait == "binary" else aireml.glmmkin_quantitative
+        ref = fit(_subset_grm(bed, mask), f0)
+        np.testing.assert_allclose(r["theta"], ref["theta"], rtol=1e-4)
+        sub = aireml.DenseGRM.from_matrix(Kc.K[np.ix_(S, S)], Kc.m_qc, Kc.diag_sum[S])
+        sub.probe_index = S
+        approx = fit(sub, f0)
+        masked_err.append(float(np.max(np.abs(approx["theta"] - ref["theta"]) / np.abs(ref["theta"]))))
+    # the masked form is an approximation: at N = 1,800 it moved tau by 0.1-6% in the CPU study of
+    # this design; it must stay within 10% here and is reported, not claimed exact
+    assert max(masked_err) < 0.1, masked_err
+    print("masked-vs-exact tau relative error per phenotype:", masked_err)
+
+
+def test_subset_exact_alone_equals_in_the_mix(exact_cohort):
+    ctx, bed, g, cases = exact_cohort
+    specs = [serve.FitSpec(f0, trait, mask=mask) for trait, mask, f0 in cases]
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    try:
+        mix, _ = native.fit_batch(ctx, specs, max_columns=256)
+        alone, _ = native.fit_batch(ctx, [specs[2]], max_columns=256)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+    np.testing.assert_array_equal(alone[0]["theta"], mix[2]["theta"])
+
+
+def test_subset_exact_full_cohort_matches_cohort_grm(exact_cohort):
+    """No mask: the subset is the cohort, and the exact engine's product is the cohort K's."""
+    ctx, bed, g, cases = exact_cohort
+    grm = aireml.DenseGRM(g)
+    V = np.random.default_rng(8).standard_normal((N, 40))
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    try:
+        Y = ctx.grm_matmul(V)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+    ref = grm.K @ V
+    assert np.abs(Y - ref).max() / np.abs(ref).max() < 6e-5

@@ -73,25 +73,44 @@ def test_grm_matvec_tf32_tc(cohort):
 
 
 @pytest.mark.parametrize("split", [False, True])
-def test_syrk_cluster_variants_bit_identical(cohort, split):
+def test_syrk_shape_variants_bit_identical(cohort, split):
+    """Single CTAs and CTA pairs (tcgen05 cta_group::2), any raster group: the same K, bit for bit,
+    also when the row blocks are odd in number (a pair's second block past n loads zeros)."""
+    from saigegpu import TC_SYRK_GROUP, TC_SYRK_PAIR
     ctx, grm = cohort
     prec = GRM_BF16X3_TC if split else GRM_BF16_TC
-    prev = ctx.get_tc_clusters()
+    prev = ctx.tc_options()
     try:
-        ctx.set_tc_clusters(1, 1)
-        ctx.grm_build(prec)
-        K1 = ctx.grm_get()
-        for c in (2, 4):
-            ctx.set_tc_clusters(c, 1)
+        for n, m in ((grm.n, 1900), (600, 1300)):  # 6 and 5 row blocks of 128
+            if n != grm.n:
+                bed, _ = synth.synth_bed(33, n, m, 0.01)
+                ctx.setgeno(bed, n, m)
+                g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+                Kref = aireml.DenseGRM(g).K
+            else:
+                Kref = grm.K
+            ctx.set_tc_option(TC_SYRK_PAIR, 0)
+            ctx.set_tc_option(TC_SYRK_GROUP, 16)
             ctx.grm_build(prec)
-            assert np.array_equal(ctx.grm_get(), K1), c
+            K1 = ctx.grm_get()
+            tol = 2e-5 * np.abs(Kref).max() if split else 2e-3
+            assert np.abs(K1 - Kref).max() < tol
+            for pair, group in ((0, 1), (1, 1), (1, 2), (1, 16)):
+                ctx.set_tc_option(TC_SYRK_PAIR, pair)
+                ctx.set_tc_option(TC_SYRK_GROUP, group)
+                ctx.grm_build(prec)
+                assert np.array_equal(ctx.grm_get(), K1), (n, pair, group)
     finally:
-        ctx.set_tc_clusters(*prev)
+        ctx.set_tc_options(prev)
+        bed, _ = synth.synth_bed(31, grm.n, 1900, 0.01)
+        ctx.setgeno(bed, grm.n, 1900)
 
 
 @pytest.mark.parametrize("mode", ["tf32x3", "bf16x3"])
-def test_grmv_cluster_variants_bit_identical(cohort, mode):
-    from saigegpu import MV_BF16X3_TC, MV_TF32X3_TC
+def test_grmv_shape_variants_bit_identical(cohort, mode):
+    """Every tile width of the split GRM.V against FP64, and for split-BF16 every (CTA pair, K slice)
+    variant the tuner chooses from, bit for bit."""
+    from saigegpu import MV_BF16X3_TC, MV_TF32X3_TC, tune
     ctx, grm = cohort
     ctx.grm_build(GRM_FP32_SIMT)
     Kg = ctx.grm_get().astype(np.float64)  # the resident FP32 K the split halves come from
@@ -99,23 +118,46 @@ def test_grmv_cluster_variants_bit_identical(cohort, mode):
     # split TF32: ~21 significant bits per operand (the MMA reads the low halves at TF32
     # precision); split BF16: 16.  Both accumulate in the tensor cores' FP32 over n terms.
     tol = 2e-5 if mode == "tf32x3" else 6e-5
-    prev = ctx.get_tc_clusters()
+    prev = ctx.grmv_plan()
+    variants = tune.GRMV_VARIANTS if mode == "bf16x3" else ((0, 0),)
     try:
         ctx.set_matvec_mode(MV_TF32X3_TC if mode == "tf32x3" else MV_BF16X3_TC)
         # every tile width: split-TF32 pads to multiples of 32; split-BF16 to multiples of 16 (32, 48,
         # 80, 112, 144, 160, 176, 208, 256, 256 here), where the odd multiples of 16 end on half a
-        # 32-column epilogue chunk and run clusters of at most 2
+        # 32-column epilogue chunk
         for k in (32, 40, 70, 100, 140, 150, 170, 200, 256, 512):
             V = rng.standard_normal((grm.n, k))
-            ctx.set_tc_clusters(1, 1)
+            ctx.set_grmv_plan([(1 << 30,) + variants[0]])
             Y1 = ctx.grm_matmul(V)
             ref = Kg @ V
             assert np.abs(Y1 - ref).max() / np.abs(ref).max() < tol, k
-            for c in (2, 4):
-                ctx.set_tc_clusters(1, c)
-                assert np.array_equal(ctx.grm_matmul(V), Y1), (k, c)
+            for v in variants[1:]:
+                ctx.set_grmv_plan([(1 << 30,) + v])
+                assert np.array_equal(ctx.grm_matmul(V), Y1), (k, v)
     finally:
-        ctx.set_tc_clusters(*prev)
+        ctx.set_grmv_plan(prev)
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+
+
+def test_grmv_bf16x3_every_tile_width_and_variant(cohort):
+    """Every split-BF16 tile width (multiples of 16 up to 256) launches with every (CTA pair, K slice)
+    variant and gives the same product."""
+    from saigegpu import MV_BF16X3_TC, tune
+    ctx, grm = cohort
+    ctx.grm_build(GRM_FP32_SIMT)
+    rng = np.random.default_rng(4)
+    prev = ctx.grmv_plan()
+    try:
+        ctx.set_matvec_mode(MV_BF16X3_TC)
+        for k in range(16, 513, 16):
+            V = rng.standard_normal((grm.n, k))
+            ctx.set_grmv_plan([(1 << 30,) + tune.GRMV_VARIANTS[0]])
+            Y1 = ctx.grm_matmul(V)
+            for v in tune.GRMV_VARIANTS[1:]:
+                ctx.set_grmv_plan([(1 << 30,) + v])
+                assert np.array_equal(ctx.grm_matmul(V), Y1), (k, v)
+    finally:
+        ctx.set_grmv_plan(prev)
         ctx.set_matvec_mode(MV_FP32_SIMT)
 
 

@@ -116,7 +116,14 @@ def test_glm_score_equations():
 
 
 def test_golden_theta_monte_carlo_band(golden_plink):
-    """The reference's example fits pin tau only loosely (probes and VR markers come from R's RNG)."""
+    """The reference's example fits pin tau only loosely (probes and VR markers come from R's RNG).
+
+    Over 20 probe seeds and random VR-marker draws (none, single-ratio and categorical exclusion
+    from the GRM) the oracle gives binary tau1 0.258 +- 0.040 (golden 0.335: +1.9 sd) and
+    quantitative tau (0.238 +- 0.006, 0.451 +- 0.009) against the golden (0.201, 0.483), whose sum
+    agrees to 0.6%.  At the golden tau the oracle's linear predictors differ from the golden ones by
+    9% (quantitative) and 2% (binary), so the golden fits come from a different Sigma than the
+    reference's code path restated here; the quantitative band below is that systematic gap."""
     bed, n, m, ph = golden_plink
     gold = json.load(open(os.path.join(GOLDEN, "golden_fits.json")))
     g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
@@ -125,14 +132,15 @@ def test_golden_theta_monte_carlo_band(golden_plink):
     fb = prep.make_fit0(ph["y_binary"], cov, "binary", True)
     rb = aireml.glmmkin_binary(grm, fb)
     t_gold = gold["example_binary_fullGRM"]["theta"][1]
-    # Monte-Carlo spread of tau1 over probe seeds here is ~0.034 (sd); allow 4 sd
-    assert abs(rb["theta"][1] - t_gold) < 4 * 0.034
+    # Monte-Carlo spread of tau1 over probe seeds and VR draws here is 0.040 (sd); allow 3 sd
+    assert abs(rb["theta"][1] - t_gold) < 3 * 0.040
     assert abs(rb["coefficients"][0] - gold["example_binary_fullGRM"]["coefficients"][0]) < 0.05
     fq = prep.make_fit0(ph["y_quantitative"], cov, "quantitative", True)
     rq = aireml.glmmkin_quantitative(grm, fq)
     tq = np.array(gold["example_quantitative_fullGRM"]["theta"])
-    assert np.all(np.abs(rq["theta"] - tq) / tq < 0.25)
-    assert abs(rq["theta"].sum() - tq.sum()) / tq.sum() < 0.05
+    rel = np.abs(rq["theta"] - tq) / tq
+    assert rel[0] < 0.25 and rel[1] < 0.10, rel
+    assert abs(rq["theta"].sum() - tq.sum()) / tq.sum() < 0.02
 
 
 def test_c_restatement_of_reference_cpu_path():
@@ -190,3 +198,34 @@ def test_output_writers_roundtrip(tmp_path):
     output.write_model(tmp_path / "m.json", fit, "binary", ["a", "b"])
     d = output.read_model(tmp_path / "m.json")
     assert d["theta"].tolist() == [1, 0.3] and d["sampleID"] == ["a", "b"]
+
+
+def test_categorical_variance_ratio_oracle_on_golden(golden_plink):
+    """Two MAC categories (10 < MAC <= 20.5 and MAC > 20.5, the fitNULLGLMM defaults) on the
+    reference's example: every marker of the first category and the random draw's markers above
+    leave the GRM; each category's null VR lands near the golden two-category file
+    (example_binary_fullGRM.varianceRatio.txt: 0.9456 and 0.9400)."""
+    from saigegpu import vr as vrmod
+    bed, n, m, ph = golden_plink
+    rng = np.random.default_rng(5)
+    vr_rand = np.unique(rng.integers(0, m, 1000))
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15, vr_rand, 10.0, True,
+                      max_mac_vr=20.5)
+    cats = vrmod.category_markers(g.vr_mac)
+    assert len(cats) == 2 and all(len(c) >= 30 for c in cats)
+    assert np.all(g.vr_mac[cats[0]] <= 20) and np.all(g.vr_mac[cats[1]] > 20)
+    # categorical selection: every marker with 10 <= MAC < 20.5 is a variance-ratio marker
+    g1 = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15, None, 10.0, True,
+                       max_mac_vr=20.5)
+    assert np.all((g1.vr_mac >= 10) & (g1.vr_mac < 20.5))
+    grm = aireml.DenseGRM(g)
+    cov = np.column_stack([ph["x1"], ph["x2"]])
+    f0 = prep.make_fit0(ph["y_binary"], cov, "binary", True)
+    fit = aireml.glmmkin_binary(grm, f0)
+    orders = [c[rng.permutation(len(c))] for c in cats]
+    vrs = aireml.categorical_variance_ratio(grm, fit, "binary", f0["Xorig"], g.vr_codes, orders)
+    gold = json.load(open(os.path.join(GOLDEN, "golden_fits.json")))["variance_ratio_null"]["example_binary_fullGRM"]
+    # measured 0.952-0.962 over three random draws against the golden 0.9456 / 0.9400: the
+    # golden run's probes, marker draw and tau (0.335 there, 0.24-0.29 here) come from R's RNG
+    for v, gv in zip(vrs, gold):
+        assert abs(v - gv) < 0.03, (vrs, gold)

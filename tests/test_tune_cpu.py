@@ -1,12 +1,22 @@
-"""Cluster-size choice of the autotuner (host logic only)."""
+"""Variant choice of the autotuner (host logic only)."""
 from saigegpu import tune
 
 
-def test_pick_keeps_smaller_cluster_within_margin():
-    # the split GRM.V at 128-256 columns: 2- and 4-CTA clusters within timing noise -> keep 2
-    assert tune._pick({1: 30.0, 2: 29.05, 4: 29.06}, (1, 2, 4)) == 2
-    assert tune._pick({1: 30.0, 2: 29.05, 4: 28.9}, (1, 2, 4)) == 2
-    # the SYRK: 4-CTA clusters clearly faster -> 4
-    assert tune._pick({1: 2.01, 2: 1.25, 4: 1.137}, (1, 2, 4)) == 4
-    # nothing beats 1 by the margin -> 1
-    assert tune._pick({1: 10.0, 2: 9.9, 4: 9.85}, (1, 2, 4)) == 1
+def test_pick_keeps_first_variant_within_margin():
+    v = tune.GRMV_VARIANTS
+    # within timing noise of the first variant -> keep it
+    assert tune._pick({v[0]: 30.0, v[1]: 29.7, v[2]: 29.6, v[3]: 29.5}, v) == v[0]
+    # a clear win -> the fastest clear winner in order
+    assert tune._pick({v[0]: 30.0, v[1]: 29.05, v[2]: 28.0, v[3]: 27.9}, v) == v[2]
+    s = tune.SYRK_VARIANTS
+    assert tune._pick({s[0]: 2.01, s[1]: 1.25, s[2]: 1.137, s[3]: 1.14}, s) == s[2]
+
+
+def test_report_json_keys():
+    rep = {"syrk": {"times_ms": {(0, 16): 1900.0, (1, 16): 1200.0}, "chosen": (1, 16)},
+           "grmv": {32: {"times_ms": {(0, 128): 6.5, (1, 64): 6.4}, "chosen": (0, 128)}},
+           "plan": [(32, 0, 128)]}
+    out = tune.report_json(rep)
+    assert out["syrk"]["chosen"] == {"pair": 1, "group": 16}
+    assert out["grmv"]["32"]["times_ms"]["pair1_slice64"] == 6.4
+    assert out["plan"] == [[32, 0, 128]]
