@@ -91,7 +91,10 @@ enum sg_tc_option {
   SG_TC_SYRK_GROUP = 3,  /* row tiles per raster group of the SYRK (1..4096); default 16 */
   SG_TC_GRMV_SLICE = 4,  /* K slice bytes per pipeline stage of the split-BF16 GRM.V: 0 = by
                             width (128 up to 160 columns, else 64), 64 or 128; default 0 */
-  SG_TC_SUBSET_PAIR = 5  /* 1: the subset-exact engine's genotype GEMMs on CTA pairs; default 0 */
+  SG_TC_SUBSET_PAIR = 5, /* the subset-exact engine's genotype GEMMs on CTA pairs: 0 never,
+                            1 always, 2 above 160 columns (default) */
+  SG_TC_SUBSET_SLICE = 6 /* their K slice bytes per pipeline stage: 0 = by width (128 up to 160
+                            columns, else 64), 64 or 128 (default) */
 };
 int sg_set_tc_option(sg_ctx *ctx, int option, int value);
 int sg_get_tc_option(sg_ctx *ctx, int option, int *value);

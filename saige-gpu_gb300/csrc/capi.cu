@@ -125,7 +125,7 @@ struct Engine {
     int32_t* flips = nullptr;     // fill-changed markers
     float* dfill = nullptr;
     int64_t flip_cap = 0;
-    uint32_t* bits = nullptr;     // np x W bit map
+    uint32_t* bits = nullptr;     // W x np bit map (word-major)
     int64_t bits_cap = 0;
     double* diag = nullptr;       // np: sum of z'^2 (the preconditioner's diagonal)
     SubsetSlot dev;               // what d_slots[slot] holds

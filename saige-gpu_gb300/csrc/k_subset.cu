@@ -80,8 +80,9 @@ void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int
                                           static_cast<__nv_bfloat16*>(Gsm));
 }
 
-// Bit map of a slot's fill-changed markers: word w of sample i has bit b set when marker
-// flips[32 w + b] is missing at sample i and i is in the subset (mask).
+// Bit map of a slot's fill-changed markers, word-major (word w of sample i at bits[w * np + i], so
+// that a warp's samples read consecutive words): bit b is set when marker flips[32 w + b] is
+// missing at sample i and i is in the subset (mask).
 __global__ void subset_bitmap_kernel(const uint8_t* __restrict__ codes, int64_t pitch,
                                      const int32_t* __restrict__ flips, int nflip, int W,
                                      const uint8_t* __restrict__ mask, int64_t nn, int64_t np,
@@ -99,7 +100,7 @@ __global__ void subset_bitmap_kernel(const uint8_t* __restrict__ codes, int64_t 
       if (f == 1u) word |= 1u << b;
     }
   }
-  bits[i * W + w] = word;
+  bits[(int64_t)w * np + i] = word;
 }
 
 void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* flips, int nflip, int W,
@@ -205,8 +206,9 @@ __global__ void subset_flip_t_kernel(const __nv_bfloat16* __restrict__ Vh, const
   float acc[32];
 #pragma unroll
   for (int b = 0; b < 32; ++b) acc[b] = 0.0f;
+  const uint32_t* bw = sl.bits + (int64_t)w * np;
   for (int64_t i = threadIdx.x; i < nn; i += kThreads) {
-    const uint32_t word = sl.bits[i * sl.W + w];
+    const uint32_t word = bw[i];
     if (word == 0u) continue;
     const float v = __bfloat162float(Vh[j * np + i]) + __bfloat162float(Vl[j * np + i]);
 #pragma unroll
@@ -285,7 +287,7 @@ __global__ void subset_finalize_kernel(const float* __restrict__ U, int64_t np, 
     if (i < nn && winv[(int64_t)slot * np + i] != 0.0) {
       double du = 0.0;
       for (int w = 0; w < sl.W; ++w) {
-        uint32_t word = sl.bits[i * sl.W + w];
+        uint32_t word = sl.bits[(int64_t)w * np + i];
         while (word) {
           const int b = __ffs(word) - 1;
           word &= word - 1u;

@@ -795,7 +795,8 @@ static int g_opt[kTcOptions] = {
     512,  // kTcDrainBytes: bytes of K per row one TMEM accumulator takes before it is drained
     16,   // kTcSyrkGroup: row tiles per raster group of the SYRK
     0,    // kTcGrmvSlice: K slice bytes of the split-BF16 GRM.V (0: by width, 64 or 128)
-    0,    // kTcSubsetPair: subset-exact genotype GEMMs on CTA pairs
+    2,    // kTcSubsetPair: subset-exact genotype GEMMs on CTA pairs (2: above 160 columns)
+    128,  // kTcSubsetSlice: their K slice bytes (0: 128 up to 160 columns, else 64; or 64 / 128)
 };
 
 bool tc_set_option(int opt, int value) {
@@ -803,8 +804,10 @@ bool tc_set_option(int opt, int value) {
   switch (opt) {
     case kTcSyrkPair:
     case kTcGrmvPair:
-    case kTcSubsetPair:
       if (value != 0 && value != 1) return false;
+      break;
+    case kTcSubsetPair:
+      if (value < 0 || value > 2) return false;
       break;
     case kTcDrainBytes:  // whole 128-byte stages, at most 4 KB (the bias grows with the length)
       if (value < 128 || value > 4096 || value % 128 != 0) return false;
@@ -813,6 +816,7 @@ bool tc_set_option(int opt, int value) {
       if (value < 1 || value > 4096) return false;
       break;
     case kTcGrmvSlice:
+    case kTcSubsetSlice:
       if (value != 0 && value != 64 && value != 128) return false;
       break;
   }
@@ -948,6 +952,13 @@ int tc_gemm_tile_n(int64_t ncols, int set) {
   return set == kTilesSplitBF16 ? 16 : 32;
 }
 
+// CTA pairs for a subset-exact genotype GEMM over ncols columns: measured at N = 100k, M = 150k,
+// 128-byte K slices, pairs took 512 columns from 49.7 to 36.5 ms and 1024 from 89.2 to 72.7 ms,
+// and were 7-11% slower up to 128 columns, where the launch streams G from HBM.
+static bool subset_pair(int64_t ncols) {
+  return g_opt[kTcSubsetPair] == 2 ? ncols > 160 : g_opt[kTcSubsetPair] != 0;
+}
+
 // Columns one GRM.V launch covers for ncols32 (a multiple of 16) live columns, padded so that the
 // modelled cost is lowest, capped at cap columns.  Cost model (L2->SM bytes of one pass, which
 // bounds these kernels, over the fraction of the last wave of 1-tile-per-SM(-pair) tiles that is
@@ -960,7 +971,7 @@ int64_t tc_grmv_padded_cols(int64_t ncols32, int64_t cap, int64_t np, int set, i
     const int64_t padded = (ncols32 + w - 1) / w * w;
     if (padded > cap) continue;
     const bool pair = (set == kTilesSplitBF16 && grmv_choice(padded).pair != 0) ||
-                      (set == kTilesSplitB && g_opt[kTcSubsetPair] != 0);
+                      (set == kTilesSplitB && subset_pair(padded));
     const int64_t nrt = pair ? (np / kTileM + 1) / 2 : np / kTileM;
     const int64_t slots = pair ? num_sms / 2 : num_sms;
     const int bn = tc_gemm_tile_n(padded, set);
@@ -1182,15 +1193,18 @@ cudaError_t tc_gemm_bf16x3(const void* Kh, const void* Kl, int64_t np, const voi
 
 // D = A (Bh + Bl)^T: A (rows x kdim) exact in BF16 (genotype values), B as BF16 high + low halves
 // (ncols x kdim), two products per K step into the drained TMEM accumulators; D RHS-major (column j
-// of the product is row j of D, leading dimension ldd).  64-byte K slices, as many stages as fit.
+// of the product is row j of D, leading dimension ldd).  K slices of 128 bytes by default (each
+// 128-byte row segment of A is a whole DRAM burst line; measured at N = 100k, M = 150k they took
+// 32-128 columns from 23-24 ms to 16 ms and, on CTA pairs, 512 columns from 54 to 36.5 ms), or
+// 64 bytes (twice the stages); as many stages as fit.
 cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void* Bh, const void* Bl,
                            int64_t ncols, float* D, int64_t ldd, cudaStream_t s, bool check, int site) {
-  if (rows % kTileM != 0 || kdim % 32 != 0 || ncols % 32 != 0 || ncols <= 0 || !A || !Bh || !Bl || site < 0 ||
+  if (rows % kTileM != 0 || kdim % 64 != 0 || ncols % 32 != 0 || ncols <= 0 || !A || !Bh || !Bl || site < 0 ||
       site > 1)
     return cudaErrorInvalidValue;
   const int BN = tc_gemm_tile_n(ncols, kTilesSplitB);
-  const bool pair = g_opt[kTcSubsetPair] != 0;
-  constexpr int RB = 64;
+  const bool pair = subset_pair(ncols);
+  const int RB = g_opt[kTcSubsetSlice] != 0 ? g_opt[kTcSubsetSlice] : (ncols <= 160 ? 128 : 64);
   const uint64_t rb = (uint64_t)kdim * 2;
   CUtensorMap a, b, b2;
   if (!make_map(&a, A, false, kdim, rows, rb, kTileM, RB) ||
@@ -1206,34 +1220,61 @@ cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void
   const int num_kb = (int)(kdim / (RB / 2));
   const int nt = (int)cache.host.size();
   const int dk = drain_stages(RB);
-#define SG_SB(BNv, Sv, Pv)                                                                                  \
-  case BNv:                                                                                                 \
-    e = launch<false, BNv, Sv, kSplitB, Pv, RB>(a, b, a, b2, cache.dev, nt, num_kb, dk, D, ldd, 1.0f, 1, s, \
-                                                 rows);                                                    \
+#define SG_SB(BNv, Sv, Pv, RBv)                                                                              \
+  case BNv:                                                                                                  \
+    e = launch<false, BNv, Sv, kSplitB, Pv, RBv>(a, b, a, b2, cache.dev, nt, num_kb, dk, D, ldd, 1.0f, 1, s, \
+                                                  rows);                                                    \
     break;
-  if (pair) {
+  // per CTA and stage: 128 A rows plus two halves of BN (BN / 2 on a CTA pair) B rows, RB bytes each
+  if (RB == 128 && pair) {
     switch (BN) {
-      SG_SB(256, 9, true)
-      SG_SB(224, 10, true)
-      SG_SB(192, 11, true)
-      SG_SB(160, 12, true)
-      SG_SB(128, 12, true)
-      SG_SB(96, 12, true)
-      SG_SB(64, 12, true)
-      SG_SB(32, 12, true)
+      SG_SB(256, 4, true, 128)
+      SG_SB(224, 4, true, 128)
+      SG_SB(192, 5, true, 128)
+      SG_SB(160, 6, true, 128)
+      SG_SB(128, 7, true, 128)
+      SG_SB(96, 8, true, 128)
+      SG_SB(64, 9, true, 128)
+      SG_SB(32, 11, true, 128)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else if (RB == 128) {
+    switch (BN) {
+      SG_SB(256, 2, false, 128)
+      SG_SB(224, 3, false, 128)
+      SG_SB(192, 3, false, 128)
+      SG_SB(160, 4, false, 128)
+      SG_SB(128, 4, false, 128)
+      SG_SB(96, 5, false, 128)
+      SG_SB(64, 7, false, 128)
+      SG_SB(32, 9, false, 128)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else if (pair) {
+    switch (BN) {
+      SG_SB(256, 9, true, 64)
+      SG_SB(224, 10, true, 64)
+      SG_SB(192, 11, true, 64)
+      SG_SB(160, 12, true, 64)
+      SG_SB(128, 12, true, 64)
+      SG_SB(96, 12, true, 64)
+      SG_SB(64, 12, true, 64)
+      SG_SB(32, 12, true, 64)
       default:
         return cudaErrorInvalidValue;
     }
   } else {
     switch (BN) {
-      SG_SB(256, 5, false)
-      SG_SB(224, 6, false)
-      SG_SB(192, 7, false)
-      SG_SB(160, 8, false)
-      SG_SB(128, 9, false)
-      SG_SB(96, 11, false)
-      SG_SB(64, 12, false)
-      SG_SB(32, 12, false)
+      SG_SB(256, 5, false, 64)
+      SG_SB(224, 6, false, 64)
+      SG_SB(192, 7, false, 64)
+      SG_SB(160, 8, false, 64)
+      SG_SB(128, 9, false, 64)
+      SG_SB(96, 11, false, 64)
+      SG_SB(64, 12, false, 64)
+      SG_SB(32, 12, false, 64)
       default:
         return cudaErrorInvalidValue;
     }

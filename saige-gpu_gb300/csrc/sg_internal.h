@@ -109,9 +109,10 @@ cudaError_t tc_wait_selftest(double budget_ms, int* waited_out, cudaStream_t s);
 // Shape options of the tcgen05 GEMMs (process-wide), in the order of sg_tc_option (saigegpu.h):
 // SYRK on CTA pairs, split-BF16 GRM.V on CTA pairs, drain length (bytes of K per row per TMEM
 // accumulator chunk), SYRK raster group (row tiles), split-BF16 GRM.V K slice bytes (0 = by width).
-// The last one: the subset-exact genotype GEMMs on CTA pairs.
+// Then the subset-exact genotype GEMMs on CTA pairs (0 never, 1 always, 2 above 160 columns) and
+// their K slice bytes (0 = by width).
 enum { kTcSyrkPair = 0, kTcGrmvPair = 1, kTcDrainBytes = 2, kTcSyrkGroup = 3, kTcGrmvSlice = 4, kTcSubsetPair = 5,
-       kTcOptions = 6 };
+       kTcSubsetSlice = 6, kTcOptions = 7 };
 bool tc_set_option(int opt, int value);
 int tc_get_option(int opt);
 // Split-BF16 GRM.V choices per launch width (n buckets, max_cols increasing; n = 0 clears).
@@ -196,7 +197,8 @@ struct SubsetSlot {
   const float* p2;        // mg: 2 p' (the subset's allele frequency, FP32 as the reference's LUT)
   const int32_t* flips;   // nflip markers whose subset fill differs from the cohort fill in G
   const float* dfill;     // nflip: subset fill - cohort fill
-  const uint32_t* bits;   // np x W: bit b of word w = sample misses marker flips[32 w + b] (in S)
+  const uint32_t* bits;   // W x np (word-major): bit b of word w of sample i = i misses marker
+                          // flips[32 w + b] (i in S)
   int32_t nflip = 0, W = 0;
   double inv_m = 0.0;     // 1 / M' (the subset's GRM marker count)
   double ns = 1.0;        // subset size

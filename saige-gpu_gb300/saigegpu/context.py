@@ -14,9 +14,11 @@ from . import _lib as L
 GRM_FP32_SIMT, GRM_BF16_TC, GRM_BF16X3_TC = 0, 1, 2
 MV_FP32_SIMT, MV_TF32_TC, MV_FP64_PLAIN, MV_TF32X3_TC, MV_BF16X3_TC, MV_SUBSET_EXACT = 0, 1, 2, 3, 4, 5
 # tcgen05 GEMM shape options (enum sg_tc_option)
-TC_SYRK_PAIR, TC_GRMV_PAIR, TC_DRAIN_BYTES, TC_SYRK_GROUP, TC_GRMV_SLICE, TC_SUBSET_PAIR = 0, 1, 2, 3, 4, 5
+TC_SYRK_PAIR, TC_GRMV_PAIR, TC_DRAIN_BYTES, TC_SYRK_GROUP, TC_GRMV_SLICE = 0, 1, 2, 3, 4
+TC_SUBSET_PAIR, TC_SUBSET_SLICE = 5, 6
 TC_OPTIONS = {"syrk_pair": TC_SYRK_PAIR, "grmv_pair": TC_GRMV_PAIR, "drain_bytes": TC_DRAIN_BYTES,
-              "syrk_group": TC_SYRK_GROUP, "grmv_slice": TC_GRMV_SLICE, "subset_pair": TC_SUBSET_PAIR}
+              "syrk_group": TC_SYRK_GROUP, "grmv_slice": TC_GRMV_SLICE, "subset_pair": TC_SUBSET_PAIR,
+              "subset_slice": TC_SUBSET_SLICE}
 
 
 def _f32(a):

@@ -10,7 +10,8 @@ import numpy as np
 import pytest
 
 from oracle import aireml, plink
-from saigegpu import MV_FP32_SIMT, MV_SUBSET_EXACT, TC_SUBSET_PAIR, native, prep, serve, synth
+from saigegpu import (MV_FP32_SIMT, MV_SUBSET_EXACT, TC_SUBSET_PAIR, TC_SUBSET_SLICE, native, prep, serve,
+                      synth)
 
 pytestmark = pytest.mark.gpu
 
@@ -69,8 +70,9 @@ def test_subset_exact_products_match_oracle(exact_cohort):
     rng = np.random.default_rng(5)
     ctx.set_matvec_mode(MV_SUBSET_EXACT)
     try:
-        for pair in (0, 1):
+        for pair, sl in ((0, 64), (1, 128), (2, 128)):
             ctx.set_tc_option(TC_SUBSET_PAIR, pair)
+            ctx.set_tc_option(TC_SUBSET_SLICE, sl)
             ctx.engine_reserve(128, len(cases))
             ids = []
             Vs = []
@@ -89,7 +91,30 @@ def test_subset_exact_products_match_oracle(exact_cohort):
                 err = np.abs(Y - ref).max() / np.abs(ref).max()
                 assert err < 6e-5, (pair, trait, err)
     finally:
-        ctx.set_tc_option(TC_SUBSET_PAIR, 0)
+        ctx.set_tc_option(TC_SUBSET_PAIR, 2)
+        ctx.set_tc_option(TC_SUBSET_SLICE, 128)
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+
+
+def test_subset_exact_variants_bit_identical(exact_cohort):
+    """CTA pairs and K slices of the genotype GEMMs give the same products, bit for bit, at every
+    launch width (one column to wide blocks)."""
+    ctx, bed, _, cases = exact_cohort
+    rng = np.random.default_rng(6)
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    try:
+        for k in (1, 40, 200, 300):
+            V = rng.standard_normal((N, k))
+            outs = []
+            for pair, sl in ((0, 64), (0, 128), (1, 64), (1, 128)):
+                ctx.set_tc_option(TC_SUBSET_PAIR, pair)
+                ctx.set_tc_option(TC_SUBSET_SLICE, sl)
+                outs.append(ctx.grm_matmul(V))
+            for o in outs[1:]:
+                np.testing.assert_array_equal(o, outs[0])
+    finally:
+        ctx.set_tc_option(TC_SUBSET_PAIR, 2)
+        ctx.set_tc_option(TC_SUBSET_SLICE, 128)
         ctx.set_matvec_mode(MV_FP32_SIMT)
 
 
