@@ -479,6 +479,11 @@ def run_ours(args, rank, world, local):
             "fp32": MV_FP32_SIMT}[args.mode]
     ctx.set_matvec_mode(mode)
     g_ms = ctx.build_timing()["zbuild_ms"] if exact else None  # the genotype matrix build
+    if exact and tune_report is not None:
+        # CTA pairs and K slices of the genotype GEMMs per launch width, from measured times
+        from saigegpu import tune
+        tune_report["subset"] = tune.tune_subset(ctx)
+        tune_report["subset_plan"] = ctx.subset_plan()
     from saigegpu import serve as _serve
     cols = _serve.columns_for(specs)
     setup_s = time.perf_counter() - t_setup

@@ -106,6 +106,11 @@ int sg_get_tc_option(sg_ctx *ctx, int option, int *value);
 int sg_set_grmv_plan(sg_ctx *ctx, int n, const int32_t *max_cols, const int32_t *pair,
                      const int32_t *slice);
 int sg_get_grmv_plan(sg_ctx *ctx, int cap, int32_t *max_cols, int32_t *pair, int32_t *slice, int *n);
+/* The same per-width table for the subset-exact engine's genotype GEMMs (SG_TC_SUBSET_PAIR and
+ * SG_TC_SUBSET_SLICE per bucket; slice 64 or 128).  No reference counterpart. */
+int sg_set_subset_plan(sg_ctx *ctx, int n, const int32_t *max_cols, const int32_t *pair,
+                       const int32_t *slice);
+int sg_get_subset_plan(sg_ctx *ctx, int cap, int32_t *max_cols, int32_t *pair, int32_t *slice, int *n);
 /* GPU kernel launches issued by this context so far (for accounting). */
 int sg_kernel_launches(const sg_ctx *ctx, uint64_t *count);
 

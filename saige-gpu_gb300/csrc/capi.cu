@@ -504,6 +504,20 @@ extern "C" int sg_set_vr_max_mac(sg_ctx* c, float max_mac) {
   return SG_OK;
 }
 
+extern "C" int sg_set_subset_plan(sg_ctx* c, int n, const int32_t* max_cols, const int32_t* pair,
+                                  const int32_t* slice) {
+  if (!c || n < 0 || n > 64 || (n > 0 && (!max_cols || !pair || !slice))) return SG_ERR_INVALID;
+  if (!tc_set_subset_plan(max_cols, pair, slice, n))
+    return set_err(c, SG_ERR_INVALID, "plan buckets need increasing max_cols, pair 0/1 and slice 64/128");
+  return SG_OK;
+}
+
+extern "C" int sg_get_subset_plan(sg_ctx* c, int cap, int32_t* max_cols, int32_t* pair, int32_t* slice, int* n) {
+  if (!c || !n || cap < 0 || (cap > 0 && (!max_cols || !pair || !slice))) return SG_ERR_INVALID;
+  *n = tc_get_subset_plan(max_cols, pair, slice, cap);
+  return SG_OK;
+}
+
 extern "C" int sg_kernel_launches(const sg_ctx* c, uint64_t* count) {
   if (!c || !count) return SG_ERR_INVALID;
   *count = c->launches;

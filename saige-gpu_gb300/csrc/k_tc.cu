@@ -862,6 +862,30 @@ static GrmvChoice grmv_choice(int64_t ncols) {
   return GrmvChoice{0, g_opt[kTcGrmvPair], g_opt[kTcGrmvSlice]};
 }
 
+// The same kind of table for the subset-exact engine's genotype GEMMs.
+static std::vector<GrmvChoice> g_subset_plan;
+
+bool tc_set_subset_plan(const int32_t* max_cols, const int32_t* pair, const int32_t* slice, int n) {
+  std::vector<GrmvChoice> plan;
+  for (int i = 0; i < n; ++i) {
+    if (max_cols[i] <= 0 || (i > 0 && max_cols[i] <= max_cols[i - 1])) return false;
+    if ((pair[i] != 0 && pair[i] != 1) || (slice[i] != 64 && slice[i] != 128)) return false;
+    plan.push_back(GrmvChoice{max_cols[i], pair[i], slice[i]});
+  }
+  g_subset_plan.swap(plan);
+  return true;
+}
+
+int tc_get_subset_plan(int32_t* max_cols, int32_t* pair, int32_t* slice, int cap) {
+  const int n = (int)g_subset_plan.size();
+  for (int i = 0; i < n && i < cap; ++i) {
+    max_cols[i] = (int32_t)g_subset_plan[i].max_cols;
+    pair[i] = g_subset_plan[i].pair;
+    slice[i] = g_subset_plan[i].slice;
+  }
+  return n;
+}
+
 static int drain_stages(int rb) { return g_opt[kTcDrainBytes] / rb > 0 ? g_opt[kTcDrainBytes] / rb : 1; }
 
 // Lower-triangle tiles of the SYRK in raster groups: ``group`` consecutive row tiles (of ``unit``
@@ -956,7 +980,15 @@ int tc_gemm_tile_n(int64_t ncols, int set) {
 // 128-byte K slices, pairs took 512 columns from 49.7 to 36.5 ms and 1024 from 89.2 to 72.7 ms,
 // and were 7-11% slower up to 128 columns, where the launch streams G from HBM.
 static bool subset_pair(int64_t ncols) {
+  for (const GrmvChoice& b : g_subset_plan)
+    if (ncols <= b.max_cols) return b.pair != 0;
   return g_opt[kTcSubsetPair] == 2 ? ncols > 160 : g_opt[kTcSubsetPair] != 0;
+}
+
+static int subset_slice(int64_t ncols) {
+  for (const GrmvChoice& b : g_subset_plan)
+    if (ncols <= b.max_cols) return b.slice;
+  return g_opt[kTcSubsetSlice] != 0 ? g_opt[kTcSubsetSlice] : (ncols <= 160 ? 128 : 64);
 }
 
 // Columns one GRM.V launch covers for ncols32 (a multiple of 16) live columns, padded so that the
@@ -1204,7 +1236,7 @@ cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void
     return cudaErrorInvalidValue;
   const int BN = tc_gemm_tile_n(ncols, kTilesSplitB);
   const bool pair = subset_pair(ncols);
-  const int RB = g_opt[kTcSubsetSlice] != 0 ? g_opt[kTcSubsetSlice] : (ncols <= 160 ? 128 : 64);
+  const int RB = subset_slice(ncols);
   const uint64_t rb = (uint64_t)kdim * 2;
   CUtensorMap a, b, b2;
   if (!make_map(&a, A, false, kdim, rows, rb, kTileM, RB) ||

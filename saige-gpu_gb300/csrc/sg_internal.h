@@ -118,6 +118,9 @@ int tc_get_option(int opt);
 // Split-BF16 GRM.V choices per launch width (n buckets, max_cols increasing; n = 0 clears).
 bool tc_set_grmv_plan(const int32_t* max_cols, const int32_t* pair, const int32_t* slice, int n);
 int tc_get_grmv_plan(int32_t* max_cols, int32_t* pair, int32_t* slice, int cap);
+// The same for the subset-exact engine's genotype GEMMs (slice 64 or 128).
+bool tc_set_subset_plan(const int32_t* max_cols, const int32_t* pair, const int32_t* slice, int n);
+int tc_get_subset_plan(int32_t* max_cols, int32_t* pair, int32_t* slice, int cap);
 // GRM.V column-tile width sets: plain TF32 / FP32, split-TF32, split-BF16 (multiples of 16), and
 // the subset-exact genotype GEMMs (multiples of 32)
 enum { kTilesPlain = 0, kTilesSplitTF32 = 1, kTilesSplitBF16 = 2, kTilesSplitB = 3 };

@@ -40,6 +40,8 @@ SIGNATURES = {
     "sg_get_tc_option": [c_ctx, C.c_int, P_i32],
     "sg_set_grmv_plan": [c_ctx, C.c_int, P_i32, P_i32, P_i32],
     "sg_get_grmv_plan": [c_ctx, C.c_int, P_i32, P_i32, P_i32, C.POINTER(C.c_int)],
+    "sg_set_subset_plan": [c_ctx, C.c_int, P_i32, P_i32, P_i32],
+    "sg_get_subset_plan": [c_ctx, C.c_int, P_i32, P_i32, P_i32, C.POINTER(C.c_int)],
     "sg_setgeno": [c_ctx, P_u8, c_u64, c_i64, c_i64, P_i32, c_i64, P_u8, C.c_float, C.c_float,
                    P_i32, c_i64, C.c_float, C.c_int, C.c_int],
     "sg_setgeno_files": [c_ctx, C.c_char_p, C.c_char_p, C.c_char_p, P_i32, c_i64, P_u8, C.c_float,

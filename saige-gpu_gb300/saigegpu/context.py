@@ -106,23 +106,36 @@ class Context:
         """All tcgen05 shape options as a dict name -> value."""
         return {name: self.get_tc_option(opt) for name, opt in TC_OPTIONS.items()}
 
-    def set_grmv_plan(self, plan):
-        """Per-width split-BF16 GRM.V choices: a list of (max_cols, pair, slice) with increasing
-        max_cols ([] clears)."""
+    def _set_plan(self, fn, plan):
         plan = sorted(plan)
         mc = np.array([p[0] for p in plan], np.int32)
         pr = np.array([p[1] for p in plan], np.int32)
         sl = np.array([p[2] for p in plan], np.int32)
         P = C.POINTER(C.c_int32)
-        self._call("sg_set_grmv_plan", len(plan), _ptr(mc, P), _ptr(pr, P), _ptr(sl, P))
+        self._call(fn, len(plan), _ptr(mc, P), _ptr(pr, P), _ptr(sl, P))
 
-    def grmv_plan(self):
+    def _get_plan(self, fn):
         cap = 64
         mc, pr, sl = (np.zeros(cap, np.int32) for _ in range(3))
         n = C.c_int()
         P = C.POINTER(C.c_int32)
-        self._call("sg_get_grmv_plan", cap, _ptr(mc, P), _ptr(pr, P), _ptr(sl, P), C.byref(n))
+        self._call(fn, cap, _ptr(mc, P), _ptr(pr, P), _ptr(sl, P), C.byref(n))
         return [(int(mc[i]), int(pr[i]), int(sl[i])) for i in range(n.value)]
+
+    def set_grmv_plan(self, plan):
+        """Per-width split-BF16 GRM.V choices: a list of (max_cols, pair, slice) with increasing
+        max_cols ([] clears)."""
+        self._set_plan("sg_set_grmv_plan", plan)
+
+    def grmv_plan(self):
+        return self._get_plan("sg_get_grmv_plan")
+
+    def set_subset_plan(self, plan):
+        """Per-width choices of the subset-exact engine's genotype GEMMs: (max_cols, pair, slice)."""
+        self._set_plan("sg_set_subset_plan", plan)
+
+    def subset_plan(self):
+        return self._get_plan("sg_get_subset_plan")
 
     def set_tc_options(self, opts):
         """Set options from a dict name -> value (as returned by ``tc_options``)."""

@@ -8,6 +8,9 @@ Split-BF16 GRM.V: per launch-width bucket, single CTAs or CTA pairs and the K sl
 stage (64 bytes: twice the stages; 128: half the barrier round trips).  The chosen table goes into
 the library (``Context.set_grmv_plan``), which applies it to every later launch.
 
+Subset-exact engine (``MV_SUBSET_EXACT``): per launch-width bucket, single CTAs or CTA pairs and
+the K slice of its two genotype GEMMs (``Context.set_subset_plan``).
+
 Every choice gives bit-identical products (same MMA order, same drain length), so tuning never
 changes a fit.  The drain length is not tuned: it sets the accumulation bias (the tensor core's
 accumulation into TMEM loses magnitude over long chunks), so it stays at the library's 512 bytes.
@@ -18,12 +21,14 @@ import time
 
 import numpy as np
 
-from .context import GRM_BF16_TC, MV_BF16X3_TC, TC_SYRK_GROUP, TC_SYRK_PAIR
+from .context import GRM_BF16_TC, MV_BF16X3_TC, MV_SUBSET_EXACT, TC_SYRK_GROUP, TC_SYRK_PAIR
 
 # launch widths the GRM.V table covers (columns after padding to a tile width)
 GRMV_BUCKETS = (32, 64, 96, 128, 160, 224, 320, 448, 640, 1024)
 GRMV_VARIANTS = ((0, 128), (0, 64), (1, 128), (1, 64))  # (CTA pair, K slice bytes)
 SYRK_VARIANTS = ((0, 16), (1, 8), (1, 16), (1, 32))     # (CTA pair, raster group)
+SUBSET_BUCKETS = (32, 64, 128, 192, 256, 384, 512, 768, 1024)
+SUBSET_VARIANTS = ((0, 128), (1, 128), (0, 64), (1, 64))  # (CTA pair, K slice bytes)
 
 # a variant other than the first is kept only when it is faster by more than the spread of
 # repeated timings
@@ -91,6 +96,36 @@ def tune_grmv(ctx, buckets=GRMV_BUCKETS, variants=GRMV_VARIANTS, mode=MV_BF16X3_
     return table
 
 
+def time_subset(ctx, V, pair, slice_bytes, reps=2):
+    """Event-timed subset-exact GRM.V launch over V's columns (ms per launch), best of reps."""
+    ctx.set_subset_plan([(1 << 30, pair, slice_bytes)])
+    ctx.grm_matmul(V)
+    best = float("inf")
+    for _ in range(reps):
+        ctx.engine_reset_timing()
+        ctx.grm_matmul(V)
+        t = ctx.engine_timing()
+        best = min(best, t["gemm_ms"] / max(1, t["gemm_launches"]))
+    return best
+
+
+def tune_subset(ctx, buckets=SUBSET_BUCKETS, variants=SUBSET_VARIANTS):
+    """Times every (pair, slice) variant of the subset-exact engine at every bucket width on the
+    resident cohort and installs the per-width plan; leaves the engine in MV_SUBSET_EXACT."""
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    ctx.engine_reserve(max(buckets), 1)
+    table, plan = {}, []
+    rng = np.random.default_rng(0)
+    for w in buckets:
+        V = rng.standard_normal((ctx.n, w))
+        times = {v: time_subset(ctx, V, *v) for v in variants}
+        best = _pick(times, variants)
+        table[w] = {"times_ms": times, "chosen": best}
+        plan.append((w, best[0], best[1]))
+    ctx.set_subset_plan(plan)
+    return table
+
+
 def tune(ctx, tune_syrk_too=True, mode=MV_BF16X3_TC, grmv=True):
     """SYRK and GRM.V choices from measured times; leaves the single-product BF16 GRM built (rebuild
     it with GRM_BF16X3_TC for fits: at N = 100k the 8-bit GRM moved binary variance components by
@@ -114,6 +149,11 @@ def report_json(report):
                             "chosen": {"pair": r["chosen"][0], "slice": r["chosen"][1]}}
                    for w, r in report["grmv"].items()}
     out["plan"] = [list(p) for p in report["plan"]]
+    if "subset" in report:
+        out["subset"] = {str(w): {"times_ms": {"pair%d_slice%d" % k: round(v, 3) for k, v in r["times_ms"].items()},
+                                  "chosen": {"pair": r["chosen"][0], "slice": r["chosen"][1]}}
+                         for w, r in report["subset"].items()}
+        out["subset_plan"] = [list(p) for p in report["subset_plan"]]
     return out
 
 
@@ -131,6 +171,8 @@ def main(argv=None):
     ctx.setgeno_device(ptr, ln, args.n, args.m)
     t0 = time.perf_counter()
     rep = tune(ctx)
+    rep["subset"] = tune_subset(ctx)
+    rep["subset_plan"] = ctx.subset_plan()
     out = report_json(rep)
     out["seconds"] = round(time.perf_counter() - t0, 1)
     out["n"], out["m"] = args.n, args.m

@@ -112,7 +112,12 @@ def test_subset_exact_variants_bit_identical(exact_cohort):
                 outs.append(ctx.grm_matmul(V))
             for o in outs[1:]:
                 np.testing.assert_array_equal(o, outs[0])
+            # and through a per-width plan (the tuner's table)
+            ctx.set_subset_plan([(64, 0, 128), (1 << 30, 1, 64)])
+            np.testing.assert_array_equal(ctx.grm_matmul(V), outs[0])
+            ctx.set_subset_plan([])
     finally:
+        ctx.set_subset_plan([])
         ctx.set_tc_option(TC_SUBSET_PAIR, 2)
         ctx.set_tc_option(TC_SUBSET_SLICE, 128)
         ctx.set_matvec_mode(MV_FP32_SIMT)

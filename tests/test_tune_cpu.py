@@ -20,3 +20,12 @@ def test_report_json_keys():
     assert out["syrk"]["chosen"] == {"pair": 1, "group": 16}
     assert out["grmv"]["32"]["times_ms"]["pair1_slice64"] == 6.4
     assert out["plan"] == [[32, 0, 128]]
+
+
+def test_report_json_subset_table():
+    rep = {"grmv": {}, "plan": [],
+           "subset": {512: {"times_ms": {(0, 128): 49.7, (1, 128): 36.5}, "chosen": (1, 128)}},
+           "subset_plan": [(512, 1, 128)]}
+    out = tune.report_json(rep)
+    assert out["subset"]["512"]["chosen"] == {"pair": 1, "slice": 128}
+    assert out["subset_plan"] == [[512, 1, 128]]
