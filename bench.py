@@ -304,13 +304,19 @@ def step_width_summary(trace):
     """How wide the engine steps were (GRM.V columns per launch) and where the GRM.V time went."""
     if len(trace) == 0:
         return None
-    cols, occ, gemm = trace[:, 0], trace[:, 1], trace[:, 2]
+    cols, occ, gemm, idle = trace[:, 0], trace[:, 1], trace[:, 2], trace[:, 4]
     narrow = cols <= 128  # K-streaming bound: the K halves' read sets the time
-    return {"steps": int(len(trace)),
-            "columns_p10_p50_p90": [float(np.percentile(cols, q)) for q in (10, 50, 90)],
-            "occupied_mean": round(float(occ.mean()), 1),
-            "grmv_ms_share_steps_le_128_columns": round(float(gemm[narrow].sum() / max(gemm.sum(), 1e-9)), 3),
-            "steps_le_128_columns": int(narrow.sum())}
+    idle = idle[idle >= 0]  # the first step of a run has no predecessor (-1)
+    out = {"steps": int(len(trace)),
+           "columns_p10_p50_p90": [float(np.percentile(cols, q)) for q in (10, 50, 90)],
+           "occupied_mean": round(float(occ.mean()), 1),
+           "grmv_ms_share_steps_le_128_columns": round(float(gemm[narrow].sum() / max(gemm.sum(), 1e-9)), 3),
+           "steps_le_128_columns": int(narrow.sum())}
+    if len(idle):
+        # device gap before each step (admission included): typical, tail and the largest
+        out["idle_ms_p50_p90_p99_max"] = [round(float(np.percentile(idle, q)), 3) for q in (50, 90, 99)] + [
+            round(float(idle.max()), 3)]
+    return out
 
 
 def serving_block(ctx, args, cols):

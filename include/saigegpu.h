@@ -84,17 +84,20 @@ int sg_selftest_wait_timeout(sg_ctx *ctx, double budget_ms);
  * Every choice gives the same products up to the drain length: the accumulation order within a
  * drain chunk and across chunks does not depend on the others. */
 enum sg_tc_option {
-  SG_TC_SYRK_PAIR = 0,   /* 1: SYRK tiles of 256 x 256 on CTA pairs (tcgen05 cta_group::2); default 0 */
+  SG_TC_SYRK_PAIR = 0,   /* 1: SYRK tiles of 256 x 256 on CTA pairs (tcgen05 cta_group::2), the
+                            default (1.31 s against 1.38 s on single CTAs at N = 100k, M = 150k) */
   SG_TC_GRMV_PAIR = 1,   /* 1: split-BF16 GRM.V tiles of 256 rows on CTA pairs; default 0 */
   SG_TC_DRAIN_BYTES = 2, /* bytes of K per row one TMEM accumulator takes before it is added into
                             registers: 128..4096, a multiple of 128; default 512 */
-  SG_TC_SYRK_GROUP = 3,  /* row tiles per raster group of the SYRK (1..4096); default 16 */
+  SG_TC_SYRK_GROUP = 3,  /* row tiles per raster group of the SYRK (1..4096); default 8 */
   SG_TC_GRMV_SLICE = 4,  /* K slice bytes per pipeline stage of the split-BF16 GRM.V: 0 = by
                             width (128 up to 160 columns, else 64), 64 or 128; default 0 */
   SG_TC_SUBSET_PAIR = 5, /* the subset-exact engine's genotype GEMMs on CTA pairs: 0 never,
                             1 always, 2 above 160 columns (default) */
   SG_TC_SUBSET_SLICE = 6 /* their K slice bytes per pipeline stage: 0 = by width (128 up to 160
-                            columns, else 64), 64 or 128 (default) */
+                            columns, else 64), 64, 128 (default) or 256 (two 128-byte boxes per
+                            operand and stage; widths without room for two such stages -- above
+                            160 columns on single CTAs -- run 128) */
 };
 int sg_set_tc_option(sg_ctx *ctx, int option, int value);
 int sg_get_tc_option(sg_ctx *ctx, int option, int *value);
@@ -107,7 +110,7 @@ int sg_set_grmv_plan(sg_ctx *ctx, int n, const int32_t *max_cols, const int32_t 
                      const int32_t *slice);
 int sg_get_grmv_plan(sg_ctx *ctx, int cap, int32_t *max_cols, int32_t *pair, int32_t *slice, int *n);
 /* The same per-width table for the subset-exact engine's genotype GEMMs (SG_TC_SUBSET_PAIR and
- * SG_TC_SUBSET_SLICE per bucket; slice 64 or 128).  No reference counterpart. */
+ * SG_TC_SUBSET_SLICE per bucket; slice 64, 128 or 256).  No reference counterpart. */
 int sg_set_subset_plan(sg_ctx *ctx, int n, const int32_t *max_cols, const int32_t *pair,
                        const int32_t *slice);
 int sg_get_subset_plan(sg_ctx *ctx, int cap, int32_t *max_cols, int32_t *pair, int32_t *slice, int *n);

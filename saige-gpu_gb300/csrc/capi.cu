@@ -139,6 +139,7 @@ struct Engine {
   void* Tb = nullptr;             // T' halves: cap_cols x mg BF16, high then low
   float* Um = nullptr;            // U = G T': cap_cols x np
   double* spart = nullptr;        // column partials: cap_cols x max(blocks over np, over mg)
+  float* sdiag_part = nullptr;    // per-chunk partial sums of a subset's diagonal (slot set-up)
 };
 constexpr int64_t kStepTrace = 65536;
 constexpr int kTraceFields = 5;
@@ -1066,6 +1067,7 @@ static void engine_free(sg_ctx* c) {
   e.Tb = nullptr;
   dev_free_t(c, e.Um);
   dev_free_t(c, e.spart);
+  dev_free_t(c, e.sdiag_part);
   e.dots_cap_sx = e.dots_cap_part = e.dots_cap_cols = 0;
   if (e.inflight) cudaStreamSynchronize(c->stream);
   e.inflight = false;
@@ -1302,8 +1304,9 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
     SG_CUDA(c, cudaMemcpyAsync(ss.dfill, dfill.data(), nflip * 4, cudaMemcpyHostToDevice, c->side));
   }
   launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, nflip, W, dmask, nn, np, ss.bits, c->side);
-  launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, ss.diag, c->side);
-  SG_LAUNCHED(c, W > 0 ? 2 : 1);
+  if (!e.sdiag_part) SG_TRY(dev_alloc_t(c, &e.sdiag_part, (size_t)subset_diag_scratch(m, np)));
+  launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, e.sdiag_part, ss.diag, c->side);
+  SG_LAUNCHED(c, W > 0 ? 3 : 2);
   ss.dev.dprime = ss.dp;
   ss.dev.p2 = ss.p2;
   ss.dev.flips = ss.flips;

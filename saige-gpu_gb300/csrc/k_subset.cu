@@ -111,36 +111,68 @@ void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* fl
 }
 
 // Diagonal of M' K_S (sum over the subset's GRM markers of z'^2, the Jacobi preconditioner's
-// Get_Diagof_StdGeno, FIT.cpp:665-704): one thread per sample, lut4[4 m + code] = d'_m (g - 2p'_m)^2
-// per packed code (the missing code carries the subset fill); FP32 over 256 markers, then FP64.
-__global__ void subset_diag_kernel(const uint8_t* __restrict__ codes, int64_t pitch, const float4* __restrict__ lut4,
-                                   int64_t m, int64_t nn, int64_t np, double* __restrict__ out) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= np) return;
-  if (i >= nn) {
-    out[i] = 0.0;
-    return;
-  }
-  const int64_t byte = i >> 2;
-  const int sh = 2 * (int)(i & 3);
-  double tot = 0.0;
-  for (int64_t m0 = 0; m0 < m; m0 += 256) {
-    const int64_t m1 = m0 + 256 < m ? m0 + 256 : m;
-    float acc = 0.0f;
-    for (int64_t mk = m0; mk < m1; ++mk) {
-      const uint32_t f = (__ldg(codes + mk * pitch + byte) >> sh) & 3u;
-      const float4 l = __ldg(lut4 + mk);
-      acc += f == 0u ? l.x : f == 1u ? l.y : f == 2u ? l.z : l.w;
+// Get_Diagof_StdGeno, FIT.cpp:665-704), lut4[4 m + code] = d'_m (g - 2p'_m)^2 per packed code (the
+// missing code carries the subset fill).  Pass 1: block = 256 words of a marker row (16 samples
+// each, so a warp reads 128 contiguous bytes) x a chunk of kDiagChunkM markers; each chunk's table
+// is staged 256 markers at a time in shared memory; FP32 sums per chunk into part[chunk][sample].
+// Pass 2: per sample, the chunks' partials added in chunk order in FP64.
+constexpr int kDiagChunkM = 2048;
+
+__global__ void __launch_bounds__(kThreads)
+subset_diag_part_kernel(const uint32_t* __restrict__ codes32, int64_t words_per_row, int64_t nwords,
+                        const float4* __restrict__ lut4, int64_t m, int64_t np, float* __restrict__ part) {
+  __shared__ float4 slut[kThreads];
+  const int64_t w = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  const int64_t m0 = (int64_t)blockIdx.y * kDiagChunkM;
+  const int64_t m1 = m0 + kDiagChunkM < m ? m0 + kDiagChunkM : m;
+  float acc[16];
+#pragma unroll
+  for (int s = 0; s < 16; ++s) acc[s] = 0.0f;
+  for (int64_t k0 = m0; k0 < m1; k0 += kThreads) {
+    __syncthreads();
+    if (k0 + threadIdx.x < m1) slut[threadIdx.x] = lut4[k0 + threadIdx.x];
+    __syncthreads();
+    const int kn = (int)(m1 - k0 < kThreads ? m1 - k0 : kThreads);
+    if (w < nwords) {
+      const uint32_t* row = codes32 + k0 * words_per_row + w;
+      for (int k = 0; k < kn; ++k) {
+        const uint32_t word = __ldg(row + (int64_t)k * words_per_row);
+        const float* l = reinterpret_cast<const float*>(&slut[k]);
+#pragma unroll
+        for (int s = 0; s < 16; ++s) acc[s] += l[(word >> (2 * s)) & 3u];
+      }
     }
-    tot += (double)acc;
   }
-  out[i] = tot;
+  if (w < nwords) {
+    float* out = part + (int64_t)blockIdx.y * np + 16 * w;
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
+      if (16 * w + s < np) out[s] = acc[s];
+  }
 }
 
+__global__ void subset_diag_sum_kernel(const float* __restrict__ part, int nchunks, int64_t nn, int64_t np,
+                                       double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  double t = 0.0;
+  if (i < nn)
+    for (int c = 0; c < nchunks; ++c) t += (double)part[(int64_t)c * np + i];
+  out[i] = t;
+}
+
+int64_t subset_diag_scratch(int64_t m, int64_t np) { return ((m + kDiagChunkM - 1) / kDiagChunkM) * np; }
+
 void launch_subset_diag(const uint8_t* codes, int64_t pitch, const float* lut4, int64_t m, int64_t nn, int64_t np,
-                        double* out, cudaStream_t s) {
-  subset_diag_kernel<<<(unsigned)((np + kThreads - 1) / kThreads), kThreads, 0, s>>>(
-      codes, pitch, reinterpret_cast<const float4*>(lut4), m, nn, np, out);
+                        float* part, double* out, cudaStream_t s) {
+  const int64_t nwords = (nn + 15) / 16;
+  const int nchunks = (int)((m + kDiagChunkM - 1) / kDiagChunkM);
+  if (nchunks > 0 && nwords > 0) {
+    dim3 grid((unsigned)((nwords + kThreads - 1) / kThreads), (unsigned)nchunks);
+    subset_diag_part_kernel<<<grid, kThreads, 0, s>>>(reinterpret_cast<const uint32_t*>(codes), pitch / 4, nwords,
+                                                      reinterpret_cast<const float4*>(lut4), m, np, part);
+  }
+  subset_diag_sum_kernel<<<(unsigned)((np + kThreads - 1) / kThreads), kThreads, 0, s>>>(part, nchunks, nn, np, out);
 }
 
 // ----------------------------------------------------------------------------------- per step
@@ -261,14 +293,22 @@ __global__ void subset_scale_split_kernel(const float* __restrict__ T, int64_t m
 }
 
 // K_S v on the subset: (U + dF T' - (2p')^T T') / M', written to column cols[j] of Y (zero outside
-// the subset); padding columns are skipped.
-__global__ void subset_finalize_kernel(const float* __restrict__ U, int64_t np, int64_t nn,
-                                       const int32_t* __restrict__ cols, const ColState* __restrict__ st,
-                                       const SubsetSlot* __restrict__ slots, const __nv_bfloat16* __restrict__ Th,
-                                       const __nv_bfloat16* __restrict__ Tl, int64_t mg,
-                                       const double* __restrict__ part, int nblk, const double* __restrict__ winv,
-                                       float* __restrict__ Yf) {
+// the subset); padding columns are skipped.  The fill-flip term of sample i sums, over the flip
+// markers k at which i is missing (set bits of the slot's word-major bit map), dfill[k] T'[j, flips[k]];
+// those products are staged per column in shared memory, kFinF flips (kFinF / 32 bit-map words) at a
+// time, so the scattered reads of T' happen once per block, not once per missing genotype.  The
+// terms are added in ascending flip order in FP64.
+constexpr int kFinF = 2048;
+constexpr int kFinPer = kChunk / kThreads;  // samples per thread
+
+__global__ void __launch_bounds__(kThreads)
+subset_finalize_kernel(const float* __restrict__ U, int64_t np, int64_t nn, const int32_t* __restrict__ cols,
+                       const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
+                       const __nv_bfloat16* __restrict__ Th, const __nv_bfloat16* __restrict__ Tl, int64_t mg,
+                       const double* __restrict__ part, int nblk, const double* __restrict__ winv,
+                       float* __restrict__ Yf) {
   __shared__ double s_c;
+  __shared__ double tf[kFinF];
   const int64_t j = blockIdx.y;
   const int32_t col = cols[j];
   if (col < 0) return;
@@ -279,26 +319,51 @@ __global__ void subset_finalize_kernel(const float* __restrict__ U, int64_t np, 
     for (int b = 0; b < nblk; ++b) c += part[j * nblk + b];
     s_c = c;
   }
-  __syncthreads();
-  const double c = s_c;
-  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
-  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
-    float y = 0.0f;
-    if (i < nn && winv[(int64_t)slot * np + i] != 0.0) {
-      double du = 0.0;
-      for (int w = 0; w < sl.W; ++w) {
-        uint32_t word = sl.bits[(int64_t)w * np + i];
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk + threadIdx.x;
+  unsigned live = 0u;
+#pragma unroll
+  for (int r = 0; r < kFinPer; ++r) {
+    const int64_t i = i0 + (int64_t)r * kThreads;
+    if (i < nn && winv[(int64_t)slot * np + i] != 0.0) live |= 1u << r;
+  }
+  double du[kFinPer];
+#pragma unroll
+  for (int r = 0; r < kFinPer; ++r) du[r] = 0.0;
+  const __nv_bfloat16* th = Th + j * mg;
+  const __nv_bfloat16* tl = Tl + j * mg;
+  for (int f0 = 0; f0 < sl.nflip; f0 += kFinF) {
+    const int fn = sl.nflip - f0 < kFinF ? sl.nflip - f0 : kFinF;
+    __syncthreads();
+    for (int k = threadIdx.x; k < fn; k += kThreads) {
+      const int64_t mk = sl.flips[f0 + k];
+      tf[k] = (double)sl.dfill[f0 + k] * ((double)__bfloat162float(th[mk]) + (double)__bfloat162float(tl[mk]));
+    }
+    __syncthreads();
+    const int w0 = f0 / 32, wn = (fn + 31) / 32;
+#pragma unroll
+    for (int r = 0; r < kFinPer; ++r) {
+      if (!((live >> r) & 1u)) continue;
+      const uint32_t* bw = sl.bits + (int64_t)w0 * np + i0 + (int64_t)r * kThreads;
+      double d = du[r];
+      for (int w = 0; w < wn; ++w) {
+        uint32_t word = bw[(int64_t)w * np];
         while (word) {
           const int b = __ffs(word) - 1;
           word &= word - 1u;
-          const int k = 32 * w + b;
-          const int64_t mk = sl.flips[k];
-          du += (double)sl.dfill[k] *
-                ((double)__bfloat162float(Th[j * mg + mk]) + (double)__bfloat162float(Tl[j * mg + mk]));
+          d += tf[32 * w + b];
         }
       }
-      y = (float)(((double)U[j * np + i] - c + du) * sl.inv_m);
+      du[r] = d;
     }
+  }
+  __syncthreads();
+  const double c = s_c;
+#pragma unroll
+  for (int r = 0; r < kFinPer; ++r) {
+    const int64_t i = i0 + (int64_t)r * kThreads;
+    if (i >= np) break;
+    float y = 0.0f;
+    if ((live >> r) & 1u) y = (float)(((double)U[j * np + i] - c + du[r]) * sl.inv_m);
     Yf[(int64_t)col * np + i] = y;
   }
 }

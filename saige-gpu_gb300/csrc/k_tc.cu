@@ -320,14 +320,19 @@ struct TileCoord {
 // K per row).  Rows >= nrows of a tile (a padding row block) are not stored.
 // RB: bytes of one operand row's K slice per pipeline stage -- 128 (SWIZZLE_128B) or 64
 // (SWIZZLE_64B: half the bytes per stage, twice the stages in the same shared memory, for the
-// split-BF16 GRM.V, whose four operand tiles per stage left it with only two stages of 128-byte slices).
+// split-BF16 GRM.V, whose four operand tiles per stage left it with only two stages of 128-byte
+// slices), or 256: two adjacent 128-byte SWIZZLE_128B boxes per operand and stage, so that each
+// stage reads 256 contiguous bytes of every operand row (twice the bytes per DRAM page opened when
+// the rows of a streamed operand lie far apart, as G's do in the genotype GEMMs).
 template <bool kTF32, int BN, int S, int kForm, bool kPair, int RB = 128>
 __global__ void __launch_bounds__(kGemmThreads, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
                const TileCoord* __restrict__ tiles, int num_kb, int drain_kb, float* __restrict__ D,
                int64_t ldd, float scale, int mode, int64_t nrows, const int32_t* __restrict__ colmap) {
-  static_assert(RB == 128 || RB == 64, "K slices of 128 or 64 bytes");
+  static_assert(RB == 256 || RB == 128 || RB == 64, "K slices of 256, 128 or 64 bytes");
+  constexpr int kSW = RB > 128 ? 128 : RB;  // bytes of one swizzled box row (the TMA box's inner size)
+  constexpr int kSub = RB / kSW;            // boxes per operand and stage, adjacent in K
   static_assert(!kPair || (BN / 2) % 8 == 0, "a CTA's half of the B tile is whole 8-row swizzle atoms");
   constexpr int kATile = kTileM * RB;
   constexpr int kBRows = kPair ? BN / 2 : BN;  // rows of the B tile this CTA loads
@@ -407,20 +412,32 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
         if (!mbar_wait(&empty[s], ph ^ 1u, 1, abort_flag)) break;
         uint8_t* st = smem + s * kStageBytes;
         const int32_t x = kb * (RB / (kTF32 ? 4 : 2));
+        // box u of an operand covers K bytes [u kSW, (u + 1) kSW) of the stage's slice and sits
+        // u * rows * kSW bytes into the operand's region
         if constexpr (kPair) {
           // the leader's full barrier counts both CTAs' bytes; only the leader arrives on it
           const uint32_t fb = cluster_addr(&full[s], 0);
           if (leader) mbar_expect_tx(&full[s], 2u * (uint32_t)kStageBytes);
-          tma_load_2d_pair(st, &mapA, fb, x, ya);
-          tma_load_2d_pair(st + kATile, &mapB, fb, x, yb);
-          if constexpr (kForm >= kSplit3) tma_load_2d_pair(st + kATile + kBTileBytes, &mapA2, fb, x, ya);
-          if constexpr (kForm >= kSplitB) tma_load_2d_pair(st + kOffB2, &mapB2, fb, x, yb);
+#pragma unroll
+          for (int u = 0; u < kSub; ++u) {
+            const int32_t xu = x + u * (kSW / (kTF32 ? 4 : 2));
+            tma_load_2d_pair(st + u * kTileM * kSW, &mapA, fb, xu, ya);
+            tma_load_2d_pair(st + kATile + u * kBRows * kSW, &mapB, fb, xu, yb);
+            if constexpr (kForm >= kSplit3)
+              tma_load_2d_pair(st + kATile + kBTileBytes + u * kTileM * kSW, &mapA2, fb, xu, ya);
+            if constexpr (kForm >= kSplitB) tma_load_2d_pair(st + kOffB2 + u * kBRows * kSW, &mapB2, fb, xu, yb);
+          }
         } else {
           mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
-          tma_load_2d(st, &mapA, &full[s], x, ya);
-          tma_load_2d(st + kATile, &mapB, &full[s], x, yb);
-          if constexpr (kForm >= kSplit3) tma_load_2d(st + kATile + kBTileBytes, &mapA2, &full[s], x, ya);
-          if constexpr (kForm >= kSplitB) tma_load_2d(st + kOffB2, &mapB2, &full[s], x, yb);
+#pragma unroll
+          for (int u = 0; u < kSub; ++u) {
+            const int32_t xu = x + u * (kSW / (kTF32 ? 4 : 2));
+            tma_load_2d(st + u * kTileM * kSW, &mapA, &full[s], xu, ya);
+            tma_load_2d(st + kATile + u * kBRows * kSW, &mapB, &full[s], xu, yb);
+            if constexpr (kForm >= kSplit3)
+              tma_load_2d(st + kATile + kBTileBytes + u * kTileM * kSW, &mapA2, &full[s], xu, ya);
+            if constexpr (kForm >= kSplitB) tma_load_2d(st + kOffB2 + u * kBRows * kSW, &mapB2, &full[s], xu, yb);
+          }
         }
       }
     }
@@ -451,15 +468,18 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
 #pragma unroll
         for (int k = 0; k < kKSteps; ++k) {
           const uint32_t acc = (kin > 0 || k > 0) ? 1u : 0u;
-          umma<kTF32, kPair>(dacc, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, acc);
+          // 32 bytes of K per MMA: box k / (kSW / 32), offset 32 (k % (kSW / 32)) within its rows
+          const uint32_t ka = (uint32_t)((k / (kSW / 32)) * kTileM * kSW + 32 * (k % (kSW / 32)));
+          const uint32_t kbo = (uint32_t)((k / (kSW / 32)) * kBRows * kSW + 32 * (k % (kSW / 32)));
+          umma<kTF32, kPair>(dacc, smem_desc_kmajor<kSW>(a0 + ka), smem_desc_kmajor<kSW>(b0 + kbo), kIdesc, acc);
           if constexpr (kForm >= kSplitB) {
             const uint32_t b1 = a0 + kOffB2;            // Bl
-            umma<kTF32, kPair>(dacc, smem_desc_kmajor<RB>(a0 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
+            umma<kTF32, kPair>(dacc, smem_desc_kmajor<kSW>(a0 + ka), smem_desc_kmajor<kSW>(b1 + kbo), kIdesc, 1u);
             if constexpr (kForm >= kSplit3) {
               const uint32_t a1 = b0 + kBTileBytes;     // Al
-              umma<kTF32, kPair>(dacc, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b0 + 32 * k), kIdesc, 1u);
+              umma<kTF32, kPair>(dacc, smem_desc_kmajor<kSW>(a1 + ka), smem_desc_kmajor<kSW>(b0 + kbo), kIdesc, 1u);
               if constexpr (kForm == kSplit4)
-                umma<kTF32, kPair>(dacc, smem_desc_kmajor<RB>(a1 + 32 * k), smem_desc_kmajor<RB>(b1 + 32 * k), kIdesc, 1u);
+                umma<kTF32, kPair>(dacc, smem_desc_kmajor<kSW>(a1 + ka), smem_desc_kmajor<kSW>(b1 + kbo), kIdesc, 1u);
             }
           }
         }
@@ -790,10 +810,10 @@ bool tc_available() {
 
 // Shape options of the tcgen05 GEMMs (process-wide; saigegpu.tune sets them from timings).
 static int g_opt[kTcOptions] = {
-    0,    // kTcSyrkPair: SYRK tiles on CTA pairs (cta_group::2, 256 x 256)
+    1,    // kTcSyrkPair: SYRK tiles on CTA pairs (cta_group::2, 256 x 256)
     0,    // kTcGrmvPair: split GRM.V tiles on CTA pairs (256 x BN)
     512,  // kTcDrainBytes: bytes of K per row one TMEM accumulator takes before it is drained
-    16,   // kTcSyrkGroup: row tiles per raster group of the SYRK
+    8,    // kTcSyrkGroup: row tiles per raster group of the SYRK
     0,    // kTcGrmvSlice: K slice bytes of the split-BF16 GRM.V (0: by width, 64 or 128)
     2,    // kTcSubsetPair: subset-exact genotype GEMMs on CTA pairs (2: above 160 columns)
     128,  // kTcSubsetSlice: their K slice bytes (0: 128 up to 160 columns, else 64; or 64 / 128)
@@ -816,8 +836,10 @@ bool tc_set_option(int opt, int value) {
       if (value < 1 || value > 4096) return false;
       break;
     case kTcGrmvSlice:
-    case kTcSubsetSlice:
       if (value != 0 && value != 64 && value != 128) return false;
+      break;
+    case kTcSubsetSlice:
+      if (value != 0 && value != 64 && value != 128 && value != 256) return false;
       break;
   }
   g_opt[opt] = value;
@@ -869,7 +891,7 @@ bool tc_set_subset_plan(const int32_t* max_cols, const int32_t* pair, const int3
   std::vector<GrmvChoice> plan;
   for (int i = 0; i < n; ++i) {
     if (max_cols[i] <= 0 || (i > 0 && max_cols[i] <= max_cols[i - 1])) return false;
-    if ((pair[i] != 0 && pair[i] != 1) || (slice[i] != 64 && slice[i] != 128)) return false;
+    if ((pair[i] != 0 && pair[i] != 1) || (slice[i] != 64 && slice[i] != 128 && slice[i] != 256)) return false;
     plan.push_back(GrmvChoice{max_cols[i], pair[i], slice[i]});
   }
   g_subset_plan.swap(plan);
@@ -990,6 +1012,10 @@ static int subset_slice(int64_t ncols) {
     if (ncols <= b.max_cols) return b.slice;
   return g_opt[kTcSubsetSlice] != 0 ? g_opt[kTcSubsetSlice] : (ncols <= 160 ? 128 : 64);
 }
+
+// 256-byte stages exist for the tile widths whose stage (128 A rows and two halves of the B rows,
+// 256 bytes each) leaves room for at least two stages; other widths run 128-byte stages.
+static bool splitb_has_256(int BN, bool pair) { return pair || BN <= 160; }
 
 // Columns one GRM.V launch covers for ncols32 (a multiple of 16) live columns, padded so that the
 // modelled cost is lowest, capped at cap columns.  Cost model (L2->SM bytes of one pass, which
@@ -1236,12 +1262,14 @@ cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void
     return cudaErrorInvalidValue;
   const int BN = tc_gemm_tile_n(ncols, kTilesSplitB);
   const bool pair = subset_pair(ncols);
-  const int RB = subset_slice(ncols);
+  int RB = subset_slice(ncols);
+  if (RB == 256 && (!splitb_has_256(BN, pair) || kdim % 128 != 0)) RB = 128;
+  const int box = RB > 128 ? 128 : RB;  // a 256-byte stage is two 128-byte boxes per operand
   const uint64_t rb = (uint64_t)kdim * 2;
   CUtensorMap a, b, b2;
-  if (!make_map(&a, A, false, kdim, rows, rb, kTileM, RB) ||
-      !make_map(&b, Bh, false, kdim, ncols, rb, pair ? BN / 2 : BN, RB) ||
-      !make_map(&b2, Bl, false, kdim, ncols, rb, pair ? BN / 2 : BN, RB))
+  if (!make_map(&a, A, false, kdim, rows, rb, kTileM, box) ||
+      !make_map(&b, Bh, false, kdim, ncols, rb, pair ? BN / 2 : BN, box) ||
+      !make_map(&b2, Bl, false, kdim, ncols, rb, pair ? BN / 2 : BN, box))
     return cudaErrorInvalidValue;
   // one tile table per call site: the two GEMMs of an engine step are queued back to back, so the
   // second must not restage the table the first one's upload may still be reading
@@ -1258,7 +1286,30 @@ cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void
                                                   rows);                                                    \
     break;
   // per CTA and stage: 128 A rows plus two halves of BN (BN / 2 on a CTA pair) B rows, RB bytes each
-  if (RB == 128 && pair) {
+  if (RB == 256 && pair) {
+    switch (BN) {
+      SG_SB(256, 2, true, 256)
+      SG_SB(224, 2, true, 256)
+      SG_SB(192, 2, true, 256)
+      SG_SB(160, 3, true, 256)
+      SG_SB(128, 3, true, 256)
+      SG_SB(96, 4, true, 256)
+      SG_SB(64, 4, true, 256)
+      SG_SB(32, 5, true, 256)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else if (RB == 256) {
+    switch (BN) {
+      SG_SB(160, 2, false, 256)
+      SG_SB(128, 2, false, 256)
+      SG_SB(96, 2, false, 256)
+      SG_SB(64, 3, false, 256)
+      SG_SB(32, 4, false, 256)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else if (RB == 128 && pair) {
     switch (BN) {
       SG_SB(256, 4, true, 128)
       SG_SB(224, 4, true, 128)

@@ -210,8 +210,10 @@ void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int
                    int64_t np, void* Gmm, void* Gsm, cudaStream_t s);
 void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* flips, int nflip, int W,
                           const uint8_t* mask, int64_t nn, int64_t np, uint32_t* bits, cudaStream_t s);
+// part: subset_diag_scratch(m, np) floats of scratch
+int64_t subset_diag_scratch(int64_t m, int64_t np);
 void launch_subset_diag(const uint8_t* codes, int64_t pitch, const float* lut4, int64_t m, int64_t nn, int64_t np,
-                        double* out, cudaStream_t s);
+                        float* part, double* out, cudaStream_t s);
 int subset_nblk(int64_t n);
 // per step: column sums over the subset, then the centred BF16 halves (compact block of ncols)
 void launch_subset_prepare(const float* Pf, int64_t np, const int32_t* cols, int64_t ncols, const ColState* st,

@@ -70,7 +70,7 @@ def test_subset_exact_products_match_oracle(exact_cohort):
     rng = np.random.default_rng(5)
     ctx.set_matvec_mode(MV_SUBSET_EXACT)
     try:
-        for pair, sl in ((0, 64), (1, 128), (2, 128)):
+        for pair, sl in ((0, 64), (1, 128), (2, 128), (0, 256), (1, 256)):
             ctx.set_tc_option(TC_SUBSET_PAIR, pair)
             ctx.set_tc_option(TC_SUBSET_SLICE, sl)
             ctx.engine_reserve(128, len(cases))
@@ -106,14 +106,14 @@ def test_subset_exact_variants_bit_identical(exact_cohort):
         for k in (1, 40, 200, 300):
             V = rng.standard_normal((N, k))
             outs = []
-            for pair, sl in ((0, 64), (0, 128), (1, 64), (1, 128)):
+            for pair, sl in ((0, 64), (0, 128), (1, 64), (1, 128), (0, 256), (1, 256)):
                 ctx.set_tc_option(TC_SUBSET_PAIR, pair)
                 ctx.set_tc_option(TC_SUBSET_SLICE, sl)
                 outs.append(ctx.grm_matmul(V))
             for o in outs[1:]:
                 np.testing.assert_array_equal(o, outs[0])
             # and through a per-width plan (the tuner's table)
-            ctx.set_subset_plan([(64, 0, 128), (1 << 30, 1, 64)])
+            ctx.set_subset_plan([(64, 0, 256), (192, 0, 128), (1 << 30, 1, 64)])
             np.testing.assert_array_equal(ctx.grm_matmul(V), outs[0])
             ctx.set_subset_plan([])
     finally:
