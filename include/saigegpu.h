@@ -95,7 +95,7 @@ enum sg_tc_option {
   SG_TC_SUBSET_PAIR = 5, /* the subset-exact engine's genotype GEMMs on CTA pairs: 0 never,
                             1 always, 2 above 160 columns (default) */
   SG_TC_SUBSET_SLICE = 6 /* their K slice bytes per pipeline stage: 0 = by width (128 up to 160
-                            columns, else 64), 64, 128 (default) or 256 (two 128-byte boxes per
+                            columns, else 64), 64, 128 or 256 (default: two 128-byte boxes per
                             operand and stage; widths without room for two such stages -- above
                             160 columns on single CTAs -- run 128) */
 };
@@ -281,6 +281,21 @@ int sg_engine_reserve(sg_ctx *ctx, int64_t max_columns, int64_t max_phenos);
  * this phenotype's subset; NULL = all). */
 int sg_engine_set_pheno(sg_ctx *ctx, int64_t slot, const double *w, const double *tau,
                         const uint8_t *mask);
+/* Subset-exact engine: a slot keeps its subset's state (allele frequencies, fill, QC, 1/sd, the
+ * fill-change map and the diagonal; setgeno over the subset, FIT.cpp:376-385, 436-495) while its
+ * mask is unchanged, so later sg_engine_set_pheno calls (new weights each AI-REML iteration) only
+ * upload weights.  This drops every slot's kept state: the next sg_engine_set_pheno of each slot
+ * rebuilds it, as for a new phenotype.  No reference counterpart. */
+int sg_engine_forget_subsets(sg_ctx *ctx);
+/* Subset-exact engine, for a driver whose threads serialise their engine calls: launch the first,
+ * longer half of slot ``slot``'s subset set-up for ``mask`` (QC over the subset, its tables and
+ * fill-change list) without waiting; sg_engine_subset_wait(slot) then blocks until that half has
+ * run and, like sg_engine_wait, need not be serialised with other threads' calls; the slot's next
+ * sg_engine_set_pheno with the same mask completes the set-up.  Both are no-ops when the slot
+ * already holds that subset, and sg_engine_prepare_subset is one for the other engines.  No
+ * reference counterpart. */
+int sg_engine_prepare_subset(sg_ctx *ctx, int64_t slot, const uint8_t *mask);
+int sg_engine_subset_wait(sg_ctx *ctx, int64_t slot);
 /* Queue k columns.  kind 0 = PCG solve of Sigma x = b, kind 1 = one GRM product K b.
  * ids[k] receives request ids. */
 int sg_engine_submit(sg_ctx *ctx, int64_t slot, int kind, const double *B, int64_t k, int maxiter,
@@ -410,6 +425,13 @@ int sg_fits_counts(sg_fits *fits, int64_t *active, int64_t *pending, int64_t *do
  * parts of the driver work spent in weight uploads, submissions, result copies and probe
  * reductions, and the part of the engine time spent launching steps */
 int sg_fits_host_times(sg_fits *fits, double *t8);
+/* t4: with worker threads, seconds of the stepping thread's engine time spent waiting for the
+ * step on the device, waiting for the driver's lock (a worker's engine call in progress),
+ * finishing the step, and marking finished requests done. */
+int sg_fits_step_times(sg_fits *fits, double *t4);
+/* t3: for a finished fit not yet collected by sg_fits_result, the seconds since sg_fits_create at
+ * which it was added, given a phenotype slot (admitted), and finished. */
+int sg_fits_fit_times(sg_fits *fits, int64_t fit_id, double *t3);
 int sg_fits_result(sg_fits *fits, int64_t fit_id, double *theta, double *alpha, double *eta, double *mu,
                    double *Y, double *cov, int32_t *iterations, int32_t *converged,
                    int64_t *column_iterations);

@@ -79,8 +79,11 @@ struct Engine {
   std::vector<int64_t> slab_pending;  // admitted requests whose slabs return once the stream drains
   int32_t* h_acols = nullptr;
   unsigned char* h_ptab = nullptr;
-  std::vector<std::pair<double*, const double*>> slab_free;  // (host, device) addresses
-  std::vector<void*> slab_blocks;
+  std::vector<std::pair<double*, const double*>> slab_free;  // (pinned host, device) slab pairs
+  std::vector<void*> slab_blocks;   // pinned host blocks
+  std::vector<void*> slab_dblocks;  // device blocks
+  cudaEvent_t ev_up = nullptr;      // the last right-hand-side upload (upload stream)
+  bool up_wait = false;             // the next admission waits for it
   double* h_stage = nullptr;      // pinned: a slot's W and sample mask on their way up
   double* d_wstage = nullptr;     // their device copy (np doubles + np bytes)
   int32_t* d_gcols = nullptr;
@@ -122,14 +125,25 @@ struct Engine {
     float* dp = nullptr;          // mg: d' = 1/sd'^2 (0 off the subset's GRM markers)
     float* p2 = nullptr;          // mg: 2p'
     float* lut = nullptr;         // mg x 4: d' (g - 2p')^2 per packed code (diagonal)
-    int32_t* flips = nullptr;     // fill-changed markers
+    int32_t* flips = nullptr;     // fill-changed markers (room for every marker)
     float* dfill = nullptr;
-    int64_t flip_cap = 0;
     uint32_t* bits = nullptr;     // W x np bit map (word-major)
     int64_t bits_cap = 0;
     double* diag = nullptr;       // np: sum of z'^2 (the preconditioner's diagonal)
     SubsetSlot dev;               // what d_slots[slot] holds
     double m_prime = 0.0;
+    // first half of a set-up launched ahead (sg_engine_prepare_subset): QC records, flags and
+    // counts of the subset in prep_mask, complete when ev_prep has
+    MarkerQC* qc = nullptr;       // m_bim
+    uint8_t* flag = nullptr;      // mg
+    uint32_t* mb = nullptr;       // the mask as 2-bit fields
+    int64_t* d_counts = nullptr;  // (changes, M')
+    int64_t* h_counts = nullptr;  // pinned copy
+    cudaEvent_t ev_prep = nullptr;
+    bool prep = false;
+    bool prep_all = false;
+    std::vector<uint8_t> prep_mask;
+    int64_t prep_ns = 0;
   };
   std::vector<SlotSub> sub;
   SubsetSlot* d_slots = nullptr;
@@ -140,6 +154,7 @@ struct Engine {
   float* Um = nullptr;            // U = G T': cap_cols x np
   double* spart = nullptr;        // column partials: cap_cols x max(blocks over np, over mg)
   float* sdiag_part = nullptr;    // per-chunk partial sums of a subset's diagonal (slot set-up)
+
 };
 constexpr int64_t kStepTrace = 65536;
 constexpr int kTraceFields = 5;
@@ -152,6 +167,7 @@ struct sg_ctx {
   uint64_t in_use = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // result copies, probe reductions and slot uploads overlap a step here
+  cudaStream_t up = nullptr;    // the engine's right-hand-side uploads
   std::string err;
   std::string err_pending;
   uint64_t launches = 0;
@@ -200,6 +216,7 @@ struct sg_ctx {
   // engine recomputes a phenotype subset's QC from
   uint8_t* d_codes = nullptr;
   uint8_t* d_vrflag_all = nullptr;
+  int32_t* d_fill_all = nullptr;  // the cohort fill of every .bim marker (subset-exact engine)
   std::vector<int32_t> fill_all;
   float qc_min_maf = 0.01f, qc_max_missing = 0.15f, qc_min_mac_vr = 20.0f, qc_max_mac_vr = -1.0f;
   // upper MAC bound of categorical variance ratios for the next setgeno (-1: a single ratio)
@@ -348,6 +365,13 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
     delete c;
     return SG_ERR_CUDA;
   }
+  // right-hand-side uploads of the engine, beside the steps (copy engine only)
+  if (cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(c->side);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return SG_ERR_CUDA;
+  }
   *out = c;
   return SG_OK;
 }
@@ -357,11 +381,13 @@ extern "C" void sg_ctx_destroy(sg_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   cudaStreamSynchronize(c->side);
+  cudaStreamSynchronize(c->up);
   if (c->eng.h_pin) cudaFreeHost(c->eng.h_pin);
   if (c->eng.h_gcols) cudaFreeHost(c->eng.h_gcols);
   if (c->eng.h_stage) cudaFreeHost(c->eng.h_stage);
   for (auto& kv : c->allocs) cudaFree(kv.first);
   c->allocs.clear();
+  cudaStreamDestroy(c->up);
   cudaStreamDestroy(c->side);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -406,7 +432,10 @@ extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
   // a slot's subset state and preconditioner belong to the engine they were set for: entering or
   // leaving the subset-exact engine asks for every slot to be set again
   if (was_exact != (mode == SG_MV_SUBSET_EXACT)) {
-    for (auto& ss : c->eng.sub) ss.valid = false;
+    for (auto& ss : c->eng.sub) {
+      if (ss.prep) cudaEventSynchronize(ss.ev_prep);
+      ss.valid = ss.prep = false;
+    }
     std::fill(c->eng.ph_set.begin(), c->eng.ph_set.end(), 0);
   }
   if (mode == SG_MV_SUBSET_EXACT) {
@@ -433,19 +462,18 @@ static int ensure_g(sg_ctx* c) {
     engine_free(c);
     c->np = np;
   }
-  int32_t* d_fill = nullptr;
-  SG_TRY(dev_alloc_t(c, &d_fill, (size_t)std::max<int64_t>(c->m_bim, 1)));
+  // the cohort fill stays on the device beside G: each subset's set-up compares its own fill with it
+  if (!c->d_fill_all) SG_TRY(dev_alloc_t(c, &c->d_fill_all, (size_t)std::max<int64_t>(c->m_bim, 1)));
   SG_TRY(dev_alloc(c, &c->d_G, (size_t)(2 * mg * np * 2)));
   if (c->m_bim)
-    SG_CUDA(c, cudaMemcpyAsync(d_fill, c->fill_all.data(), c->m_bim * 4, cudaMemcpyHostToDevice, c->stream));
+    SG_CUDA(c, cudaMemcpyAsync(c->d_fill_all, c->fill_all.data(), c->m_bim * 4, cudaMemcpyHostToDevice, c->stream));
   SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
-  launch_gbuild(c->d_codes, c->pitch, d_fill, c->m_bim, c->nn, mg, np, c->d_G,
+  launch_gbuild(c->d_codes, c->pitch, c->d_fill_all, c->m_bim, c->nn, mg, np, c->d_G,
                 static_cast<uint16_t*>(c->d_G) + mg * np, c->stream);
   SG_LAUNCHED(c, 1);
   SG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
   SG_TRY(sync(c));
   c->t_build[3] = ev_ms(c->tev[0], c->tev[1]);
-  dev_free(c, d_fill);
   c->mg = mg;
   return SG_OK;
 }
@@ -546,6 +574,7 @@ static void free_geno(sg_ctx* c) {
   dev_free_t(c, c->d_diag32);
   dev_free_t(c, c->d_codes);
   dev_free_t(c, c->d_vrflag_all);
+  dev_free_t(c, c->d_fill_all);
   dev_free(c, c->d_G);
   c->d_G = nullptr;
   c->fill_all.clear();
@@ -1056,6 +1085,9 @@ static void engine_free(sg_ctx* c) {
   for (auto& ss : e.sub) {
     dev_free_t(c, ss.dp); dev_free_t(c, ss.p2); dev_free_t(c, ss.lut); dev_free_t(c, ss.flips);
     dev_free_t(c, ss.dfill); dev_free_t(c, ss.bits); dev_free_t(c, ss.diag);
+    dev_free_t(c, ss.qc); dev_free_t(c, ss.flag); dev_free_t(c, ss.mb); dev_free_t(c, ss.d_counts);
+    if (ss.h_counts) cudaFreeHost(ss.h_counts);
+    if (ss.ev_prep) cudaEventDestroy(ss.ev_prep);
   }
   e.sub.clear();
   e.max_w = 0;
@@ -1068,6 +1100,7 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.Um);
   dev_free_t(c, e.spart);
   dev_free_t(c, e.sdiag_part);
+
   e.dots_cap_sx = e.dots_cap_part = e.dots_cap_cols = 0;
   if (e.inflight) cudaStreamSynchronize(c->stream);
   e.inflight = false;
@@ -1087,9 +1120,13 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.d_sst);
   dev_free_t(c, e.d_scol);
   e.n_sst = 0;
+  if (!e.slab_blocks.empty()) cudaStreamSynchronize(c->up);
   for (void* blk : e.slab_blocks) cudaFreeHost(blk);
   e.slab_blocks.clear();
+  for (void* blk : e.slab_dblocks) dev_free(c, blk);
+  e.slab_dblocks.clear();
   e.slab_free.clear();
+  e.up_wait = false;
   dev_free_t(c, e.d_gcols);
   e.cap_cols = e.cap_ph = 0;
   e.np = 0;
@@ -1187,6 +1224,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
     if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
   if (!e.ev_adm) SG_CUDA(c, cudaEventCreate(&e.ev_adm));
   if (!e.ev_pheno) SG_CUDA(c, cudaEventCreateWithFlags(&e.ev_pheno, cudaEventDisableTiming));
+  if (!e.ev_up) SG_CUDA(c, cudaEventCreateWithFlags(&e.ev_up, cudaEventDisableTiming));
   e.have_prev = false;
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_gcols), max_columns * sizeof(int32_t), cudaHostAllocDefault));
@@ -1230,12 +1268,14 @@ extern "C" int sg_engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phe
 // the cohort's codes of every .bim marker with the subset as the phenotype mask; the host turns them
 // into d' = 1/sd'^2 (GRM markers), 2p', the fill-changed markers and the diagonal table.  dmask: the
 // mask bytes already on the device (side stream), or nullptr for every sample.
-static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint8_t* dmask) {
+// First half of a slot's subset set-up, on the side stream: the subset's QC records (the kernel
+// setgeno uses, run with the subset as the phenotype mask), then d', 2p', the diagonal table, the
+// fill-change list and the two counts the host needs, copied to pinned memory; ev_prep marks the
+// end.  Nothing here waits for the device.
+static int subset_prepare(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   Engine& e = c->eng;
   Engine::SlotSub& ss = e.sub[slot];
   const int64_t nn = c->nn, np = e.np, mg = c->mg, m = c->m_bim;
-  if (ss.valid && ((!mask && ss.all) || (mask && !ss.all && std::memcmp(ss.mask.data(), mask, nn) == 0)))
-    return SG_OK;
   const int64_t nwords = (nn + 15) / 16;
   std::vector<uint32_t> maskbits(nwords + 1, 0u);
   int64_t ns = 0;
@@ -1245,66 +1285,70 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
       ++ns;
     }
   if (ns == 0) return set_err(c, SG_ERR_INVALID, "phenotype slot %lld: empty sample subset", (long long)slot);
-  uint32_t* d_mb = nullptr;
-  MarkerQC* d_qc = nullptr;
-  SG_TRY(dev_alloc_t(c, &d_mb, maskbits.size()));
-  SG_TRY(dev_alloc_t(c, &d_qc, (size_t)std::max<int64_t>(m, 1)));
-  SG_CUDA(c, cudaMemcpyAsync(d_mb, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, c->side));
-  launch_marker_qc(c->d_codes, c->pitch, m, nn, d_mb, ns, c->qc_min_maf, c->qc_max_missing, c->d_vrflag_all,
-                   c->qc_min_mac_vr, c->qc_max_mac_vr, c->qc_is_var_ratio, d_qc, c->side);
-  SG_LAUNCHED(c, 1);
-  std::vector<MarkerQC> qc(m);
-  if (m) SG_CUDA(c, cudaMemcpyAsync(qc.data(), d_qc, m * sizeof(MarkerQC), cudaMemcpyDeviceToHost, c->side));
-  SG_TRY(sync_side(c));
-  dev_free(c, d_mb);
-  dev_free(c, d_qc);
-  std::vector<float> dp(mg, 0.0f), p2(mg, 0.0f), lut(4 * mg, 0.0f), dfill;
-  std::vector<int32_t> flips;
-  int64_t mprime = 0;
-  for (int64_t k = 0; k < m; ++k) {
-    const MarkerQC& q = qc[k];
-    if (!q.pass_qc) continue;
-    ++mprime;
-    const double d = (double)q.invstd * (double)q.invstd;
-    const float two_p = 2.0f * q.freq;  // exact: the LUT's 2p (setStdGenoLookUpArr FIT.cpp:152-159)
-    dp[k] = (float)d;
-    p2[k] = two_p;
-    // packed codes 00 -> 2, 01 -> missing (the subset fill), 10 -> 1, 11 -> 0
-    const double g[4] = {2.0, (double)q.fill, 1.0, 0.0};
-    for (int t = 0; t < 4; ++t) lut[4 * k + t] = (float)(d * (g[t] - two_p) * (g[t] - two_p));
-    if (q.fill != c->fill_all[k]) {
-      flips.push_back((int32_t)k);
-      dfill.push_back((float)(q.fill - c->fill_all[k]));
-    }
-  }
-  if (mprime == 0) return set_err(c, SG_ERR_STATE, "phenotype slot %lld: no marker passes QC in its subset", (long long)slot);
-  const int nflip = (int)flips.size();
-  const int W = (nflip + 31) / 32;
+  // the slot's buffers (kept; the fill-change list has room for every marker)
+  if (!ss.qc) SG_TRY(dev_alloc_t(c, &ss.qc, (size_t)std::max<int64_t>(m, 1)));
+  if (!ss.flag) SG_TRY(dev_alloc_t(c, &ss.flag, (size_t)mg));
+  if (!ss.mb) SG_TRY(dev_alloc_t(c, &ss.mb, (size_t)(nwords + 1)));
+  if (!ss.d_counts) SG_TRY(dev_alloc_t(c, &ss.d_counts, (size_t)2));
+  if (!ss.h_counts) SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&ss.h_counts), 2 * sizeof(int64_t),
+                                             cudaHostAllocDefault));
+  if (!ss.ev_prep) SG_CUDA(c, cudaEventCreateWithFlags(&ss.ev_prep, cudaEventDisableTiming));
   if (!ss.dp) SG_TRY(dev_alloc_t(c, &ss.dp, (size_t)mg));
   if (!ss.p2) SG_TRY(dev_alloc_t(c, &ss.p2, (size_t)mg));
   if (!ss.lut) SG_TRY(dev_alloc_t(c, &ss.lut, (size_t)(4 * mg)));
   if (!ss.diag) SG_TRY(dev_alloc_t(c, &ss.diag, (size_t)np));
-  if (nflip > ss.flip_cap) {
-    dev_free_t(c, ss.flips);
-    dev_free_t(c, ss.dfill);
-    SG_TRY(dev_alloc_t(c, &ss.flips, (size_t)nflip));
-    SG_TRY(dev_alloc_t(c, &ss.dfill, (size_t)nflip));
-    ss.flip_cap = nflip;
-  }
+  if (!ss.flips) SG_TRY(dev_alloc_t(c, &ss.flips, (size_t)std::max<int64_t>(m, 1)));
+  if (!ss.dfill) SG_TRY(dev_alloc_t(c, &ss.dfill, (size_t)std::max<int64_t>(m, 1)));
+  if (ss.prep) SG_CUDA(c, cudaEventSynchronize(ss.ev_prep));  // an earlier prepare still owns the buffers
+  // the copy from pageable memory is staged before the call returns
+  SG_CUDA(c, cudaMemcpyAsync(ss.mb, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, c->side));
+  launch_marker_qc(c->d_codes, c->pitch, m, nn, ss.mb, ns, c->qc_min_maf, c->qc_max_missing, c->d_vrflag_all,
+                   c->qc_min_mac_vr, c->qc_max_mac_vr, c->qc_is_var_ratio, ss.qc, c->side);
+  // d' = 1/sd'^2, 2p' and the diagonal table per marker, the fill-changed markers in marker order,
+  // on the device (setGenoObj's per-marker values over the subset, FIT.cpp:436-495, 152-159)
+  launch_subset_derive(ss.qc, c->d_fill_all, m, mg, ss.dp, ss.p2, ss.lut, ss.flag, ss.flips, ss.dfill,
+                       ss.d_counts, c->side);
+  SG_LAUNCHED(c, 3);
+  SG_CUDA(c, cudaMemcpyAsync(ss.h_counts, ss.d_counts, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->side));
+  SG_CUDA(c, cudaEventRecord(ss.ev_prep, c->side));
+  ss.valid = false;
+  ss.prep = true;
+  ss.prep_all = mask == nullptr;
+  if (mask) ss.prep_mask.assign(mask, mask + nn);
+  else ss.prep_mask.clear();
+  ss.prep_ns = ns;
+  return SG_OK;
+}
+
+static bool same_mask(bool all, const std::vector<uint8_t>& kept, const uint8_t* mask, int64_t nn) {
+  return (!mask && all) || (mask && !all && std::memcmp(kept.data(), mask, nn) == 0);
+}
+
+// Subset-exact engine: the state of slot ``slot``'s sample subset, rebuilt only when its mask
+// changes.  The subset's per-marker counts, fill, QC, frequency and 1/sd come from the same kernel
+// setgeno uses (genoClass::setGenoObj over the subset, FIT.cpp:376-385, 436-495, 916-921), run on
+// the cohort's codes of every .bim marker with the subset as the phenotype mask; the device turns
+// them into d' = 1/sd'^2 (GRM markers), 2p', the fill-changed markers and the diagonal table.
+// dmask: the mask bytes already on the device (side stream), or nullptr for every sample.  The
+// first half runs here unless sg_engine_prepare_subset launched it for this mask already.
+static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint8_t* dmask) {
+  Engine& e = c->eng;
+  Engine::SlotSub& ss = e.sub[slot];
+  const int64_t nn = c->nn, np = e.np, m = c->m_bim;
+  if (ss.valid && same_mask(ss.all, ss.mask, mask, nn)) return SG_OK;
+  if (!(ss.prep && same_mask(ss.prep_all, ss.prep_mask, mask, nn))) SG_TRY(subset_prepare(c, slot, mask));
+  SG_CUDA(c, cudaEventSynchronize(ss.ev_prep));
+  ss.prep = false;
+  const int64_t nflip = ss.h_counts[0], mprime = ss.h_counts[1], ns = ss.prep_ns;
+  if (mprime == 0) return set_err(c, SG_ERR_STATE, "phenotype slot %lld: no marker passes QC in its subset", (long long)slot);
+  if (!e.sdiag_part) SG_TRY(dev_alloc_t(c, &e.sdiag_part, (size_t)subset_diag_scratch(m, np)));
+  const int W = (int)((nflip + 31) / 32);
   if ((int64_t)W * np > ss.bits_cap) {
     dev_free_t(c, ss.bits);
     SG_TRY(dev_alloc_t(c, &ss.bits, (size_t)(W * np)));
     ss.bits_cap = (int64_t)W * np;
   }
-  SG_CUDA(c, cudaMemcpyAsync(ss.dp, dp.data(), mg * 4, cudaMemcpyHostToDevice, c->side));
-  SG_CUDA(c, cudaMemcpyAsync(ss.p2, p2.data(), mg * 4, cudaMemcpyHostToDevice, c->side));
-  SG_CUDA(c, cudaMemcpyAsync(ss.lut, lut.data(), 4 * mg * 4, cudaMemcpyHostToDevice, c->side));
-  if (nflip) {
-    SG_CUDA(c, cudaMemcpyAsync(ss.flips, flips.data(), nflip * 4, cudaMemcpyHostToDevice, c->side));
-    SG_CUDA(c, cudaMemcpyAsync(ss.dfill, dfill.data(), nflip * 4, cudaMemcpyHostToDevice, c->side));
-  }
-  launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, nflip, W, dmask, nn, np, ss.bits, c->side);
-  if (!e.sdiag_part) SG_TRY(dev_alloc_t(c, &e.sdiag_part, (size_t)subset_diag_scratch(m, np)));
+  launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, (int)nflip, W, dmask, nn, np, ss.bits, c->side);
   launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, e.sdiag_part, ss.diag, c->side);
   SG_LAUNCHED(c, W > 0 ? 3 : 2);
   ss.dev.dprime = ss.dp;
@@ -1312,20 +1356,56 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
   ss.dev.flips = ss.flips;
   ss.dev.dfill = ss.dfill;
   ss.dev.bits = ss.bits;
-  ss.dev.nflip = nflip;
+  ss.dev.nflip = (int32_t)nflip;
   ss.dev.W = W;
   ss.dev.inv_m = 1.0 / (double)mprime;
   ss.dev.ns = (double)ns;
+  // a small copy from pageable memory: staged before the call returns, so nothing waits for it
   SG_CUDA(c, cudaMemcpyAsync(e.d_slots + slot, &ss.dev, sizeof(SubsetSlot), cudaMemcpyHostToDevice, c->side));
-  SG_TRY(sync_side(c));  // the host vectors above must outlive their copies
   ss.m_prime = (double)mprime;
-  ss.all = mask == nullptr;
-  if (mask) ss.mask.assign(mask, mask + nn);
-  else ss.mask.clear();
+  ss.all = ss.prep_all;
+  ss.mask.swap(ss.prep_mask);
+  ss.prep_mask.clear();
   ss.valid = true;
+  // over every slot's device record, kept ones included: a forgotten slot's columns may still run
   e.max_w = 0;
-  for (const auto& x : e.sub)
-    if (x.valid) e.max_w = std::max(e.max_w, (int)x.dev.W);
+  for (const auto& x : e.sub) e.max_w = std::max(e.max_w, (int)x.dev.W);
+  return SG_OK;
+}
+
+extern "C" int sg_engine_prepare_subset(sg_ctx* c, int64_t slot, const uint8_t* mask) {
+  NEED_OPERATOR(c);
+  Engine& e = c->eng;
+  if (c->mv_mode != SG_MV_SUBSET_EXACT) return SG_OK;  // the other engines keep no subset state
+  if (e.cap_ph == 0) SG_TRY(engine_reserve(c, 128, std::max<int64_t>(slot + 1, 1)));
+  if (slot < 0 || slot >= e.cap_ph) return set_err(c, SG_ERR_INVALID, "phenotype slot %lld out of range", (long long)slot);
+  for (auto& kv : e.reqs)
+    if (kv.second.state == 1 && kv.second.slot == slot)
+      return set_err(c, SG_ERR_STATE, "phenotype slot %lld has columns in flight", (long long)slot);
+  Engine::SlotSub& ss = e.sub[slot];
+  if (ss.valid && same_mask(ss.all, ss.mask, mask, c->nn)) return SG_OK;
+  if (ss.prep && same_mask(ss.prep_all, ss.prep_mask, mask, c->nn)) return SG_OK;
+  return subset_prepare(c, slot, mask);
+}
+
+// Reads only the slot's event (set by the prepare this thread made), so the caller may wait here
+// without serialising with other threads' engine calls.
+extern "C" int sg_engine_subset_wait(sg_ctx* c, int64_t slot) {
+  if (!c) return SG_ERR_INVALID;
+  Engine& e = c->eng;
+  if (slot < 0 || slot >= (int64_t)e.sub.size()) return SG_OK;
+  const Engine::SlotSub& ss = e.sub[slot];
+  if (ss.prep && ss.ev_prep) (void)cudaEventSynchronize(ss.ev_prep);
+  return SG_OK;
+}
+
+extern "C" int sg_engine_forget_subsets(sg_ctx* c) {
+  NEED_OPERATOR(c);
+  for (auto& ss : c->eng.sub) {
+    ss.valid = false;
+    if (ss.prep) cudaEventSynchronize(ss.ev_prep);
+    ss.prep = false;
+  }
   return SG_OK;
 }
 
@@ -1403,12 +1483,20 @@ static int engine_submit_common(sg_ctx* c, int64_t slot, int kind, const double*
     r.seed = seed;
     r.run = run0 + j;
     if (!probe) {
-      if (!slab_get(c, r)) return set_err(c, SG_ERR_NOMEM, "no pinned host memory for a right-hand side");
+      if (!slab_get(c, r)) return set_err(c, SG_ERR_NOMEM, "no memory for a right-hand side's slab");
       std::memcpy(r.b, B + j * c->nn, c->nn * sizeof(double));
+      // up now, on the upload stream, while the step in flight runs: admission gathers on the device
+      SG_CUDA(c, cudaMemcpyAsync(const_cast<double*>(r.bd), r.b, c->nn * sizeof(double), cudaMemcpyHostToDevice,
+                                 c->up));
+      e.io_h2d += (uint64_t)(c->nn * 8);
     }
     if (ids) ids[j] = r.id;
     e.queue.push_back(r.id);
     e.reqs.emplace(r.id, std::move(r));
+  }
+  if (!probe && k > 0) {
+    SG_CUDA(c, cudaEventRecord(e.ev_up, c->up));
+    e.up_wait = true;
   }
   return SG_OK;
 }
@@ -1480,21 +1568,24 @@ static int flush_states(sg_ctx* c, bool wait) {
   return wait ? sync(c) : SG_OK;
 }
 
-// Pinned, device-mapped slabs of nn doubles for queued right-hand sides (grown 32 at a time, kept
-// until the engine is freed); admission's gather kernel reads them through their device address.
+// Slabs of nn doubles for queued right-hand sides, each a pinned host buffer and a device buffer
+// (grown 32 at a time, kept until the engine is freed): a submission copies its right-hand side
+// into the host slab and uploads it to the device slab on the upload stream at once; admission's
+// gather kernel reads the device slab.
 static bool slab_get(sg_ctx* c, Req& r) {
   Engine& e = c->eng;
   if (e.slab_free.empty()) {
     constexpr int64_t kPer = 32;
+    const size_t bytes = (size_t)(kPer * c->nn) * sizeof(double);
     void* blk = nullptr;
-    if (cudaHostAlloc(&blk, (size_t)(kPer * c->nn) * sizeof(double), cudaHostAllocMapped) != cudaSuccess)
-      return false;
+    if (cudaHostAlloc(&blk, bytes, cudaHostAllocDefault) != cudaSuccess) return false;
     void* dblk = nullptr;
-    if (cudaHostGetDevicePointer(&dblk, blk, 0) != cudaSuccess) {
+    if (dev_alloc(c, &dblk, bytes) != SG_OK) {
       cudaFreeHost(blk);
       return false;
     }
     e.slab_blocks.push_back(blk);
+    e.slab_dblocks.push_back(dblk);
     for (int64_t k = 0; k < kPer; ++k)
       e.slab_free.emplace_back(static_cast<double*>(blk) + k * c->nn, static_cast<const double*>(dblk) + k * c->nn);
   }
@@ -1535,8 +1626,9 @@ static int detach_dependents(sg_ctx* c, Req& src) {
     auto it = e.reqs.find(d);
     if (it == e.reqs.end()) continue;
     Req& r = it->second;
-    if (src.state == 2 && src.col >= 0 && r.b) {
-      SG_CUDA(c, d2h(c, r.b, e.X + src.col * e.np, c->nn * 8, c->side));
+    if (src.state == 2 && src.col >= 0 && r.bd) {
+      SG_CUDA(c, cudaMemcpyAsync(const_cast<double*>(r.bd), e.X + src.col * e.np, c->nn * 8,
+                                 cudaMemcpyDeviceToDevice, c->side));
       r.src = -1;
       copied = true;
     } else {
@@ -1549,6 +1641,10 @@ static int detach_dependents(sg_ctx* c, Req& src) {
 
 static int engine_admit(sg_ctx* c) {
   Engine& e = c->eng;
+  if (e.up_wait) {  // right-hand sides uploaded since the last admission (long since, as a rule)
+    SG_CUDA(c, cudaStreamWaitEvent(c->stream, e.ev_up, 0));
+    e.up_wait = false;
+  }
   if (e.pheno_main_wait) {  // slot weights uploaded since the last launch: the step reads them
     SG_CUDA(c, cudaStreamWaitEvent(c->stream, e.ev_pheno, 0));
     e.pheno_main_wait = false;
@@ -1604,7 +1700,7 @@ static int engine_admit(sg_ctx* c) {
         pruns.push_back(r.run);
         psel.push_back((int32_t)sel);
       } else {
-        rsrc.push_back(r.bd);  // read by the gather kernel straight from mapped pinned host memory
+        rsrc.push_back(r.bd);  // the device slab, uploaded at submission
         rsel.push_back((int32_t)sel);
       }
       ColState s{};
@@ -1640,7 +1736,6 @@ static int engine_admit(sg_ctx* c) {
       launch_gather_rhs(reinterpret_cast<const double* const*>(db), reinterpret_cast<const int32_t*>(db + kr * sizeof(void*)),
                         (int64_t)kr, c->nn, e.np, e.B, c->stream);
       SG_LAUNCHED(c, 1);
-      e.io_h2d += (uint64_t)(kr * c->nn * 8);
     }
     if (!psel.empty()) {
       // one launch for every probe of this admission round; its index table (uint64 seeds |

@@ -100,6 +100,7 @@ struct Fit {
   bool started = false;   // main_start has run
   bool busy = false;      // handed to a worker thread (only the stepping thread reads or writes it)
   int64_t reserved = 0;   // engine columns set aside at admission until main_start has submitted
+  double t_submit = 0, t_admit = 0, t_done = 0;  // steady-clock seconds: added, given a slot, retired
 };
 
 // Host threads that resume fits.  The thread that steps the engine hands a fit over (push) and
@@ -190,6 +191,7 @@ struct sg_fits {
   sg_ctx* ctx = nullptr;
   int64_t n = 0, max_columns = 0, max_fits = 0;
   bool pipelined = true, launched = false;
+  double t_created = 0;  // steady-clock seconds at sg_fits_create
   std::vector<int64_t> free_slots;
   std::map<int64_t, std::unique_ptr<Fit>> active;   // admitted, running
   std::deque<std::unique_ptr<Fit>> pending;          // waiting for a slot and columns
@@ -203,6 +205,9 @@ struct sg_fits {
   double t_engine = 0, t_host = 0;
   double t_pheno = 0, t_submit = 0, t_fetch = 0, t_dots = 0;  // parts of t_host spent in engine calls
   double t_launch = 0;                                          // part of t_engine spent launching
+  // parts of t_engine on the stepping thread with workers: waiting for the step, for the driver's
+  // lock (an engine call of a worker in progress), finishing the step, scanning for ready fits
+  double t_wait = 0, t_lock = 0, t_finish = 0, t_scan = 0;
   double gpu_ms_seen = 0;                                      // engine step time already budgeted
   double launch_wait_s = 0.0;  // with workers: how long a launch may wait for the fits just made ready
   int idle_passes = 0;         // consecutive stepping passes in which nothing could run
@@ -388,9 +393,17 @@ void own(sg_fits* F, Fit& f, const std::vector<int64_t>& ids) {
 }
 
 bool set_pheno(sg_fits* F, Fit& f, const std::vector<double>& W, const double* tau) {
-  return eng(F, f, &F->t_pheno, [&] {
-    return sg_engine_set_pheno(F->ctx, f.slot, W.data(), tau, f.has_mask ? f.mask.data() : nullptr);
-  });
+  const uint8_t* mask = f.has_mask ? f.mask.data() : nullptr;
+  // a new subset: its QC and tables run on the device while this thread waits without the lock,
+  // so the stepping thread can turn steps around meanwhile (no-ops once the slot holds the subset)
+  if (!eng(F, f, &F->t_pheno, [&] { return sg_engine_prepare_subset(F->ctx, f.slot, mask); })) return false;
+  const double t = now_s();
+  sg_engine_subset_wait(F->ctx, f.slot);
+  {
+    std::lock_guard<std::mutex> g(F->mu);
+    F->t_pheno += now_s() - t;
+  }
+  return eng(F, f, &F->t_pheno, [&] { return sg_engine_set_pheno(F->ctx, f.slot, W.data(), tau, mask); });
 }
 
 bool submit(sg_fits* F, Fit& f, int kind, const double* B, int64_t k, int maxiter, double tol,
@@ -884,6 +897,7 @@ void retire(sg_fits* F, int64_t fid) {
   f->reserved = 0;
   F->free_slots.push_back(f->slot);
   F->finished_order.push_back(fid);
+  f->t_done = now_s();
   F->done_fits[fid] = std::move(f);
 }
 
@@ -925,6 +939,7 @@ void admit(sg_fits* F) {
     F->pending.pop_front();
     f->slot = F->free_slots.back();
     F->free_slots.pop_back();
+    f->t_admit = now_s();
     {
       std::lock_guard<std::mutex> g(F->mu);
       sg_engine_probe_cache_clear(F->ctx, f->slot);  // a new sample mask takes this slot
@@ -980,6 +995,7 @@ extern "C" int sg_fits_create(sg_ctx* ctx, int64_t max_columns, int64_t max_fits
   F->max_columns = max_columns;
   F->max_fits = max_fits;
   F->pipelined = pipelined != 0;
+  F->t_created = now_s();
   for (int64_t s = max_fits - 1; s >= 0; --s) F->free_slots.push_back(s);
   const unsigned hw = std::thread::hardware_concurrency();
   const int workers = (int)std::min<unsigned>(7u, hw > 2 ? hw / 2 - 1 : 0u);
@@ -1067,6 +1083,7 @@ static int fits_submit_impl(sg_fits* F, int trait, int64_t n_sub, const uint8_t*
     return fits_err(F, SG_ERR_INVALID, "a fit with %d probes needs %lld engine columns, the engine has %lld", nrun,
                     (long long)need_columns(*f), (long long)F->max_columns);
   f->id = F->next_id++;
+  f->t_submit = now_s();
   if (fit_id) *fit_id = f->id;
   F->pending.push_back(std::move(f));
   admit(F);
@@ -1185,6 +1202,8 @@ static int run_async(sg_fits* F, int64_t max_steps, size_t before) {
     if (F->active.empty() && F->pending.empty()) break;
     double t = now_s();
     if (F->launched) sg_engine_wait(F->ctx);
+    const double t_waited = now_s();
+    F->t_wait += t_waited - t;
     // under one hold of the lock: finish the step, mark its columns done, collect the fits they
     // make ready and (without a launch wait) launch the next step
     int rc = SG_OK;
@@ -1192,10 +1211,15 @@ static int run_async(sg_fits* F, int64_t max_steps, size_t before) {
     bool launch_now = F->launch_wait_s <= 0.0;
     {
       StepLock g(F);
+      const double t_locked = now_s();
+      F->t_lock += t_locked - t_waited;
       int64_t fin = 0;
       if (F->launched) rc = sg_engine_finish(F->ctx, &fin);
       F->launched = false;
+      const double t_finished = now_s();
+      F->t_finish += t_finished - t_locked;
       if (rc == SG_OK) rc = poll_done(F);
+      F->t_scan += now_s() - t_finished;
       if (rc == SG_OK) {
         take_back(F);
         for (auto& kv : F->active) {
@@ -1283,6 +1307,28 @@ extern "C" int sg_fits_host_times(sg_fits* F, double* t8) {
   t8[5] = F->t_fetch;
   t8[6] = F->t_dots;
   t8[7] = F->t_launch;
+  return SG_OK;
+}
+
+extern "C" int sg_fits_fit_times(sg_fits* F, int64_t fit_id, double* t3) {
+  if (!F || !t3) return SG_ERR_INVALID;
+  std::lock_guard<std::mutex> g(F->mu);
+  auto it = F->done_fits.find(fit_id);
+  if (it == F->done_fits.end()) return fits_err(F, SG_ERR_NOT_FOUND, "fit %lld is not finished", (long long)fit_id);
+  const Fit& f = *it->second;
+  t3[0] = f.t_submit - F->t_created;
+  t3[1] = f.t_admit - F->t_created;
+  t3[2] = f.t_done - F->t_created;
+  return SG_OK;
+}
+
+extern "C" int sg_fits_step_times(sg_fits* F, double* t4) {
+  if (!F || !t4) return SG_ERR_INVALID;
+  std::lock_guard<std::mutex> g(F->mu);
+  t4[0] = F->t_wait;
+  t4[1] = F->t_lock;
+  t4[2] = F->t_finish;
+  t4[3] = F->t_scan;
   return SG_OK;
 }
 

@@ -80,6 +80,96 @@ void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int
                                           static_cast<__nv_bfloat16*>(Gsm));
 }
 
+// A subset's GRM tables from its per-marker QC records, as setgeno over the subset builds them
+// (the LUT's 2p and 1/sd: FIT.cpp:152-159): for each GRM marker of the subset, d' = (1/sd')^2,
+// 2p', and lut4 = d' (g - 2p')^2 for the four packed codes (00 -> 2, 01 -> the subset's own fill,
+// 10 -> 1, 11 -> 0); zeros elsewhere and past m.  flag bit 0: a GRM marker whose subset fill
+// differs from the cohort fill G holds; bit 1: a GRM marker of the subset.
+__global__ void subset_derive_kernel(const MarkerQC* __restrict__ qc, const int32_t* __restrict__ fill_all,
+                                     int64_t m, int64_t mg, float* __restrict__ dp, float* __restrict__ p2,
+                                     float4* __restrict__ lut4, uint8_t* __restrict__ flag) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= mg) return;
+  float d32 = 0.0f, tp = 0.0f;
+  float4 l = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  uint8_t f = 0;
+  if (k < m) {
+    const MarkerQC q = qc[k];
+    if (q.pass_qc) {
+      const double d = (double)q.invstd * (double)q.invstd;
+      const float two_p = 2.0f * q.freq;
+      d32 = (float)d;
+      tp = two_p;
+      const double t0 = 2.0 - (double)two_p, t1 = (double)q.fill - (double)two_p;
+      const double t2 = 1.0 - (double)two_p, t3 = 0.0 - (double)two_p;
+      l.x = (float)(d * t0 * t0);
+      l.y = (float)(d * t1 * t1);
+      l.z = (float)(d * t2 * t2);
+      l.w = (float)(d * t3 * t3);
+      f = (uint8_t)(2u | (q.fill != fill_all[k] ? 1u : 0u));
+    }
+  }
+  dp[k] = d32;
+  p2[k] = tp;
+  lut4[k] = l;
+  flag[k] = f;
+}
+
+// The fill-changed markers in marker order (flips, and dfill = subset fill - cohort fill) and the
+// counts (nflip, M') in counts[0..1]: one block, each thread a contiguous run of markers, an
+// exclusive scan of the runs' flip counts giving each run its output offset.
+constexpr int kFlipThreads = 1024;
+
+__global__ void __launch_bounds__(kFlipThreads)
+subset_flips_kernel(const MarkerQC* __restrict__ qc, const int32_t* __restrict__ fill_all,
+                    const uint8_t* __restrict__ flag, int64_t m, int32_t* __restrict__ flips,
+                    float* __restrict__ dfill, int64_t* __restrict__ counts) {
+  __shared__ int32_t scan[kFlipThreads];
+  __shared__ int32_t grm[kFlipThreads];
+  const int t = threadIdx.x;
+  const int64_t per = (m + kFlipThreads - 1) / kFlipThreads;
+  const int64_t k0 = (int64_t)t * per;
+  const int64_t k1 = k0 + per < m ? k0 + per : m;
+  int32_t nf = 0, ng = 0;
+  for (int64_t k = k0; k < k1; ++k) {
+    const uint8_t f = flag[k];
+    nf += f & 1u;
+    ng += (f >> 1) & 1u;
+  }
+  scan[t] = nf;
+  grm[t] = ng;
+  __syncthreads();
+  // inclusive Hillis-Steele scan of the flip counts, tree sum of the GRM-marker counts
+  for (int o = 1; o < kFlipThreads; o <<= 1) {
+    const int32_t a = t >= o ? scan[t - o] : 0;
+    __syncthreads();
+    scan[t] += a;
+    __syncthreads();
+  }
+  for (int o = kFlipThreads / 2; o > 0; o >>= 1) {
+    if (t < o) grm[t] += grm[t + o];
+    __syncthreads();
+  }
+  int32_t pos = scan[t] - nf;
+  for (int64_t k = k0; k < k1; ++k)
+    if (flag[k] & 1u) {
+      flips[pos] = (int32_t)k;
+      dfill[pos] = (float)(qc[k].fill - fill_all[k]);
+      ++pos;
+    }
+  if (t == 0) {
+    counts[0] = scan[kFlipThreads - 1];
+    counts[1] = grm[0];
+  }
+}
+
+void launch_subset_derive(const MarkerQC* qc, const int32_t* fill_all, int64_t m, int64_t mg, float* dp, float* p2,
+                          float* lut4, uint8_t* flag, int32_t* flips, float* dfill, int64_t* counts, cudaStream_t s) {
+  subset_derive_kernel<<<(unsigned)((mg + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+      qc, fill_all, m, mg, dp, p2, reinterpret_cast<float4*>(lut4), flag);
+  subset_flips_kernel<<<1, kFlipThreads, 0, s>>>(qc, fill_all, flag, m, flips, dfill, counts);
+}
+
 // Bit map of a slot's fill-changed markers, word-major (word w of sample i at bits[w * np + i], so
 // that a warp's samples read consecutive words): bit b is set when marker flips[32 w + b] is
 // missing at sample i and i is in the subset (mask).

@@ -816,7 +816,7 @@ static int g_opt[kTcOptions] = {
     8,    // kTcSyrkGroup: row tiles per raster group of the SYRK
     0,    // kTcGrmvSlice: K slice bytes of the split-BF16 GRM.V (0: by width, 64 or 128)
     2,    // kTcSubsetPair: subset-exact genotype GEMMs on CTA pairs (2: above 160 columns)
-    128,  // kTcSubsetSlice: their K slice bytes (0: 128 up to 160 columns, else 64; or 64 / 128)
+    256,  // kTcSubsetSlice: their K-stage bytes (0: 128 up to 160 columns, else 64; or 64 / 128 / 256)
 };
 
 bool tc_set_option(int opt, int value) {
@@ -999,8 +999,8 @@ int tc_gemm_tile_n(int64_t ncols, int set) {
 }
 
 // CTA pairs for a subset-exact genotype GEMM over ncols columns: measured at N = 100k, M = 150k,
-// 128-byte K slices, pairs took 512 columns from 49.7 to 36.5 ms and 1024 from 89.2 to 72.7 ms,
-// and were 7-11% slower up to 128 columns, where the launch streams G from HBM.
+// 256-byte K stages, pairs took 512 columns from 49.7 to 32.8 ms and 1024 from 89.4 to 61.8 ms,
+// and were 5-12% slower up to 128 columns, where the launch streams G from HBM.
 static bool subset_pair(int64_t ncols) {
   for (const GrmvChoice& b : g_subset_plan)
     if (ncols <= b.max_cols) return b.pair != 0;

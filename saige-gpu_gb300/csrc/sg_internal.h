@@ -208,6 +208,10 @@ struct SubsetSlot {
 };
 void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int64_t m, int64_t nn, int64_t mg,
                    int64_t np, void* Gmm, void* Gsm, cudaStream_t s);
+// the subset's d', 2p', diagonal table, fill-change list and counts (nflip, M') from its QC records;
+// flag: mg bytes of scratch, flips / dfill: room for m entries, counts: 2 int64 on the device
+void launch_subset_derive(const MarkerQC* qc, const int32_t* fill_all, int64_t m, int64_t mg, float* dp, float* p2,
+                          float* lut4, uint8_t* flag, int32_t* flips, float* dfill, int64_t* counts, cudaStream_t s);
 void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* flips, int nflip, int W,
                           const uint8_t* mask, int64_t nn, int64_t np, uint32_t* bits, cudaStream_t s);
 // part: subset_diag_scratch(m, np) floats of scratch

@@ -91,6 +91,9 @@ SIGNATURES = {
                            C.c_int, C.c_float, C.c_float, C.c_float, c_u64],
     "sg_engine_reserve": [c_ctx, c_i64, c_i64],
     "sg_engine_set_pheno": [c_ctx, c_i64, P_f64, P_f64, P_u8],
+    "sg_engine_forget_subsets": [c_ctx],
+    "sg_engine_prepare_subset": [c_ctx, c_i64, P_u8],
+    "sg_engine_subset_wait": [c_ctx, c_i64],
     "sg_engine_submit": [c_ctx, c_i64, C.c_int, P_f64, c_i64, C.c_int, C.c_double, P_i64],
     "sg_engine_submit_probes": [c_ctx, c_i64, C.c_int, c_u64, c_i64, c_i64, C.c_int, C.c_double,
                                 P_i64],
@@ -127,6 +130,8 @@ SIGNATURES = {
     "sg_fits_poll": [C.c_void_p, P_i64, c_i64, P_i64],
     "sg_fits_counts": [C.c_void_p, P_i64, P_i64, P_i64],
     "sg_fits_host_times": [C.c_void_p, P_f64],
+    "sg_fits_step_times": [C.c_void_p, P_f64],
+    "sg_fits_fit_times": [C.c_void_p, c_i64, P_f64],
     "sg_fits_result": [C.c_void_p, c_i64, P_f64, P_f64, P_f64, P_f64, P_f64, P_f64, P_i32, P_i32, P_i64],
 }
 _RESTYPE = {"sg_ctx_destroy": None, "sg_last_error": C.c_char_p, "sg_fits_destroy": None,

@@ -146,6 +146,10 @@ class Context:
         self._call("sg_set_matvec_mode", int(mode))
         self._mv_mode = int(mode)
 
+    def matvec_mode(self):
+        """The engine last selected through set_matvec_mode (None before the first call)."""
+        return getattr(self, "_mv_mode", None)
+
     # ------------------------------------------------------------ genotypes (setgeno)
     @staticmethod
     def _geno_args(n_fam, sub_1based, pheno_mask, vr_random):
@@ -470,6 +474,18 @@ class Context:
         m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
         self._call("sg_engine_set_pheno", int(slot), _ptr(w, L.P_f64), _ptr(tau, L.P_f64),
                    None if m is None else _ptr(m, L.P_u8))
+
+    def engine_prepare_subset(self, slot, mask=None):
+        """Launch the first half of a slot's subset set-up without waiting (subset-exact engine)."""
+        m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+        self._call("sg_engine_prepare_subset", int(slot), None if m is None else _ptr(m, L.P_u8))
+
+    def engine_subset_wait(self, slot):
+        self._call("sg_engine_subset_wait", int(slot))
+
+    def engine_forget_subsets(self):
+        """Subset-exact engine: rebuild every slot's subset state at its next engine_set_pheno."""
+        self._call("sg_engine_forget_subsets")
 
     def engine_submit(self, slot, kind, B, maxiter=500, tol=1e-5):
         flat, k = _cols(np.asarray(B, np.float64))

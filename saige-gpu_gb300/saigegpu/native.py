@@ -92,8 +92,18 @@ class NativeFits:
         """Seconds: engine stepping, driver work (and its pheno / submit / fetch / probe_dots parts)."""
         t = np.zeros(8)
         self._check(self._L.sg_fits_host_times(self._h, t.ctypes.data_as(L.P_f64)))
+        u = np.zeros(4)
+        self._check(self._L.sg_fits_step_times(self._h, u.ctypes.data_as(L.P_f64)))
         return {"engine": t[0], "driver": t[1], "steps": int(t[2]), "pheno": t[3], "submit": t[4],
-                "fetch": t[5], "probe_dots": t[6], "launch": t[7]}
+                "fetch": t[5], "probe_dots": t[6], "launch": t[7], "step_wait": u[0], "lock_wait": u[1],
+                "finish": u[2], "mark_done": u[3]}
+
+    def fit_times(self, fid):
+        """(added, admitted, finished) seconds since the driver was created, for a finished fit not
+        yet collected by ``result``."""
+        t = np.zeros(3)
+        self._check(self._L.sg_fits_fit_times(self._h, int(fid), t.ctypes.data_as(L.P_f64)))
+        return float(t[0]), float(t[1]), float(t[2])
 
     def result(self, fid):
         """(result dict, column iterations); the dict has the keys of ``serve.fit_generator``'s."""
@@ -121,14 +131,20 @@ class _Job:
         self.column_iterations = 0
         self.columns = 0
         self.host_times = {}
+        self.service_s = None  # admission to a slot -> finished (native driver)
 
 
 def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True, threads=None, lib=None,
               launch_wait_ms=None):
-    """Fit all ``specs`` together in native code; returns (results or exceptions, jobs) in order."""
+    """Fit all ``specs`` together in native code; returns (results or exceptions, jobs) in order.
+    With max_phenos below len(specs) at most that many fits run at once, the others entering as
+    running ones finish (a stream through max_phenos phenotype slots)."""
     from .serve import columns_for
-    max_columns = max(max_columns or 0, columns_for(specs))
-    drv = NativeFits(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined, threads, lib, launch_wait_ms)
+    conc = max_phenos or max(1, len(specs))
+    # engine columns for the conc largest working sets that can run together
+    widest = sorted(specs, key=lambda sp: -sp.nrun)[:conc]
+    max_columns = max(max_columns or 0, columns_for(widest))
+    drv = NativeFits(ctx, max_columns, conc, pipelined, threads, lib, launch_wait_ms)
     try:
         jobs = {}
         for s in specs:
@@ -141,6 +157,9 @@ def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True, thr
             for fid in drv.poll():
                 j = jobs[fid]
                 j.t_done = time.perf_counter()
+                # service time: from the fit's admission to a phenotype slot to its end
+                t_add, t_adm, t_fin = drv.fit_times(fid)
+                j.service_s = t_fin - t_adm
                 res, j.column_iterations = drv.result(fid)
                 if isinstance(res, Exception):
                     j.error = res

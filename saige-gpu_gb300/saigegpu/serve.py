@@ -672,9 +672,11 @@ def columns_for(specs):
 
 
 def fit_batch(ctx, specs, max_columns=None, max_phenos=None, pipelined=True, workers=None):
-    """Fit all ``specs`` together; returns their result dicts (or exceptions) in order."""
-    max_columns = max(max_columns or 0, columns_for(specs))
-    r = Runner(ctx, max_columns, max_phenos or max(1, len(specs)), pipelined=pipelined, workers=workers)
+    """Fit all ``specs`` together; returns their result dicts (or exceptions) in order.  With
+    max_phenos below len(specs), at most that many run at once."""
+    conc = max_phenos or max(1, len(specs))
+    max_columns = max(max_columns or 0, columns_for(sorted(specs, key=lambda sp: -sp.nrun)[:conc]))
+    r = Runner(ctx, max_columns, conc, pipelined=pipelined, workers=workers)
     try:
         ids = [r.submit(s) for s in specs]
         r.run()

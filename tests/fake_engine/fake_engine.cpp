@@ -363,6 +363,19 @@ int sg_engine_wait(sg_ctx* c) {
   return SG_OK;
 }
 
+// the fake keeps no subset state: preparing and waiting only check their arguments
+int sg_engine_prepare_subset(sg_ctx* c, int64_t slot, const uint8_t* mask) {
+  (void)mask;
+  if (!c) return SG_ERR_INVALID;
+  if (slot < 0 || slot >= (int64_t)c->slots.size()) return fail(c, SG_ERR_INVALID, "slot out of range");
+  return SG_OK;
+}
+
+int sg_engine_subset_wait(sg_ctx* c, int64_t slot) {
+  (void)slot;
+  return c ? SG_OK : SG_ERR_INVALID;
+}
+
 int sg_engine_finish(sg_ctx* c, int64_t* n_finished) {
   if (!c) return SG_ERR_INVALID;
   int64_t fin = 0;

@@ -92,7 +92,7 @@ def test_subset_exact_products_match_oracle(exact_cohort):
                 assert err < 6e-5, (pair, trait, err)
     finally:
         ctx.set_tc_option(TC_SUBSET_PAIR, 2)
-        ctx.set_tc_option(TC_SUBSET_SLICE, 128)
+        ctx.set_tc_option(TC_SUBSET_SLICE, 256)
         ctx.set_matvec_mode(MV_FP32_SIMT)
 
 
@@ -119,7 +119,7 @@ def test_subset_exact_variants_bit_identical(exact_cohort):
     finally:
         ctx.set_subset_plan([])
         ctx.set_tc_option(TC_SUBSET_PAIR, 2)
-        ctx.set_tc_option(TC_SUBSET_SLICE, 128)
+        ctx.set_tc_option(TC_SUBSET_SLICE, 256)
         ctx.set_matvec_mode(MV_FP32_SIMT)
 
 
@@ -176,3 +176,34 @@ def test_subset_exact_full_cohort_matches_cohort_grm(exact_cohort):
         ctx.set_matvec_mode(MV_FP32_SIMT)
     ref = grm.K @ V
     assert np.abs(Y - ref).max() / np.abs(ref).max() < 6e-5
+
+
+def test_subset_exact_forget_rebuilds_identically(exact_cohort):
+    """Forgetting the kept subset states makes the next set_pheno rebuild them (QC, tables, flip map
+    and diagonal on the device); the products after the rebuild are bit-identical."""
+    ctx, bed, _, cases = exact_cohort
+    rng = np.random.default_rng(9)
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    try:
+        ctx.engine_reserve(128, len(cases))
+        Vs = []
+        for _, mask, _ in cases:
+            V = rng.standard_normal((N, 5))
+            V[~mask] = 0.0
+            Vs.append(V)
+
+        def products():
+            ids = []
+            for slot, (_, mask, _) in enumerate(cases):
+                ctx.engine_set_pheno(slot, np.ones(N), np.array([1.0, 0.5]), mask)
+                ids.append(ctx.engine_submit(slot, 1, Vs[slot]))
+            got = _run_products(ctx, np.concatenate(ids))
+            return [np.column_stack([got[int(i)] for i in idk]) for idk in ids]
+
+        first = products()
+        ctx.engine_forget_subsets()
+        again = products()
+        for a, b in zip(first, again):
+            np.testing.assert_array_equal(a, b)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
