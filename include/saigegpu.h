@@ -344,6 +344,14 @@ int sg_engine_cancel(sg_ctx *ctx, int64_t id);
 int sg_engine_probe_dots(sg_ctx *ctx, int64_t slot, const int64_t *ids_pcg, const int64_t *ids_prod,
                          int64_t k, uint64_t seed, int64_t run0, const double *SX, int64_t p,
                          double *out, int32_t *iters);
+/* The same in three calls, for a driver whose threads serialise their engine calls: _begin checks
+ * the requests and launches the reduction without waiting (one per slot at a time); _wait blocks
+ * until it has run and, like sg_engine_wait, need not be serialised with other threads' calls;
+ * _end writes out and iters and releases the 2k results.  No reference counterpart. */
+int sg_engine_probe_dots_begin(sg_ctx *ctx, int64_t slot, const int64_t *ids_pcg, const int64_t *ids_prod,
+                               int64_t k, uint64_t seed, int64_t run0, const double *SX, int64_t p);
+int sg_engine_probe_dots_wait(sg_ctx *ctx, int64_t slot);
+int sg_engine_probe_dots_end(sg_ctx *ctx, int64_t slot, double *out, int32_t *iters);
 /* K u of a slot's probes is kept on the device once computed (the probes and the slot's sample mask
  * are fixed during a fit): an ids_prod entry of -1 in sg_engine_probe_dots reads the cached K u of
  * (seed, run0 + j).  Clear a slot's cache when a new phenotype (mask) takes it (slot -1: all). */

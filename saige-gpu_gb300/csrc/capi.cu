@@ -84,7 +84,6 @@ struct Engine {
   std::vector<void*> slab_dblocks;  // device blocks
   cudaEvent_t ev_up = nullptr;      // the last right-hand-side upload (upload stream)
   bool up_wait = false;             // the next admission waits for it
-  double* h_stage = nullptr;      // pinned: a slot's W and sample mask on their way up
   double* d_wstage = nullptr;     // their device copy (np doubles + np bytes)
   int32_t* d_gcols = nullptr;
   bool inflight = false;          // a launched step has not been finished yet
@@ -101,6 +100,16 @@ struct Engine {
   double* pcache = nullptr;
   std::vector<std::vector<std::pair<uint64_t, int64_t>>> pcache_key;  // per slot: (seed, run) per entry
   size_t dots_cap_sx = 0, dots_cap_part = 0, dots_cap_cols = 0;
+  // a probe reduction launched and not yet ended, per slot (sg_engine_probe_dots_begin / _end)
+  struct DotsPending {
+    bool pending = false;
+    std::vector<int64_t> ids_pcg, ids_prod;
+    int64_t k = 0, nv = 0, nblk = 0;
+    double* h_part = nullptr;  // pinned block partials, k x nblk x nv
+    size_t cap = 0;
+    cudaEvent_t ev = nullptr;
+  };
+  std::vector<DotsPending> dots;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t ev_prev[3] = {nullptr, nullptr, nullptr};  // the previous step's (swapped per launch)
   bool have_prev = false;  // ev_prev holds a finished step whose end the idle time counts from
@@ -109,10 +118,14 @@ struct Engine {
   double t_finish_host_ms = 0.0;  // host time a finish spends after the step has drained
   cudaEvent_t ev_adm = nullptr;
   bool adm_recorded = false;
-  // set_pheno uploads without waiting: the next set_pheno reuses the staging buffer after ev_pheno,
-  // and the next launch's work on the main stream waits for it
-  cudaEvent_t ev_pheno = nullptr;
-  bool pheno_stage_busy = false, pheno_main_wait = false;
+  // set_pheno uploads without waiting, through the slot's own pinned staging; ev_slot marks the end
+  // of the slot's upload (and of any set-up before it on the side stream).  Columns of a slot whose
+  // upload has not finished wait for it at admission, or stay queued for a later step when other
+  // columns run meanwhile
+  std::vector<double*> h_wslot;      // per slot: W (np doubles) then the mask (np bytes), pinned
+  std::vector<cudaEvent_t> ev_slot;
+  std::vector<uint8_t> slot_rec;     // ev_slot recorded at least once
+  std::vector<uint8_t> slot_wait;    // the next admission of the slot's columns checks ev_slot
   double t_step_ms = 0, t_gemm_ms = 0, gemm_launches = 0, gemm_flops = 0, gemm_cols = 0, useful_cols = 0;
   // per-step records since the last timing reset (the first kStepTrace steps):
   // [columns the GRM.V computed, occupied columns, GRM.V ms, step ms, idle ms before the step]
@@ -376,15 +389,15 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
   return SG_OK;
 }
 
+static void engine_free(sg_ctx* c);
+
 extern "C" void sg_ctx_destroy(sg_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   cudaStreamSynchronize(c->side);
   cudaStreamSynchronize(c->up);
-  if (c->eng.h_pin) cudaFreeHost(c->eng.h_pin);
-  if (c->eng.h_gcols) cudaFreeHost(c->eng.h_gcols);
-  if (c->eng.h_stage) cudaFreeHost(c->eng.h_stage);
+  engine_free(c);  // the engine's device buffers, pinned staging and events
   for (auto& kv : c->allocs) cudaFree(kv.first);
   c->allocs.clear();
   cudaStreamDestroy(c->up);
@@ -1071,8 +1084,15 @@ static cudaError_t d2h(sg_ctx* c, void* dst, const void* src, size_t bytes, cuda
 
 static void engine_free(sg_ctx* c) {
   Engine& e = c->eng;
-  cudaStreamSynchronize(c->side);  // a weight upload may still read the staging buffer
-  e.pheno_stage_busy = e.pheno_main_wait = false;
+  cudaStreamSynchronize(c->side);  // a weight upload may still read a staging buffer
+  for (double* h : e.h_wslot)
+    if (h) cudaFreeHost(h);
+  for (cudaEvent_t ev : e.ev_slot)
+    if (ev) cudaEventDestroy(ev);
+  e.h_wslot.clear();
+  e.ev_slot.clear();
+  e.slot_rec.clear();
+  e.slot_wait.clear();
   dev_free_t(c, e.X); dev_free_t(c, e.R); dev_free_t(c, e.Z); dev_free_t(c, e.P);
   dev_free_t(c, e.B); dev_free_t(c, e.part); dev_free_t(c, e.winv); dev_free_t(c, e.minv);
   dev_free_t(c, e.Yd); dev_free_t(c, e.Pf); dev_free_t(c, e.Yf); dev_free_t(c, e.d_st);
@@ -1102,6 +1122,12 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.sdiag_part);
 
   e.dots_cap_sx = e.dots_cap_part = e.dots_cap_cols = 0;
+  for (auto& dp : e.dots) {
+    if (dp.ev) cudaEventSynchronize(dp.ev);
+    if (dp.h_part) cudaFreeHost(dp.h_part);
+    if (dp.ev) cudaEventDestroy(dp.ev);
+  }
+  e.dots.clear();
   if (e.inflight) cudaStreamSynchronize(c->stream);
   e.inflight = false;
   e.pending_release.clear();
@@ -1109,8 +1135,6 @@ static void engine_free(sg_ctx* c) {
   e.h_pin = nullptr;
   if (e.h_gcols) cudaFreeHost(e.h_gcols);
   e.h_gcols = nullptr;
-  if (e.h_stage) cudaFreeHost(e.h_stage);
-  e.h_stage = nullptr;
   dev_free_t(c, e.d_wstage);
   for (void** hp : {reinterpret_cast<void**>(&e.h_sst), reinterpret_cast<void**>(&e.h_scol),
                     reinterpret_cast<void**>(&e.h_acols), reinterpret_cast<void**>(&e.h_ptab)}) {
@@ -1223,12 +1247,10 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   for (auto& ev : e.ev_prev)
     if (!ev) SG_CUDA(c, cudaEventCreate(&ev));
   if (!e.ev_adm) SG_CUDA(c, cudaEventCreate(&e.ev_adm));
-  if (!e.ev_pheno) SG_CUDA(c, cudaEventCreateWithFlags(&e.ev_pheno, cudaEventDisableTiming));
   if (!e.ev_up) SG_CUDA(c, cudaEventCreateWithFlags(&e.ev_up, cudaEventDisableTiming));
   e.have_prev = false;
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_pin), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_gcols), max_columns * sizeof(int32_t), cudaHostAllocDefault));
-  SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_stage), 2 * np * sizeof(double), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_sst), max_columns * sizeof(ColState), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_scol), max_columns * sizeof(int32_t), cudaHostAllocDefault));
   SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_acols), e.stage_cols * sizeof(int32_t), cudaHostAllocDefault));
@@ -1426,15 +1448,22 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
   for (auto& kv : e.reqs)
     if (kv.second.state == 1 && kv.second.slot == slot)
       return set_err(c, SG_ERR_STATE, "phenotype slot %lld has columns in flight", (long long)slot);
-  // W (and the sample mask) go up through pinned staging; 1/W and the Jacobi preconditioner
-  // 1/diag(Sigma) are formed on the device from the resident FP64 diagonal
-  if (e.pheno_stage_busy) {  // the previous upload has left the staging buffer (long since, as a rule)
-    SG_CUDA(c, cudaEventSynchronize(e.ev_pheno));
-    e.pheno_stage_busy = false;
+  // W (and the sample mask) go up through the slot's pinned staging; 1/W and the Jacobi
+  // preconditioner 1/diag(Sigma) are formed on the device from the resident FP64 diagonal
+  if ((int64_t)e.ev_slot.size() < e.cap_ph) {
+    e.h_wslot.resize(e.cap_ph, nullptr);
+    e.ev_slot.resize(e.cap_ph, nullptr);
+    e.slot_rec.resize(e.cap_ph, 0);
+    e.slot_wait.resize(e.cap_ph, 0);
   }
+  if (!e.ev_slot[slot]) SG_CUDA(c, cudaEventCreateWithFlags(&e.ev_slot[slot], cudaEventDisableTiming));
+  if (!e.h_wslot[slot])
+    SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_wslot[slot]), e.np * (sizeof(double) + 1),
+                             cudaHostAllocDefault));
+  if (e.slot_rec[slot]) SG_CUDA(c, cudaEventSynchronize(e.ev_slot[slot]));  // its last upload (long done)
   {
-    double* hw = e.h_stage;
-    uint8_t* hm = reinterpret_cast<uint8_t*>(e.h_stage + e.np);
+    double* hw = e.h_wslot[slot];
+    uint8_t* hm = reinterpret_cast<uint8_t*>(e.h_wslot[slot] + e.np);
     std::memcpy(hw, w, c->nn * sizeof(double));
     if (mask) std::memcpy(hm, mask, c->nn);
     const bool loco = c->loco && !c->is_diag_one;
@@ -1457,8 +1486,8 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
   e.h_ph[slot] = PhenoState{tau[0], tau[1]};
   SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), c->side));
   e.ph_set[slot] = 1;
-  SG_CUDA(c, cudaEventRecord(e.ev_pheno, c->side));
-  e.pheno_stage_busy = e.pheno_main_wait = true;
+  SG_CUDA(c, cudaEventRecord(e.ev_slot[slot], c->side));
+  e.slot_rec[slot] = e.slot_wait[slot] = 1;
   return SG_OK;
 }
 
@@ -1645,10 +1674,7 @@ static int engine_admit(sg_ctx* c) {
     SG_CUDA(c, cudaStreamWaitEvent(c->stream, e.ev_up, 0));
     e.up_wait = false;
   }
-  if (e.pheno_main_wait) {  // slot weights uploaded since the last launch: the step reads them
-    SG_CUDA(c, cudaStreamWaitEvent(c->stream, e.ev_pheno, 0));
-    e.pheno_main_wait = false;
-  }
+
   // the previous admission's copies have run (the stream drained at the last finish / sync)
   for (int64_t id : e.slab_pending) {
     auto it = e.reqs.find(id);
@@ -1684,6 +1710,20 @@ static int engine_admit(sg_ctx* c) {
       auto it = e.reqs.find(id);
       if (it == e.reqs.end()) continue;  // cancelled
       Req& r = it->second;
+      if (r.slot < (int64_t)e.slot_wait.size() && e.slot_wait[r.slot]) {
+        // the slot's weights (and subset set-up) were uploaded on the side stream since its last
+        // admission: admit once they are there; while other columns run, leave it for a later step
+        // rather than hold the step back
+        if (cudaEventQuery(e.ev_slot[r.slot]) == cudaSuccess) {
+          e.slot_wait[r.slot] = 0;
+        } else if (e.n_active > 0 || !cols.empty()) {
+          later.push_back(id);
+          continue;
+        } else {
+          SG_CUDA(c, cudaStreamWaitEvent(c->stream, e.ev_slot[r.slot], 0));
+          e.slot_wait[r.slot] = 0;
+        }
+      }
       const int64_t sel = (int64_t)cols.size();
       if (r.src >= 0) {
         auto is = e.reqs.find(r.src);
@@ -2237,14 +2277,20 @@ extern "C" int sg_engine_probe_cached(sg_ctx* c, int64_t slot, uint64_t seed, in
   return pcache_find(c->eng, slot, seed, run) >= 0 ? 1 : 0;
 }
 
-extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_pcg,
-                                    const int64_t* ids_prod, int64_t k, uint64_t seed, int64_t run0,
-                                    const double* SX, int64_t p, double* out, int32_t* iters) {
+// Probe reductions in two halves: _begin checks the requests, caches K u, uploads SX and the
+// column pointers and launches the reduction on the side stream with its block partials copied to
+// pinned memory (nothing waits); _wait blocks until they have arrived; _end adds them up in a fixed
+// order and releases the 2k results.  One reduction per slot at a time.
+extern "C" int sg_engine_probe_dots_begin(sg_ctx* c, int64_t slot, const int64_t* ids_pcg, const int64_t* ids_prod,
+                                          int64_t k, uint64_t seed, int64_t run0, const double* SX, int64_t p) {
   NEED_OPERATOR(c);
   Engine& e = c->eng;
-  if (k <= 0 || !ids_pcg || !ids_prod || !out || p < 0 || p > kProbeDotsMaxP || (p > 0 && !SX))
+  if (k <= 0 || !ids_pcg || !ids_prod || p < 0 || p > kProbeDotsMaxP || (p > 0 && !SX))
     return set_err(c, SG_ERR_INVALID, "probe_dots: bad arguments (p <= %d)", kProbeDotsMaxP);
   if (slot < 0 || slot >= e.cap_ph) return set_err(c, SG_ERR_INVALID, "bad slot");
+  if ((int64_t)e.dots.size() < e.cap_ph) e.dots.resize(e.cap_ph);
+  Engine::DotsPending& dp = e.dots[slot];
+  if (dp.pending) return set_err(c, SG_ERR_STATE, "slot %lld has a probe reduction in flight", (long long)slot);
   if ((int64_t)e.pcache_key.size() < e.cap_ph) e.pcache_key.resize(e.cap_ph);
   if (!e.pcache) SG_TRY(dev_alloc_t(c, &e.pcache, (size_t)(e.cap_ph * kProbeCache * e.np)));
   // Su from held engine columns; Au from a held column (then cached) or from the slot's cache
@@ -2295,6 +2341,15 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
     e.dots_cap_part = need_part;
     e.dots_cap_cols = (size_t)(2 * k);
   }
+  if (dp.cap < need_part) {
+    if (dp.h_part) cudaFreeHost(dp.h_part);
+    dp.h_part = nullptr;
+    dp.cap = 0;
+    SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&dp.h_part), need_part * 8, cudaHostAllocDefault));
+    dp.cap = need_part;
+  }
+  if (!dp.ev) SG_CUDA(c, cudaEventCreateWithFlags(&dp.ev, cudaEventDisableTiming));
+  // the scratch above is shared by the slots; their reductions queue on the side stream in order
   if (p > 0) {
     SG_CUDA(c, cudaMemsetAsync(e.d_sx, 0, need_sx * 8, c->side));
     SG_CUDA(c, cudaMemcpy2DAsync(e.d_sx, e.np * 8, SX, c->nn * 8, c->nn * 8, p, cudaMemcpyHostToDevice, c->side));
@@ -2306,25 +2361,64 @@ extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_
   launch_probe_dots(e.np, c->nn, reinterpret_cast<const double* const*>(e.d_dcols), k,
                     e.minv + slot * e.np, seed, run0, e.d_sx, p, e.d_dpart, nblk, c->side);
   SG_LAUNCHED(c, 1);
-  std::vector<double> part(need_part);
-  SG_CUDA(c, d2h(c, part.data(), e.d_dpart, need_part * 8, c->side));
-  SG_TRY(sync_side(c));
+  SG_CUDA(c, d2h(c, dp.h_part, e.d_dpart, need_part * 8, c->side));
+  SG_CUDA(c, cudaEventRecord(dp.ev, c->side));
+  dp.ids_pcg.assign(ids_pcg, ids_pcg + k);
+  dp.ids_prod.assign(ids_prod, ids_prod + k);
+  dp.k = k;
+  dp.nv = nv;
+  dp.nblk = nblk;
+  dp.pending = true;
+  return SG_OK;
+}
+
+// Reads only the slot's event (set by the _begin this thread made).
+extern "C" int sg_engine_probe_dots_wait(sg_ctx* c, int64_t slot) {
+  if (!c) return SG_ERR_INVALID;
+  Engine& e = c->eng;
+  if (slot < 0 || slot >= (int64_t)e.dots.size()) return SG_OK;
+  const Engine::DotsPending& dp = e.dots[slot];
+  if (dp.pending && dp.ev) (void)cudaEventSynchronize(dp.ev);
+  return SG_OK;
+}
+
+extern "C" int sg_engine_probe_dots_end(sg_ctx* c, int64_t slot, double* out, int32_t* iters) {
+  NEED_OPERATOR(c);
+  Engine& e = c->eng;
+  if (!out) return set_err(c, SG_ERR_INVALID, "probe_dots: null output");
+  if (slot < 0 || slot >= (int64_t)e.dots.size() || !e.dots[slot].pending)
+    return set_err(c, SG_ERR_STATE, "slot %lld has no probe reduction in flight", (long long)slot);
+  Engine::DotsPending& dp = e.dots[slot];
+  SG_CUDA(c, cudaEventSynchronize(dp.ev));
+  dp.pending = false;
+  const int64_t k = dp.k, nv = dp.nv, nblk = dp.nblk;
   for (int64_t j = 0; j < k; ++j)
     for (int64_t v = 0; v < nv; ++v) {
       double acc = 0.0;
-      for (int64_t b = 0; b < nblk; ++b) acc += part[(j * nblk + b) * nv + v];
+      for (int64_t b = 0; b < nblk; ++b) acc += dp.h_part[(j * nblk + b) * nv + v];
       out[j * nv + v] = acc;
     }
   for (int64_t j = 0; j < 2 * k; ++j) {
-    const int64_t id = j < k ? ids_pcg[j] : ids_prod[j - k];
+    const int64_t id = j < k ? dp.ids_pcg[j] : dp.ids_prod[j - k];
     if (id < 0) continue;
     auto it = e.reqs.find(id);
+    if (it == e.reqs.end()) continue;
     if (iters && j < k) iters[j] = it->second.iters;
     SG_TRY(detach_dependents(c, it->second));
     SG_TRY(release_col(c, it->second.col));
     e.reqs.erase(it);
   }
-  return sync_side(c);
+  // the reduction (and the K u cache copies before it) read the released columns before ev, so a
+  // later admission may overwrite them; nothing else of the side stream is waited for here
+  return SG_OK;
+}
+
+extern "C" int sg_engine_probe_dots(sg_ctx* c, int64_t slot, const int64_t* ids_pcg,
+                                    const int64_t* ids_prod, int64_t k, uint64_t seed, int64_t run0,
+                                    const double* SX, int64_t p, double* out, int32_t* iters) {
+  if (!out) return set_err(c, SG_ERR_INVALID, "probe_dots: null output");
+  SG_TRY(sg_engine_probe_dots_begin(c, slot, ids_pcg, ids_prod, k, seed, run0, SX, p));
+  return sg_engine_probe_dots_end(c, slot, out, iters);
 }
 
 extern "C" int sg_engine_hold_results(sg_ctx* c, int hold) {

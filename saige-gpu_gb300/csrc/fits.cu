@@ -564,9 +564,21 @@ bool ai_after_probes(sg_fits* F, Fit& f) {
   const int64_t nv = 2 + 2 * p, k = (int64_t)f.pid.size();
   std::vector<double> D(k * nv);
   std::vector<int32_t> its(k, 0);
+  // launch the reduction, wait for it without the lock (the stepping thread may turn a step
+  // around meanwhile), then collect it
+  if (!eng(F, f, &F->t_dots, [&] {
+        return sg_engine_probe_dots_begin(F->ctx, f.slot, f.pid.data(), f.aid.data(), k, f.seed, f.run0,
+                                          f.SX.data(), p);
+      }))
+    return false;
+  const double tw = now_s();
+  sg_engine_probe_dots_wait(F->ctx, f.slot);
+  {
+    std::lock_guard<std::mutex> g(F->mu);
+    F->t_dots += now_s() - tw;
+  }
   const bool ok = eng(F, f, &F->t_dots, [&] {
-    const int rc = sg_engine_probe_dots(F->ctx, f.slot, f.pid.data(), f.aid.data(), k, f.seed, f.run0, f.SX.data(),
-                                        p, D.data(), its.data());
+    const int rc = sg_engine_probe_dots_end(F->ctx, f.slot, D.data(), its.data());
     if (rc != SG_OK) return rc;
     for (int64_t j = 0; j < k; ++j) {
       F->done_reqs.erase(f.pid[j]);

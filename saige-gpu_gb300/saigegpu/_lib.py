@@ -112,6 +112,9 @@ SIGNATURES = {
     "sg_engine_probe_cached": [c_ctx, c_i64, c_u64, c_i64],
     "sg_engine_probe_dots": [c_ctx, c_i64, P_i64, P_i64, c_i64, c_u64, c_i64, P_f64, c_i64, P_f64,
                              P_i32],
+    "sg_engine_probe_dots_begin": [c_ctx, c_i64, P_i64, P_i64, c_i64, c_u64, c_i64, P_f64, c_i64],
+    "sg_engine_probe_dots_wait": [c_ctx, c_i64],
+    "sg_engine_probe_dots_end": [c_ctx, c_i64, P_f64, P_i32],
     "sg_engine_timing": [c_ctx, P_f64],
     "sg_engine_io_bytes": [c_ctx, P_u64, P_u64],
     "sg_engine_idle_ms": [c_ctx, P_f64],

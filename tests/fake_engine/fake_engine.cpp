@@ -363,6 +363,48 @@ int sg_engine_wait(sg_ctx* c) {
   return SG_OK;
 }
 
+// the split probe reduction: _begin keeps the arguments, _end runs the whole reduction
+struct FakeDots {
+  std::vector<int64_t> pcg, prod;
+  std::vector<double> sx;
+  int64_t k = 0, p = 0, run0 = 0;
+  uint64_t seed = 0;
+  bool pending = false;
+};
+static std::map<std::pair<const sg_ctx*, int64_t>, FakeDots> g_fake_dots;
+
+int sg_engine_probe_dots_begin(sg_ctx* c, int64_t slot, const int64_t* ids_pcg, const int64_t* ids_prod, int64_t k,
+                               uint64_t seed, int64_t run0, const double* SX, int64_t p) {
+  if (!c || k <= 0 || !ids_pcg || !ids_prod || p < 0 || p > 16 || (p > 0 && !SX))
+    return fail(c, SG_ERR_INVALID, "probe_dots: bad arguments");
+  FakeDots& d = g_fake_dots[{c, slot}];
+  if (d.pending) return fail(c, SG_ERR_STATE, "probe reduction in flight");
+  d.pcg.assign(ids_pcg, ids_pcg + k);
+  d.prod.assign(ids_prod, ids_prod + k);
+  d.sx.assign(SX ? SX : nullptr, SX ? SX + p * c->n : nullptr);
+  d.k = k;
+  d.p = p;
+  d.seed = seed;
+  d.run0 = run0;
+  d.pending = true;
+  return SG_OK;
+}
+
+int sg_engine_probe_dots_wait(sg_ctx* c, int64_t slot) {
+  (void)slot;
+  return c ? SG_OK : SG_ERR_INVALID;
+}
+
+int sg_engine_probe_dots_end(sg_ctx* c, int64_t slot, double* out, int32_t* iters) {
+  if (!c) return SG_ERR_INVALID;
+  auto it = g_fake_dots.find({c, slot});
+  if (it == g_fake_dots.end() || !it->second.pending) return fail(c, SG_ERR_STATE, "no probe reduction in flight");
+  FakeDots d = it->second;
+  it->second.pending = false;
+  return sg_engine_probe_dots(c, slot, d.pcg.data(), d.prod.data(), d.k, d.seed, d.run0,
+                              d.p ? d.sx.data() : nullptr, d.p, out, iters);
+}
+
 // the fake keeps no subset state: preparing and waiting only check their arguments
 int sg_engine_prepare_subset(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   (void)mask;
