@@ -323,6 +323,14 @@ def step_width_summary(trace):
         # device gap before each step (admission included): typical, tail and the largest
         out["idle_ms_p50_p90_p99_max"] = [round(float(np.percentile(idle, q)), 3) for q in (50, 90, 99)] + [
             round(float(idle.max()), 3)]
+    if trace.shape[1] >= 8 and len(trace) > 1:
+        # the five largest gaps with their host side: ms from the previous finish to the launch,
+        # ms inside the launch, slot uploads the admission waited for
+        top = np.argsort(-trace[:, 4])[:5]
+        out["largest_gaps"] = [[round(float(trace[i, 4]), 2), round(float(trace[i, 5]), 2),
+                                round(float(trace[i, 6]), 2), int(trace[i, 7])] for i in top]
+        gaps = trace[trace[:, 5] >= 0, 5]
+        out["host_gap_ms_p50_p99"] = [round(float(np.percentile(gaps, q)), 3) for q in (50, 99)] if len(gaps) else None
     return out
 
 

@@ -373,10 +373,12 @@ int sg_engine_timing(sg_ctx *ctx, double *t6);
  * step; ms3[2]: host time finishes spent after their step had drained.  No reference counterpart. */
 int sg_engine_idle_ms(sg_ctx *ctx, double *ms3);
 int sg_engine_reset_timing(sg_ctx *ctx);
-/* Per-step records since the last sg_engine_reset_timing (at most 65536 steps), five doubles each:
+/* Per-step records since the last sg_engine_reset_timing (at most 65536 steps), eight doubles each:
  * columns the GRM.V computed (active columns padded to its tile width), occupied columns, GRM.V
- * device ms, step device ms, device idle ms before the step (-1 for the first).  Up to max_steps
- * records into out[5 * max_steps]; *n_out gets the count.  No reference counterpart. */
+ * device ms, step device ms, device idle ms before the step (-1 for the first), host ms from the
+ * previous step's finish to this step's launch (-1 for the first), host ms inside the launch, and
+ * the slot uploads its admission waited for.  Up to max_steps records into out[8 * max_steps];
+ * *n_out gets the count.  No reference counterpart. */
 int sg_engine_step_trace(sg_ctx *ctx, double *out, int64_t max_steps, int64_t *n_out);
 /* Bytes copied host->device and device->host by the engine calls (right-hand sides, weights,
  * probe tables, column states, fetched results, probe reductions) since the last

@@ -118,6 +118,12 @@ struct Engine {
   double t_finish_host_ms = 0.0;  // host time a finish spends after the step has drained
   cudaEvent_t ev_adm = nullptr;
   bool adm_recorded = false;
+  // host side of the step in flight: ms from the previous finish's return to its launch, ms inside
+  // the launch, slot uploads its admission waited for
+  std::chrono::steady_clock::time_point t_fin_end;
+  bool have_fin_end = false;
+  double inflight_gap_ms = -1.0, inflight_launch_ms = 0.0;
+  int adm_waits = 0, inflight_waits = 0;
   // set_pheno uploads without waiting, through the slot's own pinned staging; ev_slot marks the end
   // of the slot's upload (and of any set-up before it on the side stream).  Columns of a slot whose
   // upload has not finished wait for it at admission, or stay queued for a later step when other
@@ -170,7 +176,7 @@ struct Engine {
 
 };
 constexpr int64_t kStepTrace = 65536;
-constexpr int kTraceFields = 5;
+constexpr int kTraceFields = 8;
 
 }  // namespace
 
@@ -1366,9 +1372,12 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
   if (!e.sdiag_part) SG_TRY(dev_alloc_t(c, &e.sdiag_part, (size_t)subset_diag_scratch(m, np)));
   const int W = (int)((nflip + 31) / 32);
   if ((int64_t)W * np > ss.bits_cap) {
+    // with room to spare (cudaFree waits for the whole device, steps included): at least 64 words
+    // (2,048 fill changes) a sample, then half again what this subset needs
+    const int64_t words = std::max<int64_t>(64, ((int64_t)W * 3 / 2 + 31) / 32 * 32);
     dev_free_t(c, ss.bits);
-    SG_TRY(dev_alloc_t(c, &ss.bits, (size_t)(W * np)));
-    ss.bits_cap = (int64_t)W * np;
+    SG_TRY(dev_alloc_t(c, &ss.bits, (size_t)(words * np)));
+    ss.bits_cap = words * np;
   }
   launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, (int)nflip, W, dmask, nn, np, ss.bits, c->side);
   launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, e.sdiag_part, ss.diag, c->side);
@@ -1722,6 +1731,7 @@ static int engine_admit(sg_ctx* c) {
         } else {
           SG_CUDA(c, cudaStreamWaitEvent(c->stream, e.ev_slot[r.slot], 0));
           e.slot_wait[r.slot] = 0;
+          ++e.adm_waits;
         }
       }
       const int64_t sel = (int64_t)cols.size();
@@ -2009,7 +2019,8 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
     e.have_prev = true;
     if ((int64_t)e.trace.size() < kStepTrace * kTraceFields) {
       const double rec[kTraceFields] = {(double)(c->mv_mode == SG_MV_FP64_PLAIN ? occupied : ncols),
-                                        (double)occupied, ms_gemm, ms_step, had_prev ? (double)ms_idle : -1.0};
+                                        (double)occupied, ms_gemm, ms_step, had_prev ? (double)ms_idle : -1.0,
+                                        e.inflight_gap_ms, e.inflight_launch_ms, (double)e.inflight_waits};
       e.trace.insert(e.trace.end(), rec, rec + kTraceFields);
     }
     e.t_gemm_ms += ms_gemm;
@@ -2103,7 +2114,10 @@ static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
   }
   while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
   SG_TRY(flush_states(c, false));
-  return sync(c);
+  SG_TRY(sync(c));
+  e.t_fin_end = std::chrono::steady_clock::now();
+  e.have_fin_end = true;
+  return SG_OK;
 }
 
 extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) {
@@ -2147,6 +2161,10 @@ extern "C" int sg_engine_launch(sg_ctx* c, int64_t* n_finished, int* launched) {
   if (e.inflight) return set_err(c, SG_ERR_STATE, "a step is in flight: finish it first");
   int64_t fin = 0;
   if (launched) *launched = 0;
+  const auto tl0 = std::chrono::steady_clock::now();
+  const double gap_ms =
+      e.have_fin_end ? std::chrono::duration<double, std::milli>(tl0 - e.t_fin_end).count() : -1.0;
+  e.adm_waits = 0;
   SG_CUDA(c, cudaEventRecord(e.ev_adm, c->stream));
   e.adm_recorded = true;
   SG_TRY(engine_admit(c));
@@ -2161,6 +2179,9 @@ extern "C" int sg_engine_launch(sg_ctx* c, int64_t* n_finished, int* launched) {
     return SG_OK;
   }
   SG_TRY(step_launch(c));
+  e.inflight_gap_ms = gap_ms;
+  e.inflight_launch_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tl0).count();
+  e.inflight_waits = e.adm_waits;
   if (launched) *launched = 1;
   return SG_OK;
 }
@@ -2464,6 +2485,7 @@ extern "C" int sg_engine_reset_timing(sg_ctx* c) {
   e.t_admit_ms = 0.0;
   e.t_finish_host_ms = 0.0;
   e.have_prev = false;
+  e.have_fin_end = false;
   e.t_step_ms = e.t_gemm_ms = e.gemm_launches = e.gemm_flops = e.gemm_cols = e.useful_cols = 0;
   e.io_h2d = e.io_d2h = 0;
   e.trace.clear();

@@ -266,6 +266,10 @@ void launch_subset_diag(const uint8_t* codes, int64_t pitch, const float* lut4, 
 }
 
 // ----------------------------------------------------------------------------------- per step
+// FP64 arithmetic is a small fraction of this GPU's FP32 rate, so the per-element work below runs
+// in FP32: each thread sums its kChunk / kThreads elements in FP32 and the block adds the threads'
+// partials in FP64, in a fixed order.
+//
 // Column sums over the subset (rows outside S are zero in P): block partials, kChunk rows each.
 __global__ void subset_colsum_kernel(const float* __restrict__ Pf, int64_t np, const int32_t* __restrict__ cols,
                                      double* __restrict__ part, int nblk) {
@@ -273,13 +277,13 @@ __global__ void subset_colsum_kernel(const float* __restrict__ Pf, int64_t np, c
   const int64_t j = blockIdx.y;
   const int32_t col = cols[j];
   const int64_t i0 = (int64_t)blockIdx.x * kChunk;
-  double v = 0.0;
+  float v = 0.0f;
   if (col >= 0) {
     const float* p = Pf + (int64_t)col * np;
-    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) v += (double)p[i];
+    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) v += p[i];
   }
-  v = block_sum(v, sh);
-  if (threadIdx.x == 0) part[j * nblk + blockIdx.x] = v;
+  const double vd = block_sum((double)v, sh);
+  if (threadIdx.x == 0) part[j * nblk + blockIdx.x] = vd;
 }
 
 // v_c = P - mean_S(P) on the subset (0 elsewhere and for padding columns), as BF16 high + low
@@ -368,7 +372,7 @@ __global__ void subset_scale_split_kernel(const float* __restrict__ T, int64_t m
   const int32_t col = cols[j];
   const int64_t m0 = (int64_t)blockIdx.x * kChunk;
   const SubsetSlot* sl = col >= 0 ? &slots[st[col].pheno] : nullptr;
-  double c = 0.0;
+  float cf = 0.0f;
   for (int64_t mk = m0 + threadIdx.x; mk < m0 + kChunk && mk < mg; mk += kThreads) {
     float t = 0.0f;
     if (sl) t = sl->dprime[mk] * T[j * mg + mk];
@@ -376,9 +380,10 @@ __global__ void subset_scale_split_kernel(const float* __restrict__ T, int64_t m
     const __nv_bfloat16 l = __float2bfloat16_rn(t - __bfloat162float(h));
     Th[j * mg + mk] = h;
     Tl[j * mg + mk] = l;
-    if (sl) c += (double)sl->p2[mk] * ((double)__bfloat162float(h) + (double)__bfloat162float(l));
+    // h + l is exact in FP32 (16 significant bits): the value GEMM 2 multiplies
+    if (sl) cf = fmaf(sl->p2[mk], __bfloat162float(h) + __bfloat162float(l), cf);
   }
-  c = block_sum(c, sh);
+  const double c = block_sum((double)cf, sh);
   if (threadIdx.x == 0) part[j * nblk + blockIdx.x] = c;
 }
 
@@ -387,7 +392,7 @@ __global__ void subset_scale_split_kernel(const float* __restrict__ T, int64_t m
 // markers k at which i is missing (set bits of the slot's word-major bit map), dfill[k] T'[j, flips[k]];
 // those products are staged per column in shared memory, kFinF flips (kFinF / 32 bit-map words) at a
 // time, so the scattered reads of T' happen once per block, not once per missing genotype.  The
-// terms are added in ascending flip order in FP64.
+// terms (a few tens per sample) are added in ascending flip order.
 constexpr int kFinF = 2048;
 constexpr int kFinPer = kChunk / kThreads;  // samples per thread
 
@@ -398,7 +403,7 @@ subset_finalize_kernel(const float* __restrict__ U, int64_t np, int64_t nn, cons
                        const double* __restrict__ part, int nblk, const double* __restrict__ winv,
                        float* __restrict__ Yf) {
   __shared__ double s_c;
-  __shared__ double tf[kFinF];
+  __shared__ float tf[kFinF];
   const int64_t j = blockIdx.y;
   const int32_t col = cols[j];
   if (col < 0) return;
@@ -416,9 +421,9 @@ subset_finalize_kernel(const float* __restrict__ U, int64_t np, int64_t nn, cons
     const int64_t i = i0 + (int64_t)r * kThreads;
     if (i < nn && winv[(int64_t)slot * np + i] != 0.0) live |= 1u << r;
   }
-  double du[kFinPer];
+  float du[kFinPer];
 #pragma unroll
-  for (int r = 0; r < kFinPer; ++r) du[r] = 0.0;
+  for (int r = 0; r < kFinPer; ++r) du[r] = 0.0f;
   const __nv_bfloat16* th = Th + j * mg;
   const __nv_bfloat16* tl = Tl + j * mg;
   for (int f0 = 0; f0 < sl.nflip; f0 += kFinF) {
@@ -426,7 +431,7 @@ subset_finalize_kernel(const float* __restrict__ U, int64_t np, int64_t nn, cons
     __syncthreads();
     for (int k = threadIdx.x; k < fn; k += kThreads) {
       const int64_t mk = sl.flips[f0 + k];
-      tf[k] = (double)sl.dfill[f0 + k] * ((double)__bfloat162float(th[mk]) + (double)__bfloat162float(tl[mk]));
+      tf[k] = sl.dfill[f0 + k] * (__bfloat162float(th[mk]) + __bfloat162float(tl[mk]));
     }
     __syncthreads();
     const int w0 = f0 / 32, wn = (fn + 31) / 32;
@@ -434,7 +439,7 @@ subset_finalize_kernel(const float* __restrict__ U, int64_t np, int64_t nn, cons
     for (int r = 0; r < kFinPer; ++r) {
       if (!((live >> r) & 1u)) continue;
       const uint32_t* bw = sl.bits + (int64_t)w0 * np + i0 + (int64_t)r * kThreads;
-      double d = du[r];
+      float d = du[r];
       for (int w = 0; w < wn; ++w) {
         uint32_t word = bw[(int64_t)w * np];
         while (word) {
@@ -447,13 +452,13 @@ subset_finalize_kernel(const float* __restrict__ U, int64_t np, int64_t nn, cons
     }
   }
   __syncthreads();
-  const double c = s_c;
+  const float cf = (float)s_c, inv_mf = (float)sl.inv_m;
 #pragma unroll
   for (int r = 0; r < kFinPer; ++r) {
     const int64_t i = i0 + (int64_t)r * kThreads;
     if (i >= np) break;
     float y = 0.0f;
-    if ((live >> r) & 1u) y = (float)(((double)U[j * np + i] - c + du[r]) * sl.inv_m);
+    if ((live >> r) & 1u) y = (U[j * np + i] - cf + du[r]) * inv_mf;
     Yf[(int64_t)col * np + i] = y;
   }
 }

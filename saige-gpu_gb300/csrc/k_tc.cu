@@ -41,6 +41,7 @@
 //     RHS-major so each TMEM column is a coalesced row of Y^T; split variants
 //     with TF32 or BF16 high/low halves of K and P (three products).
 #include "sg_internal.h"
+#include <algorithm>
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -665,22 +666,25 @@ struct TileCache {
   size_t cap = 0;
 };
 
+// A table grows geometrically from 64 Ki tiles (512 KB): cudaFree waits for the whole device, so a
+// launch should almost never find its table too small.
 cudaError_t upload_tiles(TileCache& tc, cudaStream_t s) {
   if (tc.host.size() > tc.cap) {
     if (tc.dev) cudaFree(tc.dev);
     if (tc.pinned) cudaFreeHost(tc.pinned);
     tc.dev = nullptr;
     tc.pinned = nullptr;
+    const size_t cap = std::max<size_t>({tc.host.size(), 2 * tc.cap, (size_t)1 << 16});
     tc.cap = 0;
-    cudaError_t e = cudaMalloc(&tc.dev, tc.host.size() * sizeof(TileCoord));
-    if (e == cudaSuccess) e = cudaHostAlloc(&tc.pinned, tc.host.size() * sizeof(TileCoord), cudaHostAllocDefault);
+    cudaError_t e = cudaMalloc(&tc.dev, cap * sizeof(TileCoord));
+    if (e == cudaSuccess) e = cudaHostAlloc(&tc.pinned, cap * sizeof(TileCoord), cudaHostAllocDefault);
     if (e != cudaSuccess) {
       if (tc.dev) cudaFree(tc.dev);
       tc.dev = nullptr;
       tc.pinned = nullptr;
       return e;
     }
-    tc.cap = tc.host.size();
+    tc.cap = cap;
   }
   std::memcpy(tc.pinned, tc.host.data(), tc.host.size() * sizeof(TileCoord));
   return cudaMemcpyAsync(tc.dev, tc.pinned, tc.host.size() * sizeof(TileCoord), cudaMemcpyHostToDevice, s);

@@ -595,9 +595,11 @@ class Context:
         return float(v[0]), float(v[1]), float(v[2])
 
     def engine_step_trace(self, max_steps=65536):
-        """Per-step records since the last timing reset, shape (steps, 5): GRM.V columns, occupied
-        columns, GRM.V ms, step ms, idle ms before the step (-1 for the first)."""
-        out = np.zeros((max_steps, 5))
+        """Per-step records since the last timing reset, shape (steps, 8): GRM.V columns, occupied
+        columns, GRM.V ms, step ms, idle ms before the step (-1 for the first), host ms from the
+        previous finish to this launch (-1 for the first), host ms inside the launch, slot uploads
+        the admission waited for."""
+        out = np.zeros((max_steps, 8))
         n = C.c_int64()
         self._call("sg_engine_step_trace", _ptr(out, L.P_f64), int(max_steps), C.byref(n))
         return out[:n.value].copy()
