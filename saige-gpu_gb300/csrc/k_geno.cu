@@ -32,16 +32,27 @@ __global__ void marker_qc_kernel(const uint8_t* __restrict__ raw, int64_t pitch,
   const uint32_t* row = reinterpret_cast<const uint32_t*>(raw + marker * pitch);
   const int64_t nwords = (n_fam + 15) / 16;
   int nnon = 0, nmiss = 0, sum_ab = 0;
-  for (int64_t w = lane; w < nwords; w += 32) {
-    const uint32_t x = __ldg(row + w);
-    const uint32_t mk = __ldg(maskbits + w);
+  auto count = [&](uint32_t x, uint32_t mk) {
     const uint32_t lo = x & 0x55555555u, hi = (x >> 1) & 0x55555555u;
     const uint32_t miss = lo & ~hi;
     const uint32_t non = ~miss & mk;
     nmiss += __popc(miss & mk);
     nnon += __popc(non);
     sum_ab += __popc(hi & non) + __popc(lo & non);
+  };
+  // 16-byte loads over the row's whole quads (rows start 16-byte aligned), then the last words;
+  // the mask's quads need the same alignment, which cudaMalloc gives
+  const int64_t nquads = nwords / 4;
+  const uint4* row4 = reinterpret_cast<const uint4*>(row);
+  const uint4* mk4 = reinterpret_cast<const uint4*>(maskbits);
+  for (int64_t q = lane; q < nquads; q += 32) {
+    const uint4 x = __ldg(row4 + q), mk = __ldg(mk4 + q);
+    count(x.x, mk.x);
+    count(x.y, mk.y);
+    count(x.z, mk.z);
+    count(x.w, mk.w);
   }
+  for (int64_t w = 4 * nquads + lane; w < nwords; w += 32) count(__ldg(row + w), __ldg(maskbits + w));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     nnon += __shfl_xor_sync(0xffffffffu, nnon, o);

@@ -203,15 +203,18 @@ void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* fl
 // Diagonal of M' K_S (sum over the subset's GRM markers of z'^2, the Jacobi preconditioner's
 // Get_Diagof_StdGeno, FIT.cpp:665-704), lut4[4 m + code] = d'_m (g - 2p'_m)^2 per packed code (the
 // missing code carries the subset fill).  Pass 1: block = 256 words of a marker row (16 samples
-// each, so a warp reads 128 contiguous bytes) x a chunk of kDiagChunkM markers; each chunk's table
-// is staged 256 markers at a time in shared memory; FP32 sums per chunk into part[chunk][sample].
-// Pass 2: per sample, the chunks' partials added in chunk order in FP64.
+// each, so a warp reads 128 contiguous bytes) x a chunk of kDiagChunkM markers.  The table is
+// staged 256 markers at a time in shared memory as pair entries: entry n of a marker holds the
+// values of the two samples whose codes form the 4-bit field n, so one 8-byte shared load serves two
+// samples (the shared-memory pipe, not DRAM, bounds this loop).  FP32 sums per chunk into
+// part[chunk][sample], each sample's markers added in marker order.  Pass 2: per sample, the chunks'
+// partials added in chunk order in FP64.
 constexpr int kDiagChunkM = 2048;
 
 __global__ void __launch_bounds__(kThreads)
 subset_diag_part_kernel(const uint32_t* __restrict__ codes32, int64_t words_per_row, int64_t nwords,
                         const float4* __restrict__ lut4, int64_t m, int64_t np, float* __restrict__ part) {
-  __shared__ float4 slut[kThreads];
+  __shared__ float2 spair[kThreads][16];
   const int64_t w = (int64_t)blockIdx.x * kThreads + threadIdx.x;
   const int64_t m0 = (int64_t)blockIdx.y * kDiagChunkM;
   const int64_t m1 = m0 + kDiagChunkM < m ? m0 + kDiagChunkM : m;
@@ -219,17 +222,28 @@ subset_diag_part_kernel(const uint32_t* __restrict__ codes32, int64_t words_per_
 #pragma unroll
   for (int s = 0; s < 16; ++s) acc[s] = 0.0f;
   for (int64_t k0 = m0; k0 < m1; k0 += kThreads) {
-    __syncthreads();
-    if (k0 + threadIdx.x < m1) slut[threadIdx.x] = lut4[k0 + threadIdx.x];
-    __syncthreads();
     const int kn = (int)(m1 - k0 < kThreads ? m1 - k0 : kThreads);
+    __syncthreads();
+    // entry i = (marker i / 16, field i % 16): a warp writes 32 consecutive entries (no bank conflicts)
+    for (int i = threadIdx.x; i < 16 * kn; i += kThreads) {
+      const float4 q = __ldg(lut4 + k0 + (i >> 4));
+      const int n = i & 15;
+      const float a = (n & 3) == 0 ? q.x : (n & 3) == 1 ? q.y : (n & 3) == 2 ? q.z : q.w;
+      const float b = (n >> 2) == 0 ? q.x : (n >> 2) == 1 ? q.y : (n >> 2) == 2 ? q.z : q.w;
+      spair[i >> 4][n] = make_float2(a, b);
+    }
+    __syncthreads();
     if (w < nwords) {
       const uint32_t* row = codes32 + k0 * words_per_row + w;
       for (int k = 0; k < kn; ++k) {
         const uint32_t word = __ldg(row + (int64_t)k * words_per_row);
-        const float* l = reinterpret_cast<const float*>(&slut[k]);
+        const float2* e = spair[k];
 #pragma unroll
-        for (int s = 0; s < 16; ++s) acc[s] += l[(word >> (2 * s)) & 3u];
+        for (int s = 0; s < 16; s += 2) {
+          const float2 v = e[(word >> (2 * s)) & 15u];
+          acc[s] += v.x;
+          acc[s + 1] += v.y;
+        }
       }
     }
   }
