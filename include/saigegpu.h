@@ -95,9 +95,10 @@ enum sg_tc_option {
   SG_TC_SUBSET_PAIR = 5, /* the subset-exact engine's genotype GEMMs on CTA pairs: 0 never,
                             1 always, 2 above 160 columns (default) */
   SG_TC_SUBSET_SLICE = 6 /* their K slice bytes per pipeline stage: 0 = by width (128 up to 160
-                            columns, else 64), 64, 128 or 256 (default: two 128-byte boxes per
-                            operand and stage; widths without room for two such stages -- above
-                            160 columns on single CTAs -- run 128) */
+                            columns, else 64), 64, 128, 256 (default: two 128-byte boxes per
+                            operand and stage) or 512 (four); a width without room for two such
+                            stages runs the next smaller one (256 above 160 columns on single
+                            CTAs: 128; 512 beyond 32-column tiles, or 64 on pairs: 256) */
 };
 int sg_set_tc_option(sg_ctx *ctx, int option, int value);
 int sg_get_tc_option(sg_ctx *ctx, int option, int *value);
@@ -110,7 +111,7 @@ int sg_set_grmv_plan(sg_ctx *ctx, int n, const int32_t *max_cols, const int32_t 
                      const int32_t *slice);
 int sg_get_grmv_plan(sg_ctx *ctx, int cap, int32_t *max_cols, int32_t *pair, int32_t *slice, int *n);
 /* The same per-width table for the subset-exact engine's genotype GEMMs (SG_TC_SUBSET_PAIR and
- * SG_TC_SUBSET_SLICE per bucket; slice 64, 128 or 256).  No reference counterpart. */
+ * SG_TC_SUBSET_SLICE per bucket; slice 64, 128, 256 or 512).  No reference counterpart. */
 int sg_set_subset_plan(sg_ctx *ctx, int n, const int32_t *max_cols, const int32_t *pair,
                        const int32_t *slice);
 int sg_get_subset_plan(sg_ctx *ctx, int cap, int32_t *max_cols, int32_t *pair, int32_t *slice, int *n);

@@ -322,16 +322,16 @@ struct TileCoord {
 // RB: bytes of one operand row's K slice per pipeline stage -- 128 (SWIZZLE_128B) or 64
 // (SWIZZLE_64B: half the bytes per stage, twice the stages in the same shared memory, for the
 // split-BF16 GRM.V, whose four operand tiles per stage left it with only two stages of 128-byte
-// slices), or 256: two adjacent 128-byte SWIZZLE_128B boxes per operand and stage, so that each
-// stage reads 256 contiguous bytes of every operand row (twice the bytes per DRAM page opened when
-// the rows of a streamed operand lie far apart, as G's do in the genotype GEMMs).
+// slices), or 256 / 512: two / four adjacent 128-byte SWIZZLE_128B boxes per operand and stage, so
+// that each stage reads 256 / 512 contiguous bytes of every operand row (more bytes per DRAM page
+// opened when the rows of a streamed operand lie far apart, as G's do in the genotype GEMMs).
 template <bool kTF32, int BN, int S, int kForm, bool kPair, int RB = 128>
 __global__ void __launch_bounds__(kGemmThreads, 1)
 tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
                const TileCoord* __restrict__ tiles, int num_kb, int drain_kb, float* __restrict__ D,
                int64_t ldd, float scale, int mode, int64_t nrows, const int32_t* __restrict__ colmap) {
-  static_assert(RB == 256 || RB == 128 || RB == 64, "K slices of 256, 128 or 64 bytes");
+  static_assert(RB == 512 || RB == 256 || RB == 128 || RB == 64, "K slices of 512, 256, 128 or 64 bytes");
   constexpr int kSW = RB > 128 ? 128 : RB;  // bytes of one swizzled box row (the TMA box's inner size)
   constexpr int kSub = RB / kSW;            // boxes per operand and stage, adjacent in K
   static_assert(!kPair || (BN / 2) % 8 == 0, "a CTA's half of the B tile is whole 8-row swizzle atoms");
@@ -843,7 +843,7 @@ bool tc_set_option(int opt, int value) {
       if (value != 0 && value != 64 && value != 128) return false;
       break;
     case kTcSubsetSlice:
-      if (value != 0 && value != 64 && value != 128 && value != 256) return false;
+      if (value != 0 && value != 64 && value != 128 && value != 256 && value != 512) return false;
       break;
   }
   g_opt[opt] = value;
@@ -895,7 +895,9 @@ bool tc_set_subset_plan(const int32_t* max_cols, const int32_t* pair, const int3
   std::vector<GrmvChoice> plan;
   for (int i = 0; i < n; ++i) {
     if (max_cols[i] <= 0 || (i > 0 && max_cols[i] <= max_cols[i - 1])) return false;
-    if ((pair[i] != 0 && pair[i] != 1) || (slice[i] != 64 && slice[i] != 128 && slice[i] != 256)) return false;
+    if ((pair[i] != 0 && pair[i] != 1) ||
+        (slice[i] != 64 && slice[i] != 128 && slice[i] != 256 && slice[i] != 512))
+      return false;
     plan.push_back(GrmvChoice{max_cols[i], pair[i], slice[i]});
   }
   g_subset_plan.swap(plan);
@@ -1017,9 +1019,14 @@ static int subset_slice(int64_t ncols) {
   return g_opt[kTcSubsetSlice] != 0 ? g_opt[kTcSubsetSlice] : (ncols <= 160 ? 128 : 64);
 }
 
-// 256-byte stages exist for the tile widths whose stage (128 A rows and two halves of the B rows,
-// 256 bytes each) leaves room for at least two stages; other widths run 128-byte stages.
-static bool splitb_has_256(int BN, bool pair) { return pair || BN <= 160; }
+// 256- and 512-byte stages exist for the tile widths whose stage (128 A rows and two halves of the
+// B rows, RB bytes each) leaves room for at least two stages; other widths fall back to the next
+// smaller stage that has a table.
+static int splitb_stage_bytes(int RB, int BN, bool pair) {
+  if (RB == 512 && !(BN == 32 || (pair && BN == 64))) RB = 256;
+  if (RB == 256 && !(pair || BN <= 160)) RB = 128;
+  return RB;
+}
 
 // Columns one GRM.V launch covers for ncols32 (a multiple of 16) live columns, padded so that the
 // modelled cost is lowest, capped at cap columns.  Cost model (L2->SM bytes of one pass, which
@@ -1266,9 +1273,9 @@ cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void
     return cudaErrorInvalidValue;
   const int BN = tc_gemm_tile_n(ncols, kTilesSplitB);
   const bool pair = subset_pair(ncols);
-  int RB = subset_slice(ncols);
-  if (RB == 256 && (!splitb_has_256(BN, pair) || kdim % 128 != 0)) RB = 128;
-  const int box = RB > 128 ? 128 : RB;  // a 256-byte stage is two 128-byte boxes per operand
+  int RB = splitb_stage_bytes(subset_slice(ncols), BN, pair);
+  while (RB > 128 && kdim % (RB / 2) != 0) RB /= 2;  // whole stages over K
+  const int box = RB > 128 ? 128 : RB;  // a 256- or 512-byte stage is 2 or 4 128-byte boxes per operand
   const uint64_t rb = (uint64_t)kdim * 2;
   CUtensorMap a, b, b2;
   if (!make_map(&a, A, false, kdim, rows, rb, kTileM, box) ||
@@ -1290,7 +1297,20 @@ cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void
                                                   rows);                                                    \
     break;
   // per CTA and stage: 128 A rows plus two halves of BN (BN / 2 on a CTA pair) B rows, RB bytes each
-  if (RB == 256 && pair) {
+  if (RB == 512 && pair) {
+    switch (BN) {
+      SG_SB(64, 2, true, 512)
+      SG_SB(32, 2, true, 512)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else if (RB == 512) {
+    switch (BN) {
+      SG_SB(32, 2, false, 512)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else if (RB == 256 && pair) {
     switch (BN) {
       SG_SB(256, 2, true, 256)
       SG_SB(224, 2, true, 256)

@@ -28,7 +28,7 @@ GRMV_BUCKETS = (32, 64, 96, 128, 160, 224, 320, 448, 640, 1024)
 GRMV_VARIANTS = ((0, 128), (0, 64), (1, 128), (1, 64))  # (CTA pair, K slice bytes)
 SYRK_VARIANTS = ((1, 8), (0, 16), (1, 16), (1, 32))     # (CTA pair, raster group); the default first
 SUBSET_BUCKETS = (32, 64, 128, 192, 256, 384, 512, 768, 1024)
-SUBSET_VARIANTS = ((0, 128), (1, 128), (0, 256), (1, 256), (0, 64), (1, 64))  # (CTA pair, K slice bytes)
+SUBSET_VARIANTS = ((0, 128), (1, 128), (0, 256), (1, 256), (0, 512), (1, 512), (0, 64), (1, 64))  # (CTA pair, K-stage bytes)
 
 # a variant other than the first is kept only when it is faster by more than the spread of
 # repeated timings

@@ -106,7 +106,7 @@ def test_subset_exact_variants_bit_identical(exact_cohort):
         for k in (1, 40, 200, 300):
             V = rng.standard_normal((N, k))
             outs = []
-            for pair, sl in ((0, 64), (0, 128), (1, 64), (1, 128), (0, 256), (1, 256)):
+            for pair, sl in ((0, 64), (0, 128), (1, 64), (1, 128), (0, 256), (1, 256), (0, 512), (1, 512)):
                 ctx.set_tc_option(TC_SUBSET_PAIR, pair)
                 ctx.set_tc_option(TC_SUBSET_SLICE, sl)
                 outs.append(ctx.grm_matmul(V))
