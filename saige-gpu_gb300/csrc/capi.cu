@@ -2073,7 +2073,9 @@ static int step_finish(sg_ctx* c, int64_t* n_finished) {
   SG_TRY(flush_states(c, false));
   SG_TRY(sync(c));
   *n_finished += fin;
-  e.t_finish_host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count();
+  e.t_fin_end = std::chrono::steady_clock::now();
+  e.have_fin_end = true;
+  e.t_finish_host_ms += std::chrono::duration<double, std::milli>(e.t_fin_end - th0).count();
   return SG_OK;
 }
 
@@ -2114,10 +2116,7 @@ static int engine_retire_immediate(sg_ctx* c, int64_t* n_finished) {
   }
   while (e.hi_col > 0 && e.col_req[e.hi_col - 1] == -1) --e.hi_col;
   SG_TRY(flush_states(c, false));
-  SG_TRY(sync(c));
-  e.t_fin_end = std::chrono::steady_clock::now();
-  e.have_fin_end = true;
-  return SG_OK;
+  return sync(c);
 }
 
 extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) {

@@ -206,10 +206,10 @@ void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* fl
 // each, so a warp reads 128 contiguous bytes) x a chunk of kDiagChunkM markers.  The table is
 // staged 256 markers at a time in shared memory as pair entries: entry n of a marker holds the
 // values of the two samples whose codes form the 4-bit field n, so one 8-byte shared load serves two
-// samples (the shared-memory pipe, not DRAM, bounds this loop).  FP32 sums per chunk into
-// part[chunk][sample], each sample's markers added in marker order.  Pass 2: per sample, the chunks'
+// samples.  FP32 sums per chunk into part[chunk][sample], each sample's markers added in marker
+// order; the words of four marker rows are requested together.  Pass 2: per sample, the chunks'
 // partials added in chunk order in FP64.
-constexpr int kDiagChunkM = 2048;
+constexpr int kDiagChunkM = 1024;
 
 __global__ void __launch_bounds__(kThreads)
 subset_diag_part_kernel(const uint32_t* __restrict__ codes32, int64_t words_per_row, int64_t nwords,
@@ -235,7 +235,24 @@ subset_diag_part_kernel(const uint32_t* __restrict__ codes32, int64_t words_per_
     __syncthreads();
     if (w < nwords) {
       const uint32_t* row = codes32 + k0 * words_per_row + w;
-      for (int k = 0; k < kn; ++k) {
+      // four marker rows' words requested together, then added in marker order
+      int k = 0;
+      for (; k + 4 <= kn; k += 4) {
+        uint32_t word[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) word[u] = __ldg(row + (int64_t)(k + u) * words_per_row);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float2* e = spair[k + u];
+#pragma unroll
+          for (int s = 0; s < 16; s += 2) {
+            const float2 v = e[(word[u] >> (2 * s)) & 15u];
+            acc[s] += v.x;
+            acc[s + 1] += v.y;
+          }
+        }
+      }
+      for (; k < kn; ++k) {
         const uint32_t word = __ldg(row + (int64_t)k * words_per_row);
         const float2* e = spair[k];
 #pragma unroll
