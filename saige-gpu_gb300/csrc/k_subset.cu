@@ -347,50 +347,43 @@ __global__ void subset_center_split_kernel(const float* __restrict__ Pf, int64_t
 }
 
 // T[j, flips[k]] += dfill[k] * sum over the subset samples missing at that marker of v_c[j, i]:
-// block (j, word pair) scans every sample's two bit-map words (w, w + 1) with v_c read once for
-// both, accumulates their (at most 64) markers in registers, then reduces them over the block in a
-// fixed order.
-__global__ void __launch_bounds__(kThreads)
-subset_flip_t_kernel(const __nv_bfloat16* __restrict__ Vh, const __nv_bfloat16* __restrict__ Vl,
-                     int64_t np, int64_t nn, const int32_t* __restrict__ cols,
-                     const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
-                     float* __restrict__ T, int64_t mg) {
-  __shared__ float red[kThreads / 32][64];
+// block (j, w) scans every sample's bit-map word w and accumulates the (at most 32) markers of that
+// word in registers, then reduces them over the block in a fixed order.
+__global__ void subset_flip_t_kernel(const __nv_bfloat16* __restrict__ Vh, const __nv_bfloat16* __restrict__ Vl,
+                                     int64_t np, int64_t nn, const int32_t* __restrict__ cols,
+                                     const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
+                                     float* __restrict__ T, int64_t mg) {
+  __shared__ float red[kThreads / 32][32];
   const int64_t j = blockIdx.y;
   const int32_t col = cols[j];
   if (col < 0) return;
   const SubsetSlot sl = slots[st[col].pheno];
-  const int w0 = 2 * blockIdx.x;
-  if (w0 >= sl.W) return;
-  const bool two = w0 + 1 < sl.W;
-  float acc[64];
+  const int w = blockIdx.x;
+  if (w >= sl.W) return;
+  float acc[32];
 #pragma unroll
-  for (int b = 0; b < 64; ++b) acc[b] = 0.0f;
-  const uint32_t* bw0 = sl.bits + (int64_t)w0 * np;
-  const uint32_t* bw1 = two ? bw0 + np : bw0;
+  for (int b = 0; b < 32; ++b) acc[b] = 0.0f;
+  const uint32_t* bw = sl.bits + (int64_t)w * np;
   for (int64_t i = threadIdx.x; i < nn; i += kThreads) {
-    const uint32_t word0 = bw0[i];
-    const uint32_t word1 = two ? bw1[i] : 0u;
-    if ((word0 | word1) == 0u) continue;
+    const uint32_t word = bw[i];
+    if (word == 0u) continue;
     const float v = __bfloat162float(Vh[j * np + i]) + __bfloat162float(Vl[j * np + i]);
 #pragma unroll
-    for (int b = 0; b < 32; ++b) {
-      if ((word0 >> b) & 1u) acc[b] += v;
-      if ((word1 >> b) & 1u) acc[32 + b] += v;
-    }
+    for (int b = 0; b < 32; ++b)
+      if ((word >> b) & 1u) acc[b] += v;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int b = 0; b < 64; ++b) {
+  for (int b = 0; b < 32; ++b) {
     float x = acc[b];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == (b & 31)) red[warp][b] = x;
+    if (lane == b) red[warp][b] = x;
   }
   __syncthreads();
-  if (threadIdx.x < 64) {
+  if (threadIdx.x < 32) {
     const int b = threadIdx.x;
-    const int k = 32 * w0 + b;
+    const int k = 32 * w + b;
     if (k < sl.nflip) {
       float s = 0.0f;
       for (int q = 0; q < kThreads / 32; ++q) s += red[q][b];
@@ -518,7 +511,7 @@ void launch_subset_scale(const void* Vh, const void* Vl, int64_t np, int64_t nn,
                          const ColState* st, const SubsetSlot* slots, int max_w, float* T, int64_t mg, void* Th,
                          void* Tl, double* part, cudaStream_t s) {
   if (max_w > 0) {
-    dim3 g1((unsigned)((max_w + 1) / 2), (unsigned)ncols);
+    dim3 g1((unsigned)max_w, (unsigned)ncols);
     subset_flip_t_kernel<<<g1, kThreads, 0, s>>>(static_cast<const __nv_bfloat16*>(Vh),
                                                  static_cast<const __nv_bfloat16*>(Vl), np, nn, cols, st, slots, T,
                                                  mg);

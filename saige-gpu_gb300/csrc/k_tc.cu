@@ -57,7 +57,12 @@ namespace {
 
 constexpr int kTileM = 128;
 // products per K step of the GEMM kernel (see tc_gemm_kernel)
-constexpr int kOne = 0, kSplitB = 1, kSplit3 = 2, kSplit4 = 3;
+constexpr int kOne = 0, kSplitB = 1, kSplit3 = 2, kSplit4 = 3, kSplitB8 = 4;
+// operands of the second products (A2, B2) exist for every form but kOne (B2) and kSplitB (A2)
+__host__ __device__ constexpr bool form_has_a2(int f) { return f == kSplit3 || f == kSplit4 || f == kSplitB8; }
+__host__ __device__ constexpr bool form_has_b2(int f) { return f != kOne; }
+// row bytes of the second operands per stage: kSplitB8's are E4M3, half the bytes of FP16 A and B
+__host__ __device__ constexpr int form_rb2(int f, int rb) { return f == kSplitB8 ? rb / 2 : rb; }
 constexpr int kRowBytes = 128;                 // one SWIZZLE_128B atom row
 constexpr int kATileBytes = kTileM * kRowBytes;  // 16 KB
 constexpr unsigned long long kWaitBudgetNs = 4000000000ull;  // 4 s per wait
@@ -244,6 +249,22 @@ __device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, ui
   }
 }
 
+// kind::f8f6f4 (both operands E4M3, K = 32 elements = 32 bytes per instruction, FP32 accumulator)
+template <bool kPair>
+__device__ __forceinline__ void umma_f8(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+  if constexpr (kPair) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+  }
+}
+
 __device__ __forceinline__ uint32_t cluster_rank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -310,6 +331,8 @@ struct TileCoord {
 //   kSplitB A Bh + A Bl                  (A exact in the operand type, B as high + low halves)
 //   kSplit3 Ah Bh + Ah Bl + Al Bh        (both as halves, the low x low term dropped)
 //   kSplit4 Ah Bh + Ah Bl + Al Bh + Al Bl
+//   kSplitB8 A Bh + A8 Bl8               (A, Bh in FP16 by kind::f16; A8 = A and Bl8 = the low half in
+//                                         E4M3 by kind::f8f6f4, into the same accumulator; RB >= 256)
 // kPair: two CTAs of a 2-CTA cluster compute one 256 x BN tile with tcgen05.mma.cta_group::2, issued
 // by the even CTA (the leader).  Each CTA loads its own 128 rows of A and half of the B tile
 // (BN / 2 rows) into the same shared-memory offsets with plain TMA loads; the loads of both signal
@@ -335,18 +358,28 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
   constexpr int kSW = RB > 128 ? 128 : RB;  // bytes of one swizzled box row (the TMA box's inner size)
   constexpr int kSub = RB / kSW;            // boxes per operand and stage, adjacent in K
   static_assert(!kPair || (BN / 2) % 8 == 0, "a CTA's half of the B tile is whole 8-row swizzle atoms");
+  constexpr bool kF8 = kForm == kSplitB8;
+  static_assert(!kF8 || (RB >= 256 && !kTF32), "the E4M3 low products take whole 128-byte boxes");
   constexpr int kATile = kTileM * RB;
   constexpr int kBRows = kPair ? BN / 2 : BN;  // rows of the B tile this CTA loads
   constexpr int kBTileBytes = kBRows * RB;
-  constexpr int kStageBytes = kATile * (kForm >= kSplit3 ? 2 : 1) + kBTileBytes * (kForm >= kSplitB ? 2 : 1);
-  // stage layout: [A][B], then [B2] (kSplitB) or [A2][B2] (kSplit3, kSplit4)
-  constexpr int kOffB2 = kForm == kSplitB ? kATile + kBTileBytes : 2 * kATile + kBTileBytes;
-  constexpr uint32_t kFmt = kTF32 ? 2u : 1u;
+  constexpr int RB2 = form_rb2(kForm, RB);    // row bytes of A2 / B2 per stage
+  constexpr int kSub2 = RB2 > 128 ? RB2 / 128 : 1;
+  constexpr int kSW2 = RB2 > 128 ? 128 : RB2;
+  constexpr int kATile2 = kTileM * RB2, kBTile2 = kBRows * RB2;
+  constexpr int kStageBytes = kATile + kBTileBytes + (form_has_a2(kForm) ? kATile2 : 0) + (form_has_b2(kForm) ? kBTile2 : 0);
+  // stage layout: [A][B][A2][B2], absent operands taking no room
+  constexpr int kOffA2 = kATile + kBTileBytes;
+  constexpr int kOffB2 = kOffA2 + (form_has_a2(kForm) ? kATile2 : 0);
+  // operand formats: TF32 = 2, BF16 = 1, FP16 = 0 (kind::f16 / tf32); E4M3 = 0 (kind::f8f6f4)
+  constexpr uint32_t kFmt = kTF32 ? 2u : (kF8 ? 0u : 1u);
   constexpr int kKSteps = RB / 32;     // 32 bytes of K per MMA
+  constexpr int kKSteps2 = RB2 / 32;
   // two accumulators, each a power of two >= 32 columns wide
   constexpr uint32_t kAccCols = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
   constexpr uint32_t kTmemCols = 2 * kAccCols;
   constexpr uint32_t kIdesc = make_idesc(kFmt, kPair ? 2 * kTileM : kTileM, BN);
+  constexpr uint32_t kIdesc8 = make_idesc(0u, kPair ? 2 * kTileM : kTileM, BN);  // E4M3 x E4M3
   constexpr int kGroups = (BN + 31) / 32;     // 32-column groups of the tile
   constexpr int kHalfGroups = (kGroups + 1) / 2;
   static_assert(kDrainWarps == 8 && kGemmThreads == 32 * (kDrainWarps + 2),
@@ -424,9 +457,18 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
             const int32_t xu = x + u * (kSW / (kTF32 ? 4 : 2));
             tma_load_2d_pair(st + u * kTileM * kSW, &mapA, fb, xu, ya);
             tma_load_2d_pair(st + kATile + u * kBRows * kSW, &mapB, fb, xu, yb);
-            if constexpr (kForm >= kSplit3)
-              tma_load_2d_pair(st + kATile + kBTileBytes + u * kTileM * kSW, &mapA2, fb, xu, ya);
-            if constexpr (kForm >= kSplitB) tma_load_2d_pair(st + kOffB2 + u * kBRows * kSW, &mapB2, fb, xu, yb);
+            if constexpr (!kF8) {
+              if constexpr (form_has_a2(kForm)) tma_load_2d_pair(st + kOffA2 + u * kTileM * kSW, &mapA2, fb, xu, ya);
+              if constexpr (form_has_b2(kForm)) tma_load_2d_pair(st + kOffB2 + u * kBRows * kSW, &mapB2, fb, xu, yb);
+            }
+          }
+          if constexpr (kF8) {  // E4M3 operands: one byte per element, the same K elements
+#pragma unroll
+            for (int u = 0; u < kSub2; ++u) {
+              const int32_t xu = x + u * kSW2;
+              tma_load_2d_pair(st + kOffA2 + u * kTileM * kSW2, &mapA2, fb, xu, ya);
+              tma_load_2d_pair(st + kOffB2 + u * kBRows * kSW2, &mapB2, fb, xu, yb);
+            }
           }
         } else {
           mbar_expect_tx(&full[s], (uint32_t)kStageBytes);
@@ -435,9 +477,18 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
             const int32_t xu = x + u * (kSW / (kTF32 ? 4 : 2));
             tma_load_2d(st + u * kTileM * kSW, &mapA, &full[s], xu, ya);
             tma_load_2d(st + kATile + u * kBRows * kSW, &mapB, &full[s], xu, yb);
-            if constexpr (kForm >= kSplit3)
-              tma_load_2d(st + kATile + kBTileBytes + u * kTileM * kSW, &mapA2, &full[s], xu, ya);
-            if constexpr (kForm >= kSplitB) tma_load_2d(st + kOffB2 + u * kBRows * kSW, &mapB2, &full[s], xu, yb);
+            if constexpr (!kF8) {
+              if constexpr (form_has_a2(kForm)) tma_load_2d(st + kOffA2 + u * kTileM * kSW, &mapA2, &full[s], xu, ya);
+              if constexpr (form_has_b2(kForm)) tma_load_2d(st + kOffB2 + u * kBRows * kSW, &mapB2, &full[s], xu, yb);
+            }
+          }
+          if constexpr (kF8) {
+#pragma unroll
+            for (int u = 0; u < kSub2; ++u) {
+              const int32_t xu = x + u * kSW2;
+              tma_load_2d(st + kOffA2 + u * kTileM * kSW2, &mapA2, &full[s], xu, ya);
+              tma_load_2d(st + kOffB2 + u * kBRows * kSW2, &mapB2, &full[s], xu, yb);
+            }
           }
         }
       }
@@ -473,15 +524,25 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__
           const uint32_t ka = (uint32_t)((k / (kSW / 32)) * kTileM * kSW + 32 * (k % (kSW / 32)));
           const uint32_t kbo = (uint32_t)((k / (kSW / 32)) * kBRows * kSW + 32 * (k % (kSW / 32)));
           umma<kTF32, kPair>(dacc, smem_desc_kmajor<kSW>(a0 + ka), smem_desc_kmajor<kSW>(b0 + kbo), kIdesc, acc);
-          if constexpr (kForm >= kSplitB) {
+          if constexpr (!kF8 && form_has_b2(kForm)) {
             const uint32_t b1 = a0 + kOffB2;            // Bl
             umma<kTF32, kPair>(dacc, smem_desc_kmajor<kSW>(a0 + ka), smem_desc_kmajor<kSW>(b1 + kbo), kIdesc, 1u);
-            if constexpr (kForm >= kSplit3) {
-              const uint32_t a1 = b0 + kBTileBytes;     // Al
+            if constexpr (form_has_a2(kForm)) {
+              const uint32_t a1 = a0 + kOffA2;          // Al
               umma<kTF32, kPair>(dacc, smem_desc_kmajor<kSW>(a1 + ka), smem_desc_kmajor<kSW>(b0 + kbo), kIdesc, 1u);
               if constexpr (kForm == kSplit4)
                 umma<kTF32, kPair>(dacc, smem_desc_kmajor<kSW>(a1 + ka), smem_desc_kmajor<kSW>(b1 + kbo), kIdesc, 1u);
             }
+          }
+        }
+        if constexpr (kF8) {
+          // the low products: E4M3 A8 x Bl8 over the same K elements, after the stage's FP16 products
+          const uint32_t a8 = a0 + kOffA2, b8 = a0 + kOffB2;
+#pragma unroll
+          for (int k = 0; k < kKSteps2; ++k) {
+            const uint32_t ka = (uint32_t)((k / (kSW2 / 32)) * kTileM * kSW2 + 32 * (k % (kSW2 / 32)));
+            const uint32_t kbo = (uint32_t)((k / (kSW2 / 32)) * kBRows * kSW2 + 32 * (k % (kSW2 / 32)));
+            umma_f8<kPair>(dacc, smem_desc_kmajor<kSW2>(a8 + ka), smem_desc_kmajor<kSW2>(b8 + kbo), kIdesc8, 1u);
           }
         }
         // the stage is reusable once these MMAs have read it (in both CTAs of a pair)
@@ -604,25 +665,31 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 // 2D K-major map: rows x inner elements, row stride in bytes, box = slice_bytes (128: SWIZZLE_128B,
 // 64: SWIZZLE_64B) x box_rows.
-bool make_map(CUtensorMap* m, const void* base, bool f32, uint64_t inner, uint64_t rows,
-              uint64_t row_bytes, uint32_t box_rows, int slice_bytes = kRowBytes) {
+bool make_map_dt(CUtensorMap* m, const void* base, CUtensorMapDataType dt, int esize, uint64_t inner,
+                 uint64_t rows, uint64_t row_bytes, uint32_t box_rows, int slice_bytes) {
   auto fn = encode_fn();
   if (!fn) return false;
   const cuuint64_t dims[2] = {inner, rows};
   const cuuint64_t strides[1] = {row_bytes};
-  const cuuint32_t box[2] = {(cuuint32_t)(slice_bytes / (f32 ? 4 : 2)), box_rows};
+  const cuuint32_t box[2] = {(cuuint32_t)(slice_bytes / esize), box_rows};
   const cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
-                  const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  CUresult r = fn(m, dt, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   slice_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
+bool make_map(CUtensorMap* m, const void* base, bool f32, uint64_t inner, uint64_t rows,
+              uint64_t row_bytes, uint32_t box_rows, int slice_bytes = kRowBytes) {
+  return make_map_dt(m, base, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, f32 ? 4 : 2,
+                     inner, rows, row_bytes, box_rows, slice_bytes);
+}
+
 template <int BN, int S, int kForm, bool kPair, int RB = kRowBytes>
 constexpr size_t smem_bytes() {
-  return (size_t)S * ((size_t)kTileM * RB * (kForm >= kSplit3 ? 2 : 1) +
-                      (size_t)(kPair ? BN / 2 : BN) * RB * (kForm >= kSplitB ? 2 : 1)) +
+  const size_t brows = kPair ? BN / 2 : BN, rb2 = form_rb2(kForm, RB);
+  return (size_t)S * ((size_t)kTileM * RB + brows * RB + (form_has_a2(kForm) ? (size_t)kTileM * rb2 : 0) +
+                      (form_has_b2(kForm) ? brows * rb2 : 0)) +
          1024 + 256;
 }
 
@@ -1387,6 +1454,68 @@ cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void
     }
   }
 #undef SG_SB
+  if (e != cudaSuccess) return e;
+  return check ? check_error_flag(s) : cudaSuccess;
+}
+
+// The same GEMM with the high halves in FP16 and the low halves in E4M3: D = A Bh + A8 Bl8, A (FP16)
+// and A8 (E4M3) the same exact values, K stages of 256 bytes of A (128 elements; the E4M3 operands
+// take one 128-byte box per row and stage).  The low products run at twice the FP16 rate, so a
+// stage costs three quarters of the two FP16 (or BF16) products' time.  Tiles of more than 160
+// columns run on CTA pairs (a single CTA has room for one such stage only).
+cudaError_t tc_gemm_splitb8(const void* A, const void* A8, int64_t rows, int64_t kdim, const void* Bh,
+                            const void* Bl8, int64_t ncols, float* D, int64_t ldd, cudaStream_t s, bool check,
+                            int site) {
+  if (rows % kTileM != 0 || kdim % 128 != 0 || ncols % 32 != 0 || ncols <= 0 || !A || !A8 || !Bh || !Bl8 ||
+      site < 0 || site > 1)
+    return cudaErrorInvalidValue;
+  const int BN = tc_gemm_tile_n(ncols, kTilesSplitB);
+  const bool pair = subset_pair(ncols) || BN > 160;
+  const int brows = pair ? BN / 2 : BN;
+  CUtensorMap a, b, a8, b8;
+  if (!make_map_dt(&a, A, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, kdim, rows, (uint64_t)kdim * 2, kTileM, 128) ||
+      !make_map_dt(&b, Bh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, kdim, ncols, (uint64_t)kdim * 2, brows, 128) ||
+      !make_map_dt(&a8, A8, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, kdim, rows, (uint64_t)kdim, kTileM, 128) ||
+      !make_map_dt(&b8, Bl8, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, kdim, ncols, (uint64_t)kdim, brows, 128))
+    return cudaErrorInvalidValue;
+  static TileCache caches[2];
+  TileCache& cache = caches[site];
+  cudaError_t e = grmv_tiles(cache, rows, ncols, BN, pair, s);
+  if (e != cudaSuccess) return e;
+  const int num_kb = (int)(kdim / 128);
+  const int nt = (int)cache.host.size();
+  const int dk = drain_stages(256);
+#define SG_SB8(BNv, Sv, Pv)                                                                                  \
+  case BNv:                                                                                                  \
+    e = launch<false, BNv, Sv, kSplitB8, Pv, 256>(a, b, a8, b8, cache.dev, nt, num_kb, dk, D, ldd, 1.0f, 1, s, \
+                                                  rows);                                                    \
+    break;
+  // per CTA and stage: 128 A rows (256 B FP16 + 128 B E4M3) and BN (BN / 2 on a pair) B rows alike
+  if (pair) {
+    switch (BN) {
+      SG_SB8(256, 2, true)
+      SG_SB8(224, 2, true)
+      SG_SB8(192, 2, true)
+      SG_SB8(160, 2, true)
+      SG_SB8(128, 3, true)
+      SG_SB8(96, 3, true)
+      SG_SB8(64, 3, true)
+      SG_SB8(32, 4, true)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else {
+    switch (BN) {
+      SG_SB8(160, 2, false)
+      SG_SB8(128, 2, false)
+      SG_SB8(96, 2, false)
+      SG_SB8(64, 3, false)
+      SG_SB8(32, 3, false)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  }
+#undef SG_SB8
   if (e != cudaSuccess) return e;
   return check ? check_error_flag(s) : cudaSuccess;
 }

@@ -128,6 +128,10 @@ enum { kTilesPlain = 0, kTilesSplitTF32 = 1, kTilesSplitBF16 = 2, kTilesSplitB =
 // site (0 or 1): which of two call sites queued back to back on one stream (own tile tables).
 cudaError_t tc_gemm_splitb(const void* A, int64_t rows, int64_t kdim, const void* Bh, const void* Bl,
                            int64_t ncols, float* D, int64_t ldd, cudaStream_t s, bool check, int site);
+// The same with FP16 high halves and E4M3 low halves (A in FP16 and in E4M3, kdim a multiple of 128)
+cudaError_t tc_gemm_splitb8(const void* A, const void* A8, int64_t rows, int64_t kdim, const void* Bh,
+                            const void* Bl8, int64_t ncols, float* D, int64_t ldd, cudaStream_t s, bool check,
+                            int site);
 // Column tile width the GRM.V kernel uses for ncols columns.
 int tc_gemm_tile_n(int64_t ncols, int set);
 // Columns a GRM.V launch covers for ncols live columns (a multiple of 32, or of 16 for split-BF16),
