@@ -64,10 +64,11 @@ def parse():
     ap.add_argument("--phenos", type=int, default=64)
     ap.add_argument("--miss", type=float, default=0.02)
     ap.add_argument("--seed", type=int, default=1003)
-    ap.add_argument("--mode", default="subset", choices=["subset", "bf16x3", "tf32x3", "tf32", "fp32"],
+    ap.add_argument("--mode", default="subset", choices=["subset", "subset8", "bf16x3", "tf32x3", "tf32", "fp32"],
                     help="GRM.V engine: subset = each phenotype's GRM from its own samples (the reference's "
-                         "setgeno per phenotype; genotype GEMMs), the others restrict the cohort GRM to the "
-                         "phenotype's samples (an approximation for masked phenotypes)")
+                         "setgeno per phenotype; genotype GEMMs of BF16 halves), subset8 = the same with FP16 "
+                         "high and E4M3 low halves; the others restrict the cohort GRM to the phenotype's "
+                         "samples (an approximation for masked phenotypes)")
     ap.add_argument("--grm", default="bf16x3", choices=["bf16x3", "bf16"],
                     help="GRM build of the cohort-GRM engines: split-BF16 standardised genotypes (four "
                          "products) or BF16 (one)")
@@ -225,7 +226,7 @@ GRMV_TRAFFIC_BASIS = ("ncu DRAM bytes of two N=24576 launches (224 and 512 colum
                       "(profiles/grmv_bf16x3_n24576_and_n100k.md)")
 
 
-def subset_roofline(peaks, t_dev, np_, mg):
+def subset_roofline(peaks, t_dev, np_, mg, f8=False):
     """Roofline of the subset-exact engine's GRM.V (two genotype GEMMs and the small kernels around
     them, timed together by the engine's CUDA events).  Algorithmic work per launch over C columns:
     bytes = the genotype matrix read by both GEMMs (2 B per sample and marker each) + the centred
@@ -237,19 +238,24 @@ def subset_roofline(peaks, t_dev, np_, mg):
     cols = t_dev["gemm_cols"] / launches
     bytes_alg = 2.0 * 2.0 * np_ * mg + 8.0 * (np_ + mg) * cols
     flops_alg = 2.0 * 2.0 * np_ * mg * cols
+    # executed tensor work in BF16-product equivalents: two BF16 products, or one FP16 product plus one
+    # E4M3 product at twice the rate
+    prod = 1.5 if f8 else 2.0
     hbm = peaks.get("hbm_gbs", 6800.0)
     tc_peak = peaks.get("bf16_tflops_sustained", 1700.0)
     t = ms * 1e-3
     a_bw = bytes_alg / t / 1e9
     a_tc = flops_alg / t / 1e12
-    common = {"traffic": None, "kernel": "tc_gemm_kernel<bf16, kSplitB> x 2 (G'V, G T') + subset kernels",
+    common = {"traffic": None,
+              "kernel": ("tc_gemm_kernel<fp16 + e4m3, kSplitB8>" if f8 else "tc_gemm_kernel<bf16, kSplitB>")
+                        + " x 2 (G'V, G T') + subset kernels",
               "per_launch_ms": round(ms, 3), "columns_per_launch": round(cols, 1),
               "algorithmic_bytes_per_launch": bytes_alg, "algorithmic_flops_per_launch": flops_alg,
               "algorithmic_basis": "bytes: G read by both GEMMs + vector halves read + T and U written; "
                                    "FLOPs: 2 GEMMs x 2 N_p M_g per column",
-              "executed": {"products": 2.0, "tensor_flops_per_launch": 2.0 * flops_alg,
-                           "tflops": round(2.0 * a_tc, 1), "peak": tc_peak,
-                           "frac": round(2.0 * a_tc / tc_peak, 4),
+              "executed": {"products": prod, "tensor_flops_per_launch": prod * flops_alg,
+                           "tflops": round(prod * a_tc, 1), "peak": tc_peak,
+                           "frac": round(prod * a_tc / tc_peak, 4),
                            "peak_source": "measured bf16_tflops_sustained (MEASURED_PEAKS.json)"}}
     if a_bw / hbm >= a_tc / tc_peak:
         return dict({"bound": "hbm", "achieved": round(a_bw, 1), "peak": hbm, "unit": "GB/s",
@@ -462,8 +468,8 @@ def reference_gpu_matvec(n, m_qc, iters_per_fit, reps=5):
 def run_ours(args, rank, world, local):
     import torch
     from saigegpu import (Context, GRM_BF16_TC, GRM_BF16X3_TC, MV_BF16X3_TC, MV_TF32X3_TC, MV_TF32_TC,
-                          MV_FP32_SIMT, MV_SUBSET_EXACT)
-    exact = args.mode == "subset"
+                          MV_FP32_SIMT, MV_SUBSET_EXACT, MV_SUBSET_EXACT_F8)
+    exact = args.mode in ("subset", "subset8")
     peaks = load_peaks()
     ctx = Context(local)
     t_setup = time.perf_counter()
@@ -475,7 +481,7 @@ def run_ours(args, rank, world, local):
     d = ctx.dims()
     syrk_flops = float(d["n"]) * (d["n"] + 1) * d["m_qc"]
     syrk1_ms = None  # the single-product BF16 SYRK (the tuner's chosen shape)
-    if not args.no_tune and args.mode in ("subset", "bf16x3"):
+    if not args.no_tune and args.mode in ("subset", "subset8", "bf16x3"):
         # SYRK shape (and for the cohort-GRM engine the per-width GRM.V plan) from measured times;
         # leaves the single-product BF16 GRM built
         from saigegpu import tune
@@ -499,14 +505,14 @@ def run_ours(args, rank, world, local):
     # the timed steps: K batches of new phenotypes (their own traits and sample subsets), streamed
     # through P phenotype slots -- a fit enters as soon as one finishes, as a serving process runs
     timed_specs = [sp for b in range(args.steps) for sp in make_specs(ctx, args, args.seed + 17 * rank + 1 + b, b + 1)]
-    mode = {"subset": MV_SUBSET_EXACT, "bf16x3": MV_BF16X3_TC, "tf32x3": MV_TF32X3_TC, "tf32": MV_TF32_TC,
-            "fp32": MV_FP32_SIMT}[args.mode]
+    mode = {"subset": MV_SUBSET_EXACT, "subset8": MV_SUBSET_EXACT_F8, "bf16x3": MV_BF16X3_TC,
+            "tf32x3": MV_TF32X3_TC, "tf32": MV_TF32_TC, "fp32": MV_FP32_SIMT}[args.mode]
     ctx.set_matvec_mode(mode)
     g_ms = ctx.build_timing()["zbuild_ms"] if exact else None  # the genotype matrix build
     if exact and tune_report is not None:
         # CTA pairs and K slices of the genotype GEMMs per launch width, from measured times
         from saigegpu import tune
-        tune_report["subset"] = tune.tune_subset(ctx)
+        tune_report["subset"] = tune.tune_subset(ctx, mode=mode)
         tune_report["subset_plan"] = ctx.subset_plan()
     from saigegpu import serve as _serve
     cols = _serve.columns_for(specs)
@@ -555,14 +561,15 @@ def run_ours(args, rank, world, local):
     npad_n = ctx.grm_padded_n()
     mg = (args.m + 127) // 128 * 128
     if exact:
-        roof = subset_roofline(peaks, tdev, npad_n, mg)
+        roof = subset_roofline(peaks, tdev, npad_n, mg, f8=args.mode == "subset8")
     else:
         roof = grm_roofline(ctx, peaks, tdev, d["n"], npad_n, args.mode, traffic)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "fits/hr", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_wall / args.steps * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {"subset": "bf16x2-tc/fp64", "bf16x3": "bf16x3-tc/fp64", "tf32x3": "tf32x3-tc/fp64",
+        "dtype": {"subset": "bf16x2-tc/fp64", "subset8": "fp16+e4m3-tc/fp64", "bf16x3": "bf16x3-tc/fp64",
+                  "tf32x3": "tf32x3-tc/fp64",
                   "tf32": "tf32-tc/fp64", "fp32": "fp32/fp64"}[args.mode],
         "data": "synthetic (seeded cohort generator; the reference's 150k x 100k synthetic AFR set is external)",
         "config": {"workload": "batched null-model fits on a resident GRM", "n_samples": d["n"],
@@ -577,8 +584,9 @@ def run_ours(args, rank, world, local):
                                  "frequencies, fill, QC and 1/sd (setgeno per phenotype, FIT.cpp:376-385, 436-495)"
                                  if exact else
                                  "masked approximation: the cohort GRM restricted to each phenotype's samples"),
-                   "grm": ("genotype matrix (0/1/2, BF16) in both layouts, K_S applied as G'V then G T' with "
-                           "per-phenotype weights; no K" if exact else
+                   "grm": ("genotype matrix (0/1/2, %s) in both layouts, K_S applied as G'V then G T' with "
+                           "per-phenotype weights; no K" % ("FP16 and E4M3" if args.mode == "subset8" else "BF16")
+                           if exact else
                            "split-BF16 tcgen05 SYRK (four products), FP32 K" if args.grm == "bf16x3"
                            else "BF16 tcgen05 SYRK, FP32 K"),
                    "grm_v": args.mode,

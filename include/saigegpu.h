@@ -62,7 +62,11 @@ enum sg_matvec_mode {
                             1/sd, as setgeno over that subset computes them, FIT.cpp:376-385,
                             436-495), applied through the genotype matrix (0/1/2 in BF16, exact)
                             with two tcgen05 GEMMs of two BF16 products each; needs no sg_grm_build.
-                            The other engines restrict the cohort GRM to the subset instead */
+                            The other engines restrict the cohort GRM to the subset instead */,
+  SG_MV_SUBSET_EXACT_F8 = 6 /* the subset-exact engine with FP16 high halves (kind::f16) and E4M3
+                            low halves (kind::f8f6f4, twice the FP16 rate) of each column scaled
+                            by a power of two: 15 significant bits, three quarters of the tensor
+                            work; G is held in FP16 and in E4M3 (1.5 times the bytes) */
 };
 
 /* ------------------------------------------------------------ context */

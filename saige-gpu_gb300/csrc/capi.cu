@@ -172,6 +172,8 @@ struct Engine {
   void* Tb = nullptr;             // T' halves: cap_cols x mg BF16, high then low
   float* Um = nullptr;            // U = G T': cap_cols x np
   double* spart = nullptr;        // column partials: cap_cols x max(blocks over np, over mg)
+  float* smax = nullptr;          // FP16 / E4M3 form: column block maxima, as spart
+  float* sscale = nullptr;        //   and the columns' power-of-two scales s1, s2 (2 x cap_cols)
   float* sdiag_part = nullptr;    // per-chunk partial sums of a subset's diagonal (slot set-up)
 
 };
@@ -243,7 +245,8 @@ struct sg_ctx {
   int qc_is_var_ratio = 0;
   // subset-exact engine: genotype values 0/1/2 (cohort fill in missing calls) in BF16, marker-major
   // (mg x np) then sample-major (np x mg), mg = .bim markers rounded up to 128
-  void* d_G = nullptr;
+  void* d_G = nullptr;   // genotype matrix: BF16 (form 0) or FP16 then E4M3 (form 1), both layouts each
+  int g_form = 0;
   int64_t mg = 0;
   // synthetic bed image
   uint8_t* d_synth = nullptr;
@@ -429,38 +432,41 @@ static int ensure_k_split(sg_ctx* c, bool want);
 static int ensure_k_bf16(sg_ctx* c, bool want);
 static void engine_free(sg_ctx* c);
 
-static int ensure_g(sg_ctx* c);
+static int ensure_g(sg_ctx* c, int form);
+
+// the subset-exact engines (BF16 products, or FP16 high / E4M3 low)
+static bool exact_mode(int mode) { return mode == SG_MV_SUBSET_EXACT || mode == SG_MV_SUBSET_EXACT_F8; }
 
 extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
   if (!c) return SG_ERR_INVALID;
   if (mode != SG_MV_FP32_SIMT && mode != SG_MV_TF32_TC && mode != SG_MV_FP64_PLAIN &&
-      mode != SG_MV_TF32X3_TC && mode != SG_MV_BF16X3_TC && mode != SG_MV_SUBSET_EXACT)
+      mode != SG_MV_TF32X3_TC && mode != SG_MV_BF16X3_TC && !exact_mode(mode))
     return set_err(c, SG_ERR_INVALID, "unknown matvec mode %d", mode);
-  if ((mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC || mode == SG_MV_SUBSET_EXACT) &&
+  if ((mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC || exact_mode(mode)) &&
       !tc_available())
     return set_err(c, SG_ERR_INVALID, "tcgen05 path needs an sm_103a device");
   if (c->eng.inflight) return set_err(c, SG_ERR_STATE, "a step is in flight: finish it first");
-  if (mode == SG_MV_SUBSET_EXACT) {
+  if (exact_mode(mode)) {
     if (!c->have_geno) return set_err(c, SG_ERR_STATE, "setgeno has not run");
     if (c->loco) return set_err(c, SG_ERR_STATE, "clear the LOCO range first (sg_loco_clear)");
     for (auto& kv : c->eng.reqs)
       if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");
   }
-  const bool was_exact = c->mv_mode == SG_MV_SUBSET_EXACT;
+  const bool was_exact = exact_mode(c->mv_mode);
   c->mv_mode = mode;
   // a slot's subset state and preconditioner belong to the engine they were set for: entering or
-  // leaving the subset-exact engine asks for every slot to be set again
-  if (was_exact != (mode == SG_MV_SUBSET_EXACT)) {
+  // leaving the subset-exact engines asks for every slot to be set again (the two forms share it)
+  if (was_exact != exact_mode(mode)) {
     for (auto& ss : c->eng.sub) {
       if (ss.prep) cudaEventSynchronize(ss.ev_prep);
       ss.valid = ss.prep = false;
     }
     std::fill(c->eng.ph_set.begin(), c->eng.ph_set.end(), 0);
   }
-  if (mode == SG_MV_SUBSET_EXACT) {
+  if (exact_mode(mode)) {
     SG_TRY(ensure_k_split(c, false));
     SG_TRY(ensure_k_bf16(c, false));
-    return ensure_g(c);
+    return ensure_g(c, mode == SG_MV_SUBSET_EXACT_F8 ? 1 : 0);
   }
   if (was_exact) {  // the genotype matrix (2 bytes per sample and marker, twice) leaves HBM
     SG_TRY(sync(c));
@@ -472,9 +478,15 @@ extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
   return ensure_k_bf16(c, mode == SG_MV_BF16X3_TC);
 }
 
-// Genotype values of every .bim marker for the subset-exact engine, in BF16 (exact), both layouts.
-static int ensure_g(sg_ctx* c) {
-  if (c->d_G) return SG_OK;
+// Genotype values of every .bim marker for the subset-exact engines, both layouts: in BF16 (form 0),
+// or in FP16 and in E4M3 (form 1); all exact.
+static int ensure_g(sg_ctx* c, int form) {
+  if (c->d_G && c->g_form == form) return SG_OK;
+  if (c->d_G) {  // the other form's matrix leaves HBM first
+    SG_TRY(sync(c));
+    dev_free(c, c->d_G);
+    c->d_G = nullptr;
+  }
   const int64_t np = round_up(c->nn, kRowTile), mg = round_up(std::max<int64_t>(c->m_bim, 1), kRowTile);
   if (c->have_grm && c->np != np) return set_err(c, SG_ERR_STATE, "GRM row padding differs");
   if (!c->have_grm) {
@@ -483,12 +495,15 @@ static int ensure_g(sg_ctx* c) {
   }
   // the cohort fill stays on the device beside G: each subset's set-up compares its own fill with it
   if (!c->d_fill_all) SG_TRY(dev_alloc_t(c, &c->d_fill_all, (size_t)std::max<int64_t>(c->m_bim, 1)));
-  SG_TRY(dev_alloc(c, &c->d_G, (size_t)(2 * mg * np * 2)));
+  SG_TRY(dev_alloc(c, &c->d_G, (size_t)(2 * mg * np * (form ? 3 : 2))));
+  c->g_form = form;
   if (c->m_bim)
     SG_CUDA(c, cudaMemcpyAsync(c->d_fill_all, c->fill_all.data(), c->m_bim * 4, cudaMemcpyHostToDevice, c->stream));
   SG_CUDA(c, cudaEventRecord(c->tev[0], c->stream));
-  launch_gbuild(c->d_codes, c->pitch, c->d_fill_all, c->m_bim, c->nn, mg, np, c->d_G,
-                static_cast<uint16_t*>(c->d_G) + mg * np, c->stream);
+  uint16_t* g16 = static_cast<uint16_t*>(c->d_G);
+  uint8_t* g8 = reinterpret_cast<uint8_t*>(g16 + 2 * mg * np);
+  launch_gbuild(c->d_codes, c->pitch, c->d_fill_all, c->m_bim, c->nn, mg, np, form, g16, g16 + mg * np,
+                form ? g8 : nullptr, form ? g8 + mg * np : nullptr, c->stream);
   SG_LAUNCHED(c, 1);
   SG_CUDA(c, cudaEventRecord(c->tev[1], c->stream));
   SG_TRY(sync(c));
@@ -851,7 +866,7 @@ extern "C" int sg_setgeno_files(sg_ctx* c, const char* bed_path, const char* bim
 #define NEED_OPERATOR(c)                                                                               \
   do {                                                                                                 \
     NEED_GENO(c);                                                                                      \
-    if (!(c)->have_grm && !((c)->mv_mode == SG_MV_SUBSET_EXACT && (c)->d_G))                            \
+    if (!(c)->have_grm && !(exact_mode((c)->mv_mode) && (c)->d_G))                                      \
       return set_err((c), SG_ERR_STATE, "sg_grm_build has not run (or select SG_MV_SUBSET_EXACT)");    \
   } while (0)
 
@@ -1125,6 +1140,8 @@ static void engine_free(sg_ctx* c) {
   e.Tb = nullptr;
   dev_free_t(c, e.Um);
   dev_free_t(c, e.spart);
+  dev_free_t(c, e.smax);
+  dev_free_t(c, e.sscale);
   dev_free_t(c, e.sdiag_part);
 
   e.dots_cap_sx = e.dots_cap_part = e.dots_cap_cols = 0;
@@ -1407,7 +1424,7 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
 extern "C" int sg_engine_prepare_subset(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   NEED_OPERATOR(c);
   Engine& e = c->eng;
-  if (c->mv_mode != SG_MV_SUBSET_EXACT) return SG_OK;  // the other engines keep no subset state
+  if (!exact_mode(c->mv_mode)) return SG_OK;  // the other engines keep no subset state
   if (e.cap_ph == 0) SG_TRY(engine_reserve(c, 128, std::max<int64_t>(slot + 1, 1)));
   if (slot < 0 || slot >= e.cap_ph) return set_err(c, SG_ERR_INVALID, "phenotype slot %lld out of range", (long long)slot);
   for (auto& kv : e.reqs)
@@ -1483,7 +1500,7 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     if (mask) SG_CUDA(c, h2d(c, dm, hm, c->nn, c->side));
     const double* diag = loco ? c->d_diag_loco : c->d_diag;
     double mm = m;
-    if (c->mv_mode == SG_MV_SUBSET_EXACT) {  // the subset's own diagonal and GRM marker count
+    if (exact_mode(c->mv_mode)) {  // the subset's own diagonal and GRM marker count
       SG_TRY(subset_setup(c, slot, mask, mask ? dm : nullptr));
       diag = e.sub[slot].diag;
       mm = e.sub[slot].m_prime;
@@ -1875,7 +1892,7 @@ static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf, int64_t* la
     c->launches += 1;
     return SG_OK;
   }
-  if (c->mv_mode == SG_MV_SUBSET_EXACT) {
+  if (exact_mode(c->mv_mode)) {
     // K_S P per column's own sample subset, through the genotype matrix (k_subset.cu)
     const int64_t nact = e.nact;
     if (nact == 0) {
@@ -1898,6 +1915,32 @@ static int engine_gemm_full(sg_ctx* c, int64_t ncols, bool* used_yf, int64_t* la
     uint16_t* tl = th + cap * mg;
     const uint16_t* Gmm = static_cast<const uint16_t*>(c->d_G);
     const uint16_t* Gsm = Gmm + mg * np;
+    if (c->mv_mode == SG_MV_SUBSET_EXACT_F8) {
+      // FP16 high halves (2 bytes) then E4M3 low halves (1 byte) in the same buffers
+      const size_t nb = (size_t)std::max(subset_nblk(np), subset_nblk(mg));
+      if (!e.smax) SG_TRY(dev_alloc_t(c, &e.smax, cap * nb));
+      if (!e.sscale) SG_TRY(dev_alloc_t(c, &e.sscale, 2 * cap));
+      uint8_t* vl8 = reinterpret_cast<uint8_t*>(vh + cap * np);
+      uint8_t* tl8 = reinterpret_cast<uint8_t*>(th + cap * mg);
+      const uint8_t* Gmm8 = reinterpret_cast<const uint8_t*>(Gmm + 2 * mg * np);
+      const uint8_t* Gsm8 = Gmm8 + mg * np;
+      launch_subset_prepare_f8(e.Pf, np, e.d_gcols, npad, e.d_st, e.d_slots, e.winv, e.spart, e.smax, vh, vl8,
+                               e.sscale, c->stream);
+      c->launches += 2;
+      cudaError_t err = tc_gemm_splitb8(Gmm, Gmm8, mg, np, vh, vl8, npad, e.Tm, mg, c->stream, false, 0);
+      if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 genotype GEMM (G'V): %s", cudaGetErrorString(err));
+      launch_subset_scale_f8(vh, vl8, np, c->nn, e.d_gcols, npad, e.d_st, e.d_slots, e.max_w, e.Tm, mg, th, tl8,
+                             e.spart, e.smax, e.sscale, (int64_t)cap, c->stream);
+      c->launches += e.max_w > 0 ? 4 : 3;
+      err = tc_gemm_splitb8(Gsm, Gsm8, np, mg, th, tl8, npad, e.Um, np, c->stream, false, 1);
+      if (err != cudaSuccess) return set_err(c, SG_ERR_CUDA, "tcgen05 genotype GEMM (G T'): %s", cudaGetErrorString(err));
+      launch_subset_finalize_f8(e.Um, np, c->nn, e.d_gcols, npad, e.d_st, e.d_slots, th, tl8, mg, e.sscale + cap,
+                                e.spart, e.winv, e.Yf, c->stream);
+      c->launches += 2;
+      SG_LAUNCHED(c, 0);
+      *launched = npad;
+      return SG_OK;
+    }
     launch_subset_prepare(e.Pf, np, e.d_gcols, npad, e.d_st, e.d_slots, e.winv, e.spart, vh, vl, c->stream);
     c->launches += 2;
     cudaError_t err = tc_gemm_splitb(Gmm, mg, np, vh, vl, npad, e.Tm, mg, c->stream, false, 0);
@@ -1939,10 +1982,10 @@ static int release_col(sg_ctx* c, int64_t col);
 // Columns the GRM.V of one step covers: [0, hi_col) padded to the kernel's column tile (the
 // padding columns are free or finished, their P rows are zero).
 static bool tc_mode(int mode) {
-  return mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC || mode == SG_MV_SUBSET_EXACT;
+  return mode == SG_MV_TF32_TC || mode == SG_MV_TF32X3_TC || mode == SG_MV_BF16X3_TC || exact_mode(mode);
 }
 // engines that gather the step's active columns into a compact block themselves
-static bool compact_mode(int mode) { return mode == SG_MV_BF16X3_TC || mode == SG_MV_SUBSET_EXACT; }
+static bool compact_mode(int mode) { return mode == SG_MV_BF16X3_TC || exact_mode(mode); }
 
 static int64_t engine_gemm_cols(const sg_ctx* c) {
   const Engine& e = c->eng;
@@ -2568,7 +2611,7 @@ extern "C" int sg_loco_set(sg_ctx* c, int64_t begin, int64_t end) {
     return set_err(c, SG_ERR_INVALID, "LOCO range [%lld, %lld] outside the %lld GRM markers", (long long)begin,
                    (long long)end, (long long)c->m_qc);
   if (end - begin + 1 >= c->m_qc) return set_err(c, SG_ERR_INVALID, "LOCO range covers every GRM marker");
-  if (c->mv_mode == SG_MV_SUBSET_EXACT)
+  if (exact_mode(c->mv_mode))
     return set_err(c, SG_ERR_STATE, "LOCO runs on the resident GRM: select another engine first");
   for (auto& kv : c->eng.reqs)
     if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");

@@ -18,6 +18,8 @@
 // other columns share the step.
 #include "sg_internal.h"
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
 
 namespace sg {
 
@@ -41,16 +43,56 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return s;
 }
 
+__device__ __forceinline__ float block_max(float v, float* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  float s = 0.0f;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s = fmaxf(s, sh[i]);
+  __syncthreads();
+  return s;
+}
+
+// FP16-high / E4M3-low halves.  A column is multiplied by a power of two that brings its largest
+// magnitude (bounded by ``bound``) into [2^14, 2^15): FP16 keeps 11 significant bits of it without
+// overflow, and the low half (at most 8 in magnitude) sits in E4M3's normal range for every entry
+// within 2^-10 of the largest.  The scale is exact, and is divided out after the GEMM.
+__device__ __forceinline__ float pow2_scale(float bound) {
+  if (!(bound > 0.0f) || !(bound < 3.0e38f)) return 1.0f;
+  int e = 0;
+  frexpf(bound, &e);  // bound = f 2^e, f in [0.5, 1)
+  return ldexpf(1.0f, min(15 - e, 100));
+}
+__device__ __forceinline__ void split_f8(float x, __half& h, uint8_t& l) {
+  h = __float2half_rn(x);
+  l = (uint8_t)__nv_cvt_float_to_fp8(x - __half2float(h), __NV_SATFINITE, __NV_E4M3);
+}
+__device__ __forceinline__ float e4m3_value(uint8_t l) {
+  return __half2float(__half(__nv_cvt_fp8_to_halfraw((__nv_fp8_storage_t)l, __NV_E4M3)));
+}
+// h + l is exact in FP32 (at most 15 significant bits)
+__device__ __forceinline__ float join_f8(__half h, uint8_t l) { return __half2float(h) + e4m3_value(l); }
+
 }  // namespace
 
 // ----------------------------------------------------------------------------------- set-up
+// Genotype value g (0, 1, 2) as the bit pattern of each operand type (exact in all of them).
+__device__ __forceinline__ uint16_t g_bf16(int g) { return g == 0 ? 0x0000u : g == 1 ? 0x3F80u : 0x4000u; }
+__device__ __forceinline__ uint16_t g_f16(int g) { return g == 0 ? 0x0000u : g == 1 ? 0x3C00u : 0x4000u; }
+__device__ __forceinline__ uint8_t g_e4m3(int g) { return g == 0 ? 0x00u : g == 1 ? 0x38u : 0x40u; }
+
 // G in both layouts from the cohort's packed codes (missing calls kept as 01): block = 64 markers x
 // 128 samples staged through shared memory, written coalesced along samples (marker-major G_mm,
 // mg x np) and along markers (sample-major G_sm, np x mg).  Missing calls take the cohort fill;
 // rows and columns past m and nn are zero.
+// form 0: BF16 G in both layouts (Gmm16, Gsm16 hold BF16 bits); form 1: FP16 G in both layouts and
+// E4M3 G in both layouts (Gmm8, Gsm8), for the FP16-high / E4M3-low products.
 __global__ void gbuild_kernel(const uint8_t* __restrict__ codes, int64_t pitch, const int32_t* __restrict__ fill,
-                              int64_t m, int64_t nn, int64_t mg, int64_t np, __nv_bfloat16* __restrict__ Gmm,
-                              __nv_bfloat16* __restrict__ Gsm) {
+                              int64_t m, int64_t nn, int64_t mg, int64_t np, int form, uint16_t* __restrict__ Gmm16,
+                              uint16_t* __restrict__ Gsm16, uint8_t* __restrict__ Gmm8, uint8_t* __restrict__ Gsm8) {
   __shared__ uint8_t sval[64][128 + 2];
   const int64_t m0 = (int64_t)blockIdx.x * 64;
   const int64_t s0 = (int64_t)blockIdx.y * 128;
@@ -64,20 +106,25 @@ __global__ void gbuild_kernel(const uint8_t* __restrict__ codes, int64_t pitch, 
       g = (uint8_t)(f == 1u ? fill[mk] : field_geno(f));
     }
     sval[mm][s] = g;
-    Gmm[mk * np + smp] = __float2bfloat16_rn((float)g);
+    Gmm16[mk * np + smp] = form ? g_f16(g) : g_bf16(g);
+    if (form) Gmm8[mk * np + smp] = g_e4m3(g);
   }
   __syncthreads();
   for (int e = tid; e < 64 * 128; e += blockDim.x) {
     const int mm = e & 63, s = e >> 6;
-    Gsm[(s0 + s) * mg + m0 + mm] = __float2bfloat16_rn((float)sval[mm][s]);
+    const int g = sval[mm][s];
+    Gsm16[(s0 + s) * mg + m0 + mm] = form ? g_f16(g) : g_bf16(g);
+    if (form) Gsm8[(s0 + s) * mg + m0 + mm] = g_e4m3(g);
   }
 }
 
 void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int64_t m, int64_t nn,
-                   int64_t mg, int64_t np, void* Gmm, void* Gsm, cudaStream_t s) {
+                   int64_t mg, int64_t np, int form, void* Gmm16, void* Gsm16, void* Gmm8, void* Gsm8,
+                   cudaStream_t s) {
   dim3 grid((unsigned)(mg / 64), (unsigned)(np / 128));
-  gbuild_kernel<<<grid, kThreads, 0, s>>>(codes, pitch, fill, m, nn, mg, np, static_cast<__nv_bfloat16*>(Gmm),
-                                          static_cast<__nv_bfloat16*>(Gsm));
+  gbuild_kernel<<<grid, kThreads, 0, s>>>(codes, pitch, fill, m, nn, mg, np, form, static_cast<uint16_t*>(Gmm16),
+                                          static_cast<uint16_t*>(Gsm16), static_cast<uint8_t*>(Gmm8),
+                                          static_cast<uint8_t*>(Gsm8));
 }
 
 // A subset's GRM tables from its per-marker QC records, as setgeno over the subset builds them
@@ -302,19 +349,28 @@ void launch_subset_diag(const uint8_t* codes, int64_t pitch, const float* lut4, 
 // partials in FP64, in a fixed order.
 //
 // Column sums over the subset (rows outside S are zero in P): block partials, kChunk rows each.
+// With pmax, also the block's max |P| (the FP16 form scales each column by a power of two).
 __global__ void subset_colsum_kernel(const float* __restrict__ Pf, int64_t np, const int32_t* __restrict__ cols,
-                                     double* __restrict__ part, int nblk) {
+                                     double* __restrict__ part, float* __restrict__ pmax, int nblk) {
   __shared__ double sh[kThreads / 32];
+  __shared__ float shm[kThreads / 32];
   const int64_t j = blockIdx.y;
   const int32_t col = cols[j];
   const int64_t i0 = (int64_t)blockIdx.x * kChunk;
-  float v = 0.0f;
+  float v = 0.0f, mx = 0.0f;
   if (col >= 0) {
     const float* p = Pf + (int64_t)col * np;
-    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) v += p[i];
+    for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
+      v += p[i];
+      mx = fmaxf(mx, fabsf(p[i]));
+    }
   }
   const double vd = block_sum((double)v, sh);
   if (threadIdx.x == 0) part[j * nblk + blockIdx.x] = vd;
+  if (pmax) {
+    const float bm = block_max(mx, shm);
+    if (threadIdx.x == 0) pmax[j * nblk + blockIdx.x] = bm;
+  }
 }
 
 // v_c = P - mean_S(P) on the subset (0 elsewhere and for padding columns), as BF16 high + low
@@ -496,12 +552,261 @@ subset_finalize_kernel(const float* __restrict__ U, int64_t np, int64_t nn, cons
 
 int subset_nblk(int64_t n) { return (int)((n + kChunk - 1) / kChunk); }
 
+// ------------------------------------------------------- FP16-high / E4M3-low form of the same step
+// The same data flow with per-column power-of-two scales: v_c s1 is split into FP16 + E4M3 halves;
+// GEMM 1 gives T s1; T' s2 = d' T s1 (s2 / s1) is split the same way; GEMM 2 gives U s2, and the
+// finalize divides s2 out.  scale[j] = s1, scale[cap + j] = s2 of compact column j.
+
+__global__ void subset_center_split_f8_kernel(const float* __restrict__ Pf, int64_t np, const int32_t* __restrict__ cols,
+                                              const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
+                                              const double* __restrict__ winv, const double* __restrict__ part,
+                                              const float* __restrict__ pmax, int nblk, __half* __restrict__ Vh,
+                                              uint8_t* __restrict__ Vl, float* __restrict__ scale) {
+  __shared__ float s_mu, s_sc;
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk;
+  int slot = 0;
+  if (col >= 0) slot = st[col].pheno;
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    float mx = 0.0f;
+    if (col >= 0)
+      for (int b = 0; b < nblk; ++b) {
+        sum += part[j * nblk + b];
+        mx = fmaxf(mx, pmax[j * nblk + b]);
+      }
+    const float mu = col >= 0 ? (float)(sum / slots[slot].ns) : 0.0f;
+    s_mu = mu;
+    s_sc = pow2_scale(mx + fabsf(mu));  // bounds |P - mu| over the column
+    if (blockIdx.x == 0) scale[j] = s_sc;
+  }
+  __syncthreads();
+  const float mu = s_mu, sc = s_sc;
+  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < np; i += kThreads) {
+    float v = 0.0f;
+    if (col >= 0 && winv[(int64_t)slot * np + i] != 0.0) v = (Pf[(int64_t)col * np + i] - mu) * sc;
+    __half h;
+    uint8_t l;
+    split_f8(v, h, l);
+    Vh[j * np + i] = h;
+    Vl[j * np + i] = l;
+  }
+}
+
+// Fill-change corrections of T s1 (as subset_flip_t_kernel, over the scaled halves).
+__global__ void subset_flip_t_f8_kernel(const __half* __restrict__ Vh, const uint8_t* __restrict__ Vl, int64_t np,
+                                        int64_t nn, const int32_t* __restrict__ cols, const ColState* __restrict__ st,
+                                        const SubsetSlot* __restrict__ slots, float* __restrict__ T, int64_t mg) {
+  __shared__ float red[kThreads / 32][32];
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  if (col < 0) return;
+  const SubsetSlot sl = slots[st[col].pheno];
+  const int w = blockIdx.x;
+  if (w >= sl.W) return;
+  float acc[32];
+#pragma unroll
+  for (int b = 0; b < 32; ++b) acc[b] = 0.0f;
+  const uint32_t* bw = sl.bits + (int64_t)w * np;
+  for (int64_t i = threadIdx.x; i < nn; i += kThreads) {
+    const uint32_t word = bw[i];
+    if (word == 0u) continue;
+    const float v = join_f8(Vh[j * np + i], Vl[j * np + i]);
+#pragma unroll
+    for (int b = 0; b < 32; ++b)
+      if ((word >> b) & 1u) acc[b] += v;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int b = 0; b < 32; ++b) {
+    float x = acc[b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == b) red[warp][b] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int b = threadIdx.x;
+    const int k = 32 * w + b;
+    if (k < sl.nflip) {
+      float s = 0.0f;
+      for (int q = 0; q < kThreads / 32; ++q) s += red[q][b];
+      T[j * mg + sl.flips[k]] += sl.dfill[k] * s;
+    }
+  }
+}
+
+// Block maxima of |d' T s1| (for s2).
+__global__ void subset_tmax_kernel(const float* __restrict__ T, int64_t mg, const int32_t* __restrict__ cols,
+                                   const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
+                                   float* __restrict__ pmax, int nblk) {
+  __shared__ float shm[kThreads / 32];
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  const int64_t m0 = (int64_t)blockIdx.x * kChunk;
+  float mx = 0.0f;
+  if (col >= 0) {
+    const SubsetSlot* sl = &slots[st[col].pheno];
+    for (int64_t mk = m0 + threadIdx.x; mk < m0 + kChunk && mk < mg; mk += kThreads)
+      mx = fmaxf(mx, fabsf(sl->dprime[mk] * T[j * mg + mk]));
+  }
+  const float bm = block_max(mx, shm);
+  if (threadIdx.x == 0) pmax[j * nblk + blockIdx.x] = bm;
+}
+
+// T' s2 = d' (T s1) (s2 / s1) as FP16 + E4M3 halves, and the block partials of (2p')^T T'.
+__global__ void subset_scale_split_f8_kernel(const float* __restrict__ T, int64_t mg, const int32_t* __restrict__ cols,
+                                             const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
+                                             const float* __restrict__ pmax, float* __restrict__ scale, int64_t cap,
+                                             __half* __restrict__ Th, uint8_t* __restrict__ Tl,
+                                             double* __restrict__ part, int nblk) {
+  __shared__ double sh[kThreads / 32];
+  __shared__ float s_ratio, s_inv2;
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  const int64_t m0 = (int64_t)blockIdx.x * kChunk;
+  const SubsetSlot* sl = col >= 0 ? &slots[st[col].pheno] : nullptr;
+  if (threadIdx.x == 0) {
+    float mx = 0.0f;
+    for (int b = 0; b < nblk; ++b) mx = fmaxf(mx, pmax[j * nblk + b]);
+    const float s1 = scale[j];
+    const float s2 = pow2_scale(mx / s1);
+    s_ratio = s2 / s1;
+    s_inv2 = 1.0f / s2;
+    if (blockIdx.x == 0) scale[cap + j] = s2;
+  }
+  __syncthreads();
+  const float ratio = s_ratio;
+  float cf = 0.0f;
+  for (int64_t mk = m0 + threadIdx.x; mk < m0 + kChunk && mk < mg; mk += kThreads) {
+    float t = 0.0f;
+    if (sl) t = sl->dprime[mk] * T[j * mg + mk] * ratio;
+    __half h;
+    uint8_t l;
+    split_f8(t, h, l);
+    Th[j * mg + mk] = h;
+    Tl[j * mg + mk] = l;
+    if (sl) cf = fmaf(sl->p2[mk], join_f8(h, l), cf);
+  }
+  const double c = block_sum((double)cf, sh);
+  if (threadIdx.x == 0) part[j * nblk + blockIdx.x] = c * (double)s_inv2;
+}
+
+__global__ void __launch_bounds__(kThreads)
+subset_finalize_f8_kernel(const float* __restrict__ U, int64_t np, int64_t nn, const int32_t* __restrict__ cols,
+                          const ColState* __restrict__ st, const SubsetSlot* __restrict__ slots,
+                          const __half* __restrict__ Th, const uint8_t* __restrict__ Tl, int64_t mg,
+                          const float* __restrict__ scale2, const double* __restrict__ part, int nblk,
+                          const double* __restrict__ winv, float* __restrict__ Yf) {
+  __shared__ double s_c;
+  __shared__ float tf[kFinF];
+  const int64_t j = blockIdx.y;
+  const int32_t col = cols[j];
+  if (col < 0) return;
+  const int slot = st[col].pheno;
+  const SubsetSlot sl = slots[slot];
+  if (threadIdx.x == 0) {
+    double c = 0.0;
+    for (int b = 0; b < nblk; ++b) c += part[j * nblk + b];
+    s_c = c;
+  }
+  const float inv2 = 1.0f / scale2[j];
+  const int64_t i0 = (int64_t)blockIdx.x * kChunk + threadIdx.x;
+  unsigned live = 0u;
+#pragma unroll
+  for (int r = 0; r < kFinPer; ++r) {
+    const int64_t i = i0 + (int64_t)r * kThreads;
+    if (i < nn && winv[(int64_t)slot * np + i] != 0.0) live |= 1u << r;
+  }
+  float du[kFinPer];
+#pragma unroll
+  for (int r = 0; r < kFinPer; ++r) du[r] = 0.0f;
+  const __half* th = Th + j * mg;
+  const uint8_t* tl = Tl + j * mg;
+  for (int f0 = 0; f0 < sl.nflip; f0 += kFinF) {
+    const int fn = sl.nflip - f0 < kFinF ? sl.nflip - f0 : kFinF;
+    __syncthreads();
+    for (int k = threadIdx.x; k < fn; k += kThreads) {
+      const int64_t mk = sl.flips[f0 + k];
+      tf[k] = sl.dfill[f0 + k] * (join_f8(th[mk], tl[mk]) * inv2);
+    }
+    __syncthreads();
+    const int w0 = f0 / 32, wn = (fn + 31) / 32;
+#pragma unroll
+    for (int r = 0; r < kFinPer; ++r) {
+      if (!((live >> r) & 1u)) continue;
+      const uint32_t* bw = sl.bits + (int64_t)w0 * np + i0 + (int64_t)r * kThreads;
+      float d = du[r];
+      for (int w = 0; w < wn; ++w) {
+        uint32_t word = bw[(int64_t)w * np];
+        while (word) {
+          const int b = __ffs(word) - 1;
+          word &= word - 1u;
+          d += tf[32 * w + b];
+        }
+      }
+      du[r] = d;
+    }
+  }
+  __syncthreads();
+  const float cf = (float)s_c, inv_mf = (float)sl.inv_m;
+#pragma unroll
+  for (int r = 0; r < kFinPer; ++r) {
+    const int64_t i = i0 + (int64_t)r * kThreads;
+    if (i >= np) break;
+    float y = 0.0f;
+    if ((live >> r) & 1u) y = (U[j * np + i] * inv2 - cf + du[r]) * inv_mf;
+    Yf[(int64_t)col * np + i] = y;
+  }
+}
+
+void launch_subset_prepare_f8(const float* Pf, int64_t np, const int32_t* cols, int64_t ncols, const ColState* st,
+                              const SubsetSlot* slots, const double* winv, double* part, float* pmax, void* Vh,
+                              void* Vl, float* scale, cudaStream_t s) {
+  const int nblk = subset_nblk(np);
+  dim3 grid((unsigned)nblk, (unsigned)ncols);
+  subset_colsum_kernel<<<grid, kThreads, 0, s>>>(Pf, np, cols, part, pmax, nblk);
+  subset_center_split_f8_kernel<<<grid, kThreads, 0, s>>>(Pf, np, cols, st, slots, winv, part, pmax, nblk,
+                                                          static_cast<__half*>(Vh), static_cast<uint8_t*>(Vl),
+                                                          scale);
+}
+
+void launch_subset_scale_f8(const void* Vh, const void* Vl, int64_t np, int64_t nn, const int32_t* cols,
+                            int64_t ncols, const ColState* st, const SubsetSlot* slots, int max_w, float* T,
+                            int64_t mg, void* Th, void* Tl, double* part, float* pmax, float* scale, int64_t cap,
+                            cudaStream_t s) {
+  if (max_w > 0) {
+    dim3 g1((unsigned)max_w, (unsigned)ncols);
+    subset_flip_t_f8_kernel<<<g1, kThreads, 0, s>>>(static_cast<const __half*>(Vh), static_cast<const uint8_t*>(Vl),
+                                                    np, nn, cols, st, slots, T, mg);
+  }
+  const int nblk = subset_nblk(mg);
+  dim3 g2((unsigned)nblk, (unsigned)ncols);
+  subset_tmax_kernel<<<g2, kThreads, 0, s>>>(T, mg, cols, st, slots, pmax, nblk);
+  subset_scale_split_f8_kernel<<<g2, kThreads, 0, s>>>(T, mg, cols, st, slots, pmax, scale, cap,
+                                                       static_cast<__half*>(Th), static_cast<uint8_t*>(Tl), part,
+                                                       nblk);
+}
+
+void launch_subset_finalize_f8(const float* U, int64_t np, int64_t nn, const int32_t* cols, int64_t ncols,
+                               const ColState* st, const SubsetSlot* slots, const void* Th, const void* Tl,
+                               int64_t mg, const float* scale2, const double* part, const double* winv, float* Yf,
+                               cudaStream_t s) {
+  dim3 grid((unsigned)subset_nblk(np), (unsigned)ncols);
+  subset_finalize_f8_kernel<<<grid, kThreads, 0, s>>>(U, np, nn, cols, st, slots, static_cast<const __half*>(Th),
+                                                      static_cast<const uint8_t*>(Tl), mg, scale2, part,
+                                                      subset_nblk(mg), winv, Yf);
+}
+
+
+
 void launch_subset_prepare(const float* Pf, int64_t np, const int32_t* cols, int64_t ncols, const ColState* st,
                            const SubsetSlot* slots, const double* winv, double* part, void* Vh, void* Vl,
                            cudaStream_t s) {
   const int nblk = subset_nblk(np);
   dim3 grid((unsigned)nblk, (unsigned)ncols);
-  subset_colsum_kernel<<<grid, kThreads, 0, s>>>(Pf, np, cols, part, nblk);
+  subset_colsum_kernel<<<grid, kThreads, 0, s>>>(Pf, np, cols, part, nullptr, nblk);
   subset_center_split_kernel<<<grid, kThreads, 0, s>>>(Pf, np, cols, st, slots, winv, part, nblk,
                                                        static_cast<__nv_bfloat16*>(Vh),
                                                        static_cast<__nv_bfloat16*>(Vl));

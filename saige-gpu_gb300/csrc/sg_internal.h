@@ -210,8 +210,9 @@ struct SubsetSlot {
   double inv_m = 0.0;     // 1 / M' (the subset's GRM marker count)
   double ns = 1.0;        // subset size
 };
+// form 0: BF16 G (Gmm16, Gsm16); form 1: FP16 G (Gmm16, Gsm16) and E4M3 G (Gmm8, Gsm8)
 void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int64_t m, int64_t nn, int64_t mg,
-                   int64_t np, void* Gmm, void* Gsm, cudaStream_t s);
+                   int64_t np, int form, void* Gmm16, void* Gsm16, void* Gmm8, void* Gsm8, cudaStream_t s);
 // the subset's d', 2p', diagonal table, fill-change list and counts (nflip, M') from its QC records;
 // flag: mg bytes of scratch, flips / dfill: room for m entries, counts: 2 int64 on the device
 void launch_subset_derive(const MarkerQC* qc, const int32_t* fill_all, int64_t m, int64_t mg, float* dp, float* p2,
@@ -235,6 +236,19 @@ void launch_subset_scale(const void* Vh, const void* Vl, int64_t np, int64_t nn,
 void launch_subset_finalize(const float* U, int64_t np, int64_t nn, const int32_t* cols, int64_t ncols,
                             const ColState* st, const SubsetSlot* slots, const void* Th, const void* Tl, int64_t mg,
                             const double* part, const double* winv, float* Yf, cudaStream_t s);
+// FP16-high / E4M3-low form of the same three steps; pmax: block maxima scratch (as part), scale:
+// 2 x cap floats (s1 of compact column j at j, s2 at cap + j)
+void launch_subset_prepare_f8(const float* Pf, int64_t np, const int32_t* cols, int64_t ncols, const ColState* st,
+                              const SubsetSlot* slots, const double* winv, double* part, float* pmax, void* Vh,
+                              void* Vl, float* scale, cudaStream_t s);
+void launch_subset_scale_f8(const void* Vh, const void* Vl, int64_t np, int64_t nn, const int32_t* cols,
+                            int64_t ncols, const ColState* st, const SubsetSlot* slots, int max_w, float* T,
+                            int64_t mg, void* Th, void* Tl, double* part, float* pmax, float* scale, int64_t cap,
+                            cudaStream_t s);
+void launch_subset_finalize_f8(const float* U, int64_t np, int64_t nn, const int32_t* cols, int64_t ncols,
+                               const ColState* st, const SubsetSlot* slots, const void* Th, const void* Tl,
+                               int64_t mg, const float* scale2, const double* part, const double* winv, float* Yf,
+                               cudaStream_t s);
 constexpr int kProbeDotsMaxP = 16;
 // Per probe j (vecs[j] = Sigma^-1 u_j and vecs[k+j] = K u_j, u masked by minv != 0):
 // block partials of [Au.Su, u.Su, Au.SX_q (q < p), SX_q.u (q < p)] -> part[(j*nblk + b)*(2+2p) + v]

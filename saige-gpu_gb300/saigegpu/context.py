@@ -13,6 +13,7 @@ from . import _lib as L
 
 GRM_FP32_SIMT, GRM_BF16_TC, GRM_BF16X3_TC = 0, 1, 2
 MV_FP32_SIMT, MV_TF32_TC, MV_FP64_PLAIN, MV_TF32X3_TC, MV_BF16X3_TC, MV_SUBSET_EXACT = 0, 1, 2, 3, 4, 5
+MV_SUBSET_EXACT_F8 = 6
 # tcgen05 GEMM shape options (enum sg_tc_option)
 TC_SYRK_PAIR, TC_GRMV_PAIR, TC_DRAIN_BYTES, TC_SYRK_GROUP, TC_GRMV_SLICE = 0, 1, 2, 3, 4
 TC_SUBSET_PAIR, TC_SUBSET_SLICE = 5, 6

@@ -21,7 +21,7 @@ import time
 
 import numpy as np
 
-from .context import GRM_BF16_TC, MV_BF16X3_TC, MV_SUBSET_EXACT, TC_SYRK_GROUP, TC_SYRK_PAIR
+from .context import GRM_BF16_TC, MV_BF16X3_TC, MV_SUBSET_EXACT, MV_SUBSET_EXACT_F8, TC_SYRK_GROUP, TC_SYRK_PAIR
 
 # launch widths the GRM.V table covers (columns after padding to a tile width)
 GRMV_BUCKETS = (32, 64, 96, 128, 160, 224, 320, 448, 640, 1024)
@@ -109,10 +109,13 @@ def time_subset(ctx, V, pair, slice_bytes, reps=2):
     return best
 
 
-def tune_subset(ctx, buckets=SUBSET_BUCKETS, variants=SUBSET_VARIANTS):
-    """Times every (pair, slice) variant of the subset-exact engine at every bucket width on the
-    resident cohort and installs the per-width plan; leaves the engine in MV_SUBSET_EXACT."""
-    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+def tune_subset(ctx, buckets=SUBSET_BUCKETS, variants=SUBSET_VARIANTS, mode=MV_SUBSET_EXACT):
+    """Times every (pair, slice) variant of the subset-exact engine ``mode`` at every bucket width on
+    the resident cohort and installs the per-width plan; leaves the engine in ``mode``.  The FP16 /
+    E4M3 form has 256-byte stages only, so only its CTA-pair choice is timed."""
+    ctx.set_matvec_mode(mode)
+    if mode == MV_SUBSET_EXACT_F8:
+        variants = tuple(v for v in variants if v[1] == 256)
     ctx.engine_reserve(max(buckets), 1)
     table, plan = {}, []
     rng = np.random.default_rng(0)

@@ -10,13 +10,15 @@ import numpy as np
 import pytest
 
 from oracle import aireml, plink
-from saigegpu import (MV_FP32_SIMT, MV_SUBSET_EXACT, TC_SUBSET_PAIR, TC_SUBSET_SLICE, native, prep, serve,
-                      synth)
+from saigegpu import (MV_FP32_SIMT, MV_SUBSET_EXACT, MV_SUBSET_EXACT_F8, TC_SUBSET_PAIR, TC_SUBSET_SLICE, native,
+                      prep, serve, synth)
 
 pytestmark = pytest.mark.gpu
 
 N, M = 1800, 4000
 DROPS = (0.05, 0.2, 0.4, 0.3)
+# BF16 high + low halves, and FP16 high + E4M3 low halves of power-of-two-scaled columns
+MODES = [MV_SUBSET_EXACT, MV_SUBSET_EXACT_F8]
 
 
 def _subset_grm(bed, mask):
@@ -64,13 +66,15 @@ def exact_cohort(gpu_ctx):
     return gpu_ctx, bed, g, cases
 
 
-def test_subset_exact_products_match_oracle(exact_cohort):
+@pytest.mark.parametrize("mode", MODES)
+def test_subset_exact_products_match_oracle(exact_cohort, mode):
     """Engine products K_S v (kind 1 columns) against the FP64 GRM built over each subset."""
     ctx, bed, _, cases = exact_cohort
     rng = np.random.default_rng(5)
-    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    ctx.set_matvec_mode(mode)
+    variants = ((0, 64), (1, 128), (2, 128), (0, 256), (1, 256)) if mode == MV_SUBSET_EXACT else ((0, 256), (1, 256))
     try:
-        for pair, sl in ((0, 64), (1, 128), (2, 128), (0, 256), (1, 256)):
+        for pair, sl in variants:
             ctx.set_tc_option(TC_SUBSET_PAIR, pair)
             ctx.set_tc_option(TC_SUBSET_SLICE, sl)
             ctx.engine_reserve(128, len(cases))
@@ -123,13 +127,14 @@ def test_subset_exact_variants_bit_identical(exact_cohort):
         ctx.set_matvec_mode(MV_FP32_SIMT)
 
 
-def test_subset_exact_fits_match_oracle_and_masked_error_is_bounded(exact_cohort):
+@pytest.mark.parametrize("mode", MODES)
+def test_subset_exact_fits_match_oracle_and_masked_error_is_bounded(exact_cohort, mode):
     """Native batched fits on the subset-exact engine: tau within 1e-4 of the FP64 oracle on the
     subset-built GRM (same probes).  The masked approximation (cohort GRM restricted to S) is
     measured against the same exact answer: at this N it is off by percent, far beyond 1e-4."""
     ctx, bed, g, cases = exact_cohort
     specs = [serve.FitSpec(f0, trait, mask=mask) for trait, mask, f0 in cases]
-    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    ctx.set_matvec_mode(mode)
     try:
         res, _ = native.fit_batch(ctx, specs, max_columns=256)
     finally:
@@ -152,10 +157,11 @@ def test_subset_exact_fits_match_oracle_and_masked_error_is_bounded(exact_cohort
     print("masked-vs-exact tau relative error per phenotype:", masked_err)
 
 
-def test_subset_exact_alone_equals_in_the_mix(exact_cohort):
+@pytest.mark.parametrize("mode", MODES)
+def test_subset_exact_alone_equals_in_the_mix(exact_cohort, mode):
     ctx, bed, g, cases = exact_cohort
     specs = [serve.FitSpec(f0, trait, mask=mask) for trait, mask, f0 in cases]
-    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    ctx.set_matvec_mode(mode)
     try:
         mix, _ = native.fit_batch(ctx, specs, max_columns=256)
         alone, _ = native.fit_batch(ctx, [specs[2]], max_columns=256)
@@ -164,12 +170,13 @@ def test_subset_exact_alone_equals_in_the_mix(exact_cohort):
     np.testing.assert_array_equal(alone[0]["theta"], mix[2]["theta"])
 
 
-def test_subset_exact_full_cohort_matches_cohort_grm(exact_cohort):
+@pytest.mark.parametrize("mode", MODES)
+def test_subset_exact_full_cohort_matches_cohort_grm(exact_cohort, mode):
     """No mask: the subset is the cohort, and the exact engine's product is the cohort K's."""
     ctx, bed, g, cases = exact_cohort
     grm = aireml.DenseGRM(g)
     V = np.random.default_rng(8).standard_normal((N, 40))
-    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    ctx.set_matvec_mode(mode)
     try:
         Y = ctx.grm_matmul(V)
     finally:
@@ -178,12 +185,13 @@ def test_subset_exact_full_cohort_matches_cohort_grm(exact_cohort):
     assert np.abs(Y - ref).max() / np.abs(ref).max() < 6e-5
 
 
-def test_subset_exact_forget_rebuilds_identically(exact_cohort):
+@pytest.mark.parametrize("mode", MODES)
+def test_subset_exact_forget_rebuilds_identically(exact_cohort, mode):
     """Forgetting the kept subset states makes the next set_pheno rebuild them (QC, tables, flip map
     and diagonal on the device); the products after the rebuild are bit-identical."""
     ctx, bed, _, cases = exact_cohort
     rng = np.random.default_rng(9)
-    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    ctx.set_matvec_mode(mode)
     try:
         ctx.engine_reserve(128, len(cases))
         Vs = []
@@ -206,4 +214,22 @@ def test_subset_exact_forget_rebuilds_identically(exact_cohort):
         for a, b in zip(first, again):
             np.testing.assert_array_equal(a, b)
     finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+
+
+def test_subset_exact_f8_variants_bit_identical(exact_cohort):
+    """The FP16 / E4M3 form on single CTAs and on CTA pairs gives the same products, bit for bit."""
+    ctx, bed, _, cases = exact_cohort
+    rng = np.random.default_rng(16)
+    ctx.set_matvec_mode(MV_SUBSET_EXACT_F8)
+    try:
+        for k in (1, 40, 150):
+            V = rng.standard_normal((N, k))
+            outs = []
+            for pair in (0, 1):
+                ctx.set_tc_option(TC_SUBSET_PAIR, pair)
+                outs.append(ctx.grm_matmul(V))
+            np.testing.assert_array_equal(outs[1], outs[0])
+    finally:
+        ctx.set_tc_option(TC_SUBSET_PAIR, 2)
         ctx.set_matvec_mode(MV_FP32_SIMT)

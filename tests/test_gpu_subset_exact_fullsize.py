@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 from oracle import plink
-from saigegpu import GRM_BF16X3_TC, MV_BF16X3_TC, MV_SUBSET_EXACT, Context
+from saigegpu import GRM_BF16X3_TC, MV_BF16X3_TC, MV_SUBSET_EXACT, MV_SUBSET_EXACT_F8, Context
 
 pytestmark = pytest.mark.gpu
 
@@ -113,6 +113,16 @@ def test_fullsize_subset_product_matches_setgeno_over_subset(two_paths):
     # rms here; 1.4e-5 rms for zero-mean vectors, and its fits' tau within 3e-5 of FP64 at this size)
     assert ex_max.max() < 2e-5 and ex_rms.max() < 2e-5, (ex_max, ex_rms)
     assert sp_max.max() < 1e-3 and sp_rms.max() < 2e-3, (sp_max, sp_rms)
+    # the FP16-high / E4M3-low form (15 significant bits of each scaled column)
+    whole.set_matvec_mode(MV_SUBSET_EXACT_F8)
+    try:
+        whole.engine_set_pheno(0, np.ones(N), np.array([1.0, 0.5]), mask)
+        Y8 = _run(whole, whole.engine_submit(0, 1, V))[S]
+    finally:
+        whole.set_matvec_mode(MV_SUBSET_EXACT)
+    f8_max, f8_rms = _errs(Y8, R64)
+    print("K_S v against FP64, FP16 / E4M3 form: max %s rms %s" % (f8_max, f8_rms))
+    assert f8_max.max() < 5e-5 and f8_rms.max() < 5e-5, (f8_max, f8_rms)
 
 
 def test_fullsize_subset_solve_matches_setgeno_over_subset(two_paths):
