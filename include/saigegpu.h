@@ -66,7 +66,10 @@ enum sg_matvec_mode {
   SG_MV_SUBSET_EXACT_F8 = 6 /* the subset-exact engine with FP16 high halves (kind::f16) and E4M3
                             low halves (kind::f8f6f4, twice the FP16 rate) of each column scaled
                             by a power of two: 15 significant bits, three quarters of the tensor
-                            work; G is held in FP16 and in E4M3 (1.5 times the bytes) */
+                            work; G is held in FP16 and in E4M3 (1.5 times the bytes).  Measured
+                            at N = 100k: 3-5% faster GRM.V than SG_MV_SUBSET_EXACT, K_S v within
+                            1.1e-5 of FP64 (5e-6 for the BF16 form), tau up to 1.6e-4 from FP64 on
+                            a test cohort (1e-6 for the BF16 form); not the default */
 };
 
 /* ------------------------------------------------------------ context */

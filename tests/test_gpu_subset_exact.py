@@ -146,7 +146,12 @@ def test_subset_exact_fits_match_oracle_and_masked_error_is_bounded(exact_cohort
         S = np.nonzero(mask)[0]
         fit = aireml.glmmkin_binary if trait == "binary" else aireml.glmmkin_quantitative
         ref = fit(_subset_grm(bed, mask), f0)
-        np.testing.assert_allclose(r["theta"], ref["theta"], rtol=1e-4)
+        # BF16 halves: tau within 1e-4 of FP64 (measured 1e-6 to 3e-6 here).  FP16 + E4M3 halves
+        # (15 significant bits at a column's top, fewer for entries far below it): measured up to
+        # 1.6e-4 on the first binary phenotype, so that form is held to 3e-4 and is not the default
+        rel = np.abs(np.asarray(r["theta"]) - ref["theta"]) / np.abs(ref["theta"])
+        print("mode %d %s: tau rel error %s" % (mode, trait, rel))
+        np.testing.assert_allclose(r["theta"], ref["theta"], rtol=1e-4 if mode == MV_SUBSET_EXACT else 3e-4)
         sub = aireml.DenseGRM.from_matrix(Kc.K[np.ix_(S, S)], Kc.m_qc, Kc.diag_sum[S])
         sub.probe_index = S
         approx = fit(sub, f0)
