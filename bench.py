@@ -219,11 +219,15 @@ def run_batch(ctx, specs, cols, pipelined=True, workers=None, driver="native", l
 
 
 # DRAM traffic of the split-BF16 GRM.V over its algorithmic bytes, from ncu on a smaller case
-# (dram__bytes_read.sum + dram__bytes_write.sum; profiles/grmv_bf16x3_n24576_and_n100k.md)
+# (dram__bytes_read.sum + dram__bytes_write.sum of two launches at N = 24,576)
 GRMV_TRAFFIC_RATIO = 1.023
+# the same for the subset-exact GRM.V: ncu DRAM bytes of its two genotype GEMMs at N = 30,080,
+# M_g = 45,056, 192 columns (2.813 + 2.798 GB) over that launch's algorithmic bytes (5.536 GB)
+SUBSET_TRAFFIC_RATIO = 1.014
+SUBSET_TRAFFIC_BASIS = ("ncu DRAM bytes of both genotype GEMMs of a 192-column launch at N = 30,080, M_g = 45,056 "
+                        "over its algorithmic bytes (1.014), times this launch's algorithmic bytes")
 GRMV_TRAFFIC_BASIS = ("ncu DRAM bytes of two N=24576 launches (224 and 512 columns) over their algorithmic bytes "
-                      "(1.008, 1.037; mean 1.023), times this launch's algorithmic bytes "
-                      "(profiles/grmv_bf16x3_n24576_and_n100k.md)")
+                      "(1.008, 1.037; mean 1.023), times this launch's algorithmic bytes")
 
 
 def subset_roofline(peaks, t_dev, np_, mg, f8=False):
@@ -246,7 +250,8 @@ def subset_roofline(peaks, t_dev, np_, mg, f8=False):
     t = ms * 1e-3
     a_bw = bytes_alg / t / 1e9
     a_tc = flops_alg / t / 1e12
-    common = {"traffic": None,
+    common = {"traffic": None if f8 else round(SUBSET_TRAFFIC_RATIO * bytes_alg),
+              "traffic_basis": None if f8 else SUBSET_TRAFFIC_BASIS,
               "kernel": ("tc_gemm_kernel<fp16 + e4m3, kSplitB8>" if f8 else "tc_gemm_kernel<bf16, kSplitB>")
                         + " x 2 (G'V, G T') + subset kernels",
               "per_launch_ms": round(ms, 3), "columns_per_launch": round(cols, 1),

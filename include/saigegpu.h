@@ -303,6 +303,13 @@ int sg_engine_forget_subsets(sg_ctx *ctx);
  * already holds that subset, and sg_engine_prepare_subset is one for the other engines.  No
  * reference counterpart. */
 int sg_engine_prepare_subset(sg_ctx *ctx, int64_t slot, const uint8_t *mask);
+/* A set-up slot's variance-ratio markers as setgeno over its subset selects them: up to cap .bim
+ * indices (marker order) and their MAC over the subset; *n gets the count.  And one .bim marker's
+ * genotypes (0/1/2) for every cohort sample with missing calls at the subset's fill
+ * (Get_OneSNP_Geno_forVarRatio over the subset).  Subset-exact engines only. */
+int sg_engine_subset_vr_markers(sg_ctx *ctx, int64_t slot, int32_t *bim_index, int32_t *mac, int64_t cap,
+                                int64_t *n);
+int sg_engine_subset_geno(sg_ctx *ctx, int64_t slot, int64_t marker, int32_t *out);
 int sg_engine_subset_wait(sg_ctx *ctx, int64_t slot);
 /* Queue k columns.  kind 0 = PCG solve of Sigma x = b, kind 1 = one GRM product K b.
  * ids[k] receives request ids. */

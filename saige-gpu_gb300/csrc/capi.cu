@@ -1447,6 +1447,55 @@ extern "C" int sg_engine_subset_wait(sg_ctx* c, int64_t slot) {
   return SG_OK;
 }
 
+// The variance-ratio markers of a slot's subset, as setgeno over the subset selects them (the random
+// draw's markers with MAC >= min over the subset, or the categorical ranges; FIT.cpp:497-547): their
+// .bim indices in marker order and MAC over the subset.  From the QC records of the slot's last set-up.
+extern "C" int sg_engine_subset_vr_markers(sg_ctx* c, int64_t slot, int32_t* bim_index, int32_t* mac, int64_t cap,
+                                           int64_t* n) {
+  NEED_OPERATOR(c);
+  Engine& e = c->eng;
+  if (!exact_mode(c->mv_mode)) return set_err(c, SG_ERR_STATE, "select a subset-exact engine first");
+  if (slot < 0 || slot >= (int64_t)e.sub.size() || !e.sub[slot].valid || !e.sub[slot].qc)
+    return set_err(c, SG_ERR_STATE, "phenotype slot %lld has no subset set up", (long long)slot);
+  const int64_t m = c->m_bim;
+  std::vector<MarkerQC> qc(m);
+  if (m) SG_CUDA(c, cudaMemcpyAsync(qc.data(), e.sub[slot].qc, m * sizeof(MarkerQC), cudaMemcpyDeviceToHost, c->side));
+  SG_TRY(sync_side(c));
+  int64_t k = 0;
+  for (int64_t i = 0; i < m; ++i) {
+    if (!qc[i].pass_vr) continue;
+    if (k < cap) {
+      if (bim_index) bim_index[k] = (int32_t)i;
+      if (mac) mac[k] = qc[i].mac;
+    }
+    ++k;
+  }
+  if (n) *n = k;
+  return SG_OK;
+}
+
+// Genotypes (0/1/2) of .bim marker ``marker`` for every cohort sample, missing calls taking the fill
+// of the slot's subset (Get_OneSNP_Geno over the subset's setgeno, FIT.cpp:346-357, 447).
+extern "C" int sg_engine_subset_geno(sg_ctx* c, int64_t slot, int64_t marker, int32_t* out) {
+  NEED_OPERATOR(c);
+  Engine& e = c->eng;
+  if (!out) return set_err(c, SG_ERR_INVALID, "null output");
+  if (!exact_mode(c->mv_mode)) return set_err(c, SG_ERR_STATE, "select a subset-exact engine first");
+  if (slot < 0 || slot >= (int64_t)e.sub.size() || !e.sub[slot].valid || !e.sub[slot].qc)
+    return set_err(c, SG_ERR_STATE, "phenotype slot %lld has no subset set up", (long long)slot);
+  if (marker < 0 || marker >= c->m_bim) return set_err(c, SG_ERR_INVALID, "marker %lld out of range", (long long)marker);
+  std::vector<uint8_t> row((size_t)c->pitch);
+  MarkerQC q{};
+  SG_CUDA(c, cudaMemcpyAsync(row.data(), c->d_codes + marker * c->pitch, c->pitch, cudaMemcpyDeviceToHost, c->side));
+  SG_CUDA(c, cudaMemcpyAsync(&q, e.sub[slot].qc + marker, sizeof(MarkerQC), cudaMemcpyDeviceToHost, c->side));
+  SG_TRY(sync_side(c));
+  for (int64_t i = 0; i < c->nn; ++i) {
+    const unsigned f = (row[i >> 2] >> (2 * (i & 3))) & 3u;
+    out[i] = f == 1u ? q.fill : 2 - (int)((f & 1u) + (f >> 1));
+  }
+  return SG_OK;
+}
+
 extern "C" int sg_engine_forget_subsets(sg_ctx* c) {
   NEED_OPERATOR(c);
   for (auto& ss : c->eng.sub) {

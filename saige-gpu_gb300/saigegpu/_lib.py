@@ -93,6 +93,8 @@ SIGNATURES = {
     "sg_engine_set_pheno": [c_ctx, c_i64, P_f64, P_f64, P_u8],
     "sg_engine_forget_subsets": [c_ctx],
     "sg_engine_prepare_subset": [c_ctx, c_i64, P_u8],
+    "sg_engine_subset_vr_markers": [c_ctx, c_i64, P_i32, P_i32, c_i64, P_i64],
+    "sg_engine_subset_geno": [c_ctx, c_i64, c_i64, P_i32],
     "sg_engine_subset_wait": [c_ctx, c_i64],
     "sg_engine_submit": [c_ctx, c_i64, C.c_int, P_f64, c_i64, C.c_int, C.c_double, P_i64],
     "sg_engine_submit_probes": [c_ctx, c_i64, C.c_int, c_u64, c_i64, c_i64, C.c_int, C.c_double,

@@ -484,6 +484,21 @@ class Context:
     def engine_subset_wait(self, slot):
         self._call("sg_engine_subset_wait", int(slot))
 
+    def engine_subset_vr_markers(self, slot):
+        """(bim indices, MAC over the subset) of a set-up slot's variance-ratio markers."""
+        n = C.c_int64()
+        self._call("sg_engine_subset_vr_markers", int(slot), None, None, 0, C.byref(n))
+        idx, mac = np.empty(max(n.value, 1), np.int32), np.empty(max(n.value, 1), np.int32)
+        self._call("sg_engine_subset_vr_markers", int(slot), _ptr(idx, L.P_i32), _ptr(mac, L.P_i32), n.value,
+                   C.byref(n))
+        return idx[:n.value], mac[:n.value]
+
+    def engine_subset_geno(self, slot, marker):
+        """Genotypes of a .bim marker for every cohort sample, missing calls at the slot's subset fill."""
+        out = np.empty(self.n, np.int32)
+        self._call("sg_engine_subset_geno", int(slot), int(marker), _ptr(out, L.P_i32))
+        return out
+
     def engine_forget_subsets(self):
         """Subset-exact engine: rebuild every slot's subset state at its next engine_set_pheno."""
         self._call("sg_engine_forget_subsets")

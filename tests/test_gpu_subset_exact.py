@@ -11,7 +11,7 @@ import pytest
 
 from oracle import aireml, plink
 from saigegpu import (MV_FP32_SIMT, MV_SUBSET_EXACT, MV_SUBSET_EXACT_F8, TC_SUBSET_PAIR, TC_SUBSET_SLICE, native,
-                      prep, serve, synth)
+                      prep, serve, synth, vr)
 
 pytestmark = pytest.mark.gpu
 
@@ -238,3 +238,40 @@ def test_subset_exact_f8_variants_bit_identical(exact_cohort):
     finally:
         ctx.set_tc_option(TC_SUBSET_PAIR, 2)
         ctx.set_matvec_mode(MV_FP32_SIMT)
+
+
+@pytest.mark.parametrize("trait", ["binary", "quantitative"])
+def test_subset_exact_variance_ratio_matches_oracle(gpu_ctx, trait):
+    """Variance ratio of a phenotype on its own subset (extractVarianceRatio after setgeno over the
+    subset, FIT.R:2152-2423): the subset's variance-ratio markers and genotypes from the engine's
+    subset QC, the solves on K_S, against the oracle over setgeno of the subset.  Runs last in this
+    file: it sets the cohort up again with a variance-ratio marker draw."""
+    ctx = gpu_ctx
+    bed, _ = synth.synth_bed(78, N, M, 0.02)
+    rng = np.random.default_rng(21)
+    vr_rand = np.unique(rng.integers(0, M, 1000))
+    mask = rng.uniform(size=N) > 0.25
+    S = np.nonzero(mask)[0]
+    ctx.set_matvec_mode(MV_FP32_SIMT)
+    ctx.setgeno(bed, N, M, vr_random=vr_rand, min_mac_vr=20.0, is_var_ratio=True)
+    g_all = plink.setgeno(bed, N, M, np.arange(1, N + 1), np.ones(N, bool), 0.01, 0.15)
+    gv = synth.genetic_value_from_codes(g_all.codes, 5)
+    y, C = synth.simulate_pheno(gv / gv.std(), 77, trait, tau=0.5, prevalence=0.25, h2=0.5)
+    f0 = prep.make_fit0(y[S], C[S], trait, True)
+    gs = plink.setgeno(bed, N, M, S + 1, mask, 0.01, 0.15, vr_rand, 20, True)
+    grm = aireml.DenseGRM(gs)
+    fit = (aireml.glmmkin_binary if trait == "binary" else aireml.glmmkin_quantitative)(grm, f0)
+    order = np.random.default_rng(9).permutation(len(gs.vr_index))
+    ref, rref = aireml.variance_ratio(grm, fit, trait, f0["Xorig"], gs.vr_codes, order)
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    try:
+        ctx.engine_reserve(128, 1)
+        ctx.engine_set_pheno(0, np.ones(N), np.array([1.0, 0.5]), mask)
+        idx, mac = ctx.engine_subset_vr_markers(0)
+        np.testing.assert_array_equal(idx, gs.vr_index)
+        np.testing.assert_array_equal(ctx.engine_subset_geno(0, int(idx[3]))[S], gs.vr_codes[3])
+        got, rgot = vr.variance_ratio_subset(ctx, 0, fit, trait, f0["Xorig"], mask, order)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+    assert len(rgot) == len(rref)
+    assert abs(got - ref) / ref < 1e-4, (got, ref)
