@@ -254,7 +254,7 @@ void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* fl
 // staged 256 markers at a time in shared memory as pair entries: entry n of a marker holds the
 // values of the two samples whose codes form the 4-bit field n, so one 8-byte shared load serves two
 // samples.  FP32 sums per chunk into part[chunk][sample], each sample's markers added in marker
-// order; the words of four marker rows are requested together.  Pass 2: per sample, the chunks'
+// order; the words of eight marker rows are requested together.  Pass 2: per sample, the chunks'
 // partials added in chunk order in FP64.
 constexpr int kDiagChunkM = 1024;
 
@@ -282,14 +282,14 @@ subset_diag_part_kernel(const uint32_t* __restrict__ codes32, int64_t words_per_
     __syncthreads();
     if (w < nwords) {
       const uint32_t* row = codes32 + k0 * words_per_row + w;
-      // four marker rows' words requested together, then added in marker order
+      // eight marker rows' words requested together, then added in marker order
       int k = 0;
-      for (; k + 4 <= kn; k += 4) {
-        uint32_t word[4];
+      for (; k + 8 <= kn; k += 8) {
+        uint32_t word[8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) word[u] = __ldg(row + (int64_t)(k + u) * words_per_row);
+        for (int u = 0; u < 8; ++u) word[u] = __ldg(row + (int64_t)(k + u) * words_per_row);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < 8; ++u) {
           const float2* e = spair[k + u];
 #pragma unroll
           for (int s = 0; s < 16; s += 2) {
