@@ -1291,6 +1291,13 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   e.h_ph.assign(max_phenos, PhenoState{0.0, 0.0});
   e.ph_set.assign(max_phenos, 0);
   e.sub.assign(max_phenos, Engine::SlotSub{});
+  // per-slot records that calls made without the driver's lock read: sized here, never resized
+  // while the engine runs
+  e.dots.assign(max_phenos, Engine::DotsPending{});
+  e.h_wslot.assign(max_phenos, nullptr);
+  e.ev_slot.assign(max_phenos, nullptr);
+  e.slot_rec.assign(max_phenos, 0);
+  e.slot_wait.assign(max_phenos, 0);
   SG_TRY(dev_alloc_t(c, &e.d_slots, (size_t)max_phenos));
   SG_CUDA(c, cudaMemsetAsync(e.d_slots, 0, max_phenos * sizeof(SubsetSlot), c->stream));
   e.hi_col = 0;
