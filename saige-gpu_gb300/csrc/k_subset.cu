@@ -249,30 +249,35 @@ void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* fl
 
 // Diagonal of M' K_S (sum over the subset's GRM markers of z'^2, the Jacobi preconditioner's
 // Get_Diagof_StdGeno, FIT.cpp:665-704), lut4[4 m + code] = d'_m (g - 2p'_m)^2 per packed code (the
-// missing code carries the subset fill).  Pass 1: block = 256 words of a marker row (16 samples
+// missing code carries the subset fill).  Pass 1: block = 128 words of a marker row (16 samples
 // each, so a warp reads 128 contiguous bytes) x a chunk of kDiagChunkM markers.  The table is
-// staged 256 markers at a time in shared memory as pair entries: entry n of a marker holds the
+// staged 128 markers at a time in shared memory as pair entries: entry n of a marker holds the
 // values of the two samples whose codes form the 4-bit field n, so one 8-byte shared load serves two
 // samples.  FP32 sums per chunk into part[chunk][sample], each sample's markers added in marker
 // order; the words of eight marker rows are requested together.  Pass 2: per sample, the chunks'
 // partials added in chunk order in FP64.
 constexpr int kDiagChunkM = 1024;
+// 128 threads and a 16 KB table stage: small enough (5.6k registers, 16 KB of shared memory) for
+// two blocks to sit on an SM beside a genotype-GEMM CTA, whose one CTA per SM leaves about 11k
+// registers and 30 KB free, so a phenotype's set-up runs in the GEMM's idle issue slots rather
+// than waiting for its tiles to drain.
+constexpr int kDiagThreads = 128;
 
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kDiagThreads)
 subset_diag_part_kernel(const uint32_t* __restrict__ codes32, int64_t words_per_row, int64_t nwords,
                         const float4* __restrict__ lut4, int64_t m, int64_t np, float* __restrict__ part) {
-  __shared__ float2 spair[kThreads][16];
-  const int64_t w = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+  __shared__ float2 spair[kDiagThreads][16];
+  const int64_t w = (int64_t)blockIdx.x * kDiagThreads + threadIdx.x;
   const int64_t m0 = (int64_t)blockIdx.y * kDiagChunkM;
   const int64_t m1 = m0 + kDiagChunkM < m ? m0 + kDiagChunkM : m;
   float acc[16];
 #pragma unroll
   for (int s = 0; s < 16; ++s) acc[s] = 0.0f;
-  for (int64_t k0 = m0; k0 < m1; k0 += kThreads) {
-    const int kn = (int)(m1 - k0 < kThreads ? m1 - k0 : kThreads);
+  for (int64_t k0 = m0; k0 < m1; k0 += kDiagThreads) {
+    const int kn = (int)(m1 - k0 < kDiagThreads ? m1 - k0 : kDiagThreads);
     __syncthreads();
     // entry i = (marker i / 16, field i % 16): a warp writes 32 consecutive entries (no bank conflicts)
-    for (int i = threadIdx.x; i < 16 * kn; i += kThreads) {
+    for (int i = threadIdx.x; i < 16 * kn; i += kDiagThreads) {
       const float4 q = __ldg(lut4 + k0 + (i >> 4));
       const int n = i & 15;
       const float a = (n & 3) == 0 ? q.x : (n & 3) == 1 ? q.y : (n & 3) == 2 ? q.z : q.w;
@@ -336,8 +341,8 @@ void launch_subset_diag(const uint8_t* codes, int64_t pitch, const float* lut4, 
   const int64_t nwords = (nn + 15) / 16;
   const int nchunks = (int)((m + kDiagChunkM - 1) / kDiagChunkM);
   if (nchunks > 0 && nwords > 0) {
-    dim3 grid((unsigned)((nwords + kThreads - 1) / kThreads), (unsigned)nchunks);
-    subset_diag_part_kernel<<<grid, kThreads, 0, s>>>(reinterpret_cast<const uint32_t*>(codes), pitch / 4, nwords,
+    dim3 grid((unsigned)((nwords + kDiagThreads - 1) / kDiagThreads), (unsigned)nchunks);
+    subset_diag_part_kernel<<<grid, kDiagThreads, 0, s>>>(reinterpret_cast<const uint32_t*>(codes), pitch / 4, nwords,
                                                       reinterpret_cast<const float4*>(lut4), m, np, part);
   }
   subset_diag_sum_kernel<<<(unsigned)((np + kThreads - 1) / kThreads), kThreads, 0, s>>>(part, nchunks, nn, np, out);
