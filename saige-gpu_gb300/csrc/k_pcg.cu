@@ -389,34 +389,40 @@ void launch_probe_fill_multi(int64_t np, int64_t nn, const uint64_t* seeds, cons
 }
 
 // Hutchinson probe reductions: for probe j the block sums of Au.Su, u.Su, Au.SX_q and SX_q.u.
-__global__ void probe_dots_kernel(int64_t np, int64_t nn, const double* const* __restrict__ vecs, int64_t k,
-                                  const double* __restrict__ minv, uint64_t seed, int64_t run0,
-                                  const double* __restrict__ SX, int p, double* part, int64_t nblk) {
-  __shared__ double sh[kThreads / 32];
+// Blocks of 128 threads with the accumulators sized for p <= 4 (the usual covariate count) take
+// few enough registers to run on an SM beside a genotype-GEMM CTA, in its idle issue slots.
+constexpr int kDotsThreads = 128;
+
+template <int PMAX>
+__global__ void __launch_bounds__(kDotsThreads)
+probe_dots_kernel(int64_t np, int64_t nn, const double* const* __restrict__ vecs, int64_t k,
+                  const double* __restrict__ minv, uint64_t seed, int64_t run0,
+                  const double* __restrict__ SX, int p, double* part, int64_t nblk) {
+  __shared__ double sh[kDotsThreads / 32];
   const int64_t j = blockIdx.y;
   const double* su = vecs[j];
   const double* au = vecs[k + j];
   const int64_t i0 = (int64_t)blockIdx.x * kChunk;
-  double v[2 + 2 * kProbeDotsMaxP];
+  double v[2 + 2 * PMAX];
 #pragma unroll
-  for (int q = 0; q < 2 + 2 * kProbeDotsMaxP; ++q) v[q] = 0.0;
-  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < nn; i += kThreads) {
+  for (int q = 0; q < 2 + 2 * PMAX; ++q) v[q] = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i0 + kChunk && i < nn; i += kDotsThreads) {
     const double a = au[i], s = su[i];
     const double u = (minv[i] != 0.0) ? ((hash3(seed, (uint64_t)(run0 + j), (uint64_t)i) >> 63) ? 1.0 : -1.0) : 0.0;
     v[0] += a * s;
     v[1] += u * s;
 #pragma unroll
-    for (int q = 0; q < kProbeDotsMaxP; ++q) {
+    for (int q = 0; q < PMAX; ++q) {
       if (q < p) {
         const double x = SX[(int64_t)q * np + i];
         v[2 + q] += a * x;
-        v[2 + kProbeDotsMaxP + q] += x * u;
+        v[2 + PMAX + q] += x * u;
       }
     }
   }
   const int nv = 2 + 2 * p;
   for (int q = 0; q < nv; ++q) {
-    const int src = q < 2 + p ? q : (2 + kProbeDotsMaxP + (q - 2 - p));
+    const int src = q < 2 + p ? q : (2 + PMAX + (q - 2 - p));
     const double t = block_sum(v[src], sh);
     if (threadIdx.x == 0) part[(j * nblk + blockIdx.x) * nv + q] = t;
   }
@@ -427,7 +433,11 @@ void launch_probe_dots(int64_t np, int64_t nn, const double* const* vecs, int64_
                        int64_t p, double* part, int64_t nblk, cudaStream_t s) {
   if (k == 0) return;
   dim3 grid((unsigned)nblk, (unsigned)k);
-  probe_dots_kernel<<<grid, kThreads, 0, s>>>(np, nn, vecs, k, minv_row, seed, run0, SX, (int)p, part, nblk);
+  if (p <= 4)
+    probe_dots_kernel<4><<<grid, kDotsThreads, 0, s>>>(np, nn, vecs, k, minv_row, seed, run0, SX, (int)p, part, nblk);
+  else
+    probe_dots_kernel<kProbeDotsMaxP><<<grid, kDotsThreads, 0, s>>>(np, nn, vecs, k, minv_row, seed, run0, SX, (int)p,
+                                                                  part, nblk);
 }
 
 __global__ void f64_to_f32_kernel(const double* a, float* b, int64_t n) {
