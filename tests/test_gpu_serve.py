@@ -309,3 +309,28 @@ def test_launch_finish_retires_columns_that_converge_at_init(cohort):
         np.testing.assert_array_equal(got[ids[2]][0], ref[ids2[1]])
     finally:
         ctx.engine_hold_results(False)
+
+
+def test_native_fit_with_many_covariates_matches_oracle(cohort):
+    """Seven design columns (covariates not folded into the offset): the probe reductions carry
+    2 + 2 p = 16 sums per probe, past the kernel's four-covariate fast path."""
+    from saigegpu import native
+    ctx, grm, specs, refs = cohort
+    n = grm.n
+    rng = np.random.default_rng(17)
+    gv = synth.genetic_value_from_codes(plink.setgeno(*_cohort_bed(), np.arange(1, n + 1), np.ones(n, bool),
+                                                      0.01, 0.15).codes, 11)
+    y, C = synth.simulate_pheno(gv, 91, "binary", tau=0.6, prevalence=0.3, h2=0.5)
+    C6 = np.column_stack([C, rng.standard_normal((n, 4))])
+    f0 = prep.make_fit0(y, C6, "binary", False)
+    assert f0["X"].shape[1] == 7
+    ref = aireml.glmmkin_binary(grm, f0)
+    res, _ = native.fit_batch(ctx, [serve.FitSpec(f0, "binary")], max_columns=256)
+    assert not isinstance(res[0], Exception), res[0]
+    np.testing.assert_allclose(res[0]["theta"], ref["theta"], rtol=1e-4)
+
+
+def _cohort_bed():
+    n, m = 640, 1600
+    bed, _ = synth.synth_bed(41, n, m, 0.02)
+    return bed, n, m
