@@ -249,19 +249,17 @@ void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* fl
 
 // Diagonal of M' K_S (sum over the subset's GRM markers of z'^2, the Jacobi preconditioner's
 // Get_Diagof_StdGeno, FIT.cpp:665-704), lut4[4 m + code] = d'_m (g - 2p'_m)^2 per packed code (the
-// missing code carries the subset fill).  Pass 1: block = 128 words of a marker row (16 samples
+// missing code carries the subset fill).  Pass 1: block = 256 words of a marker row (16 samples
 // each, so a warp reads 128 contiguous bytes) x a chunk of kDiagChunkM markers.  The table is
-// staged 128 markers at a time in shared memory as pair entries: entry n of a marker holds the
+// staged 256 markers at a time in shared memory as pair entries: entry n of a marker holds the
 // values of the two samples whose codes form the 4-bit field n, so one 8-byte shared load serves two
 // samples.  FP32 sums per chunk into part[chunk][sample], each sample's markers added in marker
 // order; the words of eight marker rows are requested together.  Pass 2: per sample, the chunks'
 // partials added in chunk order in FP64.
 constexpr int kDiagChunkM = 1024;
-// 128 threads and a 16 KB table stage: small enough (5.6k registers, 16 KB of shared memory) for
-// two blocks to sit on an SM beside a genotype-GEMM CTA, whose one CTA per SM leaves about 11k
-// registers and 30 KB free, so a phenotype's set-up runs in the GEMM's idle issue slots rather
-// than waiting for its tiles to drain.
-constexpr int kDiagThreads = 128;
+// 256 threads and a 32 KB table stage.  (128-thread blocks with a 16 KB stage fit on an SM beside a
+// genotype-GEMM CTA, but measured 0.9% lower bench throughput than these in an A/B on one GPU.)
+constexpr int kDiagThreads = 256;
 
 __global__ void __launch_bounds__(kDiagThreads)
 subset_diag_part_kernel(const uint32_t* __restrict__ codes32, int64_t words_per_row, int64_t nwords,
