@@ -218,8 +218,19 @@ int sg_grm_padded_n(sg_ctx *ctx, int64_t *np);
  * getDiagOfSigma_LOCO (FIT.cpp:2370-2392): K_-j P = (M K P - Z_j Z_j' P) / (M - M_j) with the
  * chromosome's standardised genotypes in FP32, and diag minus its sum z^2.  The _LOCO drop-ins of
  * the reference (getCoefficients_LOCO, getPCG1ofSigmaAndVector_LOCO, ...) are the plain drop-ins
- * called while a range is set.  Phenotype slots read the diagonal when set, so (re)set them after. */
+ * called while a range is set.  Phenotype slots read the diagonal when set, so (re)set them after.
+ * The subset-exact engines reject it (their GRM markers differ by phenotype): use sg_loco_set_bim. */
 int sg_loco_set(sg_ctx *ctx, int64_t begin, int64_t end);
+/* Leave one chromosome out, given as .bim markers [begin, end] (0-based, inclusive).  The GRM
+ * markers inside it are those the reference's updateChrStartEndIndexVec (Util.R:29-65) finds for the
+ * chromosome.  On a resident GRM this is sg_loco_set over that range of GRM markers.  In the
+ * subset-exact engines every phenotype's GRM markers are the .bim markers passing QC over its own
+ * samples (setgeno per phenotype, FIT.cpp:376-385), so the range applies per phenotype: a slot set
+ * (sg_engine_set_pheno) after this call leaves its own GRM markers inside [begin, end] out of its
+ * GRM, its diagonal and its marker count M', as the reference's setStartEndIndex +
+ * parallelCrossProd_LOCO + getDiagOfSigma_LOCO (FIT.cpp:3067-3085, 1790-1851, 2370-2392) do over
+ * that phenotype's setgeno.  Set every slot again after the call.  sg_loco_clear ends either form. */
+int sg_loco_set_bim(sg_ctx *ctx, int64_t begin, int64_t end);
 int sg_loco_clear(sg_ctx *ctx);
 
 /* ------------------------------------------------------------ drop-ins for the Rcpp entry points */

@@ -141,6 +141,7 @@ struct Engine {
     bool valid = false;
     bool all = false;             // built for "every sample" (no mask)
     std::vector<uint8_t> mask;    // the mask it was built for
+    int64_t ex_lo = 0, ex_hi = -1;  // and the .bim markers it left out (a chromosome, or none)
     float* dp = nullptr;          // mg: d' = 1/sd'^2 (0 off the subset's GRM markers)
     float* p2 = nullptr;          // mg: 2p'
     float* lut = nullptr;         // mg x 4: d' (g - 2p')^2 per packed code (diagonal)
@@ -163,6 +164,7 @@ struct Engine {
     bool prep_all = false;
     std::vector<uint8_t> prep_mask;
     int64_t prep_ns = 0;
+    int64_t prep_lo = 0, prep_hi = -1;
   };
   std::vector<SlotSub> sub;
   SubsetSlot* d_slots = nullptr;
@@ -228,6 +230,9 @@ struct sg_ctx {
   float* d_lp = nullptr;   // P in full FP32 for the correction (cap_cols x np)
   std::vector<double> diag_loco;
   double* d_diag_loco = nullptr;  // its device copy (slot weights)
+  // the subset-exact engines: .bim markers sub_loco_lo..sub_loco_hi left out of every phenotype's
+  // GRM (none when lo > hi); each slot's subset state is rebuilt for it at the slot's next set
+  int64_t sub_loco_lo = 0, sub_loco_hi = -1;
   // device time of the last setgeno ([0] QC, [1] re-pack + LUT, [2] diagonal) and grm_build
   // ([3] Z build, [4] SYRK), in ms, from CUDA events on the context stream
   double t_build[5] = {0, 0, 0, 0, 0};
@@ -451,6 +456,8 @@ extern "C" int sg_set_matvec_mode(sg_ctx* c, int mode) {
     if (c->loco) return set_err(c, SG_ERR_STATE, "clear the LOCO range first (sg_loco_clear)");
     for (auto& kv : c->eng.reqs)
       if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");
+  } else if (c->sub_loco_lo <= c->sub_loco_hi) {
+    return set_err(c, SG_ERR_STATE, "clear the LOCO range first (sg_loco_clear)");
   }
   const bool was_exact = exact_mode(c->mv_mode);
   c->mv_mode = mode;
@@ -595,6 +602,8 @@ static void loco_free(sg_ctx* c);
 static void free_geno(sg_ctx* c) {
   engine_free(c);
   loco_free(c);
+  c->sub_loco_lo = 0;
+  c->sub_loco_hi = -1;
   dev_free_t(c, c->d_packed);
   dev_free_t(c, c->d_packed_vr);
   dev_free_t(c, c->d_lut);
@@ -1358,8 +1367,8 @@ static int subset_prepare(sg_ctx* c, int64_t slot, const uint8_t* mask) {
                    c->qc_min_mac_vr, c->qc_max_mac_vr, c->qc_is_var_ratio, ss.qc, c->side);
   // d' = 1/sd'^2, 2p' and the diagonal table per marker, the fill-changed markers in marker order,
   // on the device (setGenoObj's per-marker values over the subset, FIT.cpp:436-495, 152-159)
-  launch_subset_derive(ss.qc, c->d_fill_all, m, mg, ss.dp, ss.p2, ss.lut, ss.flag, ss.flips, ss.dfill,
-                       ss.d_counts, c->side);
+  launch_subset_derive(ss.qc, c->d_fill_all, m, mg, c->sub_loco_lo, c->sub_loco_hi, ss.dp, ss.p2, ss.lut, ss.flag,
+                       ss.flips, ss.dfill, ss.d_counts, c->side);
   SG_LAUNCHED(c, 3);
   SG_CUDA(c, cudaMemcpyAsync(ss.h_counts, ss.d_counts, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->side));
   SG_CUDA(c, cudaEventRecord(ss.ev_prep, c->side));
@@ -1369,11 +1378,21 @@ static int subset_prepare(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   if (mask) ss.prep_mask.assign(mask, mask + nn);
   else ss.prep_mask.clear();
   ss.prep_ns = ns;
+  ss.prep_lo = c->sub_loco_lo;
+  ss.prep_hi = c->sub_loco_hi;
   return SG_OK;
 }
 
 static bool same_mask(bool all, const std::vector<uint8_t>& kept, const uint8_t* mask, int64_t nn) {
   return (!mask && all) || (mask && !all && std::memcmp(kept.data(), mask, nn) == 0);
+}
+// the slot's built / prepared subset state is the one for this mask and the context's LOCO range
+static bool slot_built(const sg_ctx* c, const Engine::SlotSub& ss, const uint8_t* mask) {
+  return ss.valid && ss.ex_lo == c->sub_loco_lo && ss.ex_hi == c->sub_loco_hi && same_mask(ss.all, ss.mask, mask, c->nn);
+}
+static bool slot_prepared(const sg_ctx* c, const Engine::SlotSub& ss, const uint8_t* mask) {
+  return ss.prep && ss.prep_lo == c->sub_loco_lo && ss.prep_hi == c->sub_loco_hi &&
+         same_mask(ss.prep_all, ss.prep_mask, mask, c->nn);
 }
 
 // Subset-exact engine: the state of slot ``slot``'s sample subset, rebuilt only when its mask
@@ -1387,8 +1406,8 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
   Engine& e = c->eng;
   Engine::SlotSub& ss = e.sub[slot];
   const int64_t nn = c->nn, np = e.np, m = c->m_bim;
-  if (ss.valid && same_mask(ss.all, ss.mask, mask, nn)) return SG_OK;
-  if (!(ss.prep && same_mask(ss.prep_all, ss.prep_mask, mask, nn))) SG_TRY(subset_prepare(c, slot, mask));
+  if (slot_built(c, ss, mask)) return SG_OK;
+  if (!slot_prepared(c, ss, mask)) SG_TRY(subset_prepare(c, slot, mask));
   SG_CUDA(c, cudaEventSynchronize(ss.ev_prep));
   ss.prep = false;
   const int64_t nflip = ss.h_counts[0], mprime = ss.h_counts[1], ns = ss.prep_ns;
@@ -1419,6 +1438,8 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
   SG_CUDA(c, cudaMemcpyAsync(e.d_slots + slot, &ss.dev, sizeof(SubsetSlot), cudaMemcpyHostToDevice, c->side));
   ss.m_prime = (double)mprime;
   ss.all = ss.prep_all;
+  ss.ex_lo = ss.prep_lo;
+  ss.ex_hi = ss.prep_hi;
   ss.mask.swap(ss.prep_mask);
   ss.prep_mask.clear();
   ss.valid = true;
@@ -1438,8 +1459,7 @@ extern "C" int sg_engine_prepare_subset(sg_ctx* c, int64_t slot, const uint8_t* 
     if (kv.second.state == 1 && kv.second.slot == slot)
       return set_err(c, SG_ERR_STATE, "phenotype slot %lld has columns in flight", (long long)slot);
   Engine::SlotSub& ss = e.sub[slot];
-  if (ss.valid && same_mask(ss.all, ss.mask, mask, c->nn)) return SG_OK;
-  if (ss.prep && same_mask(ss.prep_all, ss.prep_mask, mask, c->nn)) return SG_OK;
+  if (slot_built(c, ss, mask) || slot_prepared(c, ss, mask)) return SG_OK;
   return subset_prepare(c, slot, mask);
 }
 
@@ -2668,7 +2688,7 @@ extern "C" int sg_loco_set(sg_ctx* c, int64_t begin, int64_t end) {
                    (long long)end, (long long)c->m_qc);
   if (end - begin + 1 >= c->m_qc) return set_err(c, SG_ERR_INVALID, "LOCO range covers every GRM marker");
   if (exact_mode(c->mv_mode))
-    return set_err(c, SG_ERR_STATE, "LOCO runs on the resident GRM: select another engine first");
+    return set_err(c, SG_ERR_STATE, "the subset-exact engines leave out .bim markers (sg_loco_set_bim)");
   for (auto& kv : c->eng.reqs)
     if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");
   loco_free(c);
@@ -2709,11 +2729,37 @@ extern "C" int sg_loco_set(sg_ctx* c, int64_t begin, int64_t end) {
   return SG_OK;
 }
 
+// One chromosome as .bim markers [begin, end].  On a resident GRM it is the range of GRM markers
+// inside it (the GRM markers are the .bim markers passing QC, in order); in the subset-exact engines
+// each phenotype's GRM markers are those passing QC over its own samples, so every slot's subset
+// state leaves out its own GRM markers inside [begin, end] when the slot is next set.
+extern "C" int sg_loco_set_bim(sg_ctx* c, int64_t begin, int64_t end) {
+  NEED_GENO(c);
+  if (begin < 0 || end < begin || end >= c->m_bim)
+    return set_err(c, SG_ERR_INVALID, "LOCO range [%lld, %lld] outside the %lld .bim markers", (long long)begin,
+                   (long long)end, (long long)c->m_bim);
+  for (auto& kv : c->eng.reqs)
+    if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");
+  if (exact_mode(c->mv_mode)) {
+    c->sub_loco_lo = begin;
+    c->sub_loco_hi = end;
+    return SG_OK;
+  }
+  int64_t b = 0;
+  for (int64_t i = 0; i < begin; ++i) b += c->qc_mask[i] ? 1 : 0;
+  int64_t e = b - 1;
+  for (int64_t i = begin; i <= end; ++i) e += c->qc_mask[i] ? 1 : 0;
+  if (e < b) return set_err(c, SG_ERR_INVALID, "no GRM marker in .bim markers [%lld, %lld]", (long long)begin, (long long)end);
+  return sg_loco_set(c, b, e);
+}
+
 extern "C" int sg_loco_clear(sg_ctx* c) {
   if (!c) return SG_ERR_INVALID;
   for (auto& kv : c->eng.reqs)
     if (kv.second.state == 1) return set_err(c, SG_ERR_STATE, "columns in flight");
   loco_free(c);
+  c->sub_loco_lo = 0;
+  c->sub_loco_hi = -1;
   return SG_OK;
 }
 

@@ -131,16 +131,19 @@ void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int
 // (the LUT's 2p and 1/sd: FIT.cpp:152-159): for each GRM marker of the subset, d' = (1/sd')^2,
 // 2p', and lut4 = d' (g - 2p')^2 for the four packed codes (00 -> 2, 01 -> the subset's own fill,
 // 10 -> 1, 11 -> 0); zeros elsewhere and past m.  flag bit 0: a GRM marker whose subset fill
-// differs from the cohort fill G holds; bit 1: a GRM marker of the subset.
+// differs from the cohort fill G holds; bit 1: a GRM marker of the subset.  Markers ex_lo..ex_hi
+// (one chromosome left out; none when ex_lo > ex_hi) are not GRM markers of the subset: the
+// subset's GRM over the remaining markers is K_-j of setStartEndIndex + parallelCrossProd_LOCO
+// (FIT.cpp:3067-3085, 1790-1851), its diagonal that of set_Diagof_StdGeno_LOCO (FIT.cpp:4934-4959).
 __global__ void subset_derive_kernel(const MarkerQC* __restrict__ qc, const int32_t* __restrict__ fill_all,
-                                     int64_t m, int64_t mg, float* __restrict__ dp, float* __restrict__ p2,
-                                     float4* __restrict__ lut4, uint8_t* __restrict__ flag) {
+                                     int64_t m, int64_t mg, int64_t ex_lo, int64_t ex_hi, float* __restrict__ dp,
+                                     float* __restrict__ p2, float4* __restrict__ lut4, uint8_t* __restrict__ flag) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= mg) return;
   float d32 = 0.0f, tp = 0.0f;
   float4 l = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   uint8_t f = 0;
-  if (k < m) {
+  if (k < m && (k < ex_lo || k > ex_hi)) {
     const MarkerQC q = qc[k];
     if (q.pass_qc) {
       const double d = (double)q.invstd * (double)q.invstd;
@@ -210,10 +213,11 @@ subset_flips_kernel(const MarkerQC* __restrict__ qc, const int32_t* __restrict__
   }
 }
 
-void launch_subset_derive(const MarkerQC* qc, const int32_t* fill_all, int64_t m, int64_t mg, float* dp, float* p2,
-                          float* lut4, uint8_t* flag, int32_t* flips, float* dfill, int64_t* counts, cudaStream_t s) {
+void launch_subset_derive(const MarkerQC* qc, const int32_t* fill_all, int64_t m, int64_t mg, int64_t ex_lo,
+                          int64_t ex_hi, float* dp, float* p2, float* lut4, uint8_t* flag, int32_t* flips, float* dfill,
+                          int64_t* counts, cudaStream_t s) {
   subset_derive_kernel<<<(unsigned)((mg + kThreads - 1) / kThreads), kThreads, 0, s>>>(
-      qc, fill_all, m, mg, dp, p2, reinterpret_cast<float4*>(lut4), flag);
+      qc, fill_all, m, mg, ex_lo, ex_hi, dp, p2, reinterpret_cast<float4*>(lut4), flag);
   subset_flips_kernel<<<1, kFlipThreads, 0, s>>>(qc, fill_all, flag, m, flips, dfill, counts);
 }
 

@@ -887,7 +887,7 @@ static int g_opt[kTcOptions] = {
     8,    // kTcSyrkGroup: row tiles per raster group of the SYRK
     0,    // kTcGrmvSlice: K slice bytes of the split-BF16 GRM.V (0: by width, 64 or 128)
     2,    // kTcSubsetPair: subset-exact genotype GEMMs on CTA pairs (2: above 160 columns)
-    256,  // kTcSubsetSlice: their K-stage bytes (0: 128 up to 160 columns, else 64; or 64 / 128 / 256)
+    256,  // kTcSubsetSlice: their K-stage bytes (0: 128 up to 160 columns, else 64; or 64 / 128 / 256 / 512)
 };
 
 bool tc_set_option(int opt, int value) {

@@ -118,7 +118,7 @@ int tc_get_option(int opt);
 // Split-BF16 GRM.V choices per launch width (n buckets, max_cols increasing; n = 0 clears).
 bool tc_set_grmv_plan(const int32_t* max_cols, const int32_t* pair, const int32_t* slice, int n);
 int tc_get_grmv_plan(int32_t* max_cols, int32_t* pair, int32_t* slice, int cap);
-// The same for the subset-exact engine's genotype GEMMs (slice 64 or 128).
+// The same for the subset-exact engine's genotype GEMMs (slice 64, 128, 256 or 512).
 bool tc_set_subset_plan(const int32_t* max_cols, const int32_t* pair, const int32_t* slice, int n);
 int tc_get_subset_plan(int32_t* max_cols, int32_t* pair, int32_t* slice, int cap);
 // GRM.V column-tile width sets: plain TF32 / FP32, split-TF32, split-BF16 (multiples of 16), and
@@ -214,9 +214,11 @@ struct SubsetSlot {
 void launch_gbuild(const uint8_t* codes, int64_t pitch, const int32_t* fill, int64_t m, int64_t nn, int64_t mg,
                    int64_t np, int form, void* Gmm16, void* Gsm16, void* Gmm8, void* Gsm8, cudaStream_t s);
 // the subset's d', 2p', diagonal table, fill-change list and counts (nflip, M') from its QC records;
-// flag: mg bytes of scratch, flips / dfill: room for m entries, counts: 2 int64 on the device
-void launch_subset_derive(const MarkerQC* qc, const int32_t* fill_all, int64_t m, int64_t mg, float* dp, float* p2,
-                          float* lut4, uint8_t* flag, int32_t* flips, float* dfill, int64_t* counts, cudaStream_t s);
+// flag: mg bytes of scratch, flips / dfill: room for m entries, counts: 2 int64 on the device;
+// markers ex_lo..ex_hi are left out of the subset's GRM (none when ex_lo > ex_hi)
+void launch_subset_derive(const MarkerQC* qc, const int32_t* fill_all, int64_t m, int64_t mg, int64_t ex_lo,
+                          int64_t ex_hi, float* dp, float* p2, float* lut4, uint8_t* flag, int32_t* flips, float* dfill,
+                          int64_t* counts, cudaStream_t s);
 void launch_subset_bitmap(const uint8_t* codes, int64_t pitch, const int32_t* flips, int nflip, int W,
                           const uint8_t* mask, int64_t nn, int64_t np, uint32_t* bits, cudaStream_t s);
 // part: subset_diag_scratch(m, np) floats of scratch

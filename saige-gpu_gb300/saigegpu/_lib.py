@@ -67,6 +67,7 @@ SIGNATURES = {
     "sg_grm_matmul_tf32x3_noalloc": [c_ctx, C.c_void_p, c_i64, C.c_void_p, C.c_void_p],
     "sg_grm_padded_n": [c_ctx, P_i64],
     "sg_loco_set": [c_ctx, c_i64, c_i64],
+    "sg_loco_set_bim": [c_ctx, c_i64, c_i64],
     "sg_loco_clear": [c_ctx],
     "sg_getCrossprodMatAndKin": [c_ctx, P_f32, P_f32],
     "sg_getDiagOfSigma": [c_ctx, P_f32, P_f32, P_f32],

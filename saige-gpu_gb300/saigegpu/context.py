@@ -334,6 +334,11 @@ class Context:
         """Leave GRM markers [begin, end] out (setStartEndIndex); the engine must be idle."""
         self._call("sg_loco_set", int(begin), int(end))
 
+    def loco_set_bim(self, begin, end):
+        """Leave the GRM markers inside .bim markers [begin, end] (one chromosome) out: on a resident
+        GRM at once; in the subset-exact engines per phenotype, at each slot's next set."""
+        self._call("sg_loco_set_bim", int(begin), int(end))
+
     def loco_clear(self):
         self._call("sg_loco_clear")
 

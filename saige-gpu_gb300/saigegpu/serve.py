@@ -302,7 +302,8 @@ def loco_generator(spec, fit, n_cohort):
 
 def loco_ranges(chrom_of_grm_markers):
     """Per-autosome [begin, end] of the GRM markers (updateChrStartEndIndexVec, Util.R:29-65);
-    None for chromosomes without markers.  Markers must be ordered by chromosome."""
+    None for chromosomes without markers.  Markers must be ordered by chromosome.  Given every .bim
+    marker's chromosome, the same ranges index the .bim markers (``fit_loco(..., bim=True)``)."""
     chrom = np.asarray(chrom_of_grm_markers)
     out = {}
     last_end = -1
@@ -319,14 +320,20 @@ def loco_ranges(chrom_of_grm_markers):
     return out
 
 
-def fit_loco(ctx, specs, fits, ranges, max_columns=1024):
-    """LOCO results per chromosome for fitted phenotypes: {chrom: [result or None per spec]}."""
+def fit_loco(ctx, specs, fits, ranges, max_columns=1024, bim=False):
+    """LOCO results per chromosome for fitted phenotypes: {chrom: [result or None per spec]}.
+
+    ``ranges`` ({chrom: (begin, end) or None}, from ``loco_ranges``) index the GRM markers, or with
+    ``bim`` the .bim markers; the subset-exact engines take .bim ranges only, since each phenotype's
+    GRM markers are those passing QC over its own samples (the chromosome's markers among them leave
+    its GRM)."""
     out = {}
+    set_range = ctx.loco_set_bim if bim else ctx.loco_set
     for c, rng in ranges.items():
         if rng is None:
             out[c] = [dict(isLOCO=False) for _ in specs]
             continue
-        ctx.loco_set(rng[0], rng[1])
+        set_range(rng[0], rng[1])
         try:
             r = Runner(ctx, max_columns, max(1, len(specs)))
             ids = []

@@ -57,3 +57,25 @@ def test_loco_coefficients(cohort):
         r = got[c][0]
         np.testing.assert_allclose(r["coefficients"], ref["alpha"], rtol=1e-5)
         np.testing.assert_allclose(r["linear_predictors"], ref["eta"], rtol=1e-5, atol=1e-7)
+
+
+def test_loco_bim_range_selects_the_grm_markers(cohort):
+    """A chromosome given as .bim markers leaves out the GRM markers inside it: the same products,
+    bit for bit, as the GRM-marker range (the GRM markers are the .bim markers passing QC, in order)."""
+    ctx, grm, g, chrom = cohort
+    ranges = serve.loco_ranges(chrom)
+    b, e = ranges[11]
+    bim_of_grm = np.nonzero(g.qc_mask)[0]
+    V = np.random.default_rng(2).standard_normal((grm.n, 24))
+    try:
+        ctx.loco_set(b, e)
+        Y = ctx.grm_matmul(V)
+        # from the .bim marker after the previous chromosome's last GRM marker to the one before
+        # the next chromosome's first: .bim markers failing QC at either end change nothing
+        lo = int(bim_of_grm[b - 1]) + 1 if b > 0 else 0
+        hi = int(bim_of_grm[e + 1]) - 1 if e + 1 < len(bim_of_grm) else len(g.qc_mask) - 1
+        ctx.loco_set_bim(lo, hi)
+        Yb = ctx.grm_matmul(V)
+    finally:
+        ctx.loco_clear()
+    np.testing.assert_array_equal(Yb, Y)

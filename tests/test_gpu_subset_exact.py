@@ -240,6 +240,106 @@ def test_subset_exact_f8_variants_bit_identical(exact_cohort):
         ctx.set_matvec_mode(MV_FP32_SIMT)
 
 
+def _bim_chrom():
+    """22 chromosomes as contiguous blocks of the .bim markers."""
+    return 1 + (np.arange(M) * 22) // M
+
+
+def _subset_loco_range(g, b, e):
+    """The subset's GRM markers inside .bim markers [b, e], as GRM-marker indices of its setgeno
+    (updateChrStartEndIndexVec over the subset's own GRM markers)."""
+    before = int(np.count_nonzero(g.qc_mask[:b]))
+    return before, before + int(np.count_nonzero(g.qc_mask[b:e + 1])) - 1
+
+
+def test_subset_exact_loco_products_match_oracle(exact_cohort):
+    """A chromosome left out (.bim range) in the subset-exact engine: every phenotype's K_S,-j v
+    against the oracle's LOCO GRM over setgeno of its subset (parallelCrossProd_LOCO); the range
+    cleared, the products are the full K_S v again, bit for bit as before the range was set."""
+    ctx, bed, _, cases = exact_cohort
+    rng = np.random.default_rng(31)
+    ranges = serve.loco_ranges(_bim_chrom())
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    try:
+        ctx.engine_reserve(128, len(cases))
+        Vs = []
+        for _, mask, _ in cases:
+            V = rng.standard_normal((N, 6)) + 0.4
+            V[~mask] = 0.0
+            Vs.append(V)
+
+        def products():
+            ids = []
+            for slot, (_, mask, _) in enumerate(cases):
+                ctx.engine_set_pheno(slot, np.ones(N), np.array([1.0, 0.5]), mask)
+                ids.append(ctx.engine_submit(slot, 1, Vs[slot]))
+            got = _run_products(ctx, np.concatenate(ids))
+            return [np.column_stack([got[int(i)] for i in idk]) for idk in ids]
+
+        full = products()
+        for chrom in (4, 17):
+            b, e = ranges[chrom]
+            ctx.loco_set_bim(b, e)
+            try:
+                loco = products()
+            finally:
+                ctx.loco_clear()
+            for (trait, mask, _), V, Y in zip(cases, Vs, loco):
+                S = np.nonzero(mask)[0]
+                g = plink.setgeno(bed, N, M, S + 1, mask, 0.01, 0.15)
+                grm = aireml.DenseGRM(g)
+                gb, ge = _subset_loco_range(g, b, e)
+                ref = aireml.loco_grm(grm, g, gb, ge).K @ V[S]
+                err = np.abs(Y[S] - ref).max() / np.abs(ref).max()
+                print("LOCO chr %d %s: K_S,-j v max error %.2e" % (chrom, trait, err))
+                assert err < 6e-5, (chrom, trait, err)
+                # leaving the chromosome out changed the product
+                assert np.abs(ref - grm.K @ V[S]).max() > 100 * err * np.abs(ref).max()
+        again = products()
+        for a, b_ in zip(full, again):
+            np.testing.assert_array_equal(a, b_)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+
+
+def test_subset_exact_loco_coefficients_match_oracle(exact_cohort):
+    """Get_Coef_LOCO (FIT.R:40-73, run per chromosome by FIT.R:1208-1295) for phenotypes on their
+    own subsets, through the subset-exact engine with a .bim range left out, against the oracle's
+    Get_Coef_LOCO on the LOCO GRM of setgeno over each subset, both from the oracle's full fit."""
+    ctx, bed, _, cases = exact_cohort
+    ranges = serve.loco_ranges(_bim_chrom())
+    sel = {c: ranges[c] for c in (2, 20)}
+    use = cases[:2]  # a binary and a quantitative phenotype
+    specs, fits, grms = [], [], []
+    for trait, mask, f0 in use:
+        S = np.nonzero(mask)[0]
+        g = plink.setgeno(bed, N, M, S + 1, mask, 0.01, 0.15)
+        grm = aireml.DenseGRM(g)
+        grm.probe_index = S
+        fit = (aireml.glmmkin_binary if trait == "binary" else aireml.glmmkin_quantitative)(grm, f0)
+        specs.append(serve.FitSpec(f0, trait, mask=mask))
+        fits.append(fit)
+        grms.append((g, grm))
+    ctx.set_matvec_mode(MV_SUBSET_EXACT)
+    try:
+        got = serve.fit_loco(ctx, specs, fits, sel, max_columns=256, bim=True)
+    finally:
+        ctx.set_matvec_mode(MV_FP32_SIMT)
+    for c, (b, e) in sel.items():
+        for k, ((trait, mask, f0), fit, (g, grm)) in enumerate(zip(use, fits, grms)):
+            gb, ge = _subset_loco_range(g, b, e)
+            ref = aireml.get_coef_loco(aireml.loco_grm(grm, g, gb, ge), f0, fit, trait)
+            r = got[c][k]
+            assert not isinstance(r, Exception), r
+            rel = np.abs(r["coefficients"] - ref["alpha"]) / np.abs(ref["alpha"])
+            print("LOCO chr %d %s: alpha rel error %s" % (c, trait, rel))
+            np.testing.assert_allclose(r["coefficients"], ref["alpha"], rtol=1e-4)
+            # both stop their solves on the same absolute residual rule (tol 1e-5), so entries of eta
+            # near zero differ by about that much of eta's scale (measured 2.6e-6 at a scale of 0.35)
+            np.testing.assert_allclose(r["linear_predictors"], ref["eta"], rtol=1e-4,
+                                       atol=1e-5 * np.abs(ref["eta"]).max())
+
+
 @pytest.mark.parametrize("trait", ["binary", "quantitative"])
 def test_subset_exact_variance_ratio_matches_oracle(gpu_ctx, trait):
     """Variance ratio of a phenotype on its own subset (extractVarianceRatio after setgeno over the
