@@ -67,7 +67,9 @@ def make_fit0(y, covariates, trait="binary", covariate_offset=True, covariate_tr
     """Build ``fit0`` as fitNULLGLMM does (FIT.R:1040-1129) for the null-model fit.
 
     ``covariates`` is (n, q) without the intercept (q may be 0).  Returns a
-    dict with y, X, offset, linear_predictors, coefficients and family name.
+    dict with y, X, offset, linear_predictors, coefficients and family name, and
+    with the QR transform its R factor and kept columns (``transform``), which
+    Covariate_Transform_Back (FIT.R:1653-1659) needs.
     """
     y = np.asarray(y, np.float64)
     n = len(y)
@@ -77,14 +79,16 @@ def make_fit0(y, covariates, trait="binary", covariate_offset=True, covariate_tr
     X = np.column_stack([np.ones(n), C])
     if not has_cov:
         covariate_offset = False
+    transform = None
     if covariate_transform_qr and has_cov:
-        X, _, _ = covariate_transform(X)
+        X, qrr, keep = covariate_transform(X)
+        transform = dict(qrr=qrr, keep=keep)
     g = glm_fit(y, X, family)
     if covariate_offset:
         covoffset = X[:, 1:] @ g["coefficients"][1:]
         X0 = np.ones((n, 1))
         g0 = glm_fit(y, X0, family, offset=covoffset)
         return dict(y=y, X=X0, offset=covoffset, linear_predictors=g0["linear_predictors"],
-                    coefficients=g0["coefficients"], family=family.name, Xorig=X)
+                    coefficients=g0["coefficients"], family=family.name, Xorig=X, transform=transform)
     return dict(y=y, X=X, offset=None, linear_predictors=g["linear_predictors"],
-                coefficients=g["coefficients"], family=family.name, Xorig=None)
+                coefficients=g["coefficients"], family=family.name, Xorig=None, transform=transform)

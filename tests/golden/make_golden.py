@@ -15,7 +15,13 @@ It writes (all derived from ``src/SAIGE/extdata``):
 * ``golden_fits.json``        -- theta, coefficients and the first fitted
   values of ``output/example_binary_fullGRM.rda``, ``example_binary.rda`` and
   ``example_quantitative_fullGRM.rda`` plus the null variance ratios of the
-  matching ``.varianceRatio.txt`` files.
+  matching ``.varianceRatio.txt`` files;
+* ``example_binary_includenonAutoforvarRatio.rda`` -- that step-1 model file,
+  verbatim (R's own serialisation, for the byte-exact round trip of
+  ``saigegpu.rdata``);
+* ``model_schema_binary_fullGRM.json`` -- the layout (``saigegpu.rdata.schema``)
+  of ``example_binary_fullGRM.rda``'s model: field names, types, shapes,
+  attributes and classes, with its LOCO results.
 
 The ``.rda`` files are R serialisation (XDR, version 2/3) of a list whose
 first seven elements are theta, coefficients, linear.predictors,
@@ -25,12 +31,14 @@ just enough of the format to reach them.
 import gzip
 import json
 import os
+import shutil
 import struct
 import sys
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "saige-gpu_gb300"))
 
 
 class _RReader:
@@ -155,7 +163,8 @@ def main(ref_root):
     outp = os.path.join(ext, "output")
     stem = os.path.join(inp, "plinkforGRM_1000samples_10kMarkers")
     bed = open(stem + ".bed", "rb").read()
-    with gzip.open(os.path.join(HERE, "plink_1000x10k.bed.gz"), "wb", compresslevel=9) as f:
+    with open(os.path.join(HERE, "plink_1000x10k.bed.gz"), "wb") as raw, \
+            gzip.GzipFile(fileobj=raw, mode="wb", compresslevel=9, mtime=0) as f:
         f.write(bed)
     fam = [l.split()[1] for l in open(stem + ".fam")]
     bim_n = sum(1 for _ in open(stem + ".bim"))
@@ -192,6 +201,13 @@ def main(ref_root):
     golden["variance_ratio_null"] = vr
     with open(os.path.join(HERE, "golden_fits.json"), "w") as f:
         json.dump(golden, f, indent=1)
+
+    from saigegpu import rdata
+    shutil.copyfile(os.path.join(outp, "example_binary_includenonAutoforvarRatio.rda"),
+                    os.path.join(HERE, "example_binary_includenonAutoforvarRatio.rda"))
+    _, objs = rdata.read_rda(os.path.join(outp, "example_binary_fullGRM.rda"))
+    with open(os.path.join(HERE, "model_schema_binary_fullGRM.json"), "w") as f:
+        json.dump(rdata.schema(dict(objs)["modglmm"]), f, separators=(",", ":"))
     print("wrote fixtures to", HERE)
 
 

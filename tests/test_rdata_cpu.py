@@ -1,0 +1,158 @@
+"""The step-1 model file (.rda): R's serialisation read and written byte for byte, and the model laid
+out as the reference's step 1 saves it (no GPU)."""
+import gzip
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import aireml, plink
+from saigegpu import output, prep, rdata
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+RDA = os.path.join(GOLDEN, "example_binary_includenonAutoforvarRatio.rda")
+
+
+def test_reference_model_file_round_trips_byte_for_byte():
+    """The reference's own step-1 model file, read and written again, gives R's bytes exactly:
+    the writer's flags, symbol references, string encodings, attributes and ALTREP items are R's."""
+    raw = gzip.decompress(open(RDA, "rb").read())
+    header, objs = rdata.read_rda(RDA)
+    assert [k for k, _ in objs] == ["modglmm"]
+    out = rdata.rda_bytes(objs, writer=header["writer"], min_reader=header["min_reader"],
+                          encoding=header["encoding"])
+    assert out == raw
+
+
+def test_values_round_trip(tmp_path):
+    obj = rdata.r_named_list([
+        ("d", rdata.r_double([1.5, -np.inf, np.nan], names=["a", "b", "c"])),
+        ("i", rdata.r_int([1, rdata.NA_INTEGER, 7])),
+        ("l", rdata.r_lgl([True, False])),
+        ("s", rdata.r_str(["x", None, "été"])),
+        ("m", rdata.r_matrix(np.arange(6.0).reshape(3, 2), ["u", "v"])),
+        ("z", rdata.RObj(rdata.CPLXSXP, np.array([1 + 2j, -3j]))),
+        ("r", rdata.RObj(rdata.RAWSXP, b"\x00\x01\xff")),
+        ("nested", rdata.r_named_list([("names", rdata.r_str("again"))], cls=["k1", "k2"])),
+        ("null", None),
+    ])
+    p = str(tmp_path / "x.rda")
+    rdata.write_rda(p, [("obj", obj)])
+    _, objs = rdata.read_rda(p)
+    back = dict(objs)["obj"]
+    assert back.names() == ["d", "i", "l", "s", "m", "z", "r", "nested", "null"]
+    np.testing.assert_array_equal(back["d"].value, [1.5, -np.inf, np.nan])
+    assert back["d"].names() == ["a", "b", "c"]
+    assert list(back["i"].value) == [1, rdata.NA_INTEGER, 7]
+    assert list(back["s"].value) == ["x", None, "été"]
+    np.testing.assert_array_equal(rdata.to_numpy(back["m"]), np.arange(6.0).reshape(3, 2))
+    np.testing.assert_array_equal(back["z"].value, [1 + 2j, -3j])
+    assert back["r"].value == b"\x00\x01\xff"
+    assert back["nested"].is_object and list(back["nested"].attr("class").value) == ["k1", "k2"]
+    assert back["null"] is None
+    # a symbol (SYMSXP, then its ASCII CHARSXP) is written once and referred to after: two matrices
+    # carry "dim"
+    two = rdata.r_list([rdata.r_matrix(np.eye(2)), rdata.r_matrix(np.eye(3))])
+    raw = rdata.rda_bytes([("two", two)])
+    assert raw.count(b"\x00\x00\x00\x01\x00\x04\x00\x09\x00\x00\x00\x03dim") == 1
+
+
+def _strip_row_names(s):
+    """Layout without what R's data frames add and this writer leaves out: row names (ALTREP row
+    numbers) in names / dimnames, and model.matrix's "assign" attribute."""
+    if not isinstance(s, dict):
+        return s
+    out = dict(s)
+    out["attrs"] = [a for a in s["attrs"] if a != "assign"]
+    if "dimnames" in s:
+        out["dimnames"] = [None if d == "altrep" else _strip_row_names(d) for d in s["dimnames"]]
+        if all(d is None for d in out["dimnames"]):  # only row names: no dimnames without them
+            del out["dimnames"]
+            out["attrs"] = [a for a in out["attrs"] if a != "dimnames"]
+    if "fields" in s:
+        out["fields"] = [[k, _strip_row_names(v)] for k, v in s["fields"]]
+    return out
+
+
+@pytest.fixture(scope="module")
+def golden_fit(golden_plink):
+    bed, n, m, ph = golden_plink
+    g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)
+    grm = aireml.DenseGRM(g)
+    cov = np.column_stack([ph["x1"], ph["x2"]])
+    return g, grm, cov, ph
+
+
+def test_model_file_has_the_reference_layout_without_covariate_offset(golden_fit, tmp_path):
+    """Binary trait, covariates in the design (isCovariateOffset = FALSE), no LOCO: the written
+    model's fields, order, types, shapes, dimnames and classes are those of the reference's
+    example_binary_includenonAutoforvarRatio.rda, except the fields that example's SAIGE version
+    did not write yet (isCovariateOffset, offset, useSparseGRMtoFitNULL) and R's row names."""
+    g, grm, cov, ph = golden_fit
+    f0 = prep.make_fit0(ph["y_binary"], cov, "binary", False)
+    fit = aireml.glmmkin_binary(grm, f0)
+    ids = ["s%d" % i for i in range(grm.n)]
+    p = str(tmp_path / "m.rda")
+    output.write_model_rda(p, fit, f0, "binary", ids, covariate_names=["x1", "x2"])
+    ours = rdata.schema(dict(rdata.read_rda(p)[1])["modglmm"])
+    ref = rdata.schema(dict(rdata.read_rda(RDA)[1])["modglmm"])
+    newer = {"isCovariateOffset", "offset", "useSparseGRMtoFitNULL"}
+    ours_f = [[k, _strip_row_names(v)] for k, v in ours["fields"] if k not in newer]
+    ref_f = [[k, _strip_row_names(v)] for k, v in ref["fields"]]
+    ref_f = [[k, v] if k != "y" else [k, dict(v, attrs=[])] for k, v in ref_f]  # y's row names
+    assert [k for k, _ in ours_f] == [k for k, _ in ref_f]
+    for (k, a), (_, b) in zip(ours_f, ref_f):
+        assert a == b, (k, a, b)
+    # and the values read back
+    d = output.read_model_rda(p)
+    np.testing.assert_allclose(d["theta"], fit["theta"])
+    back = output.covariate_transform_back(fit["coefficients"], f0["transform"], grm.n)
+    np.testing.assert_allclose(d["coefficients"].ravel(), back)
+    # the transform back recovers the untransformed design's coefficients: X_orig b = X_qr alpha
+    Xo = np.column_stack([np.ones(grm.n), cov])
+    np.testing.assert_allclose(Xo @ back, f0["X"] @ np.asarray(fit["coefficients"]).ravel(), rtol=1e-9, atol=1e-9)
+    nk = d["obj.noK"]
+    mu = np.asarray(fit["fitted_values"])
+    np.testing.assert_allclose(nk["XVX"], f0["X"].T @ (f0["X"] * (mu * (1 - mu))[:, None]), rtol=1e-12)
+    np.testing.assert_allclose(nk["XVX"] @ nk["XVX_inv"], np.eye(3), atol=1e-10)
+    assert d["sampleID"] == ids and d["traitType"] == ["binary"]
+
+
+def test_model_file_has_the_reference_layout_with_offset_and_loco(golden_fit, tmp_path):
+    """Binary trait with the covariate offset and LOCO results (the reference's
+    example_binary_fullGRM.rda): the same layout, each chromosome's LOCO entry included, plus the
+    alpha0 the reference's current source adds to each entry (FIT.R:291)."""
+    g, grm, cov, ph = golden_fit
+    f0 = prep.make_fit0(ph["y_binary"], cov, "binary", True)
+    fit = aireml.glmmkin_binary(grm, f0)
+    # two chromosomes as two blocks of the GRM markers
+    mq = g.codes.shape[0]
+    loco = {}
+    for c, (b, e) in {1: (0, mq // 2 - 1), 2: (mq // 2, mq - 1)}.items():
+        r = aireml.get_coef_loco(aireml.loco_grm(grm, g, b, e), f0, fit, "binary")
+        loco[c] = dict(isLOCO=True, coefficients=r["alpha"], linear_predictors=r["eta"], fitted_values=r["mu"],
+                       Y=r["Y"], cov=r["cov"])
+    p = str(tmp_path / "m.rda")
+    output.write_model_rda(p, fit, f0, "binary", ["s%d" % i for i in range(grm.n)],
+                           covariate_names=["x1", "x21"], loco=loco)
+    ours = rdata.schema(dict(rdata.read_rda(p)[1])["modglmm"])
+    ref = json.load(open(os.path.join(GOLDEN, "model_schema_binary_fullGRM.json")))
+    ours_f = [[k, _strip_row_names(v)] for k, v in ours["fields"]]
+    ref_f = [[k, _strip_row_names(v)] for k, v in ref["fields"]]
+    ref_f = [[k, v] if k != "y" else [k, dict(v, attrs=[])] for k, v in ref_f]
+    assert [k for k, _ in ours_f] == [k for k, _ in ref_f]
+    for (k, a), (_, b) in zip(ours_f, ref_f):
+        if k == "LOCOResult":
+            assert a["len"] == b["len"] == 22
+            ent_a, ent_b = a["fields"][0][1], b["fields"][0][1]
+            assert ent_a["fields"][:-1] == ent_b["fields"], "LOCO entry"
+            assert ent_a["fields"][-1][0] == "alpha0"
+            assert a["fields"][2][1]["fields"][0][0] == "isLOCO"  # chromosomes without markers
+            continue
+        assert a == b, (k, a, b)
+    d = output.read_model_rda(p)
+    assert d["LOCO"].all() and d["isCovariateOffset"].all()
+    np.testing.assert_allclose(d["LOCOResult"][0]["linear.predictors"].ravel(), loco[1]["linear_predictors"])
+    assert not d["LOCOResult"][5]["isLOCO"].any()
+    np.testing.assert_allclose(d["offset"].ravel(), f0["offset"])
