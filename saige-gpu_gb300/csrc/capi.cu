@@ -125,7 +125,7 @@ struct Engine {
   double inflight_gap_ms = -1.0, inflight_launch_ms = 0.0;
   int adm_waits = 0, inflight_waits = 0;
   // set_pheno uploads without waiting, through the slot's own pinned staging; ev_slot marks the end
-  // of the slot's upload (and of any set-up before it on the side stream).  Columns of a slot whose
+  // of the slot's upload (and of any set-up before it on the set-up stream).  Columns of a slot whose
   // upload has not finished wait for it at admission, or stay queued for a later step when other
   // columns run meanwhile
   std::vector<double*> h_wslot;      // per slot: W (np doubles) then the mask (np bytes), pinned
@@ -189,8 +189,9 @@ struct sg_ctx {
   uint64_t budget = 0;
   uint64_t in_use = 0;
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;  // result copies, probe reductions and slot uploads overlap a step here
+  cudaStream_t side = nullptr;  // result copies and probe reductions overlap a step here
   cudaStream_t up = nullptr;    // the engine's right-hand-side uploads
+  cudaStream_t setup = nullptr;  // phenotype slots' set-ups (subset QC and tables, weights)
   std::string err;
   std::string err_pending;
   uint64_t launches = 0;
@@ -378,22 +379,33 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (c->num_sms <= 0) c->num_sms = 1;
   c->budget = hbm_budget_bytes;
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  // Three priorities (numerically lower is dispatched first).  The side stream carries short
+  // reductions and copies that the driver waits on while a step's GEMM fills the GPU: highest, so
+  // its blocks are dispatched as soon as an SM frees up.  The steps run above the slots' set-ups,
+  // whose blocks then fill the SMs a step leaves idle (the last wave of each GEMM, the short kernels
+  // between them) instead of taking SMs from the GEMMs.
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  const int prio_step = prio_lo > prio_hi ? prio_lo - 1 : prio_lo;
+  if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_step) != cudaSuccess) {
     delete c;
     return SG_ERR_CUDA;
   }
   for (auto& ev : c->tev) cudaEventCreate(&ev);
-  // the side stream carries short reductions and copies that the driver waits on while a step's
-  // GEMM fills the GPU: highest priority, so its blocks are dispatched as soon as an SM frees up
-  int prio_lo = 0, prio_hi = 0;
-  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   if (cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return SG_ERR_CUDA;
+  }
+  if (cudaStreamCreateWithPriority(&c->setup, cudaStreamNonBlocking, prio_lo) != cudaSuccess) {
+    cudaStreamDestroy(c->side);
     cudaStreamDestroy(c->stream);
     delete c;
     return SG_ERR_CUDA;
   }
   // right-hand-side uploads of the engine, beside the steps (copy engine only)
   if (cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(c->setup);
     cudaStreamDestroy(c->side);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -410,11 +422,13 @@ extern "C" void sg_ctx_destroy(sg_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   cudaStreamSynchronize(c->side);
+  cudaStreamSynchronize(c->setup);
   cudaStreamSynchronize(c->up);
   engine_free(c);  // the engine's device buffers, pinned staging and events
   for (auto& kv : c->allocs) cudaFree(kv.first);
   c->allocs.clear();
   cudaStreamDestroy(c->up);
+  cudaStreamDestroy(c->setup);
   cudaStreamDestroy(c->side);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -1114,7 +1128,8 @@ static cudaError_t d2h(sg_ctx* c, void* dst, const void* src, size_t bytes, cuda
 
 static void engine_free(sg_ctx* c) {
   Engine& e = c->eng;
-  cudaStreamSynchronize(c->side);  // a weight upload may still read a staging buffer
+  cudaStreamSynchronize(c->side);
+  cudaStreamSynchronize(c->setup);  // a weight upload may still read a staging buffer
   for (double* h : e.h_wslot)
     if (h) cudaFreeHost(h);
   for (cudaEvent_t ev : e.ev_slot)
@@ -1328,8 +1343,8 @@ extern "C" int sg_engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phe
 // setgeno uses (genoClass::setGenoObj over the subset, FIT.cpp:376-385, 436-495, 916-921), run on
 // the cohort's codes of every .bim marker with the subset as the phenotype mask; the host turns them
 // into d' = 1/sd'^2 (GRM markers), 2p', the fill-changed markers and the diagonal table.  dmask: the
-// mask bytes already on the device (side stream), or nullptr for every sample.
-// First half of a slot's subset set-up, on the side stream: the subset's QC records (the kernel
+// mask bytes already on the device (set-up stream), or nullptr for every sample.
+// First half of a slot's subset set-up, on the set-up stream: the subset's QC records (the kernel
 // setgeno uses, run with the subset as the phenotype mask), then d', 2p', the diagonal table, the
 // fill-change list and the two counts the host needs, copied to pinned memory; ev_prep marks the
 // end.  Nothing here waits for the device.
@@ -1362,16 +1377,16 @@ static int subset_prepare(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   if (!ss.dfill) SG_TRY(dev_alloc_t(c, &ss.dfill, (size_t)std::max<int64_t>(m, 1)));
   if (ss.prep) SG_CUDA(c, cudaEventSynchronize(ss.ev_prep));  // an earlier prepare still owns the buffers
   // the copy from pageable memory is staged before the call returns
-  SG_CUDA(c, cudaMemcpyAsync(ss.mb, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, c->side));
+  SG_CUDA(c, cudaMemcpyAsync(ss.mb, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, c->setup));
   launch_marker_qc(c->d_codes, c->pitch, m, nn, ss.mb, ns, c->qc_min_maf, c->qc_max_missing, c->d_vrflag_all,
-                   c->qc_min_mac_vr, c->qc_max_mac_vr, c->qc_is_var_ratio, ss.qc, c->side);
+                   c->qc_min_mac_vr, c->qc_max_mac_vr, c->qc_is_var_ratio, ss.qc, c->setup);
   // d' = 1/sd'^2, 2p' and the diagonal table per marker, the fill-changed markers in marker order,
   // on the device (setGenoObj's per-marker values over the subset, FIT.cpp:436-495, 152-159)
   launch_subset_derive(ss.qc, c->d_fill_all, m, mg, c->sub_loco_lo, c->sub_loco_hi, ss.dp, ss.p2, ss.lut, ss.flag,
-                       ss.flips, ss.dfill, ss.d_counts, c->side);
+                       ss.flips, ss.dfill, ss.d_counts, c->setup);
   SG_LAUNCHED(c, 3);
-  SG_CUDA(c, cudaMemcpyAsync(ss.h_counts, ss.d_counts, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->side));
-  SG_CUDA(c, cudaEventRecord(ss.ev_prep, c->side));
+  SG_CUDA(c, cudaMemcpyAsync(ss.h_counts, ss.d_counts, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->setup));
+  SG_CUDA(c, cudaEventRecord(ss.ev_prep, c->setup));
   ss.valid = false;
   ss.prep = true;
   ss.prep_all = mask == nullptr;
@@ -1400,7 +1415,7 @@ static bool slot_prepared(const sg_ctx* c, const Engine::SlotSub& ss, const uint
 // setgeno uses (genoClass::setGenoObj over the subset, FIT.cpp:376-385, 436-495, 916-921), run on
 // the cohort's codes of every .bim marker with the subset as the phenotype mask; the device turns
 // them into d' = 1/sd'^2 (GRM markers), 2p', the fill-changed markers and the diagonal table.
-// dmask: the mask bytes already on the device (side stream), or nullptr for every sample.  The
+// dmask: the mask bytes already on the device (set-up stream), or nullptr for every sample.  The
 // first half runs here unless sg_engine_prepare_subset launched it for this mask already.
 static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint8_t* dmask) {
   Engine& e = c->eng;
@@ -1422,8 +1437,8 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
     SG_TRY(dev_alloc_t(c, &ss.bits, (size_t)(words * np)));
     ss.bits_cap = words * np;
   }
-  launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, (int)nflip, W, dmask, nn, np, ss.bits, c->side);
-  launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, e.sdiag_part, ss.diag, c->side);
+  launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, (int)nflip, W, dmask, nn, np, ss.bits, c->setup);
+  launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, e.sdiag_part, ss.diag, c->setup);
   SG_LAUNCHED(c, W > 0 ? 3 : 2);
   ss.dev.dprime = ss.dp;
   ss.dev.p2 = ss.p2;
@@ -1435,7 +1450,7 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
   ss.dev.inv_m = 1.0 / (double)mprime;
   ss.dev.ns = (double)ns;
   // a small copy from pageable memory: staged before the call returns, so nothing waits for it
-  SG_CUDA(c, cudaMemcpyAsync(e.d_slots + slot, &ss.dev, sizeof(SubsetSlot), cudaMemcpyHostToDevice, c->side));
+  SG_CUDA(c, cudaMemcpyAsync(e.d_slots + slot, &ss.dev, sizeof(SubsetSlot), cudaMemcpyHostToDevice, c->setup));
   ss.m_prime = (double)mprime;
   ss.all = ss.prep_all;
   ss.ex_lo = ss.prep_lo;
@@ -1572,8 +1587,8 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     const double m = loco ? (double)(c->m_qc - c->loco_mj) : (double)c->m_qc;
     double* dw = e.d_wstage;
     uint8_t* dm = reinterpret_cast<uint8_t*>(e.d_wstage + e.np);
-    SG_CUDA(c, h2d(c, dw, hw, c->nn * sizeof(double), c->side));
-    if (mask) SG_CUDA(c, h2d(c, dm, hm, c->nn, c->side));
+    SG_CUDA(c, h2d(c, dw, hw, c->nn * sizeof(double), c->setup));
+    if (mask) SG_CUDA(c, h2d(c, dm, hm, c->nn, c->setup));
     const double* diag = loco ? c->d_diag_loco : c->d_diag;
     double mm = m;
     if (exact_mode(c->mv_mode)) {  // the subset's own diagonal and GRM marker count
@@ -1582,13 +1597,13 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
       mm = e.sub[slot].m_prime;
     }
     launch_slot_weights(e.np, c->nn, dw, mask ? dm : nullptr, diag, mm, tau[0], tau[1],
-                        c->is_diag_one ? 1 : 0, e.winv + slot * e.np, e.minv + slot * e.np, c->side);
+                        c->is_diag_one ? 1 : 0, e.winv + slot * e.np, e.minv + slot * e.np, c->setup);
     SG_LAUNCHED(c, 1);
   }
   e.h_ph[slot] = PhenoState{tau[0], tau[1]};
-  SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), c->side));
+  SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), c->setup));
   e.ph_set[slot] = 1;
-  SG_CUDA(c, cudaEventRecord(e.ev_slot[slot], c->side));
+  SG_CUDA(c, cudaEventRecord(e.ev_slot[slot], c->setup));
   e.slot_rec[slot] = e.slot_wait[slot] = 1;
   return SG_OK;
 }
@@ -1813,7 +1828,7 @@ static int engine_admit(sg_ctx* c) {
       if (it == e.reqs.end()) continue;  // cancelled
       Req& r = it->second;
       if (r.slot < (int64_t)e.slot_wait.size() && e.slot_wait[r.slot]) {
-        // the slot's weights (and subset set-up) were uploaded on the side stream since its last
+        // the slot's weights (and subset set-up) were uploaded on the set-up stream since its last
         // admission: admit once they are there; while other columns run, leave it for a later step
         // rather than hold the step back
         if (cudaEventQuery(e.ev_slot[r.slot]) == cudaSuccess) {
@@ -2271,7 +2286,7 @@ extern "C" int sg_engine_run(sg_ctx* c, int64_t max_steps, int64_t* n_finished) 
 // Asynchronous stepping: sg_engine_launch starts one step and returns at once; sg_engine_finish
 // waits for it and retires its finished columns.  Between the two the caller may fetch held
 // results, run probe reductions, upload weights of idle slots and submit work (it joins the next
-// launch); those calls use the side stream and never wait for the step.
+// launch); those calls use the side and set-up streams and never wait for the step.
 extern "C" int sg_engine_launch(sg_ctx* c, int64_t* n_finished, int* launched) {
   NEED_OPERATOR(c);
   Engine& e = c->eng;
@@ -2488,7 +2503,9 @@ extern "C" int sg_engine_probe_dots_begin(sg_ctx* c, int64_t slot, const int64_t
     dp.cap = need_part;
   }
   if (!dp.ev) SG_CUDA(c, cudaEventCreateWithFlags(&dp.ev, cudaEventDisableTiming));
-  // the scratch above is shared by the slots; their reductions queue on the side stream in order
+  // the scratch above is shared by the slots; their reductions queue on the side stream in order,
+  // after the slot's last weight upload (set-up stream)
+  if (slot < (int64_t)e.ev_slot.size() && e.slot_rec[slot]) SG_CUDA(c, cudaStreamWaitEvent(c->side, e.ev_slot[slot], 0));
   if (p > 0) {
     SG_CUDA(c, cudaMemsetAsync(e.d_sx, 0, need_sx * 8, c->side));
     SG_CUDA(c, cudaMemcpy2DAsync(e.d_sx, e.np * 8, SX, c->nn * 8, c->nn * 8, p, cudaMemcpyHostToDevice, c->side));

@@ -11,7 +11,7 @@ import pytest
 
 from oracle import aireml, plink
 from saigegpu import (MV_FP32_SIMT, MV_SUBSET_EXACT, MV_SUBSET_EXACT_F8, TC_SUBSET_PAIR, TC_SUBSET_SLICE, native,
-                      prep, serve, synth, vr)
+                      output, prep, serve, synth, vr)
 
 pytestmark = pytest.mark.gpu
 
@@ -302,7 +302,7 @@ def test_subset_exact_loco_products_match_oracle(exact_cohort):
         ctx.set_matvec_mode(MV_FP32_SIMT)
 
 
-def test_subset_exact_loco_coefficients_match_oracle(exact_cohort):
+def test_subset_exact_loco_coefficients_match_oracle(exact_cohort, tmp_path):
     """Get_Coef_LOCO (FIT.R:40-73, run per chromosome by FIT.R:1208-1295) for phenotypes on their
     own subsets, through the subset-exact engine with a .bim range left out, against the oracle's
     Get_Coef_LOCO on the LOCO GRM of setgeno over each subset, both from the oracle's full fit."""
@@ -338,6 +338,19 @@ def test_subset_exact_loco_coefficients_match_oracle(exact_cohort):
             # near zero differ by about that much of eta's scale (measured 2.6e-6 at a scale of 0.35)
             np.testing.assert_allclose(r["linear_predictors"], ref["eta"], rtol=1e-4,
                                        atol=1e-5 * np.abs(ref["eta"]).max())
+    # the step-1 model file with these LOCO results, as the reference saves it
+    trait, mask, f0 = use[0]
+    p = str(tmp_path / "loco.rda")
+    output.write_model_rda(p, fits[0], f0, trait, ["s%d" % i for i in np.nonzero(mask)[0]],
+                           loco={c: got[c][0] for c in sel})
+    d = output.read_model_rda(p)
+    assert len(d["LOCOResult"]) == 22 and d["LOCO"].all()
+    for c in sel:
+        e = d["LOCOResult"][c - 1]
+        assert e["isLOCO"].all()
+        np.testing.assert_array_equal(e["linear.predictors"].ravel(), got[c][0]["linear_predictors"])
+        np.testing.assert_array_equal(e["alpha0"].ravel(), np.ravel(got[c][0]["coefficients"]))
+    assert not d["LOCOResult"][0]["isLOCO"].any()
 
 
 @pytest.mark.parametrize("trait", ["binary", "quantitative"])
