@@ -84,7 +84,8 @@ struct Engine {
   std::vector<void*> slab_dblocks;  // device blocks
   cudaEvent_t ev_up = nullptr;      // the last right-hand-side upload (upload stream)
   bool up_wait = false;             // the next admission waits for it
-  double* d_wstage = nullptr;     // their device copy (np doubles + np bytes)
+  double* d_wstage = nullptr;     // their device copy (np doubles + np bytes), set-up stream
+  double* d_wstage2 = nullptr;    // the same for weight-only uploads (weights stream)
   int32_t* d_gcols = nullptr;
   bool inflight = false;          // a launched step has not been finished yet
   int64_t inflight_ncols = 0, inflight_occupied = 0, inflight_hi = 0;
@@ -191,7 +192,8 @@ struct sg_ctx {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // result copies and probe reductions overlap a step here
   cudaStream_t up = nullptr;    // the engine's right-hand-side uploads
-  cudaStream_t setup = nullptr;  // phenotype slots' set-ups (subset QC and tables, weights)
+  cudaStream_t setup = nullptr;  // phenotype slots' set-ups (subset QC and tables, first weights)
+  cudaStream_t wts = nullptr;    // later weight uploads of slots already set up
   std::string err;
   std::string err_pending;
   uint64_t launches = 0;
@@ -403,8 +405,17 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
     delete c;
     return SG_ERR_CUDA;
   }
+  // a slot's new weights (every AI-REML iteration) must not queue behind other slots' set-ups
+  if (cudaStreamCreateWithPriority(&c->wts, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
+    cudaStreamDestroy(c->setup);
+    cudaStreamDestroy(c->side);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return SG_ERR_CUDA;
+  }
   // right-hand-side uploads of the engine, beside the steps (copy engine only)
   if (cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaStreamDestroy(c->wts);
     cudaStreamDestroy(c->setup);
     cudaStreamDestroy(c->side);
     cudaStreamDestroy(c->stream);
@@ -423,11 +434,13 @@ extern "C" void sg_ctx_destroy(sg_ctx* c) {
   cudaStreamSynchronize(c->stream);
   cudaStreamSynchronize(c->side);
   cudaStreamSynchronize(c->setup);
+  cudaStreamSynchronize(c->wts);
   cudaStreamSynchronize(c->up);
   engine_free(c);  // the engine's device buffers, pinned staging and events
   for (auto& kv : c->allocs) cudaFree(kv.first);
   c->allocs.clear();
   cudaStreamDestroy(c->up);
+  cudaStreamDestroy(c->wts);
   cudaStreamDestroy(c->setup);
   cudaStreamDestroy(c->side);
   cudaStreamDestroy(c->stream);
@@ -1130,6 +1143,7 @@ static void engine_free(sg_ctx* c) {
   Engine& e = c->eng;
   cudaStreamSynchronize(c->side);
   cudaStreamSynchronize(c->setup);  // a weight upload may still read a staging buffer
+  cudaStreamSynchronize(c->wts);
   for (double* h : e.h_wslot)
     if (h) cudaFreeHost(h);
   for (cudaEvent_t ev : e.ev_slot)
@@ -1183,6 +1197,7 @@ static void engine_free(sg_ctx* c) {
   if (e.h_gcols) cudaFreeHost(e.h_gcols);
   e.h_gcols = nullptr;
   dev_free_t(c, e.d_wstage);
+  dev_free_t(c, e.d_wstage2);
   for (void** hp : {reinterpret_cast<void**>(&e.h_sst), reinterpret_cast<void**>(&e.h_scol),
                     reinterpret_cast<void**>(&e.h_acols), reinterpret_cast<void**>(&e.h_ptab)}) {
     if (*hp) cudaFreeHost(*hp);
@@ -1307,6 +1322,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   e.slab_pending.clear();
   SG_TRY(dev_alloc_t(c, &e.d_scol, (size_t)max_columns));
   SG_TRY(dev_alloc_t(c, &e.d_wstage, (size_t)(2 * np)));
+  SG_TRY(dev_alloc_t(c, &e.d_wstage2, (size_t)(2 * np)));
   SG_TRY(dev_alloc_t(c, &e.d_gcols, (size_t)max_columns));
   e.h_st.assign(max_columns, ColState{});
   for (auto& s : e.h_st) { s.kind = -1; s.active = 0; }
@@ -1384,9 +1400,13 @@ static int subset_prepare(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   // on the device (setGenoObj's per-marker values over the subset, FIT.cpp:436-495, 152-159)
   launch_subset_derive(ss.qc, c->d_fill_all, m, mg, c->sub_loco_lo, c->sub_loco_hi, ss.dp, ss.p2, ss.lut, ss.flag,
                        ss.flips, ss.dfill, ss.d_counts, c->setup);
-  SG_LAUNCHED(c, 3);
   SG_CUDA(c, cudaMemcpyAsync(ss.h_counts, ss.d_counts, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->setup));
   SG_CUDA(c, cudaEventRecord(ss.ev_prep, c->setup));
+  // the diagonal needs only the tables: it follows here, after the counts the host waits for
+  // (the slot's weights, later on this stream, read it)
+  if (!e.sdiag_part) SG_TRY(dev_alloc_t(c, &e.sdiag_part, (size_t)subset_diag_scratch(m, np)));
+  launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, e.sdiag_part, ss.diag, c->setup);
+  SG_LAUNCHED(c, 5);
   ss.valid = false;
   ss.prep = true;
   ss.prep_all = mask == nullptr;
@@ -1427,7 +1447,6 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
   ss.prep = false;
   const int64_t nflip = ss.h_counts[0], mprime = ss.h_counts[1], ns = ss.prep_ns;
   if (mprime == 0) return set_err(c, SG_ERR_STATE, "phenotype slot %lld: no marker passes QC in its subset", (long long)slot);
-  if (!e.sdiag_part) SG_TRY(dev_alloc_t(c, &e.sdiag_part, (size_t)subset_diag_scratch(m, np)));
   const int W = (int)((nflip + 31) / 32);
   if ((int64_t)W * np > ss.bits_cap) {
     // with room to spare (cudaFree waits for the whole device, steps included): at least 64 words
@@ -1438,8 +1457,7 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
     ss.bits_cap = words * np;
   }
   launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, (int)nflip, W, dmask, nn, np, ss.bits, c->setup);
-  launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, e.sdiag_part, ss.diag, c->setup);
-  SG_LAUNCHED(c, W > 0 ? 3 : 2);
+  SG_LAUNCHED(c, W > 0 ? 1 : 0);
   ss.dev.dprime = ss.dp;
   ss.dev.p2 = ss.p2;
   ss.dev.flips = ss.flips;
@@ -1578,6 +1596,10 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_wslot[slot]), e.np * (sizeof(double) + 1),
                              cudaHostAllocDefault));
   if (e.slot_rec[slot]) SG_CUDA(c, cudaEventSynchronize(e.ev_slot[slot]));  // its last upload (long done)
+  // a slot whose subset is (re)built uploads behind its set-up on the set-up stream; a slot already
+  // set up only needs new weights, on the weights stream (its set-up completed: ev_slot above)
+  const bool rebuild = exact_mode(c->mv_mode) && !slot_built(c, e.sub[slot], mask);
+  cudaStream_t us = rebuild ? c->setup : c->wts;
   {
     double* hw = e.h_wslot[slot];
     uint8_t* hm = reinterpret_cast<uint8_t*>(e.h_wslot[slot] + e.np);
@@ -1585,10 +1607,10 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     if (mask) std::memcpy(hm, mask, c->nn);
     const bool loco = c->loco && !c->is_diag_one;
     const double m = loco ? (double)(c->m_qc - c->loco_mj) : (double)c->m_qc;
-    double* dw = e.d_wstage;
-    uint8_t* dm = reinterpret_cast<uint8_t*>(e.d_wstage + e.np);
-    SG_CUDA(c, h2d(c, dw, hw, c->nn * sizeof(double), c->setup));
-    if (mask) SG_CUDA(c, h2d(c, dm, hm, c->nn, c->setup));
+    double* dw = rebuild ? e.d_wstage : e.d_wstage2;
+    uint8_t* dm = reinterpret_cast<uint8_t*>(dw + e.np);
+    SG_CUDA(c, h2d(c, dw, hw, c->nn * sizeof(double), us));
+    if (mask) SG_CUDA(c, h2d(c, dm, hm, c->nn, us));
     const double* diag = loco ? c->d_diag_loco : c->d_diag;
     double mm = m;
     if (exact_mode(c->mv_mode)) {  // the subset's own diagonal and GRM marker count
@@ -1597,13 +1619,13 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
       mm = e.sub[slot].m_prime;
     }
     launch_slot_weights(e.np, c->nn, dw, mask ? dm : nullptr, diag, mm, tau[0], tau[1],
-                        c->is_diag_one ? 1 : 0, e.winv + slot * e.np, e.minv + slot * e.np, c->setup);
+                        c->is_diag_one ? 1 : 0, e.winv + slot * e.np, e.minv + slot * e.np, us);
     SG_LAUNCHED(c, 1);
   }
   e.h_ph[slot] = PhenoState{tau[0], tau[1]};
-  SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), c->setup));
+  SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), us));
   e.ph_set[slot] = 1;
-  SG_CUDA(c, cudaEventRecord(e.ev_slot[slot], c->setup));
+  SG_CUDA(c, cudaEventRecord(e.ev_slot[slot], us));
   e.slot_rec[slot] = e.slot_wait[slot] = 1;
   return SG_OK;
 }

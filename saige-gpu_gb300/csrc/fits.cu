@@ -190,11 +190,14 @@ class Workers {
 struct sg_fits {
   sg_ctx* ctx = nullptr;
   int64_t n = 0, max_columns = 0, max_fits = 0;
+  // engine slots beyond max_fits: the next queued fits take them while they wait, so that their
+  // subsets' set-ups (QC, tables, diagonal) run on the device before a running fit makes room
+  int64_t ahead = 0;
   bool pipelined = true, launched = false;
   double t_created = 0;  // steady-clock seconds at sg_fits_create
   std::vector<int64_t> free_slots;
   std::map<int64_t, std::unique_ptr<Fit>> active;   // admitted, running
-  std::deque<std::unique_ptr<Fit>> pending;          // waiting for a slot and columns
+  std::deque<std::unique_ptr<Fit>> pending;          // waiting for room (the first may hold a slot)
   std::map<int64_t, std::unique_ptr<Fit>> done_fits; // finished, not yet collected
   std::deque<int64_t> finished_order;
   std::unordered_map<int64_t, int64_t> owner;        // request id -> fit id
@@ -936,11 +939,35 @@ void take_back(sg_fits* F) {
   }
 }
 
-// Admit queued fits while slots and engine columns last.  With workers the fits start there (their
-// columns are reserved until they have submitted); without, here.
+// Give a queued fit a free slot: the slot's cached probe products go (a new sample mask takes it).
+void take_slot(sg_fits* F, Fit& f) {
+  f.slot = F->free_slots.back();
+  F->free_slots.pop_back();
+  std::lock_guard<std::mutex> g(F->mu);
+  sg_engine_probe_cache_clear(F->ctx, f.slot);
+}
+
+// The first F->ahead queued fits hold slots while they wait, and their subsets' set-ups are
+// launched there (sg_engine_prepare_subset: nothing waits for them; a failure shows again when the
+// fit sets its phenotype).
+void prepare_ahead(sg_fits* F) {
+  int64_t k = 0;
+  for (auto& p : F->pending) {
+    if (k++ >= F->ahead) break;
+    if (p->slot >= 0) continue;
+    if (F->free_slots.empty()) break;
+    take_slot(F, *p);
+    std::lock_guard<std::mutex> g(F->mu);
+    (void)sg_engine_prepare_subset(F->ctx, p->slot, p->has_mask ? p->mask.data() : nullptr);
+  }
+}
+
+// Admit queued fits while room for max_fits fits and engine columns last.  With workers the fits
+// start there (their columns are reserved until they have submitted); without, here.
 void admit(sg_fits* F) {
   std::vector<Fit*> starts;
-  while (!F->pending.empty() && !F->free_slots.empty()) {
+  while (!F->pending.empty() && (int64_t)F->active.size() < F->max_fits) {
+    if (F->pending.front()->slot < 0 && F->free_slots.empty()) break;
     int64_t inflight;
     {
       std::lock_guard<std::mutex> g(F->mu);
@@ -949,13 +976,8 @@ void admit(sg_fits* F) {
     if (inflight + F->reserved_columns + need_columns(*F->pending.front()) > F->max_columns) break;
     std::unique_ptr<Fit> f = std::move(F->pending.front());
     F->pending.pop_front();
-    f->slot = F->free_slots.back();
-    F->free_slots.pop_back();
+    if (f->slot < 0) take_slot(F, *f);
     f->t_admit = now_s();
-    {
-      std::lock_guard<std::mutex> g(F->mu);
-      sg_engine_probe_cache_clear(F->ctx, f->slot);  // a new sample mask takes this slot
-    }
     const int64_t fid = f->id;
     Fit& ref = *f;
     F->active[fid] = std::move(f);
@@ -972,6 +994,7 @@ void admit(sg_fits* F) {
     if (ref.failed || ref.phase == P_DONE) retire(F, fid);
   }
   if (F->pool) F->pool->push(starts);
+  prepare_ahead(F);
 }
 
 // Mark the requests the engine finished as done (the caller holds F->mu or runs alone).
@@ -997,7 +1020,8 @@ extern "C" int sg_fits_create(sg_ctx* ctx, int64_t max_columns, int64_t max_fits
   int64_t n = 0, mt = 0, mq = 0, mv = 0;
   int rc = sg_geno_dims(ctx, &n, &mt, &mq, &mv);
   if (rc != SG_OK) return rc;
-  rc = sg_engine_reserve(ctx, max_columns, max_fits);
+  const int64_t ahead = std::min<int64_t>(8, (max_fits + 7) / 8);
+  rc = sg_engine_reserve(ctx, max_columns, max_fits + ahead);
   if (rc != SG_OK) return rc;
   rc = sg_engine_hold_results(ctx, 1);  // probe results are reduced on the device, not copied
   if (rc != SG_OK) return rc;
@@ -1006,9 +1030,10 @@ extern "C" int sg_fits_create(sg_ctx* ctx, int64_t max_columns, int64_t max_fits
   F->n = n;
   F->max_columns = max_columns;
   F->max_fits = max_fits;
+  F->ahead = ahead;
   F->pipelined = pipelined != 0;
   F->t_created = now_s();
-  for (int64_t s = max_fits - 1; s >= 0; --s) F->free_slots.push_back(s);
+  for (int64_t s = max_fits + ahead - 1; s >= 0; --s) F->free_slots.push_back(s);
   const unsigned hw = std::thread::hardware_concurrency();
   const int workers = (int)std::min<unsigned>(7u, hw > 2 ? hw / 2 - 1 : 0u);
   if (workers > 0) F->pool.reset(new Workers(workers, ctx, [F](Fit& f) { advance(F, f); }));
