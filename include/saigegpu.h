@@ -307,12 +307,14 @@ int sg_engine_set_pheno(sg_ctx *ctx, int64_t slot, const double *w, const double
  * rebuilds it, as for a new phenotype.  No reference counterpart. */
 int sg_engine_forget_subsets(sg_ctx *ctx);
 /* Subset-exact engine, for a driver whose threads serialise their engine calls: launch the first,
- * longer half of slot ``slot``'s subset set-up for ``mask`` (QC over the subset, its tables and
- * fill-change list) without waiting; sg_engine_subset_wait(slot) then blocks until that half has
- * run and, like sg_engine_wait, need not be serialised with other threads' calls; the slot's next
- * sg_engine_set_pheno with the same mask completes the set-up.  Both are no-ops when the slot
- * already holds that subset, and sg_engine_prepare_subset is one for the other engines.  No
- * reference counterpart. */
+ * longer half of slot ``slot``'s subset set-up for ``mask`` (QC over the subset, its tables,
+ * fill-change list and diagonal) without waiting; sg_engine_subset_wait(slot) then blocks until the
+ * counts the host needs are back and, like sg_engine_wait, need not be serialised with other
+ * threads' calls; the slot's next sg_engine_set_pheno with the same mask completes the set-up.
+ * Both are no-ops when the slot already holds that subset, and sg_engine_prepare_subset is one for
+ * the other engines.  Set-ups run on the context's lowest-priority stream, below the engine steps,
+ * so they fill SMs the steps leave idle; a driver may prepare a queued phenotype in a spare slot
+ * while it waits for room.  No reference counterpart. */
 int sg_engine_prepare_subset(sg_ctx *ctx, int64_t slot, const uint8_t *mask);
 /* A set-up slot's variance-ratio markers as setgeno over its subset selects them: up to cap .bim
  * indices (marker order) and their MAC over the subset; *n gets the count.  And one .bim marker's
