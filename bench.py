@@ -88,6 +88,9 @@ def parse():
                     help="step the engine synchronously instead of overlapping the driver with the next step")
     ap.add_argument("--serve-requests", type=int, default=32,
                     help="requests of the serving-form block (Poisson arrivals, 0 = skip)")
+    ap.add_argument("--loco-chroms", type=int, default=0,
+                    help="after the timed steps, Get_Coef_LOCO of the last batch's phenotypes with this many "
+                         "chromosomes (22 blocks of the .bim markers) left out in turn, timed (0 = skip)")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
 
@@ -657,6 +660,8 @@ def run_ours(args, rank, world, local):
     out["clocks"] = clk.summary()
     if rank == 0 and args.serve_requests > 0:
         out["serving"] = serving_block(ctx, args, cols)
+    if rank == 0 and exact and args.loco_chroms > 0:
+        out["loco"] = loco_block(ctx, timed_specs[-args.phenos:], res_all[-args.phenos:], args.loco_chroms, cols)
     if rank == 0:
         out["plain_fp64_single_rhs"] = plain_fp64(ctx, col_iters)
         out["speedup_vs_plain_fp64"] = round(value / out["plain_fp64_single_rhs"]["fits_per_hr"], 1)
@@ -669,6 +674,26 @@ def run_ours(args, rank, world, local):
             out["cpu_baseline"] = cpu_baseline(ctx, col_iters)
     ctx.close()
     return out
+
+
+def loco_block(ctx, specs, fits, chroms, cols):
+    """Step 1's LOCO pass (FIT.R:251-295, 504-540) for fitted phenotypes in the subset-exact engine:
+    Get_Coef_LOCO of every phenotype with each of the first ``chroms`` of 22 chromosomes (contiguous
+    blocks of the .bim markers) left out of its own GRM (``sg_loco_set_bim``), through the Python
+    generator driver (``serve.fit_loco``); wall time of the whole pass, subset set-ups included."""
+    from saigegpu import serve
+    m = ctx.dims()["m_total"]
+    ranges = serve.loco_ranges(1 + (np.arange(m) * 22) // m)
+    sel = {c: ranges[c] for c in range(1, 1 + min(chroms, 22))}
+    t0 = time.perf_counter()
+    got = serve.fit_loco(ctx, specs, fits, sel, max_columns=cols, bim=True)
+    wall = time.perf_counter() - t0
+    bad = sum(1 for c in sel for r in got[c] if isinstance(r, Exception))
+    done = len(sel) * len(specs) - bad
+    return {"chromosomes": len(sel), "phenotypes": len(specs), "failed": bad, "wall_s": round(wall, 2),
+            "chromosome_fits_per_hr": round(done / wall * 3600.0, 1),
+            "basis": "Get_Coef_LOCO per phenotype and chromosome, each phenotype's own GRM markers of the "
+                     "chromosome left out; wall time through serve.fit_loco (Python generators)"}
 
 
 def c1_full_fit(seed=1001, n=2000, m=5000, miss=0.01):
