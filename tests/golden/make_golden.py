@@ -21,7 +21,10 @@ It writes (all derived from ``src/SAIGE/extdata``):
   ``saigegpu.rdata``);
 * ``model_schema_binary_fullGRM.json`` -- the layout (``saigegpu.rdata.schema``)
   of ``example_binary_fullGRM.rda``'s model: field names, types, shapes,
-  attributes and classes, with its LOCO results.
+  attributes and classes, with its LOCO results;
+* ``binary_fullGRM_model.npz`` -- that model's y, design X (after the QR
+  covariate transform), covariate offset, fitted values and obj.noK arrays
+  (ScoreTest_NULL_Model, FIT.R:579-591), which do not depend on the GRM.
 
 The ``.rda`` files are R serialisation (XDR, version 2/3) of a list whose
 first seven elements are theta, coefficients, linear.predictors,
@@ -208,6 +211,12 @@ def main(ref_root):
     _, objs = rdata.read_rda(os.path.join(outp, "example_binary_fullGRM.rda"))
     with open(os.path.join(HERE, "model_schema_binary_fullGRM.json"), "w") as f:
         json.dump(rdata.schema(dict(objs)["modglmm"]), f, separators=(",", ":"))
+    from saigegpu import output
+    mod = output.read_model_rda(os.path.join(outp, "example_binary_fullGRM.rda"))
+    nk = mod["obj.noK"]
+    np.savez_compressed(os.path.join(HERE, "binary_fullGRM_model.npz"), y=mod["y"], X=mod["X"],
+                        offset=np.ravel(mod["offset"]), mu=np.ravel(mod["fitted.values"]),
+                        theta=mod["theta"], **{"noK_" + k: np.asarray(v) for k, v in nk.items()})
     print("wrote fixtures to", HERE)
 
 

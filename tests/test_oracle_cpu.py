@@ -121,9 +121,9 @@ def test_golden_theta_monte_carlo_band(golden_plink):
     Over 20 probe seeds and random VR-marker draws (none, single-ratio and categorical exclusion
     from the GRM) the oracle gives binary tau1 0.258 +- 0.040 (golden 0.335: +1.9 sd) and
     quantitative tau (0.238 +- 0.006, 0.451 +- 0.009) against the golden (0.201, 0.483), whose sum
-    agrees to 0.6%.  At the golden tau the oracle's linear predictors differ from the golden ones by
-    9% (quantitative) and 2% (binary), so the golden fits come from a different Sigma than the
-    reference's code path restated here; the quantitative band below is that systematic gap."""
+    agrees to 0.6%.  The golden fits were made on another genotype set of the same samples (the
+    example commands' 22-chromosome nfam_100 set, 128,868 markers, whose .bed the checkout lacks),
+    not on this 10k-marker set, so their GRM differs; the quantitative band below is that gap."""
     bed, n, m, ph = golden_plink
     gold = json.load(open(os.path.join(GOLDEN, "golden_fits.json")))
     g = plink.setgeno(bed, n, m, np.arange(1, n + 1), np.ones(n, bool), 0.01, 0.15)

@@ -156,3 +156,21 @@ def test_model_file_has_the_reference_layout_with_offset_and_loco(golden_fit, tm
     np.testing.assert_allclose(d["LOCOResult"][0]["linear.predictors"].ravel(), loco[1]["linear_predictors"])
     assert not d["LOCOResult"][5]["isLOCO"].any()
     np.testing.assert_allclose(d["offset"].ravel(), f0["offset"])
+
+
+def test_fit0_and_score_test_pieces_match_the_reference_model(golden_plink):
+    """What the reference's example_binary_fullGRM.rda holds that does not depend on its GRM (the
+    example commands fit it on a 22-chromosome genotype set whose .bed the checkout lacks) is
+    reproduced exactly: y in sample order, the QR-transformed design Xorig (Covariate_Transform,
+    FIT.R:1612-1648), the covariate offset of isCovariateOffset (FIT.R:1054-1065), and obj.noK from
+    the model's own fitted values (ScoreTest_NULL_Model, FIT.R:579-591)."""
+    _, _, _, ph = golden_plink
+    g = np.load(os.path.join(GOLDEN, "binary_fullGRM_model.npz"))
+    f0 = prep.make_fit0(ph["y_binary"], np.column_stack([ph["x1"], ph["x2"]]), "binary", True)
+    np.testing.assert_array_equal(f0["y"], g["y"])
+    np.testing.assert_allclose(f0["Xorig"], g["X"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(f0["offset"], g["offset"], rtol=0, atol=1e-12)
+    mu = g["mu"]
+    nk = output.score_test_null_model(mu, mu * (1 - mu), g["y"], g["X"])
+    for k in ("XV", "XVX", "XXVX_inv", "XVX_inv", "S_a", "XVX_inv_XV", "V"):
+        np.testing.assert_allclose(nk[k], g["noK_" + k], rtol=1e-9, atol=1e-12, err_msg=k)
