@@ -79,3 +79,18 @@ def test_loco_bim_range_selects_the_grm_markers(cohort):
     finally:
         ctx.loco_clear()
     np.testing.assert_array_equal(Yb, Y)
+
+
+def test_loco_bim_range_is_checked(cohort):
+    """Ranges outside the .bim markers, or holding no GRM marker, are refused; the context stays usable."""
+    ctx, grm, g, chrom = cohort
+    m = len(g.qc_mask)
+    for b, e in ((-1, 5), (5, m), (9, 3)):
+        with pytest.raises(Exception):
+            ctx.loco_set_bim(b, e)
+    dropped = np.nonzero(~g.qc_mask)[0]
+    if len(dropped):  # a .bim marker that failed QC alone holds no GRM marker
+        with pytest.raises(Exception):
+            ctx.loco_set_bim(int(dropped[0]), int(dropped[0]))
+    V = np.random.default_rng(4).standard_normal((grm.n, 3))
+    np.testing.assert_allclose(ctx.grm_matmul(V), grm.K @ V, rtol=0, atol=2e-5 * np.abs(grm.K @ V).max())
