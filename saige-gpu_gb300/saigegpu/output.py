@@ -101,7 +101,7 @@ def model_object(fit, fit0, trait, sample_ids, covariate_names=None, loco=None, 
     fit: a null fit (theta, coefficients, linear_predictors, fitted_values, Y, residuals, cov,
     converged) over the phenotype's samples; fit0: its ``prep.make_fit0``; sample_ids: those
     samples' IIDs; covariate_names: the design's covariate columns without the intercept (named
-    "minus1" as Covariate_Transform names it); loco: ``serve.fit_loco``'s results for this phenotype,
+    "minus1" after Covariate_Transform, else "(Intercept)"); loco: ``serve.fit_loco``'s results for this phenotype,
     {chromosome: dict or None}, or None without LOCO.  Fields as FIT.R assembles them: the fit list
     (239-242 / 495-498), LOCO and LOCOResult (251-295 / 504-540; alpha0 and, without the covariate
     offset, the offset of 1169-1170 on each chromosome), obj.glm.null (1154), offset (1158-1178),
@@ -118,7 +118,9 @@ def model_object(fit, fit0, trait, sample_ids, covariate_names=None, loco=None, 
     cov_names = ["x%d" % (k + 1) for k in range(q)] if covariate_names is None else list(covariate_names)
     if len(cov_names) != q:
         raise ValueError("%d covariate names for %d covariates" % (len(cov_names), q))
-    colnames = ["minus1"] + cov_names
+    # Covariate_Transform renames the intercept "minus1" (FIT.R:1630-1632); without it R's model
+    # matrix calls it "(Intercept)"
+    colnames = ["minus1" if fit0.get("transform") is not None else "(Intercept)"] + cov_names
     tau = np.asarray(fit["theta"], np.float64)
 
     def mu2_of(mu):

@@ -174,3 +174,23 @@ def test_fit0_and_score_test_pieces_match_the_reference_model(golden_plink):
     nk = output.score_test_null_model(mu, mu * (1 - mu), g["y"], g["X"])
     for k in ("XV", "XVX", "XXVX_inv", "XVX_inv", "S_a", "XVX_inv_XV", "V"):
         np.testing.assert_allclose(nk[k], g["noK_" + k], rtol=1e-9, atol=1e-12, err_msg=k)
+
+
+def test_model_file_quantitative_without_covariates(tmp_path):
+    """A quantitative trait with the intercept only (no QR transform, no offset) writes and reads back."""
+    rng = np.random.default_rng(8)
+    n = 60
+    y = rng.standard_normal(n)
+    f0 = prep.make_fit0(y, None, "quantitative", True)
+    fit = dict(theta=np.array([0.7, 0.3]), coefficients=np.array([y.mean()]), linear_predictors=np.full(n, y.mean()),
+               fitted_values=np.full(n, y.mean()), Y=y.copy(), residuals=y - y.mean(), cov=np.array([[0.01]]),
+               converged=True)
+    p = str(tmp_path / "q.rda")
+    output.write_model_rda(p, fit, f0, "quantitative", ["s%d" % i for i in range(n)])
+    d = output.read_model_rda(p)
+    assert d["traitType"] == ["quantitative"] and not d["isCovariateOffset"].any()
+    assert d["X"].shape == (n, 1) and d["coefficients"].shape == (1, 1)
+    np.testing.assert_allclose(d["obj.noK"]["V"], np.full(n, 1 / 0.7))
+    np.testing.assert_allclose(d["offset"].ravel(), 0.0)
+    m = dict(rdata.read_rda(p)[1])["modglmm"]
+    assert list(m["X"].attr("dimnames").value[1].value) == ["(Intercept)"]
