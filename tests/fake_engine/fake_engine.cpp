@@ -15,6 +15,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -64,6 +65,9 @@ struct sg_ctx {
   int64_t next_id = 1;
   bool hold = false, inflight = false;
   int64_t steps = 0, retired = 0, col_iters = 0;
+  // driver checks: subset preparations, highest slot index prepared or set, most slots with
+  // requests outstanding at a launch
+  int64_t prepares = 0, max_slot = -1, max_busy_slots = 0;
   double step_ms = 0.0;  // emulated device time of a step
   std::chrono::steady_clock::time_point step_end;
   std::string err;
@@ -219,6 +223,11 @@ void fake_ctx_destroy(sg_ctx* c) { delete c; }
 // running or held columns (a finished, held result keeps its column)
 int64_t fake_columns_in_use(sg_ctx* c) { return c ? c->running_or_held : -1; }
 int64_t fake_requests(sg_ctx* c) { return c ? (int64_t)c->reqs.size() : -1; }
+void fake_slot_stats(sg_ctx* c, int64_t* out) {
+  out[0] = c->prepares;
+  out[1] = c->max_slot;
+  out[2] = c->max_busy_slots;
+}
 
 const char* sg_last_error(const sg_ctx* c) { return c ? c->err.c_str() : "null context"; }
 int sg_ctx_make_current(sg_ctx* c) { return c ? SG_OK : SG_ERR_INVALID; }
@@ -254,6 +263,7 @@ int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, const double* 
     if (kv.second.slot == slot && kv.second.state != Q_DONE)
       return fail(c, SG_ERR_STATE, "phenotype slot has columns queued or in flight");
   Slot& s = c->slots[slot];
+  c->max_slot = std::max(c->max_slot, slot);
   const int64_t n = c->n;
   s.mask.assign(n, 1);
   if (mask)
@@ -340,6 +350,11 @@ int sg_engine_launch(sg_ctx* c, int64_t* n_finished, int* launched) {
   if (c->inflight) return fail(c, SG_ERR_STATE, "a step is in flight: finish it first");
   if (n_finished) *n_finished = 0;
   if (launched) *launched = 0;
+  {
+    std::set<int64_t> busy;
+    for (const auto& kv : c->reqs) busy.insert(kv.second.slot);
+    c->max_busy_slots = std::max(c->max_busy_slots, (int64_t)busy.size());
+  }
   admit(c);
   bool any = false;
   for (auto& kv : c->reqs) {
@@ -410,6 +425,8 @@ int sg_engine_prepare_subset(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   (void)mask;
   if (!c) return SG_ERR_INVALID;
   if (slot < 0 || slot >= (int64_t)c->slots.size()) return fail(c, SG_ERR_INVALID, "slot out of range");
+  ++c->prepares;
+  c->max_slot = std::max(c->max_slot, slot);
   return SG_OK;
 }
 

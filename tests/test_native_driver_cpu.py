@@ -37,6 +37,8 @@ def fake_lib(tmp_path_factory):
     lib.fake_columns_in_use.restype = C.c_int64
     lib.fake_requests.argtypes = [C.c_void_p]
     lib.fake_requests.restype = C.c_int64
+    lib.fake_slot_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    lib.fake_slot_stats.restype = None
     return lib
 
 
@@ -59,6 +61,12 @@ class FakeCtx:
 
     def requests(self):
         return self._lib.fake_requests(self._h)
+
+    def slot_stats(self):
+        """(subset preparations, highest slot prepared or set, most slots with requests at a launch)"""
+        out = (C.c_int64 * 3)()
+        self._lib.fake_slot_stats(self._h, out)
+        return tuple(out)
 
     def close(self):
         if self._h:
@@ -139,10 +147,18 @@ def test_native_driver_schedules_agree(fake_lib, cohort, mode):
 
 def test_native_driver_queues_fits_beyond_slots(fake_lib, cohort):
     """More fits than slots: they wait in the queue and take slots as fits finish (probe caches
-    cleared between tenants), with the same results as run alone."""
+    cleared between tenants), with the same results as run alone.  The next queued fit holds the
+    one spare slot (one per eight fits) and its subset is prepared there while it waits; no more
+    than max_phenos fits have columns at once."""
     grm, specs, _ = cohort
     many = [specs[i % len(specs)] for i in range(10)]
-    res, _ = _run(fake_lib, grm, many, threads=4, max_phenos=3, step_ms=0.1)
+    ctx = _ctx(fake_lib, grm, 0.1)
+    try:
+        res, _ = native.fit_batch(ctx, many, lib=fake_lib, threads=4, max_phenos=3)
+        prepares, max_slot, busy = ctx.slot_stats()
+    finally:
+        ctx.close()
+    assert prepares >= len(many) and max_slot == 3 and busy <= 3, (prepares, max_slot, busy)
     alone, _ = _run(fake_lib, grm, specs, threads=1)
     for i, r in enumerate(res):
         assert not isinstance(r, Exception), r
