@@ -601,7 +601,10 @@ def run_ours(args, rank, world, local):
                    "l2": ("inputs larger than L2 (genotype matrix %.0f GB per GEMM)" % (2.0 * npad_n * mg / 1e9)
                           if exact else "inputs larger than L2 (GRM %.0f GB)" % (4.0 * ctx.n ** 2 / 1e9)),
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "value_basis": "device-busy time of engine steps (CUDA events)",
+                   "value_basis": ("device-busy time of engine steps (CUDA events); the phenotypes' subset "
+                                   "set-ups run on low-priority streams beside and between the steps and count "
+                                   "only where they lengthen a step (all of their time is in e2e)"
+                                   if exact else "device-busy time of engine steps (CUDA events)"),
                    "runner": "blocking" if args.blocking_runner else "pipelined",
                    "driver": args.driver,
                    "driver_threads": args.workers if args.workers is not None else (

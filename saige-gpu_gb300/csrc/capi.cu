@@ -84,7 +84,7 @@ struct Engine {
   std::vector<void*> slab_dblocks;  // device blocks
   cudaEvent_t ev_up = nullptr;      // the last right-hand-side upload (upload stream)
   bool up_wait = false;             // the next admission waits for it
-  double* d_wstage = nullptr;     // their device copy (np doubles + np bytes), set-up stream
+  double* d_wstage[4] = {};       // their device copy (np doubles + np bytes), one per set-up stream
   double* d_wstage2 = nullptr;    // the same for weight-only uploads (weights stream)
   int32_t* d_gcols = nullptr;
   bool inflight = false;          // a launched step has not been finished yet
@@ -177,7 +177,7 @@ struct Engine {
   double* spart = nullptr;        // column partials: cap_cols x max(blocks over np, over mg)
   float* smax = nullptr;          // FP16 / E4M3 form: column block maxima, as spart
   float* sscale = nullptr;        //   and the columns' power-of-two scales s1, s2 (2 x cap_cols)
-  float* sdiag_part = nullptr;    // per-chunk partial sums of a subset's diagonal (slot set-up)
+  float* sdiag_part[4] = {};      // per-chunk partial sums of a subset's diagonal, one per set-up stream
 
 };
 constexpr int64_t kStepTrace = 65536;
@@ -192,7 +192,9 @@ struct sg_ctx {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // result copies and probe reductions overlap a step here
   cudaStream_t up = nullptr;    // the engine's right-hand-side uploads
-  cudaStream_t setup = nullptr;  // phenotype slots' set-ups (subset QC and tables, first weights)
+  // phenotype slots' set-ups (subset QC and tables, first weights): slot s on setup[s % 4], so that
+  // a slot's set-up waits only for the set-ups queued before it on its own stream
+  cudaStream_t setup[4] = {};
   cudaStream_t wts = nullptr;    // later weight uploads of slots already set up
   std::string err;
   std::string err_pending;
@@ -399,15 +401,18 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
     delete c;
     return SG_ERR_CUDA;
   }
-  if (cudaStreamCreateWithPriority(&c->setup, cudaStreamNonBlocking, prio_lo) != cudaSuccess) {
-    cudaStreamDestroy(c->side);
-    cudaStreamDestroy(c->stream);
-    delete c;
-    return SG_ERR_CUDA;
-  }
+  for (auto& st : c->setup)
+    if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio_lo) != cudaSuccess) {
+      for (auto& x : c->setup)
+        if (x) cudaStreamDestroy(x);
+      cudaStreamDestroy(c->side);
+      cudaStreamDestroy(c->stream);
+      delete c;
+      return SG_ERR_CUDA;
+    }
   // a slot's new weights (every AI-REML iteration) must not queue behind other slots' set-ups
   if (cudaStreamCreateWithPriority(&c->wts, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
-    cudaStreamDestroy(c->setup);
+    for (auto& x : c->setup) cudaStreamDestroy(x);
     cudaStreamDestroy(c->side);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -416,7 +421,7 @@ extern "C" int sg_ctx_create(int device, uint64_t hbm_budget_bytes, sg_ctx** out
   // right-hand-side uploads of the engine, beside the steps (copy engine only)
   if (cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking) != cudaSuccess) {
     cudaStreamDestroy(c->wts);
-    cudaStreamDestroy(c->setup);
+    for (auto& x : c->setup) cudaStreamDestroy(x);
     cudaStreamDestroy(c->side);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -433,7 +438,7 @@ extern "C" void sg_ctx_destroy(sg_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   cudaStreamSynchronize(c->side);
-  cudaStreamSynchronize(c->setup);
+  for (auto& x : c->setup) cudaStreamSynchronize(x);
   cudaStreamSynchronize(c->wts);
   cudaStreamSynchronize(c->up);
   engine_free(c);  // the engine's device buffers, pinned staging and events
@@ -441,7 +446,7 @@ extern "C" void sg_ctx_destroy(sg_ctx* c) {
   c->allocs.clear();
   cudaStreamDestroy(c->up);
   cudaStreamDestroy(c->wts);
-  cudaStreamDestroy(c->setup);
+  for (auto& x : c->setup) cudaStreamDestroy(x);
   cudaStreamDestroy(c->side);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -1142,7 +1147,7 @@ static cudaError_t d2h(sg_ctx* c, void* dst, const void* src, size_t bytes, cuda
 static void engine_free(sg_ctx* c) {
   Engine& e = c->eng;
   cudaStreamSynchronize(c->side);
-  cudaStreamSynchronize(c->setup);  // a weight upload may still read a staging buffer
+  for (auto& x : c->setup) cudaStreamSynchronize(x);  // a weight upload may still read a staging buffer
   cudaStreamSynchronize(c->wts);
   for (double* h : e.h_wslot)
     if (h) cudaFreeHost(h);
@@ -1180,7 +1185,7 @@ static void engine_free(sg_ctx* c) {
   dev_free_t(c, e.spart);
   dev_free_t(c, e.smax);
   dev_free_t(c, e.sscale);
-  dev_free_t(c, e.sdiag_part);
+  for (auto& p : e.sdiag_part) dev_free_t(c, p);
 
   e.dots_cap_sx = e.dots_cap_part = e.dots_cap_cols = 0;
   for (auto& dp : e.dots) {
@@ -1196,7 +1201,7 @@ static void engine_free(sg_ctx* c) {
   e.h_pin = nullptr;
   if (e.h_gcols) cudaFreeHost(e.h_gcols);
   e.h_gcols = nullptr;
-  dev_free_t(c, e.d_wstage);
+  for (auto& p : e.d_wstage) dev_free_t(c, p);
   dev_free_t(c, e.d_wstage2);
   for (void** hp : {reinterpret_cast<void**>(&e.h_sst), reinterpret_cast<void**>(&e.h_scol),
                     reinterpret_cast<void**>(&e.h_acols), reinterpret_cast<void**>(&e.h_ptab)}) {
@@ -1321,7 +1326,7 @@ static int engine_reserve(sg_ctx* c, int64_t max_columns, int64_t max_phenos) {
   e.stage_idx.assign(max_columns, -1);
   e.slab_pending.clear();
   SG_TRY(dev_alloc_t(c, &e.d_scol, (size_t)max_columns));
-  SG_TRY(dev_alloc_t(c, &e.d_wstage, (size_t)(2 * np)));
+  for (auto& p : e.d_wstage) SG_TRY(dev_alloc_t(c, &p, (size_t)(2 * np)));
   SG_TRY(dev_alloc_t(c, &e.d_wstage2, (size_t)(2 * np)));
   SG_TRY(dev_alloc_t(c, &e.d_gcols, (size_t)max_columns));
   e.h_st.assign(max_columns, ColState{});
@@ -1393,19 +1398,21 @@ static int subset_prepare(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   if (!ss.dfill) SG_TRY(dev_alloc_t(c, &ss.dfill, (size_t)std::max<int64_t>(m, 1)));
   if (ss.prep) SG_CUDA(c, cudaEventSynchronize(ss.ev_prep));  // an earlier prepare still owns the buffers
   // the copy from pageable memory is staged before the call returns
-  SG_CUDA(c, cudaMemcpyAsync(ss.mb, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, c->setup));
+  const int q = (int)(slot % 4);
+  cudaStream_t st = c->setup[q];
+  SG_CUDA(c, cudaMemcpyAsync(ss.mb, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, st));
   launch_marker_qc(c->d_codes, c->pitch, m, nn, ss.mb, ns, c->qc_min_maf, c->qc_max_missing, c->d_vrflag_all,
-                   c->qc_min_mac_vr, c->qc_max_mac_vr, c->qc_is_var_ratio, ss.qc, c->setup);
+                   c->qc_min_mac_vr, c->qc_max_mac_vr, c->qc_is_var_ratio, ss.qc, st);
   // d' = 1/sd'^2, 2p' and the diagonal table per marker, the fill-changed markers in marker order,
   // on the device (setGenoObj's per-marker values over the subset, FIT.cpp:436-495, 152-159)
   launch_subset_derive(ss.qc, c->d_fill_all, m, mg, c->sub_loco_lo, c->sub_loco_hi, ss.dp, ss.p2, ss.lut, ss.flag,
-                       ss.flips, ss.dfill, ss.d_counts, c->setup);
-  SG_CUDA(c, cudaMemcpyAsync(ss.h_counts, ss.d_counts, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->setup));
-  SG_CUDA(c, cudaEventRecord(ss.ev_prep, c->setup));
+                       ss.flips, ss.dfill, ss.d_counts, st);
+  SG_CUDA(c, cudaMemcpyAsync(ss.h_counts, ss.d_counts, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(c, cudaEventRecord(ss.ev_prep, st));
   // the diagonal needs only the tables: it follows here, after the counts the host waits for
   // (the slot's weights, later on this stream, read it)
-  if (!e.sdiag_part) SG_TRY(dev_alloc_t(c, &e.sdiag_part, (size_t)subset_diag_scratch(m, np)));
-  launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, e.sdiag_part, ss.diag, c->setup);
+  if (!e.sdiag_part[q]) SG_TRY(dev_alloc_t(c, &e.sdiag_part[q], (size_t)subset_diag_scratch(m, np)));
+  launch_subset_diag(c->d_codes, c->pitch, ss.lut, m, nn, np, e.sdiag_part[q], ss.diag, st);
   SG_LAUNCHED(c, 5);
   ss.valid = false;
   ss.prep = true;
@@ -1456,7 +1463,8 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
     SG_TRY(dev_alloc_t(c, &ss.bits, (size_t)(words * np)));
     ss.bits_cap = words * np;
   }
-  launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, (int)nflip, W, dmask, nn, np, ss.bits, c->setup);
+  cudaStream_t st = c->setup[slot % 4];
+  launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, (int)nflip, W, dmask, nn, np, ss.bits, st);
   SG_LAUNCHED(c, W > 0 ? 1 : 0);
   ss.dev.dprime = ss.dp;
   ss.dev.p2 = ss.p2;
@@ -1468,7 +1476,7 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
   ss.dev.inv_m = 1.0 / (double)mprime;
   ss.dev.ns = (double)ns;
   // a small copy from pageable memory: staged before the call returns, so nothing waits for it
-  SG_CUDA(c, cudaMemcpyAsync(e.d_slots + slot, &ss.dev, sizeof(SubsetSlot), cudaMemcpyHostToDevice, c->setup));
+  SG_CUDA(c, cudaMemcpyAsync(e.d_slots + slot, &ss.dev, sizeof(SubsetSlot), cudaMemcpyHostToDevice, st));
   ss.m_prime = (double)mprime;
   ss.all = ss.prep_all;
   ss.ex_lo = ss.prep_lo;
@@ -1599,7 +1607,7 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
   // a slot whose subset is (re)built uploads behind its set-up on the set-up stream; a slot already
   // set up only needs new weights, on the weights stream (its set-up completed: ev_slot above)
   const bool rebuild = exact_mode(c->mv_mode) && !slot_built(c, e.sub[slot], mask);
-  cudaStream_t us = rebuild ? c->setup : c->wts;
+  cudaStream_t us = rebuild ? c->setup[slot % 4] : c->wts;
   {
     double* hw = e.h_wslot[slot];
     uint8_t* hm = reinterpret_cast<uint8_t*>(e.h_wslot[slot] + e.np);
@@ -1607,7 +1615,7 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     if (mask) std::memcpy(hm, mask, c->nn);
     const bool loco = c->loco && !c->is_diag_one;
     const double m = loco ? (double)(c->m_qc - c->loco_mj) : (double)c->m_qc;
-    double* dw = rebuild ? e.d_wstage : e.d_wstage2;
+    double* dw = rebuild ? e.d_wstage[slot % 4] : e.d_wstage2;
     uint8_t* dm = reinterpret_cast<uint8_t*>(dw + e.np);
     SG_CUDA(c, h2d(c, dw, hw, c->nn * sizeof(double), us));
     if (mask) SG_CUDA(c, h2d(c, dm, hm, c->nn, us));
