@@ -429,8 +429,10 @@ int sg_synth_genetic_value(sg_ctx *ctx, uint64_t seed, double *out);
  * FIT.cpp:3113-3662) for many phenotypes at once over the engine, in native code.  No reference
  * counterpart as one call: the reference runs one phenotype per R process.
  *
- * sg_fits_create reserves the engine (max_columns, max_fits slots) and holds results on the
- * device; sg_fits_submit queues a fit (admitted when a slot and its columns are free): trait 0
+ * sg_fits_create reserves the engine (max_columns; max_fits slots plus one spare per eight, at
+ * most eight, where the next queued fits' subset set-ups run while they wait) and holds results on
+ * the device; at most max_fits fits run at once.  sg_fits_submit queues a fit (admitted when
+ * room and its columns are free): trait 0
  * binary (logit), 1 quantitative; mask is cohort-length (NULL = every sample) and y, X (n_sub x p,
  * column-major), offset (NULL = 0), eta0 and alpha0 are over the n_sub selected samples, as the R
  * driver's fit0.  sg_fits_run steps the engine until a fit finishes (or max_steps);
