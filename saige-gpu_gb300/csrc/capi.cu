@@ -158,6 +158,10 @@ struct Engine {
     MarkerQC* qc = nullptr;       // m_bim
     uint8_t* flag = nullptr;      // mg
     uint32_t* mb = nullptr;       // the mask as 2-bit fields
+    // pinned staging of the mask fields and of the slot's device record: a copy from pageable
+    // memory may wait for the work queued before it on the (low-priority) set-up stream
+    uint32_t* h_mb = nullptr;
+    SubsetSlot* h_rec = nullptr;
     int64_t* d_counts = nullptr;  // (changes, M')
     int64_t* h_counts = nullptr;  // pinned copy
     cudaEvent_t ev_prep = nullptr;
@@ -1171,6 +1175,8 @@ static void engine_free(sg_ctx* c) {
     dev_free_t(c, ss.dfill); dev_free_t(c, ss.bits); dev_free_t(c, ss.diag);
     dev_free_t(c, ss.qc); dev_free_t(c, ss.flag); dev_free_t(c, ss.mb); dev_free_t(c, ss.d_counts);
     if (ss.h_counts) cudaFreeHost(ss.h_counts);
+    if (ss.h_mb) cudaFreeHost(ss.h_mb);
+    if (ss.h_rec) cudaFreeHost(ss.h_rec);
     if (ss.ev_prep) cudaEventDestroy(ss.ev_prep);
   }
   e.sub.clear();
@@ -1396,11 +1402,14 @@ static int subset_prepare(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   if (!ss.diag) SG_TRY(dev_alloc_t(c, &ss.diag, (size_t)np));
   if (!ss.flips) SG_TRY(dev_alloc_t(c, &ss.flips, (size_t)std::max<int64_t>(m, 1)));
   if (!ss.dfill) SG_TRY(dev_alloc_t(c, &ss.dfill, (size_t)std::max<int64_t>(m, 1)));
+  if (!ss.h_mb) SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&ss.h_mb), (nwords + 1) * sizeof(uint32_t),
+                                         cudaHostAllocDefault));
   if (ss.prep) SG_CUDA(c, cudaEventSynchronize(ss.ev_prep));  // an earlier prepare still owns the buffers
-  // the copy from pageable memory is staged before the call returns
+  // (the last prepare's copy out of h_mb has completed: a set-up waited for its ev_prep)
+  std::memcpy(ss.h_mb, maskbits.data(), maskbits.size() * 4);
   const int q = (int)(slot % 4);
   cudaStream_t st = c->setup[q];
-  SG_CUDA(c, cudaMemcpyAsync(ss.mb, maskbits.data(), maskbits.size() * 4, cudaMemcpyHostToDevice, st));
+  SG_CUDA(c, cudaMemcpyAsync(ss.mb, ss.h_mb, maskbits.size() * 4, cudaMemcpyHostToDevice, st));
   launch_marker_qc(c->d_codes, c->pitch, m, nn, ss.mb, ns, c->qc_min_maf, c->qc_max_missing, c->d_vrflag_all,
                    c->qc_min_mac_vr, c->qc_max_mac_vr, c->qc_is_var_ratio, ss.qc, st);
   // d' = 1/sd'^2, 2p' and the diagonal table per marker, the fill-changed markers in marker order,
@@ -1475,8 +1484,11 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
   ss.dev.W = W;
   ss.dev.inv_m = 1.0 / (double)mprime;
   ss.dev.ns = (double)ns;
-  // a small copy from pageable memory: staged before the call returns, so nothing waits for it
-  SG_CUDA(c, cudaMemcpyAsync(e.d_slots + slot, &ss.dev, sizeof(SubsetSlot), cudaMemcpyHostToDevice, st));
+  // through the slot's pinned record, so the call does not wait for the stream (the slot's last
+  // record copy has completed: set_pheno waited for the slot's event)
+  if (!ss.h_rec) SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&ss.h_rec), sizeof(SubsetSlot), cudaHostAllocDefault));
+  *ss.h_rec = ss.dev;
+  SG_CUDA(c, cudaMemcpyAsync(e.d_slots + slot, ss.h_rec, sizeof(SubsetSlot), cudaMemcpyHostToDevice, st));
   ss.m_prime = (double)mprime;
   ss.all = ss.prep_all;
   ss.ex_lo = ss.prep_lo;
@@ -1600,8 +1612,10 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     e.slot_wait.resize(e.cap_ph, 0);
   }
   if (!e.ev_slot[slot]) SG_CUDA(c, cudaEventCreateWithFlags(&e.ev_slot[slot], cudaEventDisableTiming));
+  // the slot's pinned staging: W (np doubles), the mask (np bytes), then its PhenoState
+  const size_t ph_off = (e.np * (sizeof(double) + 1) + 15) / 16 * 16;
   if (!e.h_wslot[slot])
-    SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_wslot[slot]), e.np * (sizeof(double) + 1),
+    SG_CUDA(c, cudaHostAlloc(reinterpret_cast<void**>(&e.h_wslot[slot]), ph_off + sizeof(PhenoState),
                              cudaHostAllocDefault));
   if (e.slot_rec[slot]) SG_CUDA(c, cudaEventSynchronize(e.ev_slot[slot]));  // its last upload (long done)
   // a slot whose subset is (re)built uploads behind its set-up on the set-up stream; a slot already
@@ -1631,7 +1645,9 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     SG_LAUNCHED(c, 1);
   }
   e.h_ph[slot] = PhenoState{tau[0], tau[1]};
-  SG_CUDA(c, h2d(c, e.d_ph + slot, &e.h_ph[slot], sizeof(PhenoState), us));
+  PhenoState* hph = reinterpret_cast<PhenoState*>(reinterpret_cast<uint8_t*>(e.h_wslot[slot]) + ph_off);
+  *hph = e.h_ph[slot];
+  SG_CUDA(c, h2d(c, e.d_ph + slot, hph, sizeof(PhenoState), us));
   e.ph_set[slot] = 1;
   SG_CUDA(c, cudaEventRecord(e.ev_slot[slot], us));
   e.slot_rec[slot] = e.slot_wait[slot] = 1;
