@@ -229,3 +229,27 @@ def test_categorical_variance_ratio_oracle_on_golden(golden_plink):
     # golden run's probes, marker draw and tau (0.335 there, 0.24-0.29 here) come from R's RNG
     for v, gv in zip(vrs, gold):
         assert abs(v - gv) < 0.03, (vrs, gold)
+
+
+def test_loco_on_a_subset_equals_its_grm_without_the_chromosome():
+    """What the subset-exact engine's LOCO relies on, in the oracle: the reference's LOCO GRM of a
+    phenotype's setgeno ((M K - Z_j' Z_j) / (M - M_j), diag minus the chromosome's sum z^2;
+    parallelCrossProd_LOCO FIT.cpp:1790-1851, getDiagOfSigma_LOCO FIT.cpp:2370-2392) equals the GRM
+    of that setgeno built over its GRM markers outside the chromosome."""
+    n, m = 160, 900
+    bed, _ = synth.synth_bed(21, n, m, 0.03)
+    mask = np.random.default_rng(4).uniform(size=n) > 0.3
+    S = np.nonzero(mask)[0]
+    g = plink.setgeno(bed, n, m, S + 1, mask, 0.01, 0.15)
+    grm = aireml.DenseGRM(g)
+    b_bim, e_bim = 300, 520  # one chromosome as .bim markers
+    gb = int(np.count_nonzero(g.qc_mask[:b_bim]))
+    ge = gb + int(np.count_nonzero(g.qc_mask[b_bim:e_bim + 1])) - 1
+    loco = aireml.loco_grm(grm, g, gb, ge)
+    z = plink.std_geno(g).astype(np.float64)
+    keep = np.ones(z.shape[0], bool)
+    keep[gb:ge + 1] = False
+    zk = z[keep]
+    np.testing.assert_allclose(loco.K, zk.T @ zk / zk.shape[0], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(loco.diag_sum, (zk * zk).sum(axis=0), rtol=1e-10)
+    assert loco.m_qc == zk.shape[0]
