@@ -10,25 +10,31 @@ and IEEE doubles, lengths as 32-bit integers (-1 then two words for long vectors
 items (length, bytes; -1 for NA), attributes as a trailing pairlist.  Symbols are written once and
 then referred to by their position in a table of symbols and environments (REFSXP, index << 8).
 
-Covered: NULL, symbols, pairlists, logical / integer / double / complex / character / list /
-expression / raw vectors, attributes, and ALTREP items (kept as they were read, so a file read here
-writes back byte for byte); closures, environments, language objects and byte code are not (step 1's
-model holds none of them except inside objects the reference rebuilds on load).
+Covered, for reading and for writing back byte for byte: NULL and R's singleton environments,
+symbols, dotted pairs (pairlists, calls, closures, promises), environments (and package / namespace
+environments by name), primitives, external pointers and weak references, logical / integer /
+double / complex / character / list / expression / raw vectors, S4 objects, attributes, ALTREP
+items and compiled byte code (kept as the grammar it was read in), in formats 2 and 3.
 """
 import gzip
 import struct
 
 import numpy as np
 
-NILSXP, SYMSXP, LISTSXP, CHARSXP, LGLSXP, INTSXP, REALSXP, CPLXSXP, STRSXP, VECSXP, EXPRSXP, RAWSXP = (
-    0, 1, 2, 9, 10, 13, 14, 15, 16, 19, 20, 24)
-ALTREP_SXP, REFSXP, NILVALUE_SXP = 238, 255, 254
+NILSXP, SYMSXP, LISTSXP, CLOSXP, ENVSXP, PROMSXP, LANGSXP, SPECIALSXP, BUILTINSXP, CHARSXP = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
+LGLSXP, INTSXP, REALSXP, CPLXSXP, STRSXP, DOTSXP, VECSXP, EXPRSXP, BCODESXP = 10, 13, 14, 15, 16, 17, 19, 20, 21
+EXTPTRSXP, WEAKREFSXP, RAWSXP, S4SXP = 22, 23, 24, 25
+ALTREP_SXP, ATTRLISTSXP, ATTRLANGSXP, BCREPREF, BCREPDEF = 238, 239, 240, 243, 244
+PACKAGESXP, NAMESPACESXP, REFSXP, NILVALUE_SXP = 248, 249, 255, 254
+# singleton environments and markers, written as their code alone
 _SPECIAL = {253: "globalenv", 252: "unbound", 251: "missingarg", 250: "basenamespace", 242: "emptyenv",
             241: "baseenv"}
+# dotted-pair types: (attributes), (tag), car, then the cdr as the next item
+_PAIRS = (LISTSXP, LANGSXP, CLOSXP, PROMSXP, DOTSXP)
 NA_INTEGER = -2 ** 31
 NA_LOGICAL = NA_INTEGER
 _IS_OBJECT, _HAS_ATTR, _HAS_TAG = 1 << 8, 1 << 9, 1 << 10
-_ASCII_MASK, _UTF8_MASK = 1 << 6, 1 << 3
+_ASCII_MASK, _UTF8_MASK, _LATIN1_MASK, _BYTES_MASK = 1 << 6, 1 << 3, 1 << 2, 1 << 1
 R_VERSION_4_3_2 = (4 << 16) | (3 << 8) | 2
 R_VERSION_3_5_0 = (3 << 16) | (5 << 8) | 0
 
@@ -50,15 +56,25 @@ class RSym:
         return "RSym(%r)" % self.name
 
 
+class RChar(str):
+    """A string whose encoding bits differ from the ones this writer derives (ASCII, else UTF-8)."""
+
+    def __new__(cls, value, levels):
+        obj = str.__new__(cls, value)
+        obj.levels = levels
+        return obj
+
+
 class RObj:
-    """An R vector or pairlist: ``type`` (SEXPTYPE), ``value`` and ``attrs`` (a list of (name, value)
+    """An R vector or dotted pair: ``type`` (SEXPTYPE), ``value`` and ``attrs`` (a list of (name, value)
     pairs in the order R keeps them).
 
     value by type: logical / integer -> int32 array (NA = -2^31), double -> float64 array, complex ->
     complex128 array, character -> list of str (None = NA), list / expression -> list of items, raw ->
-    bytes, pairlist -> list of (tag name or None, item), with ``tail`` the last node's cdr when it
-    is not NULL (a dotted pair).  ``levels`` are the item's general-purpose bits as read (0 for
-    vectors R builds)."""
+    bytes.  Dotted pairs (pairlist, call, closure, promise, ...) -> list of (tag, car), the tag a
+    symbol's name, None, or another item (a closure's environment); ``tail`` is the last node's cdr
+    when it is not NULL.  A pairlist keeps its nodes in one list; the other dotted-pair types hold
+    one node and their cdr in ``tail``.  ``levels`` are the item's general-purpose bits as read."""
     __slots__ = ("type", "value", "attrs", "levels", "is_object", "tail")
 
     def __init__(self, type_, value, attrs=None, levels=0, is_object=None, tail=None):
@@ -117,6 +133,59 @@ class RSpecial:
         return hash(("RSpecial", self.code))
 
 
+class REnv:
+    """An environment: locked flag, enclosure, frame (a pairlist), hash table (a list), attributes.
+    Referred to by identity: the items that point at it share this object."""
+    __slots__ = ("locked", "enclos", "frame", "hashtab", "attrib")
+
+    def __init__(self, locked=0, enclos=None, frame=None, hashtab=None, attrib=None):
+        self.locked, self.enclos, self.frame, self.hashtab, self.attrib = locked, enclos, frame, hashtab, attrib
+
+
+class RNamedEnv:
+    """A package or namespace environment, written as its name strings (type PACKAGESXP or
+    NAMESPACESXP) and found again by name when R loads it."""
+    __slots__ = ("type", "names")
+
+    def __init__(self, type_, names):
+        self.type, self.names = type_, list(names)
+
+
+class RPrim:
+    """A primitive function (SPECIALSXP / BUILTINSXP), written as its name."""
+    __slots__ = ("type", "name", "attrs", "levels", "is_object")
+
+    def __init__(self, type_, name, attrs=None, levels=0, is_object=False):
+        self.type, self.name, self.attrs, self.levels, self.is_object = type_, name, list(attrs or []), levels, is_object
+
+
+class RExtPtr:
+    """An external pointer (its address is not serialised): protected value, tag, attributes."""
+    __slots__ = ("prot", "tag", "attrs", "levels", "is_object")
+
+    def __init__(self, prot, tag, attrs=None, levels=0, is_object=False):
+        self.prot, self.tag, self.attrs, self.levels, self.is_object = prot, tag, list(attrs or []), levels, is_object
+
+
+class RWeakRef:
+    """A weak reference (serialised empty)."""
+    __slots__ = ("attrs", "levels", "is_object")
+
+    def __init__(self, attrs=None, levels=0, is_object=False):
+        self.attrs, self.levels, self.is_object = list(attrs or []), levels, is_object
+
+
+class RBytecode:
+    """Compiled code as serialised: the number of shared cells (``nreps``) and the code, a tree of
+    (code item, constants).  A constant is ("bc", code), ("lang", node) or ("item", type, item); a
+    language node is ("ref", index), ("node", def index or None, type, attrs, tag, car, cdr) with car
+    and cdr again nodes, or ("leaf", item)."""
+    __slots__ = ("nreps", "code", "attrs", "levels", "is_object")
+
+    def __init__(self, nreps, code, attrs=None, levels=0, is_object=False):
+        self.nreps, self.code, self.attrs, self.levels, self.is_object = nreps, code, list(attrs or []), levels, is_object
+
+
 # ---------------------------------------------------------------------------------- reading
 class _Reader:
     def __init__(self, data):
@@ -140,10 +209,12 @@ class _Reader:
         n = self.int()
         if n == -1:
             return None
-        raw = self.b[self.o:self.o + n]
+        raw = bytes(self.b[self.o:self.o + n])
         self.o += n
-        levels = flags >> 12
-        return raw.decode("latin-1" if levels & (1 << 2) else "utf-8")
+        levels = (flags >> 12) & (_ASCII_MASK | _UTF8_MASK | _LATIN1_MASK | _BYTES_MASK)
+        s = raw.decode("latin-1" if levels & (_LATIN1_MASK | _BYTES_MASK) else "utf-8")
+        derived = _ASCII_MASK if all(c < 128 for c in raw) else _UTF8_MASK
+        return s if levels == derived and not levels & _BYTES_MASK else RChar(s, flags >> 12)
 
     def attrs_of(self, has_attr):
         if not has_attr:
@@ -152,6 +223,45 @@ class _Reader:
         if not (isinstance(pl, RObj) and pl.type == LISTSXP):
             raise ValueError("attributes are not a pairlist")
         return [(k, v) for k, v in pl.value]
+
+    def strvec(self):
+        if self.int() != 0:
+            raise ValueError("names of a string vector are not supported")
+        return [self.item() for _ in range(self.int())]
+
+    def tag_of(self, has_tag):
+        if not has_tag:
+            return None
+        t = self.item()
+        return t.name if isinstance(t, RSym) else t
+
+    def bc_lang(self, kind):
+        if kind == BCREPREF:
+            return ("ref", self.int())
+        if kind in (BCREPDEF, LANGSXP, LISTSXP, ATTRLANGSXP, ATTRLISTSXP):
+            pos = None
+            if kind == BCREPDEF:
+                pos = self.int()
+                kind = self.int()
+            attrs = self.item() if kind in (ATTRLANGSXP, ATTRLISTSXP) else None
+            tag = self.item()
+            car = self.bc_lang(self.int())
+            cdr = self.bc_lang(self.int())
+            return ("node", pos, kind, attrs, tag, car, cdr)
+        return ("leaf", self.item())
+
+    def bc1(self):
+        code = self.item()
+        consts = []
+        for _ in range(self.int()):
+            kind = self.int()
+            if kind == BCODESXP:
+                consts.append(("bc", self.bc1()))
+            elif kind in (LANGSXP, LISTSXP, BCREPDEF, BCREPREF, ATTRLANGSXP, ATTRLISTSXP):
+                consts.append(("lang", self.bc_lang(kind)))
+            else:
+                consts.append(("item", kind, self.item()))
+        return (code, consts)
 
     def item(self):
         flags = self.int()
@@ -174,29 +284,35 @@ class _Reader:
             sym = RSym(self.charsxp(cflags))
             self.refs.append(sym)
             return sym
-        if t == LISTSXP:
-            # a pairlist: each node carries (attributes), (tag), car, then the next node or NULL
-            items, node_attrs, tail = [], None, None
+        if t in (PACKAGESXP, NAMESPACESXP):
+            env = RNamedEnv(t, self.strvec())
+            self.refs.append(env)
+            return env
+        if t == ENVSXP:
+            env = REnv()
+            self.refs.append(env)  # before its contents, which may refer to it
+            env.locked = self.int()
+            env.enclos, env.frame, env.hashtab, env.attrib = self.item(), self.item(), self.item(), self.item()
+            return env
+        if t in _PAIRS:
+            # one node, or for a pairlist every plain node of the chain; a cdr of another kind (or a
+            # pairlist node with attributes, an object bit or other bits) is the tail item
+            items = []
+            node_attrs = self.attrs_of(has_attr)
+            tail = None
             while True:
-                a = self.attrs_of(has_attr)
-                if node_attrs is None:
-                    node_attrs = a
-                elif a:
-                    raise NotImplementedError("attributes on a pairlist node after the first")
-                tag = self.item() if has_tag else None
-                car = self.item()
-                items.append((tag.name if isinstance(tag, RSym) else None, car))
+                tag = self.tag_of(has_tag)
+                items.append((tag, self.item()))
                 nflags = self.int()
-                nt = nflags & 0xFF
-                if nt == NILVALUE_SXP:
+                if nflags == NILVALUE_SXP:
                     break
-                if nt != LISTSXP or nflags >> 12:
-                    self.o -= 4
-                    tail = self.item()  # a dotted pair's cdr
-                    break
-                has_attr = bool(nflags & _HAS_ATTR)
-                has_tag = bool(nflags & _HAS_TAG)
-            return RObj(LISTSXP, items, node_attrs, levels, is_obj, tail)
+                if t == LISTSXP and nflags in (LISTSXP, LISTSXP | _HAS_TAG):
+                    has_tag = bool(nflags & _HAS_TAG)
+                    continue
+                self.o -= 4
+                tail = self.item()
+                break
+            return RObj(t, items, node_attrs, levels, is_obj, tail)
         if t == ALTREP_SXP:
             info = self.item()
             state = self.item()
@@ -204,6 +320,28 @@ class _Reader:
             return RAltrep(info, state, attr, flags)
         if t == CHARSXP:
             return self.charsxp(flags)
+        if t in (SPECIALSXP, BUILTINSXP):
+            n = self.int()
+            name = bytes(self.b[self.o:self.o + n]).decode("latin-1")
+            self.o += n
+            return RPrim(t, name, self.attrs_of(has_attr), levels, is_obj)
+        if t == EXTPTRSXP:
+            x = RExtPtr(None, None, None, levels, is_obj)
+            self.refs.append(x)
+            x.prot, x.tag = self.item(), self.item()
+            x.attrs = self.attrs_of(has_attr)
+            return x
+        if t == WEAKREFSXP:
+            x = RWeakRef(None, levels, is_obj)
+            self.refs.append(x)
+            x.attrs = self.attrs_of(has_attr)
+            return x
+        if t == BCODESXP:
+            nreps = self.int()
+            code = self.bc1()
+            return RBytecode(nreps, code, self.attrs_of(has_attr), levels, is_obj)
+        if t == S4SXP:
+            return RObj(t, None, self.attrs_of(has_attr), levels, is_obj)
         if t in (LGLSXP, INTSXP):
             n = self.length()
             v = np.frombuffer(self.b, dtype=">i4", count=n, offset=self.o).astype(np.int32)
@@ -270,9 +408,10 @@ def read_rda(path):
 
 # ---------------------------------------------------------------------------------- writing
 class _Writer:
-    def __init__(self):
+    def __init__(self, version=3):
         self.parts = []
         self.refs = {}
+        self.version = version
 
     def int(self, v):
         self.parts.append(struct.pack(">i", v))
@@ -303,8 +442,12 @@ class _Writer:
             self.int(CHARSXP)
             self.int(-1)
             return
-        raw = s.encode("utf-8")
-        levels = _ASCII_MASK if all(c < 128 for c in raw) else _UTF8_MASK
+        raw = s.encode("latin-1") if isinstance(s, RChar) and s.levels & (_LATIN1_MASK | _BYTES_MASK) \
+            else s.encode("utf-8")
+        if isinstance(s, RChar):
+            levels = s.levels
+        else:
+            levels = _ASCII_MASK if all(c < 128 for c in raw) else _UTF8_MASK
         self.int(CHARSXP | (levels << 12))
         self.int(len(raw))
         self.parts.append(raw)
@@ -312,6 +455,47 @@ class _Writer:
     def attrs(self, attrs):
         if attrs:
             self.item(RObj(LISTSXP, list(attrs)))
+
+    def flags(self, t, levels, is_object, has_attr, has_tag=False):
+        self.int(t | (levels << 12) | (_IS_OBJECT if is_object else 0) | (_HAS_ATTR if has_attr else 0)
+                 | (_HAS_TAG if has_tag else 0))
+
+    def tag(self, tag):
+        self.item(RSym(tag) if isinstance(tag, str) else tag)
+
+    def bc_lang(self, node):
+        kind = node[0]
+        if kind == "ref":
+            self.int(BCREPREF)
+            self.int(node[1])
+        elif kind == "node":
+            _, pos, t, attrs, tag, car, cdr = node
+            if pos is not None:
+                self.int(BCREPDEF)
+                self.int(pos)
+            self.int(t)
+            if t in (ATTRLANGSXP, ATTRLISTSXP):
+                self.item(attrs)
+            self.item(tag)
+            self.bc_lang(car)
+            self.bc_lang(cdr)
+        else:
+            self.int(0)
+            self.item(node[1])
+
+    def bc1(self, code):
+        body, consts = code
+        self.item(body)
+        self.int(len(consts))
+        for c in consts:
+            if c[0] == "bc":
+                self.int(BCODESXP)
+                self.bc1(c[1])
+            elif c[0] == "lang":
+                self.bc_lang(c[1])  # writes its own type word
+            else:
+                self.int(c[1])
+                self.item(c[2])
 
     def item(self, x):
         if x is None:
@@ -325,28 +509,66 @@ class _Writer:
                 self.int(SYMSXP)
                 self.charsxp(x.name)
             return
+        if isinstance(x, (REnv, RNamedEnv, RExtPtr, RWeakRef)):
+            if self.ref_or_add(("id", id(x))):
+                return
+            if isinstance(x, RNamedEnv):
+                self.int(x.type)
+                self.int(0)
+                self.int(len(x.names))
+                for s in x.names:
+                    self.item(s)
+            elif isinstance(x, REnv):
+                self.int(ENVSXP)
+                self.int(x.locked)
+                for part in (x.enclos, x.frame, x.hashtab, x.attrib):
+                    self.item(part)
+            elif isinstance(x, RExtPtr):
+                self.flags(EXTPTRSXP, x.levels, x.is_object, bool(x.attrs))
+                self.item(x.prot)
+                self.item(x.tag)
+                self.attrs(x.attrs)
+            else:
+                self.flags(WEAKREFSXP, x.levels, x.is_object, bool(x.attrs))
+                self.attrs(x.attrs)
+            return
+        if isinstance(x, str):  # a CHARSXP item (a namespace's name strings)
+            self.charsxp(x)
+            return
         if isinstance(x, RAltrep):
             self.int(x.flags)
             self.item(x.info)
             self.item(x.state)
             self.item(x.attrs)
             return
+        if isinstance(x, RPrim):
+            self.flags(x.type, x.levels, x.is_object, bool(x.attrs))
+            raw = x.name.encode("latin-1")
+            self.int(len(raw))
+            self.parts.append(raw)
+            self.attrs(x.attrs)
+            return
+        if isinstance(x, RBytecode):
+            self.flags(BCODESXP, x.levels, x.is_object, bool(x.attrs))
+            self.int(x.nreps)
+            self.bc1(x.code)
+            self.attrs(x.attrs)
+            return
         if not isinstance(x, RObj):
             raise TypeError("cannot serialise %r" % type(x))
         t = x.type
-        flags = t | (x.levels << 12) | (_IS_OBJECT if x.is_object else 0) | (_HAS_ATTR if x.attrs else 0)
-        if t == LISTSXP:
-            # every node after the first carries no attributes; tags are symbols
+        if t in _PAIRS:
+            # the first node carries the item's levels, object bit and attributes; a pairlist's
+            # further nodes are plain
             first = True
             for tag, car in x.value:
-                f = LISTSXP | (x.levels << 12 if first else 0) | (_HAS_TAG if tag is not None else 0)
                 if first:
-                    f |= (_IS_OBJECT if x.is_object else 0) | (_HAS_ATTR if x.attrs else 0)
-                self.int(f)
-                if first:
+                    self.flags(t, x.levels, x.is_object, bool(x.attrs), tag is not None)
                     self.attrs(x.attrs)
+                else:
+                    self.flags(LISTSXP, 0, False, False, tag is not None)
                 if tag is not None:
-                    self.item(RSym(tag))
+                    self.tag(tag)
                 self.item(car)
                 first = False
             if x.tail is None:
@@ -354,7 +576,7 @@ class _Writer:
             else:
                 self.item(x.tail)
             return
-        self.int(flags)
+        self.flags(t, x.levels, x.is_object, bool(x.attrs))
         v = x.value
         if t in (LGLSXP, INTSXP):
             a = np.asarray(v, dtype=">i4")
@@ -381,27 +603,36 @@ class _Writer:
         elif t == RAWSXP:
             self.length(len(v))
             self.parts.append(bytes(v))
+        elif t == S4SXP:
+            pass
         else:
             raise NotImplementedError("R item type %d is not supported" % t)
         self.attrs(x.attrs)
 
 
-def serialize(obj, writer=R_VERSION_4_3_2, min_reader=R_VERSION_3_5_0, encoding="UTF-8"):
-    """XDR serialisation (format 3) of one item."""
+def serialize(obj, writer=R_VERSION_4_3_2, min_reader=None, encoding="UTF-8", version=3):
+    """XDR serialisation of one item, format 3 (with the native encoding) or 2.  The reader's
+    header dict may be passed back as keyword arguments."""
+    if version not in (2, 3):
+        raise ValueError("serialisation format %r" % version)
     w = _Writer()
     w.parts.append(b"X\n")
-    w.int(3)
+    w.int(version)
     w.int(writer)
+    if min_reader is None:  # the oldest R that reads the format: 3.5.0 for format 3, 2.3.0 for 2
+        min_reader = R_VERSION_3_5_0 if version == 3 else (2 << 16) | (3 << 8)
     w.int(min_reader)
-    w.int(len(encoding))
-    w.parts.append(encoding.encode("ascii"))
+    if version == 3:
+        w.int(len(encoding))
+        w.parts.append(encoding.encode("ascii"))
     w.item(obj)
     return b"".join(w.parts)
 
 
 def rda_bytes(objects, **header):
     """The uncompressed bytes save() writes for [(name, object)]."""
-    return b"RDX3\n" + serialize(RObj(LISTSXP, list(objects)), **header)
+    magic = b"RDX2\n" if header.get("version", 3) == 2 else b"RDX3\n"
+    return magic + serialize(RObj(LISTSXP, list(objects)), **header)
 
 
 def write_rda(path, objects, compresslevel=6, **header):

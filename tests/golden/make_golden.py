@@ -16,9 +16,11 @@ It writes (all derived from ``src/SAIGE/extdata``):
   values of ``output/example_binary_fullGRM.rda``, ``example_binary.rda`` and
   ``example_quantitative_fullGRM.rda`` plus the null variance ratios of the
   matching ``.varianceRatio.txt`` files;
-* ``example_binary_includenonAutoforvarRatio.rda`` -- that step-1 model file,
-  verbatim (R's own serialisation, for the byte-exact round trip of
-  ``saigegpu.rdata``);
+* ``example_binary_includenonAutoforvarRatio.rda`` and
+  ``example_binary_includenonAutoforvarRatio_FemaleOnly.rda`` -- those step-1
+  model files, verbatim (R's own serialisation, for the byte-exact round trip of
+  ``saigegpu.rdata``; the second holds closures, environments, a namespace,
+  promises, calls and byte code);
 * ``model_schema_binary_fullGRM.json`` -- the layout (``saigegpu.rdata.schema``)
   of ``example_binary_fullGRM.rda``'s model: field names, types, shapes,
   attributes and classes, with its LOCO results;
@@ -206,8 +208,8 @@ def main(ref_root):
         json.dump(golden, f, indent=1)
 
     from saigegpu import rdata
-    shutil.copyfile(os.path.join(outp, "example_binary_includenonAutoforvarRatio.rda"),
-                    os.path.join(HERE, "example_binary_includenonAutoforvarRatio.rda"))
+    for f in ("example_binary_includenonAutoforvarRatio.rda", "example_binary_includenonAutoforvarRatio_FemaleOnly.rda"):
+        shutil.copyfile(os.path.join(outp, f), os.path.join(HERE, f))
     _, objs = rdata.read_rda(os.path.join(outp, "example_binary_fullGRM.rda"))
     with open(os.path.join(HERE, "model_schema_binary_fullGRM.json"), "w") as f:
         json.dump(rdata.schema(dict(objs)["modglmm"]), f, separators=(",", ":"))

@@ -25,6 +25,47 @@ def test_reference_model_file_round_trips_byte_for_byte():
     assert out == raw
 
 
+def test_model_file_with_closures_round_trips_byte_for_byte():
+    """An older step-1 model of the reference, holding the null glm object: closures, environments,
+    a namespace, promises, calls and compiled byte code, all written back with R's bytes."""
+    p = os.path.join(GOLDEN, "example_binary_includenonAutoforvarRatio_FemaleOnly.rda")
+    raw = gzip.decompress(open(p, "rb").read())
+    header, objs = rdata.read_rda(p)
+    assert rdata.rda_bytes(objs, **header) == raw
+    kinds = set()
+
+    def walk(x, seen):
+        if id(x) in seen:
+            return
+        seen.add(id(x))
+        kinds.add(type(x).__name__ if not isinstance(x, rdata.RObj) else x.type)
+        if isinstance(x, rdata.RObj):
+            for e in (x.value if isinstance(x.value, list) else []):
+                for part in (e if isinstance(e, tuple) else (e,)):
+                    walk(part, seen)
+            for _, v in x.attrs:
+                walk(v, seen)
+            walk(x.tail, seen)
+        elif isinstance(x, rdata.REnv):
+            for v in (x.enclos, x.frame, x.hashtab, x.attrib):
+                walk(v, seen)
+
+    seen = set()
+    for _, o in objs:
+        walk(o, seen)
+    assert {rdata.CLOSXP, rdata.LANGSXP, rdata.PROMSXP, "REnv", "RNamedEnv", "RBytecode"} <= kinds
+
+
+def test_format_2_round_trip():
+    """save(..., version = 2) files: no native-encoding field in the header."""
+    obj = rdata.r_named_list([("a", rdata.r_double([1.0, 2.0])), ("b", rdata.r_str(["x"]))])
+    raw = rdata.rda_bytes([("m", obj)], version=2)
+    assert raw[:5] == b"RDX2\n"
+    header, objs = rdata.unserialize(raw[5:])
+    assert header["version"] == 2 and "encoding" not in header
+    assert rdata.rda_bytes(list(objs.value), **header) == raw
+
+
 def test_values_round_trip(tmp_path):
     obj = rdata.r_named_list([
         ("d", rdata.r_double([1.5, -np.inf, np.nan], names=["a", "b", "c"])),
