@@ -25,8 +25,11 @@ It writes (all derived from ``src/SAIGE/extdata``):
   of ``example_binary_fullGRM.rda``'s model: field names, types, shapes,
   attributes and classes, with its LOCO results;
 * ``binary_fullGRM_model.npz`` -- that model's y, design X (after the QR
-  covariate transform), covariate offset, fitted values and obj.noK arrays
-  (ScoreTest_NULL_Model, FIT.R:579-591), which do not depend on the GRM.
+  covariate transform) and its column names, sample IDs, covariate offset,
+  fitted values and obj.noK arrays (ScoreTest_NULL_Model, FIT.R:579-591), which
+  do not depend on the GRM;
+* ``pheno_1000samples.txt`` and ``samples_1000.fam`` -- the example phenotype
+  file and .fam, verbatim, for the phenotype preamble (prep.read_phenotypes).
 
 The ``.rda`` files are R serialisation (XDR, version 2/3) of a list whose
 first seven elements are theta, coefficients, linear.predictors,
@@ -216,9 +219,14 @@ def main(ref_root):
     from saigegpu import output
     mod = output.read_model_rda(os.path.join(outp, "example_binary_fullGRM.rda"))
     nk = mod["obj.noK"]
+    xnames = dict(objs)["modglmm"]["X"].attr("dimnames").value[1].value
     np.savez_compressed(os.path.join(HERE, "binary_fullGRM_model.npz"), y=mod["y"], X=mod["X"],
+                        X_names=np.array(xnames), sample_ids=np.array(mod["sampleID"]),
                         offset=np.ravel(mod["offset"]), mu=np.ravel(mod["fitted.values"]),
                         theta=mod["theta"], **{"noK_" + k: np.asarray(v) for k, v in nk.items()})
+    shutil.copyfile(os.path.join(inp, "pheno_1000samples.txt_withdosages_withBothTraitTypes.txt"),
+                    os.path.join(HERE, "pheno_1000samples.txt"))
+    shutil.copyfile(stem + ".fam", os.path.join(HERE, "samples_1000.fam"))
     print("wrote fixtures to", HERE)
 
 
