@@ -223,3 +223,15 @@ def read_model_rda(path):
             return {k: conv(e) for k, e in zip(names, x.value)}
         return x
     return conv(model)
+
+
+def write_step1(prefix, fit, fit0, trait, sample_ids, covariate_names=None, loco=None, variance_ratios=None):
+    """Step 1's outputs under the reference's outputPrefix convention (FIT.R:1218, 1299, 2416-2417):
+    ``<prefix>.rda`` (the model) and, given the ratios (one per MAC category),
+    ``<prefix>.varianceRatio.txt``.  Returns the paths written."""
+    paths = [str(prefix) + ".rda"]
+    write_model_rda(paths[0], fit, fit0, trait, sample_ids, covariate_names, loco)
+    if variance_ratios is not None:
+        paths.append(str(prefix) + ".varianceRatio.txt")
+        write_variance_ratio(paths[1], list(np.atleast_1d(variance_ratios)))
+    return paths

@@ -235,3 +235,19 @@ def test_model_file_quantitative_without_covariates(tmp_path):
     np.testing.assert_allclose(d["offset"].ravel(), 0.0)
     m = dict(rdata.read_rda(p)[1])["modglmm"]
     assert list(m["X"].attr("dimnames").value[1].value) == ["(Intercept)"]
+
+
+def test_step1_outputs_under_a_prefix(tmp_path):
+    """<prefix>.rda and <prefix>.varianceRatio.txt, as the reference's outputPrefix names them."""
+    rng = np.random.default_rng(3)
+    n = 40
+    y = (rng.uniform(size=n) < 0.4).astype(float)
+    f0 = prep.make_fit0(y, rng.standard_normal((n, 1)), "binary", True)
+    mu = np.full(n, y.mean())
+    fit = dict(theta=np.array([1.0, 0.2]), coefficients=np.array([0.1]), linear_predictors=np.zeros(n),
+               fitted_values=mu, Y=y - mu, residuals=y - mu, cov=np.array([[0.02]]), converged=True)
+    paths = output.write_step1(tmp_path / "run", fit, f0, "binary", ["s%d" % i for i in range(n)],
+                               variance_ratios=[0.95, 0.97])
+    assert [os.path.basename(p) for p in paths] == ["run.rda", "run.varianceRatio.txt"]
+    assert output.read_variance_ratio(paths[1]) == [0.95, 0.97]
+    assert output.read_model_rda(paths[0])["traitType"] == ["binary"]
