@@ -253,3 +253,18 @@ def test_loco_on_a_subset_equals_its_grm_without_the_chromosome():
     np.testing.assert_allclose(loco.K, zk.T @ zk / zk.shape[0], rtol=1e-10, atol=1e-12)
     np.testing.assert_allclose(loco.diag_sum, (zk * zk).sum(axis=0), rtol=1e-10)
     assert loco.m_qc == zk.shape[0]
+
+
+def test_refinement_study_runs():
+    """The refinement study (host emulation of one-product inner solves) runs and both solves reach
+    the direct solve's accuracy class on a small problem."""
+    from saigegpu import refinement_study
+    res = refinement_study.study(n=200, m=500, trials=2)
+    assert [r["trait"] for r in res] == ["binary", "quantitative"]
+    for r in res:
+        for s in r["solves"]:
+            assert s["err_direct"] < 1e-3 and s["err_refined"] < 1e-3
+    # BF16 keeps 8 significant bits: 1 + 2^-9 rounds down, 1 + 3 2^-9 up to 1 + 2^-7, and the tie
+    # 1 + 2^-8 to the even neighbour 1
+    b = refinement_study.bf16(np.array([1.0 + 2 ** -9, 1.0 + 3 * 2 ** -9, 1.0 + 2 ** -8]))
+    np.testing.assert_array_equal(b, [1.0, 1.0 + 2 ** -7, 1.0])
