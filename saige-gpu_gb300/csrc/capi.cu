@@ -24,6 +24,9 @@ using namespace sg;
 
 namespace {
 
+// set-up streams (lowest priority): slot s uses number s % kSetupStreams
+constexpr int kSetupStreams = 4;
+
 struct Req {
   int64_t id = 0;
   int64_t slot = 0;
@@ -84,7 +87,7 @@ struct Engine {
   std::vector<void*> slab_dblocks;  // device blocks
   cudaEvent_t ev_up = nullptr;      // the last right-hand-side upload (upload stream)
   bool up_wait = false;             // the next admission waits for it
-  double* d_wstage[4] = {};       // their device copy (np doubles + np bytes), one per set-up stream
+  double* d_wstage[kSetupStreams] = {};  // their device copy (np doubles + np bytes), per set-up stream
   double* d_wstage2 = nullptr;    // the same for weight-only uploads (weights stream)
   int32_t* d_gcols = nullptr;
   bool inflight = false;          // a launched step has not been finished yet
@@ -181,7 +184,7 @@ struct Engine {
   double* spart = nullptr;        // column partials: cap_cols x max(blocks over np, over mg)
   float* smax = nullptr;          // FP16 / E4M3 form: column block maxima, as spart
   float* sscale = nullptr;        //   and the columns' power-of-two scales s1, s2 (2 x cap_cols)
-  float* sdiag_part[4] = {};      // per-chunk partial sums of a subset's diagonal, one per set-up stream
+  float* sdiag_part[kSetupStreams] = {};  // per-chunk partial sums of a subset's diagonal, per set-up stream
 
 };
 constexpr int64_t kStepTrace = 65536;
@@ -196,9 +199,9 @@ struct sg_ctx {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // result copies and probe reductions overlap a step here
   cudaStream_t up = nullptr;    // the engine's right-hand-side uploads
-  // phenotype slots' set-ups (subset QC and tables, first weights): slot s on setup[s % 4], so that
-  // a slot's set-up waits only for the set-ups queued before it on its own stream
-  cudaStream_t setup[4] = {};
+  // phenotype slots' set-ups (subset QC and tables, first weights): slot s on setup[s % kSetupStreams],
+  // so that a slot's set-up waits only for the set-ups queued before it on its own stream
+  cudaStream_t setup[kSetupStreams] = {};
   cudaStream_t wts = nullptr;    // later weight uploads of slots already set up
   std::string err;
   std::string err_pending;
@@ -1407,7 +1410,7 @@ static int subset_prepare(sg_ctx* c, int64_t slot, const uint8_t* mask) {
   if (ss.prep) SG_CUDA(c, cudaEventSynchronize(ss.ev_prep));  // an earlier prepare still owns the buffers
   // (the last prepare's copy out of h_mb has completed: a set-up waited for its ev_prep)
   std::memcpy(ss.h_mb, maskbits.data(), maskbits.size() * 4);
-  const int q = (int)(slot % 4);
+  const int q = (int)(slot % kSetupStreams);
   cudaStream_t st = c->setup[q];
   SG_CUDA(c, cudaMemcpyAsync(ss.mb, ss.h_mb, maskbits.size() * 4, cudaMemcpyHostToDevice, st));
   launch_marker_qc(c->d_codes, c->pitch, m, nn, ss.mb, ns, c->qc_min_maf, c->qc_max_missing, c->d_vrflag_all,
@@ -1472,7 +1475,7 @@ static int subset_setup(sg_ctx* c, int64_t slot, const uint8_t* mask, const uint
     SG_TRY(dev_alloc_t(c, &ss.bits, (size_t)(words * np)));
     ss.bits_cap = words * np;
   }
-  cudaStream_t st = c->setup[slot % 4];
+  cudaStream_t st = c->setup[slot % kSetupStreams];
   launch_subset_bitmap(c->d_codes, c->pitch, ss.flips, (int)nflip, W, dmask, nn, np, ss.bits, st);
   SG_LAUNCHED(c, W > 0 ? 1 : 0);
   ss.dev.dprime = ss.dp;
@@ -1621,7 +1624,7 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
   // a slot whose subset is (re)built uploads behind its set-up on the set-up stream; a slot already
   // set up only needs new weights, on the weights stream (its set-up completed: ev_slot above)
   const bool rebuild = exact_mode(c->mv_mode) && !slot_built(c, e.sub[slot], mask);
-  cudaStream_t us = rebuild ? c->setup[slot % 4] : c->wts;
+  cudaStream_t us = rebuild ? c->setup[slot % kSetupStreams] : c->wts;
   {
     double* hw = e.h_wslot[slot];
     uint8_t* hm = reinterpret_cast<uint8_t*>(e.h_wslot[slot] + e.np);
@@ -1629,7 +1632,7 @@ extern "C" int sg_engine_set_pheno(sg_ctx* c, int64_t slot, const double* w, con
     if (mask) std::memcpy(hm, mask, c->nn);
     const bool loco = c->loco && !c->is_diag_one;
     const double m = loco ? (double)(c->m_qc - c->loco_mj) : (double)c->m_qc;
-    double* dw = rebuild ? e.d_wstage[slot % 4] : e.d_wstage2;
+    double* dw = rebuild ? e.d_wstage[slot % kSetupStreams] : e.d_wstage2;
     uint8_t* dm = reinterpret_cast<uint8_t*>(dw + e.np);
     SG_CUDA(c, h2d(c, dw, hw, c->nn * sizeof(double), us));
     if (mask) SG_CUDA(c, h2d(c, dm, hm, c->nn, us));
