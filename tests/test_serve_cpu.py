@@ -283,6 +283,12 @@ class FakeLocoEngine(FakeEngine):
     def loco_clear(self):
         self.grm = self.full
 
+    def loco_set_bim(self, begin, end):
+        """A .bim range: the GRM markers inside it (the QC-passing .bim markers, in order)."""
+        qc = np.asarray(self.geno.qc_mask, bool)
+        b = int(np.count_nonzero(qc[:begin]))
+        self.loco_set(b, b + int(np.count_nonzero(qc[begin:end + 1])) - 1)
+
 
 def test_loco_generator_matches_oracle():
     grm, g = _cohort(43, n=200, m=600)
@@ -301,3 +307,23 @@ def test_loco_generator_matches_oracle():
             assert not isinstance(r, Exception), r
             np.testing.assert_allclose(r["coefficients"], ref["alpha"], rtol=1e-9)
             np.testing.assert_allclose(r["linear_predictors"], ref["eta"], rtol=1e-9, atol=1e-12)
+
+
+def test_loco_with_bim_ranges_equals_grm_ranges():
+    """fit_loco over .bim ranges (what the subset-exact engines take) gives the GRM-range results
+    when each range holds the same GRM markers."""
+    grm, g = _cohort(44, n=180, m=500)
+    gv = synth.genetic_value_from_codes(g.codes, 6)
+    y, C = synth.simulate_pheno(gv, 9, "binary", tau=0.6, prevalence=0.3)
+    f0 = prep.make_fit0(y, C, "binary", True)
+    fit = aireml.glmmkin_binary(grm, f0)
+    bim_chrom = 1 + (np.arange(len(g.qc_mask)) * 22) // len(g.qc_mask)
+    bim_ranges = serve.loco_ranges(bim_chrom)
+    grm_ranges = serve.loco_ranges(bim_chrom[np.asarray(g.qc_mask, bool)])
+    sel = (5, 19)
+    spec = [serve.FitSpec(f0, "binary")]
+    by_bim = serve.fit_loco(FakeLocoEngine(grm, g), spec, [fit], {c: bim_ranges[c] for c in sel}, bim=True)
+    by_grm = serve.fit_loco(FakeLocoEngine(grm, g), spec, [fit], {c: grm_ranges[c] for c in sel})
+    for c in sel:
+        np.testing.assert_array_equal(by_bim[c][0]["coefficients"], by_grm[c][0]["coefficients"])
+        np.testing.assert_array_equal(by_bim[c][0]["linear_predictors"], by_grm[c][0]["linear_predictors"])
